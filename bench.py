@@ -1,0 +1,379 @@
+#!/usr/bin/env python
+"""Throughput of the LatticeModels.jl evolution hot path on GB300, in ket-steps/s.
+
+Workload (the plain-method-at-GPU-scale configuration): SquareLattice(256, 256) with periodic
+boundaries on both axes, hopping t1 = 1, uniform Landau-gauge field of 0.01 flux quanta per
+plaquette, Anderson on-site disorder U[-1, 1], a block of M = 2048 complex-Gaussian normalised
+kets, dt = 0.05.  One bench step advances the whole ket block by dt through the Chebyshev
+propagator (ket-steps = M per step).
+
+  value     chosen form: ComplexF32 recurrence, FP64 coefficients and reductions, tol 1e-7
+  plain     ComplexF64 recurrence, tol 1e-12 (reported beside it)
+  e2e       the same metric through the public API (Evolution + ChebyshevGPU + localdensity)
+            with host buffers: the ket block uploaded from pinned memory, every step a
+            time-dependent H(t) input (on-site term uploaded from pinned memory, assembled on
+            the device) and the local densities downloaded to pinned memory.
+
+``--impl reference`` times the CPU restatement of the reference's KrylovKitExp step (C,
+OpenMP over kets, all host threads) on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT / "latticemodels.jl_gb300"))
+sys.path.insert(0, str(ROOT))
+
+METRIC = "ket-steps/s at <=1e-6 rel err vs FP64: chosen vs plain form, 1xGB300"
+LX = LY = 256
+M_KETS = 2048
+DT = 0.05
+B_FIELD = 0.01
+W_DISORDER = 2.0
+SEED = 20261203
+WORKLOAD = ("SquareLattice(256,256) periodic x/y, t1=1, LandauGauge(0.01), Anderson U[-1,1], "
+            "M=2048 complex-Gaussian kets, dt=0.05")
+
+
+# ------------------------------------------------------------------------------------------
+# synthetic inputs (seeded numpy PCG64)
+# ------------------------------------------------------------------------------------------
+def make_disorder(N):
+    rng = np.random.default_rng(SEED)
+    return rng.uniform(-W_DISORDER / 2, W_DISORDER / 2, size=N)
+
+
+def make_kets(N, M, rank=0, dtype=np.complex128, out=None):
+    """Complex Gaussian kets, each normalised; column-major (each ket contiguous)."""
+    rng = np.random.default_rng(SEED + 1 + rank)
+    X = out if out is not None else np.empty((N, M), dtype=dtype, order="F")
+    chunk = 256
+    for c0 in range(0, M, chunk):
+        c1 = min(M, c0 + chunk)
+        re = rng.standard_normal((c1 - c0, N))
+        im = rng.standard_normal((c1 - c0, N))
+        z = re + 1j * im
+        z /= np.linalg.norm(z, axis=1, keepdims=True)
+        X[:, c0:c1] = z.T.astype(X.dtype)
+    return X
+
+
+# ------------------------------------------------------------------------------------------
+# clocks during the timed region
+# ------------------------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._t = threading.Thread(target=self._read, daemon=True)
+            self._t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self._t.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0])); smax.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[4:8]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ------------------------------------------------------------------------------------------
+def measured_peak_hbm():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            return float(json.loads(p.read_text())["hbm_gbs"]), "measured"
+        except (KeyError, ValueError):
+            pass
+    return 6800.0, "fallback"
+
+
+def profile_traffic():
+    """DRAM bytes per launch of the dominant kernel from the committed ncu summary, if any."""
+    f = ROOT / "profiles" / "cheb_order_c32_256x256.md"
+    if not f.exists():
+        return None
+    for ln in f.read_text().splitlines():
+        if ln.startswith("traffic_bytes_per_launch_full:"):
+            try:
+                return float(ln.split(":", 1)[1].strip().split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+def dist_info():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def cpu_reference(steps, warmup, sample_kets=None):
+    """Times the oracle's C restatement of KrylovKitExp on a bounded sample of the workload."""
+    from oracle import krylov, lm_oracle as o
+    lat = o.SquareLattice(LX, LY, periodic=(True, True))
+    V = make_disorder(lat.N)
+    H, _, _, _ = o.tightbinding_hamiltonian_fast(lat, field=o.LandauGauge(B_FIELD), onsite=V)
+    csr = krylov.CSR(H)
+    threads = krylov.max_threads()
+    mk = sample_kets or 2 * threads
+    X = make_kets(lat.N, mk)
+    for _ in range(warmup):
+        X = krylov.krylov_expv_block(csr, DT, X, tol=1e-12, kdim=30, nthreads=threads)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        X = krylov.krylov_expv_block(csr, DT, X, tol=1e-12, kdim=30, nthreads=threads)
+    dt = time.perf_counter() - t0
+    return {"value": mk * steps / dt, "unit": "ket-steps/s", "cores": threads, "kind": "port",
+            "sample": f"{mk} of the {M_KETS} kets x {steps} steps (Lanczos exponentiate, tol 1e-12, "
+                      f"krylovdim 30), {dt:.2f} s wall"}
+
+
+def run_reference_arm(args):
+    rank, world, _ = dist_info()
+    if rank != 0:
+        return 0
+    cb = cpu_reference(args.steps, args.warmup)
+    line = {"metric": METRIC, "impl": "reference", "value": cb["value"], "unit": "ket-steps/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1000.0 * (2 * cb["cores"]) / cb["value"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "sample_kets_per_step": 2 * cb["cores"],
+                       "l2": "CPU run"},
+            "cpu_baseline": cb,
+            "e2e": {"value": cb["value"], "unit": "ket-steps/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+# ------------------------------------------------------------------------------------------
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="lmgpu", choices=["lmgpu", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--kets", type=int, default=M_KETS)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference_arm(args)
+
+    rank, world, local = dist_info()
+    import torch
+    import lmgpu
+    from lmgpu import device as D
+    D.set_default_device(local)
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    ctx = lmgpu.default_context()
+    ext = torch.cuda.ExternalStream(ctx.stream_ptr(), device=torch.device("cuda", local))
+    lat = lmgpu.SquareLattice(LX, LY, boundaries={"axis1": True, "axis2": True})
+    N, M = lat.N, args.kets
+    V = make_disorder(N)
+    H = lmgpu.tightbinding_hamiltonian(lat, V, field=lmgpu.LandauGauge(B_FIELD))
+    X = make_kets(N, M, rank)
+
+    def barrier():
+        ctx.synchronize()
+        if dist is not None:
+            dist.barrier()
+
+    def timed_steps(state, solver, steps, timing=False):
+        cache = solver.evolution_cache(state)
+        solver.update_solver(H, DT)
+        for _ in range(args.warmup):
+            solver.step(state, cache)
+        barrier()
+        ctx.reset_timing()
+        ctx.set_timing(timing)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(ext)
+        for _ in range(steps):
+            solver.step(state, cache)
+        e1.record(ext)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1)
+        order_ms, order_launches, launches = ctx.timing()
+        ctx.set_timing(False)
+        if dist is not None:
+            t = torch.tensor([ms], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+        return ms, order_ms, order_launches, launches
+
+    # ---- chosen form (c32) -------------------------------------------------------------
+    s32 = lmgpu.KetBlock(lat, X, precision="c32")
+    solver32 = lmgpu.ChebyshevGPU(renorm_every=20)
+    clk = ClockSampler(local)
+    clk.start()
+    ms32, _, _, launches32 = timed_steps(s32, solver32, args.steps)
+    clocks = clk.stop()
+    K32, a32, b32 = solver32.order(s32)
+    # dominant kernel timing pass (events around every Chebyshev sweep, resolved lazily)
+    _, order_ms, order_launches, _ = timed_steps(s32, solver32, args.steps, timing=True)
+
+    # ---- plain form (c64) --------------------------------------------------------------
+    s64 = lmgpu.KetBlock(lat, X, precision="c64")
+    solver64 = lmgpu.ChebyshevGPU()
+    ms64, _, _, _ = timed_steps(s64, solver64, args.steps)
+    K64, _, _ = solver64.order(s64)
+
+    # ---- error of the chosen form against FP64 after the same steps --------------------
+    # s32 ran 2*(warmup+steps) steps; bring s64 to the same time
+    for _ in range(args.warmup + args.steps):
+        solver64.step(s64)
+    r32 = lmgpu.localdensity(s32).values
+    r64 = lmgpu.localdensity(s64).values
+    J32 = lmgpu.DensityCurrents(H, s32).bond_values()
+    J64 = lmgpu.DensityCurrents(H, s64).bond_values()
+    nrm32 = s32.norms()
+    err = {"density": float(np.linalg.norm(r32 - r64) / np.linalg.norm(r64)),
+           "currents": float(np.linalg.norm(J32 - J64) / np.linalg.norm(J64)),
+           "norm_drift": float(np.abs(nrm32 - 1.0).max()),
+           "steps": 2 * (args.warmup + args.steps)}
+    del s64
+
+    # ---- end to end through the public API with host buffers ----------------------------
+    pin_X = torch.empty((M, N), dtype=torch.complex64, pin_memory=True)
+    Xh = pin_X.numpy().T  # (N, M) Fortran view of pinned memory
+    Xh[:] = X.astype(np.complex64)
+    pin_V = [torch.empty(N, dtype=torch.float64, pin_memory=True) for _ in range(2)]
+    for pv in pin_V:
+        pv.numpy()[:] = V
+    pin_rho = torch.empty(N, dtype=torch.float64, pin_memory=True).numpy()
+    field = lmgpu.LandauGauge(B_FIELD)
+    # a fresh host view every call: the on-site term is re-uploaded and H re-assembled each step
+    h = lambda t: lmgpu.tightbinding_hamiltonian(lat, pin_V[int(round(t / DT)) % 2].numpy(), field=field)
+    from lmgpu.observables import localdensity_into
+    e2e_state = lmgpu.DeviceState(lat, None, 0, "c32", shape=(N, M))
+    ev = lmgpu.Evolution(lmgpu.ChebyshevGPU(renorm_every=20), h, e2e_state)
+    evs = ev.current_states()[0]
+    times = [DT * (k + 1) for k in range(args.steps)]
+    for _ in ev([DT * (k + 1) for k in range(args.warmup)]):
+        localdensity_into(evs, pin_rho)
+    ev.time = 0.0
+    barrier()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(ext)
+    evs.upload_from(Xh)
+    for _ in ev(times):
+        localdensity_into(evs, pin_rho)
+    e1.record(ext)
+    e1.synchronize()
+    ms_e2e = e0.elapsed_time(e1)
+    if dist is not None:
+        t = torch.tensor([ms_e2e], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_e2e = float(t.item())
+    h2d = (N * M * 8 + args.steps * N * 8) / args.steps
+    d2h = N * 8
+
+    # ---- report ----------------------------------------------------------------------
+    if rank != 0:
+        if dist is not None:
+            dist.barrier()
+            dist.destroy_process_group()
+        return 0
+    value = world * M * args.steps / (ms32 / 1000.0)
+    plain = world * M * args.steps / (ms64 / 1000.0)
+    s_bytes = 8
+    alg_bytes_launch = 5.0 * N * M * s_bytes
+    avg_launch_ms = order_ms / max(order_launches, 1)
+    achieved = alg_bytes_launch / (avg_launch_ms / 1000.0) / 1e9
+    peak, peak_kind = measured_peak_hbm()
+    traffic = profile_traffic()
+    line = {
+        "metric": METRIC, "value": value, "unit": "ket-steps/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms32 / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c32",
+        "data": "synthetic (seeded PCG64: complex-Gaussian kets, U[-1,1] disorder)",
+        "config": {"workload": WORKLOAD, "N": N, "M_per_gpu": M, "dt": DT,
+                   "chebyshev_order_c32": K32, "chebyshev_order_c64": K64,
+                   "spectral_half_width": a32, "tol_c32": 1e-7, "tol_c64": 1e-12,
+                   "renorm_every": 20,
+                   "l2": f"inputs larger than L2 (ket block {N * M * 8 / 1e9:.2f} GB c32 vs 0.129 GB L2)"},
+        "plain_fp64": {"value": plain, "unit": "ket-steps/s", "ms_per_step": ms64 / args.steps,
+                       "dtype": "c64"},
+        "chosen_over_plain": value / plain,
+        "rel_err_vs_fp64": err,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": traffic,
+                     "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
+                     "kernel": "cheb_order_kernel<float> (one Chebyshev order)",
+                     "alg_bytes_per_launch": alg_bytes_launch, "avg_launch_ms": avg_launch_ms,
+                     "launches_timed": order_launches},
+        "e2e": {"value": world * M * args.steps / (ms_e2e / 1000.0), "unit": "ket-steps/s",
+                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                "ms_per_step": ms_e2e / args.steps},
+        "gpu_launches": int(launches32),
+        "clocks": clocks,
+    }
+    if world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_reference(max(1, min(args.steps, 3)), 1)
+    print(json.dumps(line))
+    if dist is not None:
+        dist.barrier()
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

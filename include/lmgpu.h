@@ -1,0 +1,169 @@
+/*
+ * lmgpu.h -- C ABI of the GB300 backend for the LatticeModels.jl time-evolution path.
+ *
+ * The path is `Evolution(t -> tightbinding_hamiltonian(l; field), P_0)` read out through
+ * `localdensity` and `DensityCurrents`.  A Julia `EvolutionSolver` subtype (or any other host
+ * language through its C FFI) drives it through the calls below.  All citations are to
+ * LatticeModels.jl v1.0.7, paths relative to that repository's root.
+ *
+ * Conventions
+ *  - Every call returns an int status: LM_OK (0) or an LM_ERR_* code; `lm_last_error(ctx)`
+ *    returns the message of the last failure on that context.
+ *  - Host pointers are borrowed for the duration of the call only.  The library owns all
+ *    device memory it allocates.  Complex numbers are interleaved (re, im) pairs.
+ *  - Site indices are those of the reference: 1-based, x-major with y fastest, i.e.
+ *    index = (x-1)*Ly + y.  Bonds follow the reference's NearestNeighbor(1) iteration order:
+ *    every +x bond (source sites in index order), then every +y bond.
+ *  - Calls on one context are ordered on that context's CUDA stream; a context is used from
+ *    one host thread at a time.  There is no CPU fallback: without a usable GPU,
+ *    lm_ctx_create fails.
+ */
+#ifndef LMGPU_H
+#define LMGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define LM_OK 0
+#define LM_ERR_ARG 1       /* bad argument (null pointer, size, mismatched objects) */
+#define LM_ERR_OOM 2       /* device allocation failed */
+#define LM_ERR_CUDA 3      /* CUDA runtime error */
+#define LM_ERR_TIMEOUT 4   /* a bounded device wait gave up */
+#define LM_ERR_NONFINITE 5 /* non-finite value detected */
+#define LM_ERR_STATE 6     /* call out of order (e.g. step before update) */
+#define LM_ERR_NOTSUP 7    /* configuration outside what the backend implements */
+
+#define LM_C64 0 /* ComplexF64 state, FP64 recurrence (the plain form) */
+#define LM_C32 1 /* ComplexF32 state, FP32 recurrence with FP64 coefficients/reductions */
+
+#define LM_KETS 0    /* N x M block of kets, column-major (each ket contiguous) */
+#define LM_DENSITY 1 /* N x N density matrix, column-major */
+
+#define LM_FIELD_LANDAU 1             /* LandauGauge(B): src/zoo/magneticfields.jl:11-15 */
+#define LM_FIELD_SYMMETRIC 2          /* SymmetricGauge(B): src/zoo/magneticfields.jl:27-31 */
+#define LM_FIELD_POINTFLUX_AXIAL 3    /* PointFlux(phi, p; gauge=:axial): :72-85 */
+#define LM_FIELD_POINTFLUX_SINGULAR 4 /* PointFlux(phi, p; gauge=:singular): :89-104 */
+
+typedef struct lm_ctx lm_ctx;
+typedef struct lm_lattice lm_lattice;
+typedef struct lm_ham lm_ham;
+typedef struct lm_state lm_state;
+typedef struct lm_solver lm_solver;
+
+/* Library version (major*10000 + minor*100 + patch). */
+int lm_version(void);
+
+/* ---- context ------------------------------------------------------------------------ */
+/* Creates a context on CUDA device `device` with its own stream. No reference counterpart:
+ * the reference runs on the CPU (src/evolution.jl:183-196 holds no device state). */
+int lm_ctx_create(int device, lm_ctx **out);
+int lm_ctx_destroy(lm_ctx *ctx);
+const char *lm_last_error(const lm_ctx *ctx);
+int lm_ctx_synchronize(lm_ctx *ctx);
+/* The context's CUDA stream (cudaStream_t), for callers that order their own work or
+ * CUDA events against the library's launches. */
+int lm_ctx_stream(lm_ctx *ctx, void **stream);
+/* Opt-in CUDA-event timing of the Chebyshev-order launches (for measurement); events are
+ * resolved lazily by lm_ctx_timing, so timing adds no host synchronisation per step. */
+int lm_ctx_set_timing(lm_ctx *ctx, int enable);
+int lm_ctx_timing(lm_ctx *ctx, double *order_ms, int64_t *order_launches, int64_t *launches);
+int lm_ctx_reset_timing(lm_ctx *ctx);
+
+/* ---- lattice ------------------------------------------------------------------------ */
+/* SquareLattice(Lx, Ly; boundaries=(:axis1 => theta_x, :axis2 => theta_y)); `ctx` may be NULL
+ * for a host-only lattice (bond and coordinate queries need no GPU).
+ * Replaces SquareLattice / span_unitcells / setboundaries (src/zoo/lattices.jl:131,
+ * src/lattices/bravais/lattice.jl:101-172, src/core/boundaries.jl:46-76, :219-226).
+ * periodic_* = 0 gives an open axis; twist_* is the TwistedBoundary angle (0 = periodic). */
+int lm_lattice_square(lm_ctx *ctx, int64_t Lx, int64_t Ly, int periodic_x, int periodic_y,
+                      double twist_x, double twist_y, lm_lattice **out);
+int lm_lattice_destroy(lm_lattice *lat);
+/* length(l) (src/lattices/bravais/lattice.jl:34). */
+int64_t lm_lattice_nsites(const lm_lattice *lat);
+/* Number of NearestNeighbor(1) bonds after boundary routing (src/core/bonds.jl:415-422). */
+int64_t lm_lattice_nbonds(const lm_lattice *lat);
+/* Bond list in iteration order, 1-based (src/core/bonds.jl:415-422,
+ * src/lattices/bravais/nearestneighbor.jl:97-131, src/core/boundaries.jl:251-289). */
+int lm_lattice_bonds(const lm_lattice *lat, int64_t *src, int64_t *dst);
+/* Site coordinates, x then y per site (2N doubles) (src/lattices/bravais/unitcell.jl:119-122). */
+int lm_lattice_coords(const lm_lattice *lat, double *xy);
+
+/* ---- Hamiltonian -------------------------------------------------------------------- */
+/* tightbinding_hamiltonian(l; t1) with on-device assembly.  Replaces
+ * construct_operator / OperatorBuilder / UniformMatrixBuilder
+ * (src/operators/constructoperator.jl:136-194, src/operators/builder.jl:86-151, :274-309). */
+int lm_ham_create(lm_ctx *ctx, lm_lattice *lat, double t1, lm_ham **out);
+int lm_ham_destroy(lm_ham *ham);
+/* Adds a gauge-field term; `amplitudes[k]` of lm_ham_assemble scales component k.
+ * `auto_pbc` = 1 applies adapt_field for lattices with boundaries (point fluxes become
+ * singular-gauge images, src/zoo/magneticfields.jl:237-266), as OperatorBuilder does by
+ * default (src/operators/builder.jl:165-174). */
+int lm_ham_add_field(lm_ham *ham, int kind, double px, double py, int auto_pbc, int *component);
+/* On-site term `LatticeValue => 1` (src/operators/constructoperator.jl:21-30); NULL clears. */
+int lm_ham_set_onsite(lm_ham *ham, const double *V);
+/* Evaluates H(t) on the device: H[i,j] = t1*f_b*exp(-2 pi i LI(r_i, r_j)), H[j,i] = conj,
+ * H[i,i] += V_i (src/operators/builder.jl:282-285, :296-309). */
+int lm_ham_assemble(lm_ham *ham, const double *amplitudes, int ncomponents);
+/* Stored entries of the assembled H as the reference's CSC (src/operators/builder.jl:143-151). */
+int lm_ham_nnz(lm_ham *ham, int64_t *nnz);
+int lm_ham_csc(lm_ham *ham, int64_t *colptr, int64_t *rowval, double *nzval);
+/* Gershgorin enclosure of the spectrum of the assembled H. */
+int lm_ham_bounds(lm_ham *ham, double *emin, double *emax);
+
+/* ---- states ------------------------------------------------------------------------- */
+/* Device state: a Ket block (N x M) or a density matrix (N x N).  The reference evolves
+ * `Ket`/`Operator` data in place (src/evolution.jl:69-80, :188-196). */
+int lm_state_create(lm_ctx *ctx, int64_t n, int64_t m, int kind, int precision, lm_state **out);
+int lm_state_destroy(lm_state *st);
+/* Host <-> device copies; `host` holds complex values in the state's precision,
+ * column-major with leading dimension `ld` (>= n). */
+int lm_state_upload(lm_state *st, const void *host, int64_t ld);
+int lm_state_download(lm_state *st, void *host, int64_t ld);
+/* Device-to-device copy of `src` into `dst` (same shape, kind and precision): the state
+ * copy `Evolution` makes at construction (src/evolution.jl:190-194). */
+int lm_state_copy(lm_state *dst, const lm_state *src);
+/* Current device buffer (it may change after a step) and its leading dimension. */
+int lm_state_device_ptr(lm_state *st, void **ptr, int64_t *ld);
+/* Ket weights w_m, so that P = sum_m w_m |psi_m><psi_m| for the readouts; NULL = all ones. */
+int lm_state_set_weights(lm_state *st, const double *w);
+/* Per-ket FP64 norms (m doubles). */
+int lm_state_norms(lm_state *st, double *out);
+/* Rescales every ket to the given FP64 norms (the FP32 form's periodic norm correction). */
+int lm_state_renormalize(lm_state *st, const double *target_norms);
+
+/* ---- evolution solver (the EvolutionSolver plugin, src/evolution.jl:5-33) ------------ */
+/* ChebyshevGPU(; tol): Chebyshev propagator exp(-i H dt) with truncation `tol`. */
+int lm_solver_create(lm_ctx *ctx, double tol, lm_solver **out);
+int lm_solver_destroy(lm_solver *s);
+/* update_solver!(solver, H, dt, force) (src/evolution.jl:83-92): recomputes the
+ * propagator unless H (same object, same assembly) and dt are unchanged and force = 0. */
+int lm_solver_update(lm_solver *s, lm_ham *ham, double dt, int force);
+/* Chebyshev order chosen by the last update (number of H applications per step). */
+int lm_solver_order(const lm_solver *s, int *K, double *a, double *b);
+/* step!(solver, state, cache) (src/evolution.jl:69-78): psi <- U psi for kets,
+ * P <- U P U^dagger for a density matrix. */
+int lm_solver_step(lm_solver *s, lm_state *st);
+
+/* Chebyshev plan (host only, needs no GPU): for x = a*|dt| >= 0 (a = spectral half-width)
+ * the order K >= 2 whose neglected tail 2*sum_{k>K}|J_k(x)| is below `tol`, and the
+ * coefficients c_k = (2 - delta_k0) (-i)^k J_k(x), k = 0..K, as (re, im) pairs in `coef`
+ * (room for `cap` coefficients).  Returns LM_ERR_ARG when cap < K + 1. */
+int lm_chebyshev_plan(double x, double tol, int cap, int *K, double *coef);
+
+/* ---- readouts ----------------------------------------------------------------------- */
+/* localdensity(state) (src/operators/latticeutils.jl:41-45): N doubles. */
+int lm_localdensity(lm_state *st, double *out);
+/* DensityCurrents(H, state) on every bond, J_b = 2 Im(H[i,j] P[j,i])
+ * (src/zoo/currents.jl:92-102), in lm_lattice_bonds order: nbonds doubles. */
+int lm_bond_currents(lm_ham *ham, lm_state *st, double *out);
+/* tr(P) = sum of the local densities, FP64 (particle number). */
+int lm_trace(lm_state *st, double *out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* LMGPU_H */

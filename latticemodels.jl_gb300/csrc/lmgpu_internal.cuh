@@ -1,0 +1,157 @@
+// Internal definitions shared by the lmgpu translation units (not part of the C ABI).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/lmgpu.h"
+
+namespace lmgpu {
+
+// ------------------------------------------------------------------------------------------
+// Square-lattice geometry.  Site index (0-based) s = (x-1)*Ly + (y-1) for x in 1..Lx,
+// y in 1..Ly: the reference sorts Bravais pointers lexicographically
+// (src/lattices/bravais/unitcell.jl:126-132), so y runs fastest.
+// ------------------------------------------------------------------------------------------
+struct Geom {
+    int64_t Lx, Ly, N;
+    int per_x, per_y;     // periodic axes
+    double twist_x, twist_y;
+};
+
+// Field component as evaluated by the assembly kernel.  `amp` is the time-dependent
+// amplitude (B or flux), the rest is fixed at creation.
+struct FieldComp {
+    int kind;             // LM_FIELD_*
+    int replicate;        // point flux replicated over the 3^d boundary images (singular gauge)
+    double px, py;
+};
+
+constexpr int kMaxFields = 8;
+
+struct FieldSet {
+    int n;
+    FieldComp c[kMaxFields];
+    double amp[kMaxFields];
+};
+
+// Per-order launch description of the Chebyshev recurrence.
+enum ChebMode { CHEB_FIRST = 0, CHEB_MID = 1, CHEB_LAST = 2 };
+
+template <typename R> struct V2;
+template <> struct V2<double> { typedef double2 T; };
+template <> struct V2<float> { typedef float2 T; };
+
+struct ChebCoef {
+    double s;        // real magnitude with sign: c_k = s (k even) or -i*s (k odd)
+    int odd;         // parity of k
+};
+
+}  // namespace lmgpu
+
+// ------------------------------------------------------------------------------------------
+// Opaque handle bodies.
+// ------------------------------------------------------------------------------------------
+struct lm_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    int sm_count = 0;
+    std::string err;
+    int timing = 0;
+    std::vector<cudaEvent_t> ev_pool;   // pairs (start, stop) of timed Chebyshev sweeps
+    std::vector<int> ev_launches;       // launches covered by each recorded pair
+    size_t ev_used = 0;                 // pairs recorded but not yet resolved
+    double order_ms = 0.0;         // accumulated device time of Chebyshev-order launches
+    int64_t order_launches = 0;
+    int64_t launches = 0;          // every kernel launched by the library
+    double* d_red = nullptr;       // small reduction scratch (owned)
+    size_t red_cap = 0;
+};
+
+struct lm_lattice {
+    lm_ctx* ctx = nullptr;
+    lmgpu::Geom g{};
+    int64_t nbonds = 0;
+};
+
+struct lm_ham {
+    lm_ctx* ctx = nullptr;
+    lm_lattice* lat = nullptr;
+    double t1 = 1.0;
+    lmgpu::FieldSet fields{};
+    double* d_onsite = nullptr;     // raw on-site V (N) or null
+    double vmin = 0.0, vmax = 0.0;  // on-site extrema (host-side bookkeeping)
+    double2* d_hop = nullptr;       // raw H[s, s+x] (N) then H[s, s+y] (N)
+    uint64_t version = 0;           // bumps on every assembly
+    int assembled = 0;
+    std::vector<double> last_amp;
+};
+
+struct lm_state {
+    lm_ctx* ctx = nullptr;
+    int64_t n = 0, m = 0, ld = 0;
+    int kind = LM_KETS;
+    int precision = LM_C64;
+    void* d_data = nullptr;   // current state buffer
+    void* d_a = nullptr;      // recurrence scratch
+    void* d_y = nullptr;      // accumulator scratch
+    double* d_w = nullptr;    // ket weights (m) or null (= all ones)
+    size_t elem = 16;
+};
+
+struct lm_solver {
+    lm_ctx* ctx = nullptr;
+    double tol = 1e-12;
+    int precision_hint = -1;
+    // cache key (update_solver! semantics)
+    const lm_ham* ham = nullptr;
+    uint64_t ham_version = ~0ull;
+    double dt = 0.0;
+    int valid = 0;
+    // propagator
+    double a = 1.0, b = 0.0;
+    int K = 0;
+    std::vector<lmgpu::ChebCoef> coef;  // k = 0..K
+    double phase_re = 1.0, phase_im = 0.0;
+    // normalised stencil tables: 2*H/a hops and 2*(V-b)/a diagonal
+    double2* d_hop2 = nullptr;  double* d_diag2 = nullptr;
+    float2* d_hop2f = nullptr;  float* d_diag2f = nullptr;
+    int64_t tab_n = 0;
+    int has_onsite = 0;
+};
+
+namespace lmgpu {
+
+int set_err(lm_ctx* ctx, int code, const std::string& msg);
+int check_cuda(lm_ctx* ctx, cudaError_t e, const char* what);
+
+// Kernel launchers (lmgpu_kernels.cu).  All launch on ctx->stream and return cudaError_t.
+cudaError_t launch_assemble(lm_ctx* ctx, const Geom& g, const FieldSet& f, double t1, double2* hop);
+cudaError_t launch_normalise(lm_ctx* ctx, const Geom& g, const double2* hop, const double* onsite,
+                             double a, double b, double2* hop2, double* diag2, float2* hop2f,
+                             float* diag2f);
+cudaError_t launch_cheb_order(lm_ctx* ctx, const Geom& g, int precision, int site_fast, int conj,
+                              int mode, const void* hop2, const void* diag2, const void* tp, void* tq,
+                              void* y, int64_t ld, int64_t m, double c0, ChebCoef ck,
+                              double ph_re, double ph_im);
+cudaError_t launch_scale(lm_ctx* ctx, int precision, void* x, int64_t n, int64_t m, int64_t ld,
+                         double re, double im);
+cudaError_t launch_localdensity(lm_ctx* ctx, int precision, int kind, const void* x, int64_t n,
+                                int64_t m, int64_t ld, const double* w, double* out);
+cudaError_t launch_bond_currents(lm_ctx* ctx, const Geom& g, int precision, int kind, const double2* hop,
+                                 const void* x, int64_t m, int64_t ld, const double* w, double* out);
+cudaError_t launch_column_norms(lm_ctx* ctx, int precision, const void* x, int64_t n, int64_t m,
+                                int64_t ld, double* out);
+cudaError_t launch_rescale_columns(lm_ctx* ctx, int precision, void* x, int64_t n, int64_t m,
+                                   int64_t ld, const double* norms, const double* target);
+cudaError_t launch_sum(lm_ctx* ctx, const double* v, int64_t n, double* out1);
+cudaError_t launch_convert(lm_ctx* ctx, int to_precision, const void* src, void* dst, int64_t n,
+                           int64_t m, int64_t ld_src, int64_t ld_dst);
+
+// Host math (lmgpu_api.cu)
+int64_t bond_count(const Geom& g);
+void bessel_j_all(double x, int kmax, std::vector<double>& out);
+
+}  // namespace lmgpu

@@ -1,0 +1,582 @@
+// CUDA kernels of the lmgpu evolution backend (sm_103a).
+//
+// Hot path: one Chebyshev order of exp(-i H dt) applied to a block of kets, with H the
+// nearest-neighbour tight-binding stencil of a square lattice whose hopping phases and
+// on-site terms are assembled on the device.  Every kernel launches on the context stream.
+#include <cuda_runtime.h>
+#include <math.h>
+
+#include "lmgpu_internal.cuh"
+
+namespace lmgpu {
+
+// ------------------------------------------------------------------------------------------
+// Complex helpers (no fused contraction where the reference's rounding is restated).
+// ------------------------------------------------------------------------------------------
+__device__ __forceinline__ double2 cmul_rn(double2 a, double2 b) {
+    return make_double2(__dsub_rn(__dmul_rn(a.x, b.x), __dmul_rn(a.y, b.y)),
+                        __dadd_rn(__dmul_rn(a.x, b.y), __dmul_rn(a.y, b.x)));
+}
+
+template <typename T> struct CT;
+template <> struct CT<double> {
+    typedef double2 V;
+    static __device__ __forceinline__ V make(double a, double b) { return make_double2(a, b); }
+};
+template <> struct CT<float> {
+    typedef float2 V;
+    static __device__ __forceinline__ V make(float a, float b) { return make_float2(a, b); }
+};
+
+// ------------------------------------------------------------------------------------------
+// Neighbour routing on the square lattice (src/core/boundaries.jl:251-289 for the periodic
+// case: a destination one step outside is wrapped by the axis translation).
+// ------------------------------------------------------------------------------------------
+struct Nbr {
+    int64_t xp, xm, yp, ym;   // neighbour site indices (self when the bond is absent)
+    bool hxp, hxm, hyp, hym;  // bond present
+};
+
+__device__ __forceinline__ Nbr neighbours(const Geom& g, int64_t s) {
+    Nbr n;
+    const int64_t xi = s / g.Ly, yi = s - xi * g.Ly;
+    // +x
+    if (xi + 1 < g.Lx) { n.xp = s + g.Ly; n.hxp = true; }
+    else if (g.per_x) { n.xp = yi; n.hxp = true; }
+    else { n.xp = s; n.hxp = false; }
+    // -x
+    if (xi > 0) { n.xm = s - g.Ly; n.hxm = true; }
+    else if (g.per_x) { n.xm = (g.Lx - 1) * g.Ly + yi; n.hxm = true; }
+    else { n.xm = s; n.hxm = false; }
+    // +y
+    if (yi + 1 < g.Ly) { n.yp = s + 1; n.hyp = true; }
+    else if (g.per_y) { n.yp = s - yi; n.hyp = true; }
+    else { n.yp = s; n.hyp = false; }
+    // -y
+    if (yi > 0) { n.ym = s - 1; n.hym = true; }
+    else if (g.per_y) { n.ym = s + g.Ly - 1; n.hym = true; }
+    else { n.ym = s; n.hym = false; }
+    return n;
+}
+
+// ------------------------------------------------------------------------------------------
+// Line integrals of the gauge fields, evaluated exactly as written in the reference
+// (src/zoo/magneticfields.jl:15, :31, :72-85, :89-104), without contraction.
+// ------------------------------------------------------------------------------------------
+__device__ double li_pointflux_axial(double flux, double px, double py, double x1, double y1,
+                                     double x2, double y2) {
+    x1 = __dsub_rn(x1, px); y1 = __dsub_rn(y1, py);
+    x2 = __dsub_rn(x2, px); y2 = __dsub_rn(y2, py);
+    const double n1 = sqrt(__dadd_rn(__dmul_rn(x1, x1), __dmul_rn(y1, y1)));
+    const double n2 = sqrt(__dadd_rn(__dmul_rn(x2, x2), __dmul_rn(y2, y2)));
+    if (n1 < 1e-11 || n2 < 1e-11) return 0.0 * flux;
+    const double nnorm = __dmul_rn(n1, n2);
+    const double det = __dsub_rn(__dmul_rn(x1, y2), __dmul_rn(x2, y1));
+    const double dot = __dadd_rn(__dmul_rn(x1, x2), __dmul_rn(y1, y2));
+    const double cosang = __ddiv_rn(__ddiv_rn(dot, nnorm), 1.0 + 1e-11);
+    const double sgn = (det > 0.0) ? 1.0 : ((det < 0.0) ? -1.0 : 0.0);
+    const double angle = __dmul_rn(acos(cosang), sgn);
+    return __ddiv_rn(__dmul_rn(angle, flux), 2.0 * M_PI);
+}
+
+__device__ double li_pointflux_singular(double flux, double px, double py, double x1, double y1,
+                                        double x2, double y2) {
+    x1 = __dsub_rn(x1, px); y1 = __dsub_rn(y1, py);
+    x2 = __dsub_rn(x2, px); y2 = __dsub_rn(y2, py);
+    const double sg = __dsub_rn(x2, x1);
+    if (fabs(sg) < 1e-11) return 0.0 * flux;
+    if (__dmul_rn(x1, x2) > 0.0 || fmax(x1, x2) == 0.0) return 0.0 * flux;
+    const double yint = __ddiv_rn(__dadd_rn(__dmul_rn(-y1, x2), __dmul_rn(y2, x1)), __dsub_rn(x1, x2));
+    if (yint > 0.0) return 0.0 * flux;
+    return __dmul_rn(flux, (sg > 0.0) ? 1.0 : -1.0);
+}
+
+__device__ double line_integral(const Geom& g, const FieldSet& f, double x1, double y1, double x2,
+                                double y2) {
+    double li = 0.0;
+    for (int c = 0; c < f.n; ++c) {
+        const FieldComp fc = f.c[c];
+        const double A = f.amp[c];
+        double v = 0.0;
+        switch (fc.kind) {
+            case LM_FIELD_LANDAU:  // (x1+x2)*(y2-y1)*B/2
+                v = __ddiv_rn(__dmul_rn(__dmul_rn(__dadd_rn(x1, x2), __dsub_rn(y2, y1)), A), 2.0);
+                break;
+            case LM_FIELD_SYMMETRIC:  // (x1*y2 - x2*y1)/2*B
+                v = __dmul_rn(__ddiv_rn(__dsub_rn(__dmul_rn(x1, y2), __dmul_rn(x2, y1)), 2.0), A);
+                break;
+            case LM_FIELD_POINTFLUX_AXIAL:
+            case LM_FIELD_POINTFLUX_SINGULAR:
+                if (fc.replicate) {
+                    // adapt_field: images p - sum_i n_i T_i over CartesianIndex(-1..1)^d,
+                    // first boundary fastest, singular gauge (magneticfields.jl:237-266)
+                    const int nb = (g.per_x ? 1 : 0) + (g.per_y ? 1 : 0);
+                    const int nimg = (nb == 2) ? 9 : 3;
+                    double acc = 0.0;
+                    for (int im = 0; im < nimg; ++im) {
+                        int n0 = im % 3 - 1, n1 = im / 3 - 1;
+                        double rx = 0.0, ry = 0.0;
+                        if (g.per_x && g.per_y) {
+                            rx = -(double)n0 * (double)g.Lx;
+                            ry = -(double)n1 * (double)g.Ly;
+                        } else if (g.per_x) {
+                            rx = -(double)n0 * (double)g.Lx;
+                        } else {
+                            ry = -(double)n0 * (double)g.Ly;
+                        }
+                        const double t = li_pointflux_singular(A, __dadd_rn(fc.px, rx), __dadd_rn(fc.py, ry),
+                                                               x1, y1, x2, y2);
+                        acc = (im == 0) ? t : __dadd_rn(acc, t);
+                    }
+                    v = acc;
+                } else if (fc.kind == LM_FIELD_POINTFLUX_AXIAL) {
+                    v = li_pointflux_axial(A, fc.px, fc.py, x1, y1, x2, y2);
+                } else {
+                    v = li_pointflux_singular(A, fc.px, fc.py, x1, y1, x2, y2);
+                }
+                break;
+            default:
+                v = 0.0;
+        }
+        li = (c == 0) ? v : __dadd_rn(li, v);
+    }
+    return li;
+}
+
+// H[s, s+e] = t1 * f * exp(-2 pi i LI(r_s, r_s + e)) for e = x (dir 0) and y (dir 1);
+// absent bonds store 0 (src/operators/builder.jl:282-285).
+__global__ void assemble_kernel(Geom g, FieldSet f, double t1, double2* __restrict__ hop) {
+    const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= g.N) return;
+    const int64_t xi = s / g.Ly, yi = s - xi * g.Ly;
+    const double x1 = (double)(xi + 1), y1 = (double)(yi + 1);
+#pragma unroll
+    for (int dir = 0; dir < 2; ++dir) {
+        const bool inside = (dir == 0) ? (xi + 1 < g.Lx) : (yi + 1 < g.Ly);
+        const bool per = (dir == 0) ? g.per_x : g.per_y;
+        double2 val = make_double2(0.0, 0.0);
+        if (inside || per) {
+            const double x2 = (dir == 0) ? x1 + 1.0 : x1;  // unwrapped destination (old_site)
+            const double y2 = (dir == 0) ? y1 : y1 + 1.0;
+            double2 fac = make_double2(1.0, 0.0);
+            if (!inside) {
+                const double th = (dir == 0) ? g.twist_x : g.twist_y;
+                if (th != 0.0) {
+                    double sn, cs;
+                    sincos(th, &sn, &cs);
+                    fac = make_double2(cs, sn);
+                }
+            }
+            const double li = (f.n > 0) ? line_integral(g, f, x1, y1, x2, y2) : 0.0;
+            const double theta = __dmul_rn(-2.0 * M_PI, li);
+            double sn, cs;
+            sincos(theta, &sn, &cs);
+            const double2 tot = cmul_rn(fac, make_double2(cs, sn));
+            val = make_double2(__dmul_rn(t1, tot.x), __dmul_rn(t1, tot.y));
+        }
+        hop[dir * g.N + s] = val;
+    }
+}
+
+cudaError_t launch_assemble(lm_ctx* ctx, const Geom& g, const FieldSet& f, double t1, double2* hop) {
+    const int thr = 128;
+    const int64_t blocks = (g.N + thr - 1) / thr;
+    assemble_kernel<<<(unsigned)blocks, thr, 0, ctx->stream>>>(g, f, t1, hop);
+    ctx->launches++;
+    return cudaGetLastError();
+}
+
+// 2*H/a hopping and 2*(V-b)/a diagonal tables in FP64 and FP32.
+__global__ void normalise_kernel(int64_t N, const double2* __restrict__ hop, const double* __restrict__ onsite,
+                                 double a, double b, double2* __restrict__ hop2, double* __restrict__ diag2,
+                                 float2* __restrict__ hop2f, float* __restrict__ diag2f) {
+    const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= N) return;
+    const double sc = 2.0 / a;
+#pragma unroll
+    for (int dir = 0; dir < 2; ++dir) {
+        const double2 h = hop[dir * N + s];
+        const double2 v = make_double2(h.x * sc, h.y * sc);
+        hop2[dir * N + s] = v;
+        hop2f[dir * N + s] = make_float2((float)v.x, (float)v.y);
+    }
+    const double V = onsite ? onsite[s] : 0.0;
+    const double d = (V - b) * sc;
+    diag2[s] = d;
+    diag2f[s] = (float)d;
+}
+
+cudaError_t launch_normalise(lm_ctx* ctx, const Geom& g, const double2* hop, const double* onsite, double a,
+                             double b, double2* hop2, double* diag2, float2* hop2f, float* diag2f) {
+    const int thr = 256;
+    const int64_t blocks = (g.N + thr - 1) / thr;
+    normalise_kernel<<<(unsigned)blocks, thr, 0, ctx->stream>>>(g.N, hop, onsite, a, b, hop2, diag2, hop2f, diag2f);
+    ctx->launches++;
+    return cudaGetLastError();
+}
+
+// ------------------------------------------------------------------------------------------
+// One order of the Chebyshev recurrence for exp(-i H dt), H~ = (H - b)/a:
+//   FIRST: T1 = H~ T0            -> tq;   y  = c0 T0 + c1 T1
+//   MID  : Tk = 2 H~ T(k-1) - T(k-2) -> tq (in place over T(k-2));  y += ck Tk
+//   LAST : out = phase * (y + cK TK)   -> tq (in place over T(K-2))
+// c_k = s (k even) or -i s (k odd); the tables hold 2H/a and 2(V-b)/a.
+// Layout: SITE_FAST -> element (site, ket) at ket*ld + site (column-major ket block);
+//         otherwise   -> element (site, ket) at site*ld + ket (row of a column-major matrix).
+// CONJ applies conj(H) (used for the right factor U^dagger of a density-matrix step).
+// ------------------------------------------------------------------------------------------
+template <typename R, int MODE, bool SITE_FAST, bool CONJ, int INNER>
+__global__ void __launch_bounds__(256) cheb_order_kernel(
+    Geom g, const typename CT<R>::V* __restrict__ hop2, const R* __restrict__ diag2,
+    const typename CT<R>::V* __restrict__ tp, typename CT<R>::V* tq, typename CT<R>::V* y,
+    int64_t ld, int64_t M, R c0, R cs, int odd, R ph_re, R ph_im) {
+    typedef typename CT<R>::V V;
+    const int64_t lane = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;  // fast dimension
+    const int64_t nfast = SITE_FAST ? g.N : M;
+    const int64_t nslow = SITE_FAST ? M : g.N;
+    if (lane >= nfast) return;
+
+    // SITE_FAST: the site is fixed per thread, so its stencil row is loaded once.
+    Nbr nb;
+    V hxp, hxm, hyp, hym;
+    R d = 0;
+    auto load_row = [&](int64_t s) {
+        nb = neighbours(g, s);
+        V z = CT<R>::make(0, 0);
+        hxp = nb.hxp ? hop2[s] : z;
+        hyp = nb.hyp ? hop2[g.N + s] : z;
+        V t = nb.hxm ? hop2[nb.xm] : z;  // H[s, s-x] = conj(H[s-x, s])
+        hxm = CT<R>::make(t.x, -t.y);
+        t = nb.hym ? hop2[g.N + nb.ym] : z;
+        hym = CT<R>::make(t.x, -t.y);
+        if (CONJ) {
+            hxp.y = -hxp.y; hyp.y = -hyp.y; hxm.y = -hxm.y; hym.y = -hym.y;
+        }
+        d = diag2[s];
+    };
+    if (SITE_FAST) load_row(lane);
+
+    for (int64_t g0 = (int64_t)blockIdx.y * INNER; g0 < nslow; g0 += (int64_t)gridDim.y * INNER) {
+#pragma unroll
+        for (int j = 0; j < INNER; ++j) {
+            const int64_t slow = g0 + j;
+            if (slow >= nslow) break;
+            int64_t site, ket;
+            if (SITE_FAST) { site = lane; ket = slow; }
+            else { site = slow; ket = lane; load_row(site); }
+            auto at = [&](int64_t s) -> int64_t { return SITE_FAST ? ket * ld + s : s * ld + ket; };
+            const V v0 = tp[at(site)];
+            const V vxp = tp[at(nb.xp)], vxm = tp[at(nb.xm)];
+            const V vyp = tp[at(nb.yp)], vym = tp[at(nb.ym)];
+            V acc;
+            if (MODE == CHEB_FIRST) {
+                acc = CT<R>::make(0, 0);
+            } else {
+                const V q = tq[at(site)];
+                acc = CT<R>::make(-q.x, -q.y);
+            }
+            acc.x = fma(hxp.x, vxp.x, acc.x); acc.x = fma(-hxp.y, vxp.y, acc.x);
+            acc.y = fma(hxp.x, vxp.y, acc.y); acc.y = fma(hxp.y, vxp.x, acc.y);
+            acc.x = fma(hxm.x, vxm.x, acc.x); acc.x = fma(-hxm.y, vxm.y, acc.x);
+            acc.y = fma(hxm.x, vxm.y, acc.y); acc.y = fma(hxm.y, vxm.x, acc.y);
+            acc.x = fma(hyp.x, vyp.x, acc.x); acc.x = fma(-hyp.y, vyp.y, acc.x);
+            acc.y = fma(hyp.x, vyp.y, acc.y); acc.y = fma(hyp.y, vyp.x, acc.y);
+            acc.x = fma(hym.x, vym.x, acc.x); acc.x = fma(-hym.y, vym.y, acc.x);
+            acc.y = fma(hym.x, vym.y, acc.y); acc.y = fma(hym.y, vym.x, acc.y);
+            acc.x = fma(d, v0.x, acc.x);
+            acc.y = fma(d, v0.y, acc.y);
+            if (MODE == CHEB_FIRST) {
+                // T1 = (sum)/2 exactly, y = c0 T0 + c1 T1 with c1 = -i s (or +i s when conj)
+                const V t1 = CT<R>::make(acc.x * R(0.5), acc.y * R(0.5));
+                tq[at(site)] = t1;
+                V yy;
+                yy.x = fma(cs, t1.y, c0 * v0.x);
+                yy.y = fma(-cs, t1.x, c0 * v0.y);
+                y[at(site)] = yy;
+            } else {
+                V yy = y[at(site)];
+                if (odd) {
+                    yy.x = fma(cs, acc.y, yy.x);
+                    yy.y = fma(-cs, acc.x, yy.y);
+                } else {
+                    yy.x = fma(cs, acc.x, yy.x);
+                    yy.y = fma(cs, acc.y, yy.y);
+                }
+                if (MODE == CHEB_MID) {
+                    tq[at(site)] = acc;
+                    y[at(site)] = yy;
+                } else {
+                    V o;
+                    o.x = fma(ph_re, yy.x, -ph_im * yy.y);
+                    o.y = fma(ph_re, yy.y, ph_im * yy.x);
+                    tq[at(site)] = o;
+                }
+            }
+        }
+    }
+}
+
+template <typename R, int MODE, bool SF, bool CJ>
+static void launch_cheb_t(lm_ctx* ctx, const Geom& g, const void* hop2, const void* diag2, const void* tp,
+                          void* tq, void* y, int64_t ld, int64_t m, double c0, ChebCoef ck, double ph_re,
+                          double ph_im) {
+    typedef typename CT<R>::V V;
+    constexpr int INNER = 4;
+    const int thr = SF ? 256 : 128;
+    const int64_t nfast = SF ? g.N : m;
+    const int64_t nslow = SF ? m : g.N;
+    const int64_t gx = (nfast + thr - 1) / thr;
+    int64_t gy = (nslow + INNER - 1) / INNER;
+    if (gy > 65535) gy = 65535;
+    dim3 grid((unsigned)gx, (unsigned)gy);
+    cheb_order_kernel<R, MODE, SF, CJ, INNER><<<grid, thr, 0, ctx->stream>>>(
+        g, (const V*)hop2, (const R*)diag2, (const V*)tp, (V*)tq, (V*)y, ld, m, (R)c0, (R)ck.s, ck.odd,
+        (R)ph_re, (R)ph_im);
+}
+
+template <typename R, bool SF, bool CJ>
+static void dispatch_mode(int mode, lm_ctx* ctx, const Geom& g, const void* hop2, const void* diag2,
+                          const void* tp, void* tq, void* y, int64_t ld, int64_t m, double c0, ChebCoef ck,
+                          double pr, double pi) {
+    if (mode == CHEB_FIRST) launch_cheb_t<R, CHEB_FIRST, SF, CJ>(ctx, g, hop2, diag2, tp, tq, y, ld, m, c0, ck, pr, pi);
+    else if (mode == CHEB_MID) launch_cheb_t<R, CHEB_MID, SF, CJ>(ctx, g, hop2, diag2, tp, tq, y, ld, m, c0, ck, pr, pi);
+    else launch_cheb_t<R, CHEB_LAST, SF, CJ>(ctx, g, hop2, diag2, tp, tq, y, ld, m, c0, ck, pr, pi);
+}
+
+cudaError_t launch_cheb_order(lm_ctx* ctx, const Geom& g, int precision, int site_fast, int conj, int mode,
+                              const void* hop2, const void* diag2, const void* tp, void* tq, void* y,
+                              int64_t ld, int64_t m, double c0, ChebCoef ck, double ph_re, double ph_im) {
+    if (precision == LM_C64) {
+        if (site_fast) {
+            if (conj) dispatch_mode<double, true, true>(mode, ctx, g, hop2, diag2, tp, tq, y, ld, m, c0, ck, ph_re, ph_im);
+            else dispatch_mode<double, true, false>(mode, ctx, g, hop2, diag2, tp, tq, y, ld, m, c0, ck, ph_re, ph_im);
+        } else {
+            if (conj) dispatch_mode<double, false, true>(mode, ctx, g, hop2, diag2, tp, tq, y, ld, m, c0, ck, ph_re, ph_im);
+            else dispatch_mode<double, false, false>(mode, ctx, g, hop2, diag2, tp, tq, y, ld, m, c0, ck, ph_re, ph_im);
+        }
+    } else {
+        if (site_fast) {
+            if (conj) dispatch_mode<float, true, true>(mode, ctx, g, hop2, diag2, tp, tq, y, ld, m, c0, ck, ph_re, ph_im);
+            else dispatch_mode<float, true, false>(mode, ctx, g, hop2, diag2, tp, tq, y, ld, m, c0, ck, ph_re, ph_im);
+        } else {
+            if (conj) dispatch_mode<float, false, true>(mode, ctx, g, hop2, diag2, tp, tq, y, ld, m, c0, ck, ph_re, ph_im);
+            else dispatch_mode<float, false, false>(mode, ctx, g, hop2, diag2, tp, tq, y, ld, m, c0, ck, ph_re, ph_im);
+        }
+    }
+    ctx->launches++;
+    return cudaGetLastError();
+}
+
+// ------------------------------------------------------------------------------------------
+// Elementwise helpers
+// ------------------------------------------------------------------------------------------
+template <typename R>
+__global__ void scale_kernel(typename CT<R>::V* x, int64_t n, int64_t m, int64_t ld, R re, R im) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    for (int64_t k = blockIdx.y; k < m; k += gridDim.y) {
+        typename CT<R>::V v = x[k * ld + i];
+        x[k * ld + i] = CT<R>::make(re * v.x - im * v.y, re * v.y + im * v.x);
+    }
+}
+
+cudaError_t launch_scale(lm_ctx* ctx, int precision, void* x, int64_t n, int64_t m, int64_t ld, double re,
+                         double im) {
+    dim3 grid((unsigned)((n + 255) / 256), (unsigned)(m < 65535 ? m : 65535));
+    if (precision == LM_C64) scale_kernel<double><<<grid, 256, 0, ctx->stream>>>((double2*)x, n, m, ld, re, im);
+    else scale_kernel<float><<<grid, 256, 0, ctx->stream>>>((float2*)x, n, m, ld, (float)re, (float)im);
+    ctx->launches++;
+    return cudaGetLastError();
+}
+
+template <typename RS, typename RD>
+__global__ void convert_kernel(const typename CT<RS>::V* src, typename CT<RD>::V* dst, int64_t n, int64_t m,
+                               int64_t lds, int64_t ldd) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    for (int64_t k = blockIdx.y; k < m; k += gridDim.y) {
+        typename CT<RS>::V v = src[k * lds + i];
+        dst[k * ldd + i] = CT<RD>::make((RD)v.x, (RD)v.y);
+    }
+}
+
+cudaError_t launch_convert(lm_ctx* ctx, int to_precision, const void* src, void* dst, int64_t n, int64_t m,
+                           int64_t ld_src, int64_t ld_dst) {
+    dim3 grid((unsigned)((n + 255) / 256), (unsigned)(m < 65535 ? m : 65535));
+    if (to_precision == LM_C32)
+        convert_kernel<double, float><<<grid, 256, 0, ctx->stream>>>((const double2*)src, (float2*)dst, n, m, ld_src, ld_dst);
+    else
+        convert_kernel<float, double><<<grid, 256, 0, ctx->stream>>>((const float2*)src, (double2*)dst, n, m, ld_src, ld_dst);
+    ctx->launches++;
+    return cudaGetLastError();
+}
+
+// ------------------------------------------------------------------------------------------
+// Readouts (FP64 accumulation)
+// ------------------------------------------------------------------------------------------
+// localdensity: rho_s = sum_m w_m |psi_sm|^2 (kets) or Re P[s,s] (density matrix).
+template <typename R>
+__global__ void localdensity_kernel(int kind, const typename CT<R>::V* __restrict__ x, int64_t n, int64_t m,
+                                    int64_t ld, const double* __restrict__ w, double* __restrict__ out) {
+    const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    if (kind == LM_DENSITY) {
+        out[s] = (double)x[s * ld + s].x;
+        return;
+    }
+    double acc = 0.0;
+    for (int64_t k = 0; k < m; ++k) {
+        const typename CT<R>::V v = x[k * ld + s];
+        const double p = (double)v.x * (double)v.x + (double)v.y * (double)v.y;
+        acc += w ? w[k] * p : p;
+    }
+    out[s] = acc;
+}
+
+cudaError_t launch_localdensity(lm_ctx* ctx, int precision, int kind, const void* x, int64_t n, int64_t m,
+                                int64_t ld, const double* w, double* out) {
+    const int thr = 128;
+    const unsigned blocks = (unsigned)((n + thr - 1) / thr);
+    if (precision == LM_C64) localdensity_kernel<double><<<blocks, thr, 0, ctx->stream>>>(kind, (const double2*)x, n, m, ld, w, out);
+    else localdensity_kernel<float><<<blocks, thr, 0, ctx->stream>>>(kind, (const float2*)x, n, m, ld, w, out);
+    ctx->launches++;
+    return cudaGetLastError();
+}
+
+// Bond currents J = 2 Im(H[i,j] P[j,i]) for the +x and +y bond of every site, written in the
+// reference's bond order (all +x bonds in source order, then all +y bonds).  H[i,j] is the
+// accumulated matrix entry: on a 2-site periodic axis the reverse bond adds conj(H[j,i]).
+template <typename R>
+__global__ void bond_currents_kernel(Geom g, int kind, const double2* __restrict__ hop,
+                                     const typename CT<R>::V* __restrict__ x, int64_t m, int64_t ld,
+                                     const double* __restrict__ w, double* __restrict__ out) {
+    const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= g.N) return;
+    const Nbr nb = neighbours(g, s);
+    const int64_t xi = s / g.Ly, yi = s - xi * g.Ly;
+    const int64_t nbx = g.per_x ? g.N : (g.Lx - 1) * g.Ly;
+#pragma unroll
+    for (int dir = 0; dir < 2; ++dir) {
+        const bool has = dir == 0 ? nb.hxp : nb.hyp;
+        if (!has) continue;
+        const int64_t j = dir == 0 ? nb.xp : nb.yp;
+        const int64_t jm = dir == 0 ? nb.xm : nb.ym;
+        double2 h = hop[dir * g.N + s];
+        if (j == jm) {  // two-site periodic axis: both bonds join s and j
+            const double2 r = hop[dir * g.N + j];
+            h.x += r.x;
+            h.y -= r.y;
+        }
+        double pr = 0.0, pi = 0.0;  // P[j, s]
+        if (kind == LM_DENSITY) {
+            const typename CT<R>::V v = x[s * ld + j];
+            pr = v.x; pi = v.y;
+        } else {
+            for (int64_t k = 0; k < m; ++k) {
+                const typename CT<R>::V a = x[k * ld + j], b = x[k * ld + s];  // a * conj(b)
+                const double re = (double)a.x * (double)b.x + (double)a.y * (double)b.y;
+                const double im = (double)a.y * (double)b.x - (double)a.x * (double)b.y;
+                const double ww = w ? w[k] : 1.0;
+                pr += ww * re;
+                pi += ww * im;
+            }
+        }
+        const double J = 2.0 * (h.x * pi + h.y * pr);  // Im(h * p)
+        int64_t bidx;
+        if (dir == 0) bidx = s;
+        else bidx = nbx + (g.per_y ? s : xi * (g.Ly - 1) + yi);
+        out[bidx] = J;
+    }
+}
+
+cudaError_t launch_bond_currents(lm_ctx* ctx, const Geom& g, int precision, int kind, const double2* hop,
+                                 const void* x, int64_t m, int64_t ld, const double* w, double* out) {
+    const int thr = 128;
+    const unsigned blocks = (unsigned)((g.N + thr - 1) / thr);
+    if (precision == LM_C64)
+        bond_currents_kernel<double><<<blocks, thr, 0, ctx->stream>>>(g, kind, hop, (const double2*)x, m, ld, w, out);
+    else
+        bond_currents_kernel<float><<<blocks, thr, 0, ctx->stream>>>(g, kind, hop, (const float2*)x, m, ld, w, out);
+    ctx->launches++;
+    return cudaGetLastError();
+}
+
+// Per-column FP64 norms: one block per column.
+template <typename R>
+__global__ void column_norms_kernel(const typename CT<R>::V* __restrict__ x, int64_t n, int64_t ld,
+                                    double* __restrict__ out) {
+    __shared__ double red[32];
+    const int64_t k = blockIdx.x;
+    double acc = 0.0;
+    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+        const typename CT<R>::V v = x[k * ld + i];
+        acc += (double)v.x * (double)v.x + (double)v.y * (double)v.y;
+    }
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        acc = (threadIdx.x < (blockDim.x >> 5)) ? red[threadIdx.x] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+        if (threadIdx.x == 0) out[k] = sqrt(acc);
+    }
+}
+
+cudaError_t launch_column_norms(lm_ctx* ctx, int precision, const void* x, int64_t n, int64_t m, int64_t ld,
+                                double* out) {
+    if (m <= 0) return cudaSuccess;
+    if (precision == LM_C64) column_norms_kernel<double><<<(unsigned)m, 256, 0, ctx->stream>>>((const double2*)x, n, ld, out);
+    else column_norms_kernel<float><<<(unsigned)m, 256, 0, ctx->stream>>>((const float2*)x, n, ld, out);
+    ctx->launches++;
+    return cudaGetLastError();
+}
+
+template <typename R>
+__global__ void rescale_columns_kernel(typename CT<R>::V* x, int64_t n, int64_t m, int64_t ld,
+                                       const double* __restrict__ norms, const double* __restrict__ target) {
+    for (int64_t k = blockIdx.y; k < m; k += gridDim.y) {
+        const double nk = norms[k];
+        const R f = (R)(nk > 0.0 ? target[k] / nk : 1.0);
+        for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+            typename CT<R>::V v = x[k * ld + i];
+            v.x *= f;
+            v.y *= f;
+            x[k * ld + i] = v;
+        }
+    }
+}
+
+cudaError_t launch_rescale_columns(lm_ctx* ctx, int precision, void* x, int64_t n, int64_t m, int64_t ld,
+                                   const double* norms, const double* target) {
+    if (m <= 0) return cudaSuccess;
+    int64_t bx = (n + 255) / 256;
+    if (bx > 1024) bx = 1024;
+    dim3 grid((unsigned)bx, (unsigned)(m < 65535 ? m : 65535));
+    if (precision == LM_C64) rescale_columns_kernel<double><<<grid, 256, 0, ctx->stream>>>((double2*)x, n, m, ld, norms, target);
+    else rescale_columns_kernel<float><<<grid, 256, 0, ctx->stream>>>((float2*)x, n, m, ld, norms, target);
+    ctx->launches++;
+    return cudaGetLastError();
+}
+
+// Single-block FP64 sum (deterministic order).
+__global__ void sum_kernel(const double* __restrict__ v, int64_t n, double* __restrict__ out) {
+    __shared__ double red[32];
+    double acc = 0.0;
+    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) acc += v[i];
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        acc = (threadIdx.x < (blockDim.x >> 5)) ? red[threadIdx.x] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+        if (threadIdx.x == 0) *out = acc;
+    }
+}
+
+cudaError_t launch_sum(lm_ctx* ctx, const double* v, int64_t n, double* out1) {
+    sum_kernel<<<1, 1024, 0, ctx->stream>>>(v, n, out1);
+    ctx->launches++;
+    return cudaGetLastError();
+}
+
+}  // namespace lmgpu

@@ -1,0 +1,25 @@
+"""lmgpu -- GB300 backend for the LatticeModels.jl time-evolution path.
+
+Host-side mirror of the reference's API for ``Evolution(t -> h(t), P_0)`` over
+``tightbinding_hamiltonian`` with Landau/point-flux fields, read out through ``localdensity``
+and ``DensityCurrents``.  All compute runs in liblmgpu.so (hand-written sm_103a CUDA); this
+package only holds the host-side bookkeeping and the ctypes bindings.
+"""
+from ._lib import LMError, load as load_library
+from .device import Context, default_context
+from .evolution import ChebyshevGPU, Evolution, EvolutionIterator, EvolutionSolver, EvolutionTimestamp
+from .fields import FieldSum, LandauGauge, NoField, PointFlux, PointFluxes, SymmetricGauge
+from .hamiltonian import Hamiltonian, tightbinding_hamiltonian
+from .lattice import LatticeValue, SquareLattice
+from .observables import Currents, DensityCurrents, localdensity
+from .spectrum import densitymatrix, diagonalize
+from .states import DensityMatrix, DeviceState, Ket, KetBlock, Operator
+
+__all__ = [
+    "LMError", "load_library", "Context", "default_context",
+    "ChebyshevGPU", "Evolution", "EvolutionIterator", "EvolutionSolver", "EvolutionTimestamp",
+    "FieldSum", "LandauGauge", "NoField", "PointFlux", "PointFluxes", "SymmetricGauge",
+    "Hamiltonian", "tightbinding_hamiltonian", "LatticeValue", "SquareLattice",
+    "Currents", "DensityCurrents", "localdensity", "densitymatrix", "diagonalize",
+    "DensityMatrix", "DeviceState", "Ket", "KetBlock", "Operator",
+]

@@ -1,0 +1,262 @@
+"""Parity of the CUDA path (through the C ABI) with the CPU oracle.
+
+Bars: bit-exact site/bond indexing and CSC structure; H values to 1e-15 (the device evaluates
+sin/cos/acos with CUDA's functions); FP64 evolution to <= 1e-10 relative Frobenius error
+against the exact exponent; particle number to 1e-12; the FP32 form to <= 1e-6 relative error
+against FP64 on densities and currents.
+"""
+import math
+
+import numpy as np
+import pytest
+import scipy.sparse as sp
+
+from oracle import lm_oracle as o
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def lm():
+    import lmgpu
+    lmgpu.default_context()  # fails loudly without a GPU or without the library
+    return lmgpu
+
+
+def rel(a, b):
+    a = np.asarray(a); b = np.asarray(b)
+    d = np.linalg.norm(b)
+    return np.linalg.norm(a - b) / (d if d > 0 else 1.0)
+
+
+def pair(lm, Lx, Ly, per=(False, False), tw=(0.0, 0.0)):
+    b = {}
+    for ax, name in enumerate(("axis1", "axis2")):
+        if per[ax]:
+            b[name] = float(tw[ax]) if tw[ax] else True
+    return o.SquareLattice(Lx, Ly, periodic=per, twist=tw), lm.SquareLattice(Lx, Ly, boundaries=b)
+
+
+def field_pair(lm, spec):
+    """spec: list of (kind, amp, point, gauge) -> (oracle field, lmgpu field)."""
+    of, lf = [], []
+    for kind, amp, pt, gauge in spec:
+        if kind == "landau":
+            of.append(o.LandauGauge(amp)); lf.append(lm.LandauGauge(amp))
+        elif kind == "sym":
+            of.append(o.SymmetricGauge(amp)); lf.append(lm.SymmetricGauge(amp))
+        else:
+            of.append(o.PointFlux(amp, pt, gauge)); lf.append(lm.PointFlux(amp, pt, gauge))
+    if not of:
+        return None, None
+    if len(of) == 1:
+        return of[0], lf[0]
+    return o.FieldSum(tuple(of)), lm.FieldSum(lf)
+
+
+def csc_of(lmH):
+    colptr, rowval, nz = lmH.csc()
+    N = len(colptr) - 1
+    return sp.csc_matrix((nz, rowval - 1, colptr - 1), shape=(N, N)), colptr, rowval
+
+
+ASSEMBLY_CASES = [
+    (10, 10, (False, False), (0, 0), [("pf", 0.2, (5.5, 5.5), "axial")], False),
+    (5, 5, (False, False), (0, 0), [("landau", 0.1, None, None)], False),
+    (16, 12, (True, True), (0, 0), [("landau", 0.01, None, None)], True),
+    (9, 7, (True, True), (0, 0), [("pf", 0.3, (4.5, 3.5), "axial")], False),
+    (9, 7, (True, False), (0, 0), [("pf", 0.3, (4.5, 3.5), "singular")], True),
+    (6, 8, (False, True), (0, 0.7), [("sym", 0.05, None, None)], True),
+    (7, 7, (False, False), (0, 0), [("landau", 0.05, None, None), ("pf", 0.4, (3.5, 4.5), "axial")], True),
+    (2, 5, (True, True), (0.3, 0), [("landau", 0.1, None, None)], True),
+    (1, 9, (False, False), (0, 0), [], True),
+    (8, 8, (False, False), (0, 0), [("pf", 0.25, (4.0, 4.0), "axial")], False),  # flux on a site
+]
+
+
+@pytest.mark.parametrize("Lx,Ly,per,tw,fspec,onsite", ASSEMBLY_CASES)
+def test_assembly_matches_oracle(lm, Lx, Ly, per, tw, fspec, onsite):
+    ol, ll = pair(lm, Lx, Ly, per, tw)
+    of, lf = field_pair(lm, fspec)
+    V = o.anderson_disorder(ol.N, 2.0, 11) if onsite else None
+    Ho = o.tightbinding_hamiltonian(ol, field=of, onsite=V)
+    import warnings
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        Hl = lm.tightbinding_hamiltonian(ll, *( [V] if V is not None else []), field=lf)
+    Hg, colptr, rowval = csc_of(Hl)
+    # structure bit-exact (same stored entries as the reference's CSC)
+    assert np.array_equal(colptr - 1, Ho.indptr)
+    assert np.array_equal(rowval - 1, Ho.indices)
+    assert np.abs(Hg.data - Ho.data).max() <= 1e-15 * max(1.0, np.abs(Ho.data).max())
+
+
+def test_nnz_doctests_on_device(lm):
+    H = lm.tightbinding_hamiltonian(lm.SquareLattice(4, 4))
+    assert csc_of(H)[0].nnz == 48
+    H = lm.tightbinding_hamiltonian(lm.SquareLattice(5, 5), field=lm.LandauGauge(0.1))
+    assert csc_of(H)[0].nnz == 80
+
+
+def _step_case(lm, Lx, Ly, per, fspec, M, dt, precision="c64", seed=3):
+    ol, ll = pair(lm, Lx, Ly, per)
+    of, lf = field_pair(lm, fspec)
+    V = o.anderson_disorder(ol.N, 2.0, seed)
+    Ho = o.tightbinding_hamiltonian(ol, field=of, onsite=V)
+    Hl = lm.tightbinding_hamiltonian(ll, V, field=lf)
+    X = o.random_kets(ol.N, M, seed + 1)
+    st = lm.KetBlock(ll, X, precision=precision)
+    solver = lm.ChebyshevGPU()
+    solver.update_solver(Hl, dt)
+    solver.step(st)
+    Y = st.to_numpy()
+    Yo = o.expm_multiply(Ho, dt, X)
+    return Y, Yo, solver, st
+
+
+@pytest.mark.parametrize("Lx,Ly,per,M", [(12, 10, (False, False), 5), (16, 16, (True, True), 8),
+                                         (33, 17, (True, False), 3), (7, 300, (False, True), 1)])
+def test_ket_step_fp64(lm, Lx, Ly, per, M):
+    Y, Yo, _, _ = _step_case(lm, Lx, Ly, per, [("landau", 0.01, None, None)], M, 0.05)
+    assert rel(Y, Yo) <= 1e-12
+
+
+def test_ket_step_pointflux_large_dt(lm):
+    Y, Yo, solver, st = _step_case(lm, 10, 10, (False, False), [("pf", 0.2, (5.5, 5.5), "axial")], 4, 1.7)
+    K, a, b = solver.order(st)
+    assert K > 10
+    assert rel(Y, Yo) <= 1e-11
+
+
+def test_backward_step_round_trip(lm):
+    ol, ll = pair(lm, 20, 20, (True, True))
+    V = o.anderson_disorder(ol.N, 2.0, 5)
+    Hl = lm.tightbinding_hamiltonian(ll, V, field=lm.LandauGauge(0.02))
+    X = o.random_kets(ol.N, 6, 9)
+    st = lm.KetBlock(ll, X)
+    s = lm.ChebyshevGPU()
+    for dt in (0.05, 0.05, 0.05):
+        s.update_solver(Hl, dt); s.step(st)
+    for dt in (-0.05, -0.05, -0.05):
+        s.update_solver(Hl, dt); s.step(st)
+    assert rel(st.to_numpy(), X) <= 1e-12
+
+
+def test_density_matrix_step_fp64(lm):
+    ol, ll = pair(lm, 10, 10)
+    Ho = o.tightbinding_hamiltonian(ol, field=o.PointFlux(0.13, (5.5, 5.5)))
+    Hl = lm.tightbinding_hamiltonian(ll, field=lm.PointFlux(0.13, (5.5, 5.5)))
+    P0, _, _ = o.densitymatrix(o.tightbinding_hamiltonian(ol), mu=0.0)
+    st = lm.DensityMatrix(ll, P0)
+    s = lm.ChebyshevGPU()
+    s.update_solver(Hl, 0.1)
+    s.step(st)
+    U = o.expm_exact(Ho, 0.1)
+    Pref = U @ P0 @ U.conj().T
+    assert rel(st.to_numpy(), Pref) <= 1e-12
+    assert abs(st.trace() - np.trace(P0).real) <= 1e-12 * max(1, abs(np.trace(P0)))
+
+
+def test_config1_full_evolution(lm):
+    """SquareLattice(10,10), open, PointFlux(B(t),(5.5,5.5)) with B ramped 0 -> 0.2 over
+    tau = 10, dt = 0.1 to t = 20 (200 steps), dense P_0 at mu = 0; localdensity and currents
+    every step against the oracle evolved with the exact exponent."""
+    ol, ll = pair(lm, 10, 10)
+    tau = 10.0
+    B = lambda t: 0.2 * min(t, tau) / tau
+    h_o = lambda t: o.tightbinding_hamiltonian(ol, field=o.PointFlux(B(t), (5.5, 5.5)))
+    h_l = lambda t: lm.tightbinding_hamiltonian(ll, field=lm.PointFlux(B(t), (5.5, 5.5)))
+    P0, _, _ = o.densitymatrix(h_o(0.0), mu=0.0)  # the shared P_0 (degenerate E = 0 fixed here)
+    times = [round(0.1 * k, 10) for k in range(201)]
+    src, dst = ll.bonds()
+    ev = lm.Evolution(h_l, lm.DensityMatrix(ll, P0))
+    orc = o.evolve(h_o, P0, times, o.OracleCachedExpSolver(exact=True))
+    tr0 = np.trace(P0).real
+    worst = {"P": 0.0, "rho": 0.0, "J": 0.0, "tr": 0.0}
+    for k, (mom, (Ho, Po, to)) in enumerate(zip(ev(times), orc)):
+        P, H, t = mom
+        assert t == pytest.approx(to, abs=1e-12)
+        if k % 20 == 0 or k == 200:
+            worst["P"] = max(worst["P"], rel(P.to_numpy(), Po))
+        rho = lm.localdensity(P).values
+        J = lm.DensityCurrents(H, P).bond_values()
+        worst["rho"] = max(worst["rho"], rel(rho, o.localdensity(Po)))
+        worst["J"] = max(worst["J"], rel(J, o.bond_currents(Ho, Po, src, dst, is_density=True)))
+        worst["tr"] = max(worst["tr"], abs(P.trace() - tr0))
+    assert worst["P"] <= 1e-10, worst
+    assert worst["rho"] <= 1e-10, worst
+    assert worst["J"] <= 1e-10, worst
+    assert worst["tr"] <= 1e-12 * tr0, worst
+
+
+def test_ket_block_readouts_match_projector(lm):
+    """Currents/densities of a weighted ket block equal those of P = sum w |psi><psi|."""
+    ol, ll = pair(lm, 9, 8, (True, False))
+    Hl = lm.tightbinding_hamiltonian(ll, field=lm.LandauGauge(0.07))
+    Ho = o.tightbinding_hamiltonian(ol, field=o.LandauGauge(0.07))
+    X = o.random_kets(ol.N, 7, 2)
+    w = np.linspace(0.2, 1.0, 7)
+    st = lm.KetBlock(ll, X, weights=w)
+    P = (X * w) @ X.conj().T
+    src, dst = ll.bonds()
+    assert rel(lm.localdensity(st).values, o.localdensity(P)) <= 1e-14
+    assert rel(lm.DensityCurrents(Hl, st).bond_values(), o.bond_currents(Ho, P, src, dst, is_density=True)) <= 1e-13
+    dm = lm.DensityMatrix(ll, P)
+    assert rel(lm.DensityCurrents(Hl, dm).bond_values(), lm.DensityCurrents(Hl, st).bond_values()) <= 1e-13
+    assert abs(st.trace() - np.trace(P).real) <= 1e-12
+
+
+def test_fp32_form_error_vs_fp64(lm):
+    """Chosen form: c32 recurrence with FP64 coefficients/reductions, against the FP64 run."""
+    ol, ll = pair(lm, 48, 48, (True, True))
+    V = o.anderson_disorder(ol.N, 2.0, 21)
+    Hl = lm.tightbinding_hamiltonian(ll, V, field=lm.LandauGauge(0.01))
+    X = o.random_kets(ol.N, 64, 4, kind="phase")
+    s64 = lm.KetBlock(ll, X, precision="c64")
+    s32 = lm.KetBlock(ll, X, precision="c32")
+    solver = lm.ChebyshevGPU(renorm_every=10)
+    ev64 = lm.Evolution(solver, Hl, s64)
+    ev32 = lm.Evolution(solver, Hl, s32)
+    times = [0.05 * k for k in range(101)]
+    for _ in ev64(times):
+        pass
+    for _ in ev32(times):
+        pass
+    a64 = ev64.current_states()[0]
+    a32 = ev32.current_states()[0]
+    r64, r32 = lm.localdensity(a64).values, lm.localdensity(a32).values
+    J64 = lm.DensityCurrents(Hl, a64).bond_values()
+    J32 = lm.DensityCurrents(Hl, a32).bond_values()
+    assert rel(r32, r64) <= 1e-6
+    assert rel(J32, J64) <= 1e-5  # currents are differences of nearby amplitudes
+    assert np.abs(a32.norms() - 1).max() <= 1e-6
+
+
+def test_edge_cases(lm):
+    # single ket on a 1 x N chain, t1 = 0 evolution is a pure phase
+    ol, ll = pair(lm, 1, 37)
+    V = o.anderson_disorder(37, 2.0, 1)
+    H0 = lm.Hamiltonian(ll, 0.0, None, V)
+    x = o.random_kets(37, 1, 1)[:, 0]
+    st = lm.Ket(ll, x)
+    s = lm.ChebyshevGPU()
+    s.update_solver(H0, 0.3)
+    s.step(st)
+    assert rel(st.to_numpy()[:, 0], np.exp(-0.3j * V) * x) <= 1e-12
+    # N not a multiple of the block size, M not a multiple of the ket tile
+    Y, Yo, _, _ = _step_case(lm, 13, 11, (False, True), [("landau", 0.03, None, None)], 7, 0.2)
+    assert rel(Y, Yo) <= 1e-12
+    # two-site periodic axis (both bonds join the same pair)
+    Y, Yo, _, _ = _step_case(lm, 2, 9, (True, True), [("landau", 0.1, None, None)], 3, 0.1)
+    assert rel(Y, Yo) <= 1e-12
+    # dt = 0 in the iterator yields the initial state untouched
+    ev = lm.Evolution(lambda t: H0, lm.Ket(ll, x))
+    m0 = next(iter(ev([0.0])))
+    assert np.array_equal(m0.state.to_numpy()[:, 0], x)
+    # errors are reported, not silently ignored
+    small = lm.KetBlock(lm.SquareLattice(3, 3), np.zeros((9, 2)))
+    s.update_solver(lm.tightbinding_hamiltonian(lm.SquareLattice(4, 4)), 0.1)
+    with pytest.raises(lm.LMError):
+        s.step(small)  # state and lattice sizes differ
+    with pytest.raises(ValueError):
+        small.renormalize(np.ones(1))
