@@ -86,7 +86,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "100"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self._t = threading.Thread(target=self._read, daemon=True)
             self._t.start()
@@ -199,7 +199,7 @@ def run_reference_arm(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="lmgpu", choices=["lmgpu", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -264,7 +264,6 @@ def main():
     clk = ClockSampler(local)
     clk.start()
     ms32, _, _, launches32 = timed_steps(s32, solver32, args.steps)
-    clocks = clk.stop()
     K32, a32, b32 = solver32.order(s32)
     # dominant kernel timing pass (events around every Chebyshev sweep, resolved lazily)
     _, order_ms, order_launches, _ = timed_steps(s32, solver32, args.steps, timing=True)
@@ -273,6 +272,8 @@ def main():
     s64 = lmgpu.KetBlock(lat, X, precision="c64")
     solver64 = lmgpu.ChebyshevGPU()
     ms64, _, _, _ = timed_steps(s64, solver64, args.steps)
+    clocks = clk.stop()
+    clocks["window"] = "sampled every 100 ms over the timed c32 and c64 passes"
     K64, _, _ = solver64.order(s64)
 
     # ---- error of the chosen form against FP64 after the same steps --------------------

@@ -169,20 +169,26 @@ def test_config1_full_evolution(lm):
     P0, _, _ = o.densitymatrix(h_o(0.0), mu=0.0)  # the shared P_0 (degenerate E = 0 fixed here)
     times = [round(0.1 * k, 10) for k in range(201)]
     src, dst = ll.bonds()
-    ev = lm.Evolution(h_l, lm.DensityMatrix(ll, P0))
+    # truncation 1e-14: the per-step series error stays below the 1e-12 particle-number bar
+    ev = lm.Evolution(lm.ChebyshevGPU(tol=1e-14), h_l, lm.DensityMatrix(ll, P0))
     orc = o.evolve(h_o, P0, times, o.OracleCachedExpSolver(exact=True))
     tr0 = np.trace(P0).real
     worst = {"P": 0.0, "rho": 0.0, "J": 0.0, "tr": 0.0}
+    Js, Jos = [], []
     for k, (mom, (Ho, Po, to)) in enumerate(zip(ev(times), orc)):
         P, H, t = mom
         assert t == pytest.approx(to, abs=1e-12)
         if k % 20 == 0 or k == 200:
             worst["P"] = max(worst["P"], rel(P.to_numpy(), Po))
         rho = lm.localdensity(P).values
-        J = lm.DensityCurrents(H, P).bond_values()
+        Js.append(lm.DensityCurrents(H, P).bond_values())
+        Jos.append(o.bond_currents(Ho, Po, src, dst, is_density=True))
         worst["rho"] = max(worst["rho"], rel(rho, o.localdensity(Po)))
-        worst["J"] = max(worst["J"], rel(J, o.bond_currents(Ho, Po, src, dst, is_density=True)))
         worst["tr"] = max(worst["tr"], abs(P.trace() - tr0))
+    # the currents vanish exactly while B(t) = 0, so their relative Frobenius error is taken
+    # over the whole (moments x bonds) series
+    worst["J"] = rel(np.array(Js), np.array(Jos))
+    print("config1 worst errors:", worst)
     assert worst["P"] <= 1e-10, worst
     assert worst["rho"] <= 1e-10, worst
     assert worst["J"] <= 1e-10, worst
