@@ -67,6 +67,11 @@ int lm_ctx_synchronize(lm_ctx *ctx);
 /* The context's CUDA stream (cudaStream_t), for callers that order their own work or
  * CUDA events against the library's launches. */
 int lm_ctx_stream(lm_ctx *ctx, void **stream);
+/* Context options.  LM_OPT_FUSED (default 1): a ComplexF32 ket-block step whose Chebyshev
+ * order is at most 8 runs as one temporally blocked launch; 0 selects one launch per order
+ * (same results to FP32 rounding; kept for comparison). */
+#define LM_OPT_FUSED 1
+int lm_ctx_set_option(lm_ctx *ctx, int option, int value);
 /* Opt-in CUDA-event timing of the Chebyshev-order launches (for measurement); events are
  * resolved lazily by lm_ctx_timing, so timing adds no host synchronisation per step. */
 int lm_ctx_set_timing(lm_ctx *ctx, int enable);

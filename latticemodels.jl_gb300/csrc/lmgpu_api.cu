@@ -222,6 +222,17 @@ static int timing_pair(lm_ctx* ctx, cudaEvent_t* e0, cudaEvent_t* e1) {
     return LM_OK;
 }
 
+int lm_ctx_set_option(lm_ctx* ctx, int option, int value) {
+    if (!ctx) return LM_ERR_ARG;
+    switch (option) {
+        case LM_OPT_FUSED:
+            ctx->fused = value ? 1 : 0;
+            return LM_OK;
+        default:
+            return set_err(ctx, LM_ERR_ARG, "lm_ctx_set_option: unknown option");
+    }
+}
+
 int lm_ctx_set_timing(lm_ctx* ctx, int enable) {
     if (!ctx) return LM_ERR_ARG;
     ctx->timing = enable ? 1 : 0;
@@ -786,6 +797,19 @@ static int cheb_apply(lm_solver* s, const Geom& g, int precision, int site_fast,
         int rc = timing_pair(ctx, &t0, &t1);
         if (rc != LM_OK) return rc;
         CUDA_TRY(ctx, cudaEventRecord(t0, ctx->stream), "cudaEventRecord");
+    }
+    if (ctx->fused && site_fast && !conj && fused_supported(precision, K)) {
+        // whole series in one temporally blocked pass; result lands in A
+        CUDA_TRY(ctx, launch_cheb_fused_c32(ctx, g, (const float2*)hop2, (const float*)diag2, (const float2*)S,
+                                            (float2*)A, ld, m, K, s->coef.data(), pr, pi),
+                 "fused chebyshev step");
+        if (ctx->timing) {
+            CUDA_TRY(ctx, cudaEventRecord(t1, ctx->stream), "cudaEventRecord");
+            ctx->ev_launches[ctx->ev_used] = K;
+            ctx->ev_used++;
+        }
+        *where = 1;
+        return LM_OK;
     }
     CUDA_TRY(ctx, launch_cheb_order(ctx, g, precision, site_fast, conj, CHEB_FIRST, hop2, diag2, S, A, Y, ld, m, c0, coef(1), pr, pi),
              "chebyshev order 1");

@@ -37,6 +37,9 @@ struct FieldSet {
     double amp[kMaxFields];
 };
 
+// Largest Chebyshev order the temporally blocked kernel handles in one pass (its halo).
+constexpr int kFusedMaxK = 8;
+
 // Per-order launch description of the Chebyshev recurrence.
 enum ChebMode { CHEB_FIRST = 0, CHEB_MID = 1, CHEB_LAST = 2 };
 
@@ -60,6 +63,7 @@ struct lm_ctx {
     int sm_count = 0;
     std::string err;
     int timing = 0;
+    int fused = 1;                      // LM_OPT_FUSED: temporally blocked c32 step enabled
     std::vector<cudaEvent_t> ev_pool;   // pairs (start, stop) of timed Chebyshev sweeps
     std::vector<int> ev_launches;       // launches covered by each recorded pair
     size_t ev_used = 0;                 // pairs recorded but not yet resolved
@@ -147,6 +151,10 @@ cudaError_t launch_column_norms(lm_ctx* ctx, int precision, const void* x, int64
 cudaError_t launch_rescale_columns(lm_ctx* ctx, int precision, void* x, int64_t n, int64_t m,
                                    int64_t ld, const double* norms, const double* target);
 cudaError_t launch_sum(lm_ctx* ctx, const double* v, int64_t n, double* out1);
+int fused_supported(int precision, int K);
+cudaError_t launch_cheb_fused_c32(lm_ctx* ctx, const Geom& g, const float2* hop2, const float* diag2,
+                                  const float2* x, float2* out, int64_t ld, int64_t m, int K,
+                                  const ChebCoef* coef, double ph_re, double ph_im);
 cudaError_t launch_convert(lm_ctx* ctx, int to_precision, const void* src, void* dst, int64_t n,
                            int64_t m, int64_t ld_src, int64_t ld_dst);
 

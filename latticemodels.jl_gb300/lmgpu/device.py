@@ -26,6 +26,10 @@ class Context:
     def synchronize(self):
         self.check(self.lib.lm_ctx_synchronize(self.handle))
 
+    def set_fused(self, on: bool):
+        """Temporally blocked c32 step (default on) or one launch per Chebyshev order."""
+        self.check(self.lib.lm_ctx_set_option(self.handle, _lib.LM_OPT_FUSED, 1 if on else 0))
+
     def set_timing(self, on: bool):
         self.check(self.lib.lm_ctx_set_timing(self.handle, 1 if on else 0))
 

@@ -266,3 +266,41 @@ def test_edge_cases(lm):
         s.step(small)  # state and lattice sizes differ
     with pytest.raises(ValueError):
         small.renormalize(np.ones(1))
+
+
+FUSED_CASES = [
+    (256, 256, (True, True), [("landau", 0.01, None, None)], 11, 0.05),
+    (10, 10, (False, False), [("pf", 0.2, (5.5, 5.5), "axial")], 9, 0.1),
+    (1, 37, (False, False), [], 3, 0.05),
+    (2, 9, (True, True), [("landau", 0.1, None, None)], 8, 0.05),
+    (70, 45, (False, True), [("pf", 0.3, (35.5, 20.5), "singular")], 17, 0.08),
+    (23, 130, (True, False), [("sym", 0.02, None, None)], 5, 0.12),
+    (40, 40, (True, True), [("landau", 0.03, None, None)], 4, 0.4),   # K > 8: per-order path
+]
+
+
+@pytest.mark.parametrize("Lx,Ly,per,fspec,M,dt", FUSED_CASES)
+def test_fused_c32_step(lm, Lx, Ly, per, fspec, M, dt):
+    """The temporally blocked c32 step agrees with the per-order c32 path and with FP64."""
+    ol, ll = pair(lm, Lx, Ly, per)
+    of, lf = field_pair(lm, fspec)
+    V = o.anderson_disorder(ol.N, 2.0, 13)
+    Ho = o.tightbinding_hamiltonian(ol, field=of, onsite=V)
+    Hl = lm.tightbinding_hamiltonian(ll, V, field=lf)
+    X = o.random_kets(ol.N, M, 17)
+    ctx = lm.default_context()
+    outs = {}
+    try:
+        for fused in (True, False):
+            ctx.set_fused(fused)
+            st = lm.KetBlock(ll, X, precision="c32")
+            s = lm.ChebyshevGPU()
+            s.update_solver(Hl, dt)
+            s.step(st)
+            outs[fused] = st.to_numpy().astype(np.complex128)
+    finally:
+        ctx.set_fused(True)
+    Yo = o.expm_multiply(Ho, dt, X)
+    assert rel(outs[True], Yo) <= 2e-6
+    assert rel(outs[False], Yo) <= 2e-6
+    assert rel(outs[True], outs[False]) <= 2e-6
