@@ -137,7 +137,7 @@ def measured_peak_hbm():
 
 def profile_traffic():
     """DRAM bytes per launch of the dominant kernel from the committed ncu summary, if any."""
-    f = ROOT / "profiles" / "cheb_order_c32_256x256.md"
+    f = ROOT / "profiles" / "cheb_fused_c32_256x256.md"
     if not f.exists():
         return None
     for ln in f.read_text().splitlines():
@@ -335,9 +335,12 @@ def main():
         return 0
     value = world * M * args.steps / (ms32 / 1000.0)
     plain = world * M * args.steps / (ms64 / 1000.0)
+    # one launch of the temporally blocked kernel applies all K32 orders of a step; its
+    # algorithmic bytes are the per-ket-step figure 5*K*N*s times the M kets it advances
     s_bytes = 8
-    alg_bytes_launch = 5.0 * N * M * s_bytes
-    avg_launch_ms = order_ms / max(order_launches, 1)
+    sweeps = max(order_launches // max(K32, 1), 1)
+    alg_bytes_launch = 5.0 * K32 * N * M * s_bytes
+    avg_launch_ms = order_ms / sweeps
     achieved = alg_bytes_launch / (avg_launch_ms / 1000.0) / 1e9
     peak, peak_kind = measured_peak_hbm()
     traffic = profile_traffic()
@@ -358,9 +361,9 @@ def main():
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic,
                      "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
-                     "kernel": "cheb_order_kernel<float> (one Chebyshev order)",
+                     "kernel": "cheb_fused_c32_kernel (all K orders of one step per launch)",
                      "alg_bytes_per_launch": alg_bytes_launch, "avg_launch_ms": avg_launch_ms,
-                     "launches_timed": order_launches},
+                     "launches_timed": sweeps},
         "e2e": {"value": world * M * args.steps / (ms_e2e / 1000.0), "unit": "ket-steps/s",
                 "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                 "ms_per_step": ms_e2e / args.steps},

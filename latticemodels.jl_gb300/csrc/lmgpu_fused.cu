@@ -32,7 +32,8 @@ struct FusedCoef {
     float s[kFusedMaxK + 1];
     int odd[kFusedMaxK + 1];
     int K;
-    float ph_re, ph_im;
+    float ph_re, ph_im;   // e^{-ib dt}
+    float a0_re, a0_im;   // e^{-ib dt} c_0
 };
 
 __device__ __forceinline__ float2 ld_site(const float2* __restrict__ p, int64_t site) {
@@ -104,12 +105,15 @@ cheb_fused_c32_kernel(Geom g, const float2* __restrict__ hop2, const float* __re
         for (int j = 0; j < S; ++j) nxt[j] = site[j] >= 0 ? __ldg(x + k_begin * ld + site[j]) : make_float2(0.f, 0.f);
 
         for (int64_t ket = k_begin; ket < k_end; ++ket) {
-            float2 t1[S], t0[S], yv[S];
+            // yv accumulates the small part sum_{k>=1} c_k T_k; the dominant c_0 T_0 term is
+            // added once at the end with a single rounding (x0 keeps T_0).
+            float2 t1[S], t0[S], yv[S], x0[S];
 #pragma unroll
             for (int j = 0; j < S; ++j) {
                 t1[j] = nxt[j];
+                x0[j] = nxt[j];
                 t0[j] = make_float2(0.f, 0.f);
-                yv[j] = make_float2(cf.s[0] * t1[j].x, cf.s[0] * t1[j].y);
+                yv[j] = make_float2(0.f, 0.f);
             }
             if (ket + 1 < k_end) {  // prefetch the next ket of this item
 #pragma unroll
@@ -182,9 +186,15 @@ cheb_fused_c32_kernel(Geom g, const float2* __restrict__ hop2, const float* __re
 #pragma unroll
             for (int j = 0; j < S; ++j) {
                 if (interior[j]) {
+                    // out = e^{-ib dt} (c_0 x + y): the small terms first, the large one last
+                    float2 r;
+                    r.x = fmaf(cf.ph_re, yv[j].x, -cf.ph_im * yv[j].y);
+                    r.y = fmaf(cf.ph_re, yv[j].y, cf.ph_im * yv[j].x);
+                    r.x = fmaf(-cf.a0_im, x0[j].y, r.x);
+                    r.y = fmaf(cf.a0_im, x0[j].x, r.y);
                     float2 o;
-                    o.x = fmaf(cf.ph_re, yv[j].x, -cf.ph_im * yv[j].y);
-                    o.y = fmaf(cf.ph_re, yv[j].y, cf.ph_im * yv[j].x);
+                    o.x = fmaf(cf.a0_re, x0[j].x, r.x);
+                    o.y = fmaf(cf.a0_re, x0[j].y, r.y);
                     out[ket * ld + site[j]] = o;
                 }
             }
@@ -205,6 +215,8 @@ cudaError_t launch_cheb_fused_c32(lm_ctx* ctx, const Geom& g, const float2* hop2
     }
     cf.ph_re = (float)ph_re;
     cf.ph_im = (float)ph_im;
+    cf.a0_re = (float)(ph_re * coef[0].s);
+    cf.a0_im = (float)(ph_im * coef[0].s);
     const int H = K;
     const int IX = RX - 2 * H, IY = RY - 2 * H;
     const int ntx = (int)((g.Lx + IX - 1) / IX), nty = (int)((g.Ly + IY - 1) / IY);

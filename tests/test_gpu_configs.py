@@ -1,0 +1,83 @@
+"""GPU runs at the sizes of the reference workload's configurations (parity by properties
+and by comparison of the chosen FP32 form with the FP64 plain form on the same seed)."""
+import math
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def lm():
+    import lmgpu
+    lmgpu.default_context()
+    return lmgpu
+
+
+def rel(a, b):
+    return float(np.linalg.norm(np.asarray(a) - np.asarray(b)) / np.linalg.norm(np.asarray(b)))
+
+
+def phase_kets(N, M, seed, dtype):
+    """Random-phase kets e^{i theta}/sqrt(N) (seeded PCG64), generated in column chunks."""
+    rng = np.random.default_rng(seed)
+    X = np.empty((N, M), dtype=dtype, order="F")
+    for c0 in range(0, M, 64):
+        c1 = min(M, c0 + 64)
+        th = rng.uniform(0, 2 * math.pi, size=(c1 - c0, N))
+        X[:, c0:c1] = (np.exp(1j * th) / math.sqrt(N)).T
+    return X
+
+
+def test_precision_config_512(lm):
+    """SquareLattice(512,512) periodic, Landau 0.01, Anderson U[-1,1], M = 1024 random-phase
+    kets, dt = 0.05, 200 steps: FP32 form against the FP64 run of the same seed."""
+    L, M, steps, dt = 512, 1024, 200, 0.05
+    lat = lm.SquareLattice(L, L, boundaries={"axis1": True, "axis2": True})
+    V = np.random.default_rng(7).uniform(-1, 1, size=lat.N)
+    H = lm.tightbinding_hamiltonian(lat, V, field=lm.LandauGauge(0.01))
+    X = phase_kets(lat.N, M, 11, np.complex64)
+    s32 = lm.KetBlock(lat, X, precision="c32")
+    s64 = lm.KetBlock(lat, X.astype(np.complex128), precision="c64")
+    del X
+    solver = lm.ChebyshevGPU(renorm_every=20)
+    for st in (s32, s64):
+        cache = solver.evolution_cache(st)
+        solver.update_solver(H, dt)
+        for _ in range(steps):
+            solver.step(st, cache)
+    r32, r64 = lm.localdensity(s32).values, lm.localdensity(s64).values
+    J32 = lm.DensityCurrents(H, s32).bond_values()
+    J64 = lm.DensityCurrents(H, s64).bond_values()
+    n32 = s32.norms()
+    err = {"density": rel(r32, r64), "currents": rel(J32, J64), "norm_drift": float(np.abs(n32 - 1).max()),
+           "trace_drift": abs(s32.trace() - s64.trace()) / s64.trace()}
+    print("precision config (512^2, M=1024, 200 steps):", err)
+    assert err["density"] <= 1e-6, err
+    assert err["norm_drift"] <= 1e-6, err
+    assert err["trace_drift"] <= 1e-6, err
+    assert err["currents"] <= 1e-5, err
+    # FP64 run: norms conserved to 1e-12
+    assert np.abs(s64.norms() - 1).max() <= 1e-12
+
+
+def test_plain_config_256_properties(lm):
+    """SquareLattice(256,256) periodic, Landau 0.01, disorder, M = 64 Gaussian kets, 400 steps in
+    FP64: norms conserved to 1e-12, and evolving forward then backward returns the input."""
+    lat = lm.SquareLattice(256, 256, boundaries={"axis1": True, "axis2": True})
+    V = np.random.default_rng(3).uniform(-1, 1, size=lat.N)
+    H = lm.tightbinding_hamiltonian(lat, V, field=lm.LandauGauge(0.01))
+    rng = np.random.default_rng(5)
+    X = rng.standard_normal((lat.N, 64)) + 1j * rng.standard_normal((lat.N, 64))
+    X /= np.linalg.norm(X, axis=0)
+    st = lm.KetBlock(lat, X)
+    s = lm.ChebyshevGPU()
+    s.update_solver(H, 0.05)
+    for _ in range(400):
+        s.step(st)
+    assert np.abs(st.norms() - 1).max() <= 1e-12
+    s.update_solver(H, -0.05)
+    for _ in range(400):
+        s.step(st)
+    assert rel(st.to_numpy(), X) <= 1e-10
