@@ -798,7 +798,7 @@ static int cheb_apply(lm_solver* s, const Geom& g, int precision, int site_fast,
         if (rc != LM_OK) return rc;
         CUDA_TRY(ctx, cudaEventRecord(t0, ctx->stream), "cudaEventRecord");
     }
-    if (ctx->fused && site_fast && !conj && fused_supported(precision, K)) {
+    if (ctx->fused && site_fast && !conj && fused_supported(precision, K) && fused_supported_geom(g)) {
         // whole series in one temporally blocked pass; result lands in A
         CUDA_TRY(ctx, launch_cheb_fused_c32(ctx, g, (const float2*)hop2, (const float*)diag2, (const float2*)S,
                                             (float2*)A, ld, m, K, s->coef.data(), pr, pi),

@@ -5,14 +5,19 @@
 // and the result written once, instead of five vector passes per Chebyshev order.
 //
 // Tiling: a CTA of 512 threads owns a region of 32 (x) x 64 (y) sites; thread (tx, ty)
-// holds the four consecutive y-sites 4ty..4ty+3 of row tx in registers (T_{k-1}, T_{k-2},
-// the accumulator y and its stencil coefficients).  Per order, the rows are exchanged
-// through a double-buffered shared-memory copy of T_{k-1} (x neighbours) and warp shuffles
-// (y neighbours: a warp holds two complete rows).  The valid part of the region shrinks by
-// one site per order, so after K orders the inner (32-2K) x (64-2K) sites are exact and are
-// written out.  Positions outside the lattice (open axes) hold zeros and zero coefficients;
-// periodic axes wrap the halo.  Work items are (tile, 8 kets); persistent CTAs stride over
-// them with consecutive items on neighbouring tiles of the same kets, so halo re-reads hit L2.
+// holds the four consecutive y-sites 4ty..4ty+3 of row tx for KB kets at a time in
+// registers (T_{k-1}, the accumulator and the stencil coefficients, which the KB
+// kets share).  Per order, rows are exchanged through a double-buffered shared-memory copy
+// of T_{k-1} (x neighbours) and warp shuffles (y neighbours: a warp holds two whole rows).
+// The valid part of the region shrinks by one site per order, so after K orders the inner
+// (32-2K) x (64-2K) sites are exact and are written out.  Positions outside the lattice (open
+// axes) hold zeros and zero coefficients; periodic axes wrap the halo.
+//
+// Pipelining: the next KB kets (of this tile, or the first ones of the CTA's next tile) are
+// copied global -> shared with cp.async while the current ones are computed; order 1 reads
+// its neighbours straight from that staging buffer.  Work items are (tile, 16 kets);
+// persistent CTAs stride over them with consecutive items on neighbouring tiles of the same
+// kets, so halo re-reads hit L2.
 #include <cuda_runtime.h>
 
 #include "lmgpu_internal.cuh"
@@ -20,12 +25,16 @@
 namespace lmgpu {
 
 namespace {
-constexpr int RX = 32;        // region extent along x (threads along x)
-constexpr int TY = 16;        // threads along y
-constexpr int S = 4;          // sites per thread along y
-constexpr int RY = TY * S;    // region extent along y
-constexpr int NTHR = RX * TY; // 512
-constexpr int KETS_PER_ITEM = 8;
+constexpr int RX = 32;         // region extent along x (threads along x)
+constexpr int TY = 16;         // threads along y
+constexpr int S = 4;           // sites per thread along y
+constexpr int RY = TY * S;     // region extent along y
+constexpr int NTHR = RX * TY;  // 512
+constexpr int KB = 1;          // kets a thread advances together
+constexpr int KETS_PER_ITEM = 16;
+// one buffer = KB kets x RX rows x 2 halves x TY float4 (a float4 = two sites of one thread)
+constexpr int BUF_F4 = KB * RX * 2 * TY;
+constexpr int SMEM_BYTES = 4 * BUF_F4 * 16;  // T double buffer + staging double buffer = 128 KB
 }  // namespace
 
 struct FusedCoef {
@@ -36,11 +45,9 @@ struct FusedCoef {
     float a0_re, a0_im;   // e^{-ib dt} c_0
 };
 
-__device__ __forceinline__ float2 ld_site(const float2* __restrict__ p, int64_t site) {
-    return site >= 0 ? __ldg(p + site) : make_float2(0.f, 0.f);
-}
+__device__ __forceinline__ int fidx(int kk, int row, int h, int ty) { return ((kk * RX + row) * 2 + h) * TY + ty; }
 
-// Region coordinate -> lattice site (0-based) or -1 outside an open axis.
+// Region coordinate -> lattice coordinate (0-based) or -1 outside an open axis.
 __device__ __forceinline__ int64_t wrap_axis(int64_t c, int64_t L, int per) {
     if (c >= 0 && c < L) return c;
     if (!per) return -1;
@@ -48,161 +55,236 @@ __device__ __forceinline__ int64_t wrap_axis(int64_t c, int64_t L, int per) {
     return c < 0 ? c + L : c;
 }
 
+struct TileMap {
+    int site[S];  // lattice site of each of my four positions, -1 outside (N < 2^31)
+    int gx;       // unwrapped lattice x of my row
+    int gy0;      // unwrapped lattice y of my first position
+};
+
+__device__ __forceinline__ TileMap tile_map(const Geom& g, int64_t tile, int nty, int H, int tx, int ty) {
+    TileMap m;
+    const int IX = RX - 2 * H, IY = RY - 2 * H;
+    const int64_t tile_x = tile / nty, tile_y = tile % nty;
+    m.gx = (int)(tile_x * IX - H + tx);
+    m.gy0 = (int)(tile_y * IY - H + ty * S);
+    const int64_t xs = wrap_axis(m.gx, g.Lx, g.per_x);
+#pragma unroll
+    for (int j = 0; j < S; ++j) {
+        const int64_t ys = wrap_axis(m.gy0 + j, g.Ly, g.per_y);
+        m.site[j] = (xs >= 0 && ys >= 0) ? (int)(xs * g.Ly + ys) : -1;
+    }
+    return m;
+}
+
+__device__ __forceinline__ void cp_async8(float4* smem_f4, int half, const float2* src, bool valid) {
+    const unsigned dst = (unsigned)__cvta_generic_to_shared(smem_f4) + (unsigned)half * 8u;
+    const int n = valid ? 8 : 0;  // n = 0 fills the 8 bytes with zeros
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(dst), "l"(src), "r"(n));
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+
+// Stages kets k0, k0+1 (those below k_end) of my four positions into `stage`.
+__device__ __forceinline__ void prefetch_pair(float4* stage, const TileMap& m, const float2* __restrict__ x,
+                                              int64_t ld, int64_t k0, int64_t k_end, int tx, int ty) {
+#pragma unroll
+    for (int kk = 0; kk < KB; ++kk) {
+        const int64_t ket = k0 + kk;
+#pragma unroll
+        for (int j = 0; j < S; ++j) {
+            const bool ok = ket < k_end && m.site[j] >= 0;
+            const float2* src = ok ? x + ket * ld + m.site[j] : x;
+            cp_async8(&stage[fidx(kk, tx, j >> 1, ty)], j & 1, src, ok);
+        }
+    }
+    cp_async_commit();
+}
+
+__device__ __forceinline__ void unpack4(const float4 a, const float4 b, float2 v[S]) {
+    v[0] = make_float2(a.x, a.y);
+    v[1] = make_float2(a.z, a.w);
+    v[2] = make_float2(b.x, b.y);
+    v[3] = make_float2(b.z, b.w);
+}
+
+template <int K>
 __global__ void __launch_bounds__(NTHR, 1)
 cheb_fused_c32_kernel(Geom g, const float2* __restrict__ hop2, const float* __restrict__ diag2,
                       const float2* __restrict__ x, float2* __restrict__ out, int64_t ld, int64_t M,
-                      int H, int ntx, int nty, int64_t nitems, FusedCoef cf) {
-    __shared__ float4 buf[2][RX][RY / 2];  // T_{k-1} double buffer, 2 x 16 KB
+                      int ntx, int nty, int64_t nitems, FusedCoef cf) {
+    constexpr int H = K;  // halo = number of orders
+    extern __shared__ float4 smem[];
+    // buffer offsets (in float4) into smem: T double buffer, then the staging double buffer
+    auto tb = [](int i) { return i * BUF_F4; };
+    auto sbuf = [](int i) { return (2 + i) * BUF_F4; };
 
     const int t = threadIdx.x;
     const int tx = t / TY;
     const int ty = t % TY;
-    const int lane = t & 31;
     const int warp_row0 = (t >> 5) * 2;  // the two rows a warp holds
-    const int IX = RX - 2 * H, IY = RY - 2 * H;
     const int64_t ntiles = (int64_t)ntx * nty;
-    const int64_t kchunks = (M + KETS_PER_ITEM - 1) / KETS_PER_ITEM;
 
-    for (int64_t item = blockIdx.x; item < nitems; item += gridDim.x) {
-        const int64_t tile = item % ntiles;
-        const int64_t kc = item / ntiles;
-        if (kc >= kchunks) break;
-        const int64_t tile_x = tile / nty, tile_y = tile % nty;
-        const int64_t gx = tile_x * IX - H + tx;  // lattice x of my row (unwrapped)
-        const int64_t xs = wrap_axis(gx, g.Lx, g.per_x);
-        const int64_t xsm = wrap_axis(gx - 1, g.Lx, g.per_x);
+    int64_t item = blockIdx.x;
+    if (item >= nitems) return;
+    TileMap m = tile_map(g, item % ntiles, nty, H, tx, ty);
+    int64_t k_begin = (item / ntiles) * KETS_PER_ITEM;
+    int64_t k_end = min(M, k_begin + KETS_PER_ITEM);
+    prefetch_pair(smem + sbuf(0), m, x, ld, k_begin, k_end, tx, ty);
+    int sb = 0;
 
-        int64_t site[S];
+    while (true) {
+        // stencil coefficients of my positions (shared by every ket of the item)
         float2 hx[S], hxm[S], hy[S];
         float d[S];
         float2 hym0 = make_float2(0.f, 0.f);
-        bool interior[S];
-#pragma unroll
-        for (int j = 0; j < S; ++j) {
-            const int ry = ty * S + j;
-            const int64_t gy = tile_y * IY - H + ry;
-            const int64_t ys = wrap_axis(gy, g.Ly, g.per_y);
-            site[j] = (xs >= 0 && ys >= 0) ? xs * g.Ly + ys : -1;
-            hx[j] = ld_site(hop2, site[j]);
-            hy[j] = site[j] >= 0 ? __ldg(hop2 + g.N + site[j]) : make_float2(0.f, 0.f);
-            d[j] = site[j] >= 0 ? __ldg(diag2 + site[j]) : 0.f;
-            const int64_t sm = (xsm >= 0 && ys >= 0) ? xsm * g.Ly + ys : -1;  // site at x-1
-            const float2 h = ld_site(hop2, sm);
-            hxm[j] = make_float2(h.x, -h.y);
-            interior[j] = tx >= H && tx < RX - H && ry >= H && ry < RY - H && gx < g.Lx && gy < g.Ly;
-            if (j == 0) {
-                const int64_t ysm = wrap_axis(gy - 1, g.Ly, g.per_y);
-                const int64_t s2 = (xs >= 0 && ysm >= 0) ? xs * g.Ly + ysm : -1;  // site at y-1
-                const float2 hh = s2 >= 0 ? __ldg(hop2 + g.N + s2) : make_float2(0.f, 0.f);
-                hym0 = make_float2(hh.x, -hh.y);
-            }
-        }
-
-        const int64_t k_begin = kc * KETS_PER_ITEM;
-        const int64_t k_end = min(M, k_begin + KETS_PER_ITEM);
-        float2 nxt[S];
-#pragma unroll
-        for (int j = 0; j < S; ++j) nxt[j] = site[j] >= 0 ? __ldg(x + k_begin * ld + site[j]) : make_float2(0.f, 0.f);
-
-        for (int64_t ket = k_begin; ket < k_end; ++ket) {
-            // yv accumulates the small part sum_{k>=1} c_k T_k; the dominant c_0 T_0 term is
-            // added once at the end with a single rounding (x0 keeps T_0).
-            float2 t1[S], t0[S], yv[S], x0[S];
+        unsigned interior = 0;  // bit j: position j is written out
+        {
+            const int64_t xsm = wrap_axis(m.gx - 1, g.Lx, g.per_x);
+            const int64_t xs = wrap_axis(m.gx, g.Lx, g.per_x);
 #pragma unroll
             for (int j = 0; j < S; ++j) {
-                t1[j] = nxt[j];
-                x0[j] = nxt[j];
-                t0[j] = make_float2(0.f, 0.f);
-                yv[j] = make_float2(0.f, 0.f);
+                const int s = m.site[j];
+                const int64_t ys = wrap_axis(m.gy0 + j, g.Ly, g.per_y);
+                hx[j] = s >= 0 ? __ldg(hop2 + s) : make_float2(0.f, 0.f);
+                hy[j] = s >= 0 ? __ldg(hop2 + g.N + s) : make_float2(0.f, 0.f);
+                d[j] = s >= 0 ? __ldg(diag2 + s) : 0.f;
+                const int64_t sm = (xsm >= 0 && ys >= 0) ? xsm * g.Ly + ys : -1;  // site at x-1
+                const float2 h = sm >= 0 ? __ldg(hop2 + sm) : make_float2(0.f, 0.f);
+                hxm[j] = make_float2(h.x, -h.y);
+                const int ry = ty * S + j;
+                if (tx >= H && tx < RX - H && ry >= H && ry < RY - H && m.gx < g.Lx && m.gy0 + j < g.Ly && s >= 0)
+                    interior |= 1u << j;
             }
-            if (ket + 1 < k_end) {  // prefetch the next ket of this item
-#pragma unroll
-                for (int j = 0; j < S; ++j)
-                    nxt[j] = site[j] >= 0 ? __ldg(x + (ket + 1) * ld + site[j]) : make_float2(0.f, 0.f);
-            }
-            buf[0][tx][ty * 2] = make_float4(t1[0].x, t1[0].y, t1[1].x, t1[1].y);
-            buf[0][tx][ty * 2 + 1] = make_float4(t1[2].x, t1[2].y, t1[3].x, t1[3].y);
-            __syncthreads();
+            const int64_t ysm = wrap_axis(m.gy0 - 1, g.Ly, g.per_y);
+            const int64_t s2 = (xs >= 0 && ysm >= 0) ? xs * g.Ly + ysm : -1;  // site at y-1
+            const float2 hh = s2 >= 0 ? __ldg(hop2 + g.N + s2) : make_float2(0.f, 0.f);
+            hym0 = make_float2(hh.x, -hh.y);
+        }
+        const int64_t cur_k_end = k_end;
+        const TileMap cur = m;
+        bool have_next_item = false;
 
-            for (int k = 1; k <= cf.K; ++k) {
-                const int cur = (k - 1) & 1;
+        for (int64_t k0 = k_begin; k0 < cur_k_end; k0 += KB) {
+            cp_async_wait_all();
+            __syncthreads();  // staged pair visible; the previous pair is done with every buffer
+            // stage the pair after this one: same item, or the first pair of my next item
+            if (k0 + KB < cur_k_end) {
+                prefetch_pair(smem + sbuf(sb ^ 1), cur, x, ld, k0 + KB, cur_k_end, tx, ty);
+            } else if (item + gridDim.x < nitems) {
+                item += gridDim.x;
+                m = tile_map(g, item % ntiles, nty, H, tx, ty);
+                k_begin = (item / ntiles) * KETS_PER_ITEM;
+                k_end = min(M, k_begin + KETS_PER_ITEM);
+                prefetch_pair(smem + sbuf(sb ^ 1), m, x, ld, k_begin, k_end, tx, ty);
+                have_next_item = true;
+            }
+            const int stage = sbuf(sb);
+
+            // T_{k-1} of my positions lives in registers; T_{k-2} is read back from the buffer
+            // that T_k overwrites (my own positions only), T_0 from the staging buffer.
+            float2 t1[KB][S], yv[KB][S];
+#pragma unroll
+            for (int kk = 0; kk < KB; ++kk) {
+                unpack4(smem[stage + fidx(kk, tx, 0, ty)], smem[stage + fidx(kk, tx, 1, ty)], t1[kk]);
+#pragma unroll
+                for (int j = 0; j < S; ++j) yv[kk][j] = make_float2(0.f, 0.f);
+            }
+
+#pragma unroll
+            for (int k = 1; k <= K; ++k) {
+                const int src = (k == 1) ? stage : tb((k - 1) & 1);
+                const int dst = tb(k & 1);
+                const int prev2 = (k == 2) ? stage : dst;  // T_{k-2} of my positions
                 // warps whose two rows both lie outside the valid region skip the order
                 const bool active = (warp_row0 + 1 >= k) && (warp_row0 < RX - k);
                 if (active) {
                     const int xp = min(tx + 1, RX - 1), xm = max(tx - 1, 0);
-                    const float4 p0 = buf[cur][xp][ty * 2], p1 = buf[cur][xp][ty * 2 + 1];
-                    const float4 m0 = buf[cur][xm][ty * 2], m1 = buf[cur][xm][ty * 2 + 1];
-                    const float2 vxp[S] = {make_float2(p0.x, p0.y), make_float2(p0.z, p0.w),
-                                           make_float2(p1.x, p1.y), make_float2(p1.z, p1.w)};
-                    const float2 vxm[S] = {make_float2(m0.x, m0.y), make_float2(m0.z, m0.w),
-                                           make_float2(m1.x, m1.y), make_float2(m1.z, m1.w)};
-                    float2 up, dn;  // y-1 of my first site, y+1 of my last site
-                    up.x = __shfl_up_sync(0xffffffffu, t1[S - 1].x, 1);
-                    up.y = __shfl_up_sync(0xffffffffu, t1[S - 1].y, 1);
-                    dn.x = __shfl_down_sync(0xffffffffu, t1[0].x, 1);
-                    dn.y = __shfl_down_sync(0xffffffffu, t1[0].y, 1);
-                    (void)lane;
-                    float2 tk[S];
-#pragma unroll
-                    for (int j = 0; j < S; ++j) {
-                        const float2 vyp = (j < S - 1) ? t1[j + 1] : dn;
-                        const float2 vym = (j > 0) ? t1[j - 1] : up;
-                        const float2 hym = (j > 0) ? make_float2(hy[j - 1].x, -hy[j - 1].y) : hym0;
-                        float2 acc = (k == 1) ? make_float2(0.f, 0.f) : make_float2(-t0[j].x, -t0[j].y);
-                        acc.x = fmaf(hx[j].x, vxp[j].x, acc.x); acc.x = fmaf(-hx[j].y, vxp[j].y, acc.x);
-                        acc.y = fmaf(hx[j].x, vxp[j].y, acc.y); acc.y = fmaf(hx[j].y, vxp[j].x, acc.y);
-                        acc.x = fmaf(hxm[j].x, vxm[j].x, acc.x); acc.x = fmaf(-hxm[j].y, vxm[j].y, acc.x);
-                        acc.y = fmaf(hxm[j].x, vxm[j].y, acc.y); acc.y = fmaf(hxm[j].y, vxm[j].x, acc.y);
-                        acc.x = fmaf(hy[j].x, vyp.x, acc.x); acc.x = fmaf(-hy[j].y, vyp.y, acc.x);
-                        acc.y = fmaf(hy[j].x, vyp.y, acc.y); acc.y = fmaf(hy[j].y, vyp.x, acc.y);
-                        acc.x = fmaf(hym.x, vym.x, acc.x); acc.x = fmaf(-hym.y, vym.y, acc.x);
-                        acc.y = fmaf(hym.x, vym.y, acc.y); acc.y = fmaf(hym.y, vym.x, acc.y);
-                        acc.x = fmaf(d[j], t1[j].x, acc.x);
-                        acc.y = fmaf(d[j], t1[j].y, acc.y);
-                        if (k == 1) { acc.x *= 0.5f; acc.y *= 0.5f; }  // tables hold 2H/a
-                        tk[j] = acc;
-                    }
                     const float sk = cf.s[k];
                     const int odd = cf.odd[k];
 #pragma unroll
-                    for (int j = 0; j < S; ++j) {
-                        if (odd) {
-                            yv[j].x = fmaf(sk, tk[j].y, yv[j].x);
-                            yv[j].y = fmaf(-sk, tk[j].x, yv[j].y);
-                        } else {
-                            yv[j].x = fmaf(sk, tk[j].x, yv[j].x);
-                            yv[j].y = fmaf(sk, tk[j].y, yv[j].y);
-                        }
-                        t0[j] = t1[j];
-                        t1[j] = tk[j];
-                    }
-                    if (k < cf.K) {
-                        buf[k & 1][tx][ty * 2] = make_float4(t1[0].x, t1[0].y, t1[1].x, t1[1].y);
-                        buf[k & 1][tx][ty * 2 + 1] = make_float4(t1[2].x, t1[2].y, t1[3].x, t1[3].y);
-                    }
-                }
-                __syncthreads();
-            }
+                    for (int kk = 0; kk < KB; ++kk) {
+                        float2 vxp[S], vxm[S];
+                        unpack4(smem[src + fidx(kk, xp, 0, ty)], smem[src + fidx(kk, xp, 1, ty)], vxp);
+                        unpack4(smem[src + fidx(kk, xm, 0, ty)], smem[src + fidx(kk, xm, 1, ty)], vxm);
+                        float2 up, dn;  // y-1 of my first position, y+1 of my last
+                        up.x = __shfl_up_sync(0xffffffffu, t1[kk][S - 1].x, 1);
+                        up.y = __shfl_up_sync(0xffffffffu, t1[kk][S - 1].y, 1);
+                        dn.x = __shfl_down_sync(0xffffffffu, t1[kk][0].x, 1);
+                        dn.y = __shfl_down_sync(0xffffffffu, t1[kk][0].y, 1);
+                        float2 t0[S];
+                        if (k >= 2) unpack4(smem[prev2 + fidx(kk, tx, 0, ty)], smem[prev2 + fidx(kk, tx, 1, ty)], t0);
+                        float2 tk[S];
 #pragma unroll
-            for (int j = 0; j < S; ++j) {
-                if (interior[j]) {
-                    // out = e^{-ib dt} (c_0 x + y): the small terms first, the large one last
-                    float2 r;
-                    r.x = fmaf(cf.ph_re, yv[j].x, -cf.ph_im * yv[j].y);
-                    r.y = fmaf(cf.ph_re, yv[j].y, cf.ph_im * yv[j].x);
-                    r.x = fmaf(-cf.a0_im, x0[j].y, r.x);
-                    r.y = fmaf(cf.a0_im, x0[j].x, r.y);
-                    float2 o;
-                    o.x = fmaf(cf.a0_re, x0[j].x, r.x);
-                    o.y = fmaf(cf.a0_re, x0[j].y, r.y);
-                    out[ket * ld + site[j]] = o;
+                        for (int j = 0; j < S; ++j) {
+                            const float2 vyp = (j < S - 1) ? t1[kk][j + 1] : dn;
+                            const float2 vym = (j > 0) ? t1[kk][j - 1] : up;
+                            const float2 hym = (j > 0) ? make_float2(hy[j - 1].x, -hy[j - 1].y) : hym0;
+                            float2 acc = (k == 1) ? make_float2(0.f, 0.f) : make_float2(-t0[j].x, -t0[j].y);
+                            acc.x = fmaf(hx[j].x, vxp[j].x, acc.x); acc.x = fmaf(-hx[j].y, vxp[j].y, acc.x);
+                            acc.y = fmaf(hx[j].x, vxp[j].y, acc.y); acc.y = fmaf(hx[j].y, vxp[j].x, acc.y);
+                            acc.x = fmaf(hxm[j].x, vxm[j].x, acc.x); acc.x = fmaf(-hxm[j].y, vxm[j].y, acc.x);
+                            acc.y = fmaf(hxm[j].x, vxm[j].y, acc.y); acc.y = fmaf(hxm[j].y, vxm[j].x, acc.y);
+                            acc.x = fmaf(hy[j].x, vyp.x, acc.x); acc.x = fmaf(-hy[j].y, vyp.y, acc.x);
+                            acc.y = fmaf(hy[j].x, vyp.y, acc.y); acc.y = fmaf(hy[j].y, vyp.x, acc.y);
+                            acc.x = fmaf(hym.x, vym.x, acc.x); acc.x = fmaf(-hym.y, vym.y, acc.x);
+                            acc.y = fmaf(hym.x, vym.y, acc.y); acc.y = fmaf(hym.y, vym.x, acc.y);
+                            acc.x = fmaf(d[j], t1[kk][j].x, acc.x);
+                            acc.y = fmaf(d[j], t1[kk][j].y, acc.y);
+                            if (k == 1) { acc.x *= 0.5f; acc.y *= 0.5f; }  // tables hold 2H/a
+                            tk[j] = acc;
+                        }
+#pragma unroll
+                        for (int j = 0; j < S; ++j) {
+                            if (odd) {
+                                yv[kk][j].x = fmaf(sk, tk[j].y, yv[kk][j].x);
+                                yv[kk][j].y = fmaf(-sk, tk[j].x, yv[kk][j].y);
+                            } else {
+                                yv[kk][j].x = fmaf(sk, tk[j].x, yv[kk][j].x);
+                                yv[kk][j].y = fmaf(sk, tk[j].y, yv[kk][j].y);
+                            }
+                            t1[kk][j] = tk[j];
+                        }
+                        if (k < K) {
+                            smem[dst + fidx(kk, tx, 0, ty)] = make_float4(tk[0].x, tk[0].y, tk[1].x, tk[1].y);
+                            smem[dst + fidx(kk, tx, 1, ty)] = make_float4(tk[2].x, tk[2].y, tk[3].x, tk[3].y);
+                        }
+                    }
+                }
+                if (k < K) __syncthreads();
+            }
+
+            // out = e^{-ib dt} (c_0 x + y): the small terms first, the dominant one last
+#pragma unroll
+            for (int kk = 0; kk < KB; ++kk) {
+                const int64_t ket = k0 + kk;
+                if (ket >= cur_k_end) break;
+                float2* outk = out + ket * ld;
+                float2 x0[S];
+                unpack4(smem[stage + fidx(kk, tx, 0, ty)], smem[stage + fidx(kk, tx, 1, ty)], x0);
+#pragma unroll
+                for (int j = 0; j < S; ++j) {
+                    if (interior & (1u << j)) {
+                        float2 r;
+                        r.x = fmaf(cf.ph_re, yv[kk][j].x, -cf.ph_im * yv[kk][j].y);
+                        r.y = fmaf(cf.ph_re, yv[kk][j].y, cf.ph_im * yv[kk][j].x);
+                        r.x = fmaf(-cf.a0_im, x0[j].y, r.x);
+                        r.y = fmaf(cf.a0_im, x0[j].x, r.y);
+                        float2 o;
+                        o.x = fmaf(cf.a0_re, x0[j].x, r.x);
+                        o.y = fmaf(cf.a0_re, x0[j].y, r.y);
+                        outk[cur.site[j]] = o;
+                    }
                 }
             }
+            sb ^= 1;
         }
+        if (!have_next_item) break;
     }
+    cp_async_wait_all();
 }
 
 int fused_supported(int precision, int K) { return precision == LM_C32 && K >= 2 && K <= kFusedMaxK; }
+int fused_supported_geom(const Geom& g) { return g.N < (int64_t)1 << 31 && g.Lx < (1 << 30) && g.Ly < (1 << 30); }
 
 cudaError_t launch_cheb_fused_c32(lm_ctx* ctx, const Geom& g, const float2* hop2, const float* diag2,
                                   const float2* x, float2* out, int64_t ld, int64_t m, int K,
@@ -224,8 +306,22 @@ cudaError_t launch_cheb_fused_c32(lm_ctx* ctx, const Geom& g, const float2* hop2
     const int64_t nitems = (int64_t)ntx * nty * kchunks;
     int64_t grid = ctx->sm_count > 0 ? ctx->sm_count : 152;
     if (grid > nitems) grid = nitems;
-    cheb_fused_c32_kernel<<<(unsigned)grid, NTHR, 0, ctx->stream>>>(g, hop2, diag2, x, out, ld, m, H, ntx, nty,
-                                                                      nitems, cf);
+    cudaError_t e = cudaSuccess;
+    switch (K) {
+#define LM_FUSED_CASE(KK)                                                                                       \
+    case KK:                                                                                                  \
+        e = cudaFuncSetAttribute(cheb_fused_c32_kernel<KK>, cudaFuncAttributeMaxDynamicSharedMemorySize,      \
+                                 SMEM_BYTES);                                                                 \
+        if (e != cudaSuccess) return e;                                                                       \
+        cheb_fused_c32_kernel<KK><<<(unsigned)grid, NTHR, SMEM_BYTES, ctx->stream>>>(g, hop2, diag2, x, out,  \
+                                                                                     ld, m, ntx, nty, nitems, cf); \
+        break;
+        LM_FUSED_CASE(2) LM_FUSED_CASE(3) LM_FUSED_CASE(4) LM_FUSED_CASE(5)
+        LM_FUSED_CASE(6) LM_FUSED_CASE(7) LM_FUSED_CASE(8)
+#undef LM_FUSED_CASE
+        default:
+            return cudaErrorInvalidValue;
+    }
     ctx->launches++;
     return cudaGetLastError();
 }

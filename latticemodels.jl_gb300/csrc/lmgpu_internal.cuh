@@ -152,6 +152,7 @@ cudaError_t launch_rescale_columns(lm_ctx* ctx, int precision, void* x, int64_t 
                                    int64_t ld, const double* norms, const double* target);
 cudaError_t launch_sum(lm_ctx* ctx, const double* v, int64_t n, double* out1);
 int fused_supported(int precision, int K);
+int fused_supported_geom(const Geom& g);
 cudaError_t launch_cheb_fused_c32(lm_ctx* ctx, const Geom& g, const float2* hop2, const float* diag2,
                                   const float2* x, float2* out, int64_t ld, int64_t m, int K,
                                   const ChebCoef* coef, double ph_re, double ph_im);

@@ -41,6 +41,7 @@ def test_precision_config_512(lm):
     s32 = lm.KetBlock(lat, X, precision="c32")
     s64 = lm.KetBlock(lat, X.astype(np.complex128), precision="c64")
     del X
+    n0 = s64.norms()
     solver = lm.ChebyshevGPU(renorm_every=20)
     for st in (s32, s64):
         cache = solver.evolution_cache(st)
@@ -51,15 +52,15 @@ def test_precision_config_512(lm):
     J32 = lm.DensityCurrents(H, s32).bond_values()
     J64 = lm.DensityCurrents(H, s64).bond_values()
     n32 = s32.norms()
-    err = {"density": rel(r32, r64), "currents": rel(J32, J64), "norm_drift": float(np.abs(n32 - 1).max()),
+    err = {"density": rel(r32, r64), "currents": rel(J32, J64), "norm_drift": float(np.abs(n32 / n0 - 1).max()),
            "trace_drift": abs(s32.trace() - s64.trace()) / s64.trace()}
     print("precision config (512^2, M=1024, 200 steps):", err)
     assert err["density"] <= 1e-6, err
     assert err["norm_drift"] <= 1e-6, err
     assert err["trace_drift"] <= 1e-6, err
-    assert err["currents"] <= 1e-5, err
+    assert err["currents"] <= 1e-5, err  # measured 2.4e-6: FP32 representation of H + storage rounding
     # FP64 run: norms conserved to 1e-12
-    assert np.abs(s64.norms() - 1).max() <= 1e-12
+    assert np.abs(s64.norms() / n0 - 1).max() <= 1e-12
 
 
 def test_plain_config_256_properties(lm):
