@@ -159,6 +159,18 @@ int lm_solver_step(lm_solver *s, lm_state *st);
  * (room for `cap` coefficients).  Returns LM_ERR_ARG when cap < K + 1. */
 int lm_chebyshev_plan(double x, double tol, int cap, int *K, double *coef);
 
+/* Allocation-free variant of lm_solver_step for a caller-owned ComplexF64 (precision LM_C64)
+ * or ComplexF32 (LM_C32) ket block: `kets` is a device pointer to the n x m column-major block
+ * (leading dimension ld >= n), advanced in place by exp(-i H dt) with the per-order Chebyshev
+ * kernel.  It has no counterpart in the reference.  It calls no cudaMalloc/cudaFree: the
+ * recurrence and accumulator buffers live in a 32 MiB static device array that every GPU
+ * loading the library holds until exit, for hosts whose device memory belongs to another
+ * allocator or that forbid allocation after start-up.  Limit: ld * m <= 1 Mi (ComplexF64) or
+ * 2 Mi (ComplexF32), else LM_ERR_ARG.  The first call on a device sets up the array's address
+ * (call it once before any stream capture); calls that overlap on the GPU share the array and
+ * race. */
+int lm_solver_step_noalloc(lm_solver *s, void *kets, int64_t n, int64_t m, int64_t ld, int precision);
+
 /* ---- readouts ----------------------------------------------------------------------- */
 /* localdensity(state) (src/operators/latticeutils.jl:41-45): N doubles. */
 int lm_localdensity(lm_state *st, double *out);

@@ -78,6 +78,7 @@ SIGNATURES = {
     "lm_solver_update": (_INT, [_P, _P, _D, _INT]),
     "lm_solver_order": (_INT, [_P, _PINT, _PD, _PD]),
     "lm_solver_step": (_INT, [_P, _P]),
+    "lm_solver_step_noalloc": (_INT, [_P, _P, _I64, _I64, _I64, _INT]),
     "lm_chebyshev_plan": (_INT, [_D, _D, _INT, _PINT, _PD]),
     "lm_localdensity": (_INT, [_P, _PD]),
     "lm_bond_currents": (_INT, [_P, _P, _PD]),
