@@ -156,8 +156,11 @@ def dist_info():
     return rank, world, local
 
 
-def cpu_reference(steps, warmup, sample_kets=None):
-    """Times the oracle's C restatement of KrylovKitExp on a bounded sample of the workload."""
+def cpu_reference(steps, warmup, sample_kets=None, cpu_seconds=None):
+    """Times the oracle's C restatement of KrylovKitExp on a bounded sample of the workload.
+
+    With ``cpu_seconds`` the number of timed steps is chosen so that the sample costs about
+    that much CPU time (wall time x threads)."""
     from oracle import krylov, lm_oracle as o
     lat = o.SquareLattice(LX, LY, periodic=(True, True))
     V = make_disorder(lat.N)
@@ -166,15 +169,20 @@ def cpu_reference(steps, warmup, sample_kets=None):
     threads = krylov.max_threads()
     mk = sample_kets or 2 * threads
     X = make_kets(lat.N, mk)
-    for _ in range(warmup):
+    t_one = None
+    for _ in range(max(warmup, 1)):
+        t0 = time.perf_counter()
         X = krylov.krylov_expv_block(csr, DT, X, tol=1e-12, kdim=30, nthreads=threads)
+        t_one = time.perf_counter() - t0
+    if cpu_seconds:
+        steps = int(min(200, max(1, math.ceil(cpu_seconds / (t_one * threads)))))
     t0 = time.perf_counter()
     for _ in range(steps):
         X = krylov.krylov_expv_block(csr, DT, X, tol=1e-12, kdim=30, nthreads=threads)
     dt = time.perf_counter() - t0
     return {"value": mk * steps / dt, "unit": "ket-steps/s", "cores": threads, "kind": "port",
             "sample": f"{mk} of the {M_KETS} kets x {steps} steps (Lanczos exponentiate, tol 1e-12, "
-                      f"krylovdim 30), {dt:.2f} s wall"}
+                      f"krylovdim 30), {dt:.2f} s wall, {dt * threads:.1f} s CPU"}
 
 
 def run_reference_arm(args):
@@ -371,7 +379,7 @@ def main():
         "clocks": clocks,
     }
     if world == 1 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_reference(max(1, min(args.steps, 3)), 1)
+        line["cpu_baseline"] = cpu_reference(1, 1, cpu_seconds=20.0)
     print(json.dumps(line))
     if dist is not None:
         dist.barrier()
