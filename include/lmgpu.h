@@ -171,6 +171,32 @@ int lm_chebyshev_plan(double x, double tol, int cap, int *K, double *coef);
  * race. */
 int lm_solver_step_noalloc(lm_solver *s, void *kets, int64_t n, int64_t m, int64_t ld, int precision);
 
+/* ---- batches of independent lattices ------------------------------------------------ */
+/* Many (Hamiltonian, state) pairs of different sizes evolved together: every step is a
+ * fixed sequence of launches over the work items of all instances (ComplexF32 with K <= 8:
+ * one temporally blocked launch per pass fed by an atomic work queue; otherwise K launches
+ * of the per-order kernel), replayed from a CUDA graph.  The reference evolves each state
+ * separately (src/evolution.jl:245-247); a batch is the same step! applied to all of them.
+ * Density matrices use U P U^dagger = U (U P)^dagger (Hermitian P). */
+typedef struct lm_batch lm_batch;
+int lm_batch_create(lm_ctx *ctx, int kind, int precision, double tol, lm_batch **out);
+int lm_batch_destroy(lm_batch *b);
+/* Adds one instance (its Hamiltonian must be assembled before lm_batch_update). */
+int lm_batch_add(lm_batch *b, lm_ham *ham, lm_state *st, int *index);
+/* update_solver! for every instance; K = the largest order over the instances. */
+int lm_batch_update(lm_batch *b, double dt);
+/* step! for every instance (the states' device buffers may swap, see lm_state_device_ptr). */
+int lm_batch_step(lm_batch *b);
+/* 1 (default): capture the step into a CUDA graph once per buffer parity and replay it. */
+int lm_batch_set_graph(lm_batch *b, int enable);
+/* Pass shape: -1 auto, 0 one temporally blocked launch per pass, 1/2/3 one launch per
+ * order with 2/4/8 kets per thread. */
+int lm_batch_set_config(lm_batch *b, int cfg);
+int lm_batch_info(lm_batch *b, int *K, int *cfg, int64_t *items, int *ninst);
+/* Autotuner: times `steps` steps of every eligible pass shape on copies of the states
+ * (ms_out[0..3], -1 when not eligible), keeps the fastest (*best). */
+int lm_batch_tune(lm_batch *b, int steps, double *ms_out, int *best);
+
 /* ---- readouts ----------------------------------------------------------------------- */
 /* localdensity(state) (src/operators/latticeutils.jl:41-45): N doubles. */
 int lm_localdensity(lm_state *st, double *out);

@@ -122,6 +122,25 @@ static void for_each_bond(const Geom& g, std::vector<std::pair<int64_t, int64_t>
     }
 }
 
+namespace lmgpu {
+// c_k = (2 - delta_k0) (-i)^k J_k(a|dt|) for k = 0..K stored as (s, parity): c_k = s (k even) or
+// -i s (k odd).  sgn = -1 (dt < 0) gives exp(+i H |dt|), the conjugate coefficients.
+void make_coefs(const std::vector<double>& J, int K, double sgn, std::vector<ChebCoef>& out) {
+    out.assign((size_t)K + 1, ChebCoef{0.0, 0});
+    for (int k = 0; k <= K; ++k) {
+        const double mag = (k == 0 ? 1.0 : 2.0) * J[(size_t)k];
+        const int r = k & 3;
+        ChebCoef c;
+        c.odd = k & 1;
+        if (r == 0) c.s = mag;
+        else if (r == 1) c.s = mag * sgn;       // -i mag (conjugate: +i mag = -i (-mag))
+        else if (r == 2) c.s = -mag;
+        else c.s = -mag * sgn;                  // +i mag = -i (-mag)
+        out[(size_t)k] = c;
+    }
+}
+}  // namespace lmgpu
+
 // Smallest K >= 2 whose neglected tail 2 sum_{k>K} |J_k(x)| is below tol; J holds J_0..J_kmax.
 static int cheb_order_for(double x, double tol, std::vector<double>& J) {
     const int kmax = (int)ceil(1.5 * x) + 60;
@@ -739,20 +758,7 @@ int lm_solver_update(lm_solver* s, lm_ham* h, double dt, int force) {
     const double x = a * fabs(dt);
     std::vector<double> J;
     const int K = cheb_order_for(x, s->tol, J);
-    s->coef.assign((size_t)K + 1, ChebCoef{0.0, 0});
-    const double sgn = dt >= 0 ? 1.0 : -1.0;  // exp(+i H |dt|) = conj coefficients
-    for (int k = 0; k <= K; ++k) {
-        // c_k = (2 - delta_k0) (-i)^k J_k(a dt)
-        double mag = (k == 0 ? 1.0 : 2.0) * J[(size_t)k];
-        const int r = k & 3;
-        ChebCoef c;
-        c.odd = k & 1;
-        if (r == 0) c.s = mag;
-        else if (r == 1) c.s = mag * sgn;       // -i * mag  (conj: +i*mag -> s = -mag)
-        else if (r == 2) c.s = -mag;
-        else c.s = -mag * sgn;                  // (+i) * mag = -i * (-mag)
-        s->coef[(size_t)k] = c;
-    }
+    make_coefs(J, K, dt >= 0 ? 1.0 : -1.0, s->coef);
     s->phase_re = cos(b * dt);
     s->phase_im = -sin(b * dt);
     s->a = a;

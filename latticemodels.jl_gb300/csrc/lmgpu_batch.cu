@@ -1,0 +1,609 @@
+// Batched evolution of many independent lattices of different sizes in the same launches.
+//
+// A batch holds (Hamiltonian, state) pairs: open or periodic square lattices of any size,
+// each with its own field, on-site term and Chebyshev coefficients (its own spectral bounds),
+// evolved with one common order K = max_i K_i (instances with smaller K_i simply keep their
+// true higher coefficients).  One step is a fixed sequence of launches over flattened work
+// items of all instances:
+//
+//   kets         : one pass  x -> U x
+//   density P    : U P (columns), conjugate transpose, U (P U^dagger)   (= U P U^dagger)
+//
+// where a pass is either one temporally blocked launch (ComplexF32, K <= 8; items pulled
+// from an atomic work queue) or K launches of the per-order kernel over (instance, site
+// block, ket group) items.  The step is captured once per buffer parity into a CUDA graph and
+// replayed.  `lm_batch_tune` times the candidate pass shapes (orders per pass: all K in one
+// launch or one per launch; kets per thread 2/4/8) on scratch copies and keeps the fastest.
+#include <cuda_runtime.h>
+#include <math.h>
+
+#include <algorithm>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "lmgpu_internal.cuh"
+#include "lmgpu_order.cuh"
+
+namespace lmgpu {
+
+constexpr int kBatchMaxK = 40;
+
+struct OrderInst {
+    Geom g;
+    const void* hop2;
+    const void* diag2;
+    void* S;  // T0 on entry; T_k for even k
+    void* A;  // T_k for odd k
+    void* Y;  // accumulator
+    int64_t ld, M;
+    int64_t item_begin;
+    int64_t lane_blocks;  // ceil(N / 256)
+    double s[kBatchMaxK + 1];
+    double ph_re, ph_im;
+};
+
+struct TransInst {
+    const void* in;
+    void* out;
+    int64_t n, ld;
+    int64_t item_begin;
+    int64_t tiles;  // tiles per dimension (32 x 32)
+};
+
+template <typename T>
+__device__ __forceinline__ int find_item_owner(const T* __restrict__ table, int ninst, int64_t item) {
+    int lo = 0, hi = ninst - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (__ldg(&table[mid].item_begin) <= item) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+// One Chebyshev order k for every instance of the table (items: instance x 256-site block x
+// INNER-ket group).
+template <typename R, int INNER>
+__global__ void __launch_bounds__(256) cheb_order_batch_kernel(const OrderInst* __restrict__ table, int ninst,
+                                                               int64_t nitems, int k, int K) {
+    typedef typename CT<R>::V V;
+    for (int64_t item = blockIdx.x; item < nitems; item += gridDim.x) {
+        const OrderInst& D = table[find_item_owner(table, ninst, item)];
+        const int64_t local = item - D.item_begin;
+        const int64_t lb = local % D.lane_blocks, grp = local / D.lane_blocks;
+        const int64_t lane = lb * blockDim.x + threadIdx.x;
+        const Geom g = D.g;
+        const V* hop2 = (const V*)D.hop2;
+        const R* diag2 = (const R*)D.diag2;
+        V* S = (V*)D.S;
+        V* A = (V*)D.A;
+        V* Y = (V*)D.Y;
+        const R c0 = (R)D.s[0], cs = (R)D.s[k], pr = (R)D.ph_re, pi = (R)D.ph_im;
+        const int64_t g0 = grp * INNER, gs = (int64_t)1 << 62;  // one group per item
+        if (k == 1)
+            cheb_order_block<R, CHEB_FIRST, true, false, INNER>(g, hop2, diag2, S, A, Y, D.ld, D.M, c0, cs, 1, pr, pi,
+                                                                lane, g0, gs);
+        else if (k < K)
+            cheb_order_block<R, CHEB_MID, true, false, INNER>(g, hop2, diag2, (k & 1) ? S : A, (k & 1) ? A : S, Y,
+                                                              D.ld, D.M, c0, cs, k & 1, pr, pi, lane, g0, gs);
+        else
+            cheb_order_block<R, CHEB_LAST, true, false, INNER>(g, hop2, diag2, (k & 1) ? S : A, (k & 1) ? A : S, Y,
+                                                               D.ld, D.M, c0, cs, k & 1, pr, pi, lane, g0, gs);
+    }
+}
+
+// out = in^dagger for every instance (32 x 32 tiles through shared memory).
+template <typename R>
+__global__ void __launch_bounds__(256) transpose_conj_batch_kernel(const TransInst* __restrict__ table, int ninst,
+                                                                   int64_t nitems) {
+    typedef typename CT<R>::V V;
+    __shared__ V tile[32][33];
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 x 8
+    for (int64_t item = blockIdx.x; item < nitems; item += gridDim.x) {
+        const TransInst& D = table[find_item_owner(table, ninst, item)];
+        const int64_t local = item - D.item_begin;
+        const int64_t tr = local / D.tiles, tc = local % D.tiles;
+        const V* in = (const V*)D.in;
+        V* out = (V*)D.out;
+        const int64_t n = D.n, ld = D.ld;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int64_t r = tr * 32 + tx, c = tc * 32 + ty + 8 * j;
+            if (r < n && c < n) tile[ty + 8 * j][tx] = in[r + c * ld];
+        }
+        __syncthreads();
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int64_t r2 = tc * 32 + tx, c2 = tr * 32 + ty + 8 * j;
+            if (r2 < n && c2 < n) {
+                const V v = tile[tx][ty + 8 * j];
+                out[r2 + c2 * ld] = CT<R>::make(v.x, -v.y);
+            }
+        }
+        __syncthreads();
+    }
+}
+
+}  // namespace lmgpu
+
+using namespace lmgpu;
+
+struct lm_batch {
+    lm_ctx* ctx = nullptr;
+    int kind = LM_KETS, precision = LM_C32;
+    double tol = 1e-7;
+    std::vector<lm_ham*> hams;
+    std::vector<lm_state*> states;
+    std::vector<lm_solver*> solvers;
+    int valid = 0;
+    double dt = 0.0;
+    int K = 0;
+    int cfg = -1;         // -1 auto; 0 fused; 1, 2, 3: per-order with 2, 4, 8 kets per thread
+    int use_graph = 1;
+    // host copies of the per-parity tables (parity p: S/A of every state swapped when p = 1)
+    std::vector<FusedInst> hf[2];
+    std::vector<OrderInst> ho1[2], ho2[2];
+    std::vector<TransInst> ht[2];
+    int64_t f_items = 0, o_items = 0, t_items = 0;
+    // device tables
+    FusedInst* df[2] = {nullptr, nullptr};
+    OrderInst* do1[2] = {nullptr, nullptr};
+    OrderInst* do2[2] = {nullptr, nullptr};
+    TransInst* dt_[2] = {nullptr, nullptr};
+    size_t cap_f[2] = {0, 0}, cap_o1[2] = {0, 0}, cap_o2[2] = {0, 0}, cap_t[2] = {0, 0};
+    unsigned long long* dqueue = nullptr;  // two work-queue counters
+    cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    int parity = 0;                         // 1: every state's data currently in its A buffer
+    std::vector<void*> base_S, base_A;      // pointers at update time (parity 0)
+};
+
+static void free_graphs(lm_batch* b) {
+    for (int p = 0; p < 2; ++p)
+        if (b->graph[p]) {
+            cudaGraphExecDestroy(b->graph[p]);
+            b->graph[p] = nullptr;
+        }
+}
+
+static void free_tables(lm_batch* b) {
+    for (int p = 0; p < 2; ++p) {
+        if (b->df[p]) cudaFree(b->df[p]);
+        if (b->do1[p]) cudaFree(b->do1[p]);
+        if (b->do2[p]) cudaFree(b->do2[p]);
+        if (b->dt_[p]) cudaFree(b->dt_[p]);
+        b->df[p] = nullptr;
+        b->do1[p] = b->do2[p] = nullptr;
+        b->dt_[p] = nullptr;
+    }
+    for (int p = 0; p < 2; ++p) b->cap_f[p] = b->cap_o1[p] = b->cap_o2[p] = b->cap_t[p] = 0;
+}
+
+static int inner_of(int cfg) { return cfg == 1 ? 2 : (cfg == 3 ? 8 : 4); }
+
+static int batch_fused_ok(const lm_batch* b) {
+    if (!b->ctx->fused || b->precision != LM_C32 || !fused_supported(b->precision, b->K)) return 0;
+    for (auto* h : b->hams)
+        if (!fused_supported_geom(h->lat->g)) return 0;
+    return 1;
+}
+
+template <typename T>
+static int upload_table(lm_ctx* ctx, T** dptr, size_t* cap, const std::vector<T>& host) {
+    const size_t need = std::max<size_t>(host.size(), 1) * sizeof(T);
+    if (*cap < need) {
+        if (*dptr) cudaFree(*dptr);
+        *dptr = nullptr;
+        *cap = 0;
+        cudaError_t e = cudaMalloc((void**)dptr, need);
+        if (e != cudaSuccess) {
+            *dptr = nullptr;
+            cudaGetLastError();
+            return set_err(ctx, LM_ERR_OOM, "lm_batch: table allocation failed");
+        }
+        *cap = need;
+    }
+    if (!host.empty())
+        return check_cuda(ctx, cudaMemcpyAsync(*dptr, host.data(), host.size() * sizeof(T), cudaMemcpyHostToDevice,
+                                               ctx->stream),
+                          "lm_batch: table upload");
+    return LM_OK;
+}
+
+// Builds every per-parity table for the current coefficients, pass shape and pointers.
+static int build_tables(lm_batch* b) {
+    lm_ctx* ctx = b->ctx;
+    const size_t n = b->states.size();
+    const int K = b->K;
+    const int inner = inner_of(b->cfg);
+    std::vector<std::vector<ChebCoef>> coefs(n);
+    std::vector<double> J;
+    for (size_t i = 0; i < n; ++i) {
+        lm_solver* s = b->solvers[i];
+        bessel_j_all(s->a * fabs(b->dt), K, J);
+        make_coefs(J, K, b->dt >= 0 ? 1.0 : -1.0, coefs[i]);
+    }
+    for (int p = 0; p < 2; ++p) {
+        b->hf[p].assign(n, FusedInst{});
+        b->ho1[p].assign(n, OrderInst{});
+        b->ho2[p].assign(n, OrderInst{});
+        b->ht[p].assign(n, TransInst{});
+        int64_t fi = 0, oi = 0, ti = 0;
+        for (size_t i = 0; i < n; ++i) {
+            lm_state* st = b->states[i];
+            lm_solver* s = b->solvers[i];
+            const Geom& g = b->hams[i]->lat->g;
+            void* S = p ? b->base_A[i] : b->base_S[i];
+            void* A = p ? b->base_S[i] : b->base_A[i];
+            const bool f32 = b->precision == LM_C32;
+            const void* hop2 = f32 ? (const void*)s->d_hop2f : (const void*)s->d_hop2;
+            const void* diag2 = f32 ? (const void*)s->d_diag2f : (const void*)s->d_diag2;
+            // fused table (x = S -> out = A)
+            FusedInst& f = b->hf[p][i];
+            f.g = g;
+            f.hop2 = (const float2*)s->d_hop2f;
+            f.diag2 = s->d_diag2f;
+            f.x = (const float2*)S;
+            f.out = (float2*)A;
+            f.ld = st->ld;
+            f.M = st->m;
+            f.item_begin = fi;
+            if (K <= kFusedMaxK) {
+                fi += fused_items(g, K, st->m, &f.ntx, &f.nty);
+                fused_fill_coef(f, K, coefs[i].data(), s->phase_re, s->phase_im);
+            }
+            // per-order tables
+            auto fill_order = [&](OrderInst& o, void* So, void* Ao) {
+                o.g = g;
+                o.hop2 = hop2;
+                o.diag2 = diag2;
+                o.S = So;
+                o.A = Ao;
+                o.Y = st->d_y;
+                o.ld = st->ld;
+                o.M = st->m;
+                o.lane_blocks = (g.N + 255) / 256;
+                for (int k = 0; k <= kBatchMaxK; ++k) o.s[k] = k <= K ? coefs[i][(size_t)k].s : 0.0;
+                o.ph_re = s->phase_re;
+                o.ph_im = s->phase_im;
+            };
+            OrderInst& o1 = b->ho1[p][i];
+            fill_order(o1, S, A);
+            o1.item_begin = oi;
+            // second density pass: on the transposed block (K even: it sits in A; odd: in S)
+            OrderInst& o2 = b->ho2[p][i];
+            if (K % 2 == 0) fill_order(o2, A, S);
+            else fill_order(o2, S, A);
+            o2.item_begin = oi;
+            oi += o1.lane_blocks * ((st->m + inner - 1) / inner);
+            // transpose table: fused and odd K transpose A -> S, even K (per-order) S -> A
+            TransInst& tr = b->ht[p][i];
+            const bool fused_path = b->cfg == 0;
+            const bool from_S = !fused_path && K % 2 == 0;
+            tr.in = from_S ? S : A;
+            tr.out = from_S ? A : S;
+            tr.n = st->n;
+            tr.ld = st->ld;
+            tr.tiles = (st->n + 31) / 32;
+            tr.item_begin = ti;
+            ti += tr.tiles * tr.tiles;
+        }
+        b->f_items = fi;
+        b->o_items = oi;
+        b->t_items = ti;
+        int rc = upload_table(ctx, &b->df[p], &b->cap_f[p], b->hf[p]);
+        if (rc == LM_OK) rc = upload_table(ctx, &b->do1[p], &b->cap_o1[p], b->ho1[p]);
+        if (rc == LM_OK) rc = upload_table(ctx, &b->do2[p], &b->cap_o2[p], b->ho2[p]);
+        if (rc == LM_OK) rc = upload_table(ctx, &b->dt_[p], &b->cap_t[p], b->ht[p]);
+        if (rc != LM_OK) return rc;
+    }
+    return LM_OK;
+}
+
+static int grid_for(lm_ctx* ctx, int64_t items, int per_sm) {
+    int64_t g = (int64_t)(ctx->sm_count > 0 ? ctx->sm_count : 152) * per_sm;
+    if (g > items) g = items;
+    if (g < 1) g = 1;
+    return (int)g;
+}
+
+static cudaError_t launch_order_pass(lm_batch* b, const OrderInst* table) {
+    lm_ctx* ctx = b->ctx;
+    const int n = (int)b->states.size();
+    const int grid = grid_for(ctx, b->o_items, 8);
+    const int inner = inner_of(b->cfg);
+    for (int k = 1; k <= b->K; ++k) {
+        if (b->precision == LM_C64) {
+            if (inner == 2) cheb_order_batch_kernel<double, 2><<<grid, 256, 0, ctx->stream>>>(table, n, b->o_items, k, b->K);
+            else if (inner == 8) cheb_order_batch_kernel<double, 8><<<grid, 256, 0, ctx->stream>>>(table, n, b->o_items, k, b->K);
+            else cheb_order_batch_kernel<double, 4><<<grid, 256, 0, ctx->stream>>>(table, n, b->o_items, k, b->K);
+        } else {
+            if (inner == 2) cheb_order_batch_kernel<float, 2><<<grid, 256, 0, ctx->stream>>>(table, n, b->o_items, k, b->K);
+            else if (inner == 8) cheb_order_batch_kernel<float, 8><<<grid, 256, 0, ctx->stream>>>(table, n, b->o_items, k, b->K);
+            else cheb_order_batch_kernel<float, 4><<<grid, 256, 0, ctx->stream>>>(table, n, b->o_items, k, b->K);
+        }
+        ctx->launches++;
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
+static cudaError_t launch_transpose(lm_batch* b, const TransInst* table) {
+    lm_ctx* ctx = b->ctx;
+    const int n = (int)b->states.size();
+    const int grid = grid_for(ctx, b->t_items, 8);
+    if (b->precision == LM_C64) transpose_conj_batch_kernel<double><<<grid, 256, 0, ctx->stream>>>(table, n, b->t_items);
+    else transpose_conj_batch_kernel<float><<<grid, 256, 0, ctx->stream>>>(table, n, b->t_items);
+    ctx->launches++;
+    return cudaGetLastError();
+}
+
+static cudaError_t launch_fused_pass(lm_batch* b, int p, int q) {
+    lm_ctx* ctx = b->ctx;
+    cudaError_t e = cudaMemsetAsync(b->dqueue + q, 0, sizeof(unsigned long long), ctx->stream);
+    if (e != cudaSuccess) return e;
+    return launch_fused_table(ctx, b->K, nullptr, b->df[p], (int)b->states.size(), b->f_items, b->dqueue + q, 0);
+}
+
+// Enqueues one step for parity p; returns whether the data moves to the other buffer.
+static cudaError_t enqueue_step(lm_batch* b, int p, int* moved) {
+    cudaError_t e = cudaSuccess;
+    if (b->cfg == 0) {
+        e = launch_fused_pass(b, p, 0);
+        if (e == cudaSuccess && b->kind == LM_DENSITY) {
+            e = launch_transpose(b, b->dt_[p]);
+            if (e == cudaSuccess) e = launch_fused_pass(b, p, 1);
+        }
+        *moved = 1;
+    } else {
+        e = launch_order_pass(b, b->do1[p]);
+        if (b->kind == LM_DENSITY) {
+            if (e == cudaSuccess) e = launch_transpose(b, b->dt_[p]);
+            if (e == cudaSuccess) e = launch_order_pass(b, b->do2[p]);
+            *moved = 1;
+        } else {
+            *moved = b->K % 2;  // odd K ends in A
+        }
+    }
+    return e;
+}
+
+extern "C" {
+
+int lm_batch_create(lm_ctx* ctx, int kind, int precision, double tol, lm_batch** out) {
+    if (!ctx) return LM_ERR_ARG;
+    if (!out) return set_err(ctx, LM_ERR_ARG, "lm_batch_create: null output");
+    *out = nullptr;
+    if (kind != LM_KETS && kind != LM_DENSITY) return set_err(ctx, LM_ERR_ARG, "lm_batch_create: unknown kind");
+    if (precision != LM_C64 && precision != LM_C32) return set_err(ctx, LM_ERR_ARG, "lm_batch_create: unknown precision");
+    if (!(tol > 0.0 && tol < 1.0)) return set_err(ctx, LM_ERR_ARG, "lm_batch_create: tol must lie in (0, 1)");
+    lm_batch* b = new (std::nothrow) lm_batch();
+    if (!b) return set_err(ctx, LM_ERR_OOM, "host allocation");
+    b->ctx = ctx;
+    b->kind = kind;
+    b->precision = precision;
+    b->tol = tol;
+    cudaSetDevice(ctx->device);
+    if (cudaMalloc((void**)&b->dqueue, 2 * sizeof(unsigned long long)) != cudaSuccess) {
+        cudaGetLastError();
+        delete b;
+        return set_err(ctx, LM_ERR_OOM, "lm_batch_create: queue allocation failed");
+    }
+    *out = b;
+    return LM_OK;
+}
+
+int lm_batch_destroy(lm_batch* b) {
+    if (!b) return LM_OK;
+    cudaSetDevice(b->ctx->device);
+    cudaStreamSynchronize(b->ctx->stream);
+    free_graphs(b);
+    free_tables(b);
+    if (b->dqueue) cudaFree(b->dqueue);
+    for (auto* s : b->solvers) lm_solver_destroy(s);
+    delete b;
+    return LM_OK;
+}
+
+int lm_batch_add(lm_batch* b, lm_ham* ham, lm_state* st, int* index) {
+    if (!b) return LM_ERR_ARG;
+    lm_ctx* ctx = b->ctx;
+    if (!ham || !st) return set_err(ctx, LM_ERR_ARG, "lm_batch_add: null argument");
+    if (ham->ctx != ctx || st->ctx != ctx) return set_err(ctx, LM_ERR_ARG, "lm_batch_add: objects from another context");
+    if (st->kind != b->kind || st->precision != b->precision)
+        return set_err(ctx, LM_ERR_ARG, "lm_batch_add: state kind/precision differ from the batch");
+    if (st->n != ham->lat->g.N) return set_err(ctx, LM_ERR_ARG, "lm_batch_add: state size does not match the lattice");
+    for (auto* s : b->states)
+        if (s == st) return set_err(ctx, LM_ERR_ARG, "lm_batch_add: state already in the batch");
+    lm_solver* s = nullptr;
+    int rc = lm_solver_create(ctx, b->tol, &s);
+    if (rc != LM_OK) return rc;
+    b->hams.push_back(ham);
+    b->states.push_back(st);
+    b->solvers.push_back(s);
+    b->valid = 0;
+    free_graphs(b);
+    if (index) *index = (int)b->states.size() - 1;
+    return LM_OK;
+}
+
+int lm_batch_update(lm_batch* b, double dt) {
+    if (!b) return LM_ERR_ARG;
+    lm_ctx* ctx = b->ctx;
+    if (b->states.empty()) return set_err(ctx, LM_ERR_STATE, "lm_batch_update: empty batch");
+    if (!isfinite(dt)) return set_err(ctx, LM_ERR_ARG, "lm_batch_update: non-finite dt");
+    cudaSetDevice(ctx->device);
+    int K = 0;
+    for (size_t i = 0; i < b->states.size(); ++i) {
+        int rc = lm_solver_update(b->solvers[i], b->hams[i], dt, 0);
+        if (rc != LM_OK) return rc;
+        K = std::max(K, b->solvers[i]->K);
+    }
+    if (K > kBatchMaxK) return set_err(ctx, LM_ERR_NOTSUP, "lm_batch_update: Chebyshev order above 40; use smaller dt");
+    const int oldK = b->K, oldcfg = b->cfg;
+    b->K = K;
+    b->dt = dt;
+    if (b->cfg < 0 || (b->cfg == 0 && !batch_fused_ok(b))) b->cfg = batch_fused_ok(b) ? 0 : 2;
+    // pointers at parity 0 follow the states as they are now
+    b->base_S.resize(b->states.size());
+    b->base_A.resize(b->states.size());
+    for (size_t i = 0; i < b->states.size(); ++i) {
+        b->base_S[i] = b->states[i]->d_data;
+        b->base_A[i] = b->states[i]->d_a;
+    }
+    b->parity = 0;
+    if (K != oldK || b->cfg != oldcfg) free_graphs(b);
+    free_graphs(b);  // tables move when the pointers at parity 0 change
+    int rc = build_tables(b);
+    if (rc != LM_OK) return rc;
+    b->valid = 1;
+    return LM_OK;
+}
+
+int lm_batch_step(lm_batch* b) {
+    if (!b) return LM_ERR_ARG;
+    lm_ctx* ctx = b->ctx;
+    if (!b->valid) return set_err(ctx, LM_ERR_STATE, "lm_batch_step: lm_batch_update must run first");
+    cudaSetDevice(ctx->device);
+    // every state must still sit where the tables expect it
+    for (size_t i = 0; i < b->states.size(); ++i) {
+        void* S = b->parity ? b->base_A[i] : b->base_S[i];
+        if (b->states[i]->d_data != S)
+            return set_err(ctx, LM_ERR_STATE, "lm_batch_step: a state was stepped outside the batch; call lm_batch_update");
+    }
+    const int p = b->parity;
+    int moved = 0;
+    if (b->cfg == 0) {  // kernel attributes are set outside any stream capture
+        int rc = check_cuda(ctx, ensure_fused_attr(ctx, b->K), "lm_batch_step: kernel attribute");
+        if (rc != LM_OK) return rc;
+    }
+    if (b->use_graph) {
+        if (!b->graph[p]) {
+            cudaGraph_t gr = nullptr;
+            int rc = check_cuda(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal),
+                                "lm_batch_step: begin capture");
+            if (rc != LM_OK) return rc;
+            cudaError_t e = enqueue_step(b, p, &moved);
+            cudaError_t e2 = cudaStreamEndCapture(ctx->stream, &gr);
+            if (e != cudaSuccess || e2 != cudaSuccess) {
+                if (gr) cudaGraphDestroy(gr);
+                return check_cuda(ctx, e != cudaSuccess ? e : e2, "lm_batch_step: capture");
+            }
+            e = cudaGraphInstantiate(&b->graph[p], gr, 0);
+            cudaGraphDestroy(gr);
+            if (e != cudaSuccess) {
+                b->graph[p] = nullptr;
+                return check_cuda(ctx, e, "lm_batch_step: graph instantiate");
+            }
+        } else {
+            moved = (b->cfg == 0 || b->kind == LM_DENSITY) ? 1 : b->K % 2;
+        }
+        int rc = check_cuda(ctx, cudaGraphLaunch(b->graph[p], ctx->stream), "lm_batch_step: graph launch");
+        if (rc != LM_OK) return rc;
+    } else {
+        int rc = check_cuda(ctx, enqueue_step(b, p, &moved), "lm_batch_step");
+        if (rc != LM_OK) return rc;
+    }
+    if (moved) {
+        for (auto* st : b->states) std::swap(st->d_data, st->d_a);
+        b->parity ^= 1;
+    }
+    return LM_OK;
+}
+
+int lm_batch_set_graph(lm_batch* b, int enable) {
+    if (!b) return LM_ERR_ARG;
+    b->use_graph = enable ? 1 : 0;
+    return LM_OK;
+}
+
+int lm_batch_set_config(lm_batch* b, int cfg) {
+    if (!b) return LM_ERR_ARG;
+    if (cfg < -1 || cfg > 3) return set_err(b->ctx, LM_ERR_ARG, "lm_batch_set_config: config must be -1..3");
+    if (cfg == 0 && b->valid && !batch_fused_ok(b))
+        return set_err(b->ctx, LM_ERR_NOTSUP, "lm_batch_set_config: the fused pass needs ComplexF32 and K <= 8");
+    b->cfg = cfg;
+    free_graphs(b);
+    if (b->valid) {
+        // rebuild for the current pointers (parity 0 = where the data is now)
+        return lm_batch_update(b, b->dt);
+    }
+    return LM_OK;
+}
+
+int lm_batch_info(lm_batch* b, int* K, int* cfg, int64_t* items, int* ninst) {
+    if (!b) return LM_ERR_ARG;
+    if (K) *K = b->K;
+    if (cfg) *cfg = b->cfg;
+    if (items) *items = b->cfg == 0 ? b->f_items : b->o_items;
+    if (ninst) *ninst = (int)b->states.size();
+    return LM_OK;
+}
+
+// Times every eligible pass shape on scratch copies of the batch's states (forward steps),
+// keeps the fastest; the batch's own states are not touched.  ms_out[c] receives the time
+// of one step with config c (negative when not eligible).
+int lm_batch_tune(lm_batch* b, int steps, double* ms_out, int* best) {
+    if (!b) return LM_ERR_ARG;
+    lm_ctx* ctx = b->ctx;
+    if (!b->valid) return set_err(ctx, LM_ERR_STATE, "lm_batch_tune: lm_batch_update must run first");
+    if (steps < 1) steps = 2;
+    cudaSetDevice(ctx->device);
+    // scratch batch over copies of the states
+    lm_batch* t = nullptr;
+    int rc = lm_batch_create(ctx, b->kind, b->precision, b->tol, &t);
+    if (rc != LM_OK) return rc;
+    std::vector<lm_state*> copies;
+    for (size_t i = 0; i < b->states.size() && rc == LM_OK; ++i) {
+        lm_state* c = nullptr;
+        rc = lm_state_create(ctx, b->states[i]->n, b->states[i]->m, b->kind, b->precision, &c);
+        if (rc == LM_OK) {
+            copies.push_back(c);
+            rc = lm_state_copy(c, b->states[i]);
+        }
+        if (rc == LM_OK) rc = lm_batch_add(t, b->hams[i], c, nullptr);
+    }
+    double best_ms = 1e300;
+    int best_cfg = b->cfg;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (rc == LM_OK) rc = check_cuda(ctx, cudaEventCreate(&e0), "cudaEventCreate");
+    if (rc == LM_OK) rc = check_cuda(ctx, cudaEventCreate(&e1), "cudaEventCreate");
+    for (int c = 0; c <= 3 && rc == LM_OK; ++c) {
+        if (ms_out) ms_out[c] = -1.0;
+        t->cfg = c;
+        t->valid = 0;
+        if (c == 0) {
+            t->K = b->K;
+            t->hams = b->hams;
+            if (!batch_fused_ok(b)) continue;
+        }
+        rc = lm_batch_update(t, b->dt);
+        if (rc != LM_OK) break;
+        if (t->cfg != c) continue;
+        rc = lm_batch_step(t);  // warm-up (and graph capture)
+        if (rc != LM_OK) break;
+        cudaEventRecord(e0, ctx->stream);
+        for (int s = 0; s < steps && rc == LM_OK; ++s) rc = lm_batch_step(t);
+        cudaEventRecord(e1, ctx->stream);
+        if (rc != LM_OK) break;
+        rc = check_cuda(ctx, cudaEventSynchronize(e1), "cudaEventSynchronize");
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        const double per = ms / steps;
+        if (ms_out) ms_out[c] = per;
+        if (per < best_ms) {
+            best_ms = per;
+            best_cfg = c;
+        }
+    }
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    lm_batch_destroy(t);
+    for (auto* c : copies) lm_state_destroy(c);
+    if (rc != LM_OK) return rc;
+    if (best) *best = best_cfg;
+    return lm_batch_set_config(b, best_cfg);
+}
+
+}  // extern "C"

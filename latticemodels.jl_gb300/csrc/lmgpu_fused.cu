@@ -1,23 +1,25 @@
-// Temporally blocked Chebyshev step (ComplexF32 recurrence) for the square-lattice stencil.
+// Temporally blocked Chebyshev step (ComplexF32 recurrence) for the square-lattice stencil,
+// for one lattice or for a batch of independent lattices of different sizes.
 //
-// One launch applies the whole series  y = e^{-ib dt} sum_{k<=K} c_k T_k(H~) x  to a
-// column-major ket block: every ket is read once (a spatial tile plus a halo of K sites)
-// and the result written once, instead of five vector passes per Chebyshev order.
+// One launch applies the whole series  y = e^{-ib dt} sum_{k<=K} c_k T_k(H~) x  to
+// column-major ket blocks: every ket is read once (a spatial tile plus a halo of K sites) and
+// the result written once, instead of five vector passes per Chebyshev order.
 //
-// Tiling: a CTA of 512 threads owns a region of 32 (x) x 64 (y) sites; thread (tx, ty)
-// holds the four consecutive y-sites 4ty..4ty+3 of row tx for KB kets at a time in
-// registers (T_{k-1}, the accumulator and the stencil coefficients, which the KB
-// kets share).  Per order, rows are exchanged through a double-buffered shared-memory copy
-// of T_{k-1} (x neighbours) and warp shuffles (y neighbours: a warp holds two whole rows).
-// The valid part of the region shrinks by one site per order, so after K orders the inner
-// (32-2K) x (64-2K) sites are exact and are written out.  Positions outside the lattice (open
-// axes) hold zeros and zero coefficients; periodic axes wrap the halo.
+// Tiling: a CTA of 512 threads owns a region of 32 (x) x 64 (y) sites; thread (tx, ty) holds
+// the four consecutive y-sites 4ty..4ty+3 of row tx in registers (T_{k-1}, the accumulator and
+// the stencil coefficients).  Per order, rows are exchanged through a double-buffered
+// shared-memory copy of T_{k-1} (x neighbours) and warp shuffles (y neighbours: a warp holds
+// two whole rows); T_{k-2} of a thread's own sites is read back from the buffer T_k
+// overwrites.  The valid part of the region shrinks by one site per order, so after K orders
+// the inner (32-2K) x (64-2K) sites are exact and are written out.  Positions outside the
+// lattice (open axes) hold zeros and zero coefficients; periodic axes wrap the halo.
 //
-// Pipelining: the next KB kets (of this tile, or the first ones of the CTA's next tile) are
-// copied global -> shared with cp.async while the current ones are computed; order 1 reads
-// its neighbours straight from that staging buffer.  Work items are (tile, 16 kets);
-// persistent CTAs stride over them with consecutive items on neighbouring tiles of the same
-// kets, so halo re-reads hit L2.
+// Work items are (instance, tile, 16 kets).  A single lattice strides over its items
+// statically; a batch pulls items from a global atomic counter (the work queue), so CTAs
+// that finish small lattices early take more items.  The next item's first ket is staged
+// global -> shared with cp.async while the current ket is computed; order 1 reads its
+// neighbours straight from that staging buffer.  Consecutive items are neighbouring tiles of
+// the same kets, so halo re-reads hit L2.
 #include <cuda_runtime.h>
 
 #include "lmgpu_internal.cuh"
@@ -31,19 +33,11 @@ constexpr int S = 4;           // sites per thread along y
 constexpr int RY = TY * S;     // region extent along y
 constexpr int NTHR = RX * TY;  // 512
 constexpr int KB = 1;          // kets a thread advances together
-constexpr int KETS_PER_ITEM = 16;
 // one buffer = KB kets x RX rows x 2 halves x TY float4 (a float4 = two sites of one thread)
 constexpr int BUF_F4 = KB * RX * 2 * TY;
-constexpr int SMEM_BYTES = 4 * BUF_F4 * 16;  // T double buffer + staging double buffer = 128 KB
+constexpr int SMEM_BYTES = 4 * BUF_F4 * 16;  // T double buffer + staging double buffer
+constexpr int DESC_WORDS = (int)(sizeof(FusedInst) + 3) / 4;
 }  // namespace
-
-struct FusedCoef {
-    float s[kFusedMaxK + 1];
-    int odd[kFusedMaxK + 1];
-    int K;
-    float ph_re, ph_im;   // e^{-ib dt}
-    float a0_re, a0_im;   // e^{-ib dt} c_0
-};
 
 __device__ __forceinline__ int fidx(int kk, int row, int h, int ty) { return ((kk * RX + row) * 2 + h) * TY + ty; }
 
@@ -84,9 +78,9 @@ __device__ __forceinline__ void cp_async8(float4* smem_f4, int half, const float
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
 
-// Stages kets k0, k0+1 (those below k_end) of my four positions into `stage`.
-__device__ __forceinline__ void prefetch_pair(float4* stage, const TileMap& m, const float2* __restrict__ x,
-                                              int64_t ld, int64_t k0, int64_t k_end, int tx, int ty) {
+// Stages kets k0 .. k0+KB-1 (those below k_end) of my four positions into `stage`.
+__device__ __forceinline__ void prefetch_kets(float4* stage, const TileMap& m, const float2* x, int64_t ld,
+                                              int64_t k0, int64_t k_end, int tx, int ty) {
 #pragma unroll
     for (int kk = 0; kk < KB; ++kk) {
         const int64_t ket = k0 + kk;
@@ -107,14 +101,30 @@ __device__ __forceinline__ void unpack4(const float4 a, const float4 b, float2 v
     v[3] = make_float2(b.z, b.w);
 }
 
+// Instance holding global item `item` (largest i with table[i].item_begin <= item).
+__device__ __forceinline__ int find_instance(const FusedInst* __restrict__ table, int ninst, int64_t item) {
+    int lo = 0, hi = ninst - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (__ldg(&table[mid].item_begin) <= item) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+// Cooperative copy of an instance descriptor into shared memory (threads < DESC_WORDS).
+__device__ __forceinline__ void load_desc(FusedInst* dst, const FusedInst* src, int t) {
+    if (t < DESC_WORDS) reinterpret_cast<int*>(dst)[t] = __ldg(reinterpret_cast<const int*>(src) + t);
+}
+
 template <int K>
 __global__ void __launch_bounds__(NTHR, 1)
-cheb_fused_c32_kernel(Geom g, const float2* __restrict__ hop2, const float* __restrict__ diag2,
-                      const float2* __restrict__ x, float2* __restrict__ out, int64_t ld, int64_t M,
-                      int ntx, int nty, int64_t nitems, FusedCoef cf) {
+cheb_fused_c32_kernel(FusedInst single, const FusedInst* __restrict__ table, int ninst, int64_t nitems,
+                      unsigned long long* queue) {
     constexpr int H = K;  // halo = number of orders
     extern __shared__ float4 smem[];
-    // buffer offsets (in float4) into smem: T double buffer, then the staging double buffer
+    __shared__ FusedInst s_desc[2];   // current and next instance
+    __shared__ long long s_item[2];   // next work items (alternating slots)
     auto tb = [](int i) { return i * BUF_F4; };
     auto sbuf = [](int i) { return (2 + i) * BUF_F4; };
 
@@ -122,23 +132,53 @@ cheb_fused_c32_kernel(Geom g, const float2* __restrict__ hop2, const float* __re
     const int tx = t / TY;
     const int ty = t % TY;
     const int warp_row0 = (t >> 5) * 2;  // the two rows a warp holds
-    const int64_t ntiles = (int64_t)ntx * nty;
 
-    int64_t item = blockIdx.x;
+    // next item id: the work queue for a batch, a static stride for one lattice
+    long long last_static = (long long)blockIdx.x - gridDim.x;
+    auto fetch = [&]() -> long long {
+        if (queue) return (long long)atomicAdd(queue, 1ull);
+        last_static += gridDim.x;
+        return last_static;
+    };
+    auto desc_of = [&](long long it) -> const FusedInst* {
+        return table ? &table[find_instance(table, ninst, it)] : nullptr;
+    };
+
+    if (t == 0) {
+        s_item[0] = fetch();
+        s_item[1] = fetch();
+    }
+    __syncthreads();
+    long long item = s_item[0];
+    int nslot = 1;  // slot holding the upcoming item
     if (item >= nitems) return;
-    TileMap m = tile_map(g, item % ntiles, nty, H, tx, ty);
-    int64_t k_begin = (item / ntiles) * KETS_PER_ITEM;
-    int64_t k_end = min(M, k_begin + KETS_PER_ITEM);
-    prefetch_pair(smem + sbuf(0), m, x, ld, k_begin, k_end, tx, ty);
+    int dslot = 0;
+    {
+        const FusedInst* src = desc_of(item);
+        if (src) load_desc(&s_desc[0], src, t);
+        else if (t == 0) s_desc[0] = single;
+    }
+    __syncthreads();
+
+    int64_t lit = item - s_desc[0].item_begin;  // item within the instance
+    int64_t ntiles = (int64_t)s_desc[0].ntx * s_desc[0].nty;
+    TileMap m = tile_map(s_desc[0].g, lit % ntiles, s_desc[0].nty, H, tx, ty);
+    int64_t k_begin = (lit / ntiles) * kFusedKetsPerItem;
+    int64_t k_end = min(s_desc[0].M, k_begin + kFusedKetsPerItem);
+    prefetch_kets(smem + sbuf(0), m, s_desc[0].x, s_desc[0].ld, k_begin, k_end, tx, ty);
     int sb = 0;
 
     while (true) {
+        const FusedInst& D = s_desc[dslot];
+        const Geom g = D.g;
         // stencil coefficients of my positions (shared by every ket of the item)
         float2 hx[S], hxm[S], hy[S];
         float d[S];
         float2 hym0 = make_float2(0.f, 0.f);
         unsigned interior = 0;  // bit j: position j is written out
         {
+            const float2* hop2 = D.hop2;
+            const float* diag2 = D.diag2;
             const int64_t xsm = wrap_axis(m.gx - 1, g.Lx, g.per_x);
             const int64_t xs = wrap_axis(m.gx, g.Lx, g.per_x);
 #pragma unroll
@@ -166,17 +206,29 @@ cheb_fused_c32_kernel(Geom g, const float2* __restrict__ hop2, const float* __re
 
         for (int64_t k0 = k_begin; k0 < cur_k_end; k0 += KB) {
             cp_async_wait_all();
-            __syncthreads();  // staged pair visible; the previous pair is done with every buffer
-            // stage the pair after this one: same item, or the first pair of my next item
+            __syncthreads();  // staged kets visible; the previous kets are done with every buffer
             if (k0 + KB < cur_k_end) {
-                prefetch_pair(smem + sbuf(sb ^ 1), cur, x, ld, k0 + KB, cur_k_end, tx, ty);
-            } else if (item + gridDim.x < nitems) {
-                item += gridDim.x;
-                m = tile_map(g, item % ntiles, nty, H, tx, ty);
-                k_begin = (item / ntiles) * KETS_PER_ITEM;
-                k_end = min(M, k_begin + KETS_PER_ITEM);
-                prefetch_pair(smem + sbuf(sb ^ 1), m, x, ld, k_begin, k_end, tx, ty);
-                have_next_item = true;
+                prefetch_kets(smem + sbuf(sb ^ 1), cur, D.x, D.ld, k0 + KB, cur_k_end, tx, ty);
+            } else {
+                // last kets of this item: take the next item and stage its first kets
+                const long long nxt = s_item[nslot];
+                if (nxt < nitems) {
+                    const FusedInst* src = desc_of(nxt);
+                    if (src) load_desc(&s_desc[dslot ^ 1], src, t);
+                    else if (t == 0) s_desc[dslot ^ 1] = single;
+                    if (t == 0) s_item[nslot ^ 1] = fetch();
+                    nslot ^= 1;
+                    __syncthreads();  // next descriptor visible
+                    const FusedInst& Dn = s_desc[dslot ^ 1];
+                    item = nxt;
+                    lit = item - Dn.item_begin;
+                    ntiles = (int64_t)Dn.ntx * Dn.nty;
+                    m = tile_map(Dn.g, lit % ntiles, Dn.nty, H, tx, ty);
+                    k_begin = (lit / ntiles) * kFusedKetsPerItem;
+                    k_end = min(Dn.M, k_begin + kFusedKetsPerItem);
+                    prefetch_kets(smem + sbuf(sb ^ 1), m, Dn.x, Dn.ld, k_begin, k_end, tx, ty);
+                    have_next_item = true;
+                }
             }
             const int stage = sbuf(sb);
 
@@ -199,8 +251,7 @@ cheb_fused_c32_kernel(Geom g, const float2* __restrict__ hop2, const float* __re
                 const bool active = (warp_row0 + 1 >= k) && (warp_row0 < RX - k);
                 if (active) {
                     const int xp = min(tx + 1, RX - 1), xm = max(tx - 1, 0);
-                    const float sk = cf.s[k];
-                    const int odd = cf.odd[k];
+                    const float sk = D.s[k];
 #pragma unroll
                     for (int kk = 0; kk < KB; ++kk) {
                         float2 vxp[S], vxm[S];
@@ -235,10 +286,10 @@ cheb_fused_c32_kernel(Geom g, const float2* __restrict__ hop2, const float* __re
                         }
 #pragma unroll
                         for (int j = 0; j < S; ++j) {
-                            if (odd) {
+                            if (k & 1) {  // c_k = -i s_k
                                 yv[kk][j].x = fmaf(sk, tk[j].y, yv[kk][j].x);
                                 yv[kk][j].y = fmaf(-sk, tk[j].x, yv[kk][j].y);
-                            } else {
+                            } else {      // c_k = s_k
                                 yv[kk][j].x = fmaf(sk, tk[j].x, yv[kk][j].x);
                                 yv[kk][j].y = fmaf(sk, tk[j].y, yv[kk][j].y);
                             }
@@ -254,24 +305,25 @@ cheb_fused_c32_kernel(Geom g, const float2* __restrict__ hop2, const float* __re
             }
 
             // out = e^{-ib dt} (c_0 x + y): the small terms first, the dominant one last
+            const float ph_re = D.ph_re, ph_im = D.ph_im, a0_re = D.a0_re, a0_im = D.a0_im;
 #pragma unroll
             for (int kk = 0; kk < KB; ++kk) {
                 const int64_t ket = k0 + kk;
                 if (ket >= cur_k_end) break;
-                float2* outk = out + ket * ld;
+                float2* outk = D.out + ket * D.ld;
                 float2 x0[S];
                 unpack4(smem[stage + fidx(kk, tx, 0, ty)], smem[stage + fidx(kk, tx, 1, ty)], x0);
 #pragma unroll
                 for (int j = 0; j < S; ++j) {
                     if (interior & (1u << j)) {
                         float2 r;
-                        r.x = fmaf(cf.ph_re, yv[kk][j].x, -cf.ph_im * yv[kk][j].y);
-                        r.y = fmaf(cf.ph_re, yv[kk][j].y, cf.ph_im * yv[kk][j].x);
-                        r.x = fmaf(-cf.a0_im, x0[j].y, r.x);
-                        r.y = fmaf(cf.a0_im, x0[j].x, r.y);
+                        r.x = fmaf(ph_re, yv[kk][j].x, -ph_im * yv[kk][j].y);
+                        r.y = fmaf(ph_re, yv[kk][j].y, ph_im * yv[kk][j].x);
+                        r.x = fmaf(-a0_im, x0[j].y, r.x);
+                        r.y = fmaf(a0_im, x0[j].x, r.y);
                         float2 o;
-                        o.x = fmaf(cf.a0_re, x0[j].x, r.x);
-                        o.y = fmaf(cf.a0_re, x0[j].y, r.y);
+                        o.x = fmaf(a0_re, x0[j].x, r.x);
+                        o.y = fmaf(a0_re, x0[j].y, r.y);
                         outk[cur.site[j]] = o;
                     }
                 }
@@ -279,6 +331,7 @@ cheb_fused_c32_kernel(Geom g, const float2* __restrict__ hop2, const float* __re
             sb ^= 1;
         }
         if (!have_next_item) break;
+        dslot ^= 1;
     }
     cp_async_wait_all();
 }
@@ -286,35 +339,55 @@ cheb_fused_c32_kernel(Geom g, const float2* __restrict__ hop2, const float* __re
 int fused_supported(int precision, int K) { return precision == LM_C32 && K >= 2 && K <= kFusedMaxK; }
 int fused_supported_geom(const Geom& g) { return g.N < (int64_t)1 << 31 && g.Lx < (1 << 30) && g.Ly < (1 << 30); }
 
-cudaError_t launch_cheb_fused_c32(lm_ctx* ctx, const Geom& g, const float2* hop2, const float* diag2,
-                                  const float2* x, float2* out, int64_t ld, int64_t m, int K,
-                                  const ChebCoef* coef, double ph_re, double ph_im) {
-    FusedCoef cf{};
-    cf.K = K;
-    for (int k = 0; k <= K; ++k) {
-        cf.s[k] = (float)coef[k].s;
-        cf.odd[k] = coef[k].odd;
+int64_t fused_items(const Geom& g, int K, int64_t m, int* ntx, int* nty) {
+    const int IX = RX - 2 * K, IY = RY - 2 * K;
+    *ntx = (int)((g.Lx + IX - 1) / IX);
+    *nty = (int)((g.Ly + IY - 1) / IY);
+    const int64_t kchunks = (m + kFusedKetsPerItem - 1) / kFusedKetsPerItem;
+    return (int64_t)(*ntx) * (*nty) * kchunks;
+}
+
+void fused_fill_coef(FusedInst& d, int K, const ChebCoef* coef, double ph_re, double ph_im) {
+    for (int k = 0; k <= kFusedMaxK; ++k) d.s[k] = k <= K ? (float)coef[k].s : 0.f;
+    d.ph_re = (float)ph_re;
+    d.ph_im = (float)ph_im;
+    d.a0_re = (float)(ph_re * coef[0].s);
+    d.a0_im = (float)(ph_im * coef[0].s);
+}
+
+cudaError_t ensure_fused_attr(lm_ctx* ctx, int K) {
+    if (ctx->fused_attr & (1u << K)) return cudaSuccess;
+    cudaError_t e = cudaErrorInvalidValue;
+    switch (K) {
+#define LM_ATTR_CASE(KK)                                                                                        \
+    case KK:                                                                                                  \
+        e = cudaFuncSetAttribute(cheb_fused_c32_kernel<KK>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES); \
+        break;
+        LM_ATTR_CASE(2) LM_ATTR_CASE(3) LM_ATTR_CASE(4) LM_ATTR_CASE(5)
+        LM_ATTR_CASE(6) LM_ATTR_CASE(7) LM_ATTR_CASE(8)
+#undef LM_ATTR_CASE
+        default:
+            break;
     }
-    cf.ph_re = (float)ph_re;
-    cf.ph_im = (float)ph_im;
-    cf.a0_re = (float)(ph_re * coef[0].s);
-    cf.a0_im = (float)(ph_im * coef[0].s);
-    const int H = K;
-    const int IX = RX - 2 * H, IY = RY - 2 * H;
-    const int ntx = (int)((g.Lx + IX - 1) / IX), nty = (int)((g.Ly + IY - 1) / IY);
-    const int64_t kchunks = (m + KETS_PER_ITEM - 1) / KETS_PER_ITEM;
-    const int64_t nitems = (int64_t)ntx * nty * kchunks;
-    int64_t grid = ctx->sm_count > 0 ? ctx->sm_count : 152;
-    if (grid > nitems) grid = nitems;
+    if (e == cudaSuccess) ctx->fused_attr |= 1u << K;
+    return e;
+}
+
+cudaError_t launch_fused_table(lm_ctx* ctx, int K, const FusedInst* single, const FusedInst* d_table, int ninst,
+                               int64_t nitems, unsigned long long* d_queue, int grid) {
+    if (nitems <= 0) return cudaSuccess;
+    if (grid <= 0) grid = ctx->sm_count > 0 ? ctx->sm_count : 152;
+    if (grid > nitems) grid = (int)nitems;
+    FusedInst one{};
+    if (single) one = *single;
     cudaError_t e = cudaSuccess;
     switch (K) {
-#define LM_FUSED_CASE(KK)                                                                                       \
-    case KK:                                                                                                  \
-        e = cudaFuncSetAttribute(cheb_fused_c32_kernel<KK>, cudaFuncAttributeMaxDynamicSharedMemorySize,      \
-                                 SMEM_BYTES);                                                                 \
-        if (e != cudaSuccess) return e;                                                                       \
-        cheb_fused_c32_kernel<KK><<<(unsigned)grid, NTHR, SMEM_BYTES, ctx->stream>>>(g, hop2, diag2, x, out,  \
-                                                                                     ld, m, ntx, nty, nitems, cf); \
+#define LM_FUSED_CASE(KK)                                                                                        \
+    case KK:                                                                                                   \
+        e = ensure_fused_attr(ctx, KK);                                                                        \
+        if (e != cudaSuccess) return e;                                                                        \
+        cheb_fused_c32_kernel<KK><<<(unsigned)grid, NTHR, SMEM_BYTES, ctx->stream>>>(one, d_table, ninst, nitems, \
+                                                                                     d_queue);                 \
         break;
         LM_FUSED_CASE(2) LM_FUSED_CASE(3) LM_FUSED_CASE(4) LM_FUSED_CASE(5)
         LM_FUSED_CASE(6) LM_FUSED_CASE(7) LM_FUSED_CASE(8)
@@ -324,6 +397,23 @@ cudaError_t launch_cheb_fused_c32(lm_ctx* ctx, const Geom& g, const float2* hop2
     }
     ctx->launches++;
     return cudaGetLastError();
+}
+
+cudaError_t launch_cheb_fused_c32(lm_ctx* ctx, const Geom& g, const float2* hop2, const float* diag2,
+                                  const float2* x, float2* out, int64_t ld, int64_t m, int K,
+                                  const ChebCoef* coef, double ph_re, double ph_im) {
+    FusedInst d{};
+    d.g = g;
+    d.hop2 = hop2;
+    d.diag2 = diag2;
+    d.x = x;
+    d.out = out;
+    d.ld = ld;
+    d.M = m;
+    d.item_begin = 0;
+    const int64_t nitems = fused_items(g, K, m, &d.ntx, &d.nty);
+    fused_fill_coef(d, K, coef, ph_re, ph_im);
+    return launch_fused_table(ctx, K, &d, nullptr, 1, nitems, nullptr, 0);
 }
 
 }  // namespace lmgpu

@@ -39,6 +39,8 @@ struct FieldSet {
 
 // Largest Chebyshev order the temporally blocked kernel handles in one pass (its halo).
 constexpr int kFusedMaxK = 8;
+// Kets per work item of the temporally blocked kernel.
+constexpr int kFusedKetsPerItem = 16;
 
 // Per-order launch description of the Chebyshev recurrence.
 enum ChebMode { CHEB_FIRST = 0, CHEB_MID = 1, CHEB_LAST = 2 };
@@ -50,6 +52,22 @@ template <> struct V2<float> { typedef float2 T; };
 struct ChebCoef {
     double s;        // real magnitude with sign: c_k = s (k even) or -i*s (k odd)
     int odd;         // parity of k
+};
+
+// One lattice of a temporally blocked launch: geometry, stencil tables, in/out ket blocks,
+// its first global work item and its Chebyshev coefficients (c_k = s_k or -i s_k by parity).
+struct FusedInst {
+    Geom g;
+    const float2* hop2;
+    const float* diag2;
+    const float2* x;
+    float2* out;
+    int64_t ld, M;
+    int ntx, nty;
+    int64_t item_begin;
+    float s[kFusedMaxK + 1];
+    float ph_re, ph_im;   // e^{-ib dt}
+    float a0_re, a0_im;   // e^{-ib dt} c_0
 };
 
 }  // namespace lmgpu
@@ -64,6 +82,7 @@ struct lm_ctx {
     std::string err;
     int timing = 0;
     int fused = 1;                      // LM_OPT_FUSED: temporally blocked c32 step enabled
+    unsigned fused_attr = 0;            // bit K: shared-memory attribute of the K-order kernel set
     std::vector<cudaEvent_t> ev_pool;   // pairs (start, stop) of timed Chebyshev sweeps
     std::vector<int> ev_launches;       // launches covered by each recorded pair
     size_t ev_used = 0;                 // pairs recorded but not yet resolved
@@ -153,6 +172,13 @@ cudaError_t launch_rescale_columns(lm_ctx* ctx, int precision, void* x, int64_t 
 cudaError_t launch_sum(lm_ctx* ctx, const double* v, int64_t n, double* out1);
 int fused_supported(int precision, int K);
 int fused_supported_geom(const Geom& g);
+int64_t fused_items(const Geom& g, int K, int64_t m, int* ntx, int* nty);
+void fused_fill_coef(FusedInst& d, int K, const ChebCoef* coef, double ph_re, double ph_im);
+// One launch over `nitems` work items of one instance (`single`) or of a device table of
+// `ninst` instances pulled from the work-queue counter `d_queue` (zeroed before the launch).
+cudaError_t launch_fused_table(lm_ctx* ctx, int K, const FusedInst* single, const FusedInst* d_table, int ninst,
+                               int64_t nitems, unsigned long long* d_queue, int grid);
+cudaError_t ensure_fused_attr(lm_ctx* ctx, int K);
 cudaError_t launch_cheb_fused_c32(lm_ctx* ctx, const Geom& g, const float2* hop2, const float* diag2,
                                   const float2* x, float2* out, int64_t ld, int64_t m, int K,
                                   const ChebCoef* coef, double ph_re, double ph_im);
@@ -162,5 +188,6 @@ cudaError_t launch_convert(lm_ctx* ctx, int to_precision, const void* src, void*
 // Host math (lmgpu_api.cu)
 int64_t bond_count(const Geom& g);
 void bessel_j_all(double x, int kmax, std::vector<double>& out);
+void make_coefs(const std::vector<double>& J, int K, double sgn, std::vector<ChebCoef>& out);
 
 }  // namespace lmgpu

@@ -6,6 +6,7 @@ and ``DensityCurrents``.  All compute runs in liblmgpu.so (hand-written sm_103a 
 package only holds the host-side bookkeeping and the ctypes bindings.
 """
 from ._lib import LMError, load as load_library
+from .batch import Batch
 from .device import Context, default_context
 from .evolution import ChebyshevGPU, Evolution, EvolutionIterator, EvolutionSolver, EvolutionTimestamp
 from .fields import FieldSum, LandauGauge, NoField, PointFlux, PointFluxes, SymmetricGauge
@@ -16,7 +17,7 @@ from .spectrum import densitymatrix, diagonalize
 from .states import DensityMatrix, DeviceState, Ket, KetBlock, Operator
 
 __all__ = [
-    "LMError", "load_library", "Context", "default_context",
+    "Batch", "LMError", "load_library", "Context", "default_context",
     "ChebyshevGPU", "Evolution", "EvolutionIterator", "EvolutionSolver", "EvolutionTimestamp",
     "FieldSum", "LandauGauge", "NoField", "PointFlux", "PointFluxes", "SymmetricGauge",
     "Hamiltonian", "tightbinding_hamiltonian", "LatticeValue", "SquareLattice",

@@ -80,6 +80,15 @@ SIGNATURES = {
     "lm_solver_step": (_INT, [_P, _P]),
     "lm_solver_step_noalloc": (_INT, [_P, _P, _I64, _I64, _I64, _INT]),
     "lm_chebyshev_plan": (_INT, [_D, _D, _INT, _PINT, _PD]),
+    "lm_batch_create": (_INT, [_P, _INT, _INT, _D, C.POINTER(_P)]),
+    "lm_batch_destroy": (_INT, [_P]),
+    "lm_batch_add": (_INT, [_P, _P, _P, _PINT]),
+    "lm_batch_update": (_INT, [_P, _D]),
+    "lm_batch_step": (_INT, [_P]),
+    "lm_batch_set_graph": (_INT, [_P, _INT]),
+    "lm_batch_set_config": (_INT, [_P, _INT]),
+    "lm_batch_info": (_INT, [_P, _PINT, _PINT, _PI64, _PINT]),
+    "lm_batch_tune": (_INT, [_P, _INT, _PD, _PINT]),
     "lm_localdensity": (_INT, [_P, _PD]),
     "lm_bond_currents": (_INT, [_P, _P, _PD]),
     "lm_trace": (_INT, [_P, _PD]),

@@ -114,6 +114,13 @@ class Hamiltonian:
         dh.ensure(self.onsite, self.field.amplitudes())
         return dh
 
+    def device_private(self, ctx=None) -> _DeviceHam:
+        """A device Hamiltonian owned by the caller (not shared through the cache), assembled."""
+        ctx = ctx or default_context()
+        dh = _DeviceHam(ctx, self.lattice, self.t1, self.field.components(), self.auto_pbc_field)
+        dh.ensure(self.onsite, self.field.amplitudes())
+        return dh
+
     def csc(self, ctx=None):
         """The assembled matrix as the reference's CSC: (colptr, rowval) 1-based, nzval complex."""
         ctx = ctx or default_context()
