@@ -204,6 +204,94 @@ def run_reference_arm(args):
 
 
 # ------------------------------------------------------------------------------------------
+BATCH_WORKLOAD = ("{n} independent LxL open lattices, L ~ U{{16..96}}, t1=1, PointFlux(B,(L//2+0.5)^2) with "
+                  "B ~ U[0,0.3], disorder U[-W/2,W/2] with W ~ U[0,3], dense P_0 per lattice, dt=0.1")
+
+
+def run_batch_workload(args):
+    """The batching workload: uneven dense-P lattices stepped together (one graph per step).
+
+    P_0 of every lattice is a principal submatrix of one seeded random Hermitian matrix (a
+    stand-in of the right shape: the step's cost does not depend on P_0's values; parity of
+    the batched path with true densitymatrix P_0 is covered by the GPU tests).  Ket-steps: a
+    dense-P step U P U^dagger counts 2N per lattice."""
+    import ctypes as C
+    import torch
+    import lmgpu
+    from lmgpu import _lib
+    ctx = lmgpu.default_context()
+    ext = torch.cuda.ExternalStream(ctx.stream_ptr(), device=torch.device("cuda", 0))
+    rng = np.random.default_rng(SEED + 7)
+    n = args.instances
+    Ls = rng.integers(16, 97, size=n)
+    Bs = rng.uniform(0, 0.3, size=n)
+    Ws = rng.uniform(0, 3, size=n)
+    prec = args.precision
+    dtype = np.complex64 if prec == "c32" else np.complex128
+    elem = 8 if prec == "c32" else 16
+    # lattices that fit: data + recurrence buffer (+ accumulator for the per-order path)
+    free = torch.cuda.mem_get_info()[0]
+    per = 2 if prec == "c32" else 3
+    budget = 0.85 * free
+    take, used = [], 0
+    for i, L in enumerate(Ls):
+        need = per * elem * int(L) ** 4
+        if used + need > budget:
+            break
+        take.append(i)
+        used += need
+    Nmax = int(max(Ls[take])) ** 2
+    R = (rng.standard_normal((Nmax, Nmax), dtype=np.float32)
+         + 1j * rng.standard_normal((Nmax, Nmax), dtype=np.float32)).astype(dtype)
+    Pbig = np.asfortranarray((R + R.conj().T) * (0.5 / math.sqrt(Nmax)))
+    del R
+    batch = lmgpu.Batch("density", prec)
+    states = []
+    t_setup = time.perf_counter()
+    for i in take:
+        L = int(Ls[i])
+        lat = lmgpu.SquareLattice(L, L)
+        V = np.random.default_rng(SEED + 1000 + i).uniform(-Ws[i] / 2, Ws[i] / 2, size=L * L)
+        H = lmgpu.tightbinding_hamiltonian(lat, V, field=lmgpu.PointFlux(float(Bs[i]), (L // 2 + 0.5, L // 2 + 0.5)))
+        st = lmgpu.DensityMatrix.__new__(lmgpu.DensityMatrix)
+        lmgpu.DeviceState.__init__(st, lat, None, _lib.LM_DENSITY, prec, None, ctx, shape=(L * L, L * L))
+        ctx.check(ctx.lib.lm_state_upload(st.handle, Pbig.ctypes.data_as(C.c_void_p), Nmax))
+        batch.add(H, st)
+        states.append(st)
+    batch.update(0.1)
+    tune = batch.tune(steps=1)
+    info = batch.info()
+    t_setup = time.perf_counter() - t_setup
+    for _ in range(args.warmup):
+        batch.step()
+    ctx.synchronize()
+    clk = ClockSampler(0)
+    clk.start()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(ext)
+    for _ in range(args.steps):
+        batch.step()
+    e1.record(ext)
+    e1.synchronize()
+    clocks = clk.stop()
+    ms = e0.elapsed_time(e1)
+    ket_steps = sum(2 * int(Ls[i]) ** 2 for i in take)
+    tr = [s.trace() for s in states[:4]]
+    line = {"metric": "ket-steps/s (batched dense-P lattices)", "value": ket_steps * args.steps / (ms / 1000.0),
+            "unit": "ket-steps/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms / args.steps, "higher_is_better": True, "dtype": prec,
+            "data": "synthetic (seeded; P_0 = principal submatrices of one random Hermitian matrix)",
+            "config": {"workload": BATCH_WORKLOAD.format(n=n), "instances_run": len(take),
+                       "instances_requested": n, "sum_N2": int(sum(int(Ls[i]) ** 4 for i in take)),
+                       "chebyshev_order": info["K"], "tuned": tune, "setup_s": t_setup,
+                       "device_bytes": used},
+            "clocks": clocks, "trace_sample": tr}
+    print(json.dumps(line))
+    return 0
+
+
+# ------------------------------------------------------------------------------------------
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -212,11 +300,17 @@ def main():
     ap.add_argument("--impl", default="lmgpu", choices=["lmgpu", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--kets", type=int, default=M_KETS)
+    ap.add_argument("--workload", default="kets", choices=["kets", "batch"],
+                    help="kets: the 256^2 ket-block workload (default); batch: 512 uneven dense-P lattices")
+    ap.add_argument("--instances", type=int, default=512)
+    ap.add_argument("--precision", default="c32", choices=["c32", "c64"])
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
         return run_reference_arm(args)
+    if args.workload == "batch":
+        return run_batch_workload(args)
 
     rank, world, local = dist_info()
     import torch

@@ -89,6 +89,14 @@ static int dalloc(lm_ctx* ctx, void** p, size_t bytes, const char* what) {
     return LM_OK;
 }
 
+namespace lmgpu {
+// Allocates the accumulator buffer of a state on first use (the per-order path needs it).
+int ensure_accumulator(lm_state* s) {
+    if (s->d_y) return LM_OK;
+    return dalloc(s->ctx, &s->d_y, s->elem * (size_t)s->ld * (size_t)s->m, "accumulator scratch");
+}
+}  // namespace lmgpu
+
 static int ensure_red(lm_ctx* ctx, size_t n) {
     if (ctx->red_cap >= n) return LM_OK;
     if (ctx->d_red) cudaFree(ctx->d_red);
@@ -564,7 +572,7 @@ int lm_state_create(lm_ctx* ctx, int64_t n, int64_t m, int kind, int precision, 
     const size_t bytes = s->elem * (size_t)n * (size_t)m;
     int rc = dalloc(ctx, &s->d_data, bytes, "state");
     if (rc == LM_OK) rc = dalloc(ctx, &s->d_a, bytes, "recurrence scratch");
-    if (rc == LM_OK) rc = dalloc(ctx, &s->d_y, bytes, "accumulator scratch");
+    // the accumulator is only needed by the per-order path; it is allocated on first use
     if (rc != LM_OK) {
         if (s->d_data) cudaFree(s->d_data);
         if (s->d_a) cudaFree(s->d_a);
@@ -844,6 +852,10 @@ int lm_solver_step(lm_solver* s, lm_state* st) {
     const Geom& g = s->ham->lat->g;
     CHECK_ARG(ctx, st->n == g.N, "lm_solver_step: state size does not match the lattice");
     cudaSetDevice(ctx->device);
+    if (!(ctx->fused && st->kind == LM_KETS && fused_supported(st->precision, s->K) && fused_supported_geom(g))) {
+        int rc0 = ensure_accumulator(st);
+        if (rc0 != LM_OK) return rc0;
+    }
     int where = 0;
     // psi <- U psi on the columns (kets, or the columns of P)
     int rc = cheb_apply(s, g, st->precision, 1, 0, st->d_data, st->d_a, st->d_y, st->ld, st->m, &where);

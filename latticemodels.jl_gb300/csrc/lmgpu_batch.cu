@@ -453,6 +453,11 @@ int lm_batch_update(lm_batch* b, double dt) {
         b->base_A[i] = b->states[i]->d_a;
     }
     b->parity = 0;
+    if (b->cfg != 0)
+        for (auto* st : b->states) {
+            int rc0 = ensure_accumulator(st);
+            if (rc0 != LM_OK) return rc0;
+        }
     if (K != oldK || b->cfg != oldcfg) free_graphs(b);
     free_graphs(b);  // tables move when the pointers at parity 0 change
     int rc = build_tables(b);

@@ -189,5 +189,6 @@ cudaError_t launch_convert(lm_ctx* ctx, int to_precision, const void* src, void*
 int64_t bond_count(const Geom& g);
 void bessel_j_all(double x, int kmax, std::vector<double>& out);
 void make_coefs(const std::vector<double>& J, int K, double sgn, std::vector<ChebCoef>& out);
+int ensure_accumulator(lm_state* s);
 
 }  // namespace lmgpu
