@@ -546,8 +546,9 @@ int lm_batch_info(lm_batch* b, int* K, int* cfg, int64_t* items, int* ninst) {
     return LM_OK;
 }
 
-// Times every eligible pass shape on scratch copies of the batch's states (forward steps),
-// keeps the fastest; the batch's own states are not touched.  ms_out[c] receives the time
+// Times every eligible pass shape on scratch copies of the batch's states (forward steps; a
+// leading sample of the instances when all copies would not fit), keeps the fastest; the
+// batch's own states are not touched.  ms_out[c] receives the time
 // of one step with config c (negative when not eligible).
 int lm_batch_tune(lm_batch* b, int steps, double* ms_out, int* best) {
     if (!b) return LM_ERR_ARG;
@@ -560,7 +561,16 @@ int lm_batch_tune(lm_batch* b, int steps, double* ms_out, int* best) {
     int rc = lm_batch_create(ctx, b->kind, b->precision, b->tol, &t);
     if (rc != LM_OK) return rc;
     std::vector<lm_state*> copies;
+    // a sample of the instances (in order) whose copies fit in a quarter of the free memory,
+    // at most 8 GiB
+    size_t free_b = 0, total_b = 0;
+    cudaMemGetInfo(&free_b, &total_b);
+    const size_t cap = std::min<size_t>(free_b / 4, (size_t)8 << 30);
+    size_t used = 0;
     for (size_t i = 0; i < b->states.size() && rc == LM_OK; ++i) {
+        const size_t need = 3 * b->states[i]->elem * (size_t)b->states[i]->ld * (size_t)b->states[i]->m;
+        if (i > 0 && used + need > cap) break;
+        used += need;
         lm_state* c = nullptr;
         rc = lm_state_create(ctx, b->states[i]->n, b->states[i]->m, b->kind, b->precision, &c);
         if (rc == LM_OK) {
@@ -578,11 +588,7 @@ int lm_batch_tune(lm_batch* b, int steps, double* ms_out, int* best) {
         if (ms_out) ms_out[c] = -1.0;
         t->cfg = c;
         t->valid = 0;
-        if (c == 0) {
-            t->K = b->K;
-            t->hams = b->hams;
-            if (!batch_fused_ok(b)) continue;
-        }
+        if (c == 0 && !batch_fused_ok(b)) continue;
         rc = lm_batch_update(t, b->dt);
         if (rc != LM_OK) break;
         if (t->cfg != c) continue;
