@@ -147,6 +147,10 @@ int lm_solver_destroy(lm_solver *s);
 /* update_solver!(solver, H, dt, force) (src/evolution.jl:83-92): recomputes the
  * propagator unless H (same object, same assembly) and dt are unchanged and force = 0. */
 int lm_solver_update(lm_solver *s, lm_ham *ham, double dt, int force);
+/* Fixes the spectral interval [emin, emax] of the propagator (the Gershgorin enclosure of the
+ * Hamiltonian otherwise; emin = emax = 0 restores it).  With fixed bounds the propagator is
+ * one polynomial in H for every parameter value, which the adjoint differentiates exactly. */
+int lm_solver_set_bounds(lm_solver *s, double emin, double emax);
 /* Chebyshev order chosen by the last update (number of H applications per step). */
 int lm_solver_order(const lm_solver *s, int *K, double *a, double *b);
 /* step!(solver, state, cache) (src/evolution.jl:69-78): psi <- U psi for kets,
@@ -196,6 +200,27 @@ int lm_batch_info(lm_batch *b, int *K, int *cfg, int64_t *items, int *ninst);
 /* Autotuner: times `steps` steps of every eligible pass shape on copies of the states
  * (ms_out[0..3], -1 when not eligible), keeps the fastest (*best). */
 int lm_batch_tune(lm_batch *b, int steps, double *ms_out, int *best);
+
+/* ---- adjoint (gradients of a density loss) ----------------------------------------- */
+/* Co-state propagation through the Chebyshev steps for L = sum_i (rho_i(T) - target_i)^2,
+ * rho_i = sum_m |psi_im|^2: gradients with respect to every on-site potential V_i and to the
+ * amplitude of one field component per step (accumulated into `nslots` slots, e.g. one per
+ * piecewise-constant flux interval).  No reference counterpart (the reference has no
+ * derivatives); it differentiates the same step! (src/evolution.jl:69-78). */
+typedef struct lm_adjoint lm_adjoint;
+int lm_adjoint_create(lm_ctx *ctx, int64_t n, int64_t m, int precision, int nslots, lm_adjoint **out);
+int lm_adjoint_destroy(lm_adjoint *a);
+/* Zeroes the accumulated gradients. */
+int lm_adjoint_reset(lm_adjoint *a);
+/* Final co-state lambda = dL/dpsi* = 4 (rho - target) psi (host target, N values) and the loss. */
+int lm_adjoint_seed(lm_adjoint *a, lm_state *psi, const double *target, lm_state *lambda, double *loss);
+/* Gradient terms of step n (psi = psi_n, lambda = lambda_{n+1}); `s` must be updated with `ham`
+ * and dt.  component >= 0 also accumulates dL/d(amplitude of that field component) into
+ * gradient slot `slot`.  The caller then applies U_n^dagger to lambda (a solver updated with -dt). */
+int lm_adjoint_step(lm_adjoint *a, lm_solver *s, lm_ham *ham, int component, int slot, lm_state *psi,
+                    lm_state *lambda);
+/* Downloads the accumulated gradients (N on-site values, nslots field amplitudes). */
+int lm_adjoint_gradients(lm_adjoint *a, double *gV, double *gA);
 
 /* ---- readouts ----------------------------------------------------------------------- */
 /* localdensity(state) (src/operators/latticeutils.jl:41-45): N doubles. */

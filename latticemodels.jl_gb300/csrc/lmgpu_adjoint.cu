@@ -1,0 +1,445 @@
+// Adjoint of the Chebyshev evolution: gradients of a density loss with respect to the
+// on-site potentials and the field amplitudes.
+//
+// Forward step n:  psi_{n+1} = U_n psi_n,  U_n = e^{-ib dt} sum_k c_k T_k(H~_n),  H~ = (H - b)/a
+// with a, b, K fixed (frozen spectral bounds), so U_n is an exact polynomial in H_n and its
+// discrete adjoint is exact.  With the co-state lambda_{n+1} = dL/dpsi*_{n+1} (L real):
+//
+//   lambda_n = U_n^dagger lambda_{n+1}           (the propagator with conjugate coefficients)
+//   dL/dtheta += Re e^{-ib dt} sum_{k>=1} < beta_k , s_k >,   s_1 = D~ T_0,  s_k = 2 D~ T_{k-1}
+//
+// where D~ = (dH/dtheta)/a and beta is the adjoint of the three-term recurrence,
+//   beta_k = conj(c_k) lambda + 2 H~ beta_{k+1} - beta_{k+2},  beta_{K+1} = beta_{K+2} = 0.
+// For an on-site potential V_i, < beta, D~ T > = conj(beta_i) T_i / a summed over kets; for a
+// field amplitude A, dH[s, s+e]/dA = -2 pi i LI_e(A = 1) H[s, s+e] on every bond.
+//
+// lm_adjoint_step recomputes T_0 .. T_{K-1} from psi_n, runs the beta recurrence and
+// accumulates both gradients in FP64; the caller applies U^dagger to lambda with a solver
+// updated for -dt (the same polynomial with conjugate coefficients).
+#include <cuda_runtime.h>
+#include <math.h>
+
+#include <new>
+#include <vector>
+
+#include "lmgpu_internal.cuh"
+#include "lmgpu_order.cuh"
+
+namespace lmgpu {
+
+// out = alpha * (2H~) tp - tpp + w * lam   (tables hold 2H/a and 2(V-b)/a; tpp, lam optional)
+// w = conj(c_k): (s, 0) for even k, (0, s) for odd k (conj(-i s) = i s).
+template <typename R>
+__global__ void __launch_bounds__(256) adj_recur_kernel(Geom g, const typename CT<R>::V* __restrict__ hop2,
+                                                        const R* __restrict__ diag2,
+                                                        const typename CT<R>::V* __restrict__ tp,
+                                                        const typename CT<R>::V* __restrict__ tpp,
+                                                        const typename CT<R>::V* __restrict__ lam,
+                                                        typename CT<R>::V* __restrict__ out, int64_t ld, int64_t M,
+                                                        R alpha, R w_re, R w_im) {
+    typedef typename CT<R>::V V;
+    const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= g.N) return;
+    const Nbr nb = neighbours(g, s);
+    const V z = CT<R>::make(0, 0);
+    const V hxp = nb.hxp ? hop2[s] : z, hyp = nb.hyp ? hop2[g.N + s] : z;
+    V t = nb.hxm ? hop2[nb.xm] : z;
+    const V hxm = CT<R>::make(t.x, -t.y);
+    t = nb.hym ? hop2[g.N + nb.ym] : z;
+    const V hym = CT<R>::make(t.x, -t.y);
+    const R d = diag2[s];
+    for (int64_t m = blockIdx.y; m < M; m += gridDim.y) {
+        const int64_t o = m * ld;
+        V acc = z;
+        if (tp) {
+            const V v0 = tp[o + s], vxp = tp[o + nb.xp], vxm = tp[o + nb.xm], vyp = tp[o + nb.yp], vym = tp[o + nb.ym];
+            acc.x = fma(hxp.x, vxp.x, acc.x); acc.x = fma(-hxp.y, vxp.y, acc.x);
+            acc.y = fma(hxp.x, vxp.y, acc.y); acc.y = fma(hxp.y, vxp.x, acc.y);
+            acc.x = fma(hxm.x, vxm.x, acc.x); acc.x = fma(-hxm.y, vxm.y, acc.x);
+            acc.y = fma(hxm.x, vxm.y, acc.y); acc.y = fma(hxm.y, vxm.x, acc.y);
+            acc.x = fma(hyp.x, vyp.x, acc.x); acc.x = fma(-hyp.y, vyp.y, acc.x);
+            acc.y = fma(hyp.x, vyp.y, acc.y); acc.y = fma(hyp.y, vyp.x, acc.y);
+            acc.x = fma(hym.x, vym.x, acc.x); acc.x = fma(-hym.y, vym.y, acc.x);
+            acc.y = fma(hym.x, vym.y, acc.y); acc.y = fma(hym.y, vym.x, acc.y);
+            acc.x = fma(d, v0.x, acc.x);
+            acc.y = fma(d, v0.y, acc.y);
+            acc.x *= alpha;
+            acc.y *= alpha;
+        }
+        if (tpp) {
+            const V q = tpp[o + s];
+            acc.x -= q.x;
+            acc.y -= q.y;
+        }
+        if (lam) {
+            const V l = lam[o + s];
+            acc.x = fma(w_re, l.x, fma(-w_im, l.y, acc.x));
+            acc.y = fma(w_re, l.y, fma(w_im, l.x, acc.y));
+        }
+        out[o + s] = acc;
+    }
+}
+
+// Gradient terms of order k: for every site s (FP64 over the kets of one chunk)
+//   gV[s]   += Re( ph * f * conj(beta_s) T_s )
+//   gA[0]   += Re( ph * f * sum_bonds [conj(beta_s) D[s,j] T_j + conj(beta_j) conj(D[s,j]) T_s] )
+// with ph = e^{-ib dt}, f = 1/a (k = 1) or 2/a (k >= 2), D = dH/dA of the bond table dhop.
+template <typename R>
+__global__ void __launch_bounds__(256) adj_grad_kernel(Geom g, const double2* __restrict__ dhop,
+                                                       const typename CT<R>::V* __restrict__ beta,
+                                                       const typename CT<R>::V* __restrict__ T, int64_t ld, int64_t M,
+                                                       int64_t chunk, double ph_re, double ph_im, double f,
+                                                       double* __restrict__ gV, double* __restrict__ gA) {
+    typedef typename CT<R>::V V;
+    __shared__ double red[8];
+    const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t m0 = (int64_t)blockIdx.y * chunk, m1 = min(M, m0 + chunk);
+    double vre = 0.0, vim = 0.0;  // sum conj(beta_s) T_s
+    double are = 0.0, aim = 0.0;  // bond terms
+    if (s < g.N) {
+        const Nbr nb = neighbours(g, s);
+        double2 dx = make_double2(0.0, 0.0), dy = make_double2(0.0, 0.0);
+        if (dhop) {  // the bond s -> s+e and its Hermitian partner (each bond owned by its source)
+            if (nb.hxp) dx = dhop[s];
+            if (nb.hyp) dy = dhop[g.N + s];
+        }
+        for (int64_t m = m0; m < m1; ++m) {
+            const int64_t o = m * ld;
+            const V b = beta[o + s], t = T[o + s];
+            vre += (double)b.x * t.x + (double)b.y * t.y;  // conj(b) t
+            vim += (double)b.x * t.y - (double)b.y * t.x;
+            if (dhop) {
+#pragma unroll
+                for (int dir = 0; dir < 2; ++dir) {
+                    const bool has = dir == 0 ? nb.hxp : nb.hyp;
+                    if (!has) continue;
+                    const int64_t j = dir == 0 ? nb.xp : nb.yp;
+                    const double2 D = dir == 0 ? dx : dy;
+                    const V bj = beta[o + j], tj = T[o + j];
+                    // conj(b_s) D T_j
+                    const double pr = D.x * tj.x - D.y * tj.y, pi = D.x * tj.y + D.y * tj.x;
+                    are += (double)b.x * pr + (double)b.y * pi;
+                    aim += (double)b.x * pi - (double)b.y * pr;
+                    // conj(b_j) conj(D) T_s
+                    const double qr = D.x * t.x + D.y * t.y, qi = D.x * t.y - D.y * t.x;
+                    are += (double)bj.x * qr + (double)bj.y * qi;
+                    aim += (double)bj.x * qi - (double)bj.y * qr;
+                }
+            }
+        }
+        if (m1 > m0) {
+            const double gv = f * (ph_re * vre - ph_im * vim);
+            atomicAdd(gV + s, gv);
+        }
+    }
+    if (gA) {
+        double ga = f * (ph_re * are - ph_im * aim);
+        for (int o = 16; o > 0; o >>= 1) ga += __shfl_down_sync(0xffffffffu, ga, o);
+        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = ga;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double tot = 0.0;
+            for (int w = 0; w < (int)(blockDim.x >> 5); ++w) tot += red[w];
+            atomicAdd(gA, tot);
+        }
+    }
+}
+
+// rho_s = sum_m |psi_sm|^2; loss = sum_s (rho_s - target_s)^2; lambda = 4 (rho_s - target_s) psi
+template <typename R>
+__global__ void __launch_bounds__(256) adj_seed_kernel(int64_t N, const typename CT<R>::V* __restrict__ psi,
+                                                       typename CT<R>::V* __restrict__ lam, int64_t ld, int64_t M,
+                                                       const double* __restrict__ target, double* __restrict__ loss) {
+    typedef typename CT<R>::V V;
+    __shared__ double red[8];
+    const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    double l = 0.0;
+    if (s < N) {
+        double rho = 0.0;
+        for (int64_t m = 0; m < M; ++m) {
+            const V v = psi[m * ld + s];
+            rho += (double)v.x * v.x + (double)v.y * v.y;
+        }
+        const double diff = rho - target[s];
+        l = diff * diff;
+        const R f = (R)(4.0 * diff);
+        for (int64_t m = 0; m < M; ++m) {
+            const V v = psi[m * ld + s];
+            lam[m * ld + s] = CT<R>::make(f * v.x, f * v.y);
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) l += __shfl_down_sync(0xffffffffu, l, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = l;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double tot = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) tot += red[w];
+        atomicAdd(loss, tot);
+    }
+}
+
+// dH[s, s+e]/dA_c = -2 pi i LI_c(A_c = 1) H[s, s+e] for field component c.
+__global__ void flux_derivative_kernel(Geom g, FieldSet f, int comp, const double2* __restrict__ hop,
+                                       double2* __restrict__ dhop) {
+    const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= g.N) return;
+    FieldSet one = f;
+    one.n = 1;
+    one.c[0] = f.c[comp];
+    one.amp[0] = 1.0;
+    const int64_t xi = s / g.Ly, yi = s - xi * g.Ly;
+    const double x1 = (double)(xi + 1), y1 = (double)(yi + 1);
+#pragma unroll
+    for (int dir = 0; dir < 2; ++dir) {
+        const double x2 = dir == 0 ? x1 + 1.0 : x1, y2 = dir == 0 ? y1 : y1 + 1.0;
+        const double li = field_line_integral(g, one, x1, y1, x2, y2);
+        const double2 h = hop[dir * g.N + s];
+        const double w = -2.0 * M_PI * li;  // d/dA e^{-2 pi i A li} = -2 pi i li (...)
+        dhop[dir * g.N + s] = make_double2(-w * h.y, w * h.x);  // (i w) h
+    }
+}
+
+}  // namespace lmgpu
+
+using namespace lmgpu;
+
+struct lm_adjoint {
+    lm_ctx* ctx = nullptr;
+    int64_t n = 0, m = 0;
+    int precision = LM_C64;
+    size_t elem = 16;
+    int K = 0;
+    std::vector<void*> T;  // T_0 .. T_{K-1} (T_0 aliases psi during a step)
+    void* B[3] = {nullptr, nullptr, nullptr};
+    double* d_gV = nullptr;
+    double* d_gA = nullptr;
+    int nslots = 0;
+    double* d_loss = nullptr;
+    double* d_target = nullptr;
+    double2* d_dhop = nullptr;
+};
+
+static void adj_free_stack(lm_adjoint* a) {
+    for (size_t i = 1; i < a->T.size(); ++i)
+        if (a->T[i]) cudaFree(a->T[i]);
+    a->T.clear();
+    for (auto& b : a->B) {
+        if (b) cudaFree(b);
+        b = nullptr;
+    }
+}
+
+static int adj_alloc(lm_ctx* ctx, void** p, size_t bytes) {
+    if (cudaMalloc(p, bytes) != cudaSuccess) {
+        *p = nullptr;
+        cudaGetLastError();
+        return set_err(ctx, LM_ERR_OOM, "lm_adjoint: device allocation failed");
+    }
+    return LM_OK;
+}
+
+static int adj_ensure_stack(lm_adjoint* a, int K) {
+    if (a->K == K && !a->T.empty()) return LM_OK;
+    adj_free_stack(a);
+    const size_t bytes = a->elem * (size_t)a->n * (size_t)a->m;
+    a->T.assign((size_t)K, nullptr);
+    for (int k = 1; k < K; ++k) {
+        int rc = adj_alloc(a->ctx, &a->T[(size_t)k], bytes);
+        if (rc != LM_OK) return rc;
+    }
+    for (auto& b : a->B) {
+        int rc = adj_alloc(a->ctx, &b, bytes);
+        if (rc != LM_OK) return rc;
+    }
+    a->K = K;
+    return LM_OK;
+}
+
+extern "C" {
+
+int lm_adjoint_create(lm_ctx* ctx, int64_t n, int64_t m, int precision, int nslots, lm_adjoint** out) {
+    if (!ctx) return LM_ERR_ARG;
+    if (!out) return set_err(ctx, LM_ERR_ARG, "lm_adjoint_create: null output");
+    *out = nullptr;
+    if (n < 1 || m < 1 || nslots < 0) return set_err(ctx, LM_ERR_ARG, "lm_adjoint_create: bad sizes");
+    if (precision != LM_C64 && precision != LM_C32) return set_err(ctx, LM_ERR_ARG, "lm_adjoint_create: unknown precision");
+    lm_adjoint* a = new (std::nothrow) lm_adjoint();
+    if (!a) return set_err(ctx, LM_ERR_OOM, "host allocation");
+    a->ctx = ctx;
+    a->n = n;
+    a->m = m;
+    a->precision = precision;
+    a->elem = precision == LM_C64 ? 16 : 8;
+    a->nslots = nslots;
+    cudaSetDevice(ctx->device);
+    int rc = adj_alloc(ctx, (void**)&a->d_gV, sizeof(double) * (size_t)n);
+    if (rc == LM_OK) rc = adj_alloc(ctx, (void**)&a->d_gA, sizeof(double) * (size_t)(nslots > 0 ? nslots : 1));
+    if (rc == LM_OK) rc = adj_alloc(ctx, (void**)&a->d_loss, sizeof(double));
+    if (rc == LM_OK) rc = adj_alloc(ctx, (void**)&a->d_target, sizeof(double) * (size_t)n);
+    if (rc == LM_OK) rc = adj_alloc(ctx, (void**)&a->d_dhop, sizeof(double2) * 2 * (size_t)n);
+    if (rc != LM_OK) {
+        if (a->d_gV) cudaFree(a->d_gV);
+        if (a->d_gA) cudaFree(a->d_gA);
+        if (a->d_loss) cudaFree(a->d_loss);
+        if (a->d_target) cudaFree(a->d_target);
+        if (a->d_dhop) cudaFree(a->d_dhop);
+        delete a;
+        return rc;
+    }
+    cudaMemsetAsync(a->d_gV, 0, sizeof(double) * (size_t)n, ctx->stream);
+    cudaMemsetAsync(a->d_gA, 0, sizeof(double) * (size_t)(nslots > 0 ? nslots : 1), ctx->stream);
+    *out = a;
+    return LM_OK;
+}
+
+int lm_adjoint_destroy(lm_adjoint* a) {
+    if (!a) return LM_OK;
+    cudaSetDevice(a->ctx->device);
+    cudaStreamSynchronize(a->ctx->stream);
+    adj_free_stack(a);
+    cudaFree(a->d_gV);
+    cudaFree(a->d_gA);
+    cudaFree(a->d_loss);
+    cudaFree(a->d_target);
+    cudaFree(a->d_dhop);
+    delete a;
+    return LM_OK;
+}
+
+int lm_adjoint_reset(lm_adjoint* a) {
+    if (!a) return LM_ERR_ARG;
+    lm_ctx* ctx = a->ctx;
+    cudaSetDevice(ctx->device);
+    CUDA_TRY(ctx, cudaMemsetAsync(a->d_gV, 0, sizeof(double) * (size_t)a->n, ctx->stream), "memset");
+    CUDA_TRY(ctx, cudaMemsetAsync(a->d_gA, 0, sizeof(double) * (size_t)(a->nslots > 0 ? a->nslots : 1), ctx->stream),
+             "memset");
+    return LM_OK;
+}
+
+int lm_adjoint_seed(lm_adjoint* a, lm_state* psi, const double* target, lm_state* lam, double* loss) {
+    if (!a) return LM_ERR_ARG;
+    lm_ctx* ctx = a->ctx;
+    if (!psi || !lam || !target || !loss) return set_err(ctx, LM_ERR_ARG, "lm_adjoint_seed: null argument");
+    if (psi->n != a->n || psi->m != a->m || lam->n != a->n || lam->m != a->m || psi->precision != a->precision ||
+        lam->precision != a->precision || psi->kind != LM_KETS || lam->kind != LM_KETS)
+        return set_err(ctx, LM_ERR_ARG, "lm_adjoint_seed: state shapes differ from the adjoint");
+    cudaSetDevice(ctx->device);
+    CUDA_TRY(ctx, cudaMemcpyAsync(a->d_target, target, sizeof(double) * (size_t)a->n, cudaMemcpyHostToDevice, ctx->stream),
+             "upload target");
+    CUDA_TRY(ctx, cudaMemsetAsync(a->d_loss, 0, sizeof(double), ctx->stream), "memset");
+    const unsigned blocks = (unsigned)((a->n + 255) / 256);
+    if (a->precision == LM_C64)
+        adj_seed_kernel<double><<<blocks, 256, 0, ctx->stream>>>(a->n, (const double2*)psi->d_data, (double2*)lam->d_data,
+                                                                 psi->ld, a->m, a->d_target, a->d_loss);
+    else
+        adj_seed_kernel<float><<<blocks, 256, 0, ctx->stream>>>(a->n, (const float2*)psi->d_data, (float2*)lam->d_data,
+                                                                psi->ld, a->m, a->d_target, a->d_loss);
+    ctx->launches++;
+    CUDA_TRY(ctx, cudaGetLastError(), "seed kernel");
+    CUDA_TRY(ctx, cudaMemcpyAsync(loss, a->d_loss, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream), "download loss");
+    CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream), "sync");
+    return LM_OK;
+}
+
+int lm_adjoint_step(lm_adjoint* a, lm_solver* s, lm_ham* h, int component, int slot, lm_state* psi, lm_state* lam) {
+    if (!a || !s) return LM_ERR_ARG;
+    lm_ctx* ctx = a->ctx;
+    if (!h || !psi || !lam) return set_err(ctx, LM_ERR_ARG, "lm_adjoint_step: null argument");
+    if (!s->valid || s->ham != h) return set_err(ctx, LM_ERR_STATE, "lm_adjoint_step: update the solver with this Hamiltonian first");
+    if (psi->n != a->n || psi->m != a->m || lam->n != a->n || lam->m != a->m || psi->precision != a->precision ||
+        lam->precision != a->precision)
+        return set_err(ctx, LM_ERR_ARG, "lm_adjoint_step: state shapes differ from the adjoint");
+    if (component >= h->fields.n || (component >= 0 && (slot < 0 || slot >= a->nslots)))
+        return set_err(ctx, LM_ERR_ARG, "lm_adjoint_step: bad field component or gradient slot");
+    cudaSetDevice(ctx->device);
+    const Geom& g = h->lat->g;
+    const int K = s->K;
+    int rc = adj_ensure_stack(a, K);
+    if (rc != LM_OK) return rc;
+    const bool f64 = a->precision == LM_C64;
+    const void* hop2 = f64 ? (const void*)s->d_hop2 : (const void*)s->d_hop2f;
+    const void* diag2 = f64 ? (const void*)s->d_diag2 : (const void*)s->d_diag2f;
+    const int64_t ld = psi->ld, M = a->m;
+    dim3 grid((unsigned)((g.N + 255) / 256), (unsigned)(M < 65535 ? M : 65535));
+    auto recur = [&](const void* tp, const void* tpp, const void* lamp, void* out, double alpha, double wre,
+                     double wim) -> cudaError_t {
+        if (f64)
+            adj_recur_kernel<double><<<grid, 256, 0, ctx->stream>>>(g, (const double2*)hop2, (const double*)diag2,
+                                                                    (const double2*)tp, (const double2*)tpp,
+                                                                    (const double2*)lamp, (double2*)out, ld, M, alpha,
+                                                                    wre, wim);
+        else
+            adj_recur_kernel<float><<<grid, 256, 0, ctx->stream>>>(g, (const float2*)hop2, (const float*)diag2,
+                                                                   (const float2*)tp, (const float2*)tpp,
+                                                                   (const float2*)lamp, (float2*)out, ld, M, (float)alpha,
+                                                                   (float)wre, (float)wim);
+        ctx->launches++;
+        return cudaGetLastError();
+    };
+    // T_0 = psi_n (aliased), T_1 = H~ T_0, T_k = 2 H~ T_{k-1} - T_{k-2}  (k < K)
+    a->T[0] = psi->d_data;
+    for (int k = 1; k < K; ++k) {
+        CUDA_TRY(ctx, recur(a->T[(size_t)k - 1], k >= 2 ? a->T[(size_t)k - 2] : nullptr, nullptr, a->T[(size_t)k],
+                            k == 1 ? 0.5 : 1.0, 0.0, 0.0),
+                 "adjoint forward recurrence");
+    }
+    // field derivative table
+    const double2* dhop = nullptr;
+    if (component >= 0) {
+        flux_derivative_kernel<<<(unsigned)((g.N + 255) / 256), 256, 0, ctx->stream>>>(g, h->fields, component, h->d_hop,
+                                                                                       a->d_dhop);
+        ctx->launches++;
+        CUDA_TRY(ctx, cudaGetLastError(), "flux derivative kernel");
+        dhop = a->d_dhop;
+    }
+    // beta_K .. beta_1 with gradient terms; B[k % 3] rotates
+    const int64_t chunk = 64;
+    dim3 ggrid((unsigned)((g.N + 255) / 256), (unsigned)((M + chunk - 1) / chunk));
+    for (int k = K; k >= 1; --k) {
+        const ChebCoef c = s->coef[(size_t)k];
+        const double wre = c.odd ? 0.0 : c.s, wim = c.odd ? c.s : 0.0;  // conj(c_k)
+        void* bk = a->B[k % 3];
+        const void* b1 = k + 1 <= K ? a->B[(k + 1) % 3] : nullptr;
+        const void* b2 = k + 2 <= K ? a->B[(k + 2) % 3] : nullptr;
+        CUDA_TRY(ctx, recur(b1, b2, lam->d_data, bk, 1.0, wre, wim), "adjoint beta recurrence");
+        const double f = (k == 1 ? 1.0 : 2.0) / s->a;
+        if (f64)
+            adj_grad_kernel<double><<<ggrid, 256, 0, ctx->stream>>>(g, dhop, (const double2*)bk, (const double2*)a->T[(size_t)k - 1],
+                                                                    ld, M, chunk, s->phase_re, s->phase_im, f, a->d_gV,
+                                                                    component >= 0 ? a->d_gA + slot : nullptr);
+        else
+            adj_grad_kernel<float><<<ggrid, 256, 0, ctx->stream>>>(g, dhop, (const float2*)bk, (const float2*)a->T[(size_t)k - 1],
+                                                                   ld, M, chunk, s->phase_re, s->phase_im, f, a->d_gV,
+                                                                   component >= 0 ? a->d_gA + slot : nullptr);
+        ctx->launches++;
+        CUDA_TRY(ctx, cudaGetLastError(), "adjoint gradient kernel");
+    }
+    return LM_OK;
+}
+
+int lm_adjoint_gradients(lm_adjoint* a, double* gV, double* gA) {
+    if (!a) return LM_ERR_ARG;
+    lm_ctx* ctx = a->ctx;
+    cudaSetDevice(ctx->device);
+    if (gV)
+        CUDA_TRY(ctx, cudaMemcpyAsync(gV, a->d_gV, sizeof(double) * (size_t)a->n, cudaMemcpyDeviceToHost, ctx->stream),
+                 "download gV");
+    if (gA && a->nslots > 0)
+        CUDA_TRY(ctx, cudaMemcpyAsync(gA, a->d_gA, sizeof(double) * (size_t)a->nslots, cudaMemcpyDeviceToHost, ctx->stream),
+                 "download gA");
+    CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream), "sync");
+    return LM_OK;
+}
+
+int lm_solver_set_bounds(lm_solver* s, double emin, double emax) {
+    if (!s) return LM_ERR_ARG;
+    if (!(emin == 0.0 && emax == 0.0) && !(isfinite(emin) && isfinite(emax) && emax > emin))
+        return set_err(s->ctx, LM_ERR_ARG, "lm_solver_set_bounds: need emin < emax (or 0, 0 for automatic)");
+    s->fixed_bounds = !(emin == 0.0 && emax == 0.0);
+    s->fix_emin = emin;
+    s->fix_emax = emax;
+    s->valid = 0;
+    return LM_OK;
+}
+
+}  // extern "C"

@@ -65,16 +65,6 @@ void bessel_j_all(double x, int kmax, std::vector<double>& out) {
 
 }  // namespace lmgpu
 
-#define CHECK_ARG(ctx, cond, msg) \
-    do {                          \
-        if (!(cond)) return set_err(ctx, LM_ERR_ARG, msg); \
-    } while (0)
-
-#define CUDA_TRY(ctx, expr, what)                              \
-    do {                                                       \
-        int _rc = check_cuda(ctx, (expr), what);               \
-        if (_rc != LM_OK) return _rc;                          \
-    } while (0)
 
 static int dalloc(lm_ctx* ctx, void** p, size_t bytes, const char* what) {
     *p = nullptr;
@@ -760,6 +750,10 @@ int lm_solver_update(lm_solver* s, lm_ham* h, double dt, int force) {
     }
     double emin, emax;
     lm_ham_bounds(h, &emin, &emax);
+    if (s->fixed_bounds) {
+        emin = s->fix_emin;
+        emax = s->fix_emax;
+    }
     const double hw = 0.5 * (emax - emin);
     const double a = std::max(hw * (1.0 + 1e-12) + 1e-300, 1e-12);
     const double b = 0.5 * (emax + emin);

@@ -143,7 +143,21 @@ struct lm_solver {
     float2* d_hop2f = nullptr;  float* d_diag2f = nullptr;
     int64_t tab_n = 0;
     int has_onsite = 0;
+    int fixed_bounds = 0;        // lm_solver_set_bounds: use [fix_emin, fix_emax] instead of Gershgorin
+    double fix_emin = 0.0, fix_emax = 0.0;
 };
+
+// Argument and CUDA-status checks that return the status from the calling C-ABI function.
+#define CHECK_ARG(ctx, cond, msg)                                   \
+    do {                                                            \
+        if (!(cond)) return lmgpu::set_err(ctx, LM_ERR_ARG, msg);   \
+    } while (0)
+
+#define CUDA_TRY(ctx, expr, what)                                   \
+    do {                                                            \
+        int _rc = lmgpu::check_cuda(ctx, (expr), what);             \
+        if (_rc != LM_OK) return _rc;                               \
+    } while (0)
 
 namespace lmgpu {
 

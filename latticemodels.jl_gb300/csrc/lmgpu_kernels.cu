@@ -19,90 +19,6 @@ __device__ __forceinline__ double2 cmul_rn(double2 a, double2 b) {
                         __dadd_rn(__dmul_rn(a.x, b.y), __dmul_rn(a.y, b.x)));
 }
 
-// ------------------------------------------------------------------------------------------
-// Line integrals of the gauge fields, evaluated exactly as written in the reference
-// (src/zoo/magneticfields.jl:15, :31, :72-85, :89-104), without contraction.
-// ------------------------------------------------------------------------------------------
-__device__ double li_pointflux_axial(double flux, double px, double py, double x1, double y1,
-                                     double x2, double y2) {
-    x1 = __dsub_rn(x1, px); y1 = __dsub_rn(y1, py);
-    x2 = __dsub_rn(x2, px); y2 = __dsub_rn(y2, py);
-    const double n1 = sqrt(__dadd_rn(__dmul_rn(x1, x1), __dmul_rn(y1, y1)));
-    const double n2 = sqrt(__dadd_rn(__dmul_rn(x2, x2), __dmul_rn(y2, y2)));
-    if (n1 < 1e-11 || n2 < 1e-11) return 0.0 * flux;
-    const double nnorm = __dmul_rn(n1, n2);
-    const double det = __dsub_rn(__dmul_rn(x1, y2), __dmul_rn(x2, y1));
-    const double dot = __dadd_rn(__dmul_rn(x1, x2), __dmul_rn(y1, y2));
-    const double cosang = __ddiv_rn(__ddiv_rn(dot, nnorm), 1.0 + 1e-11);
-    const double sgn = (det > 0.0) ? 1.0 : ((det < 0.0) ? -1.0 : 0.0);
-    const double angle = __dmul_rn(acos(cosang), sgn);
-    return __ddiv_rn(__dmul_rn(angle, flux), 2.0 * M_PI);
-}
-
-__device__ double li_pointflux_singular(double flux, double px, double py, double x1, double y1,
-                                        double x2, double y2) {
-    x1 = __dsub_rn(x1, px); y1 = __dsub_rn(y1, py);
-    x2 = __dsub_rn(x2, px); y2 = __dsub_rn(y2, py);
-    const double sg = __dsub_rn(x2, x1);
-    if (fabs(sg) < 1e-11) return 0.0 * flux;
-    if (__dmul_rn(x1, x2) > 0.0 || fmax(x1, x2) == 0.0) return 0.0 * flux;
-    const double yint = __ddiv_rn(__dadd_rn(__dmul_rn(-y1, x2), __dmul_rn(y2, x1)), __dsub_rn(x1, x2));
-    if (yint > 0.0) return 0.0 * flux;
-    return __dmul_rn(flux, (sg > 0.0) ? 1.0 : -1.0);
-}
-
-__device__ double line_integral(const Geom& g, const FieldSet& f, double x1, double y1, double x2,
-                                double y2) {
-    double li = 0.0;
-    for (int c = 0; c < f.n; ++c) {
-        const FieldComp fc = f.c[c];
-        const double A = f.amp[c];
-        double v = 0.0;
-        switch (fc.kind) {
-            case LM_FIELD_LANDAU:  // (x1+x2)*(y2-y1)*B/2
-                v = __ddiv_rn(__dmul_rn(__dmul_rn(__dadd_rn(x1, x2), __dsub_rn(y2, y1)), A), 2.0);
-                break;
-            case LM_FIELD_SYMMETRIC:  // (x1*y2 - x2*y1)/2*B
-                v = __dmul_rn(__ddiv_rn(__dsub_rn(__dmul_rn(x1, y2), __dmul_rn(x2, y1)), 2.0), A);
-                break;
-            case LM_FIELD_POINTFLUX_AXIAL:
-            case LM_FIELD_POINTFLUX_SINGULAR:
-                if (fc.replicate) {
-                    // adapt_field: images p - sum_i n_i T_i over CartesianIndex(-1..1)^d,
-                    // first boundary fastest, singular gauge (magneticfields.jl:237-266)
-                    const int nb = (g.per_x ? 1 : 0) + (g.per_y ? 1 : 0);
-                    const int nimg = (nb == 2) ? 9 : 3;
-                    double acc = 0.0;
-                    for (int im = 0; im < nimg; ++im) {
-                        int n0 = im % 3 - 1, n1 = im / 3 - 1;
-                        double rx = 0.0, ry = 0.0;
-                        if (g.per_x && g.per_y) {
-                            rx = -(double)n0 * (double)g.Lx;
-                            ry = -(double)n1 * (double)g.Ly;
-                        } else if (g.per_x) {
-                            rx = -(double)n0 * (double)g.Lx;
-                        } else {
-                            ry = -(double)n0 * (double)g.Ly;
-                        }
-                        const double t = li_pointflux_singular(A, __dadd_rn(fc.px, rx), __dadd_rn(fc.py, ry),
-                                                               x1, y1, x2, y2);
-                        acc = (im == 0) ? t : __dadd_rn(acc, t);
-                    }
-                    v = acc;
-                } else if (fc.kind == LM_FIELD_POINTFLUX_AXIAL) {
-                    v = li_pointflux_axial(A, fc.px, fc.py, x1, y1, x2, y2);
-                } else {
-                    v = li_pointflux_singular(A, fc.px, fc.py, x1, y1, x2, y2);
-                }
-                break;
-            default:
-                v = 0.0;
-        }
-        li = (c == 0) ? v : __dadd_rn(li, v);
-    }
-    return li;
-}
-
 // H[s, s+e] = t1 * f * exp(-2 pi i LI(r_s, r_s + e)) for e = x (dir 0) and y (dir 1);
 // absent bonds store 0 (src/operators/builder.jl:282-285).
 __global__ void assemble_kernel(Geom g, FieldSet f, double t1, double2* __restrict__ hop) {
@@ -127,7 +43,7 @@ __global__ void assemble_kernel(Geom g, FieldSet f, double t1, double2* __restri
                     fac = make_double2(cs, sn);
                 }
             }
-            const double li = (f.n > 0) ? line_integral(g, f, x1, y1, x2, y2) : 0.0;
+            const double li = (f.n > 0) ? field_line_integral(g, f, x1, y1, x2, y2) : 0.0;
             const double theta = __dmul_rn(-2.0 * M_PI, li);
             double sn, cs;
             sincos(theta, &sn, &cs);

@@ -6,6 +6,8 @@ and ``DensityCurrents``.  All compute runs in liblmgpu.so (hand-written sm_103a 
 package only holds the host-side bookkeeping and the ctypes bindings.
 """
 from ._lib import LMError, load as load_library
+from . import adjoint
+from .adjoint import DensityLossAdjoint
 from .batch import Batch
 from .device import Context, default_context
 from .evolution import ChebyshevGPU, Evolution, EvolutionIterator, EvolutionSolver, EvolutionTimestamp
@@ -17,7 +19,7 @@ from .spectrum import densitymatrix, diagonalize
 from .states import DensityMatrix, DeviceState, Ket, KetBlock, Operator
 
 __all__ = [
-    "Batch", "LMError", "load_library", "Context", "default_context",
+    "adjoint", "DensityLossAdjoint", "Batch", "LMError", "load_library", "Context", "default_context",
     "ChebyshevGPU", "Evolution", "EvolutionIterator", "EvolutionSolver", "EvolutionTimestamp",
     "FieldSum", "LandauGauge", "NoField", "PointFlux", "PointFluxes", "SymmetricGauge",
     "Hamiltonian", "tightbinding_hamiltonian", "LatticeValue", "SquareLattice",

@@ -77,6 +77,13 @@ SIGNATURES = {
     "lm_solver_destroy": (_INT, [_P]),
     "lm_solver_update": (_INT, [_P, _P, _D, _INT]),
     "lm_solver_order": (_INT, [_P, _PINT, _PD, _PD]),
+    "lm_solver_set_bounds": (_INT, [_P, _D, _D]),
+    "lm_adjoint_create": (_INT, [_P, _I64, _I64, _INT, _INT, C.POINTER(_P)]),
+    "lm_adjoint_destroy": (_INT, [_P]),
+    "lm_adjoint_reset": (_INT, [_P]),
+    "lm_adjoint_seed": (_INT, [_P, _P, _PD, _P, _PD]),
+    "lm_adjoint_step": (_INT, [_P, _P, _P, _INT, _INT, _P, _P]),
+    "lm_adjoint_gradients": (_INT, [_P, _PD, _PD]),
     "lm_solver_step": (_INT, [_P, _P]),
     "lm_solver_step_noalloc": (_INT, [_P, _P, _I64, _I64, _I64, _INT]),
     "lm_chebyshev_plan": (_INT, [_D, _D, _INT, _PINT, _PD]),

@@ -1,0 +1,129 @@
+"""Adjoint gradients against an FP64 dense-exponential reference (small case) and against
+central finite differences of the FP64 forward (the differentiation workload)."""
+import math
+
+import numpy as np
+import pytest
+
+from oracle import lm_oracle as o
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def lm():
+    import lmgpu
+    lmgpu.default_context()
+    return lmgpu
+
+
+def bump(lat_coords, center, sigma):
+    r2 = ((lat_coords - np.asarray(center)) ** 2).sum(axis=1)
+    return 0.5 + 0.2 * np.exp(-r2 / (2 * sigma ** 2))
+
+
+def oracle_loss(L, psi0, V, B, target, dt, nsteps, spi, point):
+    """Loss of the same evolution with the exact dense exponential (FP64)."""
+    ol = o.SquareLattice(L, L)
+    psi = psi0.astype(np.complex128)
+    for n in range(nsteps):
+        H = o.tightbinding_hamiltonian(ol, field=o.PointFlux(B[n // spi], point), onsite=V)
+        psi = o.expm_exact(H, dt) @ psi
+    rho = (np.abs(psi) ** 2).sum(axis=1)
+    return float(((rho - target) ** 2).sum())
+
+
+def test_adjoint_matches_dense_exponential_gradient(lm):
+    L, M, dt, nsteps, spi = 6, 3, 0.05, 12, 4
+    point = (3.5, 3.5)
+    rng = np.random.default_rng(2)
+    V = rng.uniform(-0.1, 0.1, L * L)
+    B = np.array([0.1, 0.15, 0.05])
+    ol = o.SquareLattice(L, L)
+    H0 = o.tightbinding_hamiltonian(ol, field=o.PointFlux(B[0], point), onsite=V)
+    w, Vec = np.linalg.eigh(H0.toarray())
+    psi0 = Vec[:, :M]
+    target = bump(ol.coords, (2.5, 4.0), 1.5)
+    lat = lm.SquareLattice(L, L)
+    prob = lm.adjoint.DensityLossAdjoint(lat, psi0, target, dt, nsteps, spi, point, precision="c64",
+                                         checkpoint_every=5)
+    loss, gV, gB = prob.loss_and_grad(V, B)
+    assert abs(loss - oracle_loss(L, psi0, V, B, target, dt, nsteps, spi, point)) <= 1e-12 * max(1.0, loss)
+    h = 1e-6
+    ref_V = np.empty(L * L)
+    for i in range(L * L):
+        e = np.zeros(L * L); e[i] = h
+        ref_V[i] = (oracle_loss(L, psi0, V + e, B, target, dt, nsteps, spi, point)
+                    - oracle_loss(L, psi0, V - e, B, target, dt, nsteps, spi, point)) / (2 * h)
+    ref_B = np.empty(len(B))
+    for j in range(len(B)):
+        e = np.zeros(len(B)); e[j] = h
+        ref_B[j] = (oracle_loss(L, psi0, V, B + e, target, dt, nsteps, spi, point)
+                    - oracle_loss(L, psi0, V, B - e, target, dt, nsteps, spi, point)) / (2 * h)
+    scale_V = np.abs(ref_V).max()
+    scale_B = np.abs(ref_B).max()
+    assert np.abs(gV - ref_V).max() <= 1e-6 * scale_V
+    assert np.abs(gB - ref_B).max() <= 1e-6 * scale_B
+    # the FP32 adjoint against the same reference
+    p32 = lm.adjoint.DensityLossAdjoint(lat, psi0, target, dt, nsteps, spi, point, precision="c32",
+                                        checkpoint_every=5)
+    _, gV32, gB32 = p32.loss_and_grad(V, B)
+    assert np.abs(gV32 - ref_V).max() <= 1e-4 * scale_V
+    assert np.abs(gB32 - ref_B).max() <= 1e-4 * scale_B
+
+
+def test_adjoint_torch_function(lm):
+    torch = pytest.importorskip("torch")
+    L, M = 5, 2
+    ol = o.SquareLattice(L, L)
+    w, Vec = np.linalg.eigh(o.tightbinding_hamiltonian(ol).toarray())
+    prob = lm.adjoint.DensityLossAdjoint(lm.SquareLattice(L, L), Vec[:, :M], np.full(L * L, 0.1), 0.05, 6, 3,
+                                         (2.5, 2.5), precision="c64")
+    V = torch.zeros(L * L, dtype=torch.float64, requires_grad=True)
+    B = torch.full((2,), 0.1, dtype=torch.float64, requires_grad=True)
+    loss = lm.adjoint.EvolutionDensityLoss.apply(V, B, prob)
+    loss.backward()
+    _, gV, gB = prob.loss_and_grad(V.detach().numpy(), B.detach().numpy())
+    assert np.allclose(V.grad.numpy(), gV) and np.allclose(B.grad.numpy(), gB)
+
+
+def test_differentiation_workload_fd(lm):
+    """SquareLattice(64,64) open, M = 2048 lowest eigenstates, V ~ U[-0.1,0.1], 50 flux
+    intervals of 8 steps (init 0.1) through (32.5, 32.5), T = 20 (400 steps of 0.05),
+    checkpoint every 20 steps, FP32 forward + adjoint; gradient against FP64 central
+    differences (h = 1e-4) on 32 random parameters."""
+    torch = pytest.importorskip("torch")
+    L, M, dt, nsteps, spi = 64, 2048, 0.05, 400, 8
+    point = (32.5, 32.5)
+    rng = np.random.default_rng(5)
+    V = rng.uniform(-0.1, 0.1, L * L)
+    B = np.full(50, 0.1)
+    ol = o.SquareLattice(L, L)
+    H0 = o.tightbinding_hamiltonian(ol, field=o.PointFlux(B[0], point), onsite=V)
+    Hd = torch.as_tensor(H0.toarray(), device="cuda")
+    w, Vec = torch.linalg.eigh(Hd)
+    psi0 = Vec[:, :M].cpu().numpy()
+    del Hd, Vec
+    c = rng.uniform(20, 44, size=2)
+    target = bump(ol.coords, c, 6.0)
+    lat = lm.SquareLattice(L, L)
+    p32 = lm.adjoint.DensityLossAdjoint(lat, psi0, target, dt, nsteps, spi, point, precision="c32")
+    loss32, gV, gB = p32.loss_and_grad(V, B)
+    p64 = lm.adjoint.DensityLossAdjoint(lat, psi0, target, dt, nsteps, spi, point, precision="c64",
+                                        bounds=p32.bounds)
+    h = 1e-4
+    iv = rng.choice(L * L, size=24, replace=False)
+    ib = rng.choice(50, size=8, replace=False)
+    errs = []
+    for i in iv:
+        e = np.zeros(L * L); e[i] = h
+        fd = (p64.loss(V + e, B) - p64.loss(V - e, B)) / (2 * h)
+        errs.append(abs(gV[i] - fd) / max(abs(fd), 1e-12))
+    for j in ib:
+        e = np.zeros(50); e[j] = h
+        fd = (p64.loss(V, B + e) - p64.loss(V, B - e)) / (2 * h)
+        errs.append(abs(gB[j] - fd) / max(abs(fd), 1e-12))
+    errs = np.array(errs)
+    print(f"differentiation workload: loss {loss32:.6e}, max rel err {errs.max():.3e}, median {np.median(errs):.3e}")
+    assert np.median(errs) <= 1e-5
+    assert errs.max() <= 1e-3
