@@ -49,21 +49,14 @@ def test_adjoint_matches_dense_exponential_gradient(lm):
                                          checkpoint_every=5)
     loss, gV, gB = prob.loss_and_grad(V, B)
     assert abs(loss - oracle_loss(L, psi0, V, B, target, dt, nsteps, spi, point)) <= 1e-12 * max(1.0, loss)
-    h = 1e-6
-    ref_V = np.empty(L * L)
-    for i in range(L * L):
-        e = np.zeros(L * L); e[i] = h
-        ref_V[i] = (oracle_loss(L, psi0, V + e, B, target, dt, nsteps, spi, point)
-                    - oracle_loss(L, psi0, V - e, B, target, dt, nsteps, spi, point)) / (2 * h)
-    ref_B = np.empty(len(B))
-    for j in range(len(B)):
-        e = np.zeros(len(B)); e[j] = h
-        ref_B[j] = (oracle_loss(L, psi0, V, B + e, target, dt, nsteps, spi, point)
-                    - oracle_loss(L, psi0, V, B - e, target, dt, nsteps, spi, point)) / (2 * h)
+    ref_loss, ref_V, ref_B = o.density_loss_gradient_exact(ol, psi0, V, B, target, dt, nsteps, spi, point)
+    assert abs(ref_loss - loss) <= 1e-12 * max(1.0, loss)
     scale_V = np.abs(ref_V).max()
     scale_B = np.abs(ref_B).max()
-    assert np.abs(gV - ref_V).max() <= 1e-6 * scale_V
-    assert np.abs(gB - ref_B).max() <= 1e-6 * scale_B
+    print("dense-exponential reference: max |dV| rel", np.abs(gV - ref_V).max() / scale_V,
+          "max |dB| rel", np.abs(gB - ref_B).max() / scale_B)
+    assert np.abs(gV - ref_V).max() <= 1e-9 * scale_V
+    assert np.abs(gB - ref_B).max() <= 1e-9 * scale_B
     # the FP32 adjoint against the same reference
     p32 = lm.adjoint.DensityLossAdjoint(lat, psi0, target, dt, nsteps, spi, point, precision="c32",
                                         checkpoint_every=5)
