@@ -6,6 +6,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <complex>
 #include <new>
 #include <string>
 #include <vector>
@@ -136,6 +137,23 @@ void make_coefs(const std::vector<double>& J, int K, double sgn, std::vector<Che
         else c.s = -mag * sgn;                  // +i mag = -i (-mag)
         out[(size_t)k] = c;
     }
+}
+ChebLo cheb_lo(double ph_re, double ph_im, double c0, double s1, bool fused) {
+    typedef std::complex<double> cd;
+    const cd ph(ph_re, ph_im);
+    const cd phh((double)(float)ph_re, (double)(float)ph_im);
+    const cd c1(0.0, -s1), c1h(0.0, -(double)(float)s1);
+    const cd a0 = ph * c0;
+    // the T0 coefficient the kernel applies from its FP32 words alone
+    const cd t0 = fused ? cd((double)(float)(ph_re * c0), (double)(float)(ph_im * c0)) : phh * (double)(float)c0;
+    const cd g0 = (a0 - t0) / phh;
+    const cd g1 = (ph * c1 - phh * c1h) / phh;
+    ChebLo lo;
+    lo.g0_re = (float)g0.real();
+    lo.g0_im = (float)g0.imag();
+    lo.g1_re = (float)g1.real();
+    lo.g1_im = (float)g1.imag();
+    return lo;
 }
 }  // namespace lmgpu
 
@@ -819,13 +837,14 @@ static int cheb_apply(lm_solver* s, const Geom& g, int precision, int site_fast,
         *where = 1;
         return LM_OK;
     }
-    CUDA_TRY(ctx, launch_cheb_order(ctx, g, precision, site_fast, conj, CHEB_FIRST, hop2, diag2, S, A, Y, ld, m, c0, coef(1), pr, pi),
+    const ChebLo lo = cheb_lo(pr, pi, c0, coef(1).s, false);
+    CUDA_TRY(ctx, launch_cheb_order(ctx, g, precision, site_fast, conj, CHEB_FIRST, hop2, diag2, S, A, Y, ld, m, c0, coef(1), pr, pi, lo),
              "chebyshev order 1");
     for (int k = 2; k <= K; ++k) {
         const void* tp = (k % 2 == 0) ? A : S;
         void* tq = (k % 2 == 0) ? S : A;
         const int mode = (k == K) ? CHEB_LAST : CHEB_MID;
-        CUDA_TRY(ctx, launch_cheb_order(ctx, g, precision, site_fast, conj, mode, hop2, diag2, tp, tq, Y, ld, m, c0, coef(k), pr, pi),
+        CUDA_TRY(ctx, launch_cheb_order(ctx, g, precision, site_fast, conj, mode, hop2, diag2, tp, tq, Y, ld, m, c0, coef(k), pr, pi, lo),
                  "chebyshev order");
     }
     if (ctx->timing) {

@@ -41,6 +41,7 @@ struct OrderInst {
     int64_t lane_blocks;  // ceil(N / 256)
     double s[kBatchMaxK + 1];
     double ph_re, ph_im;
+    ChebLo lo;  // per-order-form second words (FP32)
 };
 
 struct TransInst {
@@ -82,14 +83,14 @@ __global__ void __launch_bounds__(256) cheb_order_batch_kernel(const OrderInst* 
         const R c0 = (R)D.s[0], cs = (R)D.s[k], pr = (R)D.ph_re, pi = (R)D.ph_im;
         const int64_t g0 = grp * INNER, gs = (int64_t)1 << 62;  // one group per item
         if (k == 1)
-            cheb_order_block<R, CHEB_FIRST, true, false, INNER>(g, hop2, diag2, S, A, Y, D.ld, D.M, c0, cs, 1, pr, pi,
+            cheb_order_block<R, CHEB_FIRST, true, false, INNER>(g, hop2, diag2, S, A, Y, D.ld, D.M, c0, cs, 1, pr, pi, D.lo,
                                                                 lane, g0, gs);
         else if (k < K)
             cheb_order_block<R, CHEB_MID, true, false, INNER>(g, hop2, diag2, (k & 1) ? S : A, (k & 1) ? A : S, Y,
-                                                              D.ld, D.M, c0, cs, k & 1, pr, pi, lane, g0, gs);
+                                                              D.ld, D.M, c0, cs, k & 1, pr, pi, D.lo, lane, g0, gs);
         else
             cheb_order_block<R, CHEB_LAST, true, false, INNER>(g, hop2, diag2, (k & 1) ? S : A, (k & 1) ? A : S, Y,
-                                                               D.ld, D.M, c0, cs, k & 1, pr, pi, lane, g0, gs);
+                                                               D.ld, D.M, c0, cs, k & 1, pr, pi, D.lo, lane, g0, gs);
     }
 }
 
@@ -266,6 +267,7 @@ static int build_tables(lm_batch* b) {
                 for (int k = 0; k <= kBatchMaxK; ++k) o.s[k] = k <= K ? coefs[i][(size_t)k].s : 0.0;
                 o.ph_re = s->phase_re;
                 o.ph_im = s->phase_im;
+                o.lo = cheb_lo(o.ph_re, o.ph_im, o.s[0], o.s[1], false);
             };
             OrderInst& o1 = b->ho1[p][i];
             fill_order(o1, S, A);

@@ -286,7 +286,16 @@ cheb_fused_c32_kernel(FusedInst single, const FusedInst* __restrict__ table, int
                         }
 #pragma unroll
                         for (int j = 0; j < S; ++j) {
-                            if (k & 1) {  // c_k = -i s_k
+                            if (k == 1) {  // y = -i s_1 T1 + g0 T0 + g1 T1 (t1 still holds T0)
+                                const ChebLo lo = D.lo;
+                                const float2 x = t1[kk][j];
+                                const float lx = fmaf(lo.g0_re, x.x, fmaf(-lo.g0_im, x.y,
+                                                 fmaf(lo.g1_re, tk[j].x, -lo.g1_im * tk[j].y)));
+                                const float ly = fmaf(lo.g0_re, x.y, fmaf(lo.g0_im, x.x,
+                                                 fmaf(lo.g1_re, tk[j].y, lo.g1_im * tk[j].x)));
+                                yv[kk][j].x = fmaf(sk, tk[j].y, lx);
+                                yv[kk][j].y = fmaf(-sk, tk[j].x, ly);
+                            } else if (k & 1) {  // c_k = -i s_k
                                 yv[kk][j].x = fmaf(sk, tk[j].y, yv[kk][j].x);
                                 yv[kk][j].y = fmaf(-sk, tk[j].x, yv[kk][j].y);
                             } else {      // c_k = s_k
@@ -304,7 +313,7 @@ cheb_fused_c32_kernel(FusedInst single, const FusedInst* __restrict__ table, int
                 if (k < K) __syncthreads();
             }
 
-            // out = e^{-ib dt} (c_0 x + y): the small terms first, the dominant one last
+            // out = e^{-ib dt} y + a0 x (a0 = e^{-ib dt} c_0): the small terms first, the dominant one last
             const float ph_re = D.ph_re, ph_im = D.ph_im, a0_re = D.a0_re, a0_im = D.a0_im;
 #pragma unroll
             for (int kk = 0; kk < KB; ++kk) {
@@ -353,6 +362,7 @@ void fused_fill_coef(FusedInst& d, int K, const ChebCoef* coef, double ph_re, do
     d.ph_im = (float)ph_im;
     d.a0_re = (float)(ph_re * coef[0].s);
     d.a0_im = (float)(ph_im * coef[0].s);
+    d.lo = cheb_lo(ph_re, ph_im, coef[0].s, coef[1].s, true);
 }
 
 cudaError_t ensure_fused_attr(lm_ctx* ctx, int K) {

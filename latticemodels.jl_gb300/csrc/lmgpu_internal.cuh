@@ -54,6 +54,19 @@ struct ChebCoef {
     int odd;         // parity of k
 };
 
+// Second FP32 words of the scalar constants of one FP32 step.  The FP32 kernels apply
+//   per-order form: out = ph_h (c0_h T0 + c1_h T1 + g0 T0 + g1 T1 + sum_{k>=2} c_k T_k)
+//   fused form:     out = ph_h (c1_h T1 + g0 T0 + g1 T1 + sum_{k>=2} c_k T_k) + a0_h T0
+// with ph_h, c0_h, c1_h, a0_h the FP32 roundings of e^{-ib dt}, c_0, c_1 and e^{-ib dt} c_0;
+// g0 and g1 (complex) restore the FP64 values of the T0 and T1 terms.  Without them the
+// rounding of c_0 scales every step by the same factor 1 + O(1e-8), which compounds: after
+// 400 steps the density is off by ~1e-5.
+struct ChebLo {
+    float g0_re, g0_im, g1_re, g1_im;
+};
+// ph = e^{-ib dt} (after any conjugation), c_0 = c0, c_1 = -i s1; fused selects the form.
+ChebLo cheb_lo(double ph_re, double ph_im, double c0, double s1, bool fused);
+
 // One lattice of a temporally blocked launch: geometry, stencil tables, in/out ket blocks,
 // its first global work item and its Chebyshev coefficients (c_k = s_k or -i s_k by parity).
 struct FusedInst {
@@ -68,6 +81,7 @@ struct FusedInst {
     float s[kFusedMaxK + 1];
     float ph_re, ph_im;   // e^{-ib dt}
     float a0_re, a0_im;   // e^{-ib dt} c_0
+    ChebLo lo;            // fused-form second words
 };
 
 }  // namespace lmgpu
@@ -172,7 +186,7 @@ cudaError_t launch_normalise(lm_ctx* ctx, const Geom& g, const double2* hop, con
 cudaError_t launch_cheb_order(lm_ctx* ctx, const Geom& g, int precision, int site_fast, int conj,
                               int mode, const void* hop2, const void* diag2, const void* tp, void* tq,
                               void* y, int64_t ld, int64_t m, double c0, ChebCoef ck,
-                              double ph_re, double ph_im);
+                              double ph_re, double ph_im, ChebLo lo);
 cudaError_t launch_scale(lm_ctx* ctx, int precision, void* x, int64_t n, int64_t m, int64_t ld,
                          double re, double im);
 cudaError_t launch_localdensity(lm_ctx* ctx, int precision, int kind, const void* x, int64_t n,

@@ -49,7 +49,7 @@ __device__ __forceinline__ Nbr neighbours(const Geom& g, int64_t s) {
 
 // ------------------------------------------------------------------------------------------
 // One order of the Chebyshev recurrence for exp(-i H dt), H~ = (H - b)/a:
-//   FIRST: T1 = H~ T0            -> tq;   y  = c0 T0 + c1 T1
+//   FIRST: T1 = H~ T0            -> tq;   y  = c0 T0 + c1 T1 (+ g0 T0 + g1 T1 in FP32, see ChebLo)
 //   MID  : Tk = 2 H~ T(k-1) - T(k-2) -> tq (in place over T(k-2));  y += ck Tk
 //   LAST : out = phase * (y + cK TK)   -> tq (in place over T(K-2))
 // c_k = s (k even) or -i s (k odd); the tables hold 2H/a and 2(V-b)/a.
@@ -61,7 +61,8 @@ template <typename R, int MODE, bool SITE_FAST, bool CONJ, int INNER>
 __device__ __forceinline__ void cheb_order_block(
     const Geom& g, const typename CT<R>::V* __restrict__ hop2, const R* __restrict__ diag2,
     const typename CT<R>::V* __restrict__ tp, typename CT<R>::V* tq, typename CT<R>::V* y,
-    int64_t ld, int64_t M, R c0, R cs, int odd, R ph_re, R ph_im, int64_t lane, int64_t g_first, int64_t g_stride) {
+    int64_t ld, int64_t M, R c0, R cs, int odd, R ph_re, R ph_im, ChebLo lo, int64_t lane, int64_t g_first,
+    int64_t g_stride) {
     typedef typename CT<R>::V V;
     const int64_t nfast = SITE_FAST ? g.N : M;
     const int64_t nslow = SITE_FAST ? M : g.N;
@@ -120,8 +121,16 @@ __device__ __forceinline__ void cheb_order_block(
                 const V t1 = CT<R>::make(acc.x * R(0.5), acc.y * R(0.5));
                 tq[at(site)] = t1;
                 V yy;
-                yy.x = fma(cs, t1.y, c0 * v0.x);
-                yy.y = fma(-cs, t1.x, c0 * v0.y);
+                if (sizeof(R) == sizeof(float)) {
+                    // second words g0 T0 + g1 T1 first, the dominant c0 T0 last
+                    R lx = fma(R(lo.g0_re), v0.x, fma(R(-lo.g0_im), v0.y, fma(R(lo.g1_re), t1.x, R(-lo.g1_im) * t1.y)));
+                    R ly = fma(R(lo.g0_re), v0.y, fma(R(lo.g0_im), v0.x, fma(R(lo.g1_re), t1.y, R(lo.g1_im) * t1.x)));
+                    yy.x = fma(c0, v0.x, fma(cs, t1.y, lx));
+                    yy.y = fma(c0, v0.y, fma(-cs, t1.x, ly));
+                } else {
+                    yy.x = fma(cs, t1.y, c0 * v0.x);
+                    yy.y = fma(-cs, t1.x, c0 * v0.y);
+                }
                 y[at(site)] = yy;
             } else {
                 V yy = y[at(site)];

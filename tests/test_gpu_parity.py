@@ -304,3 +304,40 @@ def test_fused_c32_step(lm, Lx, Ly, per, fspec, M, dt):
     assert rel(outs[True], Yo) <= 2e-6
     assert rel(outs[False], Yo) <= 2e-6
     assert rel(outs[True], outs[False]) <= 2e-6
+
+
+@pytest.mark.parametrize("fused", [True, False])
+def test_fp32_long_run_keeps_norm(lm, fused):
+    """400 FP32 steps with no renormalisation.  The step carries second FP32 words for its
+    scalar constants (e^{-ib dt} c_0, e^{-ib dt}, c_1), so their rounding does not compound;
+    without them the norms drift by ~1e-5 here.  The on-site offset 0.7 makes e^{-ib dt} a
+    full complex phase."""
+    L, M, dt, nsteps = 64, 16, 0.05, 400
+    ol, ll = pair(lm, L, L)
+    rng = np.random.default_rng(21)
+    V = rng.uniform(-0.1, 0.1, L * L) + 0.7
+    Hl = lm.tightbinding_hamiltonian(ll, V, field=lm.PointFlux(0.1, (32.5, 32.5)))
+    X = o.random_kets(ol.N, M, 22)
+    X /= np.linalg.norm(X, axis=0)
+    ctx = lm.default_context()
+    try:
+        ctx.set_fused(fused)
+        s32, s64 = lm.ChebyshevGPU(tol=1e-9), lm.ChebyshevGPU(tol=1e-13)
+        st32 = lm.KetBlock(ll, X, precision="c32")
+        st64 = lm.KetBlock(ll, X, precision="c64")
+        s32.update_solver(Hl, dt)
+        s64.update_solver(Hl, dt)
+        for _ in range(nsteps):
+            s32.step(st32)
+            s64.step(st64)
+    finally:
+        ctx.set_fused(True)
+    n32 = st32.norms()
+    n64 = st64.norms()
+    rho32 = lm.localdensity(st32).values
+    rho64 = lm.localdensity(st64).values
+    print(f"fused={fused}: max |norm-1| c32 {np.abs(n32 - 1).max():.2e} c64 {np.abs(n64 - 1).max():.2e}, "
+          f"density rel {rel(rho32, rho64):.2e}")
+    assert np.abs(n64 - 1).max() <= 1e-12
+    assert np.abs(n32 - 1).max() <= 5e-7
+    assert rel(rho32, rho64) <= 1e-6
