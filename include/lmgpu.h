@@ -231,6 +231,27 @@ int lm_bond_currents(lm_ham *ham, lm_state *st, double *out);
 /* tr(P) = sum of the local densities, FP64 (particle number). */
 int lm_trace(lm_state *st, double *out);
 
+/* ---- readout ring (device side of TimeSequence(f, ev(times)), src/timesequence.jl:41-43) -- */
+/* Per-moment readouts computed into the slots of a device ring and downloaded asynchronously
+ * into pinned host memory: pushing never waits for the device, so an evolution loop that
+ * records every step keeps the GPU busy.  Entry s lives in slot s % nslots; its host copy is
+ * valid from lm_ring_wait(s) until entry s + nslots is pushed.  Extension of the reference:
+ * it has no asynchronous readout. */
+typedef struct lm_ring lm_ring;
+int lm_ring_create(lm_ctx *ctx, int nslots, int64_t len, lm_ring **out);
+int lm_ring_destroy(lm_ring *r);
+/* localdensity(state) at time t (src/operators/latticeutils.jl:41-45); *seq = entry number. */
+int lm_ring_push_localdensity(lm_ring *r, lm_state *st, double t, int64_t *seq);
+/* DensityCurrents(ham, state) on every bond (src/zoo/currents.jl:92-102) at time t. */
+int lm_ring_push_currents(lm_ring *r, lm_ham *ham, lm_state *st, double t, int64_t *seq);
+/* *ready = 1 when entry seq has reached host memory (LM_ERR_ARG once it is overwritten). */
+int lm_ring_ready(lm_ring *r, int64_t seq, int *ready);
+/* Waits for entry seq; copies it to out (if non-null), returns the pinned view, the number
+ * of values and the time stamp (each optional). */
+int lm_ring_wait(lm_ring *r, int64_t seq, double *out, const double **view, int64_t *n, double *t);
+/* Sequence number of the next entry. */
+int lm_ring_head(const lm_ring *r, int64_t *head);
+
 #ifdef __cplusplus
 }
 #endif

@@ -383,6 +383,10 @@ int lm_ham_destroy(lm_ham* h) {
     cudaStreamSynchronize(h->ctx->stream);
     if (h->d_hop) cudaFree(h->d_hop);
     if (h->d_onsite) cudaFree(h->d_onsite);
+    for (int j = 0; j < 2; ++j) {
+        if (h->h_stage[j]) cudaFreeHost(h->h_stage[j]);
+        if (h->stage_ev[j]) cudaEventDestroy(h->stage_ev[j]);
+    }
     delete h;
     return LM_OK;
 }
@@ -423,18 +427,32 @@ int lm_ham_set_onsite(lm_ham* h, const double* V) {
         h->assembled = 0;
         return LM_OK;
     }
-    double vmin = V[0], vmax = V[0];
-    for (int64_t i = 0; i < N; ++i) {
-        if (!isfinite(V[i])) return set_err(ctx, LM_ERR_NONFINITE, "lm_ham_set_onsite: non-finite on-site value");
-        vmin = std::min(vmin, V[i]);
-        vmax = std::max(vmax, V[i]);
-    }
     if (!h->d_onsite) {
         int rc = dalloc(ctx, (void**)&h->d_onsite, sizeof(double) * (size_t)N, "on-site table");
         if (rc != LM_OK) return rc;
     }
-    CUDA_TRY(ctx, cudaMemcpyAsync(h->d_onsite, V, sizeof(double) * (size_t)N, cudaMemcpyHostToDevice, ctx->stream),
+    // two pinned staging slots; a slot is rewritten only after its previous copy has run
+    const int j = h->stage_next;
+    if (!h->h_stage[j]) {
+        CUDA_TRY(ctx, cudaHostAlloc((void**)&h->h_stage[j], sizeof(double) * (size_t)N, cudaHostAllocDefault),
+                 "pinned on-site staging");
+        CUDA_TRY(ctx, cudaEventCreateWithFlags(&h->stage_ev[j], cudaEventDisableTiming), "cudaEventCreate");
+    } else {
+        CUDA_TRY(ctx, cudaEventSynchronize(h->stage_ev[j]), "on-site staging wait");
+    }
+    double* st = h->h_stage[j];
+    double vmin = V[0], vmax = V[0];
+    for (int64_t i = 0; i < N; ++i) {
+        const double v = V[i];
+        if (!isfinite(v)) return set_err(ctx, LM_ERR_NONFINITE, "lm_ham_set_onsite: non-finite on-site value");
+        vmin = std::min(vmin, v);
+        vmax = std::max(vmax, v);
+        st[i] = v;
+    }
+    CUDA_TRY(ctx, cudaMemcpyAsync(h->d_onsite, st, sizeof(double) * (size_t)N, cudaMemcpyHostToDevice, ctx->stream),
              "upload on-site");
+    CUDA_TRY(ctx, cudaEventRecord(h->stage_ev[j], ctx->stream), "cudaEventRecord");
+    h->stage_next = j ^ 1;
     h->vmin = vmin;
     h->vmax = vmax;
     h->assembled = 0;

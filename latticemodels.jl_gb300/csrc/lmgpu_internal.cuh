@@ -124,6 +124,11 @@ struct lm_ham {
     uint64_t version = 0;           // bumps on every assembly
     int assembled = 0;
     std::vector<double> last_amp;
+    // pinned staging of the on-site upload: the caller's V is copied here during the call, so
+    // the asynchronous copy never reads the caller's memory after lm_ham_set_onsite returns
+    double* h_stage[2] = {nullptr, nullptr};
+    cudaEvent_t stage_ev[2] = {nullptr, nullptr};
+    int stage_next = 0;
 };
 
 struct lm_state {

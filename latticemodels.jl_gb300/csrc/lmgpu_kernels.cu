@@ -199,33 +199,116 @@ cudaError_t launch_convert(lm_ctx* ctx, int to_precision, const void* src, void*
 }
 
 // ------------------------------------------------------------------------------------------
-// Readouts (FP64 accumulation)
+// Readouts.  Sums over kets run in FP64 for c64 states; for c32 states they run in
+// double-float FP32 (an unevaluated hi + lo pair, products split exactly by an FMA and added by
+// Knuth's TwoSum), which carries ~48 significant bits at FP32 issue rates -- GB300 runs FP64
+// at 1/64 of its FP32 rate, so an FP64 accumulator per element would bound these kernels.
+// Every sum is over a fixed order (no atomics): the readouts are bit-reproducible.
 // ------------------------------------------------------------------------------------------
-// localdensity: rho_s = sum_m w_m |psi_sm|^2 (kets) or Re P[s,s] (density matrix).
+template <typename R> struct Acc;
+template <> struct Acc<double> {
+    double v = 0.0;
+    __device__ __forceinline__ void add_prod(double a, double b) { v = fma(a, b, v); }
+    __device__ __forceinline__ double get() const { return v; }
+};
+template <> struct Acc<float> {
+    float hi = 0.f, lo = 0.f;
+    __device__ __forceinline__ void add_prod(float a, float b) {
+        const float p = __fmul_rn(a, b);
+        const float pe = __fmaf_rn(a, b, -p);  // a*b = p + pe exactly
+        const float s = __fadd_rn(hi, p);      // TwoSum(hi, p) = s + e exactly
+        const float bp = __fsub_rn(s, hi);
+        const float e = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bp)), __fsub_rn(p, bp));
+        hi = s;
+        lo = __fadd_rn(lo, __fadd_rn(e, pe));
+    }
+    __device__ __forceinline__ double get() const { return (double)hi + (double)lo; }
+};
+
+constexpr int kReadWarps = 8;  // warps of a readout block; they split the kets
+
+// localdensity of a ket block: rho_s = sum_k w_k |psi_sk|^2.  A block owns 32*VEC consecutive
+// sites (lane -> VEC sites, one 16-byte load per ket for c32 with VEC = 2); its 8 warps take
+// kets k = warp, warp + 8, ...; the 8 partial sums are added in warp order.
+template <typename R, int VEC, bool WEIGHTED>
+__global__ void __launch_bounds__(32 * kReadWarps) localdensity_kets_kernel(
+    const typename CT<R>::V* __restrict__ x, int64_t n, int64_t m, int64_t ld, const double* __restrict__ w,
+    double* __restrict__ out) {
+    typedef typename CT<R>::V V;
+    __shared__ double red[kReadWarps][32 * VEC];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int64_t s0 = (int64_t)blockIdx.x * (32 * VEC) + (int64_t)lane * VEC;
+    Acc<R> acc[VEC];
+    double accw[VEC];
+#pragma unroll
+    for (int j = 0; j < VEC; ++j) accw[j] = 0.0;
+    if (s0 < n) {
+#pragma unroll 4
+        for (int64_t k = warp; k < m; k += kReadWarps) {
+            V v[VEC];
+            if (VEC == 2) {
+                const float4 q = __ldg(reinterpret_cast<const float4*>(x + k * ld + s0));
+                v[0] = CT<R>::make(q.x, q.y);
+                v[VEC - 1] = CT<R>::make(q.z, q.w);
+            } else {
+                v[0] = x[k * ld + s0];
+            }
+#pragma unroll
+            for (int j = 0; j < VEC; ++j) {
+                if (WEIGHTED) {
+                    accw[j] = fma(w[k], (double)v[j].x * (double)v[j].x + (double)v[j].y * (double)v[j].y, accw[j]);
+                } else {
+                    acc[j].add_prod(v[j].x, v[j].x);
+                    acc[j].add_prod(v[j].y, v[j].y);
+                }
+            }
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < VEC; ++j) red[warp][lane * VEC + j] = WEIGHTED ? accw[j] : acc[j].get();
+    __syncthreads();
+    if (threadIdx.x < 32 * VEC) {
+        const int64_t s = (int64_t)blockIdx.x * (32 * VEC) + threadIdx.x;
+        if (s < n) {
+            double t = 0.0;
+#pragma unroll
+            for (int q = 0; q < kReadWarps; ++q) t += red[q][threadIdx.x];
+            out[s] = t;
+        }
+    }
+}
+
+// localdensity of a density matrix: Re P[s,s].
 template <typename R>
-__global__ void localdensity_kernel(int kind, const typename CT<R>::V* __restrict__ x, int64_t n, int64_t m,
-                                    int64_t ld, const double* __restrict__ w, double* __restrict__ out) {
+__global__ void localdensity_dm_kernel(const typename CT<R>::V* __restrict__ x, int64_t n, int64_t ld,
+                                       double* __restrict__ out) {
     const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= n) return;
-    if (kind == LM_DENSITY) {
-        out[s] = (double)x[s * ld + s].x;
-        return;
-    }
-    double acc = 0.0;
-    for (int64_t k = 0; k < m; ++k) {
-        const typename CT<R>::V v = x[k * ld + s];
-        const double p = (double)v.x * (double)v.x + (double)v.y * (double)v.y;
-        acc += w ? w[k] * p : p;
-    }
-    out[s] = acc;
+    if (s < n) out[s] = (double)x[s * ld + s].x;
+}
+
+template <typename R, int VEC>
+static void launch_ld_kets(lm_ctx* ctx, const void* x, int64_t n, int64_t m, int64_t ld, const double* w,
+                           double* out) {
+    typedef typename CT<R>::V V;
+    const unsigned blocks = (unsigned)((n + 32 * VEC - 1) / (32 * VEC));
+    if (w) localdensity_kets_kernel<R, VEC, true><<<blocks, 32 * kReadWarps, 0, ctx->stream>>>((const V*)x, n, m, ld, w, out);
+    else localdensity_kets_kernel<R, VEC, false><<<blocks, 32 * kReadWarps, 0, ctx->stream>>>((const V*)x, n, m, ld, w, out);
 }
 
 cudaError_t launch_localdensity(lm_ctx* ctx, int precision, int kind, const void* x, int64_t n, int64_t m,
                                 int64_t ld, const double* w, double* out) {
-    const int thr = 128;
-    const unsigned blocks = (unsigned)((n + thr - 1) / thr);
-    if (precision == LM_C64) localdensity_kernel<double><<<blocks, thr, 0, ctx->stream>>>(kind, (const double2*)x, n, m, ld, w, out);
-    else localdensity_kernel<float><<<blocks, thr, 0, ctx->stream>>>(kind, (const float2*)x, n, m, ld, w, out);
+    if (n <= 0) return cudaSuccess;
+    if (kind == LM_DENSITY) {
+        const unsigned blocks = (unsigned)((n + 127) / 128);
+        if (precision == LM_C64) localdensity_dm_kernel<double><<<blocks, 128, 0, ctx->stream>>>((const double2*)x, n, ld, out);
+        else localdensity_dm_kernel<float><<<blocks, 128, 0, ctx->stream>>>((const float2*)x, n, ld, out);
+    } else if (precision == LM_C64) {
+        launch_ld_kets<double, 1>(ctx, x, n, m, ld, w, out);
+    } else if (n % 2 == 0 && ld % 2 == 0 && ((uintptr_t)x & 15) == 0) {
+        launch_ld_kets<float, 2>(ctx, x, n, m, ld, w, out);  // 16-byte loads of site pairs
+    } else {
+        launch_ld_kets<float, 1>(ctx, x, n, m, ld, w, out);
+    }
     ctx->launches++;
     return cudaGetLastError();
 }
@@ -233,87 +316,155 @@ cudaError_t launch_localdensity(lm_ctx* ctx, int precision, int kind, const void
 // Bond currents J = 2 Im(H[i,j] P[j,i]) for the +x and +y bond of every site, written in the
 // reference's bond order (all +x bonds in source order, then all +y bonds).  H[i,j] is the
 // accumulated matrix entry: on a 2-site periodic axis the reverse bond adds conj(H[j,i]).
+__device__ __forceinline__ void bond_write(const Geom& g, const double2* __restrict__ hop, int64_t s, int dir,
+                                           const Nbr& nb, double pr, double pi, double* __restrict__ out) {
+    const int64_t j = dir == 0 ? nb.xp : nb.yp;
+    const int64_t jm = dir == 0 ? nb.xm : nb.ym;
+    double2 h = hop[dir * g.N + s];
+    if (j == jm) {  // two-site periodic axis: both bonds join s and j
+        const double2 r = hop[dir * g.N + j];
+        h.x += r.x;
+        h.y -= r.y;
+    }
+    const double J = 2.0 * (h.x * pi + h.y * pr);  // Im(h * p)
+    const int64_t xi = s / g.Ly, yi = s - xi * g.Ly;
+    const int64_t nbx = g.per_x ? g.N : (g.Lx - 1) * g.Ly;
+    out[dir == 0 ? s : nbx + (g.per_y ? s : xi * (g.Ly - 1) + yi)] = J;
+}
+
+// Ket blocks: P[j,s] = sum_k w_k psi_jk conj(psi_sk).  A block owns 32 consecutive sites (one
+// per lane); its 8 warps split the kets; partial sums are added in warp order.
+template <typename R, bool WEIGHTED>
+__global__ void __launch_bounds__(32 * kReadWarps) bond_currents_kets_kernel(
+    Geom g, const double2* __restrict__ hop, const typename CT<R>::V* __restrict__ x, int64_t m, int64_t ld,
+    const double* __restrict__ w, double* __restrict__ out) {
+    typedef typename CT<R>::V V;
+    __shared__ double red[kReadWarps][4][32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int64_t s = (int64_t)blockIdx.x * 32 + lane;
+    Nbr nb;
+    Acc<R> a[4];  // (re, im) of the +x bond, then of the +y bond
+    double aw[4] = {0.0, 0.0, 0.0, 0.0};
+    if (s < g.N) {
+        nb = neighbours(g, s);
+        // absent bonds read the site itself (always in bounds) and are not written
+        const int64_t jx = nb.hxp ? nb.xp : s, jy = nb.hyp ? nb.yp : s;
+        for (int64_t k = warp; k < m; k += kReadWarps) {
+            const V b = x[k * ld + s];
+            const V cx = x[k * ld + jx], cy = x[k * ld + jy];  // c * conj(b)
+            if (WEIGHTED) {
+                const double wk = w[k];
+                aw[0] += wk * ((double)cx.x * (double)b.x + (double)cx.y * (double)b.y);
+                aw[1] += wk * ((double)cx.y * (double)b.x - (double)cx.x * (double)b.y);
+                aw[2] += wk * ((double)cy.x * (double)b.x + (double)cy.y * (double)b.y);
+                aw[3] += wk * ((double)cy.y * (double)b.x - (double)cy.x * (double)b.y);
+            } else {
+                a[0].add_prod(cx.x, b.x);
+                a[0].add_prod(cx.y, b.y);
+                a[1].add_prod(cx.y, b.x);
+                a[1].add_prod(-cx.x, b.y);
+                a[2].add_prod(cy.x, b.x);
+                a[2].add_prod(cy.y, b.y);
+                a[3].add_prod(cy.y, b.x);
+                a[3].add_prod(-cy.x, b.y);
+            }
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q) red[warp][q][lane] = WEIGHTED ? aw[q] : a[q].get();
+    __syncthreads();
+    if (warp == 0 && s < g.N) {
+        double v[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            double t = 0.0;
+            for (int r = 0; r < kReadWarps; ++r) t += red[r][q][lane];
+            v[q] = t;
+        }
+        if (nb.hxp) bond_write(g, hop, s, 0, nb, v[0], v[1], out);
+        if (nb.hyp) bond_write(g, hop, s, 1, nb, v[2], v[3], out);
+    }
+}
+
+// Density matrices: P[j,s] read directly.
 template <typename R>
-__global__ void bond_currents_kernel(Geom g, int kind, const double2* __restrict__ hop,
-                                     const typename CT<R>::V* __restrict__ x, int64_t m, int64_t ld,
-                                     const double* __restrict__ w, double* __restrict__ out) {
+__global__ void bond_currents_dm_kernel(Geom g, const double2* __restrict__ hop, const typename CT<R>::V* __restrict__ x,
+                                        int64_t ld, double* __restrict__ out) {
     const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= g.N) return;
     const Nbr nb = neighbours(g, s);
-    const int64_t xi = s / g.Ly, yi = s - xi * g.Ly;
-    const int64_t nbx = g.per_x ? g.N : (g.Lx - 1) * g.Ly;
 #pragma unroll
     for (int dir = 0; dir < 2; ++dir) {
-        const bool has = dir == 0 ? nb.hxp : nb.hyp;
-        if (!has) continue;
-        const int64_t j = dir == 0 ? nb.xp : nb.yp;
-        const int64_t jm = dir == 0 ? nb.xm : nb.ym;
-        double2 h = hop[dir * g.N + s];
-        if (j == jm) {  // two-site periodic axis: both bonds join s and j
-            const double2 r = hop[dir * g.N + j];
-            h.x += r.x;
-            h.y -= r.y;
-        }
-        double pr = 0.0, pi = 0.0;  // P[j, s]
-        if (kind == LM_DENSITY) {
-            const typename CT<R>::V v = x[s * ld + j];
-            pr = v.x; pi = v.y;
-        } else {
-            for (int64_t k = 0; k < m; ++k) {
-                const typename CT<R>::V a = x[k * ld + j], b = x[k * ld + s];  // a * conj(b)
-                const double re = (double)a.x * (double)b.x + (double)a.y * (double)b.y;
-                const double im = (double)a.y * (double)b.x - (double)a.x * (double)b.y;
-                const double ww = w ? w[k] : 1.0;
-                pr += ww * re;
-                pi += ww * im;
-            }
-        }
-        const double J = 2.0 * (h.x * pi + h.y * pr);  // Im(h * p)
-        int64_t bidx;
-        if (dir == 0) bidx = s;
-        else bidx = nbx + (g.per_y ? s : xi * (g.Ly - 1) + yi);
-        out[bidx] = J;
+        if (!(dir == 0 ? nb.hxp : nb.hyp)) continue;
+        const typename CT<R>::V v = x[s * ld + (dir == 0 ? nb.xp : nb.yp)];
+        bond_write(g, hop, s, dir, nb, (double)v.x, (double)v.y, out);
     }
 }
 
 cudaError_t launch_bond_currents(lm_ctx* ctx, const Geom& g, int precision, int kind, const double2* hop,
                                  const void* x, int64_t m, int64_t ld, const double* w, double* out) {
-    const int thr = 128;
-    const unsigned blocks = (unsigned)((g.N + thr - 1) / thr);
-    if (precision == LM_C64)
-        bond_currents_kernel<double><<<blocks, thr, 0, ctx->stream>>>(g, kind, hop, (const double2*)x, m, ld, w, out);
-    else
-        bond_currents_kernel<float><<<blocks, thr, 0, ctx->stream>>>(g, kind, hop, (const float2*)x, m, ld, w, out);
+    if (g.N <= 0) return cudaSuccess;
+    if (kind == LM_DENSITY) {
+        const unsigned blocks = (unsigned)((g.N + 127) / 128);
+        if (precision == LM_C64) bond_currents_dm_kernel<double><<<blocks, 128, 0, ctx->stream>>>(g, hop, (const double2*)x, ld, out);
+        else bond_currents_dm_kernel<float><<<blocks, 128, 0, ctx->stream>>>(g, hop, (const float2*)x, ld, out);
+    } else {
+        const unsigned blocks = (unsigned)((g.N + 31) / 32);
+        const int thr = 32 * kReadWarps;
+        if (precision == LM_C64) {
+            if (w) bond_currents_kets_kernel<double, true><<<blocks, thr, 0, ctx->stream>>>(g, hop, (const double2*)x, m, ld, w, out);
+            else bond_currents_kets_kernel<double, false><<<blocks, thr, 0, ctx->stream>>>(g, hop, (const double2*)x, m, ld, w, out);
+        } else {
+            if (w) bond_currents_kets_kernel<float, true><<<blocks, thr, 0, ctx->stream>>>(g, hop, (const float2*)x, m, ld, w, out);
+            else bond_currents_kets_kernel<float, false><<<blocks, thr, 0, ctx->stream>>>(g, hop, (const float2*)x, m, ld, w, out);
+        }
+    }
     ctx->launches++;
     return cudaGetLastError();
 }
 
-// Per-column FP64 norms: one block per column.
-template <typename R>
-__global__ void column_norms_kernel(const typename CT<R>::V* __restrict__ x, int64_t n, int64_t ld,
-                                    double* __restrict__ out) {
-    __shared__ double red[32];
+// Per-column norms: one block of 512 threads per column, fixed-order tree reduction.
+template <typename R, int VEC>
+__global__ void __launch_bounds__(512) column_norms_kernel(const typename CT<R>::V* __restrict__ x, int64_t n,
+                                                           int64_t ld, double* __restrict__ out) {
+    typedef typename CT<R>::V V;
+    __shared__ double red[16];
     const int64_t k = blockIdx.x;
-    double acc = 0.0;
-    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
-        const typename CT<R>::V v = x[k * ld + i];
-        acc += (double)v.x * (double)v.x + (double)v.y * (double)v.y;
+    Acc<R> acc;
+    const V* col = x + k * ld;
+    for (int64_t i = (int64_t)threadIdx.x * VEC; i < n; i += (int64_t)blockDim.x * VEC) {
+        if (VEC == 2) {
+            const float4 q = __ldg(reinterpret_cast<const float4*>(col + i));
+            acc.add_prod(q.x, q.x);
+            acc.add_prod(q.y, q.y);
+            acc.add_prod(q.z, q.z);
+            acc.add_prod(q.w, q.w);
+        } else {
+            const V v = col[i];
+            acc.add_prod(v.x, v.x);
+            acc.add_prod(v.y, v.y);
+        }
     }
-    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
-    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+    double t = acc.get();
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = t;
     __syncthreads();
     if (threadIdx.x < 32) {
-        acc = (threadIdx.x < (blockDim.x >> 5)) ? red[threadIdx.x] : 0.0;
-        for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
-        if (threadIdx.x == 0) out[k] = sqrt(acc);
+        t = (threadIdx.x < (blockDim.x >> 5)) ? red[threadIdx.x] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+        if (threadIdx.x == 0) out[k] = sqrt(t);
     }
 }
 
 cudaError_t launch_column_norms(lm_ctx* ctx, int precision, const void* x, int64_t n, int64_t m, int64_t ld,
                                 double* out) {
     if (m <= 0) return cudaSuccess;
-    if (precision == LM_C64) column_norms_kernel<double><<<(unsigned)m, 256, 0, ctx->stream>>>((const double2*)x, n, ld, out);
-    else column_norms_kernel<float><<<(unsigned)m, 256, 0, ctx->stream>>>((const float2*)x, n, ld, out);
+    if (precision == LM_C64)
+        column_norms_kernel<double, 1><<<(unsigned)m, 512, 0, ctx->stream>>>((const double2*)x, n, ld, out);
+    else if (n % 2 == 0 && ld % 2 == 0 && ((uintptr_t)x & 15) == 0)
+        column_norms_kernel<float, 2><<<(unsigned)m, 512, 0, ctx->stream>>>((const float2*)x, n, ld, out);
+    else
+        column_norms_kernel<float, 1><<<(unsigned)m, 512, 0, ctx->stream>>>((const float2*)x, n, ld, out);
     ctx->launches++;
     return cudaGetLastError();
 }

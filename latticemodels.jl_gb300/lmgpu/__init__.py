@@ -17,6 +17,8 @@ from .lattice import LatticeValue, SquareLattice
 from .observables import Currents, DensityCurrents, localdensity
 from .spectrum import densitymatrix, diagonalize
 from .states import DensityMatrix, DeviceState, Ket, KetBlock, Operator
+from .timesequence import (ReadoutRing, TimeSequence, differentiate, integrate, moment_currents,
+                           moment_density)
 
 __all__ = [
     "adjoint", "DensityLossAdjoint", "Batch", "LMError", "load_library", "Context", "default_context",
@@ -25,4 +27,5 @@ __all__ = [
     "Hamiltonian", "tightbinding_hamiltonian", "LatticeValue", "SquareLattice",
     "Currents", "DensityCurrents", "localdensity", "densitymatrix", "diagonalize",
     "DensityMatrix", "DeviceState", "Ket", "KetBlock", "Operator",
+    "ReadoutRing", "TimeSequence", "differentiate", "integrate", "moment_currents", "moment_density",
 ]

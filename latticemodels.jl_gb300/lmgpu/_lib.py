@@ -99,6 +99,13 @@ SIGNATURES = {
     "lm_localdensity": (_INT, [_P, _PD]),
     "lm_bond_currents": (_INT, [_P, _P, _PD]),
     "lm_trace": (_INT, [_P, _PD]),
+    "lm_ring_create": (_INT, [_P, _INT, _I64, C.POINTER(_P)]),
+    "lm_ring_destroy": (_INT, [_P]),
+    "lm_ring_push_localdensity": (_INT, [_P, _P, _D, _PI64]),
+    "lm_ring_push_currents": (_INT, [_P, _P, _P, _D, _PI64]),
+    "lm_ring_ready": (_INT, [_P, _I64, _PINT]),
+    "lm_ring_wait": (_INT, [_P, _I64, _PD, C.POINTER(_PD), _PI64, _PD]),
+    "lm_ring_head": (_INT, [_P, _PI64]),
 }
 
 

@@ -1,0 +1,65 @@
+"""Readout kernels (localdensity, bond currents, column norms, trace) against numpy FP64 sums
+of the same device data: c64 data to 1e-13, c32 data (double-float accumulation) to 1e-12."""
+import numpy as np
+import pytest
+
+from oracle import lm_oracle as o
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def lm():
+    import lmgpu
+    lmgpu.default_context()
+    return lmgpu
+
+
+CASES = [(16, 16, (True, True)), (7, 9, (False, False)), (33, 5, (True, False)), (2, 6, (True, True))]
+
+
+@pytest.mark.parametrize("Lx,Ly,per", CASES)
+@pytest.mark.parametrize("precision", ["c64", "c32"])
+@pytest.mark.parametrize("weighted", [False, True])
+def test_ket_block_readouts(lm, Lx, Ly, per, precision, weighted):
+    ol = o.SquareLattice(Lx, Ly, periodic=per)
+    b = {"axis1": per[0], "axis2": per[1]}
+    ll = lm.SquareLattice(Lx, Ly, boundaries={k: v for k, v in b.items() if v})
+    V = o.anderson_disorder(ol.N, 1.0, 5)
+    Ho = o.tightbinding_hamiltonian(ol, field=o.LandauGauge(0.05), onsite=V)
+    Hl = lm.tightbinding_hamiltonian(ll, V, field=lm.LandauGauge(0.05))
+    M = 37
+    X = o.random_kets(ol.N, M, 6)
+    st = lm.KetBlock(ll, X, precision=precision)
+    Xd = st.to_numpy().astype(np.complex128)  # exactly the device data
+    w = np.random.default_rng(7).uniform(0.1, 2.0, M) if weighted else None
+    if weighted:
+        st.set_weights(w)
+    ww = w if weighted else np.ones(M)
+    rho = (np.abs(Xd) ** 2 * ww).sum(axis=1)
+    tol = 1e-13 if precision == "c64" else 1e-12
+    got = lm.localdensity(st).values
+    assert np.abs(got - rho).max() <= tol * np.abs(rho).max()
+    src, dst = zip(*[(bd.src, bd.dst) for bd in o.nn_bonds(ol)])
+    J = o.bond_currents(Ho, Xd, np.asarray(src), np.asarray(dst), weights=ww)
+    Jg = lm.DensityCurrents(Hl, st).bond_values()
+    assert np.abs(Jg - J).max() <= tol * max(np.abs(J).max(), 1e-300) * 10
+    nrm = np.linalg.norm(Xd, axis=0)
+    assert np.abs(st.norms() - nrm).max() <= tol * nrm.max()
+
+
+@pytest.mark.parametrize("precision", ["c64", "c32"])
+def test_density_matrix_readouts(lm, precision):
+    L = 9
+    ol = o.SquareLattice(L, L)
+    ll = lm.SquareLattice(L, L)
+    Ho = o.tightbinding_hamiltonian(ol, field=o.PointFlux(0.2, (4.5, 4.5)))
+    Hl = lm.tightbinding_hamiltonian(ll, field=lm.PointFlux(0.2, (4.5, 4.5)))
+    P0, _, _ = o.densitymatrix(Ho, mu=0.0)
+    st = lm.DensityMatrix(ll, P0, precision=precision)
+    Pd = st.to_numpy().astype(np.complex128)
+    assert np.array_equal(lm.localdensity(st).values, Pd.diagonal().real)
+    src, dst = zip(*[(bd.src, bd.dst) for bd in o.nn_bonds(ol)])
+    J = o.bond_currents(Ho, Pd, np.asarray(src), np.asarray(dst), is_density=True)
+    assert np.abs(lm.DensityCurrents(Hl, st).bond_values() - J).max() <= 1e-14
+    assert abs(st.trace() - Pd.diagonal().real.sum()) <= 1e-13
