@@ -292,6 +292,60 @@ def run_batch_workload(args):
 
 
 # ------------------------------------------------------------------------------------------
+ADJOINT_WORKLOAD = ("SquareLattice(64,64) open, M=2048 lowest eigenstates of h(V0), V0 ~ U[-0.1,0.1], "
+                    "50 PointFlux amplitudes at (32.5,32.5) (init 0.1, 8 steps each), dt=0.05, 400 steps, "
+                    "checkpoint every 20, loss sum_i (rho_i(T) - rho*_i)^2")
+
+
+def run_adjoint_workload(args):
+    """The differentiation workload: one loss_and_grad = the forward pass with checkpoints, the
+    recomputation of every segment, the adjoint recurrence and the co-state propagation.
+    `value` counts forward ket-steps (M x 400) per second of loss_and_grad."""
+    import torch
+    import lmgpu
+    ctx = lmgpu.default_context()
+    ext = torch.cuda.ExternalStream(ctx.stream_ptr(), device=torch.device("cuda", 0))
+    L, M, dt, nsteps, spi = 64, 2048, 0.05, 400, 8
+    point = (32.5, 32.5)
+    rng = np.random.default_rng(SEED + 11)
+    V = rng.uniform(-0.1, 0.1, L * L)
+    B = np.full(50, 0.1)
+    lat = lmgpu.SquareLattice(L, L)
+    w, vecs = lmgpu.diagonalize(lmgpu.tightbinding_hamiltonian(lat, V, field=lmgpu.PointFlux(B[0], point)))
+    psi0 = vecs[:, :M].cpu().numpy()
+    del vecs
+    c = rng.uniform(20, 44, size=2)
+    r2 = ((lat.coords() - c) ** 2).sum(axis=1)
+    target = 0.5 + 0.2 * np.exp(-r2 / (2 * 6.0 ** 2))
+    prob = lmgpu.DensityLossAdjoint(lat, psi0, target, dt, nsteps, spi, point, precision=args.precision)
+    for _ in range(max(1, args.warmup // 3)):
+        prob.loss_and_grad(V, B)
+    ctx.synchronize()
+    reps = max(1, min(args.steps, 3))
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    clk = ClockSampler(0)
+    clk.start()
+    e0.record(ext)
+    for _ in range(reps):
+        loss, gV, gB = prob.loss_and_grad(V, B)
+    e1.record(ext)
+    e1.synchronize()
+    clocks = clk.stop()
+    ms = e0.elapsed_time(e1) / reps
+    line = {"metric": "forward ket-steps/s of loss_and_grad (forward + checkpointed adjoint)",
+            "value": M * nsteps / (ms / 1000.0), "unit": "ket-steps/s", "n_gpus": 1, "steps": reps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "dtype": args.precision,
+            "data": "synthetic (seeded; psi_0 = lowest eigenstates of h(V0) from cuSOLVER eigh)",
+            "config": {"workload": ADJOINT_WORKLOAD, "N": L * L, "M": M, "tol": prob.tol,
+                       "step_unit": "one loss_and_grad"},
+            "loss": loss, "grad_norm_V": float(np.linalg.norm(gV)), "grad_norm_B": float(np.linalg.norm(gB)),
+            "clocks": clocks}
+    print(json.dumps(line))
+    return 0
+
+
+# ------------------------------------------------------------------------------------------
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -300,8 +354,9 @@ def main():
     ap.add_argument("--impl", default="lmgpu", choices=["lmgpu", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--kets", type=int, default=M_KETS)
-    ap.add_argument("--workload", default="kets", choices=["kets", "batch"],
-                    help="kets: the 256^2 ket-block workload (default); batch: 512 uneven dense-P lattices")
+    ap.add_argument("--workload", default="kets", choices=["kets", "batch", "adjoint"],
+                    help="kets: the 256^2 ket-block workload (default); batch: 512 uneven dense-P lattices; "
+                         "adjoint: loss_and_grad of the 64^2 differentiation workload")
     ap.add_argument("--instances", type=int, default=512)
     ap.add_argument("--precision", default="c32", choices=["c32", "c64"])
     args = ap.parse_args()
@@ -311,6 +366,8 @@ def main():
         return run_reference_arm(args)
     if args.workload == "batch":
         return run_batch_workload(args)
+    if args.workload == "adjoint":
+        return run_adjoint_workload(args)
 
     rank, world, local = dist_info()
     import torch

@@ -14,7 +14,7 @@
 // field amplitude A, dH[s, s+e]/dA = -2 pi i LI_e(A = 1) H[s, s+e] on every bond.
 //
 // lm_adjoint_step recomputes T_0 .. T_{K-1} from psi_n, runs the beta recurrence and
-// accumulates both gradients in FP64; the caller applies U^dagger to lambda with a solver
+// accumulates both gradients (FP64 results; c32 sums in double-float); the caller applies U^dagger to lambda with a solver
 // updated for -dt (the same polynomial with conjugate coefficients).
 #include <cuda_runtime.h>
 #include <math.h>
@@ -80,101 +80,129 @@ __global__ void __launch_bounds__(256) adj_recur_kernel(Geom g, const typename C
     }
 }
 
-// Gradient terms of order k: for every site s (FP64 over the kets of one chunk)
-//   gV[s]   += Re( ph * f * conj(beta_s) T_s )
-//   gA[0]   += Re( ph * f * sum_bonds [conj(beta_s) D[s,j] T_j + conj(beta_j) conj(D[s,j]) T_s] )
-// with ph = e^{-ib dt}, f = 1/a (k = 1) or 2/a (k >= 2), D = dH/dA of the bond table dhop.
+// Gradient terms of order k, per site s, with sums over all kets m:
+//   gV[s] += f Re( ph * sum_m conj(beta_sm) T_sm )
+//   gA    += f Re( ph * sum_s sum_e [ D[s,j] S1 + conj(D[s,j]) S2 ] ),  j = s + e,
+//            S1 = sum_m conj(beta_sm) T_jm,  S2 = sum_m conj(beta_jm) T_sm
+// with ph = e^{-ib dt}, f = 1/a (k = 1) or 2/a (k >= 2), D = dH/dA of the bond table dhop (the
+// bond s -> s+e and its Hermitian partner, each bond owned by its source).  A block owns 32
+// sites; its 8 warps split the kets and their partial sums are added in warp order.  gV has
+// one writer per site per launch and gA one partial per block (summed in block order by
+// lm_adjoint_gradients), so the gradients are bit-reproducible.  c32 data is summed in
+// double-float FP32 (Acc<float>), c64 data in FP64.
 template <typename R>
 __global__ void __launch_bounds__(256) adj_grad_kernel(Geom g, const double2* __restrict__ dhop,
                                                        const typename CT<R>::V* __restrict__ beta,
                                                        const typename CT<R>::V* __restrict__ T, int64_t ld, int64_t M,
-                                                       int64_t chunk, double ph_re, double ph_im, double f,
-                                                       double* __restrict__ gV, double* __restrict__ gA) {
+                                                       double ph_re, double ph_im, double f,
+                                                       double* __restrict__ gV, double* __restrict__ gA_part) {
     typedef typename CT<R>::V V;
-    __shared__ double red[8];
-    const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const int64_t m0 = (int64_t)blockIdx.y * chunk, m1 = min(M, m0 + chunk);
-    double vre = 0.0, vim = 0.0;  // sum conj(beta_s) T_s
-    double are = 0.0, aim = 0.0;  // bond terms
+    __shared__ double red[8][10][32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int64_t s = (int64_t)blockIdx.x * 32 + lane;
+    Acc<R> a[10];  // conj(b_s) T_s (re, im); +x: S1 (re, im), S2 (re, im); +y: the same
+    Nbr nb;
     if (s < g.N) {
-        const Nbr nb = neighbours(g, s);
-        double2 dx = make_double2(0.0, 0.0), dy = make_double2(0.0, 0.0);
-        if (dhop) {  // the bond s -> s+e and its Hermitian partner (each bond owned by its source)
-            if (nb.hxp) dx = dhop[s];
-            if (nb.hyp) dy = dhop[g.N + s];
-        }
-        for (int64_t m = m0; m < m1; ++m) {
+        nb = neighbours(g, s);
+        // absent bonds read the site itself (always in bounds); their D is never applied
+        const int64_t jx = nb.hxp ? nb.xp : s, jy = nb.hyp ? nb.yp : s;
+        for (int64_t m = warp; m < M; m += 8) {
             const int64_t o = m * ld;
             const V b = beta[o + s], t = T[o + s];
-            vre += (double)b.x * t.x + (double)b.y * t.y;  // conj(b) t
-            vim += (double)b.x * t.y - (double)b.y * t.x;
+            a[0].add_prod(b.x, t.x);
+            a[0].add_prod(b.y, t.y);
+            a[1].add_prod(b.x, t.y);
+            a[1].add_prod(-b.y, t.x);
             if (dhop) {
-#pragma unroll
-                for (int dir = 0; dir < 2; ++dir) {
-                    const bool has = dir == 0 ? nb.hxp : nb.hyp;
-                    if (!has) continue;
-                    const int64_t j = dir == 0 ? nb.xp : nb.yp;
-                    const double2 D = dir == 0 ? dx : dy;
-                    const V bj = beta[o + j], tj = T[o + j];
-                    // conj(b_s) D T_j
-                    const double pr = D.x * tj.x - D.y * tj.y, pi = D.x * tj.y + D.y * tj.x;
-                    are += (double)b.x * pr + (double)b.y * pi;
-                    aim += (double)b.x * pi - (double)b.y * pr;
-                    // conj(b_j) conj(D) T_s
-                    const double qr = D.x * t.x + D.y * t.y, qi = D.x * t.y - D.y * t.x;
-                    are += (double)bj.x * qr + (double)bj.y * qi;
-                    aim += (double)bj.x * qi - (double)bj.y * qr;
-                }
+                const V tx = T[o + jx], bx = beta[o + jx], ty = T[o + jy], by = beta[o + jy];
+                a[2].add_prod(b.x, tx.x);   // S1 = conj(b_s) T_j
+                a[2].add_prod(b.y, tx.y);
+                a[3].add_prod(b.x, tx.y);
+                a[3].add_prod(-b.y, tx.x);
+                a[4].add_prod(bx.x, t.x);   // S2 = conj(b_j) T_s
+                a[4].add_prod(bx.y, t.y);
+                a[5].add_prod(bx.x, t.y);
+                a[5].add_prod(-bx.y, t.x);
+                a[6].add_prod(b.x, ty.x);
+                a[6].add_prod(b.y, ty.y);
+                a[7].add_prod(b.x, ty.y);
+                a[7].add_prod(-b.y, ty.x);
+                a[8].add_prod(by.x, t.x);
+                a[8].add_prod(by.y, t.y);
+                a[9].add_prod(by.x, t.y);
+                a[9].add_prod(-by.y, t.x);
             }
         }
-        if (m1 > m0) {
-            const double gv = f * (ph_re * vre - ph_im * vim);
-            atomicAdd(gV + s, gv);
+    }
+#pragma unroll
+    for (int q = 0; q < 10; ++q) red[warp][q][lane] = a[q].get();
+    __syncthreads();
+    if (warp != 0) return;
+    double v[10];
+#pragma unroll
+    for (int q = 0; q < 10; ++q) {
+        double t = 0.0;
+        for (int w = 0; w < 8; ++w) t += red[w][q][lane];
+        v[q] = t;
+    }
+    double ga = 0.0;
+    if (s < g.N) {
+        if (M > 0) gV[s] += f * (ph_re * v[0] - ph_im * v[1]);
+        if (dhop) {
+#pragma unroll
+            for (int dir = 0; dir < 2; ++dir) {
+                if (!(dir == 0 ? nb.hxp : nb.hyp)) continue;
+                const double2 D = dhop[dir * g.N + s];
+                const double* S = v + 2 + 4 * dir;  // S1 re, im, S2 re, im
+                const double are = (D.x * S[0] - D.y * S[1]) + (D.x * S[2] + D.y * S[3]);
+                const double aim = (D.x * S[1] + D.y * S[0]) + (D.x * S[3] - D.y * S[2]);
+                ga += f * (ph_re * are - ph_im * aim);
+            }
         }
     }
-    if (gA) {
-        double ga = f * (ph_re * are - ph_im * aim);
+    if (gA_part) {
         for (int o = 16; o > 0; o >>= 1) ga += __shfl_down_sync(0xffffffffu, ga, o);
-        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = ga;
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            double tot = 0.0;
-            for (int w = 0; w < (int)(blockDim.x >> 5); ++w) tot += red[w];
-            atomicAdd(gA, tot);
-        }
+        if (lane == 0) gA_part[blockIdx.x] += ga;
     }
 }
 
-// rho_s = sum_m |psi_sm|^2; loss = sum_s (rho_s - target_s)^2; lambda = 4 (rho_s - target_s) psi
+// rho_s = sum_m |psi_sm|^2; loss = sum_s (rho_s - target_s)^2; lambda = 4 (rho_s - target_s) psi.
+// A block owns 32 sites (8 warps split the kets); loss_part[block] receives its partial loss.
 template <typename R>
 __global__ void __launch_bounds__(256) adj_seed_kernel(int64_t N, const typename CT<R>::V* __restrict__ psi,
                                                        typename CT<R>::V* __restrict__ lam, int64_t ld, int64_t M,
-                                                       const double* __restrict__ target, double* __restrict__ loss) {
+                                                       const double* __restrict__ target,
+                                                       double* __restrict__ loss_part) {
     typedef typename CT<R>::V V;
-    __shared__ double red[8];
-    const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    double l = 0.0;
-    if (s < N) {
-        double rho = 0.0;
-        for (int64_t m = 0; m < M; ++m) {
+    __shared__ double red[8][32];
+    __shared__ double diff_s[32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int64_t s = (int64_t)blockIdx.x * 32 + lane;
+    Acc<R> acc;
+    if (s < N)
+        for (int64_t m = warp; m < M; m += 8) {
             const V v = psi[m * ld + s];
-            rho += (double)v.x * v.x + (double)v.y * v.y;
+            acc.add_prod(v.x, v.x);
+            acc.add_prod(v.y, v.y);
         }
-        const double diff = rho - target[s];
-        l = diff * diff;
-        const R f = (R)(4.0 * diff);
-        for (int64_t m = 0; m < M; ++m) {
-            const V v = psi[m * ld + s];
-            lam[m * ld + s] = CT<R>::make(f * v.x, f * v.y);
-        }
-    }
-    for (int o = 16; o > 0; o >>= 1) l += __shfl_down_sync(0xffffffffu, l, o);
-    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = l;
+    red[warp][lane] = acc.get();
     __syncthreads();
-    if (threadIdx.x == 0) {
-        double tot = 0.0;
-        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) tot += red[w];
-        atomicAdd(loss, tot);
+    if (warp == 0) {
+        double rho = 0.0;
+        for (int w = 0; w < 8; ++w) rho += red[w][lane];
+        const double diff = s < N ? rho - target[s] : 0.0;
+        diff_s[lane] = diff;
+        double l = diff * diff;
+        for (int o = 16; o > 0; o >>= 1) l += __shfl_down_sync(0xffffffffu, l, o);
+        if (lane == 0) loss_part[blockIdx.x] = l;
+    }
+    __syncthreads();
+    if (s < N) {
+        const R fct = (R)(4.0 * diff_s[lane]);
+        for (int64_t m = warp; m < M; m += 8) {
+            const V v = psi[m * ld + s];
+            lam[m * ld + s] = CT<R>::make(fct * v.x, fct * v.y);
+        }
     }
 }
 
@@ -212,9 +240,10 @@ struct lm_adjoint {
     std::vector<void*> T;  // T_0 .. T_{K-1} (T_0 aliases psi during a step)
     void* B[3] = {nullptr, nullptr, nullptr};
     double* d_gV = nullptr;
-    double* d_gA = nullptr;
+    double* d_gA = nullptr;     // per gradient slot, one partial per 32-site block (nslots x nblk)
     int nslots = 0;
-    double* d_loss = nullptr;
+    int64_t nblk = 0;           // 32-site blocks of the gradient and seed kernels
+    double* d_loss = nullptr;   // one partial per 32-site block (nblk)
     double* d_target = nullptr;
     double2* d_dhop = nullptr;
 };
@@ -271,10 +300,12 @@ int lm_adjoint_create(lm_ctx* ctx, int64_t n, int64_t m, int precision, int nslo
     a->precision = precision;
     a->elem = precision == LM_C64 ? 16 : 8;
     a->nslots = nslots;
+    a->nblk = (n + 31) / 32;
     cudaSetDevice(ctx->device);
+    const size_t gA_len = (size_t)(nslots > 0 ? nslots : 1) * (size_t)a->nblk;
     int rc = adj_alloc(ctx, (void**)&a->d_gV, sizeof(double) * (size_t)n);
-    if (rc == LM_OK) rc = adj_alloc(ctx, (void**)&a->d_gA, sizeof(double) * (size_t)(nslots > 0 ? nslots : 1));
-    if (rc == LM_OK) rc = adj_alloc(ctx, (void**)&a->d_loss, sizeof(double));
+    if (rc == LM_OK) rc = adj_alloc(ctx, (void**)&a->d_gA, sizeof(double) * gA_len);
+    if (rc == LM_OK) rc = adj_alloc(ctx, (void**)&a->d_loss, sizeof(double) * (size_t)a->nblk);
     if (rc == LM_OK) rc = adj_alloc(ctx, (void**)&a->d_target, sizeof(double) * (size_t)n);
     if (rc == LM_OK) rc = adj_alloc(ctx, (void**)&a->d_dhop, sizeof(double2) * 2 * (size_t)n);
     if (rc != LM_OK) {
@@ -287,7 +318,7 @@ int lm_adjoint_create(lm_ctx* ctx, int64_t n, int64_t m, int precision, int nslo
         return rc;
     }
     cudaMemsetAsync(a->d_gV, 0, sizeof(double) * (size_t)n, ctx->stream);
-    cudaMemsetAsync(a->d_gA, 0, sizeof(double) * (size_t)(nslots > 0 ? nslots : 1), ctx->stream);
+    cudaMemsetAsync(a->d_gA, 0, sizeof(double) * gA_len, ctx->stream);
     *out = a;
     return LM_OK;
 }
@@ -311,7 +342,8 @@ int lm_adjoint_reset(lm_adjoint* a) {
     lm_ctx* ctx = a->ctx;
     cudaSetDevice(ctx->device);
     CUDA_TRY(ctx, cudaMemsetAsync(a->d_gV, 0, sizeof(double) * (size_t)a->n, ctx->stream), "memset");
-    CUDA_TRY(ctx, cudaMemsetAsync(a->d_gA, 0, sizeof(double) * (size_t)(a->nslots > 0 ? a->nslots : 1), ctx->stream),
+    CUDA_TRY(ctx, cudaMemsetAsync(a->d_gA, 0, sizeof(double) * (size_t)(a->nslots > 0 ? a->nslots : 1) * (size_t)a->nblk,
+                                  ctx->stream),
              "memset");
     return LM_OK;
 }
@@ -326,8 +358,7 @@ int lm_adjoint_seed(lm_adjoint* a, lm_state* psi, const double* target, lm_state
     cudaSetDevice(ctx->device);
     CUDA_TRY(ctx, cudaMemcpyAsync(a->d_target, target, sizeof(double) * (size_t)a->n, cudaMemcpyHostToDevice, ctx->stream),
              "upload target");
-    CUDA_TRY(ctx, cudaMemsetAsync(a->d_loss, 0, sizeof(double), ctx->stream), "memset");
-    const unsigned blocks = (unsigned)((a->n + 255) / 256);
+    const unsigned blocks = (unsigned)a->nblk;
     if (a->precision == LM_C64)
         adj_seed_kernel<double><<<blocks, 256, 0, ctx->stream>>>(a->n, (const double2*)psi->d_data, (double2*)lam->d_data,
                                                                  psi->ld, a->m, a->d_target, a->d_loss);
@@ -336,8 +367,14 @@ int lm_adjoint_seed(lm_adjoint* a, lm_state* psi, const double* target, lm_state
                                                                 psi->ld, a->m, a->d_target, a->d_loss);
     ctx->launches++;
     CUDA_TRY(ctx, cudaGetLastError(), "seed kernel");
-    CUDA_TRY(ctx, cudaMemcpyAsync(loss, a->d_loss, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream), "download loss");
+    std::vector<double> part((size_t)a->nblk);
+    CUDA_TRY(ctx, cudaMemcpyAsync(part.data(), a->d_loss, sizeof(double) * part.size(), cudaMemcpyDeviceToHost,
+                                  ctx->stream),
+             "download loss");
     CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream), "sync");
+    double tot = 0.0;
+    for (double v : part) tot += v;  // block order
+    *loss = tot;
     return LM_OK;
 }
 
@@ -393,8 +430,8 @@ int lm_adjoint_step(lm_adjoint* a, lm_solver* s, lm_ham* h, int component, int s
         dhop = a->d_dhop;
     }
     // beta_K .. beta_1 with gradient terms; B[k % 3] rotates
-    const int64_t chunk = 64;
-    dim3 ggrid((unsigned)((g.N + 255) / 256), (unsigned)((M + chunk - 1) / chunk));
+    const unsigned ggrid = (unsigned)a->nblk;
+    double* gA = component >= 0 ? a->d_gA + (size_t)slot * (size_t)a->nblk : nullptr;
     for (int k = K; k >= 1; --k) {
         const ChebCoef c = s->coef[(size_t)k];
         const double wre = c.odd ? 0.0 : c.s, wim = c.odd ? c.s : 0.0;  // conj(c_k)
@@ -405,12 +442,10 @@ int lm_adjoint_step(lm_adjoint* a, lm_solver* s, lm_ham* h, int component, int s
         const double f = (k == 1 ? 1.0 : 2.0) / s->a;
         if (f64)
             adj_grad_kernel<double><<<ggrid, 256, 0, ctx->stream>>>(g, dhop, (const double2*)bk, (const double2*)a->T[(size_t)k - 1],
-                                                                    ld, M, chunk, s->phase_re, s->phase_im, f, a->d_gV,
-                                                                    component >= 0 ? a->d_gA + slot : nullptr);
+                                                                    ld, M, s->phase_re, s->phase_im, f, a->d_gV, gA);
         else
             adj_grad_kernel<float><<<ggrid, 256, 0, ctx->stream>>>(g, dhop, (const float2*)bk, (const float2*)a->T[(size_t)k - 1],
-                                                                   ld, M, chunk, s->phase_re, s->phase_im, f, a->d_gV,
-                                                                   component >= 0 ? a->d_gA + slot : nullptr);
+                                                                   ld, M, s->phase_re, s->phase_im, f, a->d_gV, gA);
         ctx->launches++;
         CUDA_TRY(ctx, cudaGetLastError(), "adjoint gradient kernel");
     }
@@ -424,10 +459,19 @@ int lm_adjoint_gradients(lm_adjoint* a, double* gV, double* gA) {
     if (gV)
         CUDA_TRY(ctx, cudaMemcpyAsync(gV, a->d_gV, sizeof(double) * (size_t)a->n, cudaMemcpyDeviceToHost, ctx->stream),
                  "download gV");
-    if (gA && a->nslots > 0)
-        CUDA_TRY(ctx, cudaMemcpyAsync(gA, a->d_gA, sizeof(double) * (size_t)a->nslots, cudaMemcpyDeviceToHost, ctx->stream),
+    std::vector<double> part;
+    if (gA && a->nslots > 0) {
+        part.resize((size_t)a->nslots * (size_t)a->nblk);
+        CUDA_TRY(ctx, cudaMemcpyAsync(part.data(), a->d_gA, sizeof(double) * part.size(), cudaMemcpyDeviceToHost,
+                                      ctx->stream),
                  "download gA");
+    }
     CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream), "sync");
+    for (int j = 0; gA && j < a->nslots; ++j) {
+        double tot = 0.0;
+        for (int64_t b = 0; b < a->nblk; ++b) tot += part[(size_t)j * (size_t)a->nblk + (size_t)b];  // block order
+        gA[j] = tot;
+    }
     return LM_OK;
 }
 

@@ -199,32 +199,9 @@ cudaError_t launch_convert(lm_ctx* ctx, int to_precision, const void* src, void*
 }
 
 // ------------------------------------------------------------------------------------------
-// Readouts.  Sums over kets run in FP64 for c64 states; for c32 states they run in
-// double-float FP32 (an unevaluated hi + lo pair, products split exactly by an FMA and added by
-// Knuth's TwoSum), which carries ~48 significant bits at FP32 issue rates -- GB300 runs FP64
-// at 1/64 of its FP32 rate, so an FP64 accumulator per element would bound these kernels.
-// Every sum is over a fixed order (no atomics): the readouts are bit-reproducible.
+// Readouts.  Sums over kets use Acc<R> (FP64 for c64 states, double-float FP32 for c32
+// states).  Every sum is over a fixed order (no atomics): the readouts are bit-reproducible.
 // ------------------------------------------------------------------------------------------
-template <typename R> struct Acc;
-template <> struct Acc<double> {
-    double v = 0.0;
-    __device__ __forceinline__ void add_prod(double a, double b) { v = fma(a, b, v); }
-    __device__ __forceinline__ double get() const { return v; }
-};
-template <> struct Acc<float> {
-    float hi = 0.f, lo = 0.f;
-    __device__ __forceinline__ void add_prod(float a, float b) {
-        const float p = __fmul_rn(a, b);
-        const float pe = __fmaf_rn(a, b, -p);  // a*b = p + pe exactly
-        const float s = __fadd_rn(hi, p);      // TwoSum(hi, p) = s + e exactly
-        const float bp = __fsub_rn(s, hi);
-        const float e = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bp)), __fsub_rn(p, bp));
-        hi = s;
-        lo = __fadd_rn(lo, __fadd_rn(e, pe));
-    }
-    __device__ __forceinline__ double get() const { return (double)hi + (double)lo; }
-};
-
 constexpr int kReadWarps = 8;  // warps of a readout block; they split the kets
 
 // localdensity of a ket block: rho_s = sum_k w_k |psi_sk|^2.  A block owns 32*VEC consecutive

@@ -17,6 +17,33 @@ template <> struct CT<float> {
 };
 
 // ------------------------------------------------------------------------------------------
+// Sum of products over kets.  Acc<double> is a plain FP64 accumulator.  Acc<float> is a
+// double-float accumulator: an unevaluated pair hi + lo.  Each product is split exactly by an
+// FMA, and Knuth's TwoSum adds it.  The pair carries ~48 significant bits at FP32 issue rates.
+// GB300 runs FP64 at 1/64 of its FP32 rate, so an FP64 accumulator per element would bound the
+// readout and gradient kernels of c32 states.
+// ------------------------------------------------------------------------------------------
+template <typename R> struct Acc;
+template <> struct Acc<double> {
+    double v = 0.0;
+    __device__ __forceinline__ void add_prod(double a, double b) { v = fma(a, b, v); }
+    __device__ __forceinline__ double get() const { return v; }
+};
+template <> struct Acc<float> {
+    float hi = 0.f, lo = 0.f;
+    __device__ __forceinline__ void add_prod(float a, float b) {
+        const float p = __fmul_rn(a, b);
+        const float pe = __fmaf_rn(a, b, -p);  // a*b = p + pe exactly
+        const float s = __fadd_rn(hi, p);      // TwoSum(hi, p) = s + e exactly
+        const float bp = __fsub_rn(s, hi);
+        const float e = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bp)), __fsub_rn(p, bp));
+        hi = s;
+        lo = __fadd_rn(lo, __fadd_rn(e, pe));
+    }
+    __device__ __forceinline__ double get() const { return (double)hi + (double)lo; }
+};
+
+// ------------------------------------------------------------------------------------------
 // Neighbour routing on the square lattice (src/core/boundaries.jl:251-289 for the periodic
 // case: a destination one step outside is wrapped by the axis translation).
 // ------------------------------------------------------------------------------------------
