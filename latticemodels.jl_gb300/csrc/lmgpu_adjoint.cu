@@ -19,6 +19,7 @@
 #include <cuda_runtime.h>
 #include <math.h>
 
+#include <algorithm>
 #include <new>
 #include <vector>
 
@@ -86,27 +87,28 @@ __global__ void __launch_bounds__(256) adj_recur_kernel(Geom g, const typename C
 //            S1 = sum_m conj(beta_sm) T_jm,  S2 = sum_m conj(beta_jm) T_sm
 // with ph = e^{-ib dt}, f = 1/a (k = 1) or 2/a (k >= 2), D = dH/dA of the bond table dhop (the
 // bond s -> s+e and its Hermitian partner, each bond owned by its source).  A block owns 32
-// sites; its 8 warps split the kets and their partial sums are added in warp order.  gV has
-// one writer per site per launch and gA one partial per block (summed in block order by
-// lm_adjoint_gradients), so the gradients are bit-reproducible.  c32 data is summed in
-// double-float FP32 (Acc<float>), c64 data in FP64.
+// sites and one chunk of the kets (blockIdx.y); its 8 warps split the chunk and their partial
+// sums are added in warp order.  gV_part[chunk][s] and gA_part[chunk][block] each have one
+// writer per launch; lm_adjoint_gradients adds them in chunk and block order, so the gradients
+// are bit-reproducible.  c32 data is summed in double-float FP32 (Acc<float>), c64 in FP64.
 template <typename R>
 __global__ void __launch_bounds__(256) adj_grad_kernel(Geom g, const double2* __restrict__ dhop,
                                                        const typename CT<R>::V* __restrict__ beta,
                                                        const typename CT<R>::V* __restrict__ T, int64_t ld, int64_t M,
-                                                       double ph_re, double ph_im, double f,
-                                                       double* __restrict__ gV, double* __restrict__ gA_part) {
+                                                       int64_t mchunk, double ph_re, double ph_im, double f,
+                                                       double* __restrict__ gV_part, double* __restrict__ gA_part) {
     typedef typename CT<R>::V V;
     __shared__ double red[8][10][32];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int64_t s = (int64_t)blockIdx.x * 32 + lane;
+    const int64_t m0 = (int64_t)blockIdx.y * mchunk, m1 = min(M, m0 + mchunk);
     Acc<R> a[10];  // conj(b_s) T_s (re, im); +x: S1 (re, im), S2 (re, im); +y: the same
     Nbr nb;
     if (s < g.N) {
         nb = neighbours(g, s);
         // absent bonds read the site itself (always in bounds); their D is never applied
         const int64_t jx = nb.hxp ? nb.xp : s, jy = nb.hyp ? nb.yp : s;
-        for (int64_t m = warp; m < M; m += 8) {
+        for (int64_t m = m0 + warp; m < m1; m += 8) {
             const int64_t o = m * ld;
             const V b = beta[o + s], t = T[o + s];
             a[0].add_prod(b.x, t.x);
@@ -147,7 +149,7 @@ __global__ void __launch_bounds__(256) adj_grad_kernel(Geom g, const double2* __
     }
     double ga = 0.0;
     if (s < g.N) {
-        if (M > 0) gV[s] += f * (ph_re * v[0] - ph_im * v[1]);
+        gV_part[(int64_t)blockIdx.y * g.N + s] += f * (ph_re * v[0] - ph_im * v[1]);
         if (dhop) {
 #pragma unroll
             for (int dir = 0; dir < 2; ++dir) {
@@ -162,7 +164,7 @@ __global__ void __launch_bounds__(256) adj_grad_kernel(Geom g, const double2* __
     }
     if (gA_part) {
         for (int o = 16; o > 0; o >>= 1) ga += __shfl_down_sync(0xffffffffu, ga, o);
-        if (lane == 0) gA_part[blockIdx.x] += ga;
+        if (lane == 0) gA_part[(int64_t)blockIdx.y * gridDim.x + blockIdx.x] += ga;
     }
 }
 
@@ -239,10 +241,11 @@ struct lm_adjoint {
     int K = 0;
     std::vector<void*> T;  // T_0 .. T_{K-1} (T_0 aliases psi during a step)
     void* B[3] = {nullptr, nullptr, nullptr};
-    double* d_gV = nullptr;
-    double* d_gA = nullptr;     // per gradient slot, one partial per 32-site block (nslots x nblk)
+    double* d_gV = nullptr;     // per ket chunk, one partial per site (nchunk x n)
+    double* d_gA = nullptr;     // per gradient slot, one partial per (chunk, 32-site block)
     int nslots = 0;
     int64_t nblk = 0;           // 32-site blocks of the gradient and seed kernels
+    int64_t nchunk = 1, mchunk = 1;  // ket chunks of the gradient kernel (grid y) and their size
     double* d_loss = nullptr;   // one partial per 32-site block (nblk)
     double* d_target = nullptr;
     double2* d_dhop = nullptr;
@@ -301,9 +304,15 @@ int lm_adjoint_create(lm_ctx* ctx, int64_t n, int64_t m, int precision, int nslo
     a->elem = precision == LM_C64 ? 16 : 8;
     a->nslots = nslots;
     a->nblk = (n + 31) / 32;
+    // enough (block, chunk) pairs for ~6 blocks per SM, chunks of at least 64 kets
+    const int64_t want = ((int64_t)6 * std::max(ctx->sm_count, 1) + a->nblk - 1) / a->nblk;
+    a->nchunk = std::max<int64_t>(1, std::min<int64_t>(want, (m + 63) / 64));
+    a->mchunk = (m + a->nchunk - 1) / a->nchunk;
+    a->nchunk = (m + a->mchunk - 1) / a->mchunk;
     cudaSetDevice(ctx->device);
-    const size_t gA_len = (size_t)(nslots > 0 ? nslots : 1) * (size_t)a->nblk;
-    int rc = adj_alloc(ctx, (void**)&a->d_gV, sizeof(double) * (size_t)n);
+    const size_t gA_len = (size_t)(nslots > 0 ? nslots : 1) * (size_t)a->nblk * (size_t)a->nchunk;
+    const size_t gV_len = (size_t)n * (size_t)a->nchunk;
+    int rc = adj_alloc(ctx, (void**)&a->d_gV, sizeof(double) * gV_len);
     if (rc == LM_OK) rc = adj_alloc(ctx, (void**)&a->d_gA, sizeof(double) * gA_len);
     if (rc == LM_OK) rc = adj_alloc(ctx, (void**)&a->d_loss, sizeof(double) * (size_t)a->nblk);
     if (rc == LM_OK) rc = adj_alloc(ctx, (void**)&a->d_target, sizeof(double) * (size_t)n);
@@ -317,7 +326,7 @@ int lm_adjoint_create(lm_ctx* ctx, int64_t n, int64_t m, int precision, int nslo
         delete a;
         return rc;
     }
-    cudaMemsetAsync(a->d_gV, 0, sizeof(double) * (size_t)n, ctx->stream);
+    cudaMemsetAsync(a->d_gV, 0, sizeof(double) * gV_len, ctx->stream);
     cudaMemsetAsync(a->d_gA, 0, sizeof(double) * gA_len, ctx->stream);
     *out = a;
     return LM_OK;
@@ -341,8 +350,10 @@ int lm_adjoint_reset(lm_adjoint* a) {
     if (!a) return LM_ERR_ARG;
     lm_ctx* ctx = a->ctx;
     cudaSetDevice(ctx->device);
-    CUDA_TRY(ctx, cudaMemsetAsync(a->d_gV, 0, sizeof(double) * (size_t)a->n, ctx->stream), "memset");
-    CUDA_TRY(ctx, cudaMemsetAsync(a->d_gA, 0, sizeof(double) * (size_t)(a->nslots > 0 ? a->nslots : 1) * (size_t)a->nblk,
+    CUDA_TRY(ctx, cudaMemsetAsync(a->d_gV, 0, sizeof(double) * (size_t)a->n * (size_t)a->nchunk, ctx->stream), "memset");
+    CUDA_TRY(ctx, cudaMemsetAsync(a->d_gA, 0,
+                                  sizeof(double) * (size_t)(a->nslots > 0 ? a->nslots : 1) * (size_t)a->nblk *
+                                      (size_t)a->nchunk,
                                   ctx->stream),
              "memset");
     return LM_OK;
@@ -430,8 +441,8 @@ int lm_adjoint_step(lm_adjoint* a, lm_solver* s, lm_ham* h, int component, int s
         dhop = a->d_dhop;
     }
     // beta_K .. beta_1 with gradient terms; B[k % 3] rotates
-    const unsigned ggrid = (unsigned)a->nblk;
-    double* gA = component >= 0 ? a->d_gA + (size_t)slot * (size_t)a->nblk : nullptr;
+    const dim3 ggrid((unsigned)a->nblk, (unsigned)a->nchunk);
+    double* gA = component >= 0 ? a->d_gA + (size_t)slot * (size_t)a->nblk * (size_t)a->nchunk : nullptr;
     for (int k = K; k >= 1; --k) {
         const ChebCoef c = s->coef[(size_t)k];
         const double wre = c.odd ? 0.0 : c.s, wim = c.odd ? c.s : 0.0;  // conj(c_k)
@@ -442,10 +453,10 @@ int lm_adjoint_step(lm_adjoint* a, lm_solver* s, lm_ham* h, int component, int s
         const double f = (k == 1 ? 1.0 : 2.0) / s->a;
         if (f64)
             adj_grad_kernel<double><<<ggrid, 256, 0, ctx->stream>>>(g, dhop, (const double2*)bk, (const double2*)a->T[(size_t)k - 1],
-                                                                    ld, M, s->phase_re, s->phase_im, f, a->d_gV, gA);
+                                                                    ld, M, a->mchunk, s->phase_re, s->phase_im, f, a->d_gV, gA);
         else
             adj_grad_kernel<float><<<ggrid, 256, 0, ctx->stream>>>(g, dhop, (const float2*)bk, (const float2*)a->T[(size_t)k - 1],
-                                                                   ld, M, s->phase_re, s->phase_im, f, a->d_gV, gA);
+                                                                   ld, M, a->mchunk, s->phase_re, s->phase_im, f, a->d_gV, gA);
         ctx->launches++;
         CUDA_TRY(ctx, cudaGetLastError(), "adjoint gradient kernel");
     }
@@ -456,20 +467,29 @@ int lm_adjoint_gradients(lm_adjoint* a, double* gV, double* gA) {
     if (!a) return LM_ERR_ARG;
     lm_ctx* ctx = a->ctx;
     cudaSetDevice(ctx->device);
-    if (gV)
-        CUDA_TRY(ctx, cudaMemcpyAsync(gV, a->d_gV, sizeof(double) * (size_t)a->n, cudaMemcpyDeviceToHost, ctx->stream),
+    const size_t nc = (size_t)a->nchunk, nb = (size_t)a->nblk;
+    std::vector<double> pv, pa;
+    if (gV) {
+        pv.resize((size_t)a->n * nc);
+        CUDA_TRY(ctx, cudaMemcpyAsync(pv.data(), a->d_gV, sizeof(double) * pv.size(), cudaMemcpyDeviceToHost, ctx->stream),
                  "download gV");
-    std::vector<double> part;
+    }
     if (gA && a->nslots > 0) {
-        part.resize((size_t)a->nslots * (size_t)a->nblk);
-        CUDA_TRY(ctx, cudaMemcpyAsync(part.data(), a->d_gA, sizeof(double) * part.size(), cudaMemcpyDeviceToHost,
-                                      ctx->stream),
+        pa.resize((size_t)a->nslots * nb * nc);
+        CUDA_TRY(ctx, cudaMemcpyAsync(pa.data(), a->d_gA, sizeof(double) * pa.size(), cudaMemcpyDeviceToHost, ctx->stream),
                  "download gA");
     }
     CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream), "sync");
+    if (gV)
+        for (int64_t i = 0; i < a->n; ++i) {
+            double tot = 0.0;
+            for (size_t c = 0; c < nc; ++c) tot += pv[c * (size_t)a->n + (size_t)i];  // chunk order
+            gV[i] = tot;
+        }
     for (int j = 0; gA && j < a->nslots; ++j) {
         double tot = 0.0;
-        for (int64_t b = 0; b < a->nblk; ++b) tot += part[(size_t)j * (size_t)a->nblk + (size_t)b];  // block order
+        const double* p = pa.data() + (size_t)j * nb * nc;
+        for (size_t q = 0; q < nb * nc; ++q) tot += p[q];  // chunk-major block order
         gA[j] = tot;
     }
     return LM_OK;

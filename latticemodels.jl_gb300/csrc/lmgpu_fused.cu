@@ -11,8 +11,11 @@
 // shared-memory copy of T_{k-1} (x neighbours) and warp shuffles (y neighbours: a warp holds
 // two whole rows); T_{k-2} of a thread's own sites is read back from the buffer T_k
 // overwrites.  The valid part of the region shrinks by one site per order, so after K orders
-// the inner (32-2K) x (64-2K) sites are exact and are written out.  Positions outside the
-// lattice (open axes) hold zeros and zero coefficients; periodic axes wrap the halo.
+// the inner (32-2K) x (64-2K) sites are exact and are written out.  Periodic axes wrap the
+// halo.  Along an open axis the first and last regions of a lattice sit on the lattice edge:
+// the stencil has no bond across it, so nothing shrinks there and those regions write out up
+// to the edge (a lattice no longer than a region is one tile along that axis, with no halo).
+// Positions outside the lattice hold zeros and zero coefficients.
 //
 // Work items are (instance, tile, 16 kets).  A single lattice strides over its items
 // statically; a batch pulls items from a global atomic counter (the work queue), so CTAs
@@ -49,18 +52,68 @@ __device__ __forceinline__ int64_t wrap_axis(int64_t c, int64_t L, int per) {
     return c < 0 ? c + L : c;
 }
 
+// Tiling of one axis of length L by regions of R sites with a halo of H: region origin and
+// written range [w0, w1) of tile t (lattice coordinates; periodic origins may be negative).
+struct AxisTile {
+    int64_t origin, w0, w1;
+};
+
+__host__ __device__ __forceinline__ int64_t axis_ntiles(int64_t L, int per, int R, int H) {
+    const int64_t I = R - 2 * H;
+    if (per) return (L + I - 1) / I;
+    if (L <= R) return 1;
+    const int64_t rest = L - 2 * (int64_t)(R - H);
+    return 2 + (rest > 0 ? (rest + I - 1) / I : 0);
+}
+
+__host__ __device__ __forceinline__ AxisTile axis_tile(int64_t L, int per, int R, int H, int64_t t, int64_t n) {
+    const int64_t I = R - 2 * H;
+    AxisTile a;
+    if (per) {
+        a.w0 = t * I;
+        a.w1 = a.w0 + I < L ? a.w0 + I : L;
+        a.origin = a.w0 - H;
+    } else if (n == 1) {
+        a.origin = 0;
+        a.w0 = 0;
+        a.w1 = L;
+    } else if (t == 0) {
+        a.origin = 0;
+        a.w0 = 0;
+        a.w1 = R - H;
+    } else {
+        a.w0 = (R - H) + (t - 1) * I;
+        if (t == n - 1) {
+            a.origin = L - R;
+            a.w1 = L;
+        } else {
+            a.origin = a.w0 - H;
+            a.w1 = a.w0 + I;
+        }
+    }
+    return a;
+}
+
 struct TileMap {
     int site[S];  // lattice site of each of my four positions, -1 outside (N < 2^31)
     int gx;       // unwrapped lattice x of my row
     int gy0;      // unwrapped lattice y of my first position
+    int wx0, wx1, wy0, wy1;  // written range of the tile
+    int hard_lo, hard_hi;    // the region's low / high x edge is an open lattice edge
 };
 
 __device__ __forceinline__ TileMap tile_map(const Geom& g, int64_t tile, int nty, int H, int tx, int ty) {
     TileMap m;
-    const int IX = RX - 2 * H, IY = RY - 2 * H;
+    const int64_t ntx_all = axis_ntiles(g.Lx, g.per_x, RX, H);
     const int64_t tile_x = tile / nty, tile_y = tile % nty;
-    m.gx = (int)(tile_x * IX - H + tx);
-    m.gy0 = (int)(tile_y * IY - H + ty * S);
+    const AxisTile ax = axis_tile(g.Lx, g.per_x, RX, H, tile_x, ntx_all);
+    const AxisTile ay = axis_tile(g.Ly, g.per_y, RY, H, tile_y, nty);
+    m.wx0 = (int)ax.w0; m.wx1 = (int)ax.w1;
+    m.wy0 = (int)ay.w0; m.wy1 = (int)ay.w1;
+    m.hard_lo = !g.per_x && ax.origin == 0;
+    m.hard_hi = !g.per_x && ax.origin + RX >= g.Lx;
+    m.gx = (int)(ax.origin + tx);
+    m.gy0 = (int)(ay.origin + ty * S);
     const int64_t xs = wrap_axis(m.gx, g.Lx, g.per_x);
 #pragma unroll
     for (int j = 0; j < S; ++j) {
@@ -191,9 +244,8 @@ cheb_fused_c32_kernel(FusedInst single, const FusedInst* __restrict__ table, int
                 const int64_t sm = (xsm >= 0 && ys >= 0) ? xsm * g.Ly + ys : -1;  // site at x-1
                 const float2 h = sm >= 0 ? __ldg(hop2 + sm) : make_float2(0.f, 0.f);
                 hxm[j] = make_float2(h.x, -h.y);
-                const int ry = ty * S + j;
-                if (tx >= H && tx < RX - H && ry >= H && ry < RY - H && m.gx < g.Lx && m.gy0 + j < g.Ly && s >= 0)
-                    interior |= 1u << j;
+                const int gy = m.gy0 + j;
+                if (m.gx >= m.wx0 && m.gx < m.wx1 && gy >= m.wy0 && gy < m.wy1 && s >= 0) interior |= 1u << j;
             }
             const int64_t ysm = wrap_axis(m.gy0 - 1, g.Ly, g.per_y);
             const int64_t s2 = (xs >= 0 && ysm >= 0) ? xs * g.Ly + ysm : -1;  // site at y-1
@@ -247,8 +299,9 @@ cheb_fused_c32_kernel(FusedInst single, const FusedInst* __restrict__ table, int
                 const int src = (k == 1) ? stage : tb((k - 1) & 1);
                 const int dst = tb(k & 1);
                 const int prev2 = (k == 2) ? stage : dst;  // T_{k-2} of my positions
-                // warps whose two rows both lie outside the valid region skip the order
-                const bool active = (warp_row0 + 1 >= k) && (warp_row0 < RX - k);
+                // warps whose two rows both lie outside the valid region skip the order (the
+                // valid rows shrink by one per order, except at an open lattice edge)
+                const bool active = (cur.hard_lo || warp_row0 + 1 >= k) && (cur.hard_hi || warp_row0 < RX - k);
                 if (active) {
                     const int xp = min(tx + 1, RX - 1), xm = max(tx - 1, 0);
                     const float sk = D.s[k];
@@ -349,9 +402,8 @@ int fused_supported(int precision, int K) { return precision == LM_C32 && K >= 2
 int fused_supported_geom(const Geom& g) { return g.N < (int64_t)1 << 31 && g.Lx < (1 << 30) && g.Ly < (1 << 30); }
 
 int64_t fused_items(const Geom& g, int K, int64_t m, int* ntx, int* nty) {
-    const int IX = RX - 2 * K, IY = RY - 2 * K;
-    *ntx = (int)((g.Lx + IX - 1) / IX);
-    *nty = (int)((g.Ly + IY - 1) / IY);
+    *ntx = (int)axis_ntiles(g.Lx, g.per_x, RX, K);
+    *nty = (int)axis_ntiles(g.Ly, g.per_y, RY, K);
     const int64_t kchunks = (m + kFusedKetsPerItem - 1) / kFusedKetsPerItem;
     return (int64_t)(*ntx) * (*nty) * kchunks;
 }

@@ -29,7 +29,7 @@ class Batch:
         self.kind = _lib.LM_DENSITY if kind == "density" else _lib.LM_KETS
         self.precision = _lib.LM_C32 if precision in ("c32", _lib.LM_C32) else _lib.LM_C64
         if tol is None:
-            tol = 1e-7 if self.precision == _lib.LM_C32 else 1e-12
+            tol = 1e-9 if self.precision == _lib.LM_C32 else 1e-12
         p = C.c_void_p()
         self.ctx.check(self.ctx.lib.lm_batch_create(self.ctx.handle, self.kind, self.precision, float(tol),
                                                     C.byref(p)))

