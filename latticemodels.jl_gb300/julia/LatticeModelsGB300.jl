@@ -190,6 +190,194 @@ function bond_currents(H::DeviceHamiltonian, st::DeviceState)
     return out
 end
 
-export ChebyshevGPU, DeviceLattice, DeviceState, gpu_tightbinding, bond_currents
+# ---- readout ring behind TimeSequence(f, ev(times)) (src/timesequence.jl:41-43) --------------
+# Readouts are computed into device ring slots and downloaded asynchronously; entries are taken
+# only when their slot is about to be reused, so the evolution never waits on a readout.
+mutable struct ReadoutRing
+    ctx::Context
+    handle::Ptr{Cvoid}
+    nslots::Int
+end
+function ReadoutRing(len::Integer, nslots::Integer=8; ctx=default_context())
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:lm_ring_create, LIB), Cint, (Ptr{Cvoid}, Cint, Int64, Ref{Ptr{Cvoid}}), ctx.handle, nslots, len, h),
+          ctx.handle)
+    r = ReadoutRing(ctx, h[], nslots)
+    finalizer(r -> ccall((:lm_ring_destroy, LIB), Cint, (Ptr{Cvoid},), r.handle), r)
+    return r
+end
+function push_density!(r::ReadoutRing, st::DeviceState, t)
+    seq = Ref{Int64}(0)
+    check(ccall((:lm_ring_push_localdensity, LIB), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Cdouble, Ref{Int64}),
+                r.handle, st.handle, t, seq), r.ctx.handle)
+    return seq[]
+end
+function push_currents!(r::ReadoutRing, H::DeviceHamiltonian, st::DeviceState, t)
+    seq = Ref{Int64}(0)
+    check(ccall((:lm_ring_push_currents, LIB), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Cdouble, Ref{Int64}),
+                r.handle, H.handle, st.handle, t, seq), r.ctx.handle)
+    return seq[]
+end
+function take!(r::ReadoutRing, seq::Integer, len::Integer)
+    out = Vector{Float64}(undef, len)
+    n = Ref{Int64}(0)
+    t = Ref{Cdouble}(0.0)
+    check(ccall((:lm_ring_wait, LIB), Cint, (Ptr{Cvoid}, Int64, Ptr{Float64}, Ptr{Cvoid}, Ref{Int64}, Ref{Cdouble}),
+                r.handle, seq, out, C_NULL, n, t), r.ctx.handle)
+    return t[], resize!(out, n[])
+end
+
+"""
+    gpu_timesequence(kind, ev_iter; nslots=8)
+
+`TimeSequence(moment -> localdensity(moment.state), ev_iter)` (`kind = :density`) or the bond
+currents of `DensityCurrents(moment.H, moment.state)` (`kind = :currents`), read out through a
+`ReadoutRing`.
+"""
+function gpu_timesequence(kind::Symbol, ev_iter; nslots=8)
+    ring = nothing
+    len = 0
+    pending = Int64[]
+    ts = Float64[]
+    vals = Vector{Vector{Float64}}()
+    for moment in ev_iter
+        st = moment.state.data::DeviceState
+        if ring === nothing
+            len = kind === :density ? st.n :
+                  Int(ccall((:lm_lattice_nbonds, LIB), Int64, (Ptr{Cvoid},), st.lat.handle))
+            ring = ReadoutRing(max(len, 1), nslots; ctx=st.lat.ctx)
+        end
+        if length(pending) == nslots
+            t, v = take!(ring, popfirst!(pending), len)
+            push!(ts, t); push!(vals, v)
+        end
+        push!(pending, kind === :density ? push_density!(ring, st, moment.t) :
+                                           push_currents!(ring, moment.H.data::DeviceHamiltonian, st, moment.t))
+    end
+    for seq in pending
+        t, v = take!(ring, seq, len)
+        push!(ts, t); push!(vals, v)
+    end
+    return LatticeModels.TimeSequence(ts, vals)
+end
+
+# ---- batches of uneven lattices (lm_batch_*) ---------------------------------------------------
+mutable struct GPUBatch
+    ctx::Context
+    handle::Ptr{Cvoid}
+    members::Vector{Any}  # keeps the Hamiltonians and states alive
+end
+function GPUBatch(kind::Cint, precision::Cint; tol=precision == LM_C32 ? 1e-9 : 1e-12, ctx=default_context())
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:lm_batch_create, LIB), Cint, (Ptr{Cvoid}, Cint, Cint, Cdouble, Ref{Ptr{Cvoid}}),
+                ctx.handle, kind, precision, tol, h), ctx.handle)
+    b = GPUBatch(ctx, h[], Any[])
+    finalizer(b -> ccall((:lm_batch_destroy, LIB), Cint, (Ptr{Cvoid},), b.handle), b)
+    return b
+end
+function Base.push!(b::GPUBatch, H::DeviceHamiltonian, st::DeviceState)
+    idx = Ref{Cint}(0)
+    check(ccall((:lm_batch_add, LIB), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ref{Cint}), b.handle, H.handle,
+                st.handle, idx), b.ctx.handle)
+    push!(b.members, (H, st))
+    return b
+end
+update!(b::GPUBatch, dt) = check(ccall((:lm_batch_update, LIB), Cint, (Ptr{Cvoid}, Cdouble), b.handle, dt), b.ctx.handle)
+step!(b::GPUBatch) = check(ccall((:lm_batch_step, LIB), Cint, (Ptr{Cvoid},), b.handle), b.ctx.handle)
+function tune!(b::GPUBatch; steps=2)
+    ms = Vector{Float64}(undef, 4)
+    best = Ref{Cint}(0)
+    check(ccall((:lm_batch_tune, LIB), Cint, (Ptr{Cvoid}, Cint, Ptr{Float64}, Ref{Cint}), b.handle, steps, ms, best),
+          b.ctx.handle)
+    return best[], ms
+end
+
+# ---- adjoint: ChainRulesCore rrule of a density loss (lm_adjoint_*) -----------------------------
+# loss(V, B) = sum_i (localdensity_i(T) - target_i)^2 after `nsteps` steps of dt under
+# gpu_tightbinding(l, V; field=PointFlux(B[j], point)), B piecewise constant over `spi` steps.
+# The forward pass keeps a checkpoint every `every` steps; the pullback recomputes each segment,
+# runs lm_adjoint_step per step and propagates the co-state with a solver at -dt.  This mirrors
+# DensityLossAdjoint of the Python host (latticemodels.jl_gb300/lmgpu/adjoint.py) call for call.
+struct DensityLossProblem
+    lat::DeviceLattice
+    psi0::Matrix{ComplexF64}
+    target::Vector{Float64}
+    dt::Float64
+    nsteps::Int
+    spi::Int
+    point::NTuple{2,Float64}
+    precision::Cint
+    every::Int
+    bounds::NTuple{2,Float64}
+end
+
+function _loss_and_grad(p::DensityLossProblem, V::Vector{Float64}, B::Vector{Float64})
+    ctx = p.lat.ctx
+    tol = p.precision == LM_C32 ? 1e-9 : 1e-12
+    fwd, bwd = ChebyshevGPU(; tol=tol, ctx=ctx), ChebyshevGPU(; tol=tol, ctx=ctx)
+    for s in (fwd, bwd)
+        check(ccall((:lm_solver_set_bounds, LIB), Cint, (Ptr{Cvoid}, Cdouble, Cdouble), s.handle, p.bounds...),
+              ctx.handle)
+    end
+    H = gpu_tightbinding(p.lat, V; field=PointFlux(B[1], p.point))
+    n, m = size(p.psi0)
+    adj = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:lm_adjoint_create, LIB), Cint, (Ptr{Cvoid}, Int64, Int64, Cint, Cint, Ref{Ptr{Cvoid}}),
+                ctx.handle, n, m, p.precision, length(B), adj), ctx.handle)
+    try
+        stepwith!(s, amp, dt, st) = (H.amplitudes[1] = amp; update_solver!(s, H, dt); step!(s, st, nothing))
+        psi = DeviceState(p.lat, p.psi0; precision=p.precision)
+        cps = [copy(psi)]
+        for k in 1:p.nsteps
+            stepwith!(fwd, B[(k - 1) ÷ p.spi + 1], p.dt, psi)
+            k % p.every == 0 && k < p.nsteps && push!(cps, copy(psi))
+        end
+        lam = DeviceState(p.lat, zeros(ComplexF64, n, m); precision=p.precision)
+        loss = Ref{Cdouble}(0.0)
+        check(ccall((:lm_adjoint_seed, LIB), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Float64}, Ptr{Cvoid}, Ref{Cdouble}),
+                    adj[], psi.handle, p.target, lam.handle, loss), ctx.handle)
+        check(ccall((:lm_adjoint_reset, LIB), Cint, (Ptr{Cvoid},), adj[]), ctx.handle)
+        for c in length(cps):-1:1
+            n0 = (c - 1) * p.every
+            n1 = min(p.nsteps, n0 + p.every)
+            seg = [copy(cps[c])]
+            for k in n0+1:n1-1
+                nxt = copy(seg[end])
+                stepwith!(fwd, B[(k - 1) ÷ p.spi + 1], p.dt, nxt)
+                push!(seg, nxt)
+            end
+            for k in n1:-1:n0+1
+                j = (k - 1) ÷ p.spi + 1
+                H.amplitudes[1] = B[j]
+                update_solver!(fwd, H, p.dt)
+                check(ccall((:lm_adjoint_step, LIB), Cint,
+                            (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Cint, Cint, Ptr{Cvoid}, Ptr{Cvoid}),
+                            adj[], fwd.handle, H.handle, 0, j - 1, seg[k - n0].handle, lam.handle), ctx.handle)
+                stepwith!(bwd, B[j], -p.dt, lam)
+            end
+        end
+        gV = Vector{Float64}(undef, n)
+        gB = Vector{Float64}(undef, length(B))
+        check(ccall((:lm_adjoint_gradients, LIB), Cint, (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}), adj[], gV, gB),
+              ctx.handle)
+        return loss[], gV, gB
+    finally
+        ccall((:lm_adjoint_destroy, LIB), Cint, (Ptr{Cvoid},), adj[])
+    end
+end
+
+density_loss(V, B, p::DensityLossProblem) = _loss_and_grad(p, Vector{Float64}(V), Vector{Float64}(B))[1]
+
+# ChainRulesCore is a weak dependency: this block is an extension (ext/ChainRulesCoreExt.jl in a
+# package layout) so LatticeModels does not depend on it.
+import ChainRulesCore
+function ChainRulesCore.rrule(::typeof(density_loss), V, B, p::DensityLossProblem)
+    loss, gV, gB = _loss_and_grad(p, Vector{Float64}(V), Vector{Float64}(B))
+    pullback(dl) = (ChainRulesCore.NoTangent(), dl .* gV, dl .* gB, ChainRulesCore.NoTangent())
+    return loss, pullback
+end
+
+export ChebyshevGPU, DeviceLattice, DeviceState, gpu_tightbinding, bond_currents, ReadoutRing,
+       gpu_timesequence, GPUBatch, DensityLossProblem, density_loss
 
 end # module
