@@ -311,9 +311,12 @@ def run_adjoint_workload(args):
     V = rng.uniform(-0.1, 0.1, L * L)
     B = np.full(50, 0.1)
     lat = lmgpu.SquareLattice(L, L)
-    w, vecs = lmgpu.diagonalize(lmgpu.tightbinding_hamiltonian(lat, V, field=lmgpu.PointFlux(B[0], point)))
-    psi0 = vecs[:, :M].cpu().numpy()
-    del vecs
+    if args.adjoint_init == "random":  # same cost, no cuSOLVER (profilers that cannot load it)
+        psi0 = (rng.standard_normal((L * L, M)) + 1j * rng.standard_normal((L * L, M))) / math.sqrt(2 * L * L)
+    else:
+        w, vecs = lmgpu.diagonalize(lmgpu.tightbinding_hamiltonian(lat, V, field=lmgpu.PointFlux(B[0], point)))
+        psi0 = vecs[:, :M].cpu().numpy()
+        del vecs
     c = rng.uniform(20, 44, size=2)
     r2 = ((lat.coords() - c) ** 2).sum(axis=1)
     target = 0.5 + 0.2 * np.exp(-r2 / (2 * 6.0 ** 2))
@@ -336,7 +339,8 @@ def run_adjoint_workload(args):
     line = {"metric": "forward ket-steps/s of loss_and_grad (forward + checkpointed adjoint)",
             "value": M * nsteps / (ms / 1000.0), "unit": "ket-steps/s", "n_gpus": 1, "steps": reps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "dtype": args.precision,
-            "data": "synthetic (seeded; psi_0 = lowest eigenstates of h(V0) from cuSOLVER eigh)",
+            "data": ("synthetic (seeded; psi_0 = lowest eigenstates of h(V0) from cuSOLVER eigh)"
+                     if args.adjoint_init == "eigh" else "synthetic (seeded; psi_0 = random complex-Gaussian kets)"),
             "config": {"workload": ADJOINT_WORKLOAD, "N": L * L, "M": M, "tol": prob.tol,
                        "step_unit": "one loss_and_grad"},
             "loss": loss, "grad_norm_V": float(np.linalg.norm(gV)), "grad_norm_B": float(np.linalg.norm(gB)),
@@ -359,6 +363,8 @@ def main():
                          "adjoint: loss_and_grad of the 64^2 differentiation workload")
     ap.add_argument("--instances", type=int, default=512)
     ap.add_argument("--precision", default="c32", choices=["c32", "c64"])
+    ap.add_argument("--adjoint-init", default="eigh", choices=["eigh", "random"],
+                    help="initial kets of the adjoint workload: lowest eigenstates (default) or random")
     ap.add_argument("--tol32", type=float, default=1e-9,
                     help="series truncation of the FP32 form (1e-9 keeps 200-step runs within 1e-6; "
                          "1e-7 is one order cheaper and enough for short runs)")
