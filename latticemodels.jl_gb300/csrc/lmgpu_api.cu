@@ -138,6 +138,13 @@ void make_coefs(const std::vector<double>& J, int K, double sgn, std::vector<Che
         out[(size_t)k] = c;
     }
 }
+bool ham_x_real(const lm_ham* h) {
+    if (h->lat->g.per_x && h->lat->g.twist_x != 0.0) return false;
+    for (int c = 0; c < h->fields.n; ++c)
+        if (h->fields.c[c].kind != LM_FIELD_LANDAU) return false;  // (x1+x2)(y2-y1)B/2 = 0 on x-bonds
+    return true;
+}
+
 ChebLo cheb_lo(double ph_re, double ph_im, double c0, double s1, bool fused) {
     typedef std::complex<double> cd;
     const cd ph(ph_re, ph_im);
@@ -845,7 +852,7 @@ static int cheb_apply(lm_solver* s, const Geom& g, int precision, int site_fast,
     if (ctx->fused && site_fast && !conj && fused_supported(precision, K) && fused_supported_geom(g)) {
         // whole series in one temporally blocked pass; result lands in A
         CUDA_TRY(ctx, launch_cheb_fused_c32(ctx, g, (const float2*)hop2, (const float*)diag2, (const float2*)S,
-                                            (float2*)A, ld, m, K, s->coef.data(), pr, pi),
+                                            (float2*)A, ld, m, K, ham_x_real(s->ham), s->coef.data(), pr, pi),
                  "fused chebyshev step");
         if (ctx->timing) {
             CUDA_TRY(ctx, cudaEventRecord(t1, ctx->stream), "cudaEventRecord");

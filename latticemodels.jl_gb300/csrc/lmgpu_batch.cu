@@ -341,11 +341,19 @@ static cudaError_t launch_transpose(lm_batch* b, const TransInst* table) {
     return cudaGetLastError();
 }
 
+// Real x-hops in every instance: the fused launch takes the 2-FMA x-neighbour form.
+static bool batch_x_real(const lm_batch* b) {
+    for (const lm_ham* h : b->hams)
+        if (!ham_x_real(h)) return false;
+    return true;
+}
+
 static cudaError_t launch_fused_pass(lm_batch* b, int p, int q) {
     lm_ctx* ctx = b->ctx;
     cudaError_t e = cudaMemsetAsync(b->dqueue + q, 0, sizeof(unsigned long long), ctx->stream);
     if (e != cudaSuccess) return e;
-    return launch_fused_table(ctx, b->K, nullptr, b->df[p], (int)b->states.size(), b->f_items, b->dqueue + q, 0);
+    return launch_fused_table(ctx, b->K, batch_x_real(b), nullptr, b->df[p], (int)b->states.size(), b->f_items,
+                              b->dqueue + q, 0);
 }
 
 // Enqueues one step for parity p; returns whether the data moves to the other buffer.
@@ -482,7 +490,7 @@ int lm_batch_step(lm_batch* b) {
     const int p = b->parity;
     int moved = 0;
     if (b->cfg == 0) {  // kernel attributes are set outside any stream capture
-        int rc = check_cuda(ctx, ensure_fused_attr(ctx, b->K), "lm_batch_step: kernel attribute");
+        int rc = check_cuda(ctx, ensure_fused_attr(ctx, b->K, batch_x_real(b)), "lm_batch_step: kernel attribute");
         if (rc != LM_OK) return rc;
     }
     if (b->use_graph) {

@@ -170,7 +170,9 @@ __device__ __forceinline__ void load_desc(FusedInst* dst, const FusedInst* src, 
     if (t < DESC_WORDS) reinterpret_cast<int*>(dst)[t] = __ldg(reinterpret_cast<const int*>(src) + t);
 }
 
-template <int K>
+// XR: every x-hop of every instance is real (Landau gauge or no field, no twist across x), so
+// the x-neighbour terms take 2 FMAs instead of 4.
+template <int K, bool XR>
 __global__ void __launch_bounds__(NTHR, 1)
 cheb_fused_c32_kernel(FusedInst single, const FusedInst* __restrict__ table, int ninst, int64_t nitems,
                       unsigned long long* queue) {
@@ -324,10 +326,17 @@ cheb_fused_c32_kernel(FusedInst single, const FusedInst* __restrict__ table, int
                             const float2 vym = (j > 0) ? t1[kk][j - 1] : up;
                             const float2 hym = (j > 0) ? make_float2(hy[j - 1].x, -hy[j - 1].y) : hym0;
                             float2 acc = (k == 1) ? make_float2(0.f, 0.f) : make_float2(-t0[j].x, -t0[j].y);
-                            acc.x = fmaf(hx[j].x, vxp[j].x, acc.x); acc.x = fmaf(-hx[j].y, vxp[j].y, acc.x);
-                            acc.y = fmaf(hx[j].x, vxp[j].y, acc.y); acc.y = fmaf(hx[j].y, vxp[j].x, acc.y);
-                            acc.x = fmaf(hxm[j].x, vxm[j].x, acc.x); acc.x = fmaf(-hxm[j].y, vxm[j].y, acc.x);
-                            acc.y = fmaf(hxm[j].x, vxm[j].y, acc.y); acc.y = fmaf(hxm[j].y, vxm[j].x, acc.y);
+                            if (XR) {
+                                acc.x = fmaf(hx[j].x, vxp[j].x, acc.x);
+                                acc.y = fmaf(hx[j].x, vxp[j].y, acc.y);
+                                acc.x = fmaf(hxm[j].x, vxm[j].x, acc.x);
+                                acc.y = fmaf(hxm[j].x, vxm[j].y, acc.y);
+                            } else {
+                                acc.x = fmaf(hx[j].x, vxp[j].x, acc.x); acc.x = fmaf(-hx[j].y, vxp[j].y, acc.x);
+                                acc.y = fmaf(hx[j].x, vxp[j].y, acc.y); acc.y = fmaf(hx[j].y, vxp[j].x, acc.y);
+                                acc.x = fmaf(hxm[j].x, vxm[j].x, acc.x); acc.x = fmaf(-hxm[j].y, vxm[j].y, acc.x);
+                                acc.y = fmaf(hxm[j].x, vxm[j].y, acc.y); acc.y = fmaf(hxm[j].y, vxm[j].x, acc.y);
+                            }
                             acc.x = fmaf(hy[j].x, vyp.x, acc.x); acc.x = fmaf(-hy[j].y, vyp.y, acc.x);
                             acc.y = fmaf(hy[j].x, vyp.y, acc.y); acc.y = fmaf(hy[j].y, vyp.x, acc.y);
                             acc.x = fmaf(hym.x, vym.x, acc.x); acc.x = fmaf(-hym.y, vym.y, acc.x);
@@ -417,52 +426,62 @@ void fused_fill_coef(FusedInst& d, int K, const ChebCoef* coef, double ph_re, do
     d.lo = cheb_lo(ph_re, ph_im, coef[0].s, coef[1].s, true);
 }
 
-cudaError_t ensure_fused_attr(lm_ctx* ctx, int K) {
-    if (ctx->fused_attr & (1u << K)) return cudaSuccess;
-    cudaError_t e = cudaErrorInvalidValue;
+template <bool XR>
+static cudaError_t set_fused_attr(int K) {
     switch (K) {
-#define LM_ATTR_CASE(KK)                                                                                        \
-    case KK:                                                                                                  \
-        e = cudaFuncSetAttribute(cheb_fused_c32_kernel<KK>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES); \
-        break;
+#define LM_ATTR_CASE(KK) \
+    case KK:             \
+        return cudaFuncSetAttribute(cheb_fused_c32_kernel<KK, XR>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
         LM_ATTR_CASE(2) LM_ATTR_CASE(3) LM_ATTR_CASE(4) LM_ATTR_CASE(5)
         LM_ATTR_CASE(6) LM_ATTR_CASE(7) LM_ATTR_CASE(8)
 #undef LM_ATTR_CASE
         default:
-            break;
+            return cudaErrorInvalidValue;
     }
-    if (e == cudaSuccess) ctx->fused_attr |= 1u << K;
+}
+
+cudaError_t ensure_fused_attr(lm_ctx* ctx, int K, bool xreal) {
+    const unsigned bit = 1u << (K + (xreal ? 16 : 0));
+    if (ctx->fused_attr & bit) return cudaSuccess;
+    const cudaError_t e = xreal ? set_fused_attr<true>(K) : set_fused_attr<false>(K);
+    if (e == cudaSuccess) ctx->fused_attr |= bit;
     return e;
 }
 
-cudaError_t launch_fused_table(lm_ctx* ctx, int K, const FusedInst* single, const FusedInst* d_table, int ninst,
-                               int64_t nitems, unsigned long long* d_queue, int grid) {
-    if (nitems <= 0) return cudaSuccess;
-    if (grid <= 0) grid = ctx->sm_count > 0 ? ctx->sm_count : 152;
-    if (grid > nitems) grid = (int)nitems;
-    FusedInst one{};
-    if (single) one = *single;
-    cudaError_t e = cudaSuccess;
+template <bool XR>
+static cudaError_t launch_fused_k(lm_ctx* ctx, int K, int grid, const FusedInst& one, const FusedInst* d_table,
+                                  int ninst, int64_t nitems, unsigned long long* d_queue) {
     switch (K) {
-#define LM_FUSED_CASE(KK)                                                                                        \
-    case KK:                                                                                                   \
-        e = ensure_fused_attr(ctx, KK);                                                                        \
-        if (e != cudaSuccess) return e;                                                                        \
-        cheb_fused_c32_kernel<KK><<<(unsigned)grid, NTHR, SMEM_BYTES, ctx->stream>>>(one, d_table, ninst, nitems, \
-                                                                                     d_queue);                 \
-        break;
+#define LM_FUSED_CASE(KK)                                                                                   \
+    case KK:                                                                                              \
+        cheb_fused_c32_kernel<KK, XR><<<(unsigned)grid, NTHR, SMEM_BYTES, ctx->stream>>>(one, d_table, ninst, \
+                                                                                         nitems, d_queue);   \
+        return cudaGetLastError();
         LM_FUSED_CASE(2) LM_FUSED_CASE(3) LM_FUSED_CASE(4) LM_FUSED_CASE(5)
         LM_FUSED_CASE(6) LM_FUSED_CASE(7) LM_FUSED_CASE(8)
 #undef LM_FUSED_CASE
         default:
             return cudaErrorInvalidValue;
     }
+}
+
+cudaError_t launch_fused_table(lm_ctx* ctx, int K, bool xreal, const FusedInst* single, const FusedInst* d_table,
+                               int ninst, int64_t nitems, unsigned long long* d_queue, int grid) {
+    if (nitems <= 0) return cudaSuccess;
+    if (grid <= 0) grid = ctx->sm_count > 0 ? ctx->sm_count : 152;
+    if (grid > nitems) grid = (int)nitems;
+    FusedInst one{};
+    if (single) one = *single;
+    cudaError_t e = ensure_fused_attr(ctx, K, xreal);
+    if (e != cudaSuccess) return e;
+    e = xreal ? launch_fused_k<true>(ctx, K, grid, one, d_table, ninst, nitems, d_queue)
+              : launch_fused_k<false>(ctx, K, grid, one, d_table, ninst, nitems, d_queue);
     ctx->launches++;
-    return cudaGetLastError();
+    return e;
 }
 
 cudaError_t launch_cheb_fused_c32(lm_ctx* ctx, const Geom& g, const float2* hop2, const float* diag2,
-                                  const float2* x, float2* out, int64_t ld, int64_t m, int K,
+                                  const float2* x, float2* out, int64_t ld, int64_t m, int K, bool xreal,
                                   const ChebCoef* coef, double ph_re, double ph_im) {
     FusedInst d{};
     d.g = g;
@@ -475,7 +494,7 @@ cudaError_t launch_cheb_fused_c32(lm_ctx* ctx, const Geom& g, const float2* hop2
     d.item_begin = 0;
     const int64_t nitems = fused_items(g, K, m, &d.ntx, &d.nty);
     fused_fill_coef(d, K, coef, ph_re, ph_im);
-    return launch_fused_table(ctx, K, &d, nullptr, 1, nitems, nullptr, 0);
+    return launch_fused_table(ctx, K, xreal, &d, nullptr, 1, nitems, nullptr, 0);
 }
 
 }  // namespace lmgpu

@@ -96,7 +96,7 @@ struct lm_ctx {
     std::string err;
     int timing = 0;
     int fused = 1;                      // LM_OPT_FUSED: temporally blocked c32 step enabled
-    unsigned fused_attr = 0;            // bit K: shared-memory attribute of the K-order kernel set
+    unsigned fused_attr = 0;            // bit K (+16 for real x-hops): shared-memory attribute set
     std::vector<cudaEvent_t> ev_pool;   // pairs (start, stop) of timed Chebyshev sweeps
     std::vector<int> ev_launches;       // launches covered by each recorded pair
     size_t ev_used = 0;                 // pairs recorded but not yet resolved
@@ -209,12 +209,15 @@ int64_t fused_items(const Geom& g, int K, int64_t m, int* ntx, int* nty);
 void fused_fill_coef(FusedInst& d, int K, const ChebCoef* coef, double ph_re, double ph_im);
 // One launch over `nitems` work items of one instance (`single`) or of a device table of
 // `ninst` instances pulled from the work-queue counter `d_queue` (zeroed before the launch).
-cudaError_t launch_fused_table(lm_ctx* ctx, int K, const FusedInst* single, const FusedInst* d_table, int ninst,
-                               int64_t nitems, unsigned long long* d_queue, int grid);
-cudaError_t ensure_fused_attr(lm_ctx* ctx, int K);
+cudaError_t launch_fused_table(lm_ctx* ctx, int K, bool xreal, const FusedInst* single, const FusedInst* d_table,
+                               int ninst, int64_t nitems, unsigned long long* d_queue, int grid);
+cudaError_t ensure_fused_attr(lm_ctx* ctx, int K, bool xreal);
 cudaError_t launch_cheb_fused_c32(lm_ctx* ctx, const Geom& g, const float2* hop2, const float* diag2,
-                                  const float2* x, float2* out, int64_t ld, int64_t m, int K,
+                                  const float2* x, float2* out, int64_t ld, int64_t m, int K, bool xreal,
                                   const ChebCoef* coef, double ph_re, double ph_im);
+// Every x-hop of H is real: Landau-gauge field components only (or none) and no twist across
+// a periodic x axis.  The fused kernel then skips the imaginary parts of the x-hops.
+bool ham_x_real(const lm_ham* h);
 cudaError_t launch_convert(lm_ctx* ctx, int to_precision, const void* src, void* dst, int64_t n,
                            int64_t m, int64_t ld_src, int64_t ld_dst);
 

@@ -341,3 +341,24 @@ def test_fp32_long_run_keeps_norm(lm, fused):
     assert np.abs(n64 - 1).max() <= 1e-12
     assert np.abs(n32 - 1).max() <= 5e-7
     assert rel(rho32, rho64) <= 1e-6
+
+
+def test_fused_real_x_hops_bit_identical(lm):
+    """Landau-gauge x-hops are real, so the fused kernel skips their imaginary parts.  Adding a
+    zero point flux keeps H identical but forces the general (complex x-hop) kernel: the two
+    results must agree bit for bit."""
+    L, M, dt = 64, 24, 0.05
+    ll = lm.SquareLattice(L, L, boundaries={"axis1": True, "axis2": True})
+    V = o.anderson_disorder(L * L, 2.0, 31)
+    X = o.random_kets(L * L, M, 32)
+    outs = []
+    for field in (lm.LandauGauge(0.02),
+                  lm.FieldSum([lm.LandauGauge(0.02), lm.PointFlux(0.0, (10.5, 20.5), "singular")])):
+        H = lm.tightbinding_hamiltonian(ll, V, field=field)
+        st = lm.KetBlock(ll, X, precision="c32")
+        s = lm.ChebyshevGPU()
+        s.update_solver(H, dt)
+        for _ in range(3):
+            s.step(st)
+        outs.append(st.to_numpy())
+    assert np.array_equal(outs[0], outs[1])
