@@ -350,6 +350,56 @@ def run_adjoint_workload(args):
 
 
 # ------------------------------------------------------------------------------------------
+KPM_WORKLOAD = ("SquareLattice(256,256) periodic x/y, t1=1, LandauGauge(0.01), Anderson U[-1,1], "
+                "256 random-phase vectors, 2048 Chebyshev moments (FP64)")
+
+
+def run_kpm_workload(args):
+    """Chebyshev moments for the KPM density of states: 1024 stencil passes over a 256-vector
+    block (doubling relations), FP64.  `value` = vector-moments per second."""
+    import torch
+    import lmgpu
+    ctx = lmgpu.default_context()
+    ext = torch.cuda.ExternalStream(ctx.stream_ptr(), device=torch.device("cuda", 0))
+    lat = lmgpu.SquareLattice(LX, LY, boundaries={"axis1": True, "axis2": True})
+    N, R, nmom = lat.N, 256, 2048
+    H = lmgpu.tightbinding_hamiltonian(lat, make_disorder(N), field=lmgpu.LandauGauge(B_FIELD))
+    vecs = lmgpu.DeviceState(lat, lmgpu.kpm._phase_vectors(N, R, SEED), 0, "c64")
+    bounds = lmgpu.kpm._bounds(H, ctx)
+    for _ in range(max(1, args.warmup // 3)):
+        lmgpu.kpm.moments(H, 64, vecs, bounds=bounds)
+    reps = max(1, min(args.steps, 3))
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    clk = ClockSampler(0)
+    clk.start()
+    e0.record(ext)
+    for _ in range(reps):
+        mu, _ = lmgpu.kpm.moments(H, nmom, vecs, bounds=bounds)
+    e1.record(ext)
+    e1.synchronize()
+    clocks = clk.stop()
+    ms = e0.elapsed_time(e1) / reps
+    passes = (nmom + 1) // 2 + 1
+    # per pass: the recurrence reads T_{n+1} and T_n and writes T_{n+2}; the two dot products
+    # read T_n (twice) and T_{n+1}: six block passes of N*R*16 bytes
+    alg = 6.0 * N * R * 16 * passes
+    peak, peak_kind = measured_peak_hbm()
+    line = {"metric": "KPM vector-moments/s (FP64 Chebyshev moments)", "value": R * nmom / (ms / 1000.0),
+            "unit": "vector-moments/s", "n_gpus": 1, "steps": reps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "dtype": "c64", "data": "synthetic (seeded PCG64 random-phase vectors)",
+            "config": {"workload": KPM_WORKLOAD, "N": N, "vectors": R, "moments": nmom, "passes": passes,
+                       "step_unit": "one lm_kpm_moments call"},
+            "roofline": {"bound": "hbm", "achieved": alg / (ms / 1000.0) / 1e9, "peak": peak, "unit": "GB/s",
+                         "frac": alg / (ms / 1000.0) / 1e9 / peak, "traffic": None,
+                         "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
+                         "alg_bytes_per_call": alg, "note": "whole call (recurrence + dot kernels)"},
+            "mu0_over_N": float(mu[0] / (N * R)), "clocks": clocks}
+    print(json.dumps(line))
+    return 0
+
+
+# ------------------------------------------------------------------------------------------
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -358,9 +408,9 @@ def main():
     ap.add_argument("--impl", default="lmgpu", choices=["lmgpu", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--kets", type=int, default=M_KETS)
-    ap.add_argument("--workload", default="kets", choices=["kets", "batch", "adjoint"],
+    ap.add_argument("--workload", default="kets", choices=["kets", "batch", "adjoint", "kpm"],
                     help="kets: the 256^2 ket-block workload (default); batch: 512 uneven dense-P lattices; "
-                         "adjoint: loss_and_grad of the 64^2 differentiation workload")
+                         "adjoint: loss_and_grad of the 64^2 differentiation workload; kpm: DOS moments")
     ap.add_argument("--instances", type=int, default=512)
     ap.add_argument("--precision", default="c32", choices=["c32", "c64"])
     ap.add_argument("--adjoint-init", default="eigh", choices=["eigh", "random"],
@@ -377,6 +427,8 @@ def main():
         return run_batch_workload(args)
     if args.workload == "adjoint":
         return run_adjoint_workload(args)
+    if args.workload == "kpm":
+        return run_kpm_workload(args)
 
     rank, world, local = dist_info()
     import torch

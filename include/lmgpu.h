@@ -231,6 +231,17 @@ int lm_bond_currents(lm_ham *ham, lm_state *st, double *out);
 /* tr(P) = sum of the local densities, FP64 (particle number). */
 int lm_trace(lm_state *st, double *out);
 
+/* ---- KPM moments (DOS / LDOS without an eigensystem; the reference computes dos and ldos
+ * from an Eigensystem or GreenFunction, src/greenfunction.jl:306-339) ------------------------ */
+/* mu_n = sum over the columns v of the block of <v| T_n(H~) |v>, H~ = (H - b)/a with
+ * [b - a, b + a] = [emin, emax], which must enclose the spectrum (LM_ERR_NONFINITE when the
+ * moments show that it does not), n = 0..nmom-1, in FP64.  vecs: a ComplexF64 ket block of
+ * starting vectors (stochastic trace), or NULL for the N unit vectors (exact trace; N x N
+ * scratch).  per_column = 0: out[n] sums the columns; otherwise out[j*nmom + n] holds column j
+ * (with unit vectors: the local moments of site j).  Extension of the reference. */
+int lm_kpm_moments(lm_ham *ham, double emin, double emax, int nmom, const lm_state *vecs, int per_column,
+                   double *out);
+
 /* ---- readout ring (device side of TimeSequence(f, ev(times)), src/timesequence.jl:41-43) -- */
 /* Per-moment readouts computed into the slots of a device ring and downloaded asynchronously
  * into pinned host memory: pushing never waits for the device, so an evolution loop that

@@ -81,6 +81,27 @@ __global__ void __launch_bounds__(256) adj_recur_kernel(Geom g, const typename C
     }
 }
 
+// out = alpha (2H~) tp - tpp + w lam over an n x M block (the three-term Chebyshev recurrence
+// and its adjoint; KPM uses it for the moments).  out may alias tpp.
+cudaError_t launch_stencil_recur(lm_ctx* ctx, const Geom& g, int precision, const void* hop2, const void* diag2,
+                                 const void* tp, const void* tpp, const void* lam, void* out, int64_t ld, int64_t M,
+                                 double alpha, double wre, double wim) {
+    if (M <= 0 || g.N <= 0) return cudaSuccess;
+    const dim3 grid((unsigned)((g.N + 255) / 256), (unsigned)(M < 65535 ? M : 65535));
+    if (precision == LM_C64)
+        adj_recur_kernel<double><<<grid, 256, 0, ctx->stream>>>(g, (const double2*)hop2, (const double*)diag2,
+                                                                (const double2*)tp, (const double2*)tpp,
+                                                                (const double2*)lam, (double2*)out, ld, M, alpha, wre,
+                                                                wim);
+    else
+        adj_recur_kernel<float><<<grid, 256, 0, ctx->stream>>>(g, (const float2*)hop2, (const float*)diag2,
+                                                               (const float2*)tp, (const float2*)tpp,
+                                                               (const float2*)lam, (float2*)out, ld, M, (float)alpha,
+                                                               (float)wre, (float)wim);
+    ctx->launches++;
+    return cudaGetLastError();
+}
+
 // Gradient terms of order k, per site s, with sums over all kets m:
 //   gV[s] += f Re( ph * sum_m conj(beta_sm) T_sm )
 //   gA    += f Re( ph * sum_s sum_e [ D[s,j] S1 + conj(D[s,j]) S2 ] ),  j = s + e,
@@ -408,21 +429,9 @@ int lm_adjoint_step(lm_adjoint* a, lm_solver* s, lm_ham* h, int component, int s
     const void* hop2 = f64 ? (const void*)s->d_hop2 : (const void*)s->d_hop2f;
     const void* diag2 = f64 ? (const void*)s->d_diag2 : (const void*)s->d_diag2f;
     const int64_t ld = psi->ld, M = a->m;
-    dim3 grid((unsigned)((g.N + 255) / 256), (unsigned)(M < 65535 ? M : 65535));
     auto recur = [&](const void* tp, const void* tpp, const void* lamp, void* out, double alpha, double wre,
                      double wim) -> cudaError_t {
-        if (f64)
-            adj_recur_kernel<double><<<grid, 256, 0, ctx->stream>>>(g, (const double2*)hop2, (const double*)diag2,
-                                                                    (const double2*)tp, (const double2*)tpp,
-                                                                    (const double2*)lamp, (double2*)out, ld, M, alpha,
-                                                                    wre, wim);
-        else
-            adj_recur_kernel<float><<<grid, 256, 0, ctx->stream>>>(g, (const float2*)hop2, (const float*)diag2,
-                                                                   (const float2*)tp, (const float2*)tpp,
-                                                                   (const float2*)lamp, (float2*)out, ld, M, (float)alpha,
-                                                                   (float)wre, (float)wim);
-        ctx->launches++;
-        return cudaGetLastError();
+        return launch_stencil_recur(ctx, g, a->precision, hop2, diag2, tp, tpp, lamp, out, ld, M, alpha, wre, wim);
     };
     // T_0 = psi_n (aliased), T_1 = H~ T_0, T_k = 2 H~ T_{k-1} - T_{k-2}  (k < K)
     a->T[0] = psi->d_data;

@@ -1,0 +1,171 @@
+// Kernel polynomial method: Chebyshev moments of the tight-binding Hamiltonian on the device,
+// for the density of states and the local density of states without a full eigensystem (the
+// reference computes dos / ldos from an Eigensystem or a GreenFunction, src/greenfunction.jl:
+// 306-339).  The moments of a block of starting vectors v are
+//   mu_n = sum_v <v| T_n(H~) |v>,   H~ = (H - b)/a,
+// from the recurrence T_{n+1} = 2 H~ T_n - T_{n-1} on the block and the doubling relations
+//   mu_2n = 2 <T_n v|T_n v> - mu_0,   mu_2n+1 = 2 <T_n+1 v|T_n v> - mu_1,
+// so nmom moments take about nmom / 2 stencil passes.  With the N unit vectors as the block
+// the sum is the exact trace and column j gives the local moments of site j.
+#include <cuda_runtime.h>
+#include <math.h>
+
+#include <new>
+#include <utility>
+#include <vector>
+
+#include "lmgpu_internal.cuh"
+
+namespace lmgpu {
+
+// A = identity (n x n, leading dimension ld).
+__global__ void set_identity_kernel(double2* __restrict__ a, int64_t n, int64_t ld) {
+    for (int64_t col = blockIdx.y; col < n; col += gridDim.y)
+        for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+            a[col * ld + i] = make_double2(i == col ? 1.0 : 0.0, 0.0);
+}
+
+// out[col] = Re sum_i conj(A[i, col]) B[i, col], one block per column (fixed-order reduction).
+__global__ void __launch_bounds__(256) column_dots_kernel(const double2* __restrict__ A, const double2* __restrict__ B,
+                                                          int64_t n, int64_t ld, int64_t M, double* __restrict__ out) {
+    __shared__ double red[8];
+    for (int64_t col = blockIdx.x; col < M; col += gridDim.x) {
+        const double2* a = A + col * ld;
+        const double2* b = B + col * ld;
+        double acc = 0.0;
+        for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+            const double2 x = a[i], y = b[i];
+            acc = fma(x.x, y.x, fma(x.y, y.y, acc));
+        }
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double t = 0.0;
+            for (int w = 0; w < 8; ++w) t += red[w];
+            out[col] = t;
+        }
+        __syncthreads();
+    }
+}
+
+}  // namespace lmgpu
+
+using namespace lmgpu;
+
+extern "C" {
+
+int lm_kpm_moments(lm_ham* h, double emin, double emax, int nmom, const lm_state* vecs, int per_column,
+                   double* out) {
+    if (!h) return LM_ERR_ARG;
+    lm_ctx* ctx = h->ctx;
+    CHECK_ARG(ctx, out != nullptr, "lm_kpm_moments: null output");
+    CHECK_ARG(ctx, nmom >= 1, "lm_kpm_moments: need at least one moment");
+    CHECK_ARG(ctx, isfinite(emin) && isfinite(emax) && emax > emin, "lm_kpm_moments: need emin < emax");
+    if (!h->assembled) return set_err(ctx, LM_ERR_STATE, "lm_kpm_moments: Hamiltonian not assembled");
+    const Geom& g = h->lat->g;
+    const int64_t N = g.N;
+    if (vecs) {
+        CHECK_ARG(ctx, vecs->ctx == ctx && vecs->n == N, "lm_kpm_moments: vectors do not match the lattice");
+        CHECK_ARG(ctx, vecs->kind == LM_KETS && vecs->precision == LM_C64,
+                  "lm_kpm_moments: vectors must be a ComplexF64 ket block");
+    }
+    const int64_t M = vecs ? vecs->m : N;
+    const int64_t ld = vecs ? vecs->ld : N;
+    const double a = 0.5 * (emax - emin), b = 0.5 * (emax + emin);
+    const int64_t nsteps = (nmom + 1) / 2;  // recurrence passes: T_0 .. T_nsteps
+    cudaSetDevice(ctx->device);
+
+    double2* hop2 = nullptr;
+    double* diag2 = nullptr;
+    float2* hop2f = nullptr;
+    float* diag2f = nullptr;
+    double2* TA = nullptr;
+    double2* TB = nullptr;
+    double* dots = nullptr;
+    const size_t blk = sizeof(double2) * (size_t)ld * (size_t)M;
+    const size_t ndots = (size_t)(nsteps + 1) * 2 * (size_t)M;
+    auto release = [&]() {
+        cudaStreamSynchronize(ctx->stream);
+        cudaFree(hop2); cudaFree(diag2); cudaFree(hop2f); cudaFree(diag2f);
+        cudaFree(TA); cudaFree(TB); cudaFree(dots);
+    };
+    cudaError_t e = cudaMalloc((void**)&hop2, sizeof(double2) * 2 * (size_t)N);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&diag2, sizeof(double) * (size_t)N);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&hop2f, sizeof(float2) * 2 * (size_t)N);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&diag2f, sizeof(float) * (size_t)N);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&TA, blk);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&TB, blk);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&dots, sizeof(double) * ndots);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        release();
+        return check_cuda(ctx, e, "lm_kpm_moments: allocation");
+    }
+    auto fail = [&](cudaError_t err, const char* what) {
+        const int rc = check_cuda(ctx, err, what);
+        release();
+        return rc;
+    };
+    e = launch_normalise(ctx, g, h->d_hop, h->d_onsite, a, b, hop2, diag2, hop2f, diag2f);
+    if (e != cudaSuccess) return fail(e, "lm_kpm_moments: tables");
+    if (vecs) {
+        e = cudaMemcpy2DAsync(TA, sizeof(double2) * (size_t)ld, vecs->d_data, sizeof(double2) * (size_t)vecs->ld,
+                              sizeof(double2) * (size_t)N, (size_t)M, cudaMemcpyDeviceToDevice, ctx->stream);
+    } else {
+        const dim3 grid((unsigned)((N + 255) / 256), (unsigned)(N < 65535 ? N : 65535));
+        set_identity_kernel<<<grid, 256, 0, ctx->stream>>>(TA, N, ld);
+        ctx->launches++;
+        e = cudaGetLastError();
+    }
+    if (e != cudaSuccess) return fail(e, "lm_kpm_moments: starting block");
+    const unsigned dgrid = (unsigned)(M < 65535 ? M : 65535);
+    // T_1 = H~ T_0
+    e = launch_stencil_recur(ctx, g, LM_C64, hop2, diag2, TA, nullptr, nullptr, TB, ld, M, 0.5, 0.0, 0.0);
+    if (e != cudaSuccess) return fail(e, "lm_kpm_moments: recurrence");
+    double2* Tn = TA;   // T_n
+    double2* Tn1 = TB;  // T_{n+1}
+    for (int64_t n = 0; n <= nsteps; ++n) {
+        double* d = dots + (size_t)n * 2 * (size_t)M;
+        column_dots_kernel<<<dgrid, 256, 0, ctx->stream>>>(Tn, Tn, N, ld, M, d);
+        column_dots_kernel<<<dgrid, 256, 0, ctx->stream>>>(Tn1, Tn, N, ld, M, d + M);
+        ctx->launches += 2;
+        e = cudaGetLastError();
+        if (e != cudaSuccess) return fail(e, "lm_kpm_moments: dots");
+        if (n == nsteps) break;
+        // T_{n+2} = 2 H~ T_{n+1} - T_n, written over T_n
+        e = launch_stencil_recur(ctx, g, LM_C64, hop2, diag2, Tn1, Tn, nullptr, Tn, ld, M, 1.0, 0.0, 0.0);
+        if (e != cudaSuccess) return fail(e, "lm_kpm_moments: recurrence");
+        std::swap(Tn, Tn1);
+    }
+    std::vector<double> hd(ndots);
+    e = cudaMemcpyAsync(hd.data(), dots, sizeof(double) * ndots, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return fail(e, "lm_kpm_moments: download");
+    release();
+    // assemble the moments column by column (sums over columns in column order)
+    const double* d0 = hd.data();
+    for (int64_t col = 0; col < (per_column ? M : 1); ++col) {
+        for (int k = 0; k < nmom; ++k) {
+            const int64_t n = k / 2;
+            double v = 0.0;
+            for (int64_t c = per_column ? col : 0; c < (per_column ? col + 1 : M); ++c) {
+                const double mu0 = d0[c], mu1 = d0[M + c];
+                const double nn = d0[(size_t)n * 2 * M + c], n1n = d0[(size_t)n * 2 * M + M + c];
+                v += (k == 0) ? mu0 : (k == 1) ? mu1 : (k % 2 == 0 ? 2.0 * nn - mu0 : 2.0 * n1n - mu1);
+            }
+            out[(size_t)col * (size_t)nmom + (size_t)k] = v;
+        }
+    }
+    // |T_n(x)| <= 1 on [-1, 1]: larger moments mean that [emin, emax] misses part of the spectrum
+    for (int64_t col = 0; col < (per_column ? M : 1); ++col) {
+        const double* mu = out + (size_t)col * (size_t)nmom;
+        for (int k = 1; k < nmom; ++k)
+            if (!(fabs(mu[k]) <= fabs(mu[0]) * (1.0 + 1e-6) + 1e-12))
+                return set_err(ctx, LM_ERR_NONFINITE,
+                               "lm_kpm_moments: moments grow: [emin, emax] does not enclose the spectrum");
+    }
+    return LM_OK;
+}
+
+}  // extern "C"

@@ -6,7 +6,7 @@ and ``DensityCurrents``.  All compute runs in liblmgpu.so (hand-written sm_103a 
 package only holds the host-side bookkeeping and the ctypes bindings.
 """
 from ._lib import LMError, load as load_library
-from . import adjoint
+from . import adjoint, kpm
 from .adjoint import DensityLossAdjoint
 from .batch import Batch
 from .device import Context, default_context
@@ -21,7 +21,7 @@ from .timesequence import (ReadoutRing, TimeSequence, differentiate, integrate, 
                            moment_density)
 
 __all__ = [
-    "adjoint", "DensityLossAdjoint", "Batch", "LMError", "load_library", "Context", "default_context",
+    "adjoint", "kpm", "DensityLossAdjoint", "Batch", "LMError", "load_library", "Context", "default_context",
     "ChebyshevGPU", "Evolution", "EvolutionIterator", "EvolutionSolver", "EvolutionTimestamp",
     "FieldSum", "LandauGauge", "NoField", "PointFlux", "PointFluxes", "SymmetricGauge",
     "Hamiltonian", "tightbinding_hamiltonian", "LatticeValue", "SquareLattice",

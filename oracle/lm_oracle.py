@@ -709,3 +709,43 @@ def density_loss_gradient_exact(lat: SquareLattice, psi0, V, B, target, dt, nste
             gV[i] += float(np.real(np.sum(np.conj(lam) * (dU @ psis[n]))))
         lam = Us[n].conj().T @ lam
     return loss, gV, gB
+
+
+# ------------------------------------------------------------------------------------------
+# Density of states (src/greenfunction.jl:306-339) and Chebyshev moments for the KPM checks.
+# ------------------------------------------------------------------------------------------
+def dos_eigensystem(evals, E, broaden=0.1):
+    """dos(eig, E; broaden) = imag(sum(1 ./ (eig.values .- (E + im*broaden)))) / pi
+    (src/greenfunction.jl:306), vectorised over E."""
+    E = np.atleast_1d(np.asarray(E, dtype=np.float64))
+    ev = np.asarray(evals, dtype=np.float64)
+    return np.imag((1.0 / (ev[None, :] - (E[:, None] + 1j * broaden))).sum(axis=1)) / np.pi
+
+
+def ldos_eigensystem(evals, evecs, E, broaden=0.1):
+    """Single-particle local density of states at energy E: sum_n |psi_n(i)|^2 Im 1/(E_n - E - i*broaden) / pi,
+    the site-resolved form of dos_eigensystem."""
+    w = np.imag(1.0 / (np.asarray(evals) - (E + 1j * broaden))) / np.pi
+    return (np.abs(evecs) ** 2) @ w
+
+
+def kpm_moments(H, emin, emax, nmom, vecs=None, per_column=False):
+    """mu_n = sum_v <v|T_n(H~)|v>, H~ = (H - b)/a, by the plain three-term recurrence (no
+    doubling relations), FP64.  vecs None: the unit vectors (exact trace)."""
+    a, b = 0.5 * (emax - emin), 0.5 * (emax + emin)
+    Hs = sp.csr_matrix(H, dtype=np.complex128)
+    N = Hs.shape[0]
+    Ht = (Hs - b * sp.identity(N, format="csr")) / a
+    V = np.eye(N, dtype=np.complex128) if vecs is None else np.asarray(vecs, dtype=np.complex128)
+    ncols = V.shape[1]
+    mu = np.zeros((ncols, nmom))
+    T0 = V.copy()
+    T1 = Ht @ V
+    for n in range(nmom):
+        Tn = T0 if n == 0 else T1 if n == 1 else None
+        if n >= 2:
+            T2 = 2 * (Ht @ T1) - T0
+            T0, T1 = T1, T2
+            Tn = T1
+        mu[:, n] = np.real(np.sum(np.conj(V) * Tn, axis=0))
+    return mu if per_column else mu.sum(axis=0)

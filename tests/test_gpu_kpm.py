@@ -1,0 +1,75 @@
+"""Device Chebyshev moments (lm_kpm_moments) against the oracle's plain recurrence, and the
+KPM dos / ldos against the reference's eigensystem formula (src/greenfunction.jl:306)."""
+import numpy as np
+import pytest
+
+from oracle import lm_oracle as o
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def lm():
+    import lmgpu
+    lmgpu.default_context()
+    return lmgpu
+
+
+def case(lm, L, per, field):
+    ol = o.SquareLattice(L, L, periodic=(per, per))
+    b = {"axis1": True, "axis2": True} if per else {}
+    ll = lm.SquareLattice(L, L, boundaries=b)
+    V = o.anderson_disorder(L * L, 1.5, 11)
+    if field == "pf":
+        Ho = o.tightbinding_hamiltonian(ol, field=o.PointFlux(0.25, (L / 2 + 0.5, L / 2 + 0.5)), onsite=V)
+        Hl = lm.tightbinding_hamiltonian(ll, V, field=lm.PointFlux(0.25, (L / 2 + 0.5, L / 2 + 0.5)))
+    else:
+        Ho = o.tightbinding_hamiltonian(ol, field=o.LandauGauge(0.05), onsite=V)
+        Hl = lm.tightbinding_hamiltonian(ll, V, field=lm.LandauGauge(0.05))
+    return ol, Ho, Hl
+
+
+@pytest.mark.parametrize("L,per,field", [(9, False, "pf"), (12, True, "landau"), (16, False, "landau")])
+def test_moments_match_oracle(lm, L, per, field):
+    ol, Ho, Hl = case(lm, L, per, field)
+    bounds = lm.kpm._bounds(Hl, lm.default_context())
+    nm = 301
+    mu, _ = lm.kpm.moments(Hl, nm, bounds=bounds)
+    ref = o.kpm_moments(Ho, *bounds, nm)
+    assert np.abs(mu - ref).max() <= 1e-11 * ref[0]
+    mus, _ = lm.kpm.moments(Hl, 40, per_site=True, bounds=bounds)
+    refs = o.kpm_moments(Ho, *bounds, 40, per_column=True)
+    assert np.abs(mus - refs).max() <= 1e-12
+    R = o.random_kets(ol.N, 7, 5)
+    muv, _ = lm.kpm.moments(Hl, 101, vecs=R, bounds=bounds)
+    refv = o.kpm_moments(Ho, *bounds, 101, vecs=R)
+    assert np.abs(muv - refv).max() <= 1e-11 * abs(refv[0])
+
+
+@pytest.mark.parametrize("broaden", [0.05, 0.2])
+def test_dos_ldos_match_eigensystem(lm, broaden):
+    ol, Ho, Hl = case(lm, 14, False, "pf")
+    w, U = np.linalg.eigh(Ho.toarray())
+    E = np.linspace(-4.8, 4.8, 25)
+    d = lm.kpm.dos(Hl, E, broaden)
+    ref = o.dos_eigensystem(w, E, broaden)
+    assert np.abs(d - ref).max() <= 1e-9 * ref.max()
+    ld = lm.kpm.ldos(Hl, 0.7, broaden).values
+    lref = o.ldos_eigensystem(w, U, 0.7, broaden)
+    assert np.abs(ld - lref).max() <= 1e-9 * lref.max()
+
+
+def test_stochastic_trace_estimates_dos(lm):
+    ol, Ho, Hl = case(lm, 20, True, "landau")
+    w = np.linalg.eigvalsh(Ho.toarray())
+    E = np.linspace(-3, 3, 7)
+    d = lm.kpm.dos(Hl, E, 0.3, exact_max=0, nvec=256, seed=1)
+    ref = o.dos_eigensystem(w, E, 0.3)
+    # random-phase trace estimator: relative error ~ 1/sqrt(N * nvec)
+    assert np.abs(d - ref).max() <= 0.02 * ref.max()
+
+
+def test_bounds_must_enclose_spectrum(lm):
+    _, _, Hl = case(lm, 8, False, "pf")
+    with pytest.raises(lm.LMError):
+        lm.kpm.moments(Hl, 200, bounds=(-1.0, 1.0))
