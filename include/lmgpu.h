@@ -241,6 +241,14 @@ int lm_trace(lm_state *st, double *out);
  * (with unit vectors: the local moments of site j).  Extension of the reference. */
 int lm_kpm_moments(lm_ham *ham, double emin, double emax, int nmom, const lm_state *vecs, int per_column,
                    double *out);
+/* out = sum_{n < ncoef} coef[n] T_n(H~) in, with real coefficients and an FP64 recurrence on
+ * [emin, emax] (must enclose the spectrum).  in: an N x M state, or NULL for the identity (out
+ * is then the N x N matrix f(H), e.g. the Fermi operator of densitymatrix at T > 0,
+ * src/spectrum.jl:226-257, from the Chebyshev coefficients of the occupation).  out: N x M,
+ * ComplexF64 or ComplexF32 (rounded at the end).  Extension of the reference (which
+ * diagonalises). */
+int lm_cheb_apply(lm_ham *ham, double emin, double emax, const double *coef, int ncoef, const lm_state *in,
+                  lm_state *out);
 
 /* ---- readout ring (device side of TimeSequence(f, ev(times)), src/timesequence.jl:41-43) -- */
 /* Per-moment readouts computed into the slots of a device ring and downloaded asynchronously

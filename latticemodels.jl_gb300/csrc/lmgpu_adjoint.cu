@@ -30,6 +30,7 @@ namespace lmgpu {
 
 // out = alpha * (2H~) tp - tpp + w * lam   (tables hold 2H/a and 2(V-b)/a; tpp, lam optional)
 // w = conj(c_k): (s, 0) for even k, (0, s) for odd k (conj(-i s) = i s).
+// With y non-null, also y += cy * out (the real-coefficient Chebyshev series of lm_cheb_apply).
 template <typename R>
 __global__ void __launch_bounds__(256) adj_recur_kernel(Geom g, const typename CT<R>::V* __restrict__ hop2,
                                                         const R* __restrict__ diag2,
@@ -37,7 +38,8 @@ __global__ void __launch_bounds__(256) adj_recur_kernel(Geom g, const typename C
                                                         const typename CT<R>::V* __restrict__ tpp,
                                                         const typename CT<R>::V* __restrict__ lam,
                                                         typename CT<R>::V* __restrict__ out, int64_t ld, int64_t M,
-                                                        R alpha, R w_re, R w_im) {
+                                                        R alpha, R w_re, R w_im, typename CT<R>::V* __restrict__ y,
+                                                        R cy) {
     typedef typename CT<R>::V V;
     const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= g.N) return;
@@ -78,6 +80,12 @@ __global__ void __launch_bounds__(256) adj_recur_kernel(Geom g, const typename C
             acc.y = fma(w_re, l.y, fma(w_im, l.x, acc.y));
         }
         out[o + s] = acc;
+        if (y) {
+            V t = y[o + s];
+            t.x = fma(cy, acc.x, t.x);
+            t.y = fma(cy, acc.y, t.y);
+            y[o + s] = t;
+        }
     }
 }
 
@@ -85,19 +93,19 @@ __global__ void __launch_bounds__(256) adj_recur_kernel(Geom g, const typename C
 // and its adjoint; KPM uses it for the moments).  out may alias tpp.
 cudaError_t launch_stencil_recur(lm_ctx* ctx, const Geom& g, int precision, const void* hop2, const void* diag2,
                                  const void* tp, const void* tpp, const void* lam, void* out, int64_t ld, int64_t M,
-                                 double alpha, double wre, double wim) {
+                                 double alpha, double wre, double wim, void* y, double cy) {
     if (M <= 0 || g.N <= 0) return cudaSuccess;
     const dim3 grid((unsigned)((g.N + 255) / 256), (unsigned)(M < 65535 ? M : 65535));
     if (precision == LM_C64)
         adj_recur_kernel<double><<<grid, 256, 0, ctx->stream>>>(g, (const double2*)hop2, (const double*)diag2,
                                                                 (const double2*)tp, (const double2*)tpp,
                                                                 (const double2*)lam, (double2*)out, ld, M, alpha, wre,
-                                                                wim);
+                                                                wim, (double2*)y, cy);
     else
         adj_recur_kernel<float><<<grid, 256, 0, ctx->stream>>>(g, (const float2*)hop2, (const float*)diag2,
                                                                (const float2*)tp, (const float2*)tpp,
                                                                (const float2*)lam, (float2*)out, ld, M, (float)alpha,
-                                                               (float)wre, (float)wim);
+                                                               (float)wre, (float)wim, (float2*)y, (float)cy);
     ctx->launches++;
     return cudaGetLastError();
 }
@@ -431,7 +439,8 @@ int lm_adjoint_step(lm_adjoint* a, lm_solver* s, lm_ham* h, int component, int s
     const int64_t ld = psi->ld, M = a->m;
     auto recur = [&](const void* tp, const void* tpp, const void* lamp, void* out, double alpha, double wre,
                      double wim) -> cudaError_t {
-        return launch_stencil_recur(ctx, g, a->precision, hop2, diag2, tp, tpp, lamp, out, ld, M, alpha, wre, wim);
+        return launch_stencil_recur(ctx, g, a->precision, hop2, diag2, tp, tpp, lamp, out, ld, M, alpha, wre, wim,
+                                    nullptr, 0.0);
     };
     // T_0 = psi_n (aliased), T_1 = H~ T_0, T_k = 2 H~ T_{k-1} - T_{k-2}  (k < K)
     a->T[0] = psi->d_data;

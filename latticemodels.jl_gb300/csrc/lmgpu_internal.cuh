@@ -219,10 +219,10 @@ cudaError_t launch_cheb_fused_c32(lm_ctx* ctx, const Geom& g, const float2* hop2
 // a periodic x axis.  The fused kernel then skips the imaginary parts of the x-hops.
 bool ham_x_real(const lm_ham* h);
 // out = alpha (2H~) tp - tpp + w lam over an n x M ket block (tables 2H/a, 2(V-b)/a); tpp and
-// lam may be null; out may alias tpp (lmgpu_adjoint.cu).
+// lam may be null; out may alias tpp; with y non-null also y += cy out (lmgpu_adjoint.cu).
 cudaError_t launch_stencil_recur(lm_ctx* ctx, const Geom& g, int precision, const void* hop2, const void* diag2,
                                  const void* tp, const void* tpp, const void* lam, void* out, int64_t ld, int64_t M,
-                                 double alpha, double wre, double wim);
+                                 double alpha, double wre, double wim, void* y = nullptr, double cy = 0.0);
 cudaError_t launch_convert(lm_ctx* ctx, int to_precision, const void* src, void* dst, int64_t n,
                            int64_t m, int64_t ld_src, int64_t ld_dst);
 

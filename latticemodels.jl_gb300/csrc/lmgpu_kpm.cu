@@ -7,6 +7,10 @@
 //   mu_2n = 2 <T_n v|T_n v> - mu_0,   mu_2n+1 = 2 <T_n+1 v|T_n v> - mu_1,
 // so nmom moments take about nmom / 2 stencil passes.  With the N unit vectors as the block
 // the sum is the exact trace and column j gives the local moments of site j.
+//
+// lm_cheb_apply evaluates a real Chebyshev series sum_n c_n T_n(H~) on a block (the identity
+// gives the matrix function f(H) itself): the Fermi operator of densitymatrix at T > 0
+// (src/spectrum.jl:226-257) without an eigensystem.
 #include <cuda_runtime.h>
 #include <math.h>
 
@@ -165,6 +169,96 @@ int lm_kpm_moments(lm_ham* h, double emin, double emax, int nmom, const lm_state
                 return set_err(ctx, LM_ERR_NONFINITE,
                                "lm_kpm_moments: moments grow: [emin, emax] does not enclose the spectrum");
     }
+    return LM_OK;
+}
+
+int lm_cheb_apply(lm_ham* h, double emin, double emax, const double* coef, int ncoef, const lm_state* in,
+                  lm_state* out) {
+    if (!h) return LM_ERR_ARG;
+    lm_ctx* ctx = h->ctx;
+    CHECK_ARG(ctx, coef != nullptr && ncoef >= 1, "lm_cheb_apply: need at least one coefficient");
+    CHECK_ARG(ctx, out != nullptr && out->ctx == ctx, "lm_cheb_apply: bad output state");
+    CHECK_ARG(ctx, isfinite(emin) && isfinite(emax) && emax > emin, "lm_cheb_apply: need emin < emax");
+    for (int k = 0; k < ncoef; ++k) CHECK_ARG(ctx, isfinite(coef[k]), "lm_cheb_apply: non-finite coefficient");
+    if (!h->assembled) return set_err(ctx, LM_ERR_STATE, "lm_cheb_apply: Hamiltonian not assembled");
+    const Geom& g = h->lat->g;
+    const int64_t N = g.N;
+    if (in) CHECK_ARG(ctx, in->ctx == ctx && in->n == N, "lm_cheb_apply: input does not match the lattice");
+    const int64_t M = in ? in->m : N;
+    CHECK_ARG(ctx, out->n == N && out->m == M, "lm_cheb_apply: output shape differs from the input");
+    const double a = 0.5 * (emax - emin), b = 0.5 * (emax + emin);
+    cudaSetDevice(ctx->device);
+    double2* hop2 = nullptr;
+    double* diag2 = nullptr;
+    float2* hop2f = nullptr;
+    float* diag2f = nullptr;
+    double2* TA = nullptr;
+    double2* TB = nullptr;
+    double2* Y = nullptr;
+    const int64_t ld = N;
+    const size_t blk = sizeof(double2) * (size_t)ld * (size_t)M;
+    auto release = [&]() {
+        cudaStreamSynchronize(ctx->stream);
+        cudaFree(hop2); cudaFree(diag2); cudaFree(hop2f); cudaFree(diag2f);
+        cudaFree(TA); cudaFree(TB); cudaFree(Y);
+    };
+    cudaError_t e = cudaMalloc((void**)&hop2, sizeof(double2) * 2 * (size_t)N);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&diag2, sizeof(double) * (size_t)N);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&hop2f, sizeof(float2) * 2 * (size_t)N);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&diag2f, sizeof(float) * (size_t)N);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&TA, blk);
+    if (e == cudaSuccess && ncoef > 1) e = cudaMalloc((void**)&TB, blk);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&Y, blk);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        release();
+        return check_cuda(ctx, e, "lm_cheb_apply: allocation");
+    }
+    auto fail = [&](cudaError_t err, const char* what) {
+        const int rc = check_cuda(ctx, err, what);
+        release();
+        return rc;
+    };
+    e = launch_normalise(ctx, g, h->d_hop, h->d_onsite, a, b, hop2, diag2, hop2f, diag2f);
+    if (e != cudaSuccess) return fail(e, "lm_cheb_apply: tables");
+    // T_0
+    if (!in) {
+        const dim3 grid((unsigned)((N + 255) / 256), (unsigned)(N < 65535 ? N : 65535));
+        set_identity_kernel<<<grid, 256, 0, ctx->stream>>>(TA, N, ld);
+        ctx->launches++;
+        e = cudaGetLastError();
+    } else if (in->precision == LM_C64) {
+        e = cudaMemcpy2DAsync(TA, sizeof(double2) * (size_t)ld, in->d_data, sizeof(double2) * (size_t)in->ld,
+                              sizeof(double2) * (size_t)N, (size_t)M, cudaMemcpyDeviceToDevice, ctx->stream);
+    } else {
+        e = launch_convert(ctx, LM_C64, in->d_data, TA, N, M, in->ld, ld);
+    }
+    if (e != cudaSuccess) return fail(e, "lm_cheb_apply: input block");
+    // Y = c_0 T_0
+    e = cudaMemcpyAsync(Y, TA, blk, cudaMemcpyDeviceToDevice, ctx->stream);
+    if (e == cudaSuccess) e = launch_scale(ctx, LM_C64, Y, N, M, ld, coef[0], 0.0);
+    if (e != cudaSuccess) return fail(e, "lm_cheb_apply: first term");
+    if (ncoef > 1) {
+        // T_1 = H~ T_0, Y += c_1 T_1; then T_{n+1} = 2 H~ T_n - T_{n-1} over T_{n-1}, Y += c_{n+1} T_{n+1}
+        e = launch_stencil_recur(ctx, g, LM_C64, hop2, diag2, TA, nullptr, nullptr, TB, ld, M, 0.5, 0.0, 0.0, Y,
+                                 coef[1]);
+        if (e != cudaSuccess) return fail(e, "lm_cheb_apply: recurrence");
+        double2* Tprev = TA;
+        double2* Tn = TB;
+        for (int k = 2; k < ncoef; ++k) {
+            e = launch_stencil_recur(ctx, g, LM_C64, hop2, diag2, Tn, Tprev, nullptr, Tprev, ld, M, 1.0, 0.0, 0.0, Y,
+                                     coef[k]);
+            if (e != cudaSuccess) return fail(e, "lm_cheb_apply: recurrence");
+            std::swap(Tprev, Tn);
+        }
+    }
+    if (out->precision == LM_C64)
+        e = cudaMemcpy2DAsync(out->d_data, sizeof(double2) * (size_t)out->ld, Y, sizeof(double2) * (size_t)ld,
+                              sizeof(double2) * (size_t)N, (size_t)M, cudaMemcpyDeviceToDevice, ctx->stream);
+    else
+        e = launch_convert(ctx, LM_C32, Y, out->d_data, N, M, ld, out->ld);
+    if (e != cudaSuccess) return fail(e, "lm_cheb_apply: output");
+    release();
     return LM_OK;
 }
 

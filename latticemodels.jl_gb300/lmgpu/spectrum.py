@@ -1,8 +1,13 @@
 """``diagonalize`` / ``densitymatrix`` on the device (src/spectrum.jl:48-55, :226-257, :317-333).
 
-The dense Hermitian eigensolver is cuSOLVER (through torch.linalg.eigh on the GPU); the
-occupation f(E) and the projector V f(E) V^dagger follow the reference.  This produces the
-input P_0 of the evolution path; it runs on the GPU only (no host eigensolver).
+Two routes to P = f(H) = sum_i f(E_i) |psi_i><psi_i| with the FermiDirac occupation f:
+* T > 0: the Chebyshev series of f on the spectral interval, applied to the identity by the
+  library's own stencil kernels (``lm_cheb_apply``): no eigensystem, O(K N^2) work for K
+  terms, exact to the series tolerance.
+* T = 0 (a step function, whose series does not converge), or on request: the dense
+  Hermitian eigensolver cuSOLVER (through torch.linalg.eigh on the GPU), with the reference's
+  occupation rule (E == mu counts as occupied).
+Both run on the GPU only (no host eigensolver).
 """
 from __future__ import annotations
 
@@ -10,6 +15,8 @@ import math
 
 import numpy as np
 
+from . import _lib
+from .device import default_context
 from .hamiltonian import Hamiltonian
 from .states import DensityMatrix
 
@@ -52,8 +59,52 @@ def densfun(T: float, mu: float):
     return f
 
 
-def densitymatrix(H: Hamiltonian, mu: float = 0.0, T: float = 0.0, precision="c64") -> DensityMatrix:
-    """``densitymatrix(H; mu, T)`` for a one-particle system with FermiDirac statistics."""
+def chebyshev_coefficients(f, bounds, tol: float = 1e-13, max_nodes: int = 1 << 22):
+    """Real Chebyshev coefficients c_n of x -> f(a x + b) on [-1, 1] ([b - a, b + a] = bounds),
+    truncated where sum_{n >= K} |c_n| <= tol, from Chebyshev-Gauss nodes (a type-II DCT)."""
+    from scipy.fft import dct
+    emin, emax = bounds
+    a, b = 0.5 * (emax - emin), 0.5 * (emax + emin)
+    nodes = 4096
+    while True:
+        k = np.arange(nodes)
+        x = np.cos(math.pi * (k + 0.5) / nodes)
+        c = dct(f(a * x + b), type=2) / nodes
+        c[0] *= 0.5
+        tail = np.cumsum(np.abs(c)[::-1])[::-1]
+        below = np.nonzero(tail <= tol)[0]
+        if len(below) and below[0] <= nodes // 4:
+            return c[: max(int(below[0]), 1)]
+        if nodes >= max_nodes:
+            raise ValueError("the Chebyshev series of f does not converge on the spectral interval")
+        nodes *= 2
+
+
+def fermi_occupation(mu: float, T: float):
+    """FermiDirac f(E) = 1 / (exp((E - mu)/T) + 1) for T > 0 (src/spectrum.jl:230-232), vectorised."""
+    return lambda E: 0.5 * (1.0 - np.tanh((np.asarray(E) - mu) / (2.0 * T)))
+
+
+def densitymatrix(H: Hamiltonian, mu: float = 0.0, T: float = 0.0, precision="c64", method: str = "auto",
+                  tol: float = 1e-13) -> DensityMatrix:
+    """``densitymatrix(H; mu, T)`` for a one-particle system with FermiDirac statistics
+    (src/spectrum.jl:252-257).  method: "auto" (Chebyshev for T > 0, eigensolver for T = 0),
+    "chebyshev" or "eigh"."""
+    if method not in ("auto", "chebyshev", "eigh"):
+        raise ValueError("method must be auto, chebyshev or eigh")
+    if method == "chebyshev" and not T > 0:
+        raise ValueError("the Chebyshev route needs T > 0 (the T = 0 occupation is a step)")
+    if T > 0 and method != "eigh":
+        ctx = default_context()
+        lo, hi = H.bounds(ctx)
+        pad = 1e-3 * (hi - lo)
+        bounds = (lo - pad, hi + pad)
+        coef = np.ascontiguousarray(chebyshev_coefficients(fermi_occupation(mu, T), bounds, tol))
+        out = DensityMatrix(H.lattice, None, precision, ctx=ctx)
+        dh = H.device(ctx)
+        ctx.check(ctx.lib.lm_cheb_apply(dh.handle, float(bounds[0]), float(bounds[1]), _lib.dptr(coef), len(coef),
+                                        None, out.handle))
+        return out
     torch = _torch_cuda()
     w, V = diagonalize(H)
     f = densfun(T, mu)

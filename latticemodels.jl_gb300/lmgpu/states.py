@@ -143,7 +143,8 @@ class DensityMatrix(DeviceState):
     """N x N one-particle density matrix (the reference's ``Operator`` state)."""
 
     def __init__(self, lattice, data, precision="c64", ctx=None):
-        super().__init__(lattice, data, _lib.LM_DENSITY, precision, None, ctx)
+        # data None: an N x N zero matrix (filled on the device, e.g. by densitymatrix)
+        super().__init__(lattice, data, _lib.LM_DENSITY, precision, None, ctx, shape=(lattice.N, lattice.N))
 
 
 

@@ -73,3 +73,35 @@ def test_bounds_must_enclose_spectrum(lm):
     _, _, Hl = case(lm, 8, False, "pf")
     with pytest.raises(lm.LMError):
         lm.kpm.moments(Hl, 200, bounds=(-1.0, 1.0))
+
+
+@pytest.mark.parametrize("mu,T", [(0.0, 0.1), (0.5, 0.3), (-1.0, 0.05)])
+@pytest.mark.parametrize("precision", ["c64", "c32"])
+def test_fermi_operator_densitymatrix(lm, mu, T, precision):
+    """densitymatrix(H; mu, T > 0) from the Chebyshev series of the occupation on the device
+    against the oracle's eigensystem projector (src/spectrum.jl:226-257)."""
+    ol, Ho, Hl = case(lm, 12, False, "pf")
+    Pref, _, _ = o.densitymatrix(Ho, mu=mu, T=T)
+    P = lm.densitymatrix(Hl, mu=mu, T=T, precision=precision)
+    Pd = P.to_numpy().astype(np.complex128)
+    err = np.linalg.norm(Pd - Pref) / np.linalg.norm(Pref)
+    assert err <= (1e-11 if precision == "c64" else 1e-6), err
+    assert abs(P.trace() - np.trace(Pref).real) <= (1e-10 if precision == "c64" else 1e-5) * np.trace(Pref).real
+
+
+def test_cheb_apply_on_kets_matches_dense_function(lm):
+    """lm_cheb_apply on a ket block: f(H) X for f = exp(-(E - 0.3)^2) against the dense oracle."""
+    import ctypes as C
+    ol, Ho, Hl = case(lm, 10, True, "landau")
+    w, U = np.linalg.eigh(Ho.toarray())
+    f = lambda E: np.exp(-(np.asarray(E) - 0.3) ** 2)
+    X = o.random_kets(ol.N, 5, 9)
+    ref = (U * f(w)) @ (U.conj().T @ X)
+    ctx = lm.default_context()
+    lo, hi = Hl.bounds(ctx)
+    coef = lm.spectrum.chebyshev_coefficients(f, (lo, hi), 1e-14)
+    st = lm.KetBlock(Hl.lattice, X)
+    out = lm.KetBlock(Hl.lattice, np.zeros_like(X))
+    ctx.check(ctx.lib.lm_cheb_apply(Hl.device(ctx).handle, lo, hi, coef.ctypes.data_as(C.POINTER(C.c_double)),
+                                    len(coef), st.handle, out.handle))
+    assert np.linalg.norm(out.to_numpy() - ref) <= 1e-12 * np.linalg.norm(ref)

@@ -32,3 +32,21 @@ def test_order_grows_as_broadening_shrinks():
     assert kpm.order_for(0.0, 0.01, b) > kpm.order_for(0.0, 0.1, b) > kpm.order_for(0.0, 1.0, b)
     with pytest.raises(ValueError):
         kpm.order_for(0.0, 0.0, b)
+
+
+@pytest.mark.parametrize("mu,T", [(0.0, 0.1), (0.5, 0.3), (-1.0, 0.05)])
+def test_fermi_series_coefficients(mu, T):
+    """The truncated Chebyshev series of the FermiDirac occupation (src/spectrum.jl:230-232)
+    reproduces it to the requested tolerance on the whole interval."""
+    pytest.importorskip("scipy")
+    from lmgpu import spectrum
+    f = spectrum.fermi_occupation(mu, T)
+    b = (-5.3, 5.1)
+    c = spectrum.chebyshev_coefficients(f, b, 1e-13)
+    x = np.linspace(-1, 1, 2001)
+    a, m = 0.5 * (b[1] - b[0]), 0.5 * (b[1] + b[0])
+    assert np.abs(np.polynomial.chebyshev.chebval(x, c) - f(a * x + m)).max() <= 2e-13
+    # against the oracle's scalar occupation
+    fo = o.densfun(T, mu)
+    E = np.linspace(-5, 5, 11)
+    assert np.allclose(f(E), [fo(e) for e in E], rtol=0, atol=1e-15)
