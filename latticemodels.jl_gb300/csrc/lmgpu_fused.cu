@@ -6,11 +6,11 @@
 // the result written once, instead of five vector passes per Chebyshev order.
 //
 // Tiling: a CTA of 512 threads owns a region of 32 (x) x 64 (y) sites; thread (tx, ty) holds
-// the four consecutive y-sites 4ty..4ty+3 of row tx in registers (T_{k-1}, the accumulator and
-// the stencil coefficients).  Per order, rows are exchanged through a double-buffered
-// shared-memory copy of T_{k-1} (x neighbours) and warp shuffles (y neighbours: a warp holds
-// two whole rows); T_{k-2} of a thread's own sites is read back from the buffer T_k
-// overwrites.  The valid part of the region shrinks by one site per order, so after K orders
+// the S = 4 consecutive y-sites S ty .. S ty + S-1 of row tx in registers (T_{k-1}, the
+// accumulator and the stencil coefficients).  Per order, rows are exchanged through a
+// double-buffered shared-memory copy of T_{k-1} (x neighbours) and warp shuffles (y
+// neighbours: a warp holds whole rows); T_{k-2} of a thread's own sites is read back from the
+// buffer T_k overwrites.  Built with LM_FUSED_SITES=2 the CTA has 1024 threads of 2 sites.  The valid part of the region shrinks by one site per order, so after K orders
 // the inner (32-2K) x (64-2K) sites are exact and are written out.  Periodic axes wrap the
 // halo.  Along an open axis the first and last regions of a lattice sit on the lattice edge:
 // the stencil has no bond across it, so nothing shrinks there and those regions write out up
@@ -29,20 +29,42 @@
 
 namespace lmgpu {
 
+// Sites per thread along y: 4 (512 threads, a warp holds two rows) or 2 (1024 threads, a warp
+// holds one row); the region stays 32 x 64 either way.
+#ifndef LM_FUSED_SITES
+#define LM_FUSED_SITES 4
+#endif
 namespace {
 constexpr int RX = 32;         // region extent along x (threads along x)
-constexpr int TY = 16;         // threads along y
-constexpr int S = 4;           // sites per thread along y
+constexpr int S = LM_FUSED_SITES;  // sites per thread along y
+static_assert(S == 2 || S == 4, "LM_FUSED_SITES must be 2 or 4");
+constexpr int TY = 64 / S;     // threads along y
 constexpr int RY = TY * S;     // region extent along y
-constexpr int NTHR = RX * TY;  // 512
+constexpr int NTHR = RX * TY;  // 512 or 1024
+constexpr int HALVES = S / 2;  // float4 words per thread and row (a float4 = two sites)
+constexpr int ROWS_PER_WARP = 32 / TY;
 constexpr int KB = 1;          // kets a thread advances together
-// one buffer = KB kets x RX rows x 2 halves x TY float4 (a float4 = two sites of one thread)
-constexpr int BUF_F4 = KB * RX * 2 * TY;
+// one buffer = KB kets x RX rows x HALVES x TY float4
+constexpr int BUF_F4 = KB * RX * HALVES * TY;
 constexpr int SMEM_BYTES = 4 * BUF_F4 * 16;  // T double buffer + staging double buffer
 constexpr int DESC_WORDS = (int)(sizeof(FusedInst) + 3) / 4;
 }  // namespace
 
-__device__ __forceinline__ int fidx(int kk, int row, int h, int ty) { return ((kk * RX + row) * 2 + h) * TY + ty; }
+__device__ __forceinline__ int fidx(int kk, int row, int h, int ty) { return ((kk * RX + row) * HALVES + h) * TY + ty; }
+
+// The S sites of thread ty in row `row` of buffer `buf`, and the reverse.
+__device__ __forceinline__ void load_sites(const float4* buf, int kk, int row, int ty, float2 v[S]) {
+#pragma unroll
+    for (int h = 0; h < HALVES; ++h) {
+        const float4 q = buf[fidx(kk, row, h, ty)];
+        v[2 * h] = make_float2(q.x, q.y);
+        v[2 * h + 1] = make_float2(q.z, q.w);
+    }
+}
+__device__ __forceinline__ void store_sites(float4* buf, int kk, int row, int ty, const float2 v[S]) {
+#pragma unroll
+    for (int h = 0; h < HALVES; ++h) buf[fidx(kk, row, h, ty)] = make_float4(v[2 * h].x, v[2 * h].y, v[2 * h + 1].x, v[2 * h + 1].y);
+}
 
 // Region coordinate -> lattice coordinate (0-based) or -1 outside an open axis.
 __device__ __forceinline__ int64_t wrap_axis(int64_t c, int64_t L, int per) {
@@ -147,12 +169,6 @@ __device__ __forceinline__ void prefetch_kets(float4* stage, const TileMap& m, c
     cp_async_commit();
 }
 
-__device__ __forceinline__ void unpack4(const float4 a, const float4 b, float2 v[S]) {
-    v[0] = make_float2(a.x, a.y);
-    v[1] = make_float2(a.z, a.w);
-    v[2] = make_float2(b.x, b.y);
-    v[3] = make_float2(b.z, b.w);
-}
 
 // Instance holding global item `item` (largest i with table[i].item_begin <= item).
 __device__ __forceinline__ int find_instance(const FusedInst* __restrict__ table, int ninst, int64_t item) {
@@ -186,7 +202,7 @@ cheb_fused_c32_kernel(FusedInst single, const FusedInst* __restrict__ table, int
     const int t = threadIdx.x;
     const int tx = t / TY;
     const int ty = t % TY;
-    const int warp_row0 = (t >> 5) * 2;  // the two rows a warp holds
+    const int warp_row0 = (t >> 5) * ROWS_PER_WARP;  // the rows a warp holds
 
     // next item id: the work queue for a batch, a static stride for one lattice
     long long last_static = (long long)blockIdx.x - gridDim.x;
@@ -291,7 +307,7 @@ cheb_fused_c32_kernel(FusedInst single, const FusedInst* __restrict__ table, int
             float2 t1[KB][S], yv[KB][S];
 #pragma unroll
             for (int kk = 0; kk < KB; ++kk) {
-                unpack4(smem[stage + fidx(kk, tx, 0, ty)], smem[stage + fidx(kk, tx, 1, ty)], t1[kk]);
+                load_sites(smem + stage, kk, tx, ty, t1[kk]);
 #pragma unroll
                 for (int j = 0; j < S; ++j) yv[kk][j] = make_float2(0.f, 0.f);
             }
@@ -303,22 +319,23 @@ cheb_fused_c32_kernel(FusedInst single, const FusedInst* __restrict__ table, int
                 const int prev2 = (k == 2) ? stage : dst;  // T_{k-2} of my positions
                 // warps whose two rows both lie outside the valid region skip the order (the
                 // valid rows shrink by one per order, except at an open lattice edge)
-                const bool active = (cur.hard_lo || warp_row0 + 1 >= k) && (cur.hard_hi || warp_row0 < RX - k);
+                const bool active =
+                    (cur.hard_lo || warp_row0 + ROWS_PER_WARP - 1 >= k) && (cur.hard_hi || warp_row0 < RX - k);
                 if (active) {
                     const int xp = min(tx + 1, RX - 1), xm = max(tx - 1, 0);
                     const float sk = D.s[k];
 #pragma unroll
                     for (int kk = 0; kk < KB; ++kk) {
                         float2 vxp[S], vxm[S];
-                        unpack4(smem[src + fidx(kk, xp, 0, ty)], smem[src + fidx(kk, xp, 1, ty)], vxp);
-                        unpack4(smem[src + fidx(kk, xm, 0, ty)], smem[src + fidx(kk, xm, 1, ty)], vxm);
+                        load_sites(smem + src, kk, xp, ty, vxp);
+                        load_sites(smem + src, kk, xm, ty, vxm);
                         float2 up, dn;  // y-1 of my first position, y+1 of my last
                         up.x = __shfl_up_sync(0xffffffffu, t1[kk][S - 1].x, 1);
                         up.y = __shfl_up_sync(0xffffffffu, t1[kk][S - 1].y, 1);
                         dn.x = __shfl_down_sync(0xffffffffu, t1[kk][0].x, 1);
                         dn.y = __shfl_down_sync(0xffffffffu, t1[kk][0].y, 1);
                         float2 t0[S];
-                        if (k >= 2) unpack4(smem[prev2 + fidx(kk, tx, 0, ty)], smem[prev2 + fidx(kk, tx, 1, ty)], t0);
+                        if (k >= 2) load_sites(smem + prev2, kk, tx, ty, t0);
                         float2 tk[S];
 #pragma unroll
                         for (int j = 0; j < S; ++j) {
@@ -367,8 +384,7 @@ cheb_fused_c32_kernel(FusedInst single, const FusedInst* __restrict__ table, int
                             t1[kk][j] = tk[j];
                         }
                         if (k < K) {
-                            smem[dst + fidx(kk, tx, 0, ty)] = make_float4(tk[0].x, tk[0].y, tk[1].x, tk[1].y);
-                            smem[dst + fidx(kk, tx, 1, ty)] = make_float4(tk[2].x, tk[2].y, tk[3].x, tk[3].y);
+                            store_sites(smem + dst, kk, tx, ty, tk);
                         }
                     }
                 }
@@ -383,7 +399,7 @@ cheb_fused_c32_kernel(FusedInst single, const FusedInst* __restrict__ table, int
                 if (ket >= cur_k_end) break;
                 float2* outk = D.out + ket * D.ld;
                 float2 x0[S];
-                unpack4(smem[stage + fidx(kk, tx, 0, ty)], smem[stage + fidx(kk, tx, 1, ty)], x0);
+                load_sites(smem + stage, kk, tx, ty, x0);
 #pragma unroll
                 for (int j = 0; j < S; ++j) {
                     if (interior & (1u << j)) {

@@ -16,6 +16,9 @@ SOURCES = ["lmgpu_api.cu", "lmgpu_kernels.cu", "lmgpu_fused.cu", "lmgpu_noalloc.
            "lmgpu_ring.cu", "lmgpu_kpm.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", f"-I{INCLUDE}"]
+# extra nvcc flags for tuning builds (e.g. LMGPU_NVCC_FLAGS=-DLM_FUSED_SITES=2); the default
+# build needs none
+EXTRA = os.environ.get("LMGPU_NVCC_FLAGS", "").split()
 
 
 def nvcc_path() -> str:
@@ -44,7 +47,7 @@ def build(force: bool = False, verbose: bool = False) -> Path:
 
         def compile_one(src: str) -> str:
             obj = os.path.join(tmp, src.replace(".cu", ".o"))
-            cmd = [nvcc, *ARCH, *FLAGS, "-c", str(CSRC / src), "-o", obj]
+            cmd = [nvcc, *ARCH, *FLAGS, *EXTRA, "-c", str(CSRC / src), "-o", obj]
             r = subprocess.run(cmd, capture_output=True, text=True)
             if r.returncode != 0:
                 raise RuntimeError(f"nvcc failed for {src}:\n{r.stdout}\n{r.stderr}")
