@@ -249,6 +249,11 @@ int lm_kpm_moments(lm_ham *ham, double emin, double emax, int nmom, const lm_sta
  * diagonalises). */
 int lm_cheb_apply(lm_ham *ham, double emin, double emax, const double *coef, int ncoef, const lm_state *in,
                   lm_state *out);
+/* Spectral interval by FP64 Lanczos (iters steps from a seeded random-phase vector): the
+ * extreme Ritz values padded by their residuals and 1 % of the width, clipped to the
+ * Gershgorin interval of lm_ham_bounds.  A tighter interval lowers the Chebyshev order;
+ * pass it to lm_solver_set_bounds, lm_kpm_moments or lm_cheb_apply. */
+int lm_ham_lanczos_bounds(lm_ham *ham, int iters, unsigned long long seed, double *emin, double *emax);
 
 /* ---- readout ring (device side of TimeSequence(f, ev(times)), src/timesequence.jl:41-43) -- */
 /* Per-moment readouts computed into the slots of a device ring and downloaded asynchronously

@@ -53,9 +53,112 @@ __global__ void __launch_bounds__(256) column_dots_kernel(const double2* __restr
     }
 }
 
+// y = y + c x (real c), n complex entries
+__global__ void axpy_kernel(double2* __restrict__ y, const double2* __restrict__ x, double c, int64_t n) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        double2 v = y[i];
+        const double2 u = x[i];
+        v.x = fma(c, u.x, v.x);
+        v.y = fma(c, u.y, v.y);
+        y[i] = v;
+    }
+}
+
+// y = c x (real c)
+__global__ void scaled_copy_kernel(double2* __restrict__ y, const double2* __restrict__ x, double c, int64_t n) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        y[i] = make_double2(c * x[i].x, c * x[i].y);
+}
+
+// Lanczos start vector: entries of modulus 1/sqrt(n) with pseudo-random phases (splitmix64 of
+// (seed, i)), so every eigenvector has a component in it almost surely.
+__global__ void start_vector_kernel(double2* __restrict__ v, int64_t n, unsigned long long seed) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        unsigned long long z = seed + 0x9E3779B97F4A7C15ull * (unsigned long long)(i + 1);
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        z ^= z >> 31;
+        const double phi = 6.283185307179586 * (double)(z >> 11) * (1.0 / 9007199254740992.0);
+        double sn, cs;
+        sincos(phi, &sn, &cs);
+        const double r = rsqrt((double)n);
+        v[i] = make_double2(r * cs, r * sn);
+    }
+}
+
 }  // namespace lmgpu
 
 using namespace lmgpu;
+
+// Number of eigenvalues of the symmetric tridiagonal (a, b) below x (Sturm sequence count).
+static int sturm_count(const std::vector<double>& a, const std::vector<double>& b, double x) {
+    int cnt = 0;
+    double q = 1.0;
+    for (size_t i = 0; i < a.size(); ++i) {
+        const double bb = i ? b[i - 1] * b[i - 1] : 0.0;
+        q = (a[i] - x) - (i ? bb / q : 0.0);
+        if (q == 0.0) q = -1e-300;
+        if (q < 0.0) ++cnt;
+    }
+    return cnt;
+}
+
+// Last component of the unit eigenvector of the tridiagonal (a, b) for eigenvalue theta, by
+// inverse iteration with a slightly shifted theta and Gaussian elimination with partial
+// pivoting (the factor of a tridiagonal gains one extra superdiagonal).
+static double tridiag_last_component(const std::vector<double>& a, const std::vector<double>& b, double theta) {
+    const size_t m = a.size();
+    if (m == 1) return 1.0;
+    const double shift = theta + 1e-10 * (fabs(theta) + 1.0);
+    std::vector<double> x(m, 1.0);
+    for (int it = 0; it < 3; ++it) {
+        // rows: lower l[i] (below diag), diag d[i], upper u1[i], u2[i] (second superdiagonal)
+        std::vector<double> d(m), u1(m, 0.0), u2(m, 0.0), rhs(x);
+        std::vector<double> l(m, 0.0);
+        for (size_t i = 0; i < m; ++i) {
+            d[i] = a[i] - shift;
+            if (i + 1 < m) u1[i] = b[i];
+            if (i > 0) l[i] = b[i - 1];
+        }
+        for (size_t i = 0; i + 1 < m; ++i) {
+            // eliminate l[i+1] (row i+1, column i) with the larger of rows i, i+1 as pivot
+            if (fabs(l[i + 1]) > fabs(d[i])) {
+                std::swap(d[i], l[i + 1]);
+                std::swap(u1[i], d[i + 1]);
+                std::swap(u2[i], u1[i + 1]);
+                std::swap(rhs[i], rhs[i + 1]);
+            }
+            const double piv = d[i] != 0.0 ? d[i] : 1e-300;
+            const double f = l[i + 1] / piv;
+            d[i + 1] -= f * u1[i];
+            u1[i + 1] -= f * u2[i];
+            rhs[i + 1] -= f * rhs[i];
+            l[i + 1] = 0.0;
+        }
+        for (size_t ii = m; ii-- > 0;) {
+            double v = rhs[ii];
+            if (ii + 1 < m) v -= u1[ii] * x[ii + 1];
+            if (ii + 2 < m) v -= u2[ii] * x[ii + 2];
+            x[ii] = v / (d[ii] != 0.0 ? d[ii] : 1e-300);
+        }
+        double nrm = 0.0;
+        for (double v : x) nrm += v * v;
+        nrm = sqrt(nrm);
+        if (!(nrm > 0.0) || !isfinite(nrm)) return 1.0;  // fall back to the crude bound
+        for (double& v : x) v /= nrm;
+    }
+    return x[m - 1];
+}
+
+// The k-th smallest eigenvalue (k = 0 .. m-1) of the tridiagonal by bisection.
+static double tridiag_eig(const std::vector<double>& a, const std::vector<double>& b, int k, double lo, double hi) {
+    for (int it = 0; it < 200 && hi - lo > 1e-14 * (fabs(lo) + fabs(hi) + 1e-300); ++it) {
+        const double mid = 0.5 * (lo + hi);
+        if (sturm_count(a, b, mid) > k) hi = mid;
+        else lo = mid;
+    }
+    return 0.5 * (lo + hi);
+}
 
 extern "C" {
 
@@ -259,6 +362,102 @@ int lm_cheb_apply(lm_ham* h, double emin, double emax, const double* coef, int n
         e = launch_convert(ctx, LM_C32, Y, out->d_data, N, M, ld, out->ld);
     if (e != cudaSuccess) return fail(e, "lm_cheb_apply: output");
     release();
+    return LM_OK;
+}
+
+int lm_ham_lanczos_bounds(lm_ham* h, int iters, unsigned long long seed, double* emin, double* emax) {
+    if (!h) return LM_ERR_ARG;
+    lm_ctx* ctx = h->ctx;
+    CHECK_ARG(ctx, emin && emax, "lm_ham_lanczos_bounds: null output");
+    CHECK_ARG(ctx, iters >= 2 && iters <= 10000, "lm_ham_lanczos_bounds: iters must be in 2..10000");
+    if (!h->assembled) return set_err(ctx, LM_ERR_STATE, "lm_ham_lanczos_bounds: Hamiltonian not assembled");
+    const Geom& g = h->lat->g;
+    const int64_t N = g.N;
+    double glo = 0.0, ghi = 0.0;
+    lm_ham_bounds(h, &glo, &ghi);
+    const int m = (int)std::min<int64_t>(iters, N);
+    cudaSetDevice(ctx->device);
+    double2* hop2 = nullptr;
+    double* diag2 = nullptr;
+    float2* hop2f = nullptr;
+    float* diag2f = nullptr;
+    double2* buf = nullptr;  // three vectors
+    double* dot = nullptr;
+    auto release = [&]() {
+        cudaStreamSynchronize(ctx->stream);
+        cudaFree(hop2); cudaFree(diag2); cudaFree(hop2f); cudaFree(diag2f); cudaFree(buf); cudaFree(dot);
+    };
+    cudaError_t e = cudaMalloc((void**)&hop2, sizeof(double2) * 2 * (size_t)N);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&diag2, sizeof(double) * (size_t)N);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&hop2f, sizeof(float2) * 2 * (size_t)N);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&diag2f, sizeof(float) * (size_t)N);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&buf, sizeof(double2) * 3 * (size_t)N);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&dot, sizeof(double));
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        release();
+        return check_cuda(ctx, e, "lm_ham_lanczos_bounds: allocation");
+    }
+    auto fail = [&](cudaError_t err, const char* what) {
+        const int rc = check_cuda(ctx, err, what);
+        release();
+        return rc;
+    };
+    // tables for a = 2, b = 0 hold H itself: the recurrence kernel then computes H v - u
+    e = launch_normalise(ctx, g, h->d_hop, h->d_onsite, 2.0, 0.0, hop2, diag2, hop2f, diag2f);
+    if (e != cudaSuccess) return fail(e, "lm_ham_lanczos_bounds: tables");
+    double2* A = buf;          // v_j
+    double2* B = buf + N;      // beta_{j-1} v_{j-1}
+    double2* Cw = buf + 2 * N; // w
+    const unsigned grid = (unsigned)std::min<int64_t>((N + 255) / 256, 4096);
+    start_vector_kernel<<<grid, 256, 0, ctx->stream>>>(A, N, seed);
+    e = cudaMemsetAsync(B, 0, sizeof(double2) * (size_t)N, ctx->stream);
+    if (e != cudaSuccess) return fail(e, "lm_ham_lanczos_bounds: start");
+    std::vector<double> al, be;
+    auto read_dot = [&](const double2* x, const double2* y, double* v) -> cudaError_t {
+        column_dots_kernel<<<1, 256, 0, ctx->stream>>>(x, y, N, N, 1, dot);
+        cudaError_t err = cudaGetLastError();
+        if (err == cudaSuccess) err = cudaMemcpyAsync(v, dot, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream);
+        if (err == cudaSuccess) err = cudaStreamSynchronize(ctx->stream);
+        return err;
+    };
+    for (int j = 0; j < m; ++j) {
+        // w = H v_j - beta_{j-1} v_{j-1}
+        e = launch_stencil_recur(ctx, g, LM_C64, hop2, diag2, A, B, nullptr, Cw, N, 1, 1.0, 0.0, 0.0);
+        double alpha = 0.0, bsq = 0.0;
+        if (e == cudaSuccess) e = read_dot(A, Cw, &alpha);
+        if (e == cudaSuccess) {
+            axpy_kernel<<<grid, 256, 0, ctx->stream>>>(Cw, A, -alpha, N);
+            e = cudaGetLastError();
+        }
+        if (e == cudaSuccess) e = read_dot(Cw, Cw, &bsq);
+        if (e != cudaSuccess) return fail(e, "lm_ham_lanczos_bounds: iteration");
+        al.push_back(alpha);
+        const double beta = sqrt(std::max(bsq, 0.0));
+        if (j == m - 1 || beta <= 1e-12 * (fabs(ghi) + fabs(glo))) {
+            be.push_back(beta);
+            break;  // invariant subspace (or the last step): the tridiagonal is complete
+        }
+        be.push_back(beta);
+        // B = beta v_j, v_{j+1} = w / beta, rotate the buffers
+        scaled_copy_kernel<<<grid, 256, 0, ctx->stream>>>(B, A, beta, N);
+        scaled_copy_kernel<<<grid, 256, 0, ctx->stream>>>(Cw, Cw, 1.0 / beta, N);
+        e = cudaGetLastError();
+        if (e != cudaSuccess) return fail(e, "lm_ham_lanczos_bounds: iteration");
+        std::swap(A, Cw);
+    }
+    release();
+    const int k = (int)al.size();
+    std::vector<double> offd(be.begin(), be.begin() + (k - 1));
+    const double lo = tridiag_eig(al, offd, 0, glo - 1.0, ghi + 1.0);
+    const double hi = tridiag_eig(al, offd, k - 1, glo - 1.0, ghi + 1.0);
+    // Ritz values lie inside the spectrum; pad each extreme by its residual beta_m |s_m| (an
+    // eigenvalue lies within it) plus 1 % of the width, and never leave the Gershgorin interval
+    const double rlo = be.back() * fabs(tridiag_last_component(al, offd, lo));
+    const double rhi = be.back() * fabs(tridiag_last_component(al, offd, hi));
+    const double w = 0.01 * (hi - lo);
+    *emin = std::max(glo, lo - rlo - w);
+    *emax = std::min(ghi, hi + rhi + w);
     return LM_OK;
 }
 

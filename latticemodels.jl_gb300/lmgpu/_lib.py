@@ -101,6 +101,7 @@ SIGNATURES = {
     "lm_trace": (_INT, [_P, _PD]),
     "lm_kpm_moments": (_INT, [_P, _D, _D, _INT, _P, _INT, _PD]),
     "lm_cheb_apply": (_INT, [_P, _D, _D, _PD, _INT, _P, _P]),
+    "lm_ham_lanczos_bounds": (_INT, [_P, _INT, C.c_ulonglong, _PD, _PD]),
     "lm_ring_create": (_INT, [_P, _INT, _I64, C.POINTER(_P)]),
     "lm_ring_destroy": (_INT, [_P]),
     "lm_ring_push_localdensity": (_INT, [_P, _P, _D, _PI64]),

@@ -133,11 +133,19 @@ class Hamiltonian:
         ctx.check(ctx.lib.lm_ham_csc(dh.handle, _lib.i64ptr(colptr), _lib.i64ptr(rowval), _lib.dptr(nz)))
         return colptr, rowval, nz[0::2] + 1j * nz[1::2]
 
-    def bounds(self, ctx=None):
+    def bounds(self, ctx=None, method: str = "gershgorin", iters: int = 80, seed: int = 1):
+        """Interval enclosing the spectrum: "gershgorin" (rigorous) or "lanczos" (FP64 Lanczos
+        estimate, padded and clipped to the Gershgorin interval; tighter, for one-shot
+        expansions such as kpm.dos or densitymatrix at T > 0)."""
         ctx = ctx or default_context()
         dh = self.device(ctx)
         lo, hi = C.c_double(), C.c_double()
-        ctx.check(ctx.lib.lm_ham_bounds(dh.handle, C.byref(lo), C.byref(hi)))
+        if method == "gershgorin":
+            ctx.check(ctx.lib.lm_ham_bounds(dh.handle, C.byref(lo), C.byref(hi)))
+        elif method == "lanczos":
+            ctx.check(ctx.lib.lm_ham_lanczos_bounds(dh.handle, int(iters), int(seed), C.byref(lo), C.byref(hi)))
+        else:
+            raise ValueError("method must be gershgorin or lanczos")
         return lo.value, hi.value
 
 

@@ -31,8 +31,8 @@ from .lattice import LatticeValue
 from .states import DeviceState
 
 
-def _bounds(H: Hamiltonian, ctx, pad=1e-3):
-    lo, hi = H.bounds(ctx)
+def _bounds(H: Hamiltonian, ctx, pad=1e-3, method: str = "gershgorin"):
+    lo, hi = H.bounds(ctx, method=method)
     w = hi - lo
     return lo - pad * w, hi + pad * w
 
@@ -95,11 +95,12 @@ def resolvent_trace(mu, E, broaden: float, bounds):
 
 
 def dos(H: Hamiltonian, E, broaden: float = 0.1, *, tol: float = 1e-11, nmom=None, exact_max: int = 8192,
-        nvec: int = 64, seed: int = 0, ctx=None):
+        nvec: int = 64, seed: int = 0, bounds: str = "gershgorin", ctx=None):
     """dos(H, E; broaden): Im sum_n 1/(E_n - E - i*broaden) / pi (src/greenfunction.jl:306)
-    from device Chebyshev moments.  Returns a float for a scalar E, else an array."""
+    from device Chebyshev moments.  Returns a float for a scalar E, else an array.  bounds:
+    "gershgorin" or "lanczos" (tighter interval, fewer moments)."""
     ctx = ctx or default_context()
-    bounds = _bounds(H, ctx)
+    bounds = _bounds(H, ctx, method=bounds)
     nm = nmom or order_for(E, broaden, bounds, tol)
     vecs = None if H.lattice.N <= exact_max else _phase_vectors(H.lattice.N, nvec, seed)
     mu, bounds = moments(H, nm, vecs, False, bounds, ctx)
@@ -108,11 +109,12 @@ def dos(H: Hamiltonian, E, broaden: float = 0.1, *, tol: float = 1e-11, nmom=Non
     return float(d[0]) if np.ndim(E) == 0 else d
 
 
-def ldos(H: Hamiltonian, E: float, broaden: float = 0.1, *, tol: float = 1e-11, nmom=None, ctx=None) -> LatticeValue:
+def ldos(H: Hamiltonian, E: float, broaden: float = 0.1, *, tol: float = 1e-11, nmom=None,
+         bounds: str = "gershgorin", ctx=None) -> LatticeValue:
     """Local density of states at every site, Im sum_n |psi_n(i)|^2/(E_n - E - i*broaden) / pi,
     from the per-site moments of the N unit vectors (exact)."""
     ctx = ctx or default_context()
-    bounds = _bounds(H, ctx)
+    bounds = _bounds(H, ctx, method=bounds)
     nm = nmom or order_for(E, broaden, bounds, tol)
     mu, bounds = moments(H, nm, None, True, bounds, ctx)
     g = resolvent_trace(mu, E, broaden, bounds)[0]

@@ -86,17 +86,18 @@ def fermi_occupation(mu: float, T: float):
 
 
 def densitymatrix(H: Hamiltonian, mu: float = 0.0, T: float = 0.0, precision="c64", method: str = "auto",
-                  tol: float = 1e-13) -> DensityMatrix:
+                  tol: float = 1e-13, bounds: str = "gershgorin") -> DensityMatrix:
     """``densitymatrix(H; mu, T)`` for a one-particle system with FermiDirac statistics
     (src/spectrum.jl:252-257).  method: "auto" (Chebyshev for T > 0, eigensolver for T = 0),
-    "chebyshev" or "eigh"."""
+    "chebyshev" or "eigh".  bounds: the spectral interval of the Chebyshev route,
+    "gershgorin" or "lanczos" (tighter: fewer terms)."""
     if method not in ("auto", "chebyshev", "eigh"):
         raise ValueError("method must be auto, chebyshev or eigh")
     if method == "chebyshev" and not T > 0:
         raise ValueError("the Chebyshev route needs T > 0 (the T = 0 occupation is a step)")
     if T > 0 and method != "eigh":
         ctx = default_context()
-        lo, hi = H.bounds(ctx)
+        lo, hi = H.bounds(ctx, method=bounds)
         pad = 1e-3 * (hi - lo)
         bounds = (lo - pad, hi + pad)
         coef = np.ascontiguousarray(chebyshev_coefficients(fermi_occupation(mu, T), bounds, tol))

@@ -105,3 +105,31 @@ def test_cheb_apply_on_kets_matches_dense_function(lm):
     ctx.check(ctx.lib.lm_cheb_apply(Hl.device(ctx).handle, lo, hi, coef.ctypes.data_as(C.POINTER(C.c_double)),
                                     len(coef), st.handle, out.handle))
     assert np.linalg.norm(out.to_numpy() - ref) <= 1e-12 * np.linalg.norm(ref)
+
+
+@pytest.mark.parametrize("L,per,field", [(9, False, "pf"), (20, True, "landau"), (31, False, "landau")])
+def test_lanczos_bounds_enclose_spectrum(lm, L, per, field):
+    """FP64 Lanczos bounds (lm_ham_lanczos_bounds) enclose the exact spectrum, sit inside the
+    Gershgorin interval and close to the exact extremes."""
+    ol, Ho, Hl = case(lm, L, per, field)
+    w = np.linalg.eigvalsh(Ho.toarray())
+    ctx = lm.default_context()
+    glo, ghi = Hl.bounds(ctx)
+    lo, hi = Hl.bounds(ctx, method="lanczos")
+    assert glo <= lo <= w[0] and w[-1] <= hi <= ghi
+    assert (hi - lo) <= 1.05 * (w[-1] - w[0])
+
+
+def test_densitymatrix_with_lanczos_bounds(lm):
+    ol, Ho, Hl = case(lm, 12, False, "pf")
+    Pref, _, _ = o.densitymatrix(Ho, mu=0.2, T=0.1)
+    P = lm.densitymatrix(Hl, mu=0.2, T=0.1, bounds="lanczos").to_numpy()
+    assert np.linalg.norm(P - Pref) <= 1e-11 * np.linalg.norm(Pref)
+
+
+def test_dos_with_lanczos_bounds(lm):
+    ol, Ho, Hl = case(lm, 14, False, "pf")
+    w = np.linalg.eigvalsh(Ho.toarray())
+    E = np.linspace(-4, 4, 9)
+    d = lm.kpm.dos(Hl, E, 0.1, bounds="lanczos")
+    assert np.abs(d - o.dos_eigensystem(w, E, 0.1)).max() <= 1e-9 * d.max()
