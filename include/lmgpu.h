@@ -231,6 +231,27 @@ int lm_bond_currents(lm_ham *ham, lm_state *st, double *out);
 /* tr(P) = sum of the local densities, FP64 (particle number). */
 int lm_trace(lm_state *st, double *out);
 
+/* ---- general sparse Hamiltonians (other lattices, internal degrees of freedom) -------------- */
+/* Any Hermitian operator that the reference's construct_operator builds
+ * (src/operators/constructoperator.jl:4-47) -- HoneycombLattice, KagomeLattice, qwz and the
+ * other zoo models, next-nearest hopping -- given as its SparseMatrixCSC: 1-based colptr
+ * (n+1) and rowval (nnz), nzval as interleaved (re, im) pairs.  Stored on the device in ELL
+ * form; LM_ERR_ARG when the matrix is not Hermitian to 1e-12 of its largest entry. */
+typedef struct lm_ell lm_ell;
+int lm_ell_create_csc(lm_ctx *ctx, int64_t n, const int64_t *colptr, const int64_t *rowval, const double *nzval,
+                      lm_ell **out);
+int lm_ell_destroy(lm_ell *h);
+/* New values on the same pattern (H(t) every step). */
+int lm_ell_set_values(lm_ell *h, const double *nzval);
+/* Gershgorin interval of the current values. */
+int lm_ell_bounds(const lm_ell *h, double *emin, double *emax);
+/* update_solver!(solver, H, dt, force) for a general Hamiltonian (src/evolution.jl:83-92);
+ * lm_solver_step then applies its propagator to kets or density matrices. */
+int lm_ell_solver_update(lm_solver *s, lm_ell *h, double dt, int force);
+/* DensityCurrents(H, state)[i, j] = 2 Im(H[i,j] P[j,i]) (src/zoo/currents.jl:92-102) for every
+ * stored entry of the CSC, in its order (0 for the diagonal): nnz doubles. */
+int lm_ell_currents(lm_ell *h, lm_state *st, double *out);
+
 /* ---- KPM moments (DOS / LDOS without an eigensystem; the reference computes dos and ldos
  * from an Eigensystem or GreenFunction, src/greenfunction.jl:306-339) ------------------------ */
 /* mu_n = sum over the columns v of the block of <v| T_n(H~) |v>, H~ = (H - b)/a with

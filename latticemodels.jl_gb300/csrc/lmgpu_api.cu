@@ -761,6 +761,7 @@ int lm_solver_destroy(lm_solver* s) {
     cudaSetDevice(s->ctx->device);
     cudaStreamSynchronize(s->ctx->stream);
     free_tables(s);
+    ell_free_tables(s);
     delete s;
     return LM_OK;
 }
@@ -793,24 +794,11 @@ int lm_solver_update(lm_solver* s, lm_ham* h, double dt, int force) {
     }
     double emin, emax;
     lm_ham_bounds(h, &emin, &emax);
-    if (s->fixed_bounds) {
-        emin = s->fix_emin;
-        emax = s->fix_emax;
-    }
-    const double hw = 0.5 * (emax - emin);
-    const double a = std::max(hw * (1.0 + 1e-12) + 1e-300, 1e-12);
-    const double b = 0.5 * (emax + emin);
-    const double x = a * fabs(dt);
-    std::vector<double> J;
-    const int K = cheb_order_for(x, s->tol, J);
-    make_coefs(J, K, dt >= 0 ? 1.0 : -1.0, s->coef);
-    s->phase_re = cos(b * dt);
-    s->phase_im = -sin(b * dt);
-    s->a = a;
-    s->b = b;
-    s->K = K;
-    CUDA_TRY(ctx, launch_normalise(ctx, g, h->d_hop, h->d_onsite, a, b, s->d_hop2, s->d_diag2, s->d_hop2f, s->d_diag2f),
+    plan_propagator(s, emin, emax, dt);
+    CUDA_TRY(ctx, launch_normalise(ctx, g, h->d_hop, h->d_onsite, s->a, s->b, s->d_hop2, s->d_diag2, s->d_hop2f,
+                                   s->d_diag2f),
              "normalise kernel");
+    s->ell = nullptr;
     s->ham = h;
     s->ham_version = h->version;
     s->dt = dt;
@@ -818,6 +806,30 @@ int lm_solver_update(lm_solver* s, lm_ham* h, double dt, int force) {
     s->has_onsite = h->d_onsite != nullptr;
     return LM_OK;
 }
+
+}  // extern "C"
+
+namespace lmgpu {
+void plan_propagator(lm_solver* s, double emin, double emax, double dt) {
+    if (s->fixed_bounds) {
+        emin = s->fix_emin;
+        emax = s->fix_emax;
+    }
+    const double hw = 0.5 * (emax - emin);
+    const double a = std::max(hw * (1.0 + 1e-12) + 1e-300, 1e-12);
+    const double b = 0.5 * (emax + emin);
+    std::vector<double> J;
+    const int K = cheb_order_for(a * fabs(dt), s->tol, J);
+    make_coefs(J, K, dt >= 0 ? 1.0 : -1.0, s->coef);
+    s->phase_re = cos(b * dt);
+    s->phase_im = -sin(b * dt);
+    s->a = a;
+    s->b = b;
+    s->K = K;
+}
+}  // namespace lmgpu
+
+extern "C" {
 
 int lm_solver_order(const lm_solver* s, int* K, double* a, double* b) {
     if (!s) return LM_ERR_ARG;
@@ -887,6 +899,7 @@ int lm_solver_step(lm_solver* s, lm_state* st) {
     CHECK_ARG(ctx, st != nullptr, "lm_solver_step: null state");
     CHECK_ARG(ctx, st->ctx == ctx, "lm_solver_step: state belongs to another context");
     if (!s->valid) return set_err(ctx, LM_ERR_STATE, "lm_solver_step: update_solver must run before step");
+    if (s->ell) return ell_solver_step(s, st);
     const Geom& g = s->ham->lat->g;
     CHECK_ARG(ctx, st->n == g.N, "lm_solver_step: state size does not match the lattice");
     cudaSetDevice(ctx->device);

@@ -1,0 +1,470 @@
+// General sparse Hamiltonians: any Hermitian operator that the reference's construct_operator
+// builds (src/operators/constructoperator.jl:4-47) -- other lattices (HoneycombLattice,
+// KagomeLattice, src/zoo/lattices.jl:145-211), internal degrees of freedom (qwz,
+// src/zoo/models.jl:129-137), longer-range hopping -- given as its SparseMatrixCSC.  On the
+// device it is an ELL table (row i: up to w off-diagonal (column, value) pairs, column-major
+// over the rows so that consecutive threads read consecutive entries) plus the real diagonal.
+// The Chebyshev propagator is the same as for the square lattice; only the stencil differs.
+#include <cuda_runtime.h>
+#include <math.h>
+
+#include <algorithm>
+#include <new>
+#include <unordered_map>
+#include <vector>
+
+#include "lmgpu_internal.cuh"
+#include "lmgpu_order.cuh"
+
+namespace lmgpu {
+
+// 2H/a off the diagonal and 2(H_ii - b)/a on it, in FP64 and FP32.
+__global__ void ell_normalise_kernel(int64_t n, int w, const double2* __restrict__ vals,
+                                     const double* __restrict__ diag, double a, double b, double2* __restrict__ v2,
+                                     double* __restrict__ d2, float2* __restrict__ v2f, float* __restrict__ d2f) {
+    const double sc = 2.0 / a;
+    const int64_t tot = n * (int64_t)w;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < tot + n; i += (int64_t)gridDim.x * blockDim.x) {
+        if (i < tot) {
+            const double2 v = make_double2(vals[i].x * sc, vals[i].y * sc);
+            v2[i] = v;
+            v2f[i] = make_float2((float)v.x, (float)v.y);
+        } else {
+            const int64_t r = i - tot;
+            const double d = (diag[r] - b) * sc;
+            d2[r] = d;
+            d2f[r] = (float)d;
+        }
+    }
+}
+
+// One Chebyshev order over an n x M block with the ELL stencil (see cheb_epilogue for the
+// modes).  SITE_FAST: element (site, ket) at ket*ld + site, threads over sites; otherwise at
+// site*ld + ket (rows of a density matrix), threads over kets.  CONJ applies conj(H).
+template <typename R, int MODE, bool SITE_FAST, bool CONJ>
+__global__ void __launch_bounds__(256) cheb_order_ell_kernel(
+    int64_t n, int w, const int* __restrict__ cols, const typename CT<R>::V* __restrict__ v2,
+    const R* __restrict__ d2, const typename CT<R>::V* __restrict__ tp, typename CT<R>::V* tq,
+    typename CT<R>::V* y, int64_t ld, int64_t M, R c0, R cs, int odd, R ph_re, R ph_im, ChebLo lo) {
+    typedef typename CT<R>::V V;
+    const int64_t lane = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t nfast = SITE_FAST ? n : M;
+    const int64_t nslow = SITE_FAST ? M : n;
+    if (lane >= nfast) return;
+    for (int64_t slow = blockIdx.y; slow < nslow; slow += gridDim.y) {
+        const int64_t site = SITE_FAST ? lane : slow;
+        const int64_t ket = SITE_FAST ? slow : lane;
+        auto at = [&](int64_t s) -> int64_t { return SITE_FAST ? ket * ld + s : s * ld + ket; };
+        const V v0 = tp[at(site)];
+        V acc;
+        if (MODE == CHEB_FIRST) {
+            acc = CT<R>::make(0, 0);
+        } else {
+            const V q = tq[at(site)];
+            acc = CT<R>::make(-q.x, -q.y);
+        }
+        for (int k = 0; k < w; ++k) {
+            const int64_t e = (int64_t)k * n + site;
+            const int c = __ldg(cols + e);
+            V h = v2[e];
+            if (CONJ) h.y = -h.y;
+            const V v = tp[at(c)];
+            acc.x = fma(h.x, v.x, acc.x); acc.x = fma(-h.y, v.y, acc.x);
+            acc.y = fma(h.x, v.y, acc.y); acc.y = fma(h.y, v.x, acc.y);
+        }
+        const R d = d2[site];
+        acc.x = fma(d, v0.x, acc.x);
+        acc.y = fma(d, v0.y, acc.y);
+        cheb_epilogue<R, MODE>(acc, v0, tq, y, at(site), c0, cs, odd, ph_re, ph_im, lo);
+    }
+}
+
+template <typename R, int MODE, bool SF, bool CJ>
+static cudaError_t launch_ell_t(lm_ctx* ctx, const lm_ell* h, const void* v2, const void* d2, const void* tp, void* tq,
+                                void* y, int64_t ld, int64_t m, double c0, ChebCoef ck, double pr, double pi,
+                                ChebLo lo) {
+    typedef typename CT<R>::V V;
+    const int thr = 256;
+    const int64_t nfast = SF ? h->n : m;
+    const int64_t nslow = SF ? m : h->n;
+    dim3 grid((unsigned)((nfast + thr - 1) / thr), (unsigned)std::min<int64_t>(nslow, 65535));
+    cheb_order_ell_kernel<R, MODE, SF, CJ><<<grid, thr, 0, ctx->stream>>>(
+        h->n, h->w, h->d_cols, (const V*)v2, (const R*)d2, (const V*)tp, (V*)tq, (V*)y, ld, m, (R)c0, (R)ck.s, ck.odd,
+        (R)pr, (R)pi, lo);
+    ctx->launches++;
+    return cudaGetLastError();
+}
+
+template <typename R, bool SF, bool CJ>
+static cudaError_t launch_ell_mode(int mode, lm_ctx* ctx, const lm_ell* h, const void* v2, const void* d2,
+                                   const void* tp, void* tq, void* y, int64_t ld, int64_t m, double c0, ChebCoef ck,
+                                   double pr, double pi, ChebLo lo) {
+    if (mode == CHEB_FIRST) return launch_ell_t<R, CHEB_FIRST, SF, CJ>(ctx, h, v2, d2, tp, tq, y, ld, m, c0, ck, pr, pi, lo);
+    if (mode == CHEB_MID) return launch_ell_t<R, CHEB_MID, SF, CJ>(ctx, h, v2, d2, tp, tq, y, ld, m, c0, ck, pr, pi, lo);
+    return launch_ell_t<R, CHEB_LAST, SF, CJ>(ctx, h, v2, d2, tp, tq, y, ld, m, c0, ck, pr, pi, lo);
+}
+
+static cudaError_t launch_ell_order(lm_ctx* ctx, const lm_ell* h, int precision, int site_fast, int conj, int mode,
+                                    const void* v2, const void* d2, const void* tp, void* tq, void* y, int64_t ld,
+                                    int64_t m, double c0, ChebCoef ck, double pr, double pi, ChebLo lo) {
+    if (precision == LM_C64) {
+        if (site_fast) {
+            return conj ? launch_ell_mode<double, true, true>(mode, ctx, h, v2, d2, tp, tq, y, ld, m, c0, ck, pr, pi, lo)
+                        : launch_ell_mode<double, true, false>(mode, ctx, h, v2, d2, tp, tq, y, ld, m, c0, ck, pr, pi, lo);
+        }
+        return conj ? launch_ell_mode<double, false, true>(mode, ctx, h, v2, d2, tp, tq, y, ld, m, c0, ck, pr, pi, lo)
+                    : launch_ell_mode<double, false, false>(mode, ctx, h, v2, d2, tp, tq, y, ld, m, c0, ck, pr, pi, lo);
+    }
+    if (site_fast) {
+        return conj ? launch_ell_mode<float, true, true>(mode, ctx, h, v2, d2, tp, tq, y, ld, m, c0, ck, pr, pi, lo)
+                    : launch_ell_mode<float, true, false>(mode, ctx, h, v2, d2, tp, tq, y, ld, m, c0, ck, pr, pi, lo);
+    }
+    return conj ? launch_ell_mode<float, false, true>(mode, ctx, h, v2, d2, tp, tq, y, ld, m, c0, ck, pr, pi, lo)
+                : launch_ell_mode<float, false, false>(mode, ctx, h, v2, d2, tp, tq, y, ld, m, c0, ck, pr, pi, lo);
+}
+
+// One application of the series to (site_fast, ld, m)-laid-out columns S (T0 on entry); the
+// result lands in S (K even) or A (K odd): *where = 0 / 1.
+static int ell_apply(lm_solver* s, int precision, int site_fast, int conj, void* S, void* A, void* Y, int64_t ld,
+                     int64_t m, int* where) {
+    lm_ctx* ctx = s->ctx;
+    const lm_ell* h = s->ell;
+    const void* v2 = precision == LM_C64 ? (const void*)s->d_ev2 : (const void*)s->d_ev2f;
+    const void* d2 = precision == LM_C64 ? (const void*)s->d_ed2 : (const void*)s->d_ed2f;
+    const int K = s->K;
+    const double c0 = s->coef[0].s;
+    const double pr = s->phase_re, pi = conj ? -s->phase_im : s->phase_im;
+    auto coef = [&](int k) {
+        ChebCoef c = s->coef[(size_t)k];
+        if (conj && c.odd) c.s = -c.s;
+        return c;
+    };
+    const ChebLo lo = cheb_lo(pr, pi, c0, coef(1).s, false);
+    CUDA_TRY(ctx, launch_ell_order(ctx, h, precision, site_fast, conj, CHEB_FIRST, v2, d2, S, A, Y, ld, m, c0, coef(1), pr,
+                                   pi, lo),
+             "ell chebyshev order 1");
+    for (int k = 2; k <= K; ++k) {
+        const void* tp = (k % 2 == 0) ? A : S;
+        void* tq = (k % 2 == 0) ? S : A;
+        const int mode = (k == K) ? CHEB_LAST : CHEB_MID;
+        CUDA_TRY(ctx, launch_ell_order(ctx, h, precision, site_fast, conj, mode, v2, d2, tp, tq, Y, ld, m, c0, coef(k), pr,
+                                       pi, lo),
+                 "ell chebyshev order");
+    }
+    *where = (K % 2 == 0) ? 0 : 1;
+    return LM_OK;
+}
+
+int ell_solver_step(lm_solver* s, lm_state* st) {
+    lm_ctx* ctx = s->ctx;
+    CHECK_ARG(ctx, st->n == s->ell->n, "lm_solver_step: state size does not match the Hamiltonian");
+    cudaSetDevice(ctx->device);
+    if (!st->d_y) {
+        const size_t bytes = st->elem * (size_t)st->ld * (size_t)st->m;
+        if (cudaMalloc(&st->d_y, bytes) != cudaSuccess) {
+            st->d_y = nullptr;
+            cudaGetLastError();
+            return set_err(ctx, LM_ERR_OOM, "lm_solver_step: accumulator allocation");
+        }
+    }
+    int where = 0;
+    int rc = ell_apply(s, st->precision, 1, 0, st->d_data, st->d_a, st->d_y, st->ld, st->m, &where);
+    if (rc != LM_OK) return rc;
+    if (where == 1) std::swap(st->d_data, st->d_a);
+    if (st->kind == LM_DENSITY) {  // P <- X U^dagger: conj(U) on every row of X
+        rc = ell_apply(s, st->precision, 0, 1, st->d_data, st->d_a, st->d_y, st->ld, st->m, &where);
+        if (rc != LM_OK) return rc;
+        if (where == 1) std::swap(st->d_data, st->d_a);
+    }
+    return LM_OK;
+}
+
+void ell_free_tables(lm_solver* s) {
+    cudaFree(s->d_ev2);
+    cudaFree(s->d_ed2);
+    cudaFree(s->d_ev2f);
+    cudaFree(s->d_ed2f);
+    s->d_ev2 = nullptr;
+    s->d_ed2 = nullptr;
+    s->d_ev2f = nullptr;
+    s->d_ed2f = nullptr;
+    s->ell_tab = 0;
+}
+
+// J for every CSC entry: 2 Im(H[i,j] P[j,i]); ket blocks sum over the kets (one thread per
+// entry, FP64), density matrices read P[j,i].
+template <typename R>
+__global__ void ell_currents_kernel(int64_t nnz, const int* __restrict__ row, const int* __restrict__ col,
+                                    const double2* __restrict__ hv, int kind, const typename CT<R>::V* __restrict__ x,
+                                    int64_t m, int64_t ld, const double* __restrict__ wts, double* __restrict__ out) {
+    for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < nnz; p += (int64_t)gridDim.x * blockDim.x) {
+        const int i = row[p], j = col[p];
+        if (i == j) {
+            out[p] = 0.0;
+            continue;
+        }
+        double pr = 0.0, pim = 0.0;  // P[j, i]
+        if (kind == LM_DENSITY) {
+            const typename CT<R>::V v = x[(int64_t)i * ld + j];
+            pr = v.x;
+            pim = v.y;
+        } else {
+            for (int64_t k = 0; k < m; ++k) {
+                const typename CT<R>::V a = x[k * ld + j], b = x[k * ld + i];  // a conj(b)
+                const double ww = wts ? wts[k] : 1.0;
+                pr += ww * ((double)a.x * b.x + (double)a.y * b.y);
+                pim += ww * ((double)a.y * b.x - (double)a.x * b.y);
+            }
+        }
+        const double2 h = hv[p];
+        out[p] = 2.0 * (h.x * pim + h.y * pr);
+    }
+}
+
+}  // namespace lmgpu
+
+using namespace lmgpu;
+
+// Fills the ELL host staging from CSC values (pattern fixed at creation).
+static void ell_stage(lm_ell* h, const double* nzval) {
+    std::fill(h->h_vals.begin(), h->h_vals.end(), make_double2(0.0, 0.0));
+    std::fill(h->h_diag.begin(), h->h_diag.end(), 0.0);
+    for (int64_t p = 0; p < h->nnz; ++p) {
+        const int64_t slot = h->map[(size_t)p];
+        if (slot < 0) h->h_diag[(size_t)(-slot - 1)] += nzval[2 * p];
+        else h->h_vals[(size_t)slot] = make_double2(nzval[2 * p], nzval[2 * p + 1]);
+    }
+}
+
+static int ell_check_and_bounds(lm_ell* h, const double* nzval) {
+    lm_ctx* ctx = h->ctx;
+    double vmax = 0.0;
+    for (int64_t p = 0; p < h->nnz; ++p) {
+        if (!isfinite(nzval[2 * p]) || !isfinite(nzval[2 * p + 1]))
+            return set_err(ctx, LM_ERR_NONFINITE, "lm_ell: non-finite matrix entry");
+        vmax = std::max(vmax, hypot(nzval[2 * p], nzval[2 * p + 1]));
+    }
+    // Hermitian: H[i,j] = conj(H[j,i]) (the transpose entry must be stored too)
+    std::unordered_map<int64_t, int64_t> where;
+    where.reserve((size_t)h->nnz * 2);
+    for (int64_t p = 0; p < h->nnz; ++p) where[h->csc_row[(size_t)p] * h->n + h->csc_col[(size_t)p]] = p;
+    const double tol = 1e-12 * std::max(vmax, 1e-300);
+    std::vector<double> rad((size_t)h->n, 0.0), dia((size_t)h->n, 0.0);
+    for (int64_t p = 0; p < h->nnz; ++p) {
+        const int64_t i = h->csc_row[(size_t)p], j = h->csc_col[(size_t)p];
+        const double re = nzval[2 * p], im = nzval[2 * p + 1];
+        if (i == j) {
+            if (fabs(im) > tol) return set_err(ctx, LM_ERR_ARG, "lm_ell: diagonal entry with an imaginary part");
+            dia[(size_t)i] += re;
+            continue;
+        }
+        auto it = where.find(j * h->n + i);
+        const double tre = it == where.end() ? 0.0 : nzval[2 * it->second];
+        const double tim = it == where.end() ? 0.0 : nzval[2 * it->second + 1];
+        if (fabs(re - tre) > tol || fabs(im + tim) > tol) return set_err(ctx, LM_ERR_ARG, "lm_ell: matrix is not Hermitian");
+        rad[(size_t)i] += hypot(re, im);
+    }
+    h->emin = dia[0] - rad[0];
+    h->emax = dia[0] + rad[0];
+    for (int64_t i = 1; i < h->n; ++i) {
+        h->emin = std::min(h->emin, dia[(size_t)i] - rad[(size_t)i]);
+        h->emax = std::max(h->emax, dia[(size_t)i] + rad[(size_t)i]);
+    }
+    return LM_OK;
+}
+
+static int ell_upload(lm_ell* h, const double* nzval) {
+    lm_ctx* ctx = h->ctx;
+    ell_stage(h, nzval);
+    std::vector<double2> cval((size_t)h->nnz);
+    for (int64_t p = 0; p < h->nnz; ++p) cval[(size_t)p] = make_double2(nzval[2 * p], nzval[2 * p + 1]);
+    CUDA_TRY(ctx, cudaMemcpyAsync(h->d_vals, h->h_vals.data(), sizeof(double2) * h->h_vals.size(), cudaMemcpyHostToDevice,
+                                  ctx->stream), "upload ell values");
+    CUDA_TRY(ctx, cudaMemcpyAsync(h->d_diag, h->h_diag.data(), sizeof(double) * h->h_diag.size(), cudaMemcpyHostToDevice,
+                                  ctx->stream), "upload ell diagonal");
+    CUDA_TRY(ctx, cudaMemcpyAsync(h->d_cval, cval.data(), sizeof(double2) * cval.size(), cudaMemcpyHostToDevice,
+                                  ctx->stream), "upload csc values");
+    // the staging vectors are reused by the next call: wait for the copies
+    CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream), "sync");
+    h->version++;
+    return LM_OK;
+}
+
+extern "C" {
+
+int lm_ell_create_csc(lm_ctx* ctx, int64_t n, const int64_t* colptr, const int64_t* rowval, const double* nzval,
+                      lm_ell** out) {
+    if (!ctx) return LM_ERR_ARG;
+    CHECK_ARG(ctx, out && colptr && rowval && nzval, "lm_ell_create_csc: null argument");
+    *out = nullptr;
+    CHECK_ARG(ctx, n >= 1 && n < ((int64_t)1 << 31), "lm_ell_create_csc: bad size");
+    CHECK_ARG(ctx, colptr[0] == 1, "lm_ell_create_csc: colptr must start at 1");
+    const int64_t nnz = colptr[n] - 1;
+    CHECK_ARG(ctx, nnz >= 0, "lm_ell_create_csc: bad colptr");
+    for (int64_t j = 0; j < n; ++j) CHECK_ARG(ctx, colptr[j + 1] >= colptr[j], "lm_ell_create_csc: colptr not monotone");
+    for (int64_t p = 0; p < nnz; ++p)
+        CHECK_ARG(ctx, rowval[p] >= 1 && rowval[p] <= n, "lm_ell_create_csc: row index out of range");
+    lm_ell* h = new (std::nothrow) lm_ell();
+    if (!h) return set_err(ctx, LM_ERR_OOM, "host allocation");
+    h->ctx = ctx;
+    h->n = n;
+    h->nnz = nnz;
+    h->csc_row.resize((size_t)nnz);
+    h->csc_col.resize((size_t)nnz);
+    std::vector<int> count((size_t)n, 0);
+    for (int64_t j = 0; j < n; ++j)
+        for (int64_t p = colptr[j] - 1; p < colptr[j + 1] - 1; ++p) {
+            h->csc_row[(size_t)p] = rowval[p] - 1;
+            h->csc_col[(size_t)p] = j;
+            if (rowval[p] - 1 != j) count[(size_t)(rowval[p] - 1)]++;
+        }
+    int rc = ell_check_and_bounds(h, nzval);
+    if (rc != LM_OK) {
+        delete h;
+        return rc;
+    }
+    h->w = std::max(1, *std::max_element(count.begin(), count.end()));
+    // slots: row i's off-diagonal entries in CSC (column) order; unused slots point at i
+    std::vector<int> cols((size_t)n * h->w);
+    for (int k = 0; k < h->w; ++k)
+        for (int64_t i = 0; i < n; ++i) cols[(size_t)k * n + i] = (int)i;
+    std::vector<int> fill((size_t)n, 0);
+    h->map.resize((size_t)nnz);
+    for (int64_t p = 0; p < nnz; ++p) {
+        const int64_t i = h->csc_row[(size_t)p], j = h->csc_col[(size_t)p];
+        if (i == j) {
+            h->map[(size_t)p] = -(i + 1);
+        } else {
+            const int k = fill[(size_t)i]++;
+            cols[(size_t)k * n + i] = (int)j;
+            h->map[(size_t)p] = (int64_t)k * n + i;
+        }
+    }
+    h->h_vals.resize((size_t)n * h->w);
+    h->h_diag.resize((size_t)n);
+    std::vector<int> crow((size_t)nnz), ccol((size_t)nnz);
+    for (int64_t p = 0; p < nnz; ++p) {
+        crow[(size_t)p] = (int)h->csc_row[(size_t)p];
+        ccol[(size_t)p] = (int)h->csc_col[(size_t)p];
+    }
+    cudaSetDevice(ctx->device);
+    cudaError_t e = cudaMalloc((void**)&h->d_cols, sizeof(int) * cols.size());
+    if (e == cudaSuccess) e = cudaMalloc((void**)&h->d_vals, sizeof(double2) * h->h_vals.size());
+    if (e == cudaSuccess) e = cudaMalloc((void**)&h->d_diag, sizeof(double) * (size_t)n);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&h->d_crow, sizeof(int) * (size_t)std::max<int64_t>(nnz, 1));
+    if (e == cudaSuccess) e = cudaMalloc((void**)&h->d_ccol, sizeof(int) * (size_t)std::max<int64_t>(nnz, 1));
+    if (e == cudaSuccess) e = cudaMalloc((void**)&h->d_cval, sizeof(double2) * (size_t)std::max<int64_t>(nnz, 1));
+    if (e == cudaSuccess)
+        e = cudaMemcpy(h->d_cols, cols.data(), sizeof(int) * cols.size(), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && nnz > 0) e = cudaMemcpy(h->d_crow, crow.data(), sizeof(int) * crow.size(), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && nnz > 0) e = cudaMemcpy(h->d_ccol, ccol.data(), sizeof(int) * ccol.size(), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        rc = check_cuda(ctx, e, "lm_ell_create_csc: device tables");
+        lm_ell_destroy(h);
+        return rc;
+    }
+    rc = ell_upload(h, nzval);
+    if (rc != LM_OK) {
+        lm_ell_destroy(h);
+        return rc;
+    }
+    *out = h;
+    return LM_OK;
+}
+
+int lm_ell_destroy(lm_ell* h) {
+    if (!h) return LM_OK;
+    cudaSetDevice(h->ctx->device);
+    cudaStreamSynchronize(h->ctx->stream);
+    cudaFree(h->d_cols);
+    cudaFree(h->d_vals);
+    cudaFree(h->d_diag);
+    cudaFree(h->d_crow);
+    cudaFree(h->d_ccol);
+    cudaFree(h->d_cval);
+    delete h;
+    return LM_OK;
+}
+
+int lm_ell_set_values(lm_ell* h, const double* nzval) {
+    if (!h) return LM_ERR_ARG;
+    CHECK_ARG(h->ctx, nzval != nullptr, "lm_ell_set_values: null values");
+    int rc = ell_check_and_bounds(h, nzval);
+    if (rc != LM_OK) return rc;
+    cudaSetDevice(h->ctx->device);
+    return ell_upload(h, nzval);
+}
+
+int lm_ell_bounds(const lm_ell* h, double* emin, double* emax) {
+    if (!h) return LM_ERR_ARG;
+    CHECK_ARG(h->ctx, emin && emax, "lm_ell_bounds: null output");
+    *emin = h->emin;
+    *emax = h->emax;
+    return LM_OK;
+}
+
+int lm_ell_solver_update(lm_solver* s, lm_ell* h, double dt, int force) {
+    if (!s) return LM_ERR_ARG;
+    lm_ctx* ctx = s->ctx;
+    CHECK_ARG(ctx, h != nullptr && h->ctx == ctx, "lm_ell_solver_update: bad Hamiltonian");
+    CHECK_ARG(ctx, isfinite(dt), "lm_ell_solver_update: non-finite dt");
+    // cache hit: same H and same factor -i*dt (src/evolution.jl:86-88)
+    if (!force && s->valid && s->ell == h && s->ell_version == h->version &&
+        fabs(dt - s->dt) <= 1.4901161193847656e-08 * std::max(fabs(dt), fabs(s->dt)))
+        return LM_OK;
+    cudaSetDevice(ctx->device);
+    const int64_t tab = h->n * (int64_t)h->w;
+    if (s->ell_tab != tab + h->n) {
+        ell_free_tables(s);
+        cudaError_t e = cudaMalloc((void**)&s->d_ev2, sizeof(double2) * (size_t)tab);
+        if (e == cudaSuccess) e = cudaMalloc((void**)&s->d_ed2, sizeof(double) * (size_t)h->n);
+        if (e == cudaSuccess) e = cudaMalloc((void**)&s->d_ev2f, sizeof(float2) * (size_t)tab);
+        if (e == cudaSuccess) e = cudaMalloc((void**)&s->d_ed2f, sizeof(float) * (size_t)h->n);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            ell_free_tables(s);
+            s->valid = 0;
+            return check_cuda(ctx, e, "lm_ell_solver_update: tables");
+        }
+        s->ell_tab = tab + h->n;
+    }
+    plan_propagator(s, h->emin, h->emax, dt);
+    const unsigned grid = (unsigned)std::min<int64_t>((tab + h->n + 255) / 256, 4096);
+    ell_normalise_kernel<<<grid, 256, 0, ctx->stream>>>(h->n, h->w, h->d_vals, h->d_diag, s->a, s->b, s->d_ev2, s->d_ed2,
+                                                        s->d_ev2f, s->d_ed2f);
+    ctx->launches++;
+    CUDA_TRY(ctx, cudaGetLastError(), "ell normalise kernel");
+    s->ell = h;
+    s->ell_version = h->version;
+    s->ham = nullptr;
+    s->dt = dt;
+    s->valid = 1;
+    return LM_OK;
+}
+
+int lm_ell_currents(lm_ell* h, lm_state* st, double* out) {
+    if (!h) return LM_ERR_ARG;
+    lm_ctx* ctx = h->ctx;
+    CHECK_ARG(ctx, st != nullptr && st->ctx == ctx && st->n == h->n, "lm_ell_currents: state does not match");
+    CHECK_ARG(ctx, out != nullptr, "lm_ell_currents: null output");
+    if (h->nnz == 0) return LM_OK;
+    cudaSetDevice(ctx->device);
+    double* d_out = nullptr;
+    CUDA_TRY(ctx, cudaMalloc((void**)&d_out, sizeof(double) * (size_t)h->nnz), "lm_ell_currents: allocation");
+    const unsigned grid = (unsigned)std::min<int64_t>((h->nnz + 255) / 256, 65535);
+    if (st->precision == LM_C64)
+        ell_currents_kernel<double><<<grid, 256, 0, ctx->stream>>>(h->nnz, h->d_crow, h->d_ccol, h->d_cval, st->kind,
+                                                                   (const double2*)st->d_data, st->m, st->ld, st->d_w, d_out);
+    else
+        ell_currents_kernel<float><<<grid, 256, 0, ctx->stream>>>(h->nnz, h->d_crow, h->d_ccol, h->d_cval, st->kind,
+                                                                  (const float2*)st->d_data, st->m, st->ld, st->d_w, d_out);
+    ctx->launches++;
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out, d_out, sizeof(double) * (size_t)h->nnz, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    cudaFree(d_out);
+    return check_cuda(ctx, e, "lm_ell_currents");
+}
+
+}  // extern "C"

@@ -164,6 +164,35 @@ struct lm_solver {
     int has_onsite = 0;
     int fixed_bounds = 0;        // lm_solver_set_bounds: use [fix_emin, fix_emax] instead of Gershgorin
     double fix_emin = 0.0, fix_emax = 0.0;
+    // general sparse Hamiltonian (lm_ell_*): set by lm_ell_solver_update, cleared by
+    // lm_solver_update; its normalised ELL values 2H/a (off-diagonal) and 2(H_ii - b)/a
+    const lm_ell* ell = nullptr;
+    uint64_t ell_version = ~0ull;
+    double2* d_ev2 = nullptr;  double* d_ed2 = nullptr;
+    float2* d_ev2f = nullptr;  float* d_ed2f = nullptr;
+    int64_t ell_tab = 0;
+};
+
+// A general Hermitian sparse Hamiltonian in ELL form: row i holds up to w off-diagonal
+// entries (column cols[k*n + i], value vals[k*n + i]; unused slots point at i with value 0)
+// and its real diagonal diag[i].  Built from the reference's CSC; `map` sends every CSC
+// entry to its ELL slot (k*n + i) or, for a diagonal entry, to -(i + 1).
+struct lm_ell {
+    lm_ctx* ctx = nullptr;
+    int64_t n = 0, nnz = 0;
+    int w = 0;
+    int* d_cols = nullptr;
+    double2* d_vals = nullptr;
+    double* d_diag = nullptr;
+    std::vector<int64_t> map;          // CSC entry -> ELL slot or -(row + 1) for the diagonal
+    std::vector<int64_t> csc_row, csc_col;  // 0-based row / column of every CSC entry
+    int* d_crow = nullptr;             // the same on the device (for the currents)
+    int* d_ccol = nullptr;
+    double2* d_cval = nullptr;         // CSC values on the device
+    double emin = 0.0, emax = 0.0;     // Gershgorin interval
+    uint64_t version = 0;
+    std::vector<double2> h_vals;       // host staging of the ELL values
+    std::vector<double> h_diag;
 };
 
 // Argument and CUDA-status checks that return the status from the calling C-ABI function.
@@ -218,6 +247,12 @@ cudaError_t launch_cheb_fused_c32(lm_ctx* ctx, const Geom& g, const float2* hop2
 // Every x-hop of H is real: Landau-gauge field components only (or none) and no twist across
 // a periodic x axis.  The fused kernel then skips the imaginary parts of the x-hops.
 bool ham_x_real(const lm_ham* h);
+// a, b, K, the Chebyshev coefficients and e^{-ib dt} of exp(-i H dt) on [emin, emax] (or on
+// the solver's frozen interval), lmgpu_api.cu.
+void plan_propagator(lm_solver* s, double emin, double emax, double dt);
+// lm_solver_step / destroy for a solver updated with an lm_ell Hamiltonian (lmgpu_ell.cu).
+int ell_solver_step(lm_solver* s, lm_state* st);
+void ell_free_tables(lm_solver* s);
 // out = alpha (2H~) tp - tpp + w lam over an n x M ket block (tables 2H/a, 2(V-b)/a); tpp and
 // lam may be null; out may alias tpp; with y non-null also y += cy out (lmgpu_adjoint.cu).
 cudaError_t launch_stencil_recur(lm_ctx* ctx, const Geom& g, int precision, const void* hop2, const void* diag2,

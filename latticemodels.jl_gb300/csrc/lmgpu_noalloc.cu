@@ -60,6 +60,7 @@ extern "C" int lm_solver_step_noalloc(lm_solver* s, void* kets, int64_t n, int64
     if (precision != LM_C64 && precision != LM_C32)
         return set_err(ctx, LM_ERR_ARG, "lm_solver_step_noalloc: unknown precision");
     if (!s->valid) return set_err(ctx, LM_ERR_STATE, "lm_solver_step_noalloc: update_solver must run before step");
+    if (s->ell) return set_err(ctx, LM_ERR_NOTSUP, "lm_solver_step_noalloc: square-lattice Hamiltonians only");
     const Geom& g = s->ham->lat->g;
     if (n != g.N || m < 1 || ld < n)
         return set_err(ctx, LM_ERR_ARG, "lm_solver_step_noalloc: block shape does not match the lattice");

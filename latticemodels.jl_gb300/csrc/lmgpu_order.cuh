@@ -84,6 +84,53 @@ __device__ __forceinline__ Nbr neighbours(const Geom& g, int64_t s) {
 //         otherwise   -> element (site, ket) at site*ld + ket (row of a column-major matrix).
 // CONJ applies conj(H) (used for the right factor U^dagger of a density-matrix step).
 // ------------------------------------------------------------------------------------------
+// Order epilogue at one (site, ket) element with index i, given acc = (2H~) T_{k-1} - T_{k-2}
+// (FIRST: acc = 2H~ T0 and v0 = T0):
+//   FIRST: T1 = acc/2 -> tq;  y = c0 T0 + c1 T1 (+ g0 T0 + g1 T1 in FP32, see ChebLo)
+//   MID  : T_k = acc -> tq;   y += c_k T_k
+//   LAST : out = phase * (y + c_K T_K) -> tq
+template <typename R, int MODE>
+__device__ __forceinline__ void cheb_epilogue(typename CT<R>::V acc, typename CT<R>::V v0, typename CT<R>::V* tq,
+                                              typename CT<R>::V* y, int64_t i, R c0, R cs, int odd, R ph_re, R ph_im,
+                                              const ChebLo& lo) {
+    typedef typename CT<R>::V V;
+    if (MODE == CHEB_FIRST) {
+        // T1 = (sum)/2 exactly, y = c0 T0 + c1 T1 with c1 = -i s (or +i s when conj)
+        const V t1 = CT<R>::make(acc.x * R(0.5), acc.y * R(0.5));
+        tq[i] = t1;
+        V yy;
+        if (sizeof(R) == sizeof(float)) {
+            // second words g0 T0 + g1 T1 first, the dominant c0 T0 last
+            R lx = fma(R(lo.g0_re), v0.x, fma(R(-lo.g0_im), v0.y, fma(R(lo.g1_re), t1.x, R(-lo.g1_im) * t1.y)));
+            R ly = fma(R(lo.g0_re), v0.y, fma(R(lo.g0_im), v0.x, fma(R(lo.g1_re), t1.y, R(lo.g1_im) * t1.x)));
+            yy.x = fma(c0, v0.x, fma(cs, t1.y, lx));
+            yy.y = fma(c0, v0.y, fma(-cs, t1.x, ly));
+        } else {
+            yy.x = fma(cs, t1.y, c0 * v0.x);
+            yy.y = fma(-cs, t1.x, c0 * v0.y);
+        }
+        y[i] = yy;
+    } else {
+        V yy = y[i];
+        if (odd) {
+            yy.x = fma(cs, acc.y, yy.x);
+            yy.y = fma(-cs, acc.x, yy.y);
+        } else {
+            yy.x = fma(cs, acc.x, yy.x);
+            yy.y = fma(cs, acc.y, yy.y);
+        }
+        if (MODE == CHEB_MID) {
+            tq[i] = acc;
+            y[i] = yy;
+        } else {
+            V o;
+            o.x = fma(ph_re, yy.x, -ph_im * yy.y);
+            o.y = fma(ph_re, yy.y, ph_im * yy.x);
+            tq[i] = o;
+        }
+    }
+}
+
 template <typename R, int MODE, bool SITE_FAST, bool CONJ, int INNER>
 __device__ __forceinline__ void cheb_order_block(
     const Geom& g, const typename CT<R>::V* __restrict__ hop2, const R* __restrict__ diag2,
@@ -143,41 +190,7 @@ __device__ __forceinline__ void cheb_order_block(
             acc.y = fma(hym.x, vym.y, acc.y); acc.y = fma(hym.y, vym.x, acc.y);
             acc.x = fma(d, v0.x, acc.x);
             acc.y = fma(d, v0.y, acc.y);
-            if (MODE == CHEB_FIRST) {
-                // T1 = (sum)/2 exactly, y = c0 T0 + c1 T1 with c1 = -i s (or +i s when conj)
-                const V t1 = CT<R>::make(acc.x * R(0.5), acc.y * R(0.5));
-                tq[at(site)] = t1;
-                V yy;
-                if (sizeof(R) == sizeof(float)) {
-                    // second words g0 T0 + g1 T1 first, the dominant c0 T0 last
-                    R lx = fma(R(lo.g0_re), v0.x, fma(R(-lo.g0_im), v0.y, fma(R(lo.g1_re), t1.x, R(-lo.g1_im) * t1.y)));
-                    R ly = fma(R(lo.g0_re), v0.y, fma(R(lo.g0_im), v0.x, fma(R(lo.g1_re), t1.y, R(lo.g1_im) * t1.x)));
-                    yy.x = fma(c0, v0.x, fma(cs, t1.y, lx));
-                    yy.y = fma(c0, v0.y, fma(-cs, t1.x, ly));
-                } else {
-                    yy.x = fma(cs, t1.y, c0 * v0.x);
-                    yy.y = fma(-cs, t1.x, c0 * v0.y);
-                }
-                y[at(site)] = yy;
-            } else {
-                V yy = y[at(site)];
-                if (odd) {
-                    yy.x = fma(cs, acc.y, yy.x);
-                    yy.y = fma(-cs, acc.x, yy.y);
-                } else {
-                    yy.x = fma(cs, acc.x, yy.x);
-                    yy.y = fma(cs, acc.y, yy.y);
-                }
-                if (MODE == CHEB_MID) {
-                    tq[at(site)] = acc;
-                    y[at(site)] = yy;
-                } else {
-                    V o;
-                    o.x = fma(ph_re, yy.x, -ph_im * yy.y);
-                    o.y = fma(ph_re, yy.y, ph_im * yy.x);
-                    tq[at(site)] = o;
-                }
-            }
+            cheb_epilogue<R, MODE>(acc, v0, tq, y, at(site), c0, cs, odd, ph_re, ph_im, lo);
         }
     }
 }

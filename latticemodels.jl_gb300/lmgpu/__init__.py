@@ -15,6 +15,7 @@ from .fields import FieldSum, LandauGauge, NoField, PointFlux, PointFluxes, Symm
 from .hamiltonian import Hamiltonian, tightbinding_hamiltonian
 from .lattice import LatticeValue, SquareLattice
 from .observables import Currents, DensityCurrents, localdensity
+from .sparse import Sites, SparseHamiltonian, entry_currents
 from .spectrum import densitymatrix, diagonalize
 from .states import DensityMatrix, DeviceState, Ket, KetBlock, Operator
 from .timesequence import (ReadoutRing, TimeSequence, differentiate, integrate, moment_currents,
@@ -27,5 +28,5 @@ __all__ = [
     "Hamiltonian", "tightbinding_hamiltonian", "LatticeValue", "SquareLattice",
     "Currents", "DensityCurrents", "localdensity", "densitymatrix", "diagonalize",
     "DensityMatrix", "DeviceState", "Ket", "KetBlock", "Operator",
-    "ReadoutRing", "TimeSequence", "differentiate", "integrate", "moment_currents", "moment_density",
+    "Sites", "SparseHamiltonian", "entry_currents", "ReadoutRing", "TimeSequence", "differentiate", "integrate", "moment_currents", "moment_density",
 ]

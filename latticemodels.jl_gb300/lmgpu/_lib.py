@@ -99,6 +99,12 @@ SIGNATURES = {
     "lm_localdensity": (_INT, [_P, _PD]),
     "lm_bond_currents": (_INT, [_P, _P, _PD]),
     "lm_trace": (_INT, [_P, _PD]),
+    "lm_ell_create_csc": (_INT, [_P, _I64, _PI64, _PI64, _PD, C.POINTER(_P)]),
+    "lm_ell_destroy": (_INT, [_P]),
+    "lm_ell_set_values": (_INT, [_P, _PD]),
+    "lm_ell_bounds": (_INT, [_P, _PD, _PD]),
+    "lm_ell_solver_update": (_INT, [_P, _P, _D, _INT]),
+    "lm_ell_currents": (_INT, [_P, _P, _PD]),
     "lm_kpm_moments": (_INT, [_P, _D, _D, _INT, _P, _INT, _PD]),
     "lm_cheb_apply": (_INT, [_P, _D, _D, _PD, _INT, _P, _P]),
     "lm_ham_lanczos_bounds": (_INT, [_P, _INT, C.c_ulonglong, _PD, _PD]),

@@ -71,8 +71,9 @@ class ChebyshevGPU(EvolutionSolver):
 
     def update_solver(self, H: Hamiltonian, dt: float, force: bool = False):
         """update_solver!(solver, H, dt, force) (src/evolution.jl:83-92)."""
-        if not isinstance(H, Hamiltonian):
-            raise TypeError("ChebyshevGPU evolves device Hamiltonians (tightbinding_hamiltonian)")
+        from .sparse import SparseHamiltonian
+        if not isinstance(H, (Hamiltonian, SparseHamiltonian)):
+            raise TypeError("ChebyshevGPU evolves device Hamiltonians (tightbinding_hamiltonian, SparseHamiltonian)")
         self._H = H
         self._dt = float(dt)
         self._force = bool(force)
@@ -81,7 +82,10 @@ class ChebyshevGPU(EvolutionSolver):
         tol = self._tol_for(state)
         s = self._solver(tol)
         dh = self._H.device(self.ctx)
-        self.ctx.check(self.ctx.lib.lm_solver_update(s, dh.handle, self._dt, 1 if self._force else 0))
+        if isinstance(self._H, Hamiltonian):
+            self.ctx.check(self.ctx.lib.lm_solver_update(s, dh.handle, self._dt, 1 if self._force else 0))
+        else:  # a general sparse Hamiltonian (other lattices, internal degrees of freedom)
+            self.ctx.check(self.ctx.lib.lm_ell_solver_update(s, dh.handle, self._dt, 1 if self._force else 0))
         return s
 
     def order(self, state=None):

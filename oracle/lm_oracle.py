@@ -749,3 +749,95 @@ def kpm_moments(H, emin, emax, nmom, vecs=None, per_column=False):
             Tn = T1
         mu[:, n] = np.real(np.sum(np.conj(V) * Tn, axis=0))
     return mu if per_column else mu.sum(axis=0)
+
+
+# ------------------------------------------------------------------------------------------
+# Other lattices and internal degrees of freedom, for the general sparse path (lm_ell_*).
+# ------------------------------------------------------------------------------------------
+HONEYCOMB_T = np.array([[1.0, 0.5], [0.0, math.sqrt(3) / 2]])      # unit vectors (columns)
+HONEYCOMB_BASIS = np.array([[0.0, 0.5], [0.0, math.sqrt(3) / 6]])  # basis sites (columns)
+
+
+def honeycomb_sites(a: int, b: int):
+    """HoneycombLattice(a, b) (src/zoo/lattices.jl:145-151): unit cells (j1, j2), 1 <= j1 <= a,
+    1 <= j2 <= b, two basis sites each; sites ordered by (j1, j2, basis index) as BravaisPointer
+    isless does (src/lattices/bravais/unitcell.jl:126-132).  Returns coordinates (N x 2) and
+    the index function."""
+    idx = lambda j1, j2, s: ((j1 - 1) * b + (j2 - 1)) * 2 + (s - 1)
+    coords = np.zeros((2 * a * b, 2))
+    for j1 in range(1, a + 1):
+        for j2 in range(1, b + 1):
+            for s in (1, 2):
+                coords[idx(j1, j2, s)] = HONEYCOMB_BASIS[:, s - 1] + HONEYCOMB_T @ np.array([j1, j2], dtype=float)
+    return coords, idx
+
+
+def honeycomb_hamiltonian(a: int, b: int, t1: float = 1.0, B: float = 0.0, onsite=None):
+    """Nearest-neighbour tight-binding on HoneycombLattice(a, b), open boundaries: site A of
+    cell (j1, j2) bonds to B of (j1, j2), (j1-1, j2) and (j1, j2-1) (distance 1/sqrt(3)), with
+    H[i,j] = t1 e^{-2 pi i LI(r_i -> r_j)} for LandauGauge(B), LI = (x1+x2)(y2-y1)B/2
+    (src/zoo/magneticfields.jl:11-15), H[j,i] its conjugate, and the on-site term."""
+    coords, idx = honeycomb_sites(a, b)
+    N = 2 * a * b
+    H = sp.lil_matrix((N, N), dtype=np.complex128)
+    for j1 in range(1, a + 1):
+        for j2 in range(1, b + 1):
+            i = idx(j1, j2, 1)
+            for (k1, k2) in ((j1, j2), (j1 - 1, j2), (j1, j2 - 1)):
+                if 1 <= k1 <= a and 1 <= k2 <= b:
+                    j = idx(k1, k2, 2)
+                    (x1, y1), (x2, y2) = coords[i], coords[j]
+                    li = (x1 + x2) * (y2 - y1) * B / 2
+                    v = t1 * np.exp(-2j * math.pi * li)
+                    H[i, j] += v
+                    H[j, i] += np.conj(v)
+    if onsite is not None:
+        H.setdiag(H.diagonal() + np.asarray(onsite))
+    return H.tocsc(), coords
+
+
+def qwz_hamiltonian(Lx: int, Ly: int, m=1.0):
+    """qwz(l, m) (src/zoo/models.jl:110-137) on SquareLattice(Lx, Ly), open boundaries, two
+    internal states per site (index 2 (site - 1) + spin): m sigma_z on site,
+    c+_{i+x} (sigma_z - i sigma_x)/2 c_i and c+_{i+y} (sigma_z - i sigma_y)/2 c_i plus h.c."""
+    N = Lx * Ly
+    mz = np.array([[1, 0], [0, -1]], dtype=np.complex128)
+    Mx = np.array([[1, -1j], [-1j, -1]], dtype=np.complex128) / 2
+    My = np.array([[1, -1], [1, -1]], dtype=np.complex128) / 2
+    mm = np.broadcast_to(np.asarray(m, dtype=float), (N,))
+    H = sp.lil_matrix((2 * N, 2 * N), dtype=np.complex128)
+    site = lambda x, y: (x - 1) * Ly + (y - 1)
+    for x in range(1, Lx + 1):
+        for y in range(1, Ly + 1):
+            s = site(x, y)
+            H[2 * s:2 * s + 2, 2 * s:2 * s + 2] = mm[s] * mz
+            for (dx, dy, Mb) in ((1, 0, Mx), (0, 1, My)):
+                if x + dx <= Lx and y + dy <= Ly:
+                    t = site(x + dx, y + dy)
+                    H[2 * t:2 * t + 2, 2 * s:2 * s + 2] = Mb
+                    H[2 * s:2 * s + 2, 2 * t:2 * t + 2] = Mb.conj().T
+    return H.tocsc()
+
+
+def csc_arrays(H):
+    """(colptr, rowval, nzval) of a scipy CSC matrix in the reference's 1-based layout."""
+    H = sp.csc_matrix(H)
+    H.sort_indices()
+    return (H.indptr.astype(np.int64) + 1, H.indices.astype(np.int64) + 1, np.asarray(H.data, dtype=np.complex128))
+
+
+def csc_currents(H, state, weights=None, is_density=None):
+    """2 Im(H[i,j] P[j,i]) for every stored entry (i, j) of H in CSC order (0 on the diagonal)."""
+    H = sp.csc_matrix(H)
+    H.sort_indices()
+    cols = np.repeat(np.arange(H.shape[1]), np.diff(H.indptr))
+    rows = H.indices
+    s = np.asarray(state)
+    if is_density:
+        pji = s[cols, rows]
+    else:
+        w = np.ones(s.shape[1]) if weights is None else np.asarray(weights)
+        pji = np.einsum("bm,bm,m->b", s[cols, :], np.conj(s[rows, :]), w)
+    J = 2.0 * np.imag(H.data * pji)
+    J[rows == cols] = 0.0
+    return J
