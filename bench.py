@@ -441,6 +441,76 @@ def run_densitymatrix_workload(args):
 
 
 # ------------------------------------------------------------------------------------------
+GENERAL_WORKLOAD = ("HoneycombLattice(180,180) open (N = 64800), t1=1, LandauGauge(0.01), Anderson U[-1,1], "
+                    "M=512 complex-Gaussian kets, dt=0.05, through the general sparse (ELL) path")
+
+
+def honeycomb_csc(a, b, B, V):
+    """Nearest-neighbour honeycomb H (open, Landau phases) as a scipy CSC matrix: the workload
+    generator of the general-path bench (sites ordered by (j1, j2, basis))."""
+    import scipy.sparse as sp
+    j1, j2 = np.meshgrid(np.arange(1, a + 1), np.arange(1, b + 1), indexing="ij")
+    j1, j2 = j1.ravel(), j2.ravel()
+    A = ((j1 - 1) * b + (j2 - 1)) * 2
+    xa = j1 + 0.5 * j2
+    ya = (math.sqrt(3) / 2) * j2
+    rows, cols = [], []
+    for dj1, dj2 in ((0, 0), (-1, 0), (0, -1)):
+        ok = (j1 + dj1 >= 1) & (j2 + dj2 >= 1)
+        rows.append(A[ok])
+        cols.append((((j1 + dj1 - 1) * b + (j2 + dj2 - 1)) * 2 + 1)[ok])
+    i = np.concatenate(rows)
+    j = np.concatenate(cols)
+    xi, yi = xa[i // 2], ya[i // 2]
+    xj = (j // 2 // b + 1) + 0.5 * (j // 2 % b + 1) + 0.5
+    yj = (math.sqrt(3) / 2) * (j // 2 % b + 1) + math.sqrt(3) / 6
+    v = np.exp(-2j * math.pi * (xi + xj) * (yj - yi) * B / 2)
+    N = 2 * a * b
+    H = sp.coo_matrix((np.concatenate([v, v.conj(), V]),
+                       (np.concatenate([i, j, np.arange(N)]), np.concatenate([j, i, np.arange(N)]))), shape=(N, N))
+    return H.tocsc()
+
+
+def run_general_workload(args):
+    """Ket steps through lm_ell_* (a honeycomb lattice given as a CSC matrix), c32."""
+    import torch
+    import lmgpu
+    ctx = lmgpu.default_context()
+    ext = torch.cuda.ExternalStream(ctx.stream_ptr(), device=torch.device("cuda", 0))
+    a = b = 180
+    N, M = 2 * a * b, 512
+    V = np.random.default_rng(SEED + 5).uniform(-1, 1, N)
+    H = lmgpu.SparseHamiltonian(lmgpu.Sites(N, name="honeycomb"), honeycomb_csc(a, b, B_FIELD, V))
+    st = lmgpu.KetBlock(H.lattice, make_kets(N, M, dtype=np.complex64), precision="c32")
+    solver = lmgpu.ChebyshevGPU()
+    solver.update_solver(H, DT)
+    for _ in range(args.warmup):
+        solver.step(st)
+    K = solver.order(st)[0]
+    ctx.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(ext)
+    for _ in range(args.steps):
+        solver.step(st)
+    e1.record(ext)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    alg = 5.0 * K * N * M * 8  # the per-order formula, per step
+    peak, peak_kind = measured_peak_hbm()
+    line = {"metric": "ket-steps/s (general sparse path)", "value": M / (ms / 1000.0), "unit": "ket-steps/s",
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "dtype": "c32", "data": "synthetic (seeded PCG64)",
+            "config": {"workload": GENERAL_WORKLOAD, "N": N, "M": M, "K": K, "nnz": int(len(H.rowval))},
+            "roofline": {"bound": "hbm", "achieved": alg / (ms / 1000.0) / 1e9, "peak": peak, "unit": "GB/s",
+                         "frac": alg / (ms / 1000.0) / 1e9 / peak, "traffic": None,
+                         "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
+                         "kernel": "cheb_order_ell_kernel (one launch per order)"}}
+    print(json.dumps(line))
+    return 0
+
+
+# ------------------------------------------------------------------------------------------
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -449,10 +519,11 @@ def main():
     ap.add_argument("--impl", default="lmgpu", choices=["lmgpu", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--kets", type=int, default=M_KETS)
-    ap.add_argument("--workload", default="kets", choices=["kets", "batch", "adjoint", "kpm", "densitymatrix"],
+    ap.add_argument("--workload", default="kets",
+                    choices=["kets", "batch", "adjoint", "kpm", "densitymatrix", "general"],
                     help="kets: the 256^2 ket-block workload (default); batch: 512 uneven dense-P lattices; "
                          "adjoint: loss_and_grad of the 64^2 differentiation workload; kpm: DOS moments; "
-                         "densitymatrix: P_0 at T > 0, Chebyshev vs eigensolver")
+                         "densitymatrix: P_0 at T > 0, Chebyshev vs eigensolver; general: honeycomb via ELL")
     ap.add_argument("--instances", type=int, default=512)
     ap.add_argument("--precision", default="c32", choices=["c32", "c64"])
     ap.add_argument("--adjoint-init", default="eigh", choices=["eigh", "random"],
@@ -473,6 +544,8 @@ def main():
         return run_kpm_workload(args)
     if args.workload == "densitymatrix":
         return run_densitymatrix_workload(args)
+    if args.workload == "general":
+        return run_general_workload(args)
 
     rank, world, local = dist_info()
     import torch
