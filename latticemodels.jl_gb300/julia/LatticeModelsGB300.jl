@@ -8,6 +8,7 @@ module LatticeModelsGB300
 
 using LatticeModels
 import LatticeModels: EvolutionSolver, update_solver!, step!, evolution_cache, localdensity
+using SparseArrays: SparseMatrixCSC
 
 const LIB = get(ENV, "LMGPU_LIB", joinpath(@__DIR__, "..", "lmgpu", "liblmgpu.so"))
 
@@ -189,6 +190,29 @@ function bond_currents(H::DeviceHamiltonian, st::DeviceState)
           st.lat.ctx.handle)
     return out
 end
+
+# ---- general sparse Hamiltonians: any construct_operator output (honeycomb, kagome, qwz, ...) ----
+# The reference's SparseMatrixCSC goes to the device as an ELL table; update_solver! picks the
+# ELL propagator, step! and the readouts are unchanged.
+mutable struct GPUSparseHamiltonian <: AbstractMatrix{ComplexF64}
+    ctx::Context
+    handle::Ptr{Cvoid}
+    n::Int
+end
+Base.size(H::GPUSparseHamiltonian) = (H.n, H.n)
+function GPUSparseHamiltonian(A::SparseMatrixCSC{ComplexF64,Int64}; ctx=default_context())
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:lm_ell_create_csc, LIB), Cint, (Ptr{Cvoid}, Int64, Ptr{Int64}, Ptr{Int64}, Ptr{ComplexF64}, Ref{Ptr{Cvoid}}),
+                ctx.handle, size(A, 1), A.colptr, A.rowval, A.nzval, h), ctx.handle)
+    H = GPUSparseHamiltonian(ctx, h[], size(A, 1))
+    finalizer(H -> ccall((:lm_ell_destroy, LIB), Cint, (Ptr{Cvoid},), H.handle), H)
+    return H
+end
+set_values!(H::GPUSparseHamiltonian, A::SparseMatrixCSC{ComplexF64,Int64}) =
+    check(ccall((:lm_ell_set_values, LIB), Cint, (Ptr{Cvoid}, Ptr{ComplexF64}), H.handle, A.nzval), H.ctx.handle)
+update_solver!(s::ChebyshevGPU, H::GPUSparseHamiltonian, dt, force=false) =
+    check(ccall((:lm_ell_solver_update, LIB), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Cdouble, Cint), s.handle, H.handle, dt, force),
+          s.ctx.handle)
 
 # ---- readout ring behind TimeSequence(f, ev(times)) (src/timesequence.jl:41-43) --------------
 # Readouts are computed into device ring slots and downloaded asynchronously; entries are taken
@@ -378,6 +402,6 @@ function ChainRulesCore.rrule(::typeof(density_loss), V, B, p::DensityLossProble
 end
 
 export ChebyshevGPU, DeviceLattice, DeviceState, gpu_tightbinding, bond_currents, ReadoutRing,
-       gpu_timesequence, GPUBatch, DensityLossProblem, density_loss
+       gpu_timesequence, GPUBatch, DensityLossProblem, density_loss, GPUSparseHamiltonian, set_values!
 
 end # module
