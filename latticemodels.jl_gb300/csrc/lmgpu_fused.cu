@@ -6,12 +6,12 @@
 // the result written once, instead of five vector passes per Chebyshev order.
 //
 // Tiling: a CTA of 512 threads owns a region of 32 (x) x 64 (y) sites; thread (tx, ty) holds
-// the S = 4 consecutive y-sites S ty .. S ty + S-1 of row tx in registers (T_{k-1}, the
-// accumulator and the stencil coefficients).  Per order, rows are exchanged through a
+// the S = 4 consecutive y-sites S ty .. S ty + S-1 of row tx in registers (T_{k-1}, T_{k-2},
+// the accumulator and the stencil coefficients).  Per order, rows are exchanged through a
 // double-buffered shared-memory copy of T_{k-1} (x neighbours) and warp shuffles (y
-// neighbours: a warp holds whole rows); T_{k-2} of a thread's own sites is read back from the
-// buffer T_k overwrites.  Built with LM_FUSED_SITES=2 the CTA has 1024 threads of 2 sites.  The valid part of the region shrinks by one site per order, so after K orders
-// the inner (32-2K) x (64-2K) sites are exact and are written out.  Periodic axes wrap the
+// neighbours: a warp holds whole rows).  Built with LM_FUSED_SITES=2 the CTA has 1024
+// threads of 2 sites.  The valid part of the region shrinks by one site per order, so after
+// K orders the inner (32-2K) x (64-2K) sites are exact and are written out.  Periodic axes wrap the
 // halo.  Along an open axis the first and last regions of a lattice sit on the lattice edge:
 // the stencil has no bond across it, so nothing shrinks there and those regions write out up
 // to the edge (a lattice no longer than a region is one tile along that axis, with no halo).
@@ -302,9 +302,9 @@ cheb_fused_c32_kernel(FusedInst single, const FusedInst* __restrict__ table, int
             }
             const int stage = sbuf(sb);
 
-            // T_{k-1} of my positions lives in registers; T_{k-2} is read back from the buffer
-            // that T_k overwrites (my own positions only), T_0 from the staging buffer.
-            float2 t1[KB][S], yv[KB][S];
+            // T_{k-1} and T_{k-2} of my positions live in registers (t1, t2); the shared buffers
+            // carry T_{k-1} to the x-neighbours, T_0 comes from the staging buffer.
+            float2 t1[KB][S], t2[KB][S], yv[KB][S];
 #pragma unroll
             for (int kk = 0; kk < KB; ++kk) {
                 load_sites(smem + stage, kk, tx, ty, t1[kk]);
@@ -316,7 +316,6 @@ cheb_fused_c32_kernel(FusedInst single, const FusedInst* __restrict__ table, int
             for (int k = 1; k <= K; ++k) {
                 const int src = (k == 1) ? stage : tb((k - 1) & 1);
                 const int dst = tb(k & 1);
-                const int prev2 = (k == 2) ? stage : dst;  // T_{k-2} of my positions
                 // warps whose two rows both lie outside the valid region skip the order (the
                 // valid rows shrink by one per order, except at an open lattice edge)
                 const bool active =
@@ -334,15 +333,13 @@ cheb_fused_c32_kernel(FusedInst single, const FusedInst* __restrict__ table, int
                         up.y = __shfl_up_sync(0xffffffffu, t1[kk][S - 1].y, 1);
                         dn.x = __shfl_down_sync(0xffffffffu, t1[kk][0].x, 1);
                         dn.y = __shfl_down_sync(0xffffffffu, t1[kk][0].y, 1);
-                        float2 t0[S];
-                        if (k >= 2) load_sites(smem + prev2, kk, tx, ty, t0);
                         float2 tk[S];
 #pragma unroll
                         for (int j = 0; j < S; ++j) {
                             const float2 vyp = (j < S - 1) ? t1[kk][j + 1] : dn;
                             const float2 vym = (j > 0) ? t1[kk][j - 1] : up;
                             const float2 hym = (j > 0) ? make_float2(hy[j - 1].x, -hy[j - 1].y) : hym0;
-                            float2 acc = (k == 1) ? make_float2(0.f, 0.f) : make_float2(-t0[j].x, -t0[j].y);
+                            float2 acc = (k == 1) ? make_float2(0.f, 0.f) : make_float2(-t2[kk][j].x, -t2[kk][j].y);
                             if (XR) {
                                 acc.x = fmaf(hx[j].x, vxp[j].x, acc.x);
                                 acc.y = fmaf(hx[j].x, vxp[j].y, acc.y);
@@ -381,6 +378,7 @@ cheb_fused_c32_kernel(FusedInst single, const FusedInst* __restrict__ table, int
                                 yv[kk][j].x = fmaf(sk, tk[j].x, yv[kk][j].x);
                                 yv[kk][j].y = fmaf(sk, tk[j].y, yv[kk][j].y);
                             }
+                            t2[kk][j] = t1[kk][j];
                             t1[kk][j] = tk[j];
                         }
                         if (k < K) {
