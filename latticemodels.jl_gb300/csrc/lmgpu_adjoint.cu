@@ -13,8 +13,8 @@
 // For an on-site potential V_i, < beta, D~ T > = conj(beta_i) T_i / a summed over kets; for a
 // field amplitude A, dH[s, s+e]/dA = -2 pi i LI_e(A = 1) H[s, s+e] on every bond.
 //
-// lm_adjoint_step recomputes T_0 .. T_{K-1} from psi_n, runs the beta recurrence and
-// accumulates both gradients (FP64 results; c32 sums in double-float); the caller applies U^dagger to lambda with a solver
+// lm_adjoint_step recomputes T_0 .. T_{K-1} from psi_n, then runs the beta recurrence and the
+// gradient sums in one fused pass per order (FP64 results; c32 sums in double-float); the caller applies U^dagger to lambda with a solver
 // updated for -dt (the same polynomial with conjugate coefficients).
 #include <cuda_runtime.h>
 #include <math.h>
@@ -110,58 +110,80 @@ cudaError_t launch_stencil_recur(lm_ctx* ctx, const Geom& g, int precision, cons
     return cudaGetLastError();
 }
 
-// Gradient terms of order k, per site s, with sums over all kets m:
-//   gV[s] += f Re( ph * sum_m conj(beta_sm) T_sm )
-//   gA    += f Re( ph * sum_s sum_e [ D[s,j] S1 + conj(D[s,j]) S2 ] ),  j = s + e,
-//            S1 = sum_m conj(beta_sm) T_jm,  S2 = sum_m conj(beta_jm) T_sm
-// with ph = e^{-ib dt}, f = 1/a (k = 1) or 2/a (k >= 2), D = dH/dA of the bond table dhop (the
-// bond s -> s+e and its Hermitian partner, each bond owned by its source).  A block owns 32
-// sites and one chunk of the kets (blockIdx.y); its 8 warps split the chunk and their partial
-// sums are added in warp order.  gV_part[chunk][s] and gA_part[chunk][block] each have one
-// writer per launch; lm_adjoint_gradients adds them in chunk and block order, so the gradients
-// are bit-reproducible.  c32 data is summed in double-float FP32 (Acc<float>), c64 in FP64.
+// One order k of the adjoint, fused: the beta recurrence and the gradient sums in one pass.
+//   beta_k = conj(c_k) lambda + (2H~) beta_{k+1} - beta_{k+2}         (written to bk)
+//   gV[s] += f Re( ph * sum_m conj(beta_k,sm) T_sm )
+//   gA    += f Re( ph * sum_s [ D[s,s+x] S1x + D[s,s+y] S1y + conj(D[s-x,s]) S2x + conj(D[s-y,s]) S2y ] )
+//            S1e = sum_m conj(beta_k,sm) T_{s+e,m},  S2e = sum_m conj(beta_k,sm) T_{s-e,m}
+// with T = T_{k-1}, ph = e^{-ib dt}, f = 1/a (k = 1) or 2/a (k >= 2), D = dH/dA per bond (owned
+// by its source site).  Every bond enters twice -- conj(b_s) D T_j at its source s and
+// conj(b_j) conj(D) T_s at its destination j -- so a thread needs only its own beta_k and
+// read-only neighbours of T.  A block owns 32 sites and one chunk of the kets (blockIdx.y);
+// its 8 warps split the chunk and their partial sums are added in warp order.  gV_part and
+// gA_part have one writer per entry per launch and lm_adjoint_gradients adds them in chunk
+// and block order, so the gradients are bit-reproducible.  c32 sums are double-float.
 template <typename R>
-__global__ void __launch_bounds__(256) adj_grad_kernel(Geom g, const double2* __restrict__ dhop,
-                                                       const typename CT<R>::V* __restrict__ beta,
-                                                       const typename CT<R>::V* __restrict__ T, int64_t ld, int64_t M,
-                                                       int64_t mchunk, double ph_re, double ph_im, double f,
-                                                       double* __restrict__ gV_part, double* __restrict__ gA_part) {
+__global__ void __launch_bounds__(256, sizeof(R) == sizeof(float) ? 3 : 2) adj_beta_grad_kernel(
+    Geom g, const typename CT<R>::V* __restrict__ hop2, const R* __restrict__ diag2,
+    const typename CT<R>::V* __restrict__ b1, const typename CT<R>::V* __restrict__ b2,
+    const typename CT<R>::V* __restrict__ lam, typename CT<R>::V* __restrict__ bk, R w_re, R w_im,
+    const double2* __restrict__ dhop, const typename CT<R>::V* __restrict__ T, int64_t ld, int64_t M, int64_t mchunk,
+    double ph_re, double ph_im, double f, double* __restrict__ gV_part, double* __restrict__ gA_part) {
     typedef typename CT<R>::V V;
     __shared__ double red[8][10][32];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int64_t s = (int64_t)blockIdx.x * 32 + lane;
     const int64_t m0 = (int64_t)blockIdx.y * mchunk, m1 = min(M, m0 + mchunk);
-    Acc<R> a[10];  // conj(b_s) T_s (re, im); +x: S1 (re, im), S2 (re, im); +y: the same
+    Acc<R> a[10];  // conj(b)T_s (re, im); S1x; S1y; S2x; S2y
     Nbr nb;
     if (s < g.N) {
         nb = neighbours(g, s);
-        // absent bonds read the site itself (always in bounds); their D is never applied
-        const int64_t jx = nb.hxp ? nb.xp : s, jy = nb.hyp ? nb.yp : s;
+        const V z = CT<R>::make(0, 0);
+        const V hxp = nb.hxp ? hop2[s] : z, hyp = nb.hyp ? hop2[g.N + s] : z;
+        V t = nb.hxm ? hop2[nb.xm] : z;
+        const V hxm = CT<R>::make(t.x, -t.y);
+        t = nb.hym ? hop2[g.N + nb.ym] : z;
+        const V hym = CT<R>::make(t.x, -t.y);
+        const R d = diag2[s];
         for (int64_t m = m0 + warp; m < m1; m += 8) {
             const int64_t o = m * ld;
-            const V b = beta[o + s], t = T[o + s];
-            a[0].add_prod(b.x, t.x);
-            a[0].add_prod(b.y, t.y);
-            a[1].add_prod(b.x, t.y);
-            a[1].add_prod(-b.y, t.x);
+            V acc = z;
+            if (b1) {
+                const V v0 = b1[o + s], vxp = b1[o + nb.xp], vxm = b1[o + nb.xm], vyp = b1[o + nb.yp], vym = b1[o + nb.ym];
+                acc.x = fma(hxp.x, vxp.x, acc.x); acc.x = fma(-hxp.y, vxp.y, acc.x);
+                acc.y = fma(hxp.x, vxp.y, acc.y); acc.y = fma(hxp.y, vxp.x, acc.y);
+                acc.x = fma(hxm.x, vxm.x, acc.x); acc.x = fma(-hxm.y, vxm.y, acc.x);
+                acc.y = fma(hxm.x, vxm.y, acc.y); acc.y = fma(hxm.y, vxm.x, acc.y);
+                acc.x = fma(hyp.x, vyp.x, acc.x); acc.x = fma(-hyp.y, vyp.y, acc.x);
+                acc.y = fma(hyp.x, vyp.y, acc.y); acc.y = fma(hyp.y, vyp.x, acc.y);
+                acc.x = fma(hym.x, vym.x, acc.x); acc.x = fma(-hym.y, vym.y, acc.x);
+                acc.y = fma(hym.x, vym.y, acc.y); acc.y = fma(hym.y, vym.x, acc.y);
+                acc.x = fma(d, v0.x, acc.x);
+                acc.y = fma(d, v0.y, acc.y);
+            }
+            if (b2) {
+                const V q = b2[o + s];
+                acc.x -= q.x;
+                acc.y -= q.y;
+            }
+            const V l = lam[o + s];
+            acc.x = fma(w_re, l.x, fma(-w_im, l.y, acc.x));
+            acc.y = fma(w_re, l.y, fma(w_im, l.x, acc.y));
+            bk[o + s] = acc;
+            const V b = acc, ts = T[o + s];
+            a[0].add_prod(b.x, ts.x);
+            a[0].add_prod(b.y, ts.y);
+            a[1].add_prod(b.x, ts.y);
+            a[1].add_prod(-b.y, ts.x);
             if (dhop) {
-                const V tx = T[o + jx], bx = beta[o + jx], ty = T[o + jy], by = beta[o + jy];
-                a[2].add_prod(b.x, tx.x);   // S1 = conj(b_s) T_j
-                a[2].add_prod(b.y, tx.y);
-                a[3].add_prod(b.x, tx.y);
-                a[3].add_prod(-b.y, tx.x);
-                a[4].add_prod(bx.x, t.x);   // S2 = conj(b_j) T_s
-                a[4].add_prod(bx.y, t.y);
-                a[5].add_prod(bx.x, t.y);
-                a[5].add_prod(-bx.y, t.x);
-                a[6].add_prod(b.x, ty.x);
-                a[6].add_prod(b.y, ty.y);
-                a[7].add_prod(b.x, ty.y);
-                a[7].add_prod(-b.y, ty.x);
-                a[8].add_prod(by.x, t.x);
-                a[8].add_prod(by.y, t.y);
-                a[9].add_prod(by.x, t.y);
-                a[9].add_prod(-by.y, t.x);
+                const V tn[4] = {T[o + nb.xp], T[o + nb.yp], T[o + nb.xm], T[o + nb.ym]};
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {  // conj(b) T_n
+                    a[2 + 2 * q].add_prod(b.x, tn[q].x);
+                    a[2 + 2 * q].add_prod(b.y, tn[q].y);
+                    a[3 + 2 * q].add_prod(b.x, tn[q].y);
+                    a[3 + 2 * q].add_prod(-b.y, tn[q].x);
+                }
             }
         }
     }
@@ -180,15 +202,22 @@ __global__ void __launch_bounds__(256) adj_grad_kernel(Geom g, const double2* __
     if (s < g.N) {
         gV_part[(int64_t)blockIdx.y * g.N + s] += f * (ph_re * v[0] - ph_im * v[1]);
         if (dhop) {
+            const double2 zz = make_double2(0.0, 0.0);
+            const double2 D[4] = {nb.hxp ? dhop[s] : zz, nb.hyp ? dhop[g.N + s] : zz, nb.hxm ? dhop[nb.xm] : zz,
+                                  nb.hym ? dhop[g.N + nb.ym] : zz};
+            double zr = 0.0, zi = 0.0;
 #pragma unroll
-            for (int dir = 0; dir < 2; ++dir) {
-                if (!(dir == 0 ? nb.hxp : nb.hyp)) continue;
-                const double2 D = dhop[dir * g.N + s];
-                const double* S = v + 2 + 4 * dir;  // S1 re, im, S2 re, im
-                const double are = (D.x * S[0] - D.y * S[1]) + (D.x * S[2] + D.y * S[3]);
-                const double aim = (D.x * S[1] + D.y * S[0]) + (D.x * S[3] - D.y * S[2]);
-                ga += f * (ph_re * are - ph_im * aim);
+            for (int q = 0; q < 4; ++q) {
+                const double sr = v[2 + 2 * q], si = v[3 + 2 * q];
+                if (q < 2) {  // D S
+                    zr += D[q].x * sr - D[q].y * si;
+                    zi += D[q].x * si + D[q].y * sr;
+                } else {      // conj(D) S
+                    zr += D[q].x * sr + D[q].y * si;
+                    zi += D[q].x * si - D[q].y * sr;
+                }
             }
+            ga = f * (ph_re * zr - ph_im * zi);
         }
     }
     if (gA_part) {
@@ -467,16 +496,19 @@ int lm_adjoint_step(lm_adjoint* a, lm_solver* s, lm_ham* h, int component, int s
         void* bk = a->B[k % 3];
         const void* b1 = k + 1 <= K ? a->B[(k + 1) % 3] : nullptr;
         const void* b2 = k + 2 <= K ? a->B[(k + 2) % 3] : nullptr;
-        CUDA_TRY(ctx, recur(b1, b2, lam->d_data, bk, 1.0, wre, wim), "adjoint beta recurrence");
         const double f = (k == 1 ? 1.0 : 2.0) / s->a;
         if (f64)
-            adj_grad_kernel<double><<<ggrid, 256, 0, ctx->stream>>>(g, dhop, (const double2*)bk, (const double2*)a->T[(size_t)k - 1],
-                                                                    ld, M, a->mchunk, s->phase_re, s->phase_im, f, a->d_gV, gA);
+            adj_beta_grad_kernel<double><<<ggrid, 256, 0, ctx->stream>>>(
+                g, (const double2*)hop2, (const double*)diag2, (const double2*)b1, (const double2*)b2,
+                (const double2*)lam->d_data, (double2*)bk, wre, wim, dhop, (const double2*)a->T[(size_t)k - 1], ld, M,
+                a->mchunk, s->phase_re, s->phase_im, f, a->d_gV, gA);
         else
-            adj_grad_kernel<float><<<ggrid, 256, 0, ctx->stream>>>(g, dhop, (const float2*)bk, (const float2*)a->T[(size_t)k - 1],
-                                                                   ld, M, a->mchunk, s->phase_re, s->phase_im, f, a->d_gV, gA);
+            adj_beta_grad_kernel<float><<<ggrid, 256, 0, ctx->stream>>>(
+                g, (const float2*)hop2, (const float*)diag2, (const float2*)b1, (const float2*)b2,
+                (const float2*)lam->d_data, (float2*)bk, (float)wre, (float)wim, dhop,
+                (const float2*)a->T[(size_t)k - 1], ld, M, a->mchunk, s->phase_re, s->phase_im, f, a->d_gV, gA);
         ctx->launches++;
-        CUDA_TRY(ctx, cudaGetLastError(), "adjoint gradient kernel");
+        CUDA_TRY(ctx, cudaGetLastError(), "adjoint beta/gradient kernel");
     }
     return LM_OK;
 }

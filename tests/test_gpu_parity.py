@@ -362,3 +362,30 @@ def test_fused_real_x_hops_bit_identical(lm):
             s.step(st)
         outs.append(st.to_numpy())
     assert np.array_equal(outs[0], outs[1])
+
+
+@pytest.mark.parametrize("tw", [(0.7, 0.0), (0.0, 1.3), (0.4, -0.9)])
+def test_fused_twisted_boundaries(lm, tw):
+    """Twisted periodic axes (complex seam hops, so the general x-hop kernel) through the fused
+    c32 step, against the per-order path and the exact exponent; Landau field included."""
+    ol, ll = pair(lm, 48, 70, (True, True), tw)
+    V = o.anderson_disorder(ol.N, 1.0, 19)
+    Ho = o.tightbinding_hamiltonian(ol, field=o.LandauGauge(0.02), onsite=V)
+    Hl = lm.tightbinding_hamiltonian(ll, V, field=lm.LandauGauge(0.02))
+    X = o.random_kets(ol.N, 6, 23)
+    ctx = lm.default_context()
+    outs = {}
+    try:
+        for fused in (True, False):
+            ctx.set_fused(fused)
+            st = lm.KetBlock(ll, X, precision="c32")
+            s = lm.ChebyshevGPU()
+            s.update_solver(Hl, 0.07)
+            for _ in range(2):
+                s.step(st)
+            outs[fused] = st.to_numpy().astype(np.complex128)
+    finally:
+        ctx.set_fused(True)
+    Y = o.expm_multiply(Ho, 0.07, o.expm_multiply(Ho, 0.07, X))
+    assert rel(outs[True], Y) <= 2e-6
+    assert rel(outs[True], outs[False]) <= 2e-6
