@@ -193,6 +193,11 @@ int lm_batch_update(lm_batch *b, double dt);
 int lm_batch_step(lm_batch *b);
 /* 1 (default): capture the step into a CUDA graph once per buffer parity and replay it. */
 int lm_batch_set_graph(lm_batch *b, int enable);
+/* Column panels of `width` columns (0: off): the per-order recurrence runs in place on each
+ * panel with per-lattice panel scratch (2 x n x width), and a density matrix takes in-place
+ * conjugate transposes, so the batch needs no full-size recurrence buffers (~3x less memory;
+ * ComplexF64 batches that would not fit otherwise).  Takes effect at the next update. */
+int lm_batch_set_panel(lm_batch *b, int64_t width);
 /* Pass shape: -1 auto, 0 one temporally blocked launch per pass, 1/2/3 one launch per
  * order with 2/4/8 kets per thread. */
 int lm_batch_set_config(lm_batch *b, int cfg);

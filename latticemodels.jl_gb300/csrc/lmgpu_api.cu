@@ -86,6 +86,12 @@ int ensure_accumulator(lm_state* s) {
     if (s->d_y) return LM_OK;
     return dalloc(s->ctx, &s->d_y, s->elem * (size_t)s->ld * (size_t)s->m, "accumulator scratch");
 }
+// Allocates the recurrence scratch (T_{k-1}/T_k ping-pong) of a state on first use; a state
+// stepped only through a panelled batch never needs it.
+int ensure_scratch(lm_state* s) {
+    if (s->d_a) return LM_OK;
+    return dalloc(s->ctx, &s->d_a, s->elem * (size_t)s->ld * (size_t)s->m, "recurrence scratch");
+}
 }  // namespace lmgpu
 
 static int ensure_red(lm_ctx* ctx, size_t n) {
@@ -604,11 +610,8 @@ int lm_state_create(lm_ctx* ctx, int64_t n, int64_t m, int kind, int precision, 
     cudaSetDevice(ctx->device);
     const size_t bytes = s->elem * (size_t)n * (size_t)m;
     int rc = dalloc(ctx, &s->d_data, bytes, "state");
-    if (rc == LM_OK) rc = dalloc(ctx, &s->d_a, bytes, "recurrence scratch");
-    // the accumulator is only needed by the per-order path; it is allocated on first use
+    // the recurrence scratch and the accumulator are allocated on first use
     if (rc != LM_OK) {
-        if (s->d_data) cudaFree(s->d_data);
-        if (s->d_a) cudaFree(s->d_a);
         delete s;
         return rc;
     }
@@ -903,6 +906,10 @@ int lm_solver_step(lm_solver* s, lm_state* st) {
     const Geom& g = s->ham->lat->g;
     CHECK_ARG(ctx, st->n == g.N, "lm_solver_step: state size does not match the lattice");
     cudaSetDevice(ctx->device);
+    {
+        int rc0 = ensure_scratch(st);
+        if (rc0 != LM_OK) return rc0;
+    }
     if (!(ctx->fused && st->kind == LM_KETS && fused_supported(st->precision, s->K) && fused_supported_geom(g))) {
         int rc0 = ensure_accumulator(st);
         if (rc0 != LM_OK) return rc0;

@@ -52,6 +52,23 @@ struct TransInst {
     int64_t tiles;  // tiles per dimension (32 x 32)
 };
 
+// Panelled batches: dst = src over n x m columns (an odd-K result moved back into place).
+struct CopyInst {
+    const void* src;
+    void* dst;
+    int64_t n, m, ld;
+    int64_t item_begin;
+    int64_t lane_blocks;  // ceil(n / 256)
+};
+
+// Panelled batches: P <- P^dagger in place, over the 32 x 32 tile pairs (ti <= tj).
+struct IPTransInst {
+    void* data;
+    int64_t n, ld;
+    int64_t item_begin;
+    int64_t tiles;  // tiles per dimension
+};
+
 template <typename T>
 __device__ __forceinline__ int find_item_owner(const T* __restrict__ table, int ninst, int64_t item) {
     int lo = 0, hi = ninst - 1;
@@ -126,6 +143,65 @@ __global__ void __launch_bounds__(256) transpose_conj_batch_kernel(const TransIn
     }
 }
 
+template <typename R>
+__global__ void __launch_bounds__(256) copy_batch_kernel(const CopyInst* __restrict__ table, int ninst,
+                                                         int64_t nitems) {
+    typedef typename CT<R>::V V;
+    for (int64_t item = blockIdx.x; item < nitems; item += gridDim.x) {
+        const CopyInst& D = table[find_item_owner(table, ninst, item)];
+        const int64_t local = item - D.item_begin;
+        const int64_t col = local / D.lane_blocks, row = (local % D.lane_blocks) * 256 + threadIdx.x;
+        if (row < D.n) ((V*)D.dst)[col * D.ld + row] = ((const V*)D.src)[col * D.ld + row];
+    }
+}
+
+// In place P <- P^dagger for every instance: an item swaps the tiles (ti, tj) and (tj, ti)
+// (ti <= tj) through shared memory, conjugating both; a diagonal tile is transposed in place.
+template <typename R>
+__global__ void __launch_bounds__(256) transpose_conj_inplace_batch_kernel(const IPTransInst* __restrict__ table,
+                                                                           int ninst, int64_t nitems) {
+    typedef typename CT<R>::V V;
+    __shared__ V ta[32][33], tb[32][33];
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 x 8
+    for (int64_t item = blockIdx.x; item < nitems; item += gridDim.x) {
+        const IPTransInst& D = table[find_item_owner(table, ninst, item)];
+        int64_t local = item - D.item_begin;
+        int64_t ti = 0;
+        while (local >= D.tiles - ti) {  // row ti holds the pairs (ti, ti .. tiles-1)
+            local -= D.tiles - ti;
+            ++ti;
+        }
+        const int64_t tj = ti + local;
+        V* P = (V*)D.data;
+        const int64_t n = D.n, ld = D.ld;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int64_t c = ty + 8 * j;
+            const int64_t ra = ti * 32 + tx, ca = tj * 32 + c;  // tile (ti, tj)
+            if (ra < n && ca < n) ta[c][tx] = P[ra + ca * ld];
+            const int64_t rb = tj * 32 + tx, cb = ti * 32 + c;  // tile (tj, ti)
+            if (ti != tj && rb < n && cb < n) tb[c][tx] = P[rb + cb * ld];
+        }
+        __syncthreads();
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int64_t c = ty + 8 * j;
+            // (P^dagger)[tj*32 + tx, ti*32 + c] = conj(P[ti*32 + c, tj*32 + tx]) = conj(ta[tx][c])
+            const int64_t r1 = tj * 32 + tx, c1 = ti * 32 + c;
+            if (r1 < n && c1 < n) {
+                const V v = ta[tx][c];
+                P[r1 + c1 * ld] = CT<R>::make(v.x, -v.y);
+            }
+            const int64_t r2 = ti * 32 + tx, c2 = tj * 32 + c;
+            if (ti != tj && r2 < n && c2 < n) {
+                const V v = tb[tx][c];
+                P[r2 + c2 * ld] = CT<R>::make(v.x, -v.y);
+            }
+        }
+        __syncthreads();
+    }
+}
+
 }  // namespace lmgpu
 
 using namespace lmgpu;
@@ -157,6 +233,17 @@ struct lm_batch {
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
     int parity = 0;                         // 1: every state's data currently in its A buffer
     std::vector<void*> base_S, base_A;      // pointers at update time (parity 0)
+    // panelled per-order path (lm_batch_set_panel): the recurrence runs on column panels of
+    // width panel_w with per-instance panel scratch, in place on the states' data
+    int64_t panel_w = 0;
+    std::vector<void*> pa, py;              // per-instance panel scratch (A, Y)
+    std::vector<size_t> pbytes;             // their sizes
+    std::vector<OrderInst*> dpo;            // per panel: order table (device)
+    std::vector<CopyInst*> dpc;             // per panel: copy-back table (device, odd K)
+    std::vector<int> pn;                    // per panel: instances in the table
+    std::vector<int64_t> po_items, pc_items;
+    IPTransInst* dip = nullptr;
+    int64_t ip_items = 0;
 };
 
 static void free_graphs(lm_batch* b) {
@@ -178,6 +265,24 @@ static void free_tables(lm_batch* b) {
         b->dt_[p] = nullptr;
     }
     for (int p = 0; p < 2; ++p) b->cap_f[p] = b->cap_o1[p] = b->cap_o2[p] = b->cap_t[p] = 0;
+}
+
+static void free_panel(lm_batch* b) {
+    for (void* q : b->pa) cudaFree(q);
+    for (void* q : b->py) cudaFree(q);
+    for (auto* t : b->dpo) cudaFree(t);
+    for (auto* t : b->dpc) cudaFree(t);
+    if (b->dip) cudaFree(b->dip);
+    b->pa.clear();
+    b->py.clear();
+    b->pbytes.clear();
+    b->dpo.clear();
+    b->dpc.clear();
+    b->pn.clear();
+    b->po_items.clear();
+    b->pc_items.clear();
+    b->dip = nullptr;
+    b->ip_items = 0;
 }
 
 static int inner_of(int cfg) { return cfg == 1 ? 2 : (cfg == 3 ? 8 : 4); }
@@ -302,6 +407,134 @@ static int build_tables(lm_batch* b) {
     return LM_OK;
 }
 
+template <typename T>
+static int upload_new(lm_ctx* ctx, T** dptr, const std::vector<T>& host) {
+    *dptr = nullptr;
+    cudaError_t e = cudaMalloc((void**)dptr, std::max<size_t>(host.size(), 1) * sizeof(T));
+    if (e == cudaSuccess && !host.empty())
+        e = cudaMemcpy(*dptr, host.data(), host.size() * sizeof(T), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return set_err(ctx, LM_ERR_OOM, "lm_batch: panel table allocation failed");
+    }
+    return LM_OK;
+}
+
+// Panelled per-order path: per-instance panel scratch (A, Y: n x min(w, m) each) and, per
+// column panel q, an order table over the instances that still have columns there (S = the
+// panel's columns of the state, in place), the copy-back table for odd K and the in-place
+// transpose table.
+static int build_panel_tables(lm_batch* b) {
+    lm_ctx* ctx = b->ctx;
+    const size_t n = b->states.size();
+    const int K = b->K;
+    const int inner = inner_of(b->cfg);
+    const int64_t w = b->panel_w;
+    std::vector<std::vector<ChebCoef>> coefs(n);
+    std::vector<double> J;
+    for (size_t i = 0; i < n; ++i) {
+        bessel_j_all(b->solvers[i]->a * fabs(b->dt), K, J);
+        make_coefs(J, K, b->dt >= 0 ? 1.0 : -1.0, coefs[i]);
+    }
+    // scratch: reuse when the sizes are unchanged
+    std::vector<size_t> need(n);
+    int64_t npanels = 0;
+    for (size_t i = 0; i < n; ++i) {
+        const lm_state* st = b->states[i];
+        need[i] = st->elem * (size_t)st->ld * (size_t)std::min<int64_t>(w, st->m);
+        npanels = std::max<int64_t>(npanels, (st->m + w - 1) / w);
+    }
+    if (b->pbytes != need) {
+        free_panel(b);
+        b->pa.assign(n, nullptr);
+        b->py.assign(n, nullptr);
+        for (size_t i = 0; i < n; ++i) {
+            cudaError_t e = cudaMalloc(&b->pa[i], need[i]);
+            if (e == cudaSuccess) e = cudaMalloc(&b->py[i], need[i]);
+            if (e != cudaSuccess) {
+                cudaGetLastError();
+                free_panel(b);
+                return set_err(ctx, LM_ERR_OOM, "lm_batch: panel scratch allocation failed");
+            }
+        }
+        b->pbytes = need;
+    } else {
+        for (auto* t : b->dpo) cudaFree(t);
+        for (auto* t : b->dpc) cudaFree(t);
+        if (b->dip) cudaFree(b->dip);
+        b->dpo.clear();
+        b->dpc.clear();
+        b->dip = nullptr;
+    }
+    b->pn.clear();
+    b->po_items.clear();
+    b->pc_items.clear();
+    const bool f32 = b->precision == LM_C32;
+    for (int64_t q = 0; q < npanels; ++q) {
+        std::vector<OrderInst> ot;
+        std::vector<CopyInst> ct;
+        int64_t oi = 0, ci = 0;
+        for (size_t i = 0; i < n; ++i) {
+            lm_state* st = b->states[i];
+            if (st->m <= q * w) continue;
+            const int64_t cols = std::min<int64_t>(w, st->m - q * w);
+            lm_solver* sv = b->solvers[i];
+            const Geom& g = b->hams[i]->lat->g;
+            void* S = (unsigned char*)st->d_data + st->elem * (size_t)st->ld * (size_t)(q * w);
+            OrderInst o{};
+            o.g = g;
+            o.hop2 = f32 ? (const void*)sv->d_hop2f : (const void*)sv->d_hop2;
+            o.diag2 = f32 ? (const void*)sv->d_diag2f : (const void*)sv->d_diag2;
+            o.S = S;
+            o.A = b->pa[i];
+            o.Y = b->py[i];
+            o.ld = st->ld;
+            o.M = cols;
+            o.lane_blocks = (g.N + 255) / 256;
+            for (int k = 0; k <= kBatchMaxK; ++k) o.s[k] = k <= K ? coefs[i][(size_t)k].s : 0.0;
+            o.ph_re = sv->phase_re;
+            o.ph_im = sv->phase_im;
+            o.lo = cheb_lo(o.ph_re, o.ph_im, o.s[0], o.s[1], false);
+            o.item_begin = oi;
+            oi += o.lane_blocks * ((cols + inner - 1) / inner);
+            ot.push_back(o);
+            CopyInst c{};
+            c.src = b->pa[i];
+            c.dst = S;
+            c.n = st->n;
+            c.m = cols;
+            c.ld = st->ld;
+            c.lane_blocks = (st->n + 255) / 256;
+            c.item_begin = ci;
+            ci += c.lane_blocks * cols;
+            ct.push_back(c);
+        }
+        OrderInst* d1 = nullptr;
+        CopyInst* d2 = nullptr;
+        int rc = upload_new(ctx, &d1, ot);
+        if (rc == LM_OK) rc = upload_new(ctx, &d2, ct);
+        b->dpo.push_back(d1);
+        b->dpc.push_back(d2);
+        if (rc != LM_OK) return rc;
+        b->pn.push_back((int)ot.size());
+        b->po_items.push_back(oi);
+        b->pc_items.push_back(ci);
+    }
+    std::vector<IPTransInst> it(n);
+    int64_t ti = 0;
+    for (size_t i = 0; i < n; ++i) {
+        const lm_state* st = b->states[i];
+        it[i].data = st->d_data;
+        it[i].n = st->n;
+        it[i].ld = st->ld;
+        it[i].tiles = (st->n + 31) / 32;
+        it[i].item_begin = ti;
+        ti += it[i].tiles * (it[i].tiles + 1) / 2;
+    }
+    b->ip_items = b->kind == LM_DENSITY ? ti : 0;
+    return upload_new(ctx, &b->dip, it);
+}
+
 static int grid_for(lm_ctx* ctx, int64_t items, int per_sm) {
     int64_t g = (int64_t)(ctx->sm_count > 0 ? ctx->sm_count : 152) * per_sm;
     if (g > items) g = items;
@@ -309,20 +542,20 @@ static int grid_for(lm_ctx* ctx, int64_t items, int per_sm) {
     return (int)g;
 }
 
-static cudaError_t launch_order_pass(lm_batch* b, const OrderInst* table) {
+static cudaError_t launch_order_pass(lm_batch* b, const OrderInst* table, int n, int64_t items) {
     lm_ctx* ctx = b->ctx;
-    const int n = (int)b->states.size();
-    const int grid = grid_for(ctx, b->o_items, 8);
+    if (items <= 0) return cudaSuccess;
+    const int grid = grid_for(ctx, items, 8);
     const int inner = inner_of(b->cfg);
     for (int k = 1; k <= b->K; ++k) {
         if (b->precision == LM_C64) {
-            if (inner == 2) cheb_order_batch_kernel<double, 2><<<grid, 256, 0, ctx->stream>>>(table, n, b->o_items, k, b->K);
-            else if (inner == 8) cheb_order_batch_kernel<double, 8><<<grid, 256, 0, ctx->stream>>>(table, n, b->o_items, k, b->K);
-            else cheb_order_batch_kernel<double, 4><<<grid, 256, 0, ctx->stream>>>(table, n, b->o_items, k, b->K);
+            if (inner == 2) cheb_order_batch_kernel<double, 2><<<grid, 256, 0, ctx->stream>>>(table, n, items, k, b->K);
+            else if (inner == 8) cheb_order_batch_kernel<double, 8><<<grid, 256, 0, ctx->stream>>>(table, n, items, k, b->K);
+            else cheb_order_batch_kernel<double, 4><<<grid, 256, 0, ctx->stream>>>(table, n, items, k, b->K);
         } else {
-            if (inner == 2) cheb_order_batch_kernel<float, 2><<<grid, 256, 0, ctx->stream>>>(table, n, b->o_items, k, b->K);
-            else if (inner == 8) cheb_order_batch_kernel<float, 8><<<grid, 256, 0, ctx->stream>>>(table, n, b->o_items, k, b->K);
-            else cheb_order_batch_kernel<float, 4><<<grid, 256, 0, ctx->stream>>>(table, n, b->o_items, k, b->K);
+            if (inner == 2) cheb_order_batch_kernel<float, 2><<<grid, 256, 0, ctx->stream>>>(table, n, items, k, b->K);
+            else if (inner == 8) cheb_order_batch_kernel<float, 8><<<grid, 256, 0, ctx->stream>>>(table, n, items, k, b->K);
+            else cheb_order_batch_kernel<float, 4><<<grid, 256, 0, ctx->stream>>>(table, n, items, k, b->K);
         }
         ctx->launches++;
         cudaError_t e = cudaGetLastError();
@@ -356,9 +589,50 @@ static cudaError_t launch_fused_pass(lm_batch* b, int p, int q) {
                               b->dqueue + q, 0);
 }
 
+// Panelled step: per pass, every column panel runs the K orders in place (an odd-K result is
+// copied back from the panel scratch); a density matrix takes an in-place X <- X^dagger
+// between its two passes (U P U^dagger = U (U P)^dagger for Hermitian P), as the full-buffer
+// path does.
+static cudaError_t enqueue_step_panel(lm_batch* b) {
+    lm_ctx* ctx = b->ctx;
+    const int passes = b->kind == LM_DENSITY ? 2 : 1;
+    for (int pass = 0; pass < passes; ++pass) {
+        for (size_t q = 0; q < b->dpo.size(); ++q) {
+            cudaError_t e = launch_order_pass(b, b->dpo[q], b->pn[q], b->po_items[q]);
+            if (e != cudaSuccess) return e;
+            if (b->K % 2 == 1 && b->pc_items[q] > 0) {
+                const int grid = grid_for(ctx, b->pc_items[q], 8);
+                if (b->precision == LM_C64)
+                    copy_batch_kernel<double><<<grid, 256, 0, ctx->stream>>>(b->dpc[q], b->pn[q], b->pc_items[q]);
+                else
+                    copy_batch_kernel<float><<<grid, 256, 0, ctx->stream>>>(b->dpc[q], b->pn[q], b->pc_items[q]);
+                ctx->launches++;
+                e = cudaGetLastError();
+                if (e != cudaSuccess) return e;
+            }
+        }
+        if (b->kind == LM_DENSITY && pass == 0) {
+            const int grid = grid_for(ctx, b->ip_items, 8);
+            const int n = (int)b->states.size();
+            if (b->precision == LM_C64)
+                transpose_conj_inplace_batch_kernel<double><<<grid, 256, 0, ctx->stream>>>(b->dip, n, b->ip_items);
+            else
+                transpose_conj_inplace_batch_kernel<float><<<grid, 256, 0, ctx->stream>>>(b->dip, n, b->ip_items);
+            ctx->launches++;
+            cudaError_t e = cudaGetLastError();
+            if (e != cudaSuccess) return e;
+        }
+    }
+    return cudaSuccess;
+}
+
 // Enqueues one step for parity p; returns whether the data moves to the other buffer.
 static cudaError_t enqueue_step(lm_batch* b, int p, int* moved) {
     cudaError_t e = cudaSuccess;
+    if (b->panel_w > 0) {
+        *moved = 0;
+        return enqueue_step_panel(b);
+    }
     if (b->cfg == 0) {
         e = launch_fused_pass(b, p, 0);
         if (e == cudaSuccess && b->kind == LM_DENSITY) {
@@ -367,10 +641,11 @@ static cudaError_t enqueue_step(lm_batch* b, int p, int* moved) {
         }
         *moved = 1;
     } else {
-        e = launch_order_pass(b, b->do1[p]);
+        const int n = (int)b->states.size();
+        e = launch_order_pass(b, b->do1[p], n, b->o_items);
         if (b->kind == LM_DENSITY) {
             if (e == cudaSuccess) e = launch_transpose(b, b->dt_[p]);
-            if (e == cudaSuccess) e = launch_order_pass(b, b->do2[p]);
+            if (e == cudaSuccess) e = launch_order_pass(b, b->do2[p], n, b->o_items);
             *moved = 1;
         } else {
             *moved = b->K % 2;  // odd K ends in A
@@ -410,6 +685,7 @@ int lm_batch_destroy(lm_batch* b) {
     cudaStreamSynchronize(b->ctx->stream);
     free_graphs(b);
     free_tables(b);
+    free_panel(b);
     if (b->dqueue) cudaFree(b->dqueue);
     for (auto* s : b->solvers) lm_solver_destroy(s);
     delete b;
@@ -455,14 +731,26 @@ int lm_batch_update(lm_batch* b, double dt) {
     b->K = K;
     b->dt = dt;
     if (b->cfg < 0 || (b->cfg == 0 && !batch_fused_ok(b))) b->cfg = batch_fused_ok(b) ? 0 : 2;
+    if (b->panel_w > 0 && b->cfg == 0) b->cfg = 2;  // panels run the per-order kernels
     // pointers at parity 0 follow the states as they are now
     b->base_S.resize(b->states.size());
     b->base_A.resize(b->states.size());
     for (size_t i = 0; i < b->states.size(); ++i) {
+        if (b->panel_w == 0) {
+            int rc0 = ensure_scratch(b->states[i]);
+            if (rc0 != LM_OK) return rc0;
+        }
         b->base_S[i] = b->states[i]->d_data;
         b->base_A[i] = b->states[i]->d_a;
     }
     b->parity = 0;
+    if (b->panel_w > 0) {
+        free_graphs(b);
+        int rc = build_panel_tables(b);
+        if (rc != LM_OK) return rc;
+        b->valid = 1;
+        return LM_OK;
+    }
     if (b->cfg != 0)
         for (auto* st : b->states) {
             int rc0 = ensure_accumulator(st);
@@ -512,7 +800,7 @@ int lm_batch_step(lm_batch* b) {
                 return check_cuda(ctx, e, "lm_batch_step: graph instantiate");
             }
         } else {
-            moved = (b->cfg == 0 || b->kind == LM_DENSITY) ? 1 : b->K % 2;
+            moved = b->panel_w > 0 ? 0 : ((b->cfg == 0 || b->kind == LM_DENSITY) ? 1 : b->K % 2);
         }
         int rc = check_cuda(ctx, cudaGraphLaunch(b->graph[p], ctx->stream), "lm_batch_step: graph launch");
         if (rc != LM_OK) return rc;
@@ -523,6 +811,20 @@ int lm_batch_step(lm_batch* b) {
     if (moved) {
         for (auto* st : b->states) std::swap(st->d_data, st->d_a);
         b->parity ^= 1;
+    }
+    return LM_OK;
+}
+
+int lm_batch_set_panel(lm_batch* b, int64_t width) {
+    if (!b) return LM_ERR_ARG;
+    if (width < 0) return set_err(b->ctx, LM_ERR_ARG, "lm_batch_set_panel: width must be >= 0");
+    if (width != b->panel_w) {
+        cudaSetDevice(b->ctx->device);
+        cudaStreamSynchronize(b->ctx->stream);
+        free_graphs(b);
+        free_panel(b);
+        b->panel_w = width;
+        b->valid = 0;
     }
     return LM_OK;
 }
@@ -551,7 +853,11 @@ int lm_batch_info(lm_batch* b, int* K, int* cfg, int64_t* items, int* ninst) {
     if (!b) return LM_ERR_ARG;
     if (K) *K = b->K;
     if (cfg) *cfg = b->cfg;
-    if (items) *items = b->cfg == 0 ? b->f_items : b->o_items;
+    if (items) {
+        int64_t pitems = 0;
+        for (int64_t v : b->po_items) pitems += v;
+        *items = b->panel_w > 0 ? pitems : (b->cfg == 0 ? b->f_items : b->o_items);
+    }
     if (ninst) *ninst = (int)b->states.size();
     return LM_OK;
 }
@@ -598,7 +904,7 @@ int lm_batch_tune(lm_batch* b, int steps, double* ms_out, int* best) {
         if (ms_out) ms_out[c] = -1.0;
         t->cfg = c;
         t->valid = 0;
-        if (c == 0 && !batch_fused_ok(b)) continue;
+        if (c == 0 && (!batch_fused_ok(b) || b->panel_w > 0)) continue;
         rc = lm_batch_update(t, b->dt);
         if (rc != LM_OK) break;
         if (t->cfg != c) continue;

@@ -159,6 +159,10 @@ int ell_solver_step(lm_solver* s, lm_state* st) {
     lm_ctx* ctx = s->ctx;
     CHECK_ARG(ctx, st->n == s->ell->n, "lm_solver_step: state size does not match the Hamiltonian");
     cudaSetDevice(ctx->device);
+    {
+        int rc0 = ensure_scratch(st);
+        if (rc0 != LM_OK) return rc0;
+    }
     if (!st->d_y) {
         const size_t bytes = st->elem * (size_t)st->ld * (size_t)st->m;
         if (cudaMalloc(&st->d_y, bytes) != cudaSuccess) {

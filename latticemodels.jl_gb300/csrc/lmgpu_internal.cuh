@@ -137,7 +137,7 @@ struct lm_state {
     int kind = LM_KETS;
     int precision = LM_C64;
     void* d_data = nullptr;   // current state buffer
-    void* d_a = nullptr;      // recurrence scratch
+    void* d_a = nullptr;      // recurrence scratch (allocated on first use)
     void* d_y = nullptr;      // accumulator scratch
     double* d_w = nullptr;    // ket weights (m) or null (= all ones)
     size_t elem = 16;
@@ -266,5 +266,6 @@ int64_t bond_count(const Geom& g);
 void bessel_j_all(double x, int kmax, std::vector<double>& out);
 void make_coefs(const std::vector<double>& J, int K, double sgn, std::vector<ChebCoef>& out);
 int ensure_accumulator(lm_state* s);
+int ensure_scratch(lm_state* s);
 
 }  // namespace lmgpu

@@ -93,6 +93,7 @@ SIGNATURES = {
     "lm_batch_update": (_INT, [_P, _D]),
     "lm_batch_step": (_INT, [_P]),
     "lm_batch_set_graph": (_INT, [_P, _INT]),
+    "lm_batch_set_panel": (_INT, [_P, _I64]),
     "lm_batch_set_config": (_INT, [_P, _INT]),
     "lm_batch_info": (_INT, [_P, _PINT, _PINT, _PI64, _PINT]),
     "lm_batch_tune": (_INT, [_P, _INT, _PD, _PINT]),

@@ -57,6 +57,11 @@ class Batch:
     def set_graph(self, on: bool):
         self.ctx.check(self.ctx.lib.lm_batch_set_graph(self.handle, 1 if on else 0))
 
+    def set_panel(self, width: int):
+        """Run the per-order recurrence on column panels of ``width`` columns in place (0: off):
+        no full-size recurrence buffers, for batches that would not fit otherwise."""
+        self.ctx.check(self.ctx.lib.lm_batch_set_panel(self.handle, int(width)))
+
     def set_config(self, cfg: int):
         self.ctx.check(self.ctx.lib.lm_batch_set_config(self.handle, int(cfg)))
 
