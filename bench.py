@@ -229,13 +229,15 @@ def run_batch_workload(args):
     prec = args.precision
     dtype = np.complex64 if prec == "c32" else np.complex128
     elem = 8 if prec == "c32" else 16
-    # lattices that fit: data + recurrence buffer (+ accumulator for the per-order path)
+    # c64 runs the per-order kernels on column panels in place (P + 2 N w scratch per lattice);
+    # c32 runs the fused kernel on full buffers (P + one recurrence buffer)
+    panel = args.panel if args.panel is not None else (1024 if prec == "c64" else 0)
     free = torch.cuda.mem_get_info()[0]
-    per = 2 if prec == "c32" else 3
     budget = 0.85 * free
     take, used = [], 0
     for i, L in enumerate(Ls):
-        need = per * elem * int(L) ** 4
+        N_i = int(L) ** 2
+        need = elem * N_i * N_i + (2 * elem * N_i * min(panel, N_i) if panel else elem * N_i * N_i)
         if used + need > budget:
             break
         take.append(i)
@@ -246,6 +248,8 @@ def run_batch_workload(args):
     Pbig = np.asfortranarray((R + R.conj().T) * (0.5 / math.sqrt(Nmax)))
     del R
     batch = lmgpu.Batch("density", prec)
+    if panel:
+        batch.set_panel(panel)
     states = []
     t_setup = time.perf_counter()
     for i in take:
@@ -285,7 +289,7 @@ def run_batch_workload(args):
             "config": {"workload": BATCH_WORKLOAD.format(n=n), "instances_run": len(take),
                        "instances_requested": n, "sum_N2": int(sum(int(Ls[i]) ** 4 for i in take)),
                        "chebyshev_order": info["K"], "tuned": tune, "setup_s": t_setup,
-                       "device_bytes": used},
+                       "device_bytes": used, "panel_columns": panel},
             "clocks": clocks, "trace_sample": tr}
     print(json.dumps(line))
     return 0
@@ -525,6 +529,8 @@ def main():
                          "adjoint: loss_and_grad of the 64^2 differentiation workload; kpm: DOS moments; "
                          "densitymatrix: P_0 at T > 0, Chebyshev vs eigensolver; general: honeycomb via ELL")
     ap.add_argument("--instances", type=int, default=512)
+    ap.add_argument("--panel", type=int, default=None,
+                    help="batch: column-panel width of the per-order path (default 1024 for c64, off for c32)")
     ap.add_argument("--precision", default="c32", choices=["c32", "c64"])
     ap.add_argument("--adjoint-init", default="eigh", choices=["eigh", "random"],
                     help="initial kets of the adjoint workload: lowest eigenstates (default) or random")
