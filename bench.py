@@ -722,7 +722,13 @@ def main():
                      "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
                      "kernel": "cheb_fused_c32_kernel (all K orders of one step per launch)",
                      "alg_bytes_per_launch": alg_bytes_launch, "avg_launch_ms": avg_launch_ms,
-                     "launches_timed": sweeps},
+                     "launches_timed": sweeps,
+                     # the temporally blocked kernel moves ~1.8 block passes per step instead of
+                     # the 5 K of the per-order formula: its DRAM rate is far below the peak
+                     "dram_gbs": (traffic / (avg_launch_ms / 1000.0) / 1e9) if traffic else None,
+                     "dram_frac": (traffic / (avg_launch_ms / 1000.0) / 1e9 / peak) if traffic else None,
+                     "note": "frac > 1: all K orders of a step run on chip, so the per-order algorithmic "
+                             "bytes exceed the DRAM bytes moved (see dram_gbs); the kernel is issue-bound"},
         "e2e": {"value": world * M * args.steps / (ms_e2e / 1000.0), "unit": "ket-steps/s",
                 "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                 "ms_per_step": ms_e2e / args.steps,
