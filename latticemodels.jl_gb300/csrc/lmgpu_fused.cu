@@ -320,6 +320,9 @@ cheb_fused_c32_kernel(FusedInst single, const FusedInst* __restrict__ table, int
                 // valid rows shrink by one per order, except at an open lattice edge)
                 const bool active =
                     (cur.hard_lo || warp_row0 + ROWS_PER_WARP - 1 >= k) && (cur.hard_hi || warp_row0 < RX - k);
+                // T_k of my positions; a skipped warp takes zeros (its rows stay invalid), so the
+                // register rotation below is unconditional and compiles to renaming
+                float2 tk[KB][S];
                 if (active) {
                     const int xp = min(tx + 1, RX - 1), xm = max(tx - 1, 0);
                     const float sk = D.s[k];
@@ -333,7 +336,6 @@ cheb_fused_c32_kernel(FusedInst single, const FusedInst* __restrict__ table, int
                         up.y = __shfl_up_sync(0xffffffffu, t1[kk][S - 1].y, 1);
                         dn.x = __shfl_down_sync(0xffffffffu, t1[kk][0].x, 1);
                         dn.y = __shfl_down_sync(0xffffffffu, t1[kk][0].y, 1);
-                        float2 tk[S];
 #pragma unroll
                         for (int j = 0; j < S; ++j) {
                             const float2 vyp = (j < S - 1) ? t1[kk][j + 1] : dn;
@@ -358,34 +360,45 @@ cheb_fused_c32_kernel(FusedInst single, const FusedInst* __restrict__ table, int
                             acc.x = fmaf(d[j], t1[kk][j].x, acc.x);
                             acc.y = fmaf(d[j], t1[kk][j].y, acc.y);
                             if (k == 1) { acc.x *= 0.5f; acc.y *= 0.5f; }  // tables hold 2H/a
-                            tk[j] = acc;
+                            tk[kk][j] = acc;
                         }
 #pragma unroll
                         for (int j = 0; j < S; ++j) {
+                            const float2 t = tk[kk][j];
                             if (k == 1) {  // y = -i s_1 T1 + g0 T0 + g1 T1 (t1 still holds T0)
                                 const ChebLo lo = D.lo;
                                 const float2 x = t1[kk][j];
                                 const float lx = fmaf(lo.g0_re, x.x, fmaf(-lo.g0_im, x.y,
-                                                 fmaf(lo.g1_re, tk[j].x, -lo.g1_im * tk[j].y)));
+                                                 fmaf(lo.g1_re, t.x, -lo.g1_im * t.y)));
                                 const float ly = fmaf(lo.g0_re, x.y, fmaf(lo.g0_im, x.x,
-                                                 fmaf(lo.g1_re, tk[j].y, lo.g1_im * tk[j].x)));
-                                yv[kk][j].x = fmaf(sk, tk[j].y, lx);
-                                yv[kk][j].y = fmaf(-sk, tk[j].x, ly);
+                                                 fmaf(lo.g1_re, t.y, lo.g1_im * t.x)));
+                                yv[kk][j].x = fmaf(sk, t.y, lx);
+                                yv[kk][j].y = fmaf(-sk, t.x, ly);
                             } else if (k & 1) {  // c_k = -i s_k
-                                yv[kk][j].x = fmaf(sk, tk[j].y, yv[kk][j].x);
-                                yv[kk][j].y = fmaf(-sk, tk[j].x, yv[kk][j].y);
+                                yv[kk][j].x = fmaf(sk, t.y, yv[kk][j].x);
+                                yv[kk][j].y = fmaf(-sk, t.x, yv[kk][j].y);
                             } else {      // c_k = s_k
-                                yv[kk][j].x = fmaf(sk, tk[j].x, yv[kk][j].x);
-                                yv[kk][j].y = fmaf(sk, tk[j].y, yv[kk][j].y);
+                                yv[kk][j].x = fmaf(sk, t.x, yv[kk][j].x);
+                                yv[kk][j].y = fmaf(sk, t.y, yv[kk][j].y);
                             }
-                            t2[kk][j] = t1[kk][j];
-                            t1[kk][j] = tk[j];
                         }
                         if (k < K) {
-                            store_sites(smem + dst, kk, tx, ty, tk);
+                            store_sites(smem + dst, kk, tx, ty, tk[kk]);
                         }
                     }
+                } else {
+#pragma unroll
+                    for (int kk = 0; kk < KB; ++kk)
+#pragma unroll
+                        for (int j = 0; j < S; ++j) tk[kk][j] = make_float2(0.f, 0.f);
                 }
+#pragma unroll
+                for (int kk = 0; kk < KB; ++kk)
+#pragma unroll
+                    for (int j = 0; j < S; ++j) {
+                        t2[kk][j] = t1[kk][j];
+                        t1[kk][j] = tk[kk][j];
+                    }
                 if (k < K) __syncthreads();
             }
 
