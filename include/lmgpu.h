@@ -256,6 +256,13 @@ int lm_ell_solver_update(lm_solver *s, lm_ell *h, double dt, int force);
 /* DensityCurrents(H, state)[i, j] = 2 Im(H[i,j] P[j,i]) (src/zoo/currents.jl:92-102) for every
  * stored entry of the CSC, in its order (0 for the diagonal): nnz doubles. */
 int lm_ell_currents(lm_ell *h, lm_state *st, double *out);
+/* LocalOperatorCurrents(H, state, op)[i, j] (src/zoo/currents.jl:170-184) per stored entry:
+ * with ndof internal states per site (matrix index = ndof (site - 1) + alpha), the entry
+ * (r, c) = ((i, k), (j, beta)) contributes 2 Im(H[r,c] sum_alpha op[alpha,k] P[c, (i, alpha)]);
+ * summing the entries of the (i, j) site block gives the reference's value.  Entries inside
+ * one site block give 0.  op: ndof x ndof complex, column-major, interleaved re/im; NULL is
+ * the identity (DensityCurrents summed per site block).  1 <= ndof <= 8, n divisible by ndof. */
+int lm_ell_op_currents(lm_ell *h, lm_state *st, int ndof, const double *op, double *out);
 
 /* ---- KPM moments (DOS / LDOS without an eigensystem; the reference computes dos and ldos
  * from an Eigensystem or GreenFunction, src/greenfunction.jl:306-339) ------------------------ */
@@ -294,6 +301,10 @@ int lm_ring_destroy(lm_ring *r);
 int lm_ring_push_localdensity(lm_ring *r, lm_state *st, double t, int64_t *seq);
 /* DensityCurrents(ham, state) on every bond (src/zoo/currents.jl:92-102) at time t. */
 int lm_ring_push_currents(lm_ring *r, lm_ham *ham, lm_state *st, double t, int64_t *seq);
+/* LocalOperatorCurrents (lm_ell_op_currents) of a general Hamiltonian into the next slot:
+ * nnz values in CSC order. */
+int lm_ring_push_op_currents(lm_ring *r, lm_ell *h, lm_state *st, int ndof, const double *op, double t,
+                             int64_t *seq);
 /* *ready = 1 when entry seq has reached host memory (LM_ERR_ARG once it is overwritten). */
 int lm_ring_ready(lm_ring *r, int64_t seq, int *ready);
 /* Waits for entry seq; copies it to out (if non-null), returns the pinned view, the number

@@ -225,6 +225,85 @@ __global__ void ell_currents_kernel(int64_t nnz, const int* __restrict__ row, co
     }
 }
 
+// LocalOperatorCurrents per stored entry (r, c) = ((i, k), (j, beta)):
+// 2 Im(H[r,c] Q), Q = sum_alpha op[alpha,k] P[c, (i, alpha)]; ket blocks build
+// P[c, q] = sum_m w_m x[c,m] conj(x[q,m]) with the operator applied to the conjugated side.
+template <typename R>
+__global__ void ell_op_currents_kernel(int64_t nnz, const int* __restrict__ row, const int* __restrict__ col,
+                                       const double2* __restrict__ hv, int kind,
+                                       const typename CT<R>::V* __restrict__ x, int64_t m, int64_t ld,
+                                       const double* __restrict__ wts, int ndof, LocalOp op,
+                                       double* __restrict__ out) {
+    for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < nnz; p += (int64_t)gridDim.x * blockDim.x) {
+        const int r = row[p], c = col[p];
+        const int si = r / ndof, kr = r - si * ndof;
+        if (si == c / ndof) {
+            out[p] = 0.0;
+            continue;
+        }
+        const int64_t q0 = (int64_t)si * ndof;
+        double qr = 0.0, qi = 0.0;
+        if (kind == LM_DENSITY) {
+            for (int a = 0; a < ndof; ++a) {
+                const double2 o = op.o[a + kr * ndof];
+                const typename CT<R>::V v = x[(q0 + a) * ld + c];  // P[c, q0 + a]
+                qr += o.x * v.x - o.y * v.y;
+                qi += o.x * v.y + o.y * v.x;
+            }
+        } else {
+            for (int64_t k = 0; k < m; ++k) {
+                double sr = 0.0, sim = 0.0;  // sum_alpha op[alpha,kr] conj(x[q0+alpha, k])
+                for (int a = 0; a < ndof; ++a) {
+                    const double2 o = op.o[a + kr * ndof];
+                    const typename CT<R>::V b = x[k * ld + q0 + a];
+                    sr += o.x * b.x + o.y * b.y;
+                    sim += o.y * b.x - o.x * b.y;
+                }
+                const typename CT<R>::V v = x[k * ld + c];
+                const double ww = wts ? wts[k] : 1.0;
+                qr += ww * (v.x * sr - v.y * sim);
+                qi += ww * (v.x * sim + v.y * sr);
+            }
+        }
+        const double2 h = hv[p];
+        out[p] = 2.0 * (h.x * qi + h.y * qr);
+    }
+}
+
+int make_local_op(lm_ctx* ctx, const lm_ell* h, int ndof, const double* op, LocalOp* lop, const char* who) {
+    if (!(ndof >= 1 && ndof <= 8 && h->n % ndof == 0))
+        return set_err(ctx, LM_ERR_ARG, std::string(who) + ": ndof must be in 1..8 and divide the matrix size");
+    *lop = LocalOp{};
+    for (int a = 0; a < ndof; ++a)
+        for (int b = 0; b < ndof; ++b) {
+            const int idx = a + b * ndof;
+            if (op) {
+                if (!std::isfinite(op[2 * idx]) || !std::isfinite(op[2 * idx + 1]))
+                    return set_err(ctx, LM_ERR_ARG, std::string(who) + ": non-finite operator entry");
+                lop->o[idx] = make_double2(op[2 * idx], op[2 * idx + 1]);
+            } else {
+                lop->o[idx] = make_double2(a == b ? 1.0 : 0.0, 0.0);
+            }
+        }
+    return LM_OK;
+}
+
+cudaError_t launch_ell_op_currents(lm_ctx* ctx, const lm_ell* h, const lm_state* st, int ndof, const LocalOp& lop,
+                                   double* d_out) {
+    if (h->nnz == 0) return cudaSuccess;
+    const unsigned grid = (unsigned)std::min<int64_t>((h->nnz + 255) / 256, 65535);
+    if (st->precision == LM_C64)
+        ell_op_currents_kernel<double><<<grid, 256, 0, ctx->stream>>>(
+            h->nnz, h->d_crow, h->d_ccol, h->d_cval, st->kind, (const double2*)st->d_data, st->m, st->ld, st->d_w,
+            ndof, lop, d_out);
+    else
+        ell_op_currents_kernel<float><<<grid, 256, 0, ctx->stream>>>(
+            h->nnz, h->d_crow, h->d_ccol, h->d_cval, st->kind, (const float2*)st->d_data, st->m, st->ld, st->d_w,
+            ndof, lop, d_out);
+    ctx->launches++;
+    return cudaGetLastError();
+}
+
 }  // namespace lmgpu
 
 using namespace lmgpu;
@@ -469,6 +548,25 @@ int lm_ell_currents(lm_ell* h, lm_state* st, double* out) {
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
     cudaFree(d_out);
     return check_cuda(ctx, e, "lm_ell_currents");
+}
+
+int lm_ell_op_currents(lm_ell* h, lm_state* st, int ndof, const double* op, double* out) {
+    if (!h) return LM_ERR_ARG;
+    lm_ctx* ctx = h->ctx;
+    CHECK_ARG(ctx, st != nullptr && st->ctx == ctx && st->n == h->n, "lm_ell_op_currents: state does not match");
+    CHECK_ARG(ctx, out != nullptr, "lm_ell_op_currents: null output");
+    LocalOp lop;
+    const int rc = make_local_op(ctx, h, ndof, op, &lop, "lm_ell_op_currents");
+    if (rc != LM_OK) return rc;
+    if (h->nnz == 0) return LM_OK;
+    cudaSetDevice(ctx->device);
+    double* d_out = nullptr;
+    CUDA_TRY(ctx, cudaMalloc((void**)&d_out, sizeof(double) * (size_t)h->nnz), "lm_ell_op_currents: allocation");
+    cudaError_t e = launch_ell_op_currents(ctx, h, st, ndof, lop, d_out);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out, d_out, sizeof(double) * (size_t)h->nnz, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    cudaFree(d_out);
+    return check_cuda(ctx, e, "lm_ell_op_currents");
 }
 
 }  // extern "C"

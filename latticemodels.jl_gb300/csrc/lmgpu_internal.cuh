@@ -253,6 +253,15 @@ void plan_propagator(lm_solver* s, double emin, double emax, double dt);
 // lm_solver_step / destroy for a solver updated with an lm_ell Hamiltonian (lmgpu_ell.cu).
 int ell_solver_step(lm_solver* s, lm_state* st);
 void ell_free_tables(lm_solver* s);
+// A local (on-site) operator of up to 8 internal states, column-major, passed by value.
+struct LocalOp {
+    double2 o[64];
+};
+// Checks ndof / op against h and fills lop (op null: the identity); an lm_status.
+int make_local_op(lm_ctx* ctx, const lm_ell* h, int ndof, const double* op, LocalOp* lop, const char* who);
+// LocalOperatorCurrents per stored CSC entry of h into d_out (nnz doubles), lmgpu_ell.cu.
+cudaError_t launch_ell_op_currents(lm_ctx* ctx, const lm_ell* h, const lm_state* st, int ndof, const LocalOp& lop,
+                                   double* d_out);
 // out = alpha (2H~) tp - tpp + w lam over an n x M ket block (tables 2H/a, 2(V-b)/a); tpp and
 // lam may be null; out may alias tpp; with y non-null also y += cy out (lmgpu_adjoint.cu).
 cudaError_t launch_stencil_recur(lm_ctx* ctx, const Geom& g, int precision, const void* hop2, const void* diag2,

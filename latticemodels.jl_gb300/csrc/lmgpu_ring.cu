@@ -130,6 +130,21 @@ int lm_ring_push_currents(lm_ring* r, lm_ham* h, lm_state* st, double t, int64_t
     });
 }
 
+int lm_ring_push_op_currents(lm_ring* r, lm_ell* h, lm_state* st, int ndof, const double* op, double t,
+                             int64_t* seq) {
+    if (!r) return LM_ERR_ARG;
+    lm_ctx* ctx = r->ctx;
+    CHECK_ARG(ctx, h != nullptr && h->ctx == ctx, "lm_ring_push_op_currents: Hamiltonian from another context");
+    CHECK_ARG(ctx, st != nullptr && st->ctx == ctx && st->n == h->n,
+              "lm_ring_push_op_currents: state does not match the Hamiltonian");
+    CHECK_ARG(ctx, h->nnz <= r->len, "lm_ring_push_op_currents: slot shorter than the stored entries");
+    LocalOp lop;
+    const int rc = make_local_op(ctx, h, ndof, op, &lop, "lm_ring_push_op_currents");
+    if (rc != LM_OK) return rc;
+    cudaSetDevice(ctx->device);
+    return ring_push(r, t, h->nnz, seq, [&](double* d) { return launch_ell_op_currents(ctx, h, st, ndof, lop, d); });
+}
+
 int lm_ring_ready(lm_ring* r, int64_t seq, int* ready) {
     if (!r || !ready) return LM_ERR_ARG;
     int k = 0;

@@ -214,6 +214,26 @@ update_solver!(s::ChebyshevGPU, H::GPUSparseHamiltonian, dt, force=false) =
     check(ccall((:lm_ell_solver_update, LIB), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Cdouble, Cint), s.handle, H.handle, dt, force),
           s.ctx.handle)
 
+# LocalOperatorCurrents(H, state, op) (src/zoo/currents.jl:150-184) on a general Hamiltonian with
+# ndof internal states per site: one device pass gives every stored entry's share, the site-pair
+# value is the sum over its block (`sparse` adds the duplicates).  op === nothing: DensityCurrents.
+function gpu_operator_currents(H::GPUSparseHamiltonian, A::SparseMatrixCSC{ComplexF64,Int64}, st, ndof::Integer,
+                               op=nothing)
+    out = Vector{Float64}(undef, nnz(A))
+    opm = op === nothing ? Ptr{ComplexF64}(C_NULL) : convert(Matrix{ComplexF64}, op)
+    check(ccall((:lm_ell_op_currents, LIB), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Cint, Ptr{ComplexF64}, Ptr{Float64}),
+                H.handle, st.handle, ndof, opm, out), H.ctx.handle)
+    I, J, V = Int[], Int[], Float64[]
+    rows = rowvals(A)
+    for c in 1:size(A, 2), p in nzrange(A, c)
+        si, sj = (rows[p] - 1) ÷ ndof + 1, (c - 1) ÷ ndof + 1
+        si == sj && continue
+        push!(I, si); push!(J, sj); push!(V, out[p])
+    end
+    ns = size(A, 1) ÷ ndof
+    return sparse(I, J, V, ns, ns)  # M[i, j] = curr[i, j]
+end
+
 # ---- readout ring behind TimeSequence(f, ev(times)) (src/timesequence.jl:41-43) --------------
 # Readouts are computed into device ring slots and downloaded asynchronously; entries are taken
 # only when their slot is about to be reused, so the evolution never waits on a readout.
@@ -402,6 +422,6 @@ function ChainRulesCore.rrule(::typeof(density_loss), V, B, p::DensityLossProble
 end
 
 export ChebyshevGPU, DeviceLattice, DeviceState, gpu_tightbinding, bond_currents, ReadoutRing,
-       gpu_timesequence, GPUBatch, DensityLossProblem, density_loss, GPUSparseHamiltonian, set_values!
+       gpu_timesequence, GPUBatch, DensityLossProblem, density_loss, GPUSparseHamiltonian, set_values!, gpu_operator_currents
 
 end # module

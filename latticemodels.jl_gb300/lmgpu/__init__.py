@@ -14,8 +14,8 @@ from .evolution import ChebyshevGPU, Evolution, EvolutionIterator, EvolutionSolv
 from .fields import FieldSum, LandauGauge, NoField, PointFlux, PointFluxes, SymmetricGauge
 from .hamiltonian import Hamiltonian, tightbinding_hamiltonian
 from .lattice import LatticeValue, SquareLattice
-from .observables import Currents, DensityCurrents, localdensity
-from .sparse import Sites, SparseHamiltonian, entry_currents
+from .observables import Currents, DensityCurrents, currentsfromto, localdensity
+from .sparse import LocalOperatorCurrents, SiteCurrents, Sites, SparseHamiltonian, entry_currents
 from .spectrum import densitymatrix, diagonalize
 from .states import DensityMatrix, DeviceState, Ket, KetBlock, Operator
 from .timesequence import (ReadoutRing, TimeSequence, differentiate, integrate, moment_currents,
@@ -26,7 +26,7 @@ __all__ = [
     "ChebyshevGPU", "Evolution", "EvolutionIterator", "EvolutionSolver", "EvolutionTimestamp",
     "FieldSum", "LandauGauge", "NoField", "PointFlux", "PointFluxes", "SymmetricGauge",
     "Hamiltonian", "tightbinding_hamiltonian", "LatticeValue", "SquareLattice",
-    "Currents", "DensityCurrents", "localdensity", "densitymatrix", "diagonalize",
+    "Currents", "DensityCurrents", "currentsfromto", "localdensity", "densitymatrix", "diagonalize",
     "DensityMatrix", "DeviceState", "Ket", "KetBlock", "Operator",
-    "Sites", "SparseHamiltonian", "entry_currents", "ReadoutRing", "TimeSequence", "differentiate", "integrate", "moment_currents", "moment_density",
+    "LocalOperatorCurrents", "SiteCurrents", "Sites", "SparseHamiltonian", "entry_currents", "ReadoutRing", "TimeSequence", "differentiate", "integrate", "moment_currents", "moment_density",
 ]

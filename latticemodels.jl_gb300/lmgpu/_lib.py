@@ -106,6 +106,8 @@ SIGNATURES = {
     "lm_ell_bounds": (_INT, [_P, _PD, _PD]),
     "lm_ell_solver_update": (_INT, [_P, _P, _D, _INT]),
     "lm_ell_currents": (_INT, [_P, _P, _PD]),
+    "lm_ell_op_currents": (_INT, [_P, _P, C.c_int, _PD, _PD]),
+    "lm_ring_push_op_currents": (_INT, [_P, _P, _P, C.c_int, _PD, _D, _PI64]),
     "lm_kpm_moments": (_INT, [_P, _D, _D, _INT, _P, _INT, _PD]),
     "lm_cheb_apply": (_INT, [_P, _D, _D, _PD, _INT, _P, _P]),
     "lm_ham_lanczos_bounds": (_INT, [_P, _INT, C.c_ulonglong, _PD, _PD]),

@@ -138,7 +138,7 @@ class LatticeValue:
     def __init__(self, lattice: SquareLattice, values):
         self.lattice = lattice
         self.values = np.asarray(values)
-        if self.values.shape[0] != lattice.N:
+        if self.values.shape[0] != getattr(lattice, "nsites", lattice.N):
             raise ValueError("value count does not match the lattice")
 
     def __getitem__(self, i):

@@ -18,10 +18,16 @@ from .states import DeviceState
 CURRENTS_EPS = 1e-10  # src/currents.jl:4
 
 
+def _site_sum(lattice, vals):
+    n = getattr(lattice, "internal", 1)
+    return vals if n == 1 else vals.reshape(-1, n).sum(axis=1)
+
+
 def localdensity(state: DeviceState) -> LatticeValue:
+    """Re P[i,i] summed over the internal states of every site (latticeutils.jl:44)."""
     out = np.empty(state.n, dtype=np.float64)
     state.ctx.check(state.ctx.lib.lm_localdensity(state.handle, _lib.dptr(out)))
-    return LatticeValue(state.lattice, out)
+    return LatticeValue(state.lattice, _site_sum(state.lattice, out))
 
 
 def localdensity_into(state: DeviceState, out: np.ndarray) -> np.ndarray:
@@ -31,7 +37,15 @@ def localdensity_into(state: DeviceState, out: np.ndarray) -> np.ndarray:
 
 
 class DensityCurrents:
-    """Lazy density currents of ``state`` under ``H``; bond values come from one device pass."""
+    """Lazy density currents of ``state`` under ``H``; bond values come from one device pass.
+    For a SparseHamiltonian this is a ``SiteCurrents`` (per stored entry, summed per site
+    block)."""
+
+    def __new__(cls, H, state):
+        from .sparse import SiteCurrents, SparseHamiltonian
+        if isinstance(H, SparseHamiltonian):
+            return SiteCurrents(H, state)
+        return super().__new__(cls)
 
     def __init__(self, H: Hamiltonian, state: DeviceState):
         if H.lattice != state.lattice:
@@ -78,6 +92,13 @@ class Currents:
 
     def __init__(self, curr: DensityCurrents, bonds=None):
         import scipy.sparse as sp
+        from .sparse import SiteCurrents, site_currents_matrix
+        if isinstance(curr, SiteCurrents):
+            if bonds is not None:
+                raise ValueError("bond subsets are defined for the square-lattice path only")
+            self.lattice = curr.lattice
+            self.currents = site_currents_matrix(curr)
+            return
         lat = curr.lattice
         src, dst = lat.bonds()
         v = curr.bond_values()
@@ -96,3 +117,15 @@ class Currents:
 
     def toarray(self):
         return self.currents.toarray()
+
+
+def currentsfromto(curr, src, dst=None) -> float:
+    """currentsfromto(curr, src[, dst]) (src/currents.jl:104-109): the sum of curr[i, j] over
+    i in ``src`` and j in ``dst`` (default: every other site); 1-based site indices."""
+    ns = getattr(curr.lattice, "nsites", curr.lattice.N)
+    src = [src] if np.ndim(src) == 0 else list(src)
+    dst = [j for j in range(1, ns + 1) if j not in src] if dst is None else ([dst] if np.ndim(dst) == 0 else list(dst))
+    if isinstance(curr, Currents):
+        M = curr.currents.tocsr()
+        return float(sum(M[i - 1, j - 1] for i in src for j in dst))
+    return float(sum(curr[i, j] for i in src for j in dst))

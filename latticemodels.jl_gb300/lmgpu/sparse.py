@@ -21,10 +21,16 @@ from .device import default_context
 
 
 class Sites:
-    """The site set of a general Hamiltonian: N sites, optional coordinates (N x d)."""
+    """The site set of a general Hamiltonian.  ``N`` is the matrix size (lattice sites times
+    ``internal`` states per site, index = internal (site - 1) + alpha as in the reference's
+    one-particle basis); optional coordinates, one row per site."""
 
-    def __init__(self, N: int, coords=None, name: str = "Sites"):
+    def __init__(self, N: int, coords=None, name: str = "Sites", internal: int = 1):
         self.N = int(N)
+        self.internal = int(internal)
+        if self.internal < 1 or self.N % self.internal:
+            raise ValueError("internal must be a positive divisor of N")
+        self.nsites = self.N // self.internal
         self.coords_ = None if coords is None else np.asarray(coords, dtype=np.float64)
         self.name = name
 
@@ -35,9 +41,11 @@ class Sites:
         return ("sites", self.N, id(self))
 
     def __len__(self):
-        return self.N
+        return self.nsites
 
     def __repr__(self):
+        if self.internal > 1:
+            return f"{self.name}({self.nsites} sites x {self.internal} internal states)"
         return f"{self.name}({self.N} sites)"
 
 
@@ -122,6 +130,103 @@ class SparseHamiltonian:
 
     def __repr__(self):
         return f"SparseHamiltonian({self.N}x{self.N}, nnz={len(self.rowval)}) on {self.lattice!r}"
+
+
+def _local_op(H: SparseHamiltonian, op):
+    n = H.lattice.internal
+    if op is None:
+        return None
+    O = np.asarray(op, dtype=np.complex128)
+    if O.shape != (n, n):
+        raise ValueError(f"operator must be {n}x{n}, the internal basis of the Hamiltonian")
+    return np.ascontiguousarray(O.T).view(np.float64).ravel()  # column-major, interleaved
+
+
+class SiteCurrents:
+    """DensityCurrents (src/zoo/currents.jl:81-102) or LocalOperatorCurrents (:150-184) of a
+    state under a SparseHamiltonian.  One device pass gives the value of every stored entry of
+    H (``lm_ell_op_currents``); ``curr[i, j]`` (1-based sites) is the sum over the entries of
+    the (i, j) site block, which is the reference's ``getindex``."""
+
+    def __init__(self, H: SparseHamiltonian, state, op=None):
+        if H.lattice is not state.lattice and H.N != state.n:
+            raise ValueError("Hamiltonian and state live on different site sets")
+        self.hamiltonian = H
+        self.state = state
+        self.op = None if op is None else np.asarray(op, dtype=np.complex128)
+        self._op_buf = _local_op(H, op)
+        self._entries = None
+        self._pairs = None
+
+    @property
+    def lattice(self):
+        return self.hamiltonian.lattice
+
+    def entry_values(self, out: np.ndarray = None) -> np.ndarray:
+        """The contribution of every stored entry of H, in CSC order (0 inside a site block)."""
+        if self._entries is None or out is not None:
+            ctx = self.state.ctx
+            dh = self.hamiltonian.device(ctx)
+            vals = out if out is not None else np.empty(len(self.hamiltonian.rowval), dtype=np.float64)
+            opp = None if self._op_buf is None else _lib.dptr(self._op_buf)
+            ctx.check(ctx.lib.lm_ell_op_currents(dh.handle, self.state.handle, int(self.lattice.internal), opp,
+                                                 _lib.dptr(vals)))
+            if out is not None:
+                return out
+            self._entries = vals
+        return self._entries
+
+    bond_values = entry_values
+
+    def site_pairs(self):
+        """(src, dst, values): every ordered pair of distinct sites (1-based) with a stored
+        block, and the summed current of that block."""
+        if self._pairs is None:
+            H = self.hamiltonian
+            self._pairs = _aggregate_pairs(H, self.entry_values())
+        return self._pairs
+
+    def __getitem__(self, ij):
+        i, j = ij
+        src, dst, v = self.site_pairs()
+        k = np.nonzero((src == i) & (dst == j))[0]
+        return float(v[k[0]]) if len(k) else 0.0
+
+
+def _entry_sites(H: SparseHamiltonian):
+    n = H.lattice.internal
+    cols = np.repeat(np.arange(H.N, dtype=np.int64), np.diff(H.colptr))
+    return (H.rowval - 1) // n, cols // n
+
+
+def _aggregate_pairs(H: SparseHamiltonian, entries):
+    si, sj = _entry_sites(H)
+    off = si != sj
+    key = si[off] * H.lattice.nsites + sj[off]
+    uk, inv = np.unique(key, return_inverse=True)
+    vals = np.bincount(inv, weights=entries[off], minlength=len(uk))
+    return uk // H.lattice.nsites + 1, uk % H.lattice.nsites + 1, vals
+
+
+def LocalOperatorCurrents(H: SparseHamiltonian, state, op) -> SiteCurrents:
+    """LocalOperatorCurrents(H, state, op) (src/zoo/currents.jl:150-170): currents of the local
+    operator ``op`` (internal x internal) on a Hamiltonian with internal degrees of freedom."""
+    if not isinstance(H, SparseHamiltonian) or H.lattice.internal < 2:
+        raise ValueError("System expected to have internal degrees of freedom")
+    return SiteCurrents(H, state, op)
+
+
+def site_currents_matrix(curr: SiteCurrents):
+    """Currents(curr) (src/currents.jl:223-237): curr[i, j] at [i, j] and -curr[i, j] at [j, i]
+    for every site pair i > j, |value| < 1e-10 dropped; a scipy CSC matrix over the sites."""
+    import scipy.sparse as sp
+    src, dst, v = curr.site_pairs()
+    lo = (src > dst) & (np.abs(v) >= 1e-10)
+    r = np.concatenate([src[lo] - 1, dst[lo] - 1])
+    c = np.concatenate([dst[lo] - 1, src[lo] - 1])
+    d = np.concatenate([v[lo], -v[lo]])
+    ns = curr.lattice.nsites
+    return sp.csc_matrix((d, (r, c)), shape=(ns, ns))
 
 
 def entry_currents(H: SparseHamiltonian, state) -> np.ndarray:

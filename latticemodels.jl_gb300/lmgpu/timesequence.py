@@ -46,6 +46,19 @@ class ReadoutRing:
                                                           C.byref(seq)))
         return seq.value
 
+    def push_op_currents(self, H, state, t: float, op=None) -> int:
+        """DensityCurrents (op None) or LocalOperatorCurrents of a SparseHamiltonian: the value
+        of every stored entry, in CSC order."""
+        from . import _lib
+        from .sparse import _local_op
+        dh = H.device(self.ctx)
+        buf = _local_op(H, op)
+        seq = C.c_int64()
+        self.ctx.check(self.ctx.lib.lm_ring_push_op_currents(
+            self.handle, dh.handle, state.handle, int(H.lattice.internal), None if buf is None else _lib.dptr(buf),
+            float(t), C.byref(seq)))
+        return seq.value
+
     def ready(self, seq: int) -> bool:
         r = C.c_int()
         self.ctx.check(self.ctx.lib.lm_ring_ready(self.handle, int(seq), C.byref(r)))
@@ -89,7 +102,8 @@ def moment_density(moment):
 
 
 def moment_currents(moment):
-    """f(moment) = bond values of DensityCurrents(moment.H, moment.state) (src/zoo/currents.jl:92-102)."""
+    """f(moment) = bond values of DensityCurrents(moment.H, moment.state) (src/zoo/currents.jl:92-102);
+    for a SparseHamiltonian the value of every stored entry (SiteCurrents.entry_values)."""
     from .observables import DensityCurrents
     return DensityCurrents(moment.H, moment.state).bond_values()
 
@@ -132,16 +146,27 @@ class TimeSequence:
         ring = None
         pending = []  # sequence numbers not yet collected
         wrap = None
+        from .observables import _site_sum
+        from .sparse import SparseHamiltonian
         for moment in it:
             st = moment.state
+            general = isinstance(moment.H, SparseHamiltonian)
             if ring is None:
-                length = st.n if kind == "density" else max(st.lattice.nbonds(), 1)
+                if kind == "density":
+                    length = st.n
+                elif general:
+                    length = max(len(moment.H.rowval), 1)
+                else:
+                    length = max(st.lattice.nbonds(), 1)
                 ring = _ring_for(st.ctx, length, nslots)
-                wrap = (lambda v, lat=st.lattice: LatticeValue(lat, v)) if kind == "density" else (lambda v: v)
+                wrap = ((lambda v, lat=st.lattice: LatticeValue(lat, _site_sum(lat, v))) if kind == "density"
+                        else (lambda v: v))
             if len(pending) == ring.nslots:  # the oldest slot is about to be reused
                 self._take(ring, pending.pop(0), wrap)
             if kind == "density":
                 pending.append(ring.push_density(st, moment.t))
+            elif general:
+                pending.append(ring.push_op_currents(moment.H, st, moment.t))
             else:
                 pending.append(ring.push_currents(moment.H, st, moment.t))
         for seq in pending:

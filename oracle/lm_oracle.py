@@ -796,15 +796,21 @@ def honeycomb_hamiltonian(a: int, b: int, t1: float = 1.0, B: float = 0.0, onsit
     return H.tocsc(), coords
 
 
-def qwz_hamiltonian(Lx: int, Ly: int, m=1.0):
-    """qwz(l, m) (src/zoo/models.jl:110-137) on SquareLattice(Lx, Ly), open boundaries, two
-    internal states per site (index 2 (site - 1) + spin): m sigma_z on site,
-    c+_{i+x} (sigma_z - i sigma_x)/2 c_i and c+_{i+y} (sigma_z - i sigma_y)/2 c_i plus h.c."""
+def qwz_hamiltonian(Lx: int, Ly: int, m=1.0, field=None):
+    """qwz(l, m; field) (src/zoo/models.jl:129-137) on SquareLattice(Lx, Ly), open boundaries,
+    two internal states per site (matrix index 2 (site - 1) + spin).  The builder places each
+    term as written (src/operators/builder.jl:134-151, constructoperator.jl:14-19): for the
+    bond (i, i + e) of BravaisTranslation(axis) -- the pair (site, destination(site)),
+    src/lattices/bravais/bonds.jl:87-98 -- the block H[i, i+e] = M e^{-2 pi i LI(r_i, r_{i+e})}
+    with M = [1 -i; -i -1]/2 (x) or [1 -1; 1 -1]/2 (y), and H[i+e, i] its adjoint; the
+    on-site block is m_i sigma_z."""
+    lat = SquareLattice(Lx, Ly)
     N = Lx * Ly
     mz = np.array([[1, 0], [0, -1]], dtype=np.complex128)
     Mx = np.array([[1, -1j], [-1j, -1]], dtype=np.complex128) / 2
     My = np.array([[1, -1], [1, -1]], dtype=np.complex128) / 2
     mm = np.broadcast_to(np.asarray(m, dtype=float), (N,))
+    fld = adapt_field(field, lat) if field is not None else None
     H = sp.lil_matrix((2 * N, 2 * N), dtype=np.complex128)
     site = lambda x, y: (x - 1) * Ly + (y - 1)
     for x in range(1, Lx + 1):
@@ -814,8 +820,10 @@ def qwz_hamiltonian(Lx: int, Ly: int, m=1.0):
             for (dx, dy, Mb) in ((1, 0, Mx), (0, 1, My)):
                 if x + dx <= Lx and y + dy <= Ly:
                     t = site(x + dx, y + dy)
-                    H[2 * t:2 * t + 2, 2 * s:2 * s + 2] = Mb
-                    H[2 * s:2 * s + 2, 2 * t:2 * t + 2] = Mb.conj().T
+                    li = 0.0 if fld is None else fld.line_integral((x, y), (x + dx, y + dy))
+                    blk = Mb * np.exp(-2j * math.pi * li)
+                    H[2 * s:2 * s + 2, 2 * t:2 * t + 2] = blk
+                    H[2 * t:2 * t + 2, 2 * s:2 * s + 2] = blk.conj().T
     return H.tocsc()
 
 
@@ -840,4 +848,84 @@ def csc_currents(H, state, weights=None, is_density=None):
         pji = np.einsum("bm,bm,m->b", s[cols, :], np.conj(s[rows, :]), w)
     J = 2.0 * np.imag(H.data * pji)
     J[rows == cols] = 0.0
+    return J
+
+
+# ----------------------------------------------------------------------------------------
+# f3: currents with internal degrees of freedom      src/zoo/currents.jl:24-27, :81-102, :170-184
+#                                                     src/currents.jl:104-109, :223-237
+# ----------------------------------------------------------------------------------------
+def _dense_state(state, weights=None, is_density=None):
+    s = np.asarray(state)
+    if s.ndim == 1:
+        return np.outer(s, np.conj(s))
+    if is_density or (is_density is None and weights is None and s.shape[0] == s.shape[1]):
+        return s
+    w = np.ones(s.shape[1]) if weights is None else np.asarray(weights, dtype=np.float64)
+    return (s * w[None, :]) @ np.conj(s).T
+
+
+def local_operator_current(H, P, ndof, op, i, j):
+    """LocalOperatorCurrents(H, P, op)[i, j] with 0-based sites (src/zoo/currents.jl:170-184):
+    T = the (i, j) block of H (``_block``, :24-27); sum over alpha, beta of
+    2 Im((op T)[alpha, beta] * P[(j, beta), (i, alpha)]).  op = identity is DensityCurrents
+    (:92-102)."""
+    n = ndof
+    T = np.asarray(sp.csr_matrix(H)[i * n:(i + 1) * n, j * n:(j + 1) * n].todense())
+    O = np.eye(n) if op is None else np.asarray(op, dtype=np.complex128)
+    OT = O @ T
+    tot = 0.0
+    for a in range(n):
+        for b in range(n):
+            tot += 2.0 * np.imag(OT[a, b] * P[j * n + b, i * n + a])
+    return tot
+
+
+def site_currents(H, state, ndof, op=None, weights=None, is_density=None):
+    """{(i, j): value} for every ordered pair of distinct sites whose H block is nonzero."""
+    P = _dense_state(state, weights, is_density)
+    A = sp.coo_matrix(H)
+    pairs = sorted({(int(r) // ndof, int(c) // ndof) for r, c in zip(A.row, A.col) if r // ndof != c // ndof})
+    return {(i, j): local_operator_current(H, P, ndof, op, i, j) for (i, j) in pairs}
+
+
+def site_currents_matrix(H, state, ndof, op=None, **kw):
+    """Currents(curr) (src/currents.jl:223-237): for every site pair i > j the value curr[i, j]
+    at [i, j] and its negative at [j, i]; |value| < 1e-10 dropped.  Pairs with a zero block
+    carry zero current and are skipped."""
+    nsites = H.shape[0] // ndof
+    vals = site_currents(H, state, ndof, op, **kw)
+    I, J, V = [], [], []
+    for (i, j), v in vals.items():
+        if i > j and abs(v) >= CURRENTS_EPS:
+            I += [i, j]
+            J += [j, i]
+            V += [v, -v]
+    return sp.csc_matrix((V, (I, J)), shape=(nsites, nsites))
+
+
+def currentsfromto(M, src):
+    """currentsfromto(curr, src) (src/currents.jl:104-109) on a materialised matrix: the sum of
+    M[src, j] over every other site j (0-based src)."""
+    row = np.asarray(sp.csr_matrix(M)[src, :].todense()).ravel()
+    return float(row.sum() - row[src])
+
+
+def entry_op_currents(H, state, ndof, op=None, weights=None, is_density=None):
+    """The per-entry split of local_operator_current: for the stored entry
+    (r, c) = ((i, k), (j, beta)) of H with i != j, 2 Im(H[r,c] sum_alpha op[alpha,k] P[c, (i, alpha)]),
+    in CSC order (0 for entries inside one site block).  Summing the entries of the (i, j)
+    block gives local_operator_current(H, P, ndof, op, i, j)."""
+    P = _dense_state(state, weights, is_density)
+    A = sp.csc_matrix(H)
+    A.sort_indices()
+    cols = np.repeat(np.arange(A.shape[1]), np.diff(A.indptr))
+    rows = A.indices
+    O = np.eye(ndof) if op is None else np.asarray(op, dtype=np.complex128)
+    si, k = rows // ndof, rows % ndof
+    Q = np.zeros(len(rows), dtype=np.complex128)
+    for a in range(ndof):
+        Q += O[a, k] * P[cols, si * ndof + a]
+    J = 2.0 * np.imag(A.data * Q)
+    J[si == cols // ndof] = 0.0
     return J

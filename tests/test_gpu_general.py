@@ -99,3 +99,107 @@ def test_rejects_non_hermitian(lm):
     M = sp.random(12, 12, density=0.3, random_state=1, format="csc") * (1 + 1j)
     with pytest.raises(lm.LMError):
         lm.SparseHamiltonian(lm.Sites(12), M).device()
+
+
+SZ = np.array([[1, 0], [0, -1]])
+OPS = [None, SZ, np.array([[1, 0], [0, 0]]), np.array([[0.3, 1 - 2j], [1 + 2j, -0.5]])]
+
+
+def qwz_setup(lm):
+    """qwz(SquareLattice(4, 4), field=LandauGauge(0.1)) with the field-free ground state
+    (test/test_currents.jl:1-9)."""
+    H0 = o.qwz_hamiltonian(4, 4).toarray()
+    H1 = o.qwz_hamiltonian(4, 4, field=o.LandauGauge(0.1))
+    gs = np.linalg.eigh(H0)[1][:, 0]
+    sites = lm.Sites(32, None, "qwz", internal=2)
+    return H1, gs, sites, lm.SparseHamiltonian(sites, H1)
+
+
+@pytest.mark.parametrize("kind", ["ket", "density"])
+@pytest.mark.parametrize("precision", ["c64", "c32"])
+def test_local_operator_currents(lm, kind, precision):
+    H1, gs, sites, H = qwz_setup(lm)
+    if kind == "ket":
+        st = lm.KetBlock(sites, gs[:, None], precision=precision)
+        ref_state, kw = gs, {}
+    else:
+        P = np.outer(gs, gs.conj())
+        st = lm.DensityMatrix(sites, P, precision=precision)
+        ref_state, kw = P, {"is_density": True}
+    tol = 1e-13 if precision == "c64" else 1e-6
+    for op in OPS:
+        curr = lm.LocalOperatorCurrents(H, st, op) if op is not None else lm.DensityCurrents(H, st)
+        ent = curr.entry_values()
+        ref = o.entry_op_currents(H1, ref_state, 2, op, **kw)
+        assert np.abs(ent - ref).max() <= tol * max(np.abs(ref).max(), 1e-3)
+        M = lm.Currents(curr).currents
+        Mref = o.site_currents_matrix(H1, ref_state, 2, op, **kw)
+        assert abs(M - Mref).max() <= tol * max(abs(Mref).max(), 1e-3)
+        src, dst, v = curr.site_pairs()
+        pairs = o.site_currents(H1, ref_state, 2, op, **kw)
+        for a, b, x in zip(src, dst, v):
+            assert abs(x - pairs[(a - 1, b - 1)]) <= tol * max(np.abs(v).max(), 1e-3)
+            assert curr[a, b] == x
+    # test/test_currents.jl:88-93 through the device: Heisenberg identity at l[6]
+    spin = lm.Currents(lm.LocalOperatorCurrents(H, st, SZ))
+    Hd = H1.toarray()
+    S = np.zeros_like(Hd)
+    S[10:12, 10:12] = SZ
+    dt = (gs.conj() @ (1j * (Hd @ S - S @ Hd)) @ gs).real
+    assert abs(lm.currentsfromto(spin, 6) - dt) <= (1e-12 if precision == "c64" else 1e-6)
+
+
+def test_internal_density_and_evolved_currents(lm):
+    """An evolved weighted ket block: localdensity sums the internal states of a site
+    (src/operators/latticeutils.jl:44), the spin currents follow the state."""
+    H1, gs, sites, H = qwz_setup(lm)
+    X = o.random_kets(32, 4, 9)
+    w = np.array([0.1, 0.2, 0.3, 0.4])
+    st = lm.KetBlock(sites, X, weights=w)
+    s = lm.ChebyshevGPU()
+    s.update_solver(H, 0.1)
+    for _ in range(5):
+        s.step(st)
+    Y = X
+    for _ in range(5):
+        Y = o.expm_multiply(H1, 0.1, Y)
+    rho = lm.localdensity(st).values
+    assert rho.shape == (16,)
+    ref = o.localdensity(Y, w).reshape(16, 2).sum(axis=1)
+    assert np.abs(rho - ref).max() <= 1e-11
+    ent = lm.LocalOperatorCurrents(H, st, SZ).entry_values()
+    # the readout is exact in FP64; the 5 propagator steps (1e-12 each) set the tolerance
+    assert np.abs(ent - o.entry_op_currents(H1, st.to_numpy(), 2, SZ, weights=w)).max() <= 1e-14
+    ref = o.entry_op_currents(H1, Y, 2, SZ, weights=w)
+    assert np.abs(ent - ref).max() <= 1e-11 * np.abs(ref).max()
+
+
+def test_timesequence_ring_general(lm):
+    """TimeSequence(moment_currents / moment_density) over a general Hamiltonian: the ring
+    holds the per-entry currents and the site densities, equal to the synchronous calls."""
+    H1, gs, sites, H = qwz_setup(lm)
+    X = o.random_kets(32, 3, 2)
+    times = [0.1 * k for k in range(1, 12)]
+    ev = lambda: lm.Evolution(lm.ChebyshevGPU(), lambda t: H, lm.KetBlock(sites, X))
+    tc = lm.TimeSequence(lm.moment_currents, ev()(times))
+    td = lm.TimeSequence(lm.moment_density, ev()(times))
+    sync_c, sync_d = [], []
+    for m in ev()(times):
+        sync_c.append(lm.DensityCurrents(m.H, m.state).entry_values().copy())
+        sync_d.append(lm.localdensity(m.state).values)
+    assert len(tc) == len(sync_c) == len(td)
+    for (t, v), ref in zip(tc, sync_c):
+        assert np.array_equal(v, ref)
+    for (t, v), ref in zip(td, sync_d):
+        assert np.array_equal(v.values, ref)
+
+
+def test_local_operator_rejects(lm):
+    H1, gs, sites, H = qwz_setup(lm)
+    st = lm.KetBlock(sites, gs[:, None])
+    with pytest.raises(ValueError):
+        lm.LocalOperatorCurrents(H, st, np.eye(3))
+    Hh, coords = o.honeycomb_hamiltonian(3, 3)
+    hs = lm.Sites(18, coords, "honeycomb")
+    with pytest.raises(ValueError):
+        lm.LocalOperatorCurrents(lm.SparseHamiltonian(hs, Hh), lm.KetBlock(hs, o.random_kets(18, 1, 0)), np.eye(1))
