@@ -135,9 +135,9 @@ def measured_peak_hbm():
     return 6800.0, "fallback"
 
 
-def profile_traffic():
+def profile_traffic(summary: str = "cheb_fused_c32_256x256.md"):
     """DRAM bytes per launch of the dominant kernel from the committed ncu summary, if any."""
-    f = ROOT / "profiles" / "cheb_fused_c32_256x256.md"
+    f = ROOT / "profiles" / summary
     if not f.exists():
         return None
     for ln in f.read_text().splitlines():
@@ -534,6 +534,8 @@ def main():
     ap.add_argument("--precision", default="c32", choices=["c32", "c64"])
     ap.add_argument("--adjoint-init", default="eigh", choices=["eigh", "random"],
                     help="initial kets of the adjoint workload: lowest eigenstates (default) or random")
+    ap.add_argument("--fused-form", default="stream", choices=["stream", "region"],
+                    help="form of the fused c32 step: x-streaming (where the lattice allows) or region")
     ap.add_argument("--tol32", type=float, default=1e-9,
                     help="series truncation of the FP32 form (1e-9 keeps 200-step runs within 1e-6; "
                          "1e-7 is one order cheaper and enough for short runs)")
@@ -565,6 +567,7 @@ def main():
         dist.init_process_group("nccl")
 
     ctx = lmgpu.default_context()
+    ctx.set_stream_form(args.fused_form == "stream")
     ext = torch.cuda.ExternalStream(ctx.stream_ptr(), device=torch.device("cuda", local))
     lat = lmgpu.SquareLattice(LX, LY, boundaries={"axis1": True, "axis2": True})
     N, M = lat.N, args.kets
@@ -606,7 +609,9 @@ def main():
     solver32 = lmgpu.ChebyshevGPU(tol=args.tol32, renorm_every=20)
     clk = ClockSampler(local)
     clk.start()
+    n_stream0 = ctx.stream_launches()
     ms32, _, _, launches32 = timed_steps(s32, solver32, args.steps)
+    streamed = ctx.stream_launches() - n_stream0 > 0
     K32, a32, b32 = solver32.order(s32)
     # dominant kernel timing pass (events around every Chebyshev sweep, resolved lazily)
     _, order_ms, order_launches, _ = timed_steps(s32, solver32, args.steps, timing=True)
@@ -702,7 +707,12 @@ def main():
     avg_launch_ms = order_ms / sweeps
     achieved = alg_bytes_launch / (avg_launch_ms / 1000.0) / 1e9
     peak, peak_kind = measured_peak_hbm()
-    traffic = profile_traffic()
+    if streamed:
+        kname = "cheb_stream_c32_kernel (x-streaming form: all K orders of one step per launch)"
+        traffic = profile_traffic("cheb_stream_c32_256x256.md")
+    else:
+        kname = "cheb_fused_c32_kernel (region form: all K orders of one step per launch)"
+        traffic = profile_traffic()
     line = {
         "metric": METRIC, "value": value, "unit": "ket-steps/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms32 / args.steps,
@@ -720,7 +730,7 @@ def main():
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic,
                      "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
-                     "kernel": "cheb_fused_c32_kernel (all K orders of one step per launch)",
+                     "kernel": kname,
                      "alg_bytes_per_launch": alg_bytes_launch, "avg_launch_ms": avg_launch_ms,
                      "launches_timed": sweeps,
                      # the temporally blocked kernel moves ~1.8 block passes per step instead of

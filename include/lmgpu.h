@@ -71,7 +71,13 @@ int lm_ctx_stream(lm_ctx *ctx, void **stream);
  * order is at most 8 runs as one temporally blocked launch; 0 selects one launch per order
  * (same results to FP32 rounding; kept for comparison). */
 #define LM_OPT_FUSED 1
+/* LM_OPT_STREAM (default 1): a single lattice with even Ly, Lx >= 2K + 3 and K <= 6 runs the
+ * fused step in its x-streaming form (a warp walks one ket along x with a halo only in y);
+ * 0 selects the region form (a halo on both axes).  Both give bit-identical results. */
+#define LM_OPT_STREAM 2
 int lm_ctx_set_option(lm_ctx *ctx, int option, int value);
+/* Number of fused steps that ran in the x-streaming form on this context so far. */
+int lm_ctx_stream_launches(lm_ctx *ctx, int64_t *n);
 /* Opt-in CUDA-event timing of the Chebyshev-order launches (for measurement); events are
  * resolved lazily by lm_ctx_timing, so timing adds no host synchronisation per step. */
 int lm_ctx_set_timing(lm_ctx *ctx, int enable);

@@ -276,9 +276,18 @@ int lm_ctx_set_option(lm_ctx* ctx, int option, int value) {
         case LM_OPT_FUSED:
             ctx->fused = value ? 1 : 0;
             return LM_OK;
+        case LM_OPT_STREAM:
+            ctx->fused_form = value ? 1 : 0;
+            return LM_OK;
         default:
             return set_err(ctx, LM_ERR_ARG, "lm_ctx_set_option: unknown option");
     }
+}
+
+int lm_ctx_stream_launches(lm_ctx* ctx, int64_t* n) {
+    if (!ctx || !n) return LM_ERR_ARG;
+    *n = ctx->stream_launches;
+    return LM_OK;
 }
 
 int lm_ctx_set_timing(lm_ctx* ctx, int enable) {
@@ -752,6 +761,10 @@ static void free_tables(lm_solver* s) {
     if (s->d_diag2) cudaFree(s->d_diag2);
     if (s->d_hop2f) cudaFree(s->d_hop2f);
     if (s->d_diag2f) cudaFree(s->d_diag2f);
+    if (s->d_spack) cudaFree(s->d_spack);
+    s->d_spack = nullptr;
+    s->spack_f4 = 0;
+    s->spack_version = ~0ull;
     s->d_hop2 = nullptr;
     s->d_diag2 = nullptr;
     s->d_hop2f = nullptr;
@@ -801,6 +814,7 @@ int lm_solver_update(lm_solver* s, lm_ham* h, double dt, int force) {
     CUDA_TRY(ctx, launch_normalise(ctx, g, h->d_hop, h->d_onsite, s->a, s->b, s->d_hop2, s->d_diag2, s->d_hop2f,
                                    s->d_diag2f),
              "normalise kernel");
+    s->tab_version++;
     s->ell = nullptr;
     s->ham = h;
     s->ham_version = h->version;
@@ -866,8 +880,15 @@ static int cheb_apply(lm_solver* s, const Geom& g, int precision, int site_fast,
     }
     if (ctx->fused && site_fast && !conj && fused_supported(precision, K) && fused_supported_geom(g)) {
         // whole series in one temporally blocked pass; result lands in A
+        const bool xr = ham_x_real(s->ham);
+        const float4* spack = nullptr;
+        if (ctx->fused_form == 1 && stream_supported(g, K, xr, S, A, ld)) {
+            const int rc = ensure_stream_pack(s, g);
+            if (rc != LM_OK) return rc;
+            spack = s->d_spack;
+        }
         CUDA_TRY(ctx, launch_cheb_fused_c32(ctx, g, (const float2*)hop2, (const float*)diag2, (const float2*)S,
-                                            (float2*)A, ld, m, K, ham_x_real(s->ham), s->coef.data(), pr, pi),
+                                            (float2*)A, ld, m, K, xr, s->coef.data(), pr, pi, spack),
                  "fused chebyshev step");
         if (ctx->timing) {
             CUDA_TRY(ctx, cudaEventRecord(t1, ctx->stream), "cudaEventRecord");

@@ -97,6 +97,9 @@ struct lm_ctx {
     int timing = 0;
     int fused = 1;                      // LM_OPT_FUSED: temporally blocked c32 step enabled
     unsigned fused_attr = 0;            // bit K (+16 for real x-hops): shared-memory attribute set
+    unsigned stream_attr = 0;           // the same for the x-streaming form (bit K, +8 for real x-hops)
+    int fused_form = 1;                 // LM_OPT_STREAM: 1 = x-streaming form where supported, 0 = region form
+    int64_t stream_launches = 0;        // fused steps run in the x-streaming form
     std::vector<cudaEvent_t> ev_pool;   // pairs (start, stop) of timed Chebyshev sweeps
     std::vector<int> ev_launches;       // launches covered by each recorded pair
     size_t ev_used = 0;                 // pairs recorded but not yet resolved
@@ -161,6 +164,11 @@ struct lm_solver {
     double2* d_hop2 = nullptr;  double* d_diag2 = nullptr;
     float2* d_hop2f = nullptr;  float* d_diag2f = nullptr;
     int64_t tab_n = 0;
+    uint64_t tab_version = 0;    // bumped whenever the tables are rewritten
+    // x-streaming form: padded, packed FP32 coefficient planes (lmgpu_stream.cu)
+    float4* d_spack = nullptr;
+    size_t spack_f4 = 0;
+    uint64_t spack_version = ~0ull;
     int has_onsite = 0;
     int fixed_bounds = 0;        // lm_solver_set_bounds: use [fix_emin, fix_emax] instead of Gershgorin
     double fix_emin = 0.0, fix_emax = 0.0;
@@ -241,9 +249,14 @@ void fused_fill_coef(FusedInst& d, int K, const ChebCoef* coef, double ph_re, do
 cudaError_t launch_fused_table(lm_ctx* ctx, int K, bool xreal, const FusedInst* single, const FusedInst* d_table,
                                int ninst, int64_t nitems, unsigned long long* d_queue, int grid);
 cudaError_t ensure_fused_attr(lm_ctx* ctx, int K, bool xreal);
+// x-streaming form of the single-lattice c32 step (lmgpu_stream.cu): its preconditions, its
+// packed coefficient planes (rebuilt from the FP32 tables when they change) and the launch.
+bool stream_supported(const Geom& g, int K, bool xreal, const void* x, const void* out, int64_t ld);
+int ensure_stream_pack(lm_solver* s, const Geom& g);
+cudaError_t launch_cheb_stream_c32(lm_ctx* ctx, const FusedInst& d, int K, bool xreal, const float4* spack);
 cudaError_t launch_cheb_fused_c32(lm_ctx* ctx, const Geom& g, const float2* hop2, const float* diag2,
                                   const float2* x, float2* out, int64_t ld, int64_t m, int K, bool xreal,
-                                  const ChebCoef* coef, double ph_re, double ph_im);
+                                  const ChebCoef* coef, double ph_re, double ph_im, const float4* spack = nullptr);
 // Every x-hop of H is real: Landau-gauge field components only (or none) and no twist across
 // a periodic x axis.  The fused kernel then skips the imaginary parts of the x-hops.
 bool ham_x_real(const lm_ham* h);

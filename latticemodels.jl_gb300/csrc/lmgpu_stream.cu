@@ -1,0 +1,496 @@
+// x-streaming form of the temporally blocked Chebyshev step (ComplexF32 recurrence) for one
+// square lattice: y = e^{-ib dt} sum_{k<=K} c_k T_k(H~) x applied to a column-major ket block.
+//
+// A warp owns one ket and one strip of 64 sites along y (lane l holds the site pair
+// 2l, 2l+1) and walks along x.  At step s it loads column s of the ket (order 0) and advances
+// every order k = 1..K by one column, order k working on column s - k: T_k(x) needs
+// T_{k-1} at x-1, x, x+1 and T_{k-2} at x, and order k-1 produced column x+1 earlier in the
+// same step.  So each order keeps the last three columns of its T in registers (a rotation
+// of period three), the y-neighbours come from the adjacent lanes by shuffles,
+// and the accumulator y(x) = sum_k c_k T_k(x) waits in a per-warp shared-memory ring of
+// K+1 columns until order K completes it.  Column s + 3 of the ket is staged into a second
+// ring by cp.async while column s is being used.
+//
+// Only the y direction has a halo: after K orders the sites K .. 63-K of a strip are exact
+// (at an open lattice edge the strip sits on the edge and writes up to it), while along x a
+// range [xa, xb) of columns costs (xb - xa) + 2K steps.  Every warp takes an equal share of
+// all the (strip, ket, column) work, so the only redundancy along x is 2K steps per item a
+// warp starts or finishes.  The region form (32 x 64 sites
+// with a halo on both axes) computes about twice the sites it writes at K = 6; this form
+// computes about 1.25 times.  Each site-order uses the same sequence of FMAs as the region
+// form, so the two give bit-identical results.
+//
+// Requirements (checked by stream_supported): Ly even, so every lane's pair is a 16-byte
+// aligned, unsplit pair of sites; Lx >= 2K + 3, so a column index leaves [0, Lx) by less
+// than one lattice length; K <= 6 with real x-hops, K <= 5 otherwise (the register budget of
+// the three-column windows).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdint>
+
+#include "lmgpu_internal.cuh"
+
+namespace lmgpu {
+
+// Warps per CTA (one ket each); 16 caps a thread at 128 registers, 12 at 170.
+#ifndef LM_STREAM_WARPS
+#define LM_STREAM_WARPS 16
+#endif
+// 1: the three-column windows rotate by register moves at the end of every step; 0: the
+// step loop is unrolled three times and the rotation is renaming (more code in flight).
+#ifndef LM_STREAM_ROTATE
+#define LM_STREAM_ROTATE 1
+#endif
+
+namespace {
+constexpr int SW = LM_STREAM_WARPS;
+constexpr int SR = 64;       // strip width along y: 32 lanes x 2 sites
+constexpr int SPF = 3;       // columns of the ket staged ahead
+constexpr int kStreamMaxK = 6;
+// Packed coefficient planes: padded columns x = -kPadL .. Lx + kPadR - 1 (periodic columns
+// wrapped, open ones zero), one float4 per (column, site pair) and plane, plus one zero pair
+// at the end of every plane for lanes outside the lattice.
+constexpr int kPadL = 2 * kStreamMaxK + 2;
+constexpr int kPadR = kStreamMaxK;
+constexpr int kPlanes = 5;
+// plane 0: real parts {hx0, hx1, hxm0, hxm1} (real x-hops); 1: {hx0, hx1}; 2: {hxm0, hxm1};
+// 3: {hy0, hy1}; 4: {hym0, d0, d1}.  hx: hop to x+1; hxm: conj of the hop from x-1 to x;
+// hy: hop to y+1; hym0: conj of the hop from y-1 to the first site; d: diagonal.
+
+__host__ __device__ constexpr int stream_halo(int K) { return K + (K & 1); }  // even: pairs stay aligned
+__host__ __device__ constexpr int stream_ring_f4(int K) { return ((K + 1) + (K + 1 + SPF)) * 32; }
+
+__device__ __forceinline__ void cp_async16(float4* dst_smem, const void* src, bool valid) {
+    const unsigned dst = (unsigned)__cvta_generic_to_shared(dst_smem);
+    const int n = valid ? 16 : 0;  // n = 0 fills the 16 bytes with zeros
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(dst), "l"(src), "r"(n));
+}
+__device__ __forceinline__ void cp_async_commit_s() { asm volatile("cp.async.commit_group;\n" ::); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait_s() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+__device__ __forceinline__ int wrap_axis_i(int64_t c, int64_t L, int per) {
+    if (c >= 0 && c < L) return (int)c;
+    if (!per) return -1;
+    c %= L;
+    return (int)(c < 0 ? c + L : c);
+}
+
+// Tiling of the y axis into strips of SR sites with halo H (the same rule as the region form).
+__host__ __device__ __forceinline__ int64_t strip_count(int64_t L, int per, int H) {
+    const int64_t I = SR - 2 * H;
+    if (per) return (L + I - 1) / I;
+    if (L <= SR) return 1;
+    const int64_t rest = L - 2 * (int64_t)(SR - H);
+    return 2 + (rest > 0 ? (rest + I - 1) / I : 0);
+}
+__device__ __forceinline__ void strip_range(int64_t L, int per, int H, int64_t t, int64_t n, int64_t* origin,
+                                            int64_t* w0, int64_t* w1) {
+    const int64_t I = SR - 2 * H;
+    if (per) {
+        *w0 = t * I;
+        *w1 = *w0 + I < L ? *w0 + I : L;
+        *origin = *w0 - H;
+    } else if (n == 1) {
+        *origin = 0; *w0 = 0; *w1 = L;
+    } else if (t == 0) {
+        *origin = 0; *w0 = 0; *w1 = SR - H;
+    } else {
+        *w0 = (SR - H) + (t - 1) * I;
+        if (t == n - 1) {
+            *origin = L - SR;
+            *w1 = L;
+        } else {
+            *origin = *w0 - H;
+            *w1 = *w0 + I;
+        }
+    }
+}
+}  // namespace
+
+__device__ __forceinline__ int wrap_mod(int64_t c, int64_t L) {
+    c %= L;
+    return (int)(c < 0 ? c + L : c);
+}
+
+__global__ void stream_pack_kernel(const Geom g, const float2* __restrict__ hop2, const float* __restrict__ diag2,
+                                   float4* __restrict__ pk, int npair, int Xp, long long plane) {
+    const long long n = (long long)Xp * npair + 1;
+    const float2 z = make_float2(0.f, 0.f);
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        float2 hx[2] = {z, z}, hxm[2] = {z, z}, hy[2] = {z, z}, hym0 = z;
+        float d[2] = {0.f, 0.f};
+        if (i < n - 1) {
+            const int xp = (int)(i / npair), yp = (int)(i % npair);
+            const int64_t x = (int64_t)xp - kPadL;
+            const int xs = g.per_x ? wrap_mod(x, g.Lx) : ((x >= 0 && x < g.Lx) ? (int)x : -1);
+            if (xs >= 0) {
+                const int y0 = 2 * yp;
+                const int xsm = g.per_x ? wrap_mod((int64_t)xs - 1, g.Lx) : xs - 1;
+                const int ysm = g.per_y ? wrap_mod((int64_t)y0 - 1, g.Ly) : y0 - 1;
+                const float2* hopy = hop2 + g.N;
+                for (int j = 0; j < 2; ++j) {
+                    const int64_t site = (int64_t)xs * g.Ly + y0 + j;
+                    hx[j] = hop2[site];
+                    hy[j] = hopy[site];
+                    d[j] = diag2[site];
+                    if (xsm >= 0) {
+                        const float2 h = hop2[(int64_t)xsm * g.Ly + y0 + j];
+                        hxm[j] = make_float2(h.x, -h.y);
+                    }
+                }
+                if (ysm >= 0) {
+                    const float2 h = hopy[(int64_t)xs * g.Ly + ysm];
+                    hym0 = make_float2(h.x, -h.y);
+                }
+            }
+        }
+        pk[i] = make_float4(hx[0].x, hx[1].x, hxm[0].x, hxm[1].x);
+        pk[plane + i] = make_float4(hx[0].x, hx[0].y, hx[1].x, hx[1].y);
+        pk[2 * plane + i] = make_float4(hxm[0].x, hxm[0].y, hxm[1].x, hxm[1].y);
+        pk[3 * plane + i] = make_float4(hy[0].x, hy[0].y, hy[1].x, hy[1].y);
+        pk[4 * plane + i] = make_float4(hym0.x, hym0.y, d[0], d[1]);
+    }
+}
+
+template <int K, bool XR>
+__global__ void __launch_bounds__(SW * 32, 1)
+cheb_stream_c32_kernel(const FusedInst D, const float4* __restrict__ pk, int npair, long long plane, int nty,
+                       long long ncols, long long nwarps) {
+    constexpr int H = stream_halo(K);
+    constexpr int YR = K + 1;          // accumulator ring: columns x .. x+K in flight
+    constexpr int XS = K + 1 + SPF;    // ket ring: column s+SPF staged, column s-K still read
+    constexpr bool ROT = LM_STREAM_ROTATE != 0;
+    constexpr int NP = ROT ? 1 : 3;    // steps per unrolled loop body
+    extern __shared__ float4 smem[];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    float4* yring = smem + warp * stream_ring_f4(K);
+    float4* xring = yring + YR * 32;
+    const Geom g = D.g;
+    const int Lx = (int)g.Lx, Ly = (int)g.Ly;
+    const int per_x = g.per_x;
+    const float4* __restrict__ P0 = pk;
+    const float4* __restrict__ P1 = pk + plane;
+    const float4* __restrict__ P2 = pk + 2 * plane;
+    const float4* __restrict__ P3 = pk + 3 * plane;
+    const float4* __restrict__ P4 = pk + 4 * plane;
+
+    // Work: the columns of every (strip, ket) item, items in the order strip-major, ket-minor;
+    // warp w takes the contiguous share [w ncols / nwarps, (w+1) ncols / nwarps) of them, i.e.
+    // column ranges [xa, xb) of one or more consecutive items.
+    const long long w = (long long)blockIdx.x * SW + warp;
+    if (w >= nwarps) return;
+    const long long c_end = (w + 1) * ncols / nwarps;  // ncols * nwarps < 2^63
+    for (long long c = w * ncols / nwarps; c < c_end;) {
+        const long long item = c / Lx;
+        const int xa = (int)(c - item * Lx);
+        const long long rest = c_end - c;
+        const int xb = rest < (long long)(Lx - xa) ? xa + (int)rest : Lx;
+        c += xb - xa;
+        const long long ket = item % D.M;
+        const long long tile = item / D.M;
+        const int strip = (int)tile;
+        int64_t origin, w0, w1;
+        strip_range(g.Ly, g.per_y, H, strip, nty, &origin, &w0, &w1);
+        const int gy = (int)origin + 2 * lane;
+        const int ys = wrap_axis_i(gy, g.Ly, g.per_y);       // my pair (ys, ys+1), or -1 outside
+        const bool wr = ys >= 0 && gy >= w0 && gy < w1;
+        // my coefficient records: column x at offset loff + (x + kPadL) * lstep of every plane;
+        // the zero pair outside the lattice
+        const int loff = ys >= 0 ? ys / 2 : (int)(plane - 1);
+        const int lstep = ys >= 0 ? npair : 0;
+        const int n0 = xb - xa + 2 * K;
+        const int nsteps = n0 + (NP - n0 % NP) % NP;
+        const int s0 = xb + K - nsteps;  // xa - K, moved back so that nsteps is a multiple of NP
+        const float2* xk = D.x + ket * D.ld;
+        float2* outk = D.out + ket * D.ld;
+
+        auto column = [&](int x) -> int {  // lattice column of x, or -1 outside an open axis
+            if (per_x) return x < 0 ? x + Lx : (x >= Lx ? x - Lx : x);
+            return (x >= 0 && x < Lx) ? x : -1;
+        };
+        int stage_slot = 0;  // ring slot of the next staged column
+        auto stage = [&](int idx) {
+            const int xs = column(s0 + idx);
+            const bool v = idx < nsteps && xs >= 0 && ys >= 0;
+            const float2* src = v ? xk + (long long)xs * Ly + ys : xk;
+            cp_async16(&xring[stage_slot * 32 + lane], src, v);
+            cp_async_commit_s();
+            stage_slot = stage_slot + 1 == XS ? 0 : stage_slot + 1;
+        };
+#pragma unroll
+        for (int i = 0; i < SPF; ++i) stage(i);
+
+        // T_j of my sites, three columns per order 1 <= j < K (slot = producing step mod 3);
+        // T_0 is read from the ket ring instead (W[0] stays unused)
+        float2 W[K][3][2];
+#pragma unroll
+        for (int j = 1; j < K; ++j)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) W[j][c][0] = W[j][c][1] = make_float2(0.f, 0.f);
+
+        int xslot = 0;  // idx mod XS
+        int yslot = 0;  // idx mod YR
+        for (int base = 0; base < nsteps; base += NP) {
+#pragma unroll
+            for (int p = 0; p < NP; ++p) {
+                // window slots of the columns produced at this step, one and two steps ago
+                const int c0 = ROT ? 0 : p, c1 = ROT ? 1 : (p + 2) % 3, c2 = ROT ? 2 : (p + 1) % 3;
+                const int idx = base + p;
+                const int s = s0 + idx;
+                stage(idx + SPF);
+                cp_async_wait_s<SPF>();  // the group of column idx has landed
+                // ket ring slots of columns s-1 and s-2 (T_0 of order 1's x and x-1)
+                const int xs1 = xslot == 0 ? XS - 1 : xslot - 1;
+                const int xs2 = xs1 == 0 ? XS - 1 : xs1 - 1;
+                const int ro = loff + (s + kPadL) * lstep;  // records of column s
+#pragma unroll
+                for (int k = 1; k <= K; ++k) {
+                    const int x = s - k;
+                    const int o = ro - k * lstep;
+                    float2 hx[2], hxm[2], hy[2], hym[2];
+                    float d[2];
+                    if (o >= 0) {
+                        const float4 qy = __ldg(P3 + o), qd = __ldg(P4 + o);
+                        hy[0] = make_float2(qy.x, qy.y);
+                        hy[1] = make_float2(qy.z, qy.w);
+                        hym[0] = make_float2(qd.x, qd.y);
+                        hym[1] = make_float2(hy[0].x, -hy[0].y);
+                        d[0] = qd.z;
+                        d[1] = qd.w;
+                        if (XR) {
+                            const float4 q = __ldg(P0 + o);
+                            hx[0] = make_float2(q.x, 0.f);
+                            hx[1] = make_float2(q.y, 0.f);
+                            hxm[0] = make_float2(q.z, 0.f);
+                            hxm[1] = make_float2(q.w, 0.f);
+                        } else {
+                            const float4 q = __ldg(P1 + o), r = __ldg(P2 + o);
+                            hx[0] = make_float2(q.x, q.y);
+                            hx[1] = make_float2(q.z, q.w);
+                            hxm[0] = make_float2(r.x, r.y);
+                            hxm[1] = make_float2(r.z, r.w);
+                        }
+                    } else {
+                        hx[0] = hx[1] = hxm[0] = hxm[1] = hy[0] = hy[1] = hym[0] = hym[1] = make_float2(0.f, 0.f);
+                        d[0] = d[1] = 0.f;
+                    }
+
+                    // T_{k-1} at x+1 (this step), x and x-1
+                    float2 tp[2], tc[2], tm[2];
+                    if (k == 1) {
+                        const float4 a = xring[xslot * 32 + lane], b = xring[xs1 * 32 + lane], c = xring[xs2 * 32 + lane];
+                        tp[0] = make_float2(a.x, a.y); tp[1] = make_float2(a.z, a.w);
+                        tc[0] = make_float2(b.x, b.y); tc[1] = make_float2(b.z, b.w);
+                        tm[0] = make_float2(c.x, c.y); tm[1] = make_float2(c.z, c.w);
+                    } else {
+                        tp[0] = W[k - 1][c0][0]; tp[1] = W[k - 1][c0][1];
+                        tc[0] = W[k - 1][c1][0]; tc[1] = W[k - 1][c1][1];
+                        tm[0] = W[k - 1][c2][0]; tm[1] = W[k - 1][c2][1];
+                    }
+                    float2 up, dn;  // y-1 of my first site, y+1 of my second
+                    up.x = __shfl_up_sync(0xffffffffu, tc[1].x, 1);
+                    up.y = __shfl_up_sync(0xffffffffu, tc[1].y, 1);
+                    dn.x = __shfl_down_sync(0xffffffffu, tc[0].x, 1);
+                    dn.y = __shfl_down_sync(0xffffffffu, tc[0].y, 1);
+                    const float2 vyp[2] = {tc[1], dn};
+                    const float2 vym[2] = {up, tc[0]};
+
+                    float2 tk[2];
+#pragma unroll
+                    for (int j = 0; j < 2; ++j) {
+                        float2 acc = make_float2(0.f, 0.f);
+                        if (k == 2) {  // T_0(x) = column s-2 of the ket ring
+                            const float4 q = xring[xs2 * 32 + lane];
+                            const float2 t2 = j == 0 ? make_float2(q.x, q.y) : make_float2(q.z, q.w);
+                            acc = make_float2(-t2.x, -t2.y);
+                        } else if (k > 2) {
+                            const float2 t2 = W[k - 2][c2][j];  // T_{k-2}(x)
+                            acc = make_float2(-t2.x, -t2.y);
+                        }
+                        const float2 vxp = tp[j], vxm = tm[j];
+                        if (XR) {
+                            acc.x = fmaf(hx[j].x, vxp.x, acc.x);
+                            acc.y = fmaf(hx[j].x, vxp.y, acc.y);
+                            acc.x = fmaf(hxm[j].x, vxm.x, acc.x);
+                            acc.y = fmaf(hxm[j].x, vxm.y, acc.y);
+                        } else {
+                            acc.x = fmaf(hx[j].x, vxp.x, acc.x); acc.x = fmaf(-hx[j].y, vxp.y, acc.x);
+                            acc.y = fmaf(hx[j].x, vxp.y, acc.y); acc.y = fmaf(hx[j].y, vxp.x, acc.y);
+                            acc.x = fmaf(hxm[j].x, vxm.x, acc.x); acc.x = fmaf(-hxm[j].y, vxm.y, acc.x);
+                            acc.y = fmaf(hxm[j].x, vxm.y, acc.y); acc.y = fmaf(hxm[j].y, vxm.x, acc.y);
+                        }
+                        acc.x = fmaf(hy[j].x, vyp[j].x, acc.x); acc.x = fmaf(-hy[j].y, vyp[j].y, acc.x);
+                        acc.y = fmaf(hy[j].x, vyp[j].y, acc.y); acc.y = fmaf(hy[j].y, vyp[j].x, acc.y);
+                        acc.x = fmaf(hym[j].x, vym[j].x, acc.x); acc.x = fmaf(-hym[j].y, vym[j].y, acc.x);
+                        acc.y = fmaf(hym[j].x, vym[j].y, acc.y); acc.y = fmaf(hym[j].y, vym[j].x, acc.y);
+                        acc.x = fmaf(d[j], tc[j].x, acc.x);
+                        acc.y = fmaf(d[j], tc[j].y, acc.y);
+                        if (k == 1) { acc.x *= 0.5f; acc.y *= 0.5f; }  // tables hold 2H/a
+                        tk[j] = acc;
+                    }
+                    if (k < K) {
+                        W[k][c0][0] = tk[0];
+                        W[k][c0][1] = tk[1];
+                    }
+
+                    // accumulator of column x
+                    int ys_k = yslot - k;
+                    if (ys_k < 0) ys_k += YR;
+                    float4* yr = &yring[ys_k * 32 + lane];
+                    const float sk = D.s[k];
+                    float2 yv[2];
+                    if (k == 1) {  // y = -i s_1 T1 + g0 T0 + g1 T1
+                        const ChebLo lo = D.lo;
+#pragma unroll
+                        for (int j = 0; j < 2; ++j) {
+                            const float2 x0 = tc[j], t = tk[j];
+                            const float lx = fmaf(lo.g0_re, x0.x, fmaf(-lo.g0_im, x0.y, fmaf(lo.g1_re, t.x, -lo.g1_im * t.y)));
+                            const float ly = fmaf(lo.g0_re, x0.y, fmaf(lo.g0_im, x0.x, fmaf(lo.g1_re, t.y, lo.g1_im * t.x)));
+                            yv[j].x = fmaf(sk, t.y, lx);
+                            yv[j].y = fmaf(-sk, t.x, ly);
+                        }
+                    } else {
+                        const float4 q = *yr;
+                        yv[0] = make_float2(q.x, q.y);
+                        yv[1] = make_float2(q.z, q.w);
+#pragma unroll
+                        for (int j = 0; j < 2; ++j) {
+                            const float2 t = tk[j];
+                            if (k & 1) {  // c_k = -i s_k
+                                yv[j].x = fmaf(sk, t.y, yv[j].x);
+                                yv[j].y = fmaf(-sk, t.x, yv[j].y);
+                            } else {      // c_k = s_k
+                                yv[j].x = fmaf(sk, t.x, yv[j].x);
+                                yv[j].y = fmaf(sk, t.y, yv[j].y);
+                            }
+                        }
+                    }
+                    if (k < K) {
+                        *yr = make_float4(yv[0].x, yv[0].y, yv[1].x, yv[1].y);
+                    } else if (wr && x >= xa && x < xb) {
+                        const int xs = column(x);
+                        // out = e^{-ib dt} y + a0 x (a0 = e^{-ib dt} c_0): the small terms first
+                        int xo = xslot - K;
+                        if (xo < 0) xo += XS;
+                        const float4 q = xring[xo * 32 + lane];
+                        const float2 x0[2] = {make_float2(q.x, q.y), make_float2(q.z, q.w)};
+                        const float ph_re = D.ph_re, ph_im = D.ph_im, a0_re = D.a0_re, a0_im = D.a0_im;
+                        float2 o[2];
+#pragma unroll
+                        for (int j = 0; j < 2; ++j) {
+                            float2 r;
+                            r.x = fmaf(ph_re, yv[j].x, -ph_im * yv[j].y);
+                            r.y = fmaf(ph_re, yv[j].y, ph_im * yv[j].x);
+                            r.x = fmaf(-a0_im, x0[j].y, r.x);
+                            r.y = fmaf(a0_im, x0[j].x, r.y);
+                            o[j].x = fmaf(a0_re, x0[j].x, r.x);
+                            o[j].y = fmaf(a0_re, x0[j].y, r.y);
+                        }
+                        *reinterpret_cast<float4*>(outk + (long long)xs * Ly + ys) = make_float4(o[0].x, o[0].y, o[1].x, o[1].y);
+                    }
+                }
+                xslot = xslot + 1 == XS ? 0 : xslot + 1;
+                yslot = yslot + 1 == YR ? 0 : yslot + 1;
+                if (ROT) {
+#pragma unroll
+                    for (int j = 1; j < K; ++j) {
+                        W[j][2][0] = W[j][1][0]; W[j][2][1] = W[j][1][1];
+                        W[j][1][0] = W[j][0][0]; W[j][1][1] = W[j][0][1];
+                    }
+                }
+            }
+        }
+        cp_async_wait_s<0>();
+        __syncwarp();  // the next item reuses this warp's rings
+    }
+}
+
+bool stream_supported(const Geom& g, int K, bool xreal, const void* x, const void* out, int64_t ld) {
+    return K >= 2 && K <= (xreal ? kStreamMaxK : kStreamMaxK - 1) && g.Ly % 2 == 0 && g.Lx >= 2 * K + 3 && g.N < ((int64_t)1 << 31) &&
+           ld % 2 == 0 && ((uintptr_t)x & 15) == 0 && ((uintptr_t)out & 15) == 0;
+}
+
+static void pack_dims(const Geom& g, int* npair, int* Xp, long long* plane) {
+    *npair = (int)(g.Ly / 2);
+    *Xp = (int)g.Lx + kPadL + kPadR;
+    *plane = (long long)(*Xp) * (*npair) + 1;
+}
+
+int ensure_stream_pack(lm_solver* s, const Geom& g) {
+    lm_ctx* ctx = s->ctx;
+    int npair, Xp;
+    long long plane;
+    pack_dims(g, &npair, &Xp, &plane);
+    const size_t need = (size_t)kPlanes * (size_t)plane;
+    if (s->spack_f4 != need) {
+        if (s->d_spack) cudaFree(s->d_spack);
+        s->d_spack = nullptr;
+        s->spack_f4 = 0;
+        s->spack_version = ~0ull;
+        const cudaError_t e = cudaMalloc((void**)&s->d_spack, sizeof(float4) * need);
+        if (e != cudaSuccess) {
+            s->d_spack = nullptr;
+            cudaGetLastError();
+            return set_err(ctx, LM_ERR_OOM, "x-streaming coefficient planes: out of device memory");
+        }
+        s->spack_f4 = need;
+    }
+    if (s->spack_version == s->tab_version) return LM_OK;
+    const long long n = plane;
+    const unsigned grid = (unsigned)std::min<long long>((n + 255) / 256, 4096);
+    stream_pack_kernel<<<grid, 256, 0, ctx->stream>>>(g, s->d_hop2f, s->d_diag2f, s->d_spack, npair, Xp, plane);
+    ctx->launches++;
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return check_cuda(ctx, e, "x-streaming coefficient planes");
+    s->spack_version = s->tab_version;
+    return LM_OK;
+}
+
+template <bool XR>
+static cudaError_t launch_stream_k(lm_ctx* ctx, int K, int grid, const FusedInst& d, const float4* pk, int nty,
+                                   long long ncols, long long nwarps) {
+    int npair, Xp;
+    long long plane;
+    pack_dims(d.g, &npair, &Xp, &plane);
+    const unsigned bit = 1u << (K + (XR ? 8 : 0));
+    switch (K) {
+#define LM_STREAM_CASE(KK)                                                                                       \
+    case KK: {                                                                                                   \
+        const int smem = SW * stream_ring_f4(KK) * 16;                                                           \
+        if (!(ctx->stream_attr & bit)) {                                                                         \
+            cudaError_t e = cudaFuncSetAttribute(cheb_stream_c32_kernel<KK, XR>,                                 \
+                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, smem);             \
+            if (e != cudaSuccess) return e;                                                                      \
+            ctx->stream_attr |= bit;                                                                             \
+        }                                                                                                        \
+        cheb_stream_c32_kernel<KK, XR><<<(unsigned)grid, SW * 32, smem, ctx->stream>>>(d, pk, npair, plane,     \
+                                                                                         nty, ncols, nwarps);    \
+        return cudaGetLastError();                                                                               \
+    }
+        LM_STREAM_CASE(2) LM_STREAM_CASE(3) LM_STREAM_CASE(4) LM_STREAM_CASE(5) LM_STREAM_CASE(6)
+#undef LM_STREAM_CASE
+        default:
+            return cudaErrorInvalidValue;
+    }
+}
+
+cudaError_t launch_cheb_stream_c32(lm_ctx* ctx, const FusedInst& d, int K, bool xreal, const float4* spack) {
+    const int H = stream_halo(K);
+    const int64_t nty = strip_count(d.g.Ly, d.g.per_y, H);
+    const long long ncols = (long long)nty * d.M * d.g.Lx;
+    if (ncols <= 0) return cudaSuccess;
+    // one warp per SM slot, but at least 8K columns per warp (a share costs 2K extra steps
+    // for every item it touches)
+    const long long slots = (long long)(ctx->sm_count > 0 ? ctx->sm_count : 152) * SW;
+    const long long nwarps = std::max<long long>(1, std::min<long long>(slots, ncols / (8 * K)));
+    const int grid = (int)((nwarps + SW - 1) / SW);
+    const cudaError_t e = xreal ? launch_stream_k<true>(ctx, K, grid, d, spack, (int)nty, ncols, nwarps)
+                                : launch_stream_k<false>(ctx, K, grid, d, spack, (int)nty, ncols, nwarps);
+    ctx->launches++;
+    ctx->stream_launches++;
+    return e;
+}
+
+}  // namespace lmgpu

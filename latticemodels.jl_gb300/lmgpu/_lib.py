@@ -25,6 +25,7 @@ ERR_NAMES = {1: "bad argument", 2: "out of device memory", 3: "CUDA error", 4: "
 
 LM_C64, LM_C32 = 0, 1
 LM_OPT_FUSED = 1
+LM_OPT_STREAM = 2
 LM_KETS, LM_DENSITY = 0, 1
 LM_FIELD_LANDAU, LM_FIELD_SYMMETRIC, LM_FIELD_POINTFLUX_AXIAL, LM_FIELD_POINTFLUX_SINGULAR = 1, 2, 3, 4
 
@@ -47,6 +48,7 @@ SIGNATURES = {
     "lm_ctx_synchronize": (_INT, [_P]),
     "lm_ctx_stream": (_INT, [_P, C.POINTER(_P)]),
     "lm_ctx_set_option": (_INT, [_P, _INT, _INT]),
+    "lm_ctx_stream_launches": (_INT, [_P, _PI64]),
     "lm_ctx_set_timing": (_INT, [_P, _INT]),
     "lm_ctx_timing": (_INT, [_P, _PD, _PI64, _PI64]),
     "lm_ctx_reset_timing": (_INT, [_P]),

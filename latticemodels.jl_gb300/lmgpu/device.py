@@ -30,6 +30,17 @@ class Context:
         """Temporally blocked c32 step (default on) or one launch per Chebyshev order."""
         self.check(self.lib.lm_ctx_set_option(self.handle, _lib.LM_OPT_FUSED, 1 if on else 0))
 
+    def set_stream_form(self, on: bool):
+        """x-streaming form of the fused step where the lattice allows it (default on), or the
+        region form; both give bit-identical results."""
+        self.check(self.lib.lm_ctx_set_option(self.handle, _lib.LM_OPT_STREAM, 1 if on else 0))
+
+    def stream_launches(self) -> int:
+        """Fused steps that ran in the x-streaming form so far."""
+        n = C.c_int64()
+        self.check(self.lib.lm_ctx_stream_launches(self.handle, C.byref(n)))
+        return n.value
+
     def set_timing(self, on: bool):
         self.check(self.lib.lm_ctx_set_timing(self.handle, 1 if on else 0))
 

@@ -389,3 +389,60 @@ def test_fused_twisted_boundaries(lm, tw):
     Y = o.expm_multiply(Ho, 0.07, o.expm_multiply(Ho, 0.07, X))
     assert rel(outs[True], Y) <= 2e-6
     assert rel(outs[True], outs[False]) <= 2e-6
+
+
+STREAM_CASES = [
+    # (Lx, Ly, periodic x, periodic y, field, dt, kets): K from the FP32 default tolerance
+    (64, 64, True, True, "landau", 0.05, 24),     # K = 6, real x-hops, 2 strips
+    (256, 256, True, True, "landau", 0.05, 5),    # the benchmark lattice, 5 strips, 2 x segments
+    (47, 130, False, False, "landau", 0.05, 9),   # open, uneven edge strips
+    (40, 70, True, False, "pointflux", 0.03, 7),  # complex x-hops (K <= 5)
+    (33, 64, False, True, "pointflux", 0.03, 3),
+    (20, 200, True, True, "landau", 0.05, 1),     # one ket, many strips
+    (64, 31, True, True, "landau", 0.05, 4),      # odd Ly: region form only
+    (12, 64, True, True, "landau", 0.05, 4),      # Lx < 2K + 3: region form only
+]
+
+
+@pytest.mark.parametrize("case", STREAM_CASES, ids=[f"{c[0]}x{c[1]}-{c[4]}-M{c[6]}" for c in STREAM_CASES])
+def test_stream_form_bit_identical_to_region(lm, case):
+    """The x-streaming form of the fused step performs every site-order with the same FMAs as
+    the region form, so three steps agree bit for bit; both against the exact exponent."""
+    Lx, Ly, px, py, fk, dt, M = case
+    ol, ll = pair(lm, Lx, Ly, (px, py))
+    V = o.anderson_disorder(ol.N, 1.0, 41)
+    if fk == "landau":
+        fo, fl = o.LandauGauge(0.02), lm.LandauGauge(0.02)
+    else:
+        pt = (Lx / 2 + 0.5, Ly / 2 + 0.5)
+        fo, fl = o.PointFlux(0.3, pt), lm.PointFlux(0.3, pt)
+    Ho = o.tightbinding_hamiltonian(ol, field=fo, onsite=V)
+    Hl = lm.tightbinding_hamiltonian(ll, V, field=fl)
+    X = o.random_kets(ol.N, M, 42)
+    ctx = lm.default_context()
+    outs = {}
+    eligible = Ly % 2 == 0
+    try:
+        for form in (True, False):
+            ctx.set_stream_form(form)
+            st = lm.KetBlock(ll, X, precision="c32")
+            s = lm.ChebyshevGPU()
+            s.update_solver(Hl, dt)
+            n0 = ctx.stream_launches()
+            for _ in range(3):
+                s.step(st)
+            ran = ctx.stream_launches() - n0
+            if form:
+                K = s.order(st)[0]
+                expect = eligible and Lx >= 2 * K + 3 and K <= (6 if fk == "landau" else 5)
+                assert ran == (3 if expect else 0)
+            else:
+                assert ran == 0
+            outs[form] = st.to_numpy()
+    finally:
+        ctx.set_stream_form(True)
+    assert np.array_equal(outs[True], outs[False])
+    Y = X
+    for _ in range(3):
+        Y = o.expm_multiply(Ho, dt, Y)
+    assert rel(outs[True].astype(np.complex128), Y) <= 3e-6
