@@ -151,6 +151,10 @@ bool ham_x_real(const lm_ham* h) {
     return true;
 }
 
+bool ham_uniform_columns(const lm_ham* h) {
+    return ham_x_real(h) && !(h->lat->g.per_y && h->lat->g.twist_y != 0.0);
+}
+
 ChebLo cheb_lo(double ph_re, double ph_im, double c0, double s1, bool fused) {
     typedef std::complex<double> cd;
     const cd ph(ph_re, ph_im);
@@ -881,14 +885,15 @@ static int cheb_apply(lm_solver* s, const Geom& g, int precision, int site_fast,
     if (ctx->fused && site_fast && !conj && fused_supported(precision, K) && fused_supported_geom(g)) {
         // whole series in one temporally blocked pass; result lands in A
         const bool xr = ham_x_real(s->ham);
+        const int mode = ham_uniform_columns(s->ham) ? 2 : (xr ? 1 : 0);
         const float4* spack = nullptr;
-        if (ctx->fused_form == 1 && stream_supported(g, K, xr, S, A, ld)) {
+        if (ctx->fused_form == 1 && stream_supported(g, K, mode, S, A, ld)) {
             const int rc = ensure_stream_pack(s, g);
             if (rc != LM_OK) return rc;
             spack = s->d_spack;
         }
         CUDA_TRY(ctx, launch_cheb_fused_c32(ctx, g, (const float2*)hop2, (const float*)diag2, (const float2*)S,
-                                            (float2*)A, ld, m, K, xr, s->coef.data(), pr, pi, spack),
+                                            (float2*)A, ld, m, K, xr, s->coef.data(), pr, pi, spack, mode),
                  "fused chebyshev step");
         if (ctx->timing) {
             CUDA_TRY(ctx, cudaEventRecord(t1, ctx->stream), "cudaEventRecord");

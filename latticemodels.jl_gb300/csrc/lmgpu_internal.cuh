@@ -251,15 +251,19 @@ cudaError_t launch_fused_table(lm_ctx* ctx, int K, bool xreal, const FusedInst* 
 cudaError_t ensure_fused_attr(lm_ctx* ctx, int K, bool xreal);
 // x-streaming form of the single-lattice c32 step (lmgpu_stream.cu): its preconditions, its
 // packed coefficient planes (rebuilt from the FP32 tables when they change) and the launch.
-bool stream_supported(const Geom& g, int K, bool xreal, const void* x, const void* out, int64_t ld);
+bool stream_supported(const Geom& g, int K, int mode, const void* x, const void* out, int64_t ld);
 int ensure_stream_pack(lm_solver* s, const Geom& g);
-cudaError_t launch_cheb_stream_c32(lm_ctx* ctx, const FusedInst& d, int K, bool xreal, const float4* spack);
+cudaError_t launch_cheb_stream_c32(lm_ctx* ctx, const FusedInst& d, int K, int mode, const float4* spack);
 cudaError_t launch_cheb_fused_c32(lm_ctx* ctx, const Geom& g, const float2* hop2, const float* diag2,
                                   const float2* x, float2* out, int64_t ld, int64_t m, int K, bool xreal,
-                                  const ChebCoef* coef, double ph_re, double ph_im, const float4* spack = nullptr);
+                                  const ChebCoef* coef, double ph_re, double ph_im, const float4* spack = nullptr,
+                                  int stream_mode = 0);
 // Every x-hop of H is real: Landau-gauge field components only (or none) and no twist across
 // a periodic x axis.  The fused kernel then skips the imaginary parts of the x-hops.
 bool ham_x_real(const lm_ham* h);
+// ham_x_real and every hop of a lattice column equal (no twist across a periodic y axis): the
+// Landau line integral of a y-bond, (x1+x2)(y2-y1)B/2, depends on x only.
+bool ham_uniform_columns(const lm_ham* h);
 // a, b, K, the Chebyshev coefficients and e^{-ib dt} of exp(-i H dt) on [emin, emax] (or on
 // the solver's frozen interval), lmgpu_api.cu.
 void plan_propagator(lm_solver* s, double emin, double emax, double dt);

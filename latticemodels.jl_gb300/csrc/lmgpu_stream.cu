@@ -115,7 +115,8 @@ __device__ __forceinline__ int wrap_mod(int64_t c, int64_t L) {
 }
 
 __global__ void stream_pack_kernel(const Geom g, const float2* __restrict__ hop2, const float* __restrict__ diag2,
-                                   float4* __restrict__ pk, int npair, int Xp, long long plane) {
+                                   float4* __restrict__ pk, float2* __restrict__ pd, float4* __restrict__ pc, int npair,
+                                   int Xp, long long plane) {
     const long long n = (long long)Xp * npair + 1;
     const float2 z = make_float2(0.f, 0.f);
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
@@ -146,6 +147,10 @@ __global__ void stream_pack_kernel(const Geom g, const float2* __restrict__ hop2
                 }
             }
         }
+        pd[i] = make_float2(d[0], d[1]);
+        if (i < n - 1 && i % npair == 0) {  // column record: the hops of row 0 (pair 0)
+            pc[i / npair] = make_float4(hx[0].x, hxm[0].x, hy[0].x, hy[0].y);
+        }
         pk[i] = make_float4(hx[0].x, hx[1].x, hxm[0].x, hxm[1].x);
         pk[plane + i] = make_float4(hx[0].x, hx[0].y, hx[1].x, hx[1].y);
         pk[2 * plane + i] = make_float4(hxm[0].x, hxm[0].y, hxm[1].x, hxm[1].y);
@@ -154,10 +159,16 @@ __global__ void stream_pack_kernel(const Geom g, const float2* __restrict__ hop2
     }
 }
 
-template <int K, bool XR>
+// MODE 0: complex x-hops (planes 1-4); 1: real x-hops (planes 0, 3, 4); 2: uniform columns --
+// real x-hops and every hop of a column equal (the Landau gauge without a twist along y), so an
+// order reads the diagonal pair of its sites and one column record shared by the warp.
+template <int K, int MODE>
 __global__ void __launch_bounds__(SW * 32, 1)
-cheb_stream_c32_kernel(const FusedInst D, const float4* __restrict__ pk, int npair, long long plane, int nty,
-                       long long ncols, long long nwarps) {
+cheb_stream_c32_kernel(const FusedInst D, const float4* __restrict__ pk, const float2* __restrict__ pd,
+                       const float4* __restrict__ pc, int npair, long long plane, int nty, long long ncols,
+                       long long nwarps) {
+    constexpr bool XR = MODE >= 1;
+    constexpr bool UC = MODE == 2;
     constexpr int H = stream_halo(K);
     constexpr int YR = K + 1;          // accumulator ring: columns x .. x+K in flight
     constexpr int XS = K + 1 + SPF;    // ket ring: column s+SPF staged, column s-K still read
@@ -200,6 +211,9 @@ cheb_stream_c32_kernel(const FusedInst D, const float4* __restrict__ pk, int npa
         // the zero pair outside the lattice
         const int loff = ys >= 0 ? ys / 2 : (int)(plane - 1);
         const int lstep = ys >= 0 ? npair : 0;
+        // uniform columns along an open y axis: no bond above the last row or below the first
+        const bool y_last = UC && !g.per_y && ys + 1 == Ly - 1;
+        const bool y_first = UC && !g.per_y && ys == 0;
         const int n0 = xb - xa + 2 * K;
         const int nsteps = n0 + (NP - n0 % NP) % NP;
         const int s0 = xb + K - nsteps;  // xa - K, moved back so that nsteps is a multiple of NP
@@ -251,7 +265,18 @@ cheb_stream_c32_kernel(const FusedInst D, const float4* __restrict__ pk, int npa
                     const int o = ro - k * lstep;
                     float2 hx[2], hxm[2], hy[2], hym[2];
                     float d[2];
-                    if (o >= 0) {
+                    if (UC) {
+                        const float2 qd = __ldg(pd + o);
+                        const float4 qc = __ldg(pc + (s - k + kPadL));
+                        d[0] = qd.x;
+                        d[1] = qd.y;
+                        hx[0] = hx[1] = make_float2(qc.x, 0.f);
+                        hxm[0] = hxm[1] = make_float2(qc.y, 0.f);
+                        hy[0] = make_float2(qc.z, qc.w);
+                        hy[1] = y_last ? make_float2(0.f, 0.f) : hy[0];
+                        hym[0] = y_first ? make_float2(0.f, 0.f) : make_float2(qc.z, -qc.w);
+                        hym[1] = make_float2(qc.z, -qc.w);
+                    } else if (o >= 0) {
                         const float4 qy = __ldg(P3 + o), qd = __ldg(P4 + o);
                         hy[0] = make_float2(qy.x, qy.y);
                         hy[1] = make_float2(qy.z, qy.w);
@@ -407,8 +432,8 @@ cheb_stream_c32_kernel(const FusedInst D, const float4* __restrict__ pk, int npa
     }
 }
 
-bool stream_supported(const Geom& g, int K, bool xreal, const void* x, const void* out, int64_t ld) {
-    return K >= 2 && K <= (xreal ? kStreamMaxK : kStreamMaxK - 1) && g.Ly % 2 == 0 && g.Lx >= 2 * K + 3 && g.N < ((int64_t)1 << 31) &&
+bool stream_supported(const Geom& g, int K, int mode, const void* x, const void* out, int64_t ld) {
+    return K >= 2 && K <= (mode >= 1 ? kStreamMaxK : kStreamMaxK - 1) && g.Ly % 2 == 0 && g.Lx >= 2 * K + 3 && g.N < ((int64_t)1 << 31) &&
            ld % 2 == 0 && ((uintptr_t)x & 15) == 0 && ((uintptr_t)out & 15) == 0;
 }
 
@@ -418,12 +443,36 @@ static void pack_dims(const Geom& g, int* npair, int* Xp, long long* plane) {
     *plane = (long long)(*Xp) * (*npair) + 1;
 }
 
+// Layout of the packed buffer (float4 units): kPlanes planes, the diagonal pairs (float2, one
+// per record), the column records.
+struct PackPtrs {
+    float4* pk;
+    float2* pd;
+    float4* pc;
+};
+static size_t pack_f4(const Geom& g) {
+    int npair, Xp;
+    long long plane;
+    pack_dims(g, &npair, &Xp, &plane);
+    return (size_t)kPlanes * plane + (size_t)(plane + 1) / 2 + (size_t)Xp;
+}
+static PackPtrs pack_ptrs(float4* base, const Geom& g) {
+    int npair, Xp;
+    long long plane;
+    pack_dims(g, &npair, &Xp, &plane);
+    PackPtrs p;
+    p.pk = base;
+    p.pd = reinterpret_cast<float2*>(base + (size_t)kPlanes * plane);
+    p.pc = base + (size_t)kPlanes * plane + (size_t)(plane + 1) / 2;
+    return p;
+}
+
 int ensure_stream_pack(lm_solver* s, const Geom& g) {
     lm_ctx* ctx = s->ctx;
     int npair, Xp;
     long long plane;
     pack_dims(g, &npair, &Xp, &plane);
-    const size_t need = (size_t)kPlanes * (size_t)plane;
+    const size_t need = pack_f4(g);
     if (s->spack_f4 != need) {
         if (s->d_spack) cudaFree(s->d_spack);
         s->d_spack = nullptr;
@@ -440,7 +489,9 @@ int ensure_stream_pack(lm_solver* s, const Geom& g) {
     if (s->spack_version == s->tab_version) return LM_OK;
     const long long n = plane;
     const unsigned grid = (unsigned)std::min<long long>((n + 255) / 256, 4096);
-    stream_pack_kernel<<<grid, 256, 0, ctx->stream>>>(g, s->d_hop2f, s->d_diag2f, s->d_spack, npair, Xp, plane);
+    const PackPtrs pp = pack_ptrs(s->d_spack, g);
+    stream_pack_kernel<<<grid, 256, 0, ctx->stream>>>(g, s->d_hop2f, s->d_diag2f, pp.pk, pp.pd, pp.pc, npair, Xp,
+                                                      plane);
     ctx->launches++;
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return check_cuda(ctx, e, "x-streaming coefficient planes");
@@ -448,25 +499,26 @@ int ensure_stream_pack(lm_solver* s, const Geom& g) {
     return LM_OK;
 }
 
-template <bool XR>
-static cudaError_t launch_stream_k(lm_ctx* ctx, int K, int grid, const FusedInst& d, const float4* pk, int nty,
+template <int MODE>
+static cudaError_t launch_stream_k(lm_ctx* ctx, int K, int grid, const FusedInst& d, const float4* spack, int nty,
                                    long long ncols, long long nwarps) {
     int npair, Xp;
     long long plane;
     pack_dims(d.g, &npair, &Xp, &plane);
-    const unsigned bit = 1u << (K + (XR ? 8 : 0));
+    const PackPtrs pp = pack_ptrs(const_cast<float4*>(spack), d.g);
+    const unsigned bit = 1u << (K + 8 * MODE);
     switch (K) {
 #define LM_STREAM_CASE(KK)                                                                                       \
     case KK: {                                                                                                   \
         const int smem = SW * stream_ring_f4(KK) * 16;                                                           \
         if (!(ctx->stream_attr & bit)) {                                                                         \
-            cudaError_t e = cudaFuncSetAttribute(cheb_stream_c32_kernel<KK, XR>,                                 \
+            cudaError_t e = cudaFuncSetAttribute(cheb_stream_c32_kernel<KK, MODE>,                               \
                                                  cudaFuncAttributeMaxDynamicSharedMemorySize, smem);             \
             if (e != cudaSuccess) return e;                                                                      \
             ctx->stream_attr |= bit;                                                                             \
         }                                                                                                        \
-        cheb_stream_c32_kernel<KK, XR><<<(unsigned)grid, SW * 32, smem, ctx->stream>>>(d, pk, npair, plane,     \
-                                                                                         nty, ncols, nwarps);    \
+        cheb_stream_c32_kernel<KK, MODE><<<(unsigned)grid, SW * 32, smem, ctx->stream>>>(                       \
+            d, pp.pk, pp.pd, pp.pc, npair, plane, nty, ncols, nwarps);                                           \
         return cudaGetLastError();                                                                               \
     }
         LM_STREAM_CASE(2) LM_STREAM_CASE(3) LM_STREAM_CASE(4) LM_STREAM_CASE(5) LM_STREAM_CASE(6)
@@ -476,7 +528,7 @@ static cudaError_t launch_stream_k(lm_ctx* ctx, int K, int grid, const FusedInst
     }
 }
 
-cudaError_t launch_cheb_stream_c32(lm_ctx* ctx, const FusedInst& d, int K, bool xreal, const float4* spack) {
+cudaError_t launch_cheb_stream_c32(lm_ctx* ctx, const FusedInst& d, int K, int mode, const float4* spack) {
     const int H = stream_halo(K);
     const int64_t nty = strip_count(d.g.Ly, d.g.per_y, H);
     const long long ncols = (long long)nty * d.M * d.g.Lx;
@@ -486,8 +538,9 @@ cudaError_t launch_cheb_stream_c32(lm_ctx* ctx, const FusedInst& d, int K, bool 
     const long long slots = (long long)(ctx->sm_count > 0 ? ctx->sm_count : 152) * SW;
     const long long nwarps = std::max<long long>(1, std::min<long long>(slots, ncols / (8 * K)));
     const int grid = (int)((nwarps + SW - 1) / SW);
-    const cudaError_t e = xreal ? launch_stream_k<true>(ctx, K, grid, d, spack, (int)nty, ncols, nwarps)
-                                : launch_stream_k<false>(ctx, K, grid, d, spack, (int)nty, ncols, nwarps);
+    const cudaError_t e = mode == 2   ? launch_stream_k<2>(ctx, K, grid, d, spack, (int)nty, ncols, nwarps)
+                          : mode == 1 ? launch_stream_k<1>(ctx, K, grid, d, spack, (int)nty, ncols, nwarps)
+                                      : launch_stream_k<0>(ctx, K, grid, d, spack, (int)nty, ncols, nwarps);
     ctx->launches++;
     ctx->stream_launches++;
     return e;
