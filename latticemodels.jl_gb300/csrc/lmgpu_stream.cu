@@ -242,7 +242,7 @@ cheb_stream_c32_kernel(const FusedInst D, const float4* __restrict__ pk, const f
 #pragma unroll
         for (int j = 1; j < K; ++j)
 #pragma unroll
-            for (int c = 0; c < 3; ++c) W[j][c][0] = W[j][c][1] = make_float2(0.f, 0.f);
+            for (int cc = 0; cc < 3; ++cc) W[j][cc][0] = W[j][cc][1] = make_float2(0.f, 0.f);
 
         int xslot = 0;  // idx mod XS
         int yslot = 0;  // idx mod YR

@@ -399,6 +399,9 @@ STREAM_CASES = [
     (40, 70, True, False, "pointflux", 0.03, 7),  # complex x-hops (K <= 5)
     (33, 64, False, True, "pointflux", 0.03, 3),
     (20, 200, True, True, "landau", 0.05, 1),     # one ket, many strips
+    (24, 128, True, True, "landau", 0.05, 7),     # ring groups of 2 warps
+    (16, 512, True, True, "landau", 0.05, 3),     # ring groups of 8 warps
+    (40, 64, True, True, "pointflux", 0.03, 5),   # periodic 64 rows, complex hops: strips
     (41, 30, False, False, "landau", 0.05, 5),    # Ly < 64 open: lanes outside the lattice
     (33, 50, True, False, "landau", 0.05, 3),
     (64, 31, True, True, "landau", 0.05, 4),      # odd Ly: region form only
