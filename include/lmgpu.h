@@ -131,7 +131,8 @@ int lm_ham_bounds(lm_ham *ham, double *emin, double *emax);
 int lm_state_create(lm_ctx *ctx, int64_t n, int64_t m, int kind, int precision, lm_state **out);
 int lm_state_destroy(lm_state *st);
 /* Host <-> device copies; `host` holds complex values in the state's precision,
- * column-major with leading dimension `ld` (>= n). */
+ * column-major with leading dimension `ld` (>= n).  lm_state_upload also accepts a device
+ * pointer (unified addressing): the copy then stays on the device. */
 int lm_state_upload(lm_state *st, const void *host, int64_t ld);
 int lm_state_download(lm_state *st, void *host, int64_t ld);
 /* Device-to-device copy of `src` into `dst` (same shape, kind and precision): the state

@@ -652,7 +652,7 @@ int lm_state_upload(lm_state* s, const void* host, int64_t ld) {
     CHECK_ARG(ctx, ld >= s->n, "lm_state_upload: leading dimension smaller than n");
     cudaSetDevice(ctx->device);
     CUDA_TRY(ctx, cudaMemcpy2DAsync(s->d_data, s->elem * (size_t)s->ld, host, s->elem * (size_t)ld, s->elem * (size_t)s->n,
-                                    (size_t)s->m, cudaMemcpyHostToDevice, ctx->stream),
+                                    (size_t)s->m, cudaMemcpyDefault, ctx->stream),
              "upload state");
     return LM_OK;
 }

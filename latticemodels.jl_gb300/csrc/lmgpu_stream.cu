@@ -161,14 +161,16 @@ __global__ void stream_pack_kernel(const Geom g, const float2* __restrict__ hop2
 
 // MODE 0: complex x-hops (planes 1-4); 1: real x-hops (planes 0, 3, 4); 2: uniform columns --
 // real x-hops and every hop of a column equal (the Landau gauge without a twist along y), so an
-// order reads the diagonal pair of its sites and one column record shared by the warp.
+// order reads the diagonal pair of its sites and one column record shared by the warp; 3: the
+// same on a periodic y axis (no edge rows).
 template <int K, int MODE>
 __global__ void __launch_bounds__(SW * 32, 1)
 cheb_stream_c32_kernel(const FusedInst D, const float4* __restrict__ pk, const float2* __restrict__ pd,
                        const float4* __restrict__ pc, int npair, long long plane, int nty, long long ncols,
                        long long nwarps) {
     constexpr bool XR = MODE >= 1;
-    constexpr bool UC = MODE == 2;
+    constexpr bool UC = MODE >= 2;
+    constexpr bool YEDGE = MODE == 2;
     constexpr int H = stream_halo(K);
     constexpr int YR = K + 1;          // accumulator ring: columns x .. x+K in flight
     constexpr int XS = K + 1 + SPF;    // ket ring: column s+SPF staged, column s-K still read
@@ -212,8 +214,8 @@ cheb_stream_c32_kernel(const FusedInst D, const float4* __restrict__ pk, const f
         const int loff = ys >= 0 ? ys / 2 : (int)(plane - 1);
         const int lstep = ys >= 0 ? npair : 0;
         // uniform columns along an open y axis: no bond above the last row or below the first
-        const bool y_last = UC && !g.per_y && ys + 1 == Ly - 1;
-        const bool y_first = UC && !g.per_y && ys == 0;
+        const bool y_last = YEDGE && !g.per_y && ys + 1 == Ly - 1;
+        const bool y_first = YEDGE && !g.per_y && ys == 0;
         const int n0 = xb - xa + 2 * K;
         const int nsteps = n0 + (NP - n0 % NP) % NP;
         const int s0 = xb + K - nsteps;  // xa - K, moved back so that nsteps is a multiple of NP
@@ -273,8 +275,8 @@ cheb_stream_c32_kernel(const FusedInst D, const float4* __restrict__ pk, const f
                         hx[0] = hx[1] = make_float2(qc.x, 0.f);
                         hxm[0] = hxm[1] = make_float2(qc.y, 0.f);
                         hy[0] = make_float2(qc.z, qc.w);
-                        hy[1] = y_last ? make_float2(0.f, 0.f) : hy[0];
-                        hym[0] = y_first ? make_float2(0.f, 0.f) : make_float2(qc.z, -qc.w);
+                        hy[1] = (YEDGE && y_last) ? make_float2(0.f, 0.f) : hy[0];
+                        hym[0] = (YEDGE && y_first) ? make_float2(0.f, 0.f) : make_float2(qc.z, -qc.w);
                         hym[1] = make_float2(qc.z, -qc.w);
                     } else if (o >= 0) {
                         const float4 qy = __ldg(P3 + o), qd = __ldg(P4 + o);
@@ -538,9 +540,11 @@ cudaError_t launch_cheb_stream_c32(lm_ctx* ctx, const FusedInst& d, int K, int m
     const long long slots = (long long)(ctx->sm_count > 0 ? ctx->sm_count : 152) * SW;
     const long long nwarps = std::max<long long>(1, std::min<long long>(slots, ncols / (8 * K)));
     const int grid = (int)((nwarps + SW - 1) / SW);
-    const cudaError_t e = mode == 2   ? launch_stream_k<2>(ctx, K, grid, d, spack, (int)nty, ncols, nwarps)
-                          : mode == 1 ? launch_stream_k<1>(ctx, K, grid, d, spack, (int)nty, ncols, nwarps)
-                                      : launch_stream_k<0>(ctx, K, grid, d, spack, (int)nty, ncols, nwarps);
+    const int m = (mode == 2 && d.g.per_y) ? 3 : mode;
+    const cudaError_t e = m == 3   ? launch_stream_k<3>(ctx, K, grid, d, spack, (int)nty, ncols, nwarps)
+                          : m == 2 ? launch_stream_k<2>(ctx, K, grid, d, spack, (int)nty, ncols, nwarps)
+                          : m == 1 ? launch_stream_k<1>(ctx, K, grid, d, spack, (int)nty, ncols, nwarps)
+                                   : launch_stream_k<0>(ctx, K, grid, d, spack, (int)nty, ncols, nwarps);
     ctx->launches++;
     ctx->stream_launches++;
     return e;

@@ -11,6 +11,7 @@ Both run on the GPU only (no host eigensolver).
 """
 from __future__ import annotations
 
+import ctypes as C
 import math
 
 import numpy as np
@@ -111,4 +112,13 @@ def densitymatrix(H: Hamiltonian, mu: float = 0.0, T: float = 0.0, precision="c6
     f = densfun(T, mu)
     occ = torch.as_tensor(np.array([f(e) for e in w]), device="cuda", dtype=torch.float64)
     P = (V * occ) @ V.conj().T
-    return DensityMatrix(H.lattice, P.cpu().numpy(), precision)
+    if precision == "c32":
+        P = P.to(torch.complex64)
+    # the library's layout is column-major: a row-major copy of P^T holds P column-major
+    Pc = P.transpose(0, 1).contiguous()
+    torch.cuda.current_stream().synchronize()
+    ctx = default_context()
+    out = DensityMatrix(H.lattice, None, precision, ctx=ctx)
+    ctx.check(ctx.lib.lm_state_upload(out.handle, C.c_void_p(Pc.data_ptr()), H.lattice.N))
+    ctx.synchronize()  # Pc stays alive until the device copy is done
+    return out

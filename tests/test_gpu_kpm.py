@@ -89,6 +89,22 @@ def test_fermi_operator_densitymatrix(lm, mu, T, precision):
     assert abs(P.trace() - np.trace(Pref).real) <= (1e-10 if precision == "c64" else 1e-5) * np.trace(Pref).real
 
 
+@pytest.mark.parametrize("precision", ["c64", "c32"])
+def test_zero_temperature_densitymatrix(lm, precision):
+    """densitymatrix(H; mu) at T = 0: the device eigensystem (cuSOLVER) and the projector
+    stay on the device and go into the state without a host round trip; against the oracle's
+    eigh projector (src/spectrum.jl:226-257).  mu sits between levels."""
+    ol, Ho, Hl = case(lm, 12, False, "pf")
+    w = np.linalg.eigvalsh(Ho.toarray())
+    mu = 0.5 * (w[70] + w[71])
+    Pref, _, _ = o.densitymatrix(Ho, mu=mu)
+    P = lm.densitymatrix(Hl, mu=mu, precision=precision)
+    Pd = P.to_numpy().astype(np.complex128)
+    err = np.linalg.norm(Pd - Pref) / np.linalg.norm(Pref)
+    assert err <= (1e-12 if precision == "c64" else 1e-6), err
+    assert abs(P.trace() - 71) <= (1e-10 if precision == "c64" else 1e-4)
+
+
 def test_cheb_apply_on_kets_matches_dense_function(lm):
     """lm_cheb_apply on a ket block: f(H) X for f = exp(-(E - 0.3)^2) against the dense oracle."""
     import ctypes as C
