@@ -205,8 +205,9 @@ cudaError_t launch_convert(lm_ctx* ctx, int to_precision, const void* src, void*
 constexpr int kReadWarps = 8;  // warps of a readout block; they split the kets
 
 // localdensity of a ket block: rho_s = sum_k w_k |psi_sk|^2.  A block owns 32*VEC consecutive
-// sites (lane -> VEC sites, one 16-byte load per ket for c32 with VEC = 2); its 8 warps take
-// kets k = warp, warp + 8, ...; the 8 partial sums are added in warp order.
+// sites (lane -> VEC sites: c32 with VEC = 8 reads four 16-byte words per ket, so a warp reads
+// 2 KB of one ket at a time); its 8 warps take kets k = warp, warp + 8, ...; the 8 partial
+// sums are added in warp order.
 template <typename R, int VEC, bool WEIGHTED>
 __global__ void __launch_bounds__(32 * kReadWarps) localdensity_kets_kernel(
     const typename CT<R>::V* __restrict__ x, int64_t n, int64_t m, int64_t ld, const double* __restrict__ w,
@@ -223,10 +224,13 @@ __global__ void __launch_bounds__(32 * kReadWarps) localdensity_kets_kernel(
 #pragma unroll 4
         for (int64_t k = warp; k < m; k += kReadWarps) {
             V v[VEC];
-            if (VEC == 2) {
-                const float4 q = __ldg(reinterpret_cast<const float4*>(x + k * ld + s0));
-                v[0] = CT<R>::make(q.x, q.y);
-                v[VEC - 1] = CT<R>::make(q.z, q.w);
+            if (VEC >= 2) {
+#pragma unroll
+                for (int h = 0; h < VEC / 2; ++h) {
+                    const float4 q = __ldg(reinterpret_cast<const float4*>(x + k * ld + s0) + h);
+                    v[2 * h] = CT<R>::make(q.x, q.y);
+                    v[2 * h + 1] = CT<R>::make(q.z, q.w);
+                }
             } else {
                 v[0] = x[k * ld + s0];
             }
@@ -280,7 +284,10 @@ cudaError_t launch_localdensity(lm_ctx* ctx, int precision, int kind, const void
         if (precision == LM_C64) localdensity_dm_kernel<double><<<blocks, 128, 0, ctx->stream>>>((const double2*)x, n, ld, out);
         else localdensity_dm_kernel<float><<<blocks, 128, 0, ctx->stream>>>((const float2*)x, n, ld, out);
     } else if (precision == LM_C64) {
+        // the FP64 pipe bounds c64 (two DFMAs per element): wider lanes measured slower
         launch_ld_kets<double, 1>(ctx, x, n, m, ld, w, out);
+    } else if (n % 8 == 0 && ld % 2 == 0 && ((uintptr_t)x & 15) == 0) {
+        launch_ld_kets<float, 8>(ctx, x, n, m, ld, w, out);  // 2 KB of a ket per warp load
     } else if (n % 2 == 0 && ld % 2 == 0 && ((uintptr_t)x & 15) == 0) {
         launch_ld_kets<float, 2>(ctx, x, n, m, ld, w, out);  // 16-byte loads of site pairs
     } else {
