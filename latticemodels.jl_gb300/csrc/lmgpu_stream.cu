@@ -60,11 +60,20 @@ constexpr int kPlanes = 5;
 
 __host__ __device__ constexpr int stream_halo(int K) { return K + (K & 1); }  // even: pairs stay aligned
 __host__ __device__ constexpr int stream_ring_f4(int K) { return ((K + 1) + (K + 1 + SPF)) * 32; }
+// Uniform-column modes also keep, per warp, a ring of the diagonal pairs of the staged columns
+// (same slots as the ket ring) and, per CTA, the column records of the whole lattice.
+__host__ __device__ constexpr int stream_dring_f4(int K) { return (K + 1 + SPF) * 16; }
+constexpr int kStreamSmemMax = 232448;  // bytes of shared memory a CTA may use
 
 __device__ __forceinline__ void cp_async16(float4* dst_smem, const void* src, bool valid) {
     const unsigned dst = (unsigned)__cvta_generic_to_shared(dst_smem);
     const int n = valid ? 16 : 0;  // n = 0 fills the 16 bytes with zeros
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(dst), "l"(src), "r"(n));
+}
+__device__ __forceinline__ void cp_async8s(float2* dst_smem, const void* src, bool valid) {
+    const unsigned dst = (unsigned)__cvta_generic_to_shared(dst_smem);
+    const int n = valid ? 8 : 0;
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(dst), "l"(src), "r"(n));
 }
 __device__ __forceinline__ void cp_async_commit_s() { asm volatile("cp.async.commit_group;\n" ::); }
 template <int N>
@@ -188,6 +197,14 @@ cheb_stream_c32_kernel(const FusedInst D, const float4* __restrict__ pk, const f
     const float4* __restrict__ P2 = pk + 2 * plane;
     const float4* __restrict__ P3 = pk + 3 * plane;
     const float4* __restrict__ P4 = pk + 4 * plane;
+    // uniform columns: diagonal-pair ring per warp, column records per CTA
+    float2* dring = reinterpret_cast<float2*>(smem + SW * stream_ring_f4(K)) + warp * XS * 32;
+    float4* ctab = smem + SW * (stream_ring_f4(K) + stream_dring_f4(K));
+    if (UC) {
+        const int Xp = Lx + kPadL + kPadR;
+        for (int i = threadIdx.x; i < Xp; i += SW * 32) ctab[i] = __ldg(pc + i);
+        __syncthreads();
+    }
 
     // Work: the columns of every (strip, ket) item, items in the order strip-major, ket-minor;
     // warp w takes the contiguous share [w ncols / nwarps, (w+1) ncols / nwarps) of them, i.e.
@@ -232,6 +249,11 @@ cheb_stream_c32_kernel(const FusedInst D, const float4* __restrict__ pk, const f
             const bool v = idx < nsteps && xs >= 0 && ys >= 0;
             const float2* src = v ? xk + (long long)xs * Ly + ys : xk;
             cp_async16(&xring[stage_slot * 32 + lane], src, v);
+            if (UC) {  // the diagonal pair of the same column (padded records: always in range)
+                const bool vd = idx < nsteps;
+                cp_async8s(&dring[stage_slot * 32 + lane], vd ? pd + loff + (long long)(s0 + idx + kPadL) * lstep : pd,
+                           vd);
+            }
             cp_async_commit_s();
             stage_slot = stage_slot + 1 == XS ? 0 : stage_slot + 1;
         };
@@ -268,8 +290,10 @@ cheb_stream_c32_kernel(const FusedInst D, const float4* __restrict__ pk, const f
                     float2 hx[2], hxm[2], hy[2], hym[2];
                     float d[2];
                     if (UC) {
-                        const float2 qd = __ldg(pd + o);
-                        const float4 qc = __ldg(pc + (s - k + kPadL));
+                        int dsl = xslot - k;
+                        if (dsl < 0) dsl += XS;
+                        const float2 qd = dring[dsl * 32 + lane];
+                        const float4 qc = ctab[s - k + kPadL];
                         d[0] = qd.x;
                         d[1] = qd.y;
                         hx[0] = hx[1] = make_float2(qc.x, 0.f);
@@ -501,6 +525,10 @@ int ensure_stream_pack(lm_solver* s, const Geom& g) {
     return LM_OK;
 }
 
+static int stream_smem_bytes(int K, int mode, int Xp) {
+    return SW * stream_ring_f4(K) * 16 + (mode >= 2 ? SW * stream_dring_f4(K) * 16 + Xp * 16 : 0);
+}
+
 template <int MODE>
 static cudaError_t launch_stream_k(lm_ctx* ctx, int K, int grid, const FusedInst& d, const float4* spack, int nty,
                                    long long ncols, long long nwarps) {
@@ -512,10 +540,10 @@ static cudaError_t launch_stream_k(lm_ctx* ctx, int K, int grid, const FusedInst
     switch (K) {
 #define LM_STREAM_CASE(KK)                                                                                       \
     case KK: {                                                                                                   \
-        const int smem = SW * stream_ring_f4(KK) * 16;                                                           \
+        const int smem = stream_smem_bytes(KK, MODE, Xp);                                                        \
         if (!(ctx->stream_attr & bit)) {                                                                         \
             cudaError_t e = cudaFuncSetAttribute(cheb_stream_c32_kernel<KK, MODE>,                               \
-                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, smem);             \
+                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, kStreamSmemMax);   \
             if (e != cudaSuccess) return e;                                                                      \
             ctx->stream_attr |= bit;                                                                             \
         }                                                                                                        \
@@ -540,7 +568,8 @@ cudaError_t launch_cheb_stream_c32(lm_ctx* ctx, const FusedInst& d, int K, int m
     const long long slots = (long long)(ctx->sm_count > 0 ? ctx->sm_count : 152) * SW;
     const long long nwarps = std::max<long long>(1, std::min<long long>(slots, ncols / (8 * K)));
     const int grid = (int)((nwarps + SW - 1) / SW);
-    const int m = (mode == 2 && d.g.per_y) ? 3 : mode;
+    int m = (mode == 2 && d.g.per_y) ? 3 : mode;
+    if (m >= 2 && stream_smem_bytes(K, m, (int)d.g.Lx + kPadL + kPadR) > kStreamSmemMax) m = 1;  // very long x
     const cudaError_t e = m == 3   ? launch_stream_k<3>(ctx, K, grid, d, spack, (int)nty, ncols, nwarps)
                           : m == 2 ? launch_stream_k<2>(ctx, K, grid, d, spack, (int)nty, ncols, nwarps)
                           : m == 1 ? launch_stream_k<1>(ctx, K, grid, d, spack, (int)nty, ncols, nwarps)
