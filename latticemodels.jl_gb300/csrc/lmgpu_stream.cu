@@ -38,9 +38,10 @@ namespace lmgpu {
 #define LM_STREAM_WARPS 16
 #endif
 // 1: the three-column windows rotate by register moves at the end of every step; 0: the
-// step loop is unrolled three times and the rotation is renaming (more code in flight).
+// step loop is unrolled three times and the rotation is renaming (more code in flight);
+// 2: unrolled in the uniform-column modes (few coefficient registers), rotating otherwise.
 #ifndef LM_STREAM_ROTATE
-#define LM_STREAM_ROTATE 1
+#define LM_STREAM_ROTATE 2
 #endif
 
 namespace {
@@ -183,7 +184,7 @@ cheb_stream_c32_kernel(const FusedInst D, const float4* __restrict__ pk, const f
     constexpr int H = stream_halo(K);
     constexpr int YR = K + 1;          // accumulator ring: columns x .. x+K in flight
     constexpr int XS = K + 1 + SPF;    // ket ring: column s+SPF staged, column s-K still read
-    constexpr bool ROT = LM_STREAM_ROTATE != 0;
+    constexpr bool ROT = LM_STREAM_ROTATE == 1 || (LM_STREAM_ROTATE == 2 && MODE < 2);
     constexpr int NP = ROT ? 1 : 3;    // steps per unrolled loop body
     extern __shared__ float4 smem[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
