@@ -144,7 +144,9 @@ int lm_state_device_ptr(lm_state *st, void **ptr, int64_t *ld);
 int lm_state_set_weights(lm_state *st, const double *w);
 /* Per-ket FP64 norms (m doubles). */
 int lm_state_norms(lm_state *st, double *out);
-/* Rescales every ket to the given FP64 norms (the FP32 form's periodic norm correction). */
+/* Rescales every ket to the given FP64 norms (the FP32 form's periodic norm correction).
+ * Stream-ordered: returns without waiting for the device; target_norms is copied during the
+ * call. */
 int lm_state_renormalize(lm_state *st, const double *target_norms);
 
 /* ---- evolution solver (the EvolutionSolver plugin, src/evolution.jl:5-33) ------------ */

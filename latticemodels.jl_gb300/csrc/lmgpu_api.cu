@@ -735,12 +735,16 @@ int lm_state_renormalize(lm_state* s, const double* target) {
     cudaSetDevice(ctx->device);
     int rc = ensure_red(ctx, 2 * (size_t)s->m);
     if (rc != LM_OK) return rc;
-    CUDA_TRY(ctx, cudaMemcpyAsync(ctx->d_red + s->m, target, sizeof(double) * (size_t)s->m, cudaMemcpyHostToDevice, ctx->stream),
+    // a library-owned pageable copy: the driver stages it during the call, so the caller's
+    // buffer (pinned or not) is free again on return and the stream is not drained
+    ctx->h_norms.assign(target, target + s->m);
+    CUDA_TRY(ctx, cudaMemcpyAsync(ctx->d_red + s->m, ctx->h_norms.data(), sizeof(double) * (size_t)s->m,
+                                  cudaMemcpyHostToDevice, ctx->stream),
              "upload target norms");
     CUDA_TRY(ctx, launch_column_norms(ctx, s->precision, s->d_data, s->n, s->m, s->ld, ctx->d_red), "column norms");
     CUDA_TRY(ctx, launch_rescale_columns(ctx, s->precision, s->d_data, s->n, s->m, s->ld, ctx->d_red, ctx->d_red + s->m),
              "rescale columns");
-    CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream), "sync");
+    // no host synchronisation: the target norms were staged by the (pageable) copy above
     return LM_OK;
 }
 

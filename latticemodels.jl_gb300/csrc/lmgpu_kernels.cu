@@ -6,6 +6,8 @@
 #include <cuda_runtime.h>
 #include <math.h>
 
+#include <algorithm>
+
 #include "lmgpu_internal.cuh"
 #include "lmgpu_order.cuh"
 
@@ -453,17 +455,35 @@ cudaError_t launch_column_norms(lm_ctx* ctx, int precision, const void* x, int64
     return cudaGetLastError();
 }
 
-template <typename R>
-__global__ void rescale_columns_kernel(typename CT<R>::V* x, int64_t n, int64_t m, int64_t ld,
-                                       const double* __restrict__ norms, const double* __restrict__ target) {
+// x[:, k] *= target[k] / norms[k].  A block rescales 256 * 4 * VEC consecutive elements of one
+// column (VEC = 2: c32 site pairs as 16-byte words).
+template <typename R, int VEC>
+__global__ void __launch_bounds__(256) rescale_columns_kernel(typename CT<R>::V* x, int64_t n, int64_t m, int64_t ld,
+                                                              const double* __restrict__ norms,
+                                                              const double* __restrict__ target) {
+    constexpr int PER = 4 * VEC;  // elements per thread
     for (int64_t k = blockIdx.y; k < m; k += gridDim.y) {
         const double nk = norms[k];
         const R f = (R)(nk > 0.0 ? target[k] / nk : 1.0);
-        for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-            typename CT<R>::V v = x[k * ld + i];
-            v.x *= f;
-            v.y *= f;
-            x[k * ld + i] = v;
+        typename CT<R>::V* col = x + k * ld;
+        for (int64_t i0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) * VEC; i0 < n;
+             i0 += (int64_t)gridDim.x * blockDim.x * PER) {
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int64_t i = i0 + (int64_t)u * blockDim.x * VEC;
+                if (i >= n) break;
+                if (VEC == 2) {
+                    float4* p = reinterpret_cast<float4*>(col + i);
+                    float4 q = *p;
+                    q.x *= f; q.y *= f; q.z *= f; q.w *= f;
+                    *p = q;
+                } else {
+                    typename CT<R>::V v = col[i];
+                    v.x *= f;
+                    v.y *= f;
+                    col[i] = v;
+                }
+            }
         }
     }
 }
@@ -471,11 +491,16 @@ __global__ void rescale_columns_kernel(typename CT<R>::V* x, int64_t n, int64_t 
 cudaError_t launch_rescale_columns(lm_ctx* ctx, int precision, void* x, int64_t n, int64_t m, int64_t ld,
                                    const double* norms, const double* target) {
     if (m <= 0) return cudaSuccess;
-    int64_t bx = (n + 255) / 256;
-    if (bx > 1024) bx = 1024;
-    dim3 grid((unsigned)bx, (unsigned)(m < 65535 ? m : 65535));
-    if (precision == LM_C64) rescale_columns_kernel<double><<<grid, 256, 0, ctx->stream>>>((double2*)x, n, m, ld, norms, target);
-    else rescale_columns_kernel<float><<<grid, 256, 0, ctx->stream>>>((float2*)x, n, m, ld, norms, target);
+    const bool pairs = precision == LM_C32 && n % 2 == 0 && ld % 2 == 0 && ((uintptr_t)x & 15) == 0;
+    const int64_t per_block = 256 * 4 * (pairs ? 2 : 1);
+    const int64_t bx = std::min<int64_t>((n + per_block - 1) / per_block, 1024);
+    const dim3 grid((unsigned)bx, (unsigned)(m < 65535 ? m : 65535));
+    if (precision == LM_C64)
+        rescale_columns_kernel<double, 1><<<grid, 256, 0, ctx->stream>>>((double2*)x, n, m, ld, norms, target);
+    else if (pairs)
+        rescale_columns_kernel<float, 2><<<grid, 256, 0, ctx->stream>>>((float2*)x, n, m, ld, norms, target);
+    else
+        rescale_columns_kernel<float, 1><<<grid, 256, 0, ctx->stream>>>((float2*)x, n, m, ld, norms, target);
     ctx->launches++;
     return cudaGetLastError();
 }

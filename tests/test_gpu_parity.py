@@ -268,6 +268,26 @@ def test_edge_cases(lm):
         small.renormalize(np.ones(1))
 
 
+@pytest.mark.parametrize("precision", ["c64", "c32"])
+@pytest.mark.parametrize("n", [1000, 1001])
+def test_renormalize(lm, precision, n):
+    """lm_state_renormalize rescales every ket to its target FP64 norm without waiting for the
+    device; the target buffer is copied during the call (overwriting it afterwards changes
+    nothing).  Even n takes the 16-byte site-pair path for c32."""
+    lat = lm.SquareLattice(n, 1)
+    X = o.random_kets(n, 37, 5)
+    st = lm.KetBlock(lat, X, precision=precision)
+    target = np.linspace(0.5, 2.0, 37)
+    keep = target.copy()
+    st.renormalize(target)
+    target[:] = 7.0
+    got = st.norms()
+    tol = 1e-14 if precision == "c64" else 1e-6
+    assert np.abs(got - keep).max() <= tol * keep.max()
+    ref = X / np.linalg.norm(X, axis=0) * keep
+    assert rel(st.to_numpy().astype(np.complex128), ref) <= (1e-14 if precision == "c64" else 1e-6)
+
+
 FUSED_CASES = [
     (256, 256, (True, True), [("landau", 0.01, None, None)], 11, 0.05),
     (10, 10, (False, False), [("pf", 0.2, (5.5, 5.5), "axial")], 9, 0.1),
