@@ -13,8 +13,8 @@ from .device import Context, default_context
 from .evolution import ChebyshevGPU, Evolution, EvolutionIterator, EvolutionSolver, EvolutionTimestamp
 from .fields import FieldSum, LandauGauge, NoField, PointFlux, PointFluxes, SymmetricGauge
 from .hamiltonian import Hamiltonian, tightbinding_hamiltonian
-from .lattice import LatticeValue, SquareLattice
-from .observables import Currents, DensityCurrents, currentsfromto, localdensity
+from .lattice import LatticeValue, SquareLattice, coordvalues
+from .observables import Currents, DensityCurrents, SubCurrents, currentsfrom, currentsfromto, localdensity
 from .sparse import LocalOperatorCurrents, SiteCurrents, Sites, SparseHamiltonian, entry_currents
 from .spectrum import densitymatrix, diagonalize
 from .states import DensityMatrix, DeviceState, Ket, KetBlock, Operator
@@ -25,8 +25,8 @@ __all__ = [
     "adjoint", "kpm", "DensityLossAdjoint", "Batch", "LMError", "load_library", "Context", "default_context",
     "ChebyshevGPU", "Evolution", "EvolutionIterator", "EvolutionSolver", "EvolutionTimestamp",
     "FieldSum", "LandauGauge", "NoField", "PointFlux", "PointFluxes", "SymmetricGauge",
-    "Hamiltonian", "tightbinding_hamiltonian", "LatticeValue", "SquareLattice",
-    "Currents", "DensityCurrents", "currentsfromto", "localdensity", "densitymatrix", "diagonalize",
+    "Hamiltonian", "tightbinding_hamiltonian", "LatticeValue", "SquareLattice", "coordvalues",
+    "Currents", "DensityCurrents", "SubCurrents", "currentsfrom", "currentsfromto", "localdensity", "densitymatrix", "diagonalize",
     "DensityMatrix", "DeviceState", "Ket", "KetBlock", "Operator",
     "LocalOperatorCurrents", "SiteCurrents", "Sites", "SparseHamiltonian", "entry_currents", "ReadoutRing", "TimeSequence", "differentiate", "integrate", "moment_currents", "moment_density",
 ]

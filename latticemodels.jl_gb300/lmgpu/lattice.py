@@ -152,3 +152,37 @@ class LatticeValue:
 
     def __repr__(self):
         return f"LatticeValue{{{self.values.dtype}}} on {self.lattice!r}"
+
+    # elementwise comparisons give Bool masks (x .< y in the reference)
+    def _cmp(self, other, op):
+        o = other.values if isinstance(other, LatticeValue) else other
+        return LatticeValue(self.lattice, op(self.values, o))
+
+    def __lt__(self, other):
+        return self._cmp(other, np.less)
+
+    def __le__(self, other):
+        return self._cmp(other, np.less_equal)
+
+    def __gt__(self, other):
+        return self._cmp(other, np.greater)
+
+    def __ge__(self, other):
+        return self._cmp(other, np.greater_equal)
+
+
+def coordvalues(lattice):
+    """``coordvalues(l)`` (src/core/latticevalue.jl:95-100): one LatticeValue per coordinate."""
+    xy = lattice.coords()
+    return tuple(LatticeValue(lattice, xy[:, d].copy()) for d in range(xy.shape[1]))
+
+
+def site_indices(lattice, sel) -> np.ndarray:
+    """1-based site indices of a selection: a Bool LatticeValue or mask, an index, or indices
+    (the reference's ``to_inds``)."""
+    if isinstance(sel, LatticeValue):
+        sel = sel.values
+    a = np.asarray(sel)
+    if a.dtype == bool:
+        return np.nonzero(a)[0] + 1
+    return np.atleast_1d(a).astype(np.int64)

@@ -18,6 +18,7 @@ import numpy as np
 
 from . import _lib
 from .device import default_context
+from .observables import _CurrentsOps
 
 
 class Sites:
@@ -142,7 +143,7 @@ def _local_op(H: SparseHamiltonian, op):
     return np.ascontiguousarray(O.T).view(np.float64).ravel()  # column-major, interleaved
 
 
-class SiteCurrents:
+class SiteCurrents(_CurrentsOps):
     """DensityCurrents (src/zoo/currents.jl:81-102) or LocalOperatorCurrents (:150-184) of a
     state under a SparseHamiltonian.  One device pass gives the value of every stored entry of
     H (``lm_ell_op_currents``); ``curr[i, j]`` (1-based sites) is the sum over the entries of
@@ -187,6 +188,8 @@ class SiteCurrents:
         return self._pairs
 
     def __getitem__(self, ij):
+        if not isinstance(ij, tuple):
+            return self.select(ij)
         i, j = ij
         src, dst, v = self.site_pairs()
         k = np.nonzero((src == i) & (dst == j))[0]

@@ -63,3 +63,31 @@ def test_density_matrix_readouts(lm, precision):
     J = o.bond_currents(Ho, Pd, np.asarray(src), np.asarray(dst), is_density=True)
     assert np.abs(lm.DensityCurrents(Hl, st).bond_values() - J).max() <= 1e-14
     assert abs(st.trace() - Pd.diagonal().real.sum()) <= 1e-13
+
+
+def test_subcurrents_and_currentsfrom_on_device_values(lm):
+    """DensityCurrents of a device state: Currents(dc)[x .< y] == Currents(dc[x .< y]) against
+    the oracle's materialised currents on the same subset, and currentsfrom /
+    currentsfromto (test/test_currents.jl:11-62)."""
+    L = 6
+    ol = o.SquareLattice(L, L)
+    ll = lm.SquareLattice(L, L)
+    Ho = o.tightbinding_hamiltonian(ol, field=o.LandauGauge(0.1))
+    Hl = lm.tightbinding_hamiltonian(ll, field=lm.LandauGauge(0.1))
+    P0, _, _ = o.densitymatrix(o.tightbinding_hamiltonian(ol), mu=0.1)
+    st = lm.DensityMatrix(ll, P0)
+    dc = lm.DensityCurrents(Hl, st)
+    ref = o.currents_matrix(Ho, P0, is_density=True).toarray()  # all pairs, |J| < 1e-10 dropped
+    x, y = lm.coordvalues(ll)
+    mask = x < y
+    idx = np.nonzero(mask.values)[0]
+    m1 = lm.Currents(dc)[mask]
+    m2 = lm.Currents(dc[mask])
+    assert np.abs(np.asarray(m1._matrix()) - ref[np.ix_(idx, idx)]).max() <= 1e-13
+    assert np.abs(m2.toarray() - ref[np.ix_(idx, idx)]).max() <= 1e-13
+    site = 8
+    cf = lm.currentsfrom(dc, site).values
+    want = ref[site - 1].copy()
+    want[site - 1] = 0.0
+    assert np.abs(cf - want).max() <= 1e-13
+    assert abs(lm.currentsfromto(dc, site) - want.sum()) <= 1e-13
