@@ -908,13 +908,14 @@ static int cheb_apply(lm_solver* s, const Geom& g, int precision, int site_fast,
         return LM_OK;
     }
     const ChebLo lo = cheb_lo(pr, pi, c0, coef(1).s, false);
-    CUDA_TRY(ctx, launch_cheb_order(ctx, g, precision, site_fast, conj, CHEB_FIRST, hop2, diag2, S, A, Y, ld, m, c0, coef(1), pr, pi, lo),
+    const bool xr = ham_x_real(s->ham);
+    CUDA_TRY(ctx, launch_cheb_order(ctx, g, precision, site_fast, conj, CHEB_FIRST, hop2, diag2, S, A, Y, ld, m, c0, coef(1), pr, pi, lo, xr),
              "chebyshev order 1");
     for (int k = 2; k <= K; ++k) {
         const void* tp = (k % 2 == 0) ? A : S;
         void* tq = (k % 2 == 0) ? S : A;
         const int mode = (k == K) ? CHEB_LAST : CHEB_MID;
-        CUDA_TRY(ctx, launch_cheb_order(ctx, g, precision, site_fast, conj, mode, hop2, diag2, tp, tq, Y, ld, m, c0, coef(k), pr, pi, lo),
+        CUDA_TRY(ctx, launch_cheb_order(ctx, g, precision, site_fast, conj, mode, hop2, diag2, tp, tq, Y, ld, m, c0, coef(k), pr, pi, lo, xr),
                  "chebyshev order");
     }
     if (ctx->timing) {

@@ -229,7 +229,7 @@ cudaError_t launch_normalise(lm_ctx* ctx, const Geom& g, const double2* hop, con
 cudaError_t launch_cheb_order(lm_ctx* ctx, const Geom& g, int precision, int site_fast, int conj,
                               int mode, const void* hop2, const void* diag2, const void* tp, void* tq,
                               void* y, int64_t ld, int64_t m, double c0, ChebCoef ck,
-                              double ph_re, double ph_im, ChebLo lo);
+                              double ph_re, double ph_im, ChebLo lo, bool xreal = false);
 cudaError_t launch_scale(lm_ctx* ctx, int precision, void* x, int64_t n, int64_t m, int64_t ld,
                          double re, double im);
 cudaError_t launch_localdensity(lm_ctx* ctx, int precision, int kind, const void* x, int64_t n,

@@ -94,17 +94,18 @@ cudaError_t launch_normalise(lm_ctx* ctx, const Geom& g, const double2* hop, con
 }
 
 // One order of the Chebyshev recurrence for one lattice (see cheb_order_block).
-template <typename R, int MODE, bool SITE_FAST, bool CONJ, int INNER>
+template <typename R, int MODE, bool SITE_FAST, bool CONJ, int INNER, bool XR>
 __global__ void __launch_bounds__(256) cheb_order_kernel(
     Geom g, const typename CT<R>::V* __restrict__ hop2, const R* __restrict__ diag2,
     const typename CT<R>::V* __restrict__ tp, typename CT<R>::V* tq, typename CT<R>::V* y,
     int64_t ld, int64_t M, R c0, R cs, int odd, R ph_re, R ph_im, ChebLo lo) {
     const int64_t lane = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;  // fast dimension
-    cheb_order_block<R, MODE, SITE_FAST, CONJ, INNER>(g, hop2, diag2, tp, tq, y, ld, M, c0, cs, odd, ph_re, ph_im,
-                                                      lo, lane, (int64_t)blockIdx.y * INNER, (int64_t)gridDim.y * INNER);
+    cheb_order_block<R, MODE, SITE_FAST, CONJ, INNER, XR>(g, hop2, diag2, tp, tq, y, ld, M, c0, cs, odd, ph_re,
+                                                          ph_im, lo, lane, (int64_t)blockIdx.y * INNER,
+                                                          (int64_t)gridDim.y * INNER);
 }
 
-template <typename R, int MODE, bool SF, bool CJ>
+template <typename R, int MODE, bool SF, bool CJ, bool XR>
 static void launch_cheb_t(lm_ctx* ctx, const Geom& g, const void* hop2, const void* diag2, const void* tp,
                           void* tq, void* y, int64_t ld, int64_t m, double c0, ChebCoef ck, double ph_re,
                           double ph_im, ChebLo lo) {
@@ -117,39 +118,47 @@ static void launch_cheb_t(lm_ctx* ctx, const Geom& g, const void* hop2, const vo
     int64_t gy = (nslow + INNER - 1) / INNER;
     if (gy > 65535) gy = 65535;
     dim3 grid((unsigned)gx, (unsigned)gy);
-    cheb_order_kernel<R, MODE, SF, CJ, INNER><<<grid, thr, 0, ctx->stream>>>(
+    cheb_order_kernel<R, MODE, SF, CJ, INNER, XR><<<grid, thr, 0, ctx->stream>>>(
         g, (const V*)hop2, (const R*)diag2, (const V*)tp, (V*)tq, (V*)y, ld, m, (R)c0, (R)ck.s, ck.odd,
         (R)ph_re, (R)ph_im, lo);
 }
 
+template <typename R, bool SF, bool CJ, bool XR>
+static void dispatch_mode_x(int mode, lm_ctx* ctx, const Geom& g, const void* hop2, const void* diag2,
+                            const void* tp, void* tq, void* y, int64_t ld, int64_t m, double c0, ChebCoef ck,
+                            double pr, double pi, ChebLo lo) {
+    if (mode == CHEB_FIRST) launch_cheb_t<R, CHEB_FIRST, SF, CJ, XR>(ctx, g, hop2, diag2, tp, tq, y, ld, m, c0, ck, pr, pi, lo);
+    else if (mode == CHEB_MID) launch_cheb_t<R, CHEB_MID, SF, CJ, XR>(ctx, g, hop2, diag2, tp, tq, y, ld, m, c0, ck, pr, pi, lo);
+    else launch_cheb_t<R, CHEB_LAST, SF, CJ, XR>(ctx, g, hop2, diag2, tp, tq, y, ld, m, c0, ck, pr, pi, lo);
+}
+
 template <typename R, bool SF, bool CJ>
-static void dispatch_mode(int mode, lm_ctx* ctx, const Geom& g, const void* hop2, const void* diag2,
+static void dispatch_mode(int mode, bool xreal, lm_ctx* ctx, const Geom& g, const void* hop2, const void* diag2,
                           const void* tp, void* tq, void* y, int64_t ld, int64_t m, double c0, ChebCoef ck,
                           double pr, double pi, ChebLo lo) {
-    if (mode == CHEB_FIRST) launch_cheb_t<R, CHEB_FIRST, SF, CJ>(ctx, g, hop2, diag2, tp, tq, y, ld, m, c0, ck, pr, pi, lo);
-    else if (mode == CHEB_MID) launch_cheb_t<R, CHEB_MID, SF, CJ>(ctx, g, hop2, diag2, tp, tq, y, ld, m, c0, ck, pr, pi, lo);
-    else launch_cheb_t<R, CHEB_LAST, SF, CJ>(ctx, g, hop2, diag2, tp, tq, y, ld, m, c0, ck, pr, pi, lo);
+    if (xreal) dispatch_mode_x<R, SF, CJ, true>(mode, ctx, g, hop2, diag2, tp, tq, y, ld, m, c0, ck, pr, pi, lo);
+    else dispatch_mode_x<R, SF, CJ, false>(mode, ctx, g, hop2, diag2, tp, tq, y, ld, m, c0, ck, pr, pi, lo);
 }
 
 cudaError_t launch_cheb_order(lm_ctx* ctx, const Geom& g, int precision, int site_fast, int conj, int mode,
                               const void* hop2, const void* diag2, const void* tp, void* tq, void* y,
                               int64_t ld, int64_t m, double c0, ChebCoef ck, double ph_re, double ph_im,
-                              ChebLo lo) {
+                              ChebLo lo, bool xreal) {
     if (precision == LM_C64) {
         if (site_fast) {
-            if (conj) dispatch_mode<double, true, true>(mode, ctx, g, hop2, diag2, tp, tq, y, ld, m, c0, ck, ph_re, ph_im, lo);
-            else dispatch_mode<double, true, false>(mode, ctx, g, hop2, diag2, tp, tq, y, ld, m, c0, ck, ph_re, ph_im, lo);
+            if (conj) dispatch_mode<double, true, true>(mode, xreal, ctx, g, hop2, diag2, tp, tq, y, ld, m, c0, ck, ph_re, ph_im, lo);
+            else dispatch_mode<double, true, false>(mode, xreal, ctx, g, hop2, diag2, tp, tq, y, ld, m, c0, ck, ph_re, ph_im, lo);
         } else {
-            if (conj) dispatch_mode<double, false, true>(mode, ctx, g, hop2, diag2, tp, tq, y, ld, m, c0, ck, ph_re, ph_im, lo);
-            else dispatch_mode<double, false, false>(mode, ctx, g, hop2, diag2, tp, tq, y, ld, m, c0, ck, ph_re, ph_im, lo);
+            if (conj) dispatch_mode<double, false, true>(mode, xreal, ctx, g, hop2, diag2, tp, tq, y, ld, m, c0, ck, ph_re, ph_im, lo);
+            else dispatch_mode<double, false, false>(mode, xreal, ctx, g, hop2, diag2, tp, tq, y, ld, m, c0, ck, ph_re, ph_im, lo);
         }
     } else {
         if (site_fast) {
-            if (conj) dispatch_mode<float, true, true>(mode, ctx, g, hop2, diag2, tp, tq, y, ld, m, c0, ck, ph_re, ph_im, lo);
-            else dispatch_mode<float, true, false>(mode, ctx, g, hop2, diag2, tp, tq, y, ld, m, c0, ck, ph_re, ph_im, lo);
+            if (conj) dispatch_mode<float, true, true>(mode, xreal, ctx, g, hop2, diag2, tp, tq, y, ld, m, c0, ck, ph_re, ph_im, lo);
+            else dispatch_mode<float, true, false>(mode, xreal, ctx, g, hop2, diag2, tp, tq, y, ld, m, c0, ck, ph_re, ph_im, lo);
         } else {
-            if (conj) dispatch_mode<float, false, true>(mode, ctx, g, hop2, diag2, tp, tq, y, ld, m, c0, ck, ph_re, ph_im, lo);
-            else dispatch_mode<float, false, false>(mode, ctx, g, hop2, diag2, tp, tq, y, ld, m, c0, ck, ph_re, ph_im, lo);
+            if (conj) dispatch_mode<float, false, true>(mode, xreal, ctx, g, hop2, diag2, tp, tq, y, ld, m, c0, ck, ph_re, ph_im, lo);
+            else dispatch_mode<float, false, false>(mode, xreal, ctx, g, hop2, diag2, tp, tq, y, ld, m, c0, ck, ph_re, ph_im, lo);
         }
     }
     ctx->launches++;

@@ -84,8 +84,9 @@ extern "C" int lm_solver_step_noalloc(lm_solver* s, void* kets, int64_t n, int64
     const double c0 = s->coef[0].s;
     const ChebLo lo = cheb_lo(s->phase_re, s->phase_im, c0, s->coef[1].s, false);
     // T_k overwrites T_{k-2}: even orders land in the caller's block, odd orders in A
+    const bool xr = ham_x_real(s->ham);
     rc = check_cuda(ctx, launch_cheb_order(ctx, g, precision, 1, 0, CHEB_FIRST, hop2, diag2, kets, A, Y, ld, m, c0,
-                                           s->coef[1], s->phase_re, s->phase_im, lo),
+                                           s->coef[1], s->phase_re, s->phase_im, lo, xr),
                     "lm_solver_step_noalloc: order 1");
     if (rc != LM_OK) return rc;
     for (int k = 2; k <= K; ++k) {
@@ -93,7 +94,7 @@ extern "C" int lm_solver_step_noalloc(lm_solver* s, void* kets, int64_t n, int64
         void* tq = (k % 2 == 0) ? kets : A;
         const int mode = (k == K) ? CHEB_LAST : CHEB_MID;
         rc = check_cuda(ctx, launch_cheb_order(ctx, g, precision, 1, 0, mode, hop2, diag2, tp, tq, Y, ld, m, c0,
-                                               s->coef[(size_t)k], s->phase_re, s->phase_im, lo),
+                                               s->coef[(size_t)k], s->phase_re, s->phase_im, lo, xr),
                         "lm_solver_step_noalloc: order");
         if (rc != LM_OK) return rc;
     }

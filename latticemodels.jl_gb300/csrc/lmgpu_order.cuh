@@ -131,7 +131,9 @@ __device__ __forceinline__ void cheb_epilogue(typename CT<R>::V acc, typename CT
     }
 }
 
-template <typename R, int MODE, bool SITE_FAST, bool CONJ, int INNER>
+// XR: every x-hop is real (the Landau gauge, no twist across x), so the x-neighbour terms take
+// 2 FMAs instead of 4; the skipped terms multiply a zero imaginary part.
+template <typename R, int MODE, bool SITE_FAST, bool CONJ, int INNER, bool XR = false>
 __device__ __forceinline__ void cheb_order_block(
     const Geom& g, const typename CT<R>::V* __restrict__ hop2, const R* __restrict__ diag2,
     const typename CT<R>::V* __restrict__ tp, typename CT<R>::V* tq, typename CT<R>::V* y,
@@ -180,10 +182,17 @@ __device__ __forceinline__ void cheb_order_block(
                 const V q = tq[at(site)];
                 acc = CT<R>::make(-q.x, -q.y);
             }
-            acc.x = fma(hxp.x, vxp.x, acc.x); acc.x = fma(-hxp.y, vxp.y, acc.x);
-            acc.y = fma(hxp.x, vxp.y, acc.y); acc.y = fma(hxp.y, vxp.x, acc.y);
-            acc.x = fma(hxm.x, vxm.x, acc.x); acc.x = fma(-hxm.y, vxm.y, acc.x);
-            acc.y = fma(hxm.x, vxm.y, acc.y); acc.y = fma(hxm.y, vxm.x, acc.y);
+            if (XR) {
+                acc.x = fma(hxp.x, vxp.x, acc.x);
+                acc.y = fma(hxp.x, vxp.y, acc.y);
+                acc.x = fma(hxm.x, vxm.x, acc.x);
+                acc.y = fma(hxm.x, vxm.y, acc.y);
+            } else {
+                acc.x = fma(hxp.x, vxp.x, acc.x); acc.x = fma(-hxp.y, vxp.y, acc.x);
+                acc.y = fma(hxp.x, vxp.y, acc.y); acc.y = fma(hxp.y, vxp.x, acc.y);
+                acc.x = fma(hxm.x, vxm.x, acc.x); acc.x = fma(-hxm.y, vxm.y, acc.x);
+                acc.y = fma(hxm.x, vxm.y, acc.y); acc.y = fma(hxm.y, vxm.x, acc.y);
+            }
             acc.x = fma(hyp.x, vyp.x, acc.x); acc.x = fma(-hyp.y, vyp.y, acc.x);
             acc.y = fma(hyp.x, vyp.y, acc.y); acc.y = fma(hyp.y, vyp.x, acc.y);
             acc.x = fma(hym.x, vym.x, acc.x); acc.x = fma(-hym.y, vym.y, acc.x);

@@ -363,24 +363,35 @@ def test_fp32_long_run_keeps_norm(lm, fused):
     assert rel(rho32, rho64) <= 1e-6
 
 
-def test_fused_real_x_hops_bit_identical(lm):
-    """Landau-gauge x-hops are real, so the fused kernel skips their imaginary parts.  Adding a
-    zero point flux keeps H identical but forces the general (complex x-hop) kernel: the two
-    results must agree bit for bit."""
-    L, M, dt = 64, 24, 0.05
+@pytest.mark.parametrize("form", ["c32-fused", "c32-per-order", "c64", "c64-density"])
+def test_real_x_hops_bit_identical(lm, form):
+    """Landau-gauge x-hops are real, so the kernels skip their imaginary parts (the fused c32
+    step and the per-order kernels of either precision).  Adding a zero point flux keeps H
+    identical but forces the general (complex x-hop) kernels: the two results must agree bit
+    for bit, kets and density matrices (whose row pass uses conj(H))."""
+    L, M, dt = (16, 24, 0.05) if form == "c64-density" else (64, 24, 0.05)
     ll = lm.SquareLattice(L, L, boundaries={"axis1": True, "axis2": True})
     V = o.anderson_disorder(L * L, 2.0, 31)
     X = o.random_kets(L * L, M, 32)
+    P = X @ X.conj().T / M
+    ctx = lm.default_context()
     outs = []
-    for field in (lm.LandauGauge(0.02),
-                  lm.FieldSum([lm.LandauGauge(0.02), lm.PointFlux(0.0, (10.5, 20.5), "singular")])):
-        H = lm.tightbinding_hamiltonian(ll, V, field=field)
-        st = lm.KetBlock(ll, X, precision="c32")
-        s = lm.ChebyshevGPU()
-        s.update_solver(H, dt)
-        for _ in range(3):
-            s.step(st)
-        outs.append(st.to_numpy())
+    try:
+        ctx.set_fused(form != "c32-per-order")
+        for field in (lm.LandauGauge(0.02),
+                      lm.FieldSum([lm.LandauGauge(0.02), lm.PointFlux(0.0, (10.5, 20.5), "singular")])):
+            H = lm.tightbinding_hamiltonian(ll, V, field=field)
+            if form == "c64-density":
+                st = lm.DensityMatrix(ll, P)
+            else:
+                st = lm.KetBlock(ll, X, precision="c64" if form == "c64" else "c32")
+            s = lm.ChebyshevGPU()
+            s.update_solver(H, dt)
+            for _ in range(3):
+                s.step(st)
+            outs.append(st.to_numpy())
+    finally:
+        ctx.set_fused(True)
     assert np.array_equal(outs[0], outs[1])
 
 
