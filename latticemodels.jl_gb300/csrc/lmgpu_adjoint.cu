@@ -31,7 +31,8 @@ namespace lmgpu {
 // out = alpha * (2H~) tp - tpp + w * lam   (tables hold 2H/a and 2(V-b)/a; tpp, lam optional)
 // w = conj(c_k): (s, 0) for even k, (0, s) for odd k (conj(-i s) = i s).
 // With y non-null, also y += cy * out (the real-coefficient Chebyshev series of lm_cheb_apply).
-template <typename R>
+// XR: every x-hop is real, so the x-neighbour terms take 2 FMAs instead of 4.
+template <typename R, bool XR>
 __global__ void __launch_bounds__(256) adj_recur_kernel(Geom g, const typename CT<R>::V* __restrict__ hop2,
                                                         const R* __restrict__ diag2,
                                                         const typename CT<R>::V* __restrict__ tp,
@@ -56,10 +57,17 @@ __global__ void __launch_bounds__(256) adj_recur_kernel(Geom g, const typename C
         V acc = z;
         if (tp) {
             const V v0 = tp[o + s], vxp = tp[o + nb.xp], vxm = tp[o + nb.xm], vyp = tp[o + nb.yp], vym = tp[o + nb.ym];
-            acc.x = fma(hxp.x, vxp.x, acc.x); acc.x = fma(-hxp.y, vxp.y, acc.x);
-            acc.y = fma(hxp.x, vxp.y, acc.y); acc.y = fma(hxp.y, vxp.x, acc.y);
-            acc.x = fma(hxm.x, vxm.x, acc.x); acc.x = fma(-hxm.y, vxm.y, acc.x);
-            acc.y = fma(hxm.x, vxm.y, acc.y); acc.y = fma(hxm.y, vxm.x, acc.y);
+            if (XR) {
+                acc.x = fma(hxp.x, vxp.x, acc.x);
+                acc.y = fma(hxp.x, vxp.y, acc.y);
+                acc.x = fma(hxm.x, vxm.x, acc.x);
+                acc.y = fma(hxm.x, vxm.y, acc.y);
+            } else {
+                acc.x = fma(hxp.x, vxp.x, acc.x); acc.x = fma(-hxp.y, vxp.y, acc.x);
+                acc.y = fma(hxp.x, vxp.y, acc.y); acc.y = fma(hxp.y, vxp.x, acc.y);
+                acc.x = fma(hxm.x, vxm.x, acc.x); acc.x = fma(-hxm.y, vxm.y, acc.x);
+                acc.y = fma(hxm.x, vxm.y, acc.y); acc.y = fma(hxm.y, vxm.x, acc.y);
+            }
             acc.x = fma(hyp.x, vyp.x, acc.x); acc.x = fma(-hyp.y, vyp.y, acc.x);
             acc.y = fma(hyp.x, vyp.y, acc.y); acc.y = fma(hyp.y, vyp.x, acc.y);
             acc.x = fma(hym.x, vym.x, acc.x); acc.x = fma(-hym.y, vym.y, acc.x);
@@ -93,19 +101,21 @@ __global__ void __launch_bounds__(256) adj_recur_kernel(Geom g, const typename C
 // and its adjoint; KPM uses it for the moments).  out may alias tpp.
 cudaError_t launch_stencil_recur(lm_ctx* ctx, const Geom& g, int precision, const void* hop2, const void* diag2,
                                  const void* tp, const void* tpp, const void* lam, void* out, int64_t ld, int64_t M,
-                                 double alpha, double wre, double wim, void* y, double cy) {
+                                 double alpha, double wre, double wim, void* y, double cy, bool xreal) {
     if (M <= 0 || g.N <= 0) return cudaSuccess;
     const dim3 grid((unsigned)((g.N + 255) / 256), (unsigned)(M < 65535 ? M : 65535));
-    if (precision == LM_C64)
-        adj_recur_kernel<double><<<grid, 256, 0, ctx->stream>>>(g, (const double2*)hop2, (const double*)diag2,
-                                                                (const double2*)tp, (const double2*)tpp,
-                                                                (const double2*)lam, (double2*)out, ld, M, alpha, wre,
-                                                                wim, (double2*)y, cy);
-    else
-        adj_recur_kernel<float><<<grid, 256, 0, ctx->stream>>>(g, (const float2*)hop2, (const float*)diag2,
-                                                               (const float2*)tp, (const float2*)tpp,
-                                                               (const float2*)lam, (float2*)out, ld, M, (float)alpha,
-                                                               (float)wre, (float)wim, (float2*)y, (float)cy);
+#define LM_RECUR(R, V, XRV)                                                                                   \
+    adj_recur_kernel<R, XRV><<<grid, 256, 0, ctx->stream>>>(g, (const V*)hop2, (const R*)diag2, (const V*)tp, \
+                                                           (const V*)tpp, (const V*)lam, (V*)out, ld, M,        \
+                                                           (R)alpha, (R)wre, (R)wim, (V*)y, (R)cy)
+    if (precision == LM_C64) {
+        if (xreal) LM_RECUR(double, double2, true);
+        else LM_RECUR(double, double2, false);
+    } else {
+        if (xreal) LM_RECUR(float, float2, true);
+        else LM_RECUR(float, float2, false);
+    }
+#undef LM_RECUR
     ctx->launches++;
     return cudaGetLastError();
 }

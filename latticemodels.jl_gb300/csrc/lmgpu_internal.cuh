@@ -284,7 +284,8 @@ cudaError_t launch_ell_op_currents(lm_ctx* ctx, const lm_ell* h, const lm_state*
 // lam may be null; out may alias tpp; with y non-null also y += cy out (lmgpu_adjoint.cu).
 cudaError_t launch_stencil_recur(lm_ctx* ctx, const Geom& g, int precision, const void* hop2, const void* diag2,
                                  const void* tp, const void* tpp, const void* lam, void* out, int64_t ld, int64_t M,
-                                 double alpha, double wre, double wim, void* y = nullptr, double cy = 0.0);
+                                 double alpha, double wre, double wim, void* y = nullptr, double cy = 0.0,
+                                 bool xreal = false);
 cudaError_t launch_convert(lm_ctx* ctx, int to_precision, const void* src, void* dst, int64_t n,
                            int64_t m, int64_t ld_src, int64_t ld_dst);
 

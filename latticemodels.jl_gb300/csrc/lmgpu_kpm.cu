@@ -228,7 +228,9 @@ int lm_kpm_moments(lm_ham* h, double emin, double emax, int nmom, const lm_state
     if (e != cudaSuccess) return fail(e, "lm_kpm_moments: starting block");
     const unsigned dgrid = (unsigned)(M < 65535 ? M : 65535);
     // T_1 = H~ T_0
-    e = launch_stencil_recur(ctx, g, LM_C64, hop2, diag2, TA, nullptr, nullptr, TB, ld, M, 0.5, 0.0, 0.0);
+    const bool xr = ham_x_real(h);
+    e = launch_stencil_recur(ctx, g, LM_C64, hop2, diag2, TA, nullptr, nullptr, TB, ld, M, 0.5, 0.0, 0.0, nullptr, 0.0,
+                             xr);
     if (e != cudaSuccess) return fail(e, "lm_kpm_moments: recurrence");
     double2* Tn = TA;   // T_n
     double2* Tn1 = TB;  // T_{n+1}
@@ -241,7 +243,8 @@ int lm_kpm_moments(lm_ham* h, double emin, double emax, int nmom, const lm_state
         if (e != cudaSuccess) return fail(e, "lm_kpm_moments: dots");
         if (n == nsteps) break;
         // T_{n+2} = 2 H~ T_{n+1} - T_n, written over T_n
-        e = launch_stencil_recur(ctx, g, LM_C64, hop2, diag2, Tn1, Tn, nullptr, Tn, ld, M, 1.0, 0.0, 0.0);
+        e = launch_stencil_recur(ctx, g, LM_C64, hop2, diag2, Tn1, Tn, nullptr, Tn, ld, M, 1.0, 0.0, 0.0, nullptr,
+                                 0.0, xr);
         if (e != cudaSuccess) return fail(e, "lm_kpm_moments: recurrence");
         std::swap(Tn, Tn1);
     }
@@ -343,14 +346,15 @@ int lm_cheb_apply(lm_ham* h, double emin, double emax, const double* coef, int n
     if (e != cudaSuccess) return fail(e, "lm_cheb_apply: first term");
     if (ncoef > 1) {
         // T_1 = H~ T_0, Y += c_1 T_1; then T_{n+1} = 2 H~ T_n - T_{n-1} over T_{n-1}, Y += c_{n+1} T_{n+1}
+        const bool xr = ham_x_real(h);
         e = launch_stencil_recur(ctx, g, LM_C64, hop2, diag2, TA, nullptr, nullptr, TB, ld, M, 0.5, 0.0, 0.0, Y,
-                                 coef[1]);
+                                 coef[1], xr);
         if (e != cudaSuccess) return fail(e, "lm_cheb_apply: recurrence");
         double2* Tprev = TA;
         double2* Tn = TB;
         for (int k = 2; k < ncoef; ++k) {
             e = launch_stencil_recur(ctx, g, LM_C64, hop2, diag2, Tn, Tprev, nullptr, Tprev, ld, M, 1.0, 0.0, 0.0, Y,
-                                     coef[k]);
+                                     coef[k], xr);
             if (e != cudaSuccess) return fail(e, "lm_cheb_apply: recurrence");
             std::swap(Tprev, Tn);
         }
@@ -423,7 +427,8 @@ int lm_ham_lanczos_bounds(lm_ham* h, int iters, unsigned long long seed, double*
     };
     for (int j = 0; j < m; ++j) {
         // w = H v_j - beta_{j-1} v_{j-1}
-        e = launch_stencil_recur(ctx, g, LM_C64, hop2, diag2, A, B, nullptr, Cw, N, 1, 1.0, 0.0, 0.0);
+        e = launch_stencil_recur(ctx, g, LM_C64, hop2, diag2, A, B, nullptr, Cw, N, 1, 1.0, 0.0, 0.0, nullptr, 0.0,
+                                 ham_x_real(h));
         double alpha = 0.0, bsq = 0.0;
         if (e == cudaSuccess) e = read_dot(A, Cw, &alpha);
         if (e == cudaSuccess) {
