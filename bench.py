@@ -42,8 +42,9 @@ DT = 0.05
 B_FIELD = 0.01
 W_DISORDER = 2.0
 SEED = 20261203
-WORKLOAD = ("SquareLattice(256,256) periodic x/y, t1=1, LandauGauge(0.01), Anderson U[-1,1], "
-            "M=2048 complex-Gaussian kets, dt=0.05")
+WORKLOAD_FMT = ("SquareLattice({L},{L}) periodic x/y, t1=1, LandauGauge(0.01), Anderson U[-1,1], "
+                "M={M} complex-Gaussian kets, dt=0.05")
+WORKLOAD = WORKLOAD_FMT.format(L=LX, M=M_KETS)
 
 
 # ------------------------------------------------------------------------------------------
@@ -534,6 +535,8 @@ def main():
     ap.add_argument("--precision", default="c32", choices=["c32", "c64"])
     ap.add_argument("--adjoint-init", default="eigh", choices=["eigh", "random"],
                     help="initial kets of the adjoint workload: lowest eigenstates (default) or random")
+    ap.add_argument("--L", type=int, default=256,
+                    help="kets workload: side of the periodic square lattice (512 with --kets 1024 is config 3)")
     ap.add_argument("--fused-form", default="stream", choices=["stream", "region"],
                     help="form of the fused c32 step: x-streaming (where the lattice allows) or region")
     ap.add_argument("--tol32", type=float, default=1e-9,
@@ -542,6 +545,9 @@ def main():
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    global LX, LY, WORKLOAD
+    LX = LY = int(args.L)
+    WORKLOAD = WORKLOAD_FMT.format(L=LX, M=args.kets)
     if args.impl == "reference":
         return run_reference_arm(args)
     if args.workload == "batch":

@@ -435,6 +435,10 @@ STREAM_CASES = [
     (40, 64, True, True, "pointflux", 0.03, 5),   # periodic 64 rows, complex hops: strips
     (41, 30, False, False, "landau", 0.05, 5),    # Ly < 64 open: lanes outside the lattice
     (33, 50, True, False, "landau", 0.05, 3),
+    (15, 64, True, True, "landau", 0.05, 6),      # Lx = 2K + 3 (K = 6): the smallest streaming Lx
+    (14, 64, True, True, "landau", 0.05, 6),      # Lx = 2K + 2: region form
+    (20, 2, True, True, "landau", 0.05, 5),       # a 2-row periodic ring (both y-bonds join one pair)
+    (18, 4, False, True, "landau", 0.05, 4),      # a 4-row periodic ring, open x
     (64, 31, True, True, "landau", 0.05, 4),      # odd Ly: region form only
     (12, 64, True, True, "landau", 0.05, 4),      # Lx < 2K + 3: region form only
 ]
