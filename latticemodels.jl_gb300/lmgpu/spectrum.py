@@ -47,16 +47,19 @@ def diagonalize(H: Hamiltonian):
     return w.cpu().numpy(), V
 
 
-def densfun(T: float, mu: float):
-    """FermiDirac occupation; at T = 0, E == mu counts as occupied (src/spectrum.jl:230-232)."""
+def densfun(T: float, mu: float, statistics: str = "FermiDirac"):
+    """E -> (E - mu == T == 0) ? 1 : 1 / (exp((E - mu)/T) + s), s = +1 FermiDirac, -1
+    BoseEinstein (src/spectrum.jl:230-232).  At T = 0 a level below mu gets 1/s."""
+    sgn = 1.0 if statistics == "FermiDirac" else -1.0
+
     def f(E):
         d = E - mu
         if d == 0 and T == 0:
             return 1.0
         if T == 0:
-            return 1.0 if d < 0 else 0.0
+            return 1.0 / sgn if d < 0 else 0.0
         z = d / T
-        return 1.0 / (math.exp(z) + 1.0) if z < 700 else 0.0
+        return 1.0 / (math.exp(z) + sgn) if z < 700 else 0.0
     return f
 
 
@@ -86,17 +89,83 @@ def fermi_occupation(mu: float, T: float):
     return lambda E: 0.5 * (1.0 - np.tanh((np.asarray(E) - mu) / (2.0 * T)))
 
 
-def densitymatrix(H: Hamiltonian, mu: float = 0.0, T: float = 0.0, precision="c64", method: str = "auto",
-                  tol: float = 1e-13, bounds: str = "gershgorin") -> DensityMatrix:
-    """``densitymatrix(H; mu, T)`` for a one-particle system with FermiDirac statistics
-    (src/spectrum.jl:252-257).  method: "auto" (Chebyshev for T > 0, eigensolver for T = 0),
-    "chebyshev" or "eigh".  bounds: the spectral interval of the Chebyshev route,
-    "gershgorin" or "lanczos" (tighter: fewer terms)."""
+_STATISTICS = ("FermiDirac", "BoseEinstein")
+
+
+def occupations(w, mu=None, T: float = 0.0, N=None, statistics=None) -> np.ndarray:
+    """Weights f(E_i) of the eigenvalues ``w`` (ascending) that ``densitymatrix`` puts on the
+    eigenvectors, following the reference's dispatch for a one-particle system
+    (src/spectrum.jl:239-333):
+    * ``N``: fixn_densitymatrix -- at T = 0 the Fermi sphere (the lowest N states) or, for
+      BoseEinstein, N times the ground state; at T > 0 mu from the reference's Newton
+      iteration on the eigenvalues (start 0, step (N_ev - N)/dN_ev, atol sqrt(eps));
+    * ``mu`` or ``statistics``: ensemble_densitymatrix, densfun(T, mu, statistics);
+    * neither: gibbs_densitymatrix -- the ground state at T = 0, else exp(-E/T)/Z (shifted by
+      the lowest level, which gives the same weights without overflow)."""
+    import warnings
+    w = np.asarray(w, dtype=np.float64)
+    stat = statistics or "FermiDirac"
+    if stat not in _STATISTICS:
+        raise ValueError("statistics must be FermiDirac or BoseEinstein")
+    if N is not None:
+        if mu is not None:
+            raise ValueError("cannot specify both N and μ")
+        N = int(N)
+        occ = np.zeros(len(w))
+        if abs(T) < 1e-10:
+            if stat == "BoseEinstein":
+                occ[0] = N
+                return occ
+            if len(w) < N:
+                raise ValueError(f"cannot build Fermi sphere with {N} particles: only {len(w)} bands present")
+            if N < len(w) and math.isclose(w[N - 1], w[N], rel_tol=math.sqrt(np.finfo(float).eps)):
+                warnings.warn("degenerate levels on the Fermi sphere")
+            occ[:N] = 1.0
+            return occ
+        newmu = 0.0
+        sgn = 1.0 if stat == "FermiDirac" else -1.0
+        for _ in range(1000):
+            z = np.minimum((w - newmu) / T, 700.0)
+            ez = np.exp(z)
+            n_ev = np.sum(np.where(z >= 700.0, 0.0, 1.0 / (ez + sgn)))
+            dn_ev = np.sum(np.where(z >= 700.0, 0.0, -ez / T / (ez + sgn) ** 2))
+            dmu = (n_ev - N) / dn_ev
+            if abs(dmu) < math.sqrt(np.finfo(float).eps):
+                f = densfun(T, newmu, stat)
+                return np.array([f(e) for e in w])
+            newmu += dmu
+        raise ValueError("did not converge")
+    if mu is not None or statistics is not None:
+        f = densfun(T, 0.0 if mu is None else mu, stat)
+        return np.array([f(e) for e in w])
+    occ = np.zeros(len(w))
+    if abs(T) < 1e-10:
+        occ[0] = 1.0
+        return occ
+    occ = np.exp(-(w - w[0]) / T)
+    return occ / occ.sum()
+
+
+def densitymatrix(H: Hamiltonian, mu=None, T: float = 0.0, *, N=None, statistics=None, precision="c64",
+                  method: str = "auto", tol: float = 1e-13, bounds: str = "gershgorin") -> DensityMatrix:
+    """``densitymatrix(H; mu, T, N, statistics)`` of a one-particle system (src/spectrum.jl:239-333;
+    the dispatch is ``occupations``).  The FermiDirac ensemble at T > 0 runs the Chebyshev
+    Fermi operator on the device (``lm_cheb_apply``) unless method="eigh"; every other case
+    weights the device eigensystem (cuSOLVER).  bounds: the spectral interval of the
+    Chebyshev route, "gershgorin" or "lanczos" (tighter: fewer terms)."""
     if method not in ("auto", "chebyshev", "eigh"):
         raise ValueError("method must be auto, chebyshev or eigh")
-    if method == "chebyshev" and not T > 0:
-        raise ValueError("the Chebyshev route needs T > 0 (the T = 0 occupation is a step)")
-    if T > 0 and method != "eigh":
+    if N is not None and mu is not None:
+        raise ValueError("cannot specify both N and μ")
+    stat = statistics or "FermiDirac"
+    if stat not in _STATISTICS:
+        raise ValueError("statistics must be FermiDirac or BoseEinstein")
+    fermi_ensemble = N is None and (mu is not None or statistics is not None) and stat == "FermiDirac"
+    if method == "chebyshev" and not (fermi_ensemble and T > 0):
+        raise ValueError("the Chebyshev route covers the FermiDirac ensemble at T > 0 (the T = 0 occupation "
+                         "is a step)")
+    if fermi_ensemble and T > 0 and method != "eigh":
+        mu = 0.0 if mu is None else mu
         ctx = default_context()
         lo, hi = H.bounds(ctx, method=bounds)
         pad = 1e-3 * (hi - lo)
@@ -109,8 +178,7 @@ def densitymatrix(H: Hamiltonian, mu: float = 0.0, T: float = 0.0, precision="c6
         return out
     torch = _torch_cuda()
     w, V = diagonalize(H)
-    f = densfun(T, mu)
-    occ = torch.as_tensor(np.array([f(e) for e in w]), device="cuda", dtype=torch.float64)
+    occ = torch.as_tensor(occupations(w, mu, T, N, statistics), device="cuda", dtype=torch.float64)
     P = (V * occ) @ V.conj().T
     if precision == "c32":
         P = P.to(torch.complex64)

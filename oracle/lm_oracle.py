@@ -412,15 +412,73 @@ def diagonalize(H):
     return vals[order], vecs[:, order]
 
 
-def densfun(T: float, mu: float):
-    """src/spectrum.jl:230-232 with FermiDirac statistics."""
+def densfun(T: float, mu: float, statistics: str = "FermiDirac"):
+    """src/spectrum.jl:230-232: E -> (E - mu == T == 0) ? 1 : 1 / (exp((E - mu)/T) + s) with
+    s = Int(statistics): +1 FermiDirac, -1 BoseEinstein."""
+    sgn = 1.0 if statistics == "FermiDirac" else -1.0
+
     def f(E):
         if E - mu == 0 and T == 0:
             return 1.0
         with np.errstate(over="ignore", divide="ignore"):
             z = (E - mu) / T if T != 0 else (math.inf if E > mu else -math.inf)
-        return 1.0 / (math.exp(z) + 1) if z < 700 else 0.0
+        return 1.0 / (math.exp(z) + sgn) if z < 700 else 0.0
     return f
+
+
+def ddensfun(T: float, mu: float, statistics: str = "FermiDirac"):
+    """src/spectrum.jl:233-235: d f / d mu ... as the reference writes it: -e^z / T / (e^z + s)^2."""
+    sgn = 1.0 if statistics == "FermiDirac" else -1.0
+
+    def f(E):
+        z = (E - mu) / T
+        if z > 700:
+            return 0.0
+        ez = math.exp(z)
+        return -ez / T / (ez + sgn) ** 2
+    return f
+
+
+def densitymatrix_dispatch(H, mu=None, T: float = 0.0, N=None, statistics=None):
+    """``densitymatrix(ham; kw...)`` of a one-particle system (src/spectrum.jl:226-333):
+    * N given: fixn_densitymatrix -- at T = 0 the Fermi sphere (the lowest N states;
+      BoseEinstein: N times the ground state), else mu by the reference's Newton iteration on
+      the eigenvalues (start 0, step (N_ev - N) / dN_ev, atol sqrt(eps), 1000 iterations);
+    * mu or statistics given: ensemble_densitymatrix with densfun(T, mu, statistics);
+    * neither: gibbs_densitymatrix -- the ground state at T = 0 (|T| < 1e-10), else
+      exp(-E/T)/Z (evaluated here as exp(-(E - E_min)/T)/Z', the same matrix)."""
+    vals, vecs = diagonalize(H)
+    stat = statistics or "FermiDirac"
+    if N is not None:
+        if mu is not None:
+            raise ValueError("cannot specify both N and mu")
+        if abs(T) < 1e-10:
+            if stat == "BoseEinstein":
+                return np.outer(vecs[:, 0], vecs[:, 0].conj()) * N
+            if len(vals) < N:
+                raise ValueError(f"cannot build Fermi sphere with {N} particles: only {len(vals)} bands present")
+            V = vecs[:, :N]
+            return V @ V.conj().T
+        newmu = 0.0
+        for _ in range(1000):
+            f, df = densfun(T, newmu, stat), ddensfun(T, newmu, stat)
+            n_ev = sum(f(e) for e in vals)
+            dn_ev = sum(df(e) for e in vals)
+            dmu = (n_ev - N) / dn_ev
+            if abs(dmu) < math.sqrt(np.finfo(float).eps):
+                w = np.array([densfun(T, newmu, stat)(e) for e in vals])
+                return (vecs * w) @ vecs.conj().T
+            newmu += dmu
+        raise ValueError("did not converge")
+    if mu is not None or statistics is not None:
+        f = densfun(T, 0.0 if mu is None else mu, stat)
+        w = np.array([f(e) for e in vals])
+        return (vecs * w) @ vecs.conj().T
+    if abs(T) < 1e-10:
+        return np.outer(vecs[:, 0], vecs[:, 0].conj())
+    w = np.exp(-(vals - vals[0]) / T)
+    w /= w.sum()
+    return (vecs * w) @ vecs.conj().T
 
 
 def densitymatrix(H, mu: float = 0.0, T: float = 0.0):

@@ -149,3 +149,20 @@ def test_dos_with_lanczos_bounds(lm):
     E = np.linspace(-4, 4, 9)
     d = lm.kpm.dos(Hl, E, 0.1, bounds="lanczos")
     assert np.abs(d - o.dos_eigensystem(w, E, 0.1)).max() <= 1e-9 * d.max()
+
+
+@pytest.mark.parametrize("kw", [dict(), dict(T=0.3), dict(N=20), dict(N=20, T=0.2),
+                                dict(mu=-3.5, T=0.4, statistics="BoseEinstein")],
+                         ids=["gibbs-T0", "gibbs-T", "fermi-sphere", "fixed-N", "bose-ensemble"])
+def test_densitymatrix_dispatch_on_device(lm, kw):
+    """densitymatrix(H; ...) without mu (the Gibbs state), with N (Fermi sphere, fixed N at
+    T > 0) and with BoseEinstein statistics: the device eigensystem weighted by the reference's
+    occupations, against the oracle (src/spectrum.jl:239-333).  Disorder lifts degeneracies."""
+    ol = o.SquareLattice(8, 8)
+    ll = lm.SquareLattice(8, 8)
+    V = o.anderson_disorder(64, 1.5, 11)
+    Ho = o.tightbinding_hamiltonian(ol, field=o.PointFlux(0.2, (4.5, 4.5)), onsite=V)
+    Hl = lm.tightbinding_hamiltonian(ll, V, field=lm.PointFlux(0.2, (4.5, 4.5)))
+    Pref = o.densitymatrix_dispatch(Ho, **kw)
+    P = lm.densitymatrix(Hl, **kw).to_numpy()
+    assert np.abs(P - Pref).max() <= 1e-12 * max(1.0, np.abs(Pref).max())
