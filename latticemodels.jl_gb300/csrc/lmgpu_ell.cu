@@ -79,11 +79,81 @@ __global__ void __launch_bounds__(256) cheb_order_ell_kernel(
     }
 }
 
+// Site-fast form with the row in registers: a thread owns one site, loads its (at most WMAX)
+// stored entries once and applies them to INNER kets (the generic kernel reloads the row for
+// every ket).  Same FMA sequence per site-ket as cheb_order_ell_kernel.
+template <typename R, int MODE, bool CONJ, int WMAX, int INNER>
+__global__ void __launch_bounds__(256) cheb_order_ell_rows_kernel(
+    int64_t n, int w, const int* __restrict__ cols, const typename CT<R>::V* __restrict__ v2,
+    const R* __restrict__ d2, const typename CT<R>::V* __restrict__ tp, typename CT<R>::V* tq,
+    typename CT<R>::V* y, int64_t ld, int64_t M, R c0, R cs, int odd, R ph_re, R ph_im, ChebLo lo) {
+    typedef typename CT<R>::V V;
+    const int64_t site = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (site >= n) return;
+    int c[WMAX];
+    V hv[WMAX];
+#pragma unroll
+    for (int k = 0; k < WMAX; ++k) {
+        if (k < w) {
+            const int64_t e = (int64_t)k * n + site;
+            c[k] = __ldg(cols + e);
+            hv[k] = v2[e];
+            if (CONJ) hv[k].y = -hv[k].y;
+        } else {
+            c[k] = (int)site;
+            hv[k] = CT<R>::make(0, 0);
+        }
+    }
+    const R d = d2[site];
+    for (int64_t k0 = (int64_t)blockIdx.y * INNER; k0 < M; k0 += (int64_t)gridDim.y * INNER) {
+#pragma unroll
+        for (int j = 0; j < INNER; ++j) {
+            const int64_t ket = k0 + j;
+            if (ket >= M) break;
+            const int64_t base = ket * ld;
+            const V v0 = tp[base + site];
+            V acc;
+            if (MODE == CHEB_FIRST) {
+                acc = CT<R>::make(0, 0);
+            } else {
+                const V q = tq[base + site];
+                acc = CT<R>::make(-q.x, -q.y);
+            }
+#pragma unroll
+            for (int k = 0; k < WMAX; ++k) {
+                if (k < w) {
+                    const V h = hv[k];
+                    const V v = tp[base + c[k]];
+                    acc.x = fma(h.x, v.x, acc.x); acc.x = fma(-h.y, v.y, acc.x);
+                    acc.y = fma(h.x, v.y, acc.y); acc.y = fma(h.y, v.x, acc.y);
+                }
+            }
+            acc.x = fma(d, v0.x, acc.x);
+            acc.y = fma(d, v0.y, acc.y);
+            cheb_epilogue<R, MODE>(acc, v0, tq, y, base + site, c0, cs, odd, ph_re, ph_im, lo);
+        }
+    }
+}
+
 template <typename R, int MODE, bool SF, bool CJ>
 static cudaError_t launch_ell_t(lm_ctx* ctx, const lm_ell* h, const void* v2, const void* d2, const void* tp, void* tq,
                                 void* y, int64_t ld, int64_t m, double c0, ChebCoef ck, double pr, double pi,
                                 ChebLo lo) {
     typedef typename CT<R>::V V;
+    if (SF && h->w <= 8) {
+        constexpr int INNER = 4;
+        const dim3 grid((unsigned)((h->n + 255) / 256), (unsigned)std::min<int64_t>((m + INNER - 1) / INNER, 65535));
+        if (h->w <= 4)
+            cheb_order_ell_rows_kernel<R, MODE, CJ, 4, INNER><<<grid, 256, 0, ctx->stream>>>(
+                h->n, h->w, h->d_cols, (const V*)v2, (const R*)d2, (const V*)tp, (V*)tq, (V*)y, ld, m, (R)c0,
+                (R)ck.s, ck.odd, (R)pr, (R)pi, lo);
+        else
+            cheb_order_ell_rows_kernel<R, MODE, CJ, 8, INNER><<<grid, 256, 0, ctx->stream>>>(
+                h->n, h->w, h->d_cols, (const V*)v2, (const R*)d2, (const V*)tp, (V*)tq, (V*)y, ld, m, (R)c0,
+                (R)ck.s, ck.odd, (R)pr, (R)pi, lo);
+        ctx->launches++;
+        return cudaGetLastError();
+    }
     const int thr = 256;
     const int64_t nfast = SF ? h->n : m;
     const int64_t nslow = SF ? m : h->n;
