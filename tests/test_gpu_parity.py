@@ -486,3 +486,29 @@ def test_stream_form_bit_identical_to_region(lm, case):
     for _ in range(3):
         Y = o.expm_multiply(Ho, dt, Y)
     assert rel(outs[True].astype(np.complex128), Y) <= 3e-6
+
+
+def test_stream_form_follows_time_dependent_h(lm):
+    """H(t) changes every step (Landau field ramp and on-site term): the streaming kernel's packed
+    coefficient planes must be rebuilt for every new H.  c32 kets through Evolution against the
+    oracle stepping the same left-endpoint Hamiltonians with the exact exponent."""
+    L, M, dt, nsteps = 32, 6, 0.05, 6
+    ol, ll = pair(lm, L, L, (True, True))
+    rng = np.random.default_rng(77)
+    Vs = [rng.uniform(-1, 1, L * L) for _ in range(nsteps)]
+    B = lambda t: 0.005 + 0.02 * t
+    k_of = lambda t: min(int(round(t / dt)), nsteps - 1)
+    h_l = lambda t: lm.tightbinding_hamiltonian(ll, Vs[k_of(t)], field=lm.LandauGauge(B(t)))
+    h_o = lambda t: o.tightbinding_hamiltonian(ol, field=o.LandauGauge(B(t)), onsite=Vs[k_of(t)])
+    X = o.random_kets(ol.N, M, 78)
+    ctx = lm.default_context()
+    n0 = ctx.stream_launches()
+    ev = lm.Evolution(lm.ChebyshevGPU(), h_l, lm.KetBlock(ll, X, precision="c32"))
+    times = [dt * k for k in range(1, nsteps + 1)]
+    Y = X
+    t0 = 0.0
+    for moment, t in zip(ev(times), times):
+        Y = o.expm_multiply(h_o(t0), t - t0, Y)
+        t0 = t
+        assert rel(moment.state.to_numpy().astype(np.complex128), Y) <= 5e-6
+    assert ctx.stream_launches() - n0 == nsteps
