@@ -20,6 +20,13 @@
 // computes about 1.25 times.  Each site-order uses the same sequence of FMAs as the region
 // form, so the two give bit-identical results.
 //
+// Coefficients come from planes that stream_pack_kernel packs whenever the FP32 stencil
+// tables change: columns padded on both sides (periodic ones wrapped, open ones zero), so an
+// order's record sits at a linear offset with no wrap or bounds logic.  With uniform columns
+// (every hop of a column equal: the Landau gauge without a twist along y, MODE 2/3) a
+// column's hops are one record kept in shared memory for the whole lattice, and an order
+// reads only the diagonal pair of its sites, staged by cp.async together with the ket column.
+//
 // Requirements (checked by stream_supported): Ly even, so every lane's pair is a 16-byte
 // aligned, unsplit pair of sites; Lx >= 2K + 3, so a column index leaves [0, Lx) by less
 // than one lattice length; K <= 6 with real x-hops, K <= 5 otherwise (the register budget of
