@@ -512,3 +512,58 @@ def test_stream_form_follows_time_dependent_h(lm):
         t0 = t
         assert rel(moment.state.to_numpy().astype(np.complex128), Y) <= 5e-6
     assert ctx.stream_launches() - n0 == nsteps
+
+
+def _random_stream_cases(n, seed=2026):
+    rng = np.random.default_rng(seed)
+    cases = []
+    for _ in range(n):
+        Lx = int(rng.integers(15, 70))
+        Ly = int(rng.integers(2, 140))
+        px, py = bool(rng.integers(0, 2)), bool(rng.integers(0, 2))
+        tw = (float(rng.uniform(-1, 1)) if (px and rng.random() < 0.3) else 0.0,
+              float(rng.uniform(-1, 1)) if (py and rng.random() < 0.3) else 0.0)
+        fk = ["landau", "pointflux", "sym"][int(rng.integers(0, 3))]
+        dt = float(rng.choice([0.01, 0.02, 0.035, 0.05]))
+        M = int(rng.integers(1, 12))
+        cases.append((Lx, Ly, px, py, tw, fk, dt, M))
+    return cases
+
+
+@pytest.mark.parametrize("case", _random_stream_cases(16), ids=lambda c: f"{c[0]}x{c[1]}-{c[5]}")
+def test_stream_form_random_geometries(lm, case):
+    """Seeded random shapes, boundaries (with twists), fields and step sizes (so K = 2..6): the
+    fused step in its streaming form (where eligible) and in its region form agree bit for bit,
+    and both follow the exact exponent."""
+    Lx, Ly, px, py, tw, fk, dt, M = case
+    ol, ll = pair(lm, Lx, Ly, (px, py), tw)
+    V = o.anderson_disorder(ol.N, 1.0, Lx * 1000 + Ly)
+    if fk == "landau":
+        fo, fl = o.LandauGauge(0.02), lm.LandauGauge(0.02)
+    elif fk == "sym":
+        fo, fl = o.SymmetricGauge(0.015), lm.SymmetricGauge(0.015)
+    else:
+        pt = (Lx / 2 + 0.3, Ly / 2 + 0.7)
+        fo, fl = o.PointFlux(0.25, pt), lm.PointFlux(0.25, pt)
+    import warnings
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        Ho = o.tightbinding_hamiltonian(ol, field=fo, onsite=V)
+        Hl = lm.tightbinding_hamiltonian(ll, V, field=fl)
+    X = o.random_kets(ol.N, M, 3)
+    ctx = lm.default_context()
+    outs = {}
+    try:
+        for form in (True, False):
+            ctx.set_stream_form(form)
+            st = lm.KetBlock(ll, X, precision="c32")
+            s = lm.ChebyshevGPU()
+            s.update_solver(Hl, dt)
+            for _ in range(2):
+                s.step(st)
+            outs[form] = st.to_numpy()
+    finally:
+        ctx.set_stream_form(True)
+    assert np.array_equal(outs[True], outs[False])
+    Y = o.expm_multiply(Ho, dt, o.expm_multiply(Ho, dt, X))
+    assert rel(outs[True].astype(np.complex128), Y) <= 3e-6
