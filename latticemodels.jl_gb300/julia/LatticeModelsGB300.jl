@@ -223,6 +223,11 @@ function gpu_operator_currents(H::GPUSparseHamiltonian, A::SparseMatrixCSC{Compl
     opm = op === nothing ? Ptr{ComplexF64}(C_NULL) : convert(Matrix{ComplexF64}, op)
     check(ccall((:lm_ell_op_currents, LIB), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Cint, Ptr{ComplexF64}, Ptr{Float64}),
                 H.handle, st.handle, ndof, opm, out), H.ctx.handle)
+    return site_pair_currents(A, out, ndof)
+end
+
+# Per-entry shares (CSC order of A) -> site-pair matrix M[i, j] = curr[i, j].
+function site_pair_currents(A::SparseMatrixCSC, out::AbstractVector{Float64}, ndof::Integer)
     I, J, V = Int[], Int[], Float64[]
     rows = rowvals(A)
     for c in 1:size(A, 2), p in nzrange(A, c)
@@ -260,6 +265,14 @@ function push_currents!(r::ReadoutRing, H::DeviceHamiltonian, st::DeviceState, t
     seq = Ref{Int64}(0)
     check(ccall((:lm_ring_push_currents, LIB), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Cdouble, Ref{Int64}),
                 r.handle, H.handle, st.handle, t, seq), r.ctx.handle)
+    return seq[]
+end
+function push_op_currents!(r::ReadoutRing, H::GPUSparseHamiltonian, st, ndof::Integer, t, op=nothing)
+    seq = Ref{Int64}(0)
+    opm = op === nothing ? Ptr{ComplexF64}(C_NULL) : convert(Matrix{ComplexF64}, op)
+    check(ccall((:lm_ring_push_op_currents, LIB), Cint,
+                (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Cint, Ptr{ComplexF64}, Cdouble, Ref{Int64}),
+                r.handle, H.handle, st.handle, ndof, opm, t, seq), r.ctx.handle)
     return seq[]
 end
 function take!(r::ReadoutRing, seq::Integer, len::Integer)
@@ -301,6 +314,34 @@ function gpu_timesequence(kind::Symbol, ev_iter; nslots=8)
     for seq in pending
         t, v = take!(ring, seq, len)
         push!(ts, t); push!(vals, v)
+    end
+    return LatticeModels.TimeSequence(ts, vals)
+end
+
+"""
+    gpu_operator_timesequence(H, A, ev_iter, ndof; op=nothing, nslots=8)
+
+`TimeSequence(moment -> LocalOperatorCurrents(H, moment.state, op), ev_iter)` for a general
+(sparse) Hamiltonian with ndof internal states per site (src/zoo/currents.jl:150-184); `op ===
+nothing` gives `DensityCurrents`.  The per-entry shares go through a `ReadoutRing`; each is
+summed into site pairs on the host once its slot is taken.
+"""
+function gpu_operator_timesequence(H::GPUSparseHamiltonian, A::SparseMatrixCSC{ComplexF64,Int64}, ev_iter,
+                                   ndof::Integer; op=nothing, nslots=8)
+    ring = ReadoutRing(max(nnz(A), 1), nslots; ctx=H.ctx)
+    pending = Int64[]
+    ts = Float64[]
+    vals = Any[]
+    for moment in ev_iter
+        if length(pending) == nslots
+            t, v = take!(ring, popfirst!(pending), nnz(A))
+            push!(ts, t); push!(vals, site_pair_currents(A, v, ndof))
+        end
+        push!(pending, push_op_currents!(ring, H, moment.state.data, ndof, moment.t, op))
+    end
+    for seq in pending
+        t, v = take!(ring, seq, nnz(A))
+        push!(ts, t); push!(vals, site_pair_currents(A, v, ndof))
     end
     return LatticeModels.TimeSequence(ts, vals)
 end
@@ -422,6 +463,7 @@ function ChainRulesCore.rrule(::typeof(density_loss), V, B, p::DensityLossProble
 end
 
 export ChebyshevGPU, DeviceLattice, DeviceState, gpu_tightbinding, bond_currents, ReadoutRing,
-       gpu_timesequence, GPUBatch, DensityLossProblem, density_loss, GPUSparseHamiltonian, set_values!, gpu_operator_currents
+       gpu_timesequence, GPUBatch, DensityLossProblem, density_loss, GPUSparseHamiltonian, set_values!, gpu_operator_currents,
+       gpu_operator_timesequence
 
 end # module

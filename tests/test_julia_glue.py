@@ -1,0 +1,120 @@
+"""The Julia glue module (julia/LatticeModelsGB300.jl) against the C header include/lmgpu.h.
+
+Julia is not installed here, so the glue cannot be run; these tests read it as text and check
+every `ccall` against the header declaration it binds: the function exists, the number of
+arguments agrees, and each argument and the return value have a Julia type of the right
+width and kind (pointer or scalar).  A wrong count or width in a ccall corrupts the stack on
+the first call, so this is the check that matters most for the glue.
+"""
+import os
+import re
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "lmgpu.h")
+GLUE = os.path.join(ROOT, "latticemodels.jl_gb300", "julia", "LatticeModelsGB300.jl")
+
+# C scalar type -> Julia types of the same width
+SCALARS = {
+    "int": {"Cint", "Int32"},
+    "int64_t": {"Int64"},
+    "double": {"Cdouble", "Float64"},
+    "size_t": {"Csize_t", "UInt64"},
+}
+POINTER_JL = re.compile(r"^(Ptr|Ref)\{.*\}$|^Cstring$")
+
+
+def _strip_comments(text):
+    text = re.sub(r"/\*.*?\*/", " ", text, flags=re.S)
+    return re.sub(r"//[^\n]*", " ", text)
+
+
+def header_decls():
+    text = _strip_comments(open(HEADER).read())
+    decls = {}
+    for m in re.finditer(r"\b((?:const\s+)?[A-Za-z_0-9]+\s*\**)\s*\b(lm_[a-z_0-9]+)\s*\(([^;{]*?)\)\s*;", text, re.S):
+        ret, name, args = m.group(1).strip(), m.group(2), " ".join(m.group(3).split())
+        params = [] if args in ("", "void") else [a.strip() for a in args.split(",")]
+        decls[name] = (ret, params)
+    return decls
+
+
+def _split_top(s):
+    """Split a Julia tuple body at top-level commas."""
+    out, depth, cur = [], 0, ""
+    for ch in s:
+        if ch in "({[":
+            depth += 1
+        elif ch in ")}]":
+            depth -= 1
+        if ch == "," and depth == 0:
+            out.append(cur.strip())
+            cur = ""
+        else:
+            cur += ch
+    if cur.strip():
+        out.append(cur.strip())
+    return out
+
+
+def glue_ccalls():
+    text = open(GLUE).read()
+    calls = []
+    for m in re.finditer(r"ccall\(\(:(lm_[a-z_0-9]+), LIB\),\s*([A-Za-z0-9{}]+),\s*\(", text):
+        # the argument-type tuple starts at m.end() - 1; find its matching parenthesis
+        i, depth = m.end() - 1, 0
+        for j in range(i, len(text)):
+            if text[j] == "(":
+                depth += 1
+            elif text[j] == ")":
+                depth -= 1
+                if depth == 0:
+                    break
+        types = _split_top(text[i + 1:j])
+        line = text.count("\n", 0, m.start()) + 1
+        calls.append((m.group(1), m.group(2), types, line))
+    return calls
+
+
+def _c_kind(ctype):
+    if "*" in ctype:
+        return "ptr", None
+    words = [w for w in ctype.replace("const", " ").split() if w]
+    # a named parameter: "int ndof" -> "int"; an unnamed one: "int"
+    base = words[0] if words else ctype
+    return "scalar", base
+
+
+def test_glue_present_and_has_ccalls():
+    assert os.path.exists(GLUE)
+    assert len(glue_ccalls()) >= 40
+
+
+@pytest.mark.parametrize("name,ret,types,line", glue_ccalls(), ids=lambda v: str(v) if isinstance(v, (str, int)) else None)
+def test_ccall_matches_header(name, ret, types, line):
+    decls = header_decls()
+    assert name in decls, f"line {line}: {name} is not declared in lmgpu.h"
+    cret, params = decls[name]
+    assert len(types) == len(params), \
+        f"line {line}: {name} takes {len(params)} arguments in the header, the ccall passes {len(types)}"
+    kind, base = _c_kind(cret)
+    if kind == "ptr":
+        assert POINTER_JL.match(ret), f"line {line}: {name} returns {cret}, ccall says {ret}"
+    else:
+        assert ret in SCALARS[base], f"line {line}: {name} returns {cret}, ccall says {ret}"
+    for k, (jt, cp) in enumerate(zip(types, params)):
+        kind, base = _c_kind(cp)
+        if kind == "ptr":
+            assert POINTER_JL.match(jt), f"line {line}: {name} argument {k + 1} is '{cp}', ccall passes {jt}"
+        else:
+            assert base in SCALARS, f"{name}: unknown C type {cp}"
+            assert jt in SCALARS[base], f"line {line}: {name} argument {k + 1} is '{cp}', ccall passes {jt}"
+
+
+def test_glue_binds_the_plugin_and_readout_entry_points():
+    bound = {c[0] for c in glue_ccalls()}
+    for fn in ("lm_solver_update", "lm_solver_step", "lm_localdensity", "lm_bond_currents",
+               "lm_ring_push_localdensity", "lm_ring_push_currents", "lm_ring_push_op_currents",
+               "lm_ell_op_currents", "lm_state_upload", "lm_state_download"):
+        assert fn in bound, fn
