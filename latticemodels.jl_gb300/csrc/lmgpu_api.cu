@@ -3,6 +3,7 @@
 // EvolutionSolver plugin (src/evolution.jl:5-33, :83-92, :69-78).
 #include <cuda_runtime.h>
 #include <math.h>
+#include <stdlib.h>
 #include <string.h>
 
 #include <algorithm>
@@ -210,6 +211,7 @@ int lm_ctx_create(int device, lm_ctx** out) {
         return LM_ERR_CUDA;
     }
     cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device);
+    if (const char* v = getenv("LMGPU_READOUT_SLICES")) c->ld_slices_override = std::max(0, std::min(64, atoi(v)));
     *out = c;
     return LM_OK;
 }
@@ -219,6 +221,7 @@ int lm_ctx_destroy(lm_ctx* ctx) {
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
     if (ctx->d_red) cudaFree(ctx->d_red);
+    if (ctx->d_ld_part) cudaFree(ctx->d_ld_part);
     for (cudaEvent_t e : ctx->ev_pool) cudaEventDestroy(e);
     cudaStreamDestroy(ctx->stream);
     delete ctx;

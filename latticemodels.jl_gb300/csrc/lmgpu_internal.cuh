@@ -109,6 +109,9 @@ struct lm_ctx {
     int64_t launches = 0;          // every kernel launched by the library
     double* d_red = nullptr;       // small reduction scratch (owned)
     size_t red_cap = 0;
+    double* d_ld_part = nullptr;   // per-slice partial densities of the ket readout (owned)
+    size_t ld_part_cap = 0;
+    int ld_slices_override = 0;    // LMGPU_READOUT_SLICES: fixed ket-slice count of the readout (0 = chosen)
 };
 
 struct lm_lattice {

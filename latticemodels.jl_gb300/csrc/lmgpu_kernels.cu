@@ -217,23 +217,28 @@ constexpr int kReadWarps = 8;  // warps of a readout block; they split the kets
 
 // localdensity of a ket block: rho_s = sum_k w_k |psi_sk|^2.  A block owns 32*VEC consecutive
 // sites (lane -> VEC sites: c32 with VEC = 8 reads four 16-byte words per ket, so a warp reads
-// 2 KB of one ket at a time); its 8 warps take kets k = warp, warp + 8, ...; the 8 partial
-// sums are added in warp order.
+// 2 KB of one ket at a time) and the kets of slice blockIdx.y, [y*kslice, (y+1)*kslice); its 8
+// warps take kets k = k0 + warp, k0 + warp + 8, ...; the 8 partial sums are added in warp order
+// and written to plane y of out (out + y*n).  With more than one slice, slice_sum_kernel adds
+// the planes in slice order.
 template <typename R, int VEC, bool WEIGHTED>
 __global__ void __launch_bounds__(32 * kReadWarps) localdensity_kets_kernel(
     const typename CT<R>::V* __restrict__ x, int64_t n, int64_t m, int64_t ld, const double* __restrict__ w,
-    double* __restrict__ out) {
+    double* __restrict__ out, int64_t kslice) {
     typedef typename CT<R>::V V;
     __shared__ double red[kReadWarps][32 * VEC];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int64_t s0 = (int64_t)blockIdx.x * (32 * VEC) + (int64_t)lane * VEC;
+    const int64_t k0 = (int64_t)blockIdx.y * kslice;
+    const int64_t k1 = k0 + kslice < m ? k0 + kslice : m;
+    out += (int64_t)blockIdx.y * n;
     Acc<R> acc[VEC];
     double accw[VEC];
 #pragma unroll
     for (int j = 0; j < VEC; ++j) accw[j] = 0.0;
     if (s0 < n) {
 #pragma unroll 4
-        for (int64_t k = warp; k < m; k += kReadWarps) {
+        for (int64_t k = k0 + warp; k < k1; k += kReadWarps) {
             V v[VEC];
             if (VEC >= 2) {
 #pragma unroll
@@ -278,13 +283,73 @@ __global__ void localdensity_dm_kernel(const typename CT<R>::V* __restrict__ x, 
     if (s < n) out[s] = (double)x[s * ld + s].x;
 }
 
-template <typename R, int VEC>
-static void launch_ld_kets(lm_ctx* ctx, const void* x, int64_t n, int64_t m, int64_t ld, const double* w,
-                           double* out) {
+// out[s] = sum over q = 0..S-1, in that order, of part[q*n + s].
+__global__ void slice_sum_kernel(const double* __restrict__ part, int64_t n, int S, double* __restrict__ out) {
+    const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    double t = part[s];
+    for (int q = 1; q < S; ++q) t += part[(int64_t)q * n + s];
+    out[s] = t;
+}
+
+// Number of ket slices for a readout grid of `chunks` site chunks: the most slices whose blocks
+// all fit in one wave of resident blocks, with at least 64 kets (8 per warp) in a slice.  A grid
+// smaller than a wave leaves SMs idle or unevenly loaded (N = 65536 sites: 256 chunks of 256
+// sites against 152 SMs x 4 blocks); a grid of several waves gains nothing on this HBM-bound
+// read and pays the partial planes.  Measured on 256x256 sites x 2048 c32 kets: 0.215 ms with
+// one slice, 0.173 ms with two; on 512x512 x 1024 one slice (1024 chunks) is fastest.
+static int readout_slices(int64_t chunks, int64_t m, int64_t wave) {
+    if (wave <= 0 || chunks <= 0) return 1;
+    const int64_t by_wave = wave / chunks, by_kets = m / 64;
+    return (int)std::max<int64_t>(1, std::min<int64_t>(64, std::min(by_wave, by_kets)));
+}
+
+static cudaError_t ensure_readout_part(lm_ctx* ctx, size_t n) {
+    if (ctx->ld_part_cap >= n) return cudaSuccess;
+    if (ctx->d_ld_part) cudaFree(ctx->d_ld_part);
+    ctx->d_ld_part = nullptr;
+    ctx->ld_part_cap = 0;
+    cudaError_t e = cudaMalloc((void**)&ctx->d_ld_part, n * sizeof(double));
+    if (e == cudaSuccess) ctx->ld_part_cap = n;
+    return e;
+}
+
+template <typename R, int VEC, bool WEIGHTED>
+static cudaError_t launch_ld_kets_w(lm_ctx* ctx, const void* x, int64_t n, int64_t m, int64_t ld, const double* w,
+                                    double* out) {
     typedef typename CT<R>::V V;
-    const unsigned blocks = (unsigned)((n + 32 * VEC - 1) / (32 * VEC));
-    if (w) localdensity_kets_kernel<R, VEC, true><<<blocks, 32 * kReadWarps, 0, ctx->stream>>>((const V*)x, n, m, ld, w, out);
-    else localdensity_kets_kernel<R, VEC, false><<<blocks, 32 * kReadWarps, 0, ctx->stream>>>((const V*)x, n, m, ld, w, out);
+    auto kern = localdensity_kets_kernel<R, VEC, WEIGHTED>;
+    const int64_t chunks = (n + 32 * VEC - 1) / (32 * VEC);
+    static const int per_sm = [] {  // resident blocks per SM of this instantiation
+        int b = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, localdensity_kets_kernel<R, VEC, WEIGHTED>,
+                                                          32 * kReadWarps, 0) != cudaSuccess) {
+            (void)cudaGetLastError();
+            b = 0;
+        }
+        return b;
+    }();
+    int S = readout_slices(chunks, m, (int64_t)per_sm * ctx->sm_count);
+    if (ctx->ld_slices_override > 0) S = ctx->ld_slices_override;
+    if (S > 1 && ensure_readout_part(ctx, (size_t)S * (size_t)n) != cudaSuccess) {
+        (void)cudaGetLastError();  // clear the failed allocation: the single-slice grid needs no scratch
+        S = 1;
+    }
+    const int64_t kslice = (m + S - 1) / S;
+    dim3 grid((unsigned)chunks, (unsigned)S);
+    kern<<<grid, 32 * kReadWarps, 0, ctx->stream>>>((const V*)x, n, m, ld, w, S > 1 ? ctx->d_ld_part : out, kslice);
+    if (S > 1) {
+        slice_sum_kernel<<<(unsigned)((n + 255) / 256), 256, 0, ctx->stream>>>(ctx->d_ld_part, n, S, out);
+        ctx->launches++;
+    }
+    return cudaSuccess;
+}
+
+template <typename R, int VEC>
+static cudaError_t launch_ld_kets(lm_ctx* ctx, const void* x, int64_t n, int64_t m, int64_t ld, const double* w,
+                                  double* out) {
+    return w ? launch_ld_kets_w<R, VEC, true>(ctx, x, n, m, ld, w, out)
+             : launch_ld_kets_w<R, VEC, false>(ctx, x, n, m, ld, w, out);
 }
 
 cudaError_t launch_localdensity(lm_ctx* ctx, int precision, int kind, const void* x, int64_t n, int64_t m,
