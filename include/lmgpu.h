@@ -132,7 +132,11 @@ int lm_state_create(lm_ctx *ctx, int64_t n, int64_t m, int kind, int precision, 
 int lm_state_destroy(lm_state *st);
 /* Host <-> device copies; `host` holds complex values in the state's precision,
  * column-major with leading dimension `ld` (>= n).  lm_state_upload also accepts a device
- * pointer (unified addressing): the copy then stays on the device. */
+ * pointer (unified addressing): the copy then stays on the device.  From pageable memory the
+ * upload has read `host` when it returns; from pinned or device memory it is asynchronous
+ * (ordered on the context's stream, large states split over several copy engines), so keep
+ * that buffer unchanged until a synchronising call (lm_ctx_synchronize, a download, a
+ * readout). */
 int lm_state_upload(lm_state *st, const void *host, int64_t ld);
 int lm_state_download(lm_state *st, void *host, int64_t ld);
 /* Device-to-device copy of `src` into `dst` (same shape, kind and precision): the state
