@@ -72,6 +72,17 @@ __host__ __device__ constexpr int stream_ring_f4(int K) { return ((K + 1) + (K +
 // (same slots as the ket ring) and, per CTA, the column records of the whole lattice.
 __host__ __device__ constexpr int stream_dring_f4(int K) { return (K + 1 + SPF) * 16; }
 constexpr int kStreamSmemMax = 232448;  // bytes of shared memory a CTA may use
+// Column records per lattice column in shared memory: MODE 2 keeps {hx, hxm, hy.re, hy.im};
+// MODE 3 keeps the pair forms {hx, hx, hxm, hxm}, {hy.re, hy.re, hy.im, 0} and their negatives.
+__host__ __device__ constexpr int stream_crec_f4(int mode) { return mode == 3 ? 4 : 1; }
+}  // namespace
+
+// Accumulator coefficients of the paired form (MODE 3): {sigma_k s_k, sigma_k s_k}.
+struct StreamPairs {
+    float2 s2[kStreamMaxK + 1];
+};
+
+namespace {
 
 __device__ __forceinline__ void cp_async16(float4* dst_smem, const void* src, bool valid) {
     const unsigned dst = (unsigned)__cvta_generic_to_shared(dst_smem);
@@ -84,6 +95,17 @@ __device__ __forceinline__ void cp_async8s(float2* dst_smem, const void* src, bo
     asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(dst), "l"(src), "r"(n));
 }
 __device__ __forceinline__ void cp_async_commit_s() { asm volatile("cp.async.commit_group;\n" ::); }
+// d = a * b + c on both halves of a float pair in one instruction (two round-to-nearest FMAs:
+// the same results as two fmaf calls).
+__device__ __forceinline__ float2 ffma2(float2 a, float2 b, float2 c) {
+    float2 d;
+    asm("{\n\t.reg .b64 ra, rb, rc, rd;\n\t"
+        "mov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\tmov.b64 rc, {%6, %7};\n\t"
+        "fma.rn.f32x2 rd, ra, rb, rc;\n\tmov.b64 {%0, %1}, rd;\n\t}"
+        : "=f"(d.x), "=f"(d.y)
+        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y), "f"(c.x), "f"(c.y));
+    return d;
+}
 template <int N>
 __device__ __forceinline__ void cp_async_wait_s() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
 
@@ -182,12 +204,18 @@ __global__ void stream_pack_kernel(const Geom g, const float2* __restrict__ hop2
 // same on a periodic y axis (no edge rows).
 template <int K, int MODE>
 __global__ void __launch_bounds__(SW * 32, 1)
-cheb_stream_c32_kernel(const FusedInst D, const float4* __restrict__ pk, const float2* __restrict__ pd,
-                       const float4* __restrict__ pc, int npair, long long plane, int nty, long long ncols,
-                       long long nwarps) {
+cheb_stream_c32_kernel(const FusedInst D, const StreamPairs SP, const float4* __restrict__ pk,
+                       const float2* __restrict__ pd, const float4* __restrict__ pc, int npair, long long plane,
+                       int nty, long long ncols, long long nwarps) {
     constexpr bool XR = MODE >= 1;
     constexpr bool UC = MODE >= 2;
     constexpr bool YEDGE = MODE == 2;
+    // MODE 3 runs the stencil on float pairs (ffma2).  It keeps S_k = sigma_k T_k with sigma_k = +1
+    // for k mod 4 in {0, 1} and -1 otherwise, so that the T_{k-2} term enters every chain with a
+    // plus sign (sigma_k = -sigma_{k-2}); the hops of order k then carry the sign
+    // sigma_k sigma_{k-1} = (-1)^(k+1), taken from the negated column records for even k.  Round
+    // to nearest is symmetric under negation, so S_k is exactly sigma_k T_k of the other modes.
+    constexpr bool PAIRED = MODE == 3;
     constexpr int H = stream_halo(K);
     constexpr int YR = K + 1;          // accumulator ring: columns x .. x+K in flight
     constexpr int XS = K + 1 + SPF;    // ket ring: column s+SPF staged, column s-K still read
@@ -210,7 +238,17 @@ cheb_stream_c32_kernel(const FusedInst D, const float4* __restrict__ pk, const f
     float4* ctab = smem + SW * (stream_ring_f4(K) + stream_dring_f4(K));
     if (UC) {
         const int Xp = Lx + kPadL + kPadR;
-        for (int i = threadIdx.x; i < Xp; i += SW * 32) ctab[i] = __ldg(pc + i);
+        for (int i = threadIdx.x; i < Xp; i += SW * 32) {
+            const float4 q = __ldg(pc + i);  // {hx, hxm, hy.re, hy.im}
+            if (PAIRED) {
+                ctab[4 * i + 0] = make_float4(q.x, q.x, q.y, q.y);
+                ctab[4 * i + 1] = make_float4(q.z, q.z, q.w, 0.f);
+                ctab[4 * i + 2] = make_float4(-q.x, -q.x, -q.y, -q.y);
+                ctab[4 * i + 3] = make_float4(-q.z, -q.z, -q.w, 0.f);
+            } else {
+                ctab[i] = q;
+            }
+        }
         __syncthreads();
     }
 
@@ -301,9 +339,10 @@ cheb_stream_c32_kernel(const FusedInst D, const float4* __restrict__ pk, const f
                         int dsl = xslot - k;
                         if (dsl < 0) dsl += XS;
                         const float2 qd = dring[dsl * 32 + lane];
-                        const float4 qc = ctab[s - k + kPadL];
                         d[0] = qd.x;
                         d[1] = qd.y;
+                        // MODE 3 reads its paired records in the stencil below
+                        const float4 qc = PAIRED ? make_float4(0.f, 0.f, 0.f, 0.f) : ctab[s - k + kPadL];
                         hx[0] = hx[1] = make_float2(qc.x, 0.f);
                         hxm[0] = hxm[1] = make_float2(qc.y, 0.f);
                         hy[0] = make_float2(qc.z, qc.w);
@@ -357,6 +396,37 @@ cheb_stream_c32_kernel(const FusedInst D, const float4* __restrict__ pk, const f
                     const float2 vym[2] = {up, tc[0]};
 
                     float2 tk[2];
+                    if (PAIRED) {
+                        // signed records of column x: {h hx, h hx, h hxm, h hxm}, {h hy.re, h hy.re, h hy.im, 0}
+                        const float4* cr = ctab + 4 * (s - k + kPadL) + ((k & 1) ? 0 : 2);
+                        const float4 r0 = cr[0], r1 = cr[1];
+                        const float2 px = make_float2(r0.x, r0.y), pxm = make_float2(r0.z, r0.w);
+                        const float2 py = make_float2(r1.x, r1.y);
+                        const float hyi = r1.z;
+                        const float dd[2] = {(k & 1) ? d[0] : -d[0], (k & 1) ? d[1] : -d[1]};
+#pragma unroll
+                        for (int j = 0; j < 2; ++j) {
+                            float2 acc = make_float2(0.f, 0.f);
+                            if (k == 2) {  // S_0 = T_0(x): column s-2 of the ket ring
+                                const float4 q = xring[xs2 * 32 + lane];
+                                acc = j == 0 ? make_float2(q.x, q.y) : make_float2(q.z, q.w);
+                            } else if (k > 2) {
+                                acc = W[k - 2][c2][j];  // S_{k-2}(x)
+                            }
+                            acc = ffma2(px, tp[j], acc);
+                            acc = ffma2(pxm, tm[j], acc);
+                            acc = ffma2(py, vyp[j], acc);
+                            acc.x = fmaf(-hyi, vyp[j].y, acc.x);
+                            acc.y = fmaf(hyi, vyp[j].x, acc.y);
+                            acc = ffma2(py, vym[j], acc);  // the conjugate hop: same real part
+                            acc.x = fmaf(hyi, vym[j].y, acc.x);
+                            acc.y = fmaf(-hyi, vym[j].x, acc.y);
+                            acc.x = fmaf(dd[j], tc[j].x, acc.x);
+                            acc.y = fmaf(dd[j], tc[j].y, acc.y);
+                            if (k == 1) { acc.x *= 0.5f; acc.y *= 0.5f; }
+                            tk[j] = acc;
+                        }
+                    } else
 #pragma unroll
                     for (int j = 0; j < 2; ++j) {
                         float2 acc = make_float2(0.f, 0.f);
@@ -417,7 +487,15 @@ cheb_stream_c32_kernel(const FusedInst D, const float4* __restrict__ pk, const f
 #pragma unroll
                         for (int j = 0; j < 2; ++j) {
                             const float2 t = tk[j];
-                            if (k & 1) {  // c_k = -i s_k
+                            if (PAIRED) {  // t = S_k = sigma_k T_k
+                                const float sks = (k & 2) ? -sk : sk;
+                                if (k & 1) {
+                                    yv[j].x = fmaf(sks, t.y, yv[j].x);
+                                    yv[j].y = fmaf(-sks, t.x, yv[j].y);
+                                } else {
+                                    yv[j] = ffma2(SP.s2[k], t, yv[j]);
+                                }
+                            } else if (k & 1) {  // c_k = -i s_k
                                 yv[j].x = fmaf(sk, t.y, yv[j].x);
                                 yv[j].y = fmaf(-sk, t.x, yv[j].y);
                             } else {      // c_k = s_k
@@ -534,12 +612,12 @@ int ensure_stream_pack(lm_solver* s, const Geom& g) {
 }
 
 static int stream_smem_bytes(int K, int mode, int Xp) {
-    return SW * stream_ring_f4(K) * 16 + (mode >= 2 ? SW * stream_dring_f4(K) * 16 + Xp * 16 : 0);
+    return SW * stream_ring_f4(K) * 16 + (mode >= 2 ? SW * stream_dring_f4(K) * 16 + Xp * 16 * stream_crec_f4(mode) : 0);
 }
 
 template <int MODE>
-static cudaError_t launch_stream_k(lm_ctx* ctx, int K, int grid, const FusedInst& d, const float4* spack, int nty,
-                                   long long ncols, long long nwarps) {
+static cudaError_t launch_stream_k(lm_ctx* ctx, int K, int grid, const FusedInst& d, const StreamPairs& sp,
+                                   const float4* spack, int nty, long long ncols, long long nwarps) {
     int npair, Xp;
     long long plane;
     pack_dims(d.g, &npair, &Xp, &plane);
@@ -556,7 +634,7 @@ static cudaError_t launch_stream_k(lm_ctx* ctx, int K, int grid, const FusedInst
             ctx->stream_attr |= bit;                                                                             \
         }                                                                                                        \
         cheb_stream_c32_kernel<KK, MODE><<<(unsigned)grid, SW * 32, smem, ctx->stream>>>(                       \
-            d, pp.pk, pp.pd, pp.pc, npair, plane, nty, ncols, nwarps);                                           \
+            d, sp, pp.pk, pp.pd, pp.pc, npair, plane, nty, ncols, nwarps);                                           \
         return cudaGetLastError();                                                                               \
     }
         LM_STREAM_CASE(2) LM_STREAM_CASE(3) LM_STREAM_CASE(4) LM_STREAM_CASE(5) LM_STREAM_CASE(6)
@@ -578,10 +656,15 @@ cudaError_t launch_cheb_stream_c32(lm_ctx* ctx, const FusedInst& d, int K, int m
     const int grid = (int)((nwarps + SW - 1) / SW);
     int m = (mode == 2 && d.g.per_y) ? 3 : mode;
     if (m >= 2 && stream_smem_bytes(K, m, (int)d.g.Lx + kPadL + kPadR) > kStreamSmemMax) m = 1;  // very long x
-    const cudaError_t e = m == 3   ? launch_stream_k<3>(ctx, K, grid, d, spack, (int)nty, ncols, nwarps)
-                          : m == 2 ? launch_stream_k<2>(ctx, K, grid, d, spack, (int)nty, ncols, nwarps)
-                          : m == 1 ? launch_stream_k<1>(ctx, K, grid, d, spack, (int)nty, ncols, nwarps)
-                                   : launch_stream_k<0>(ctx, K, grid, d, spack, (int)nty, ncols, nwarps);
+    StreamPairs sp;
+    for (int k = 0; k <= kStreamMaxK; ++k) {
+        const float v = k <= K ? ((k & 2) ? -d.s[k] : d.s[k]) : 0.f;  // sigma_k s_k
+        sp.s2[k] = make_float2(v, v);
+    }
+    const cudaError_t e = m == 3   ? launch_stream_k<3>(ctx, K, grid, d, sp, spack, (int)nty, ncols, nwarps)
+                          : m == 2 ? launch_stream_k<2>(ctx, K, grid, d, sp, spack, (int)nty, ncols, nwarps)
+                          : m == 1 ? launch_stream_k<1>(ctx, K, grid, d, sp, spack, (int)nty, ncols, nwarps)
+                                   : launch_stream_k<0>(ctx, K, grid, d, sp, spack, (int)nty, ncols, nwarps);
     ctx->launches++;
     ctx->stream_launches++;
     return e;
