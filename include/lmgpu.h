@@ -134,7 +134,7 @@ int lm_state_destroy(lm_state *st);
  * column-major with leading dimension `ld` (>= n).  lm_state_upload also accepts a device
  * pointer (unified addressing): the copy then stays on the device.  From pageable memory the
  * upload has read `host` when it returns; from pinned or device memory it is asynchronous
- * (ordered on the context's stream, large states split over several copy engines), so keep
+ * (ordered on the context's stream), so keep
  * that buffer unchanged until a synchronising call (lm_ctx_synchronize, a download, a
  * readout). */
 int lm_state_upload(lm_state *st, const void *host, int64_t ld);

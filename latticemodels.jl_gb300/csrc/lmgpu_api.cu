@@ -212,7 +212,6 @@ int lm_ctx_create(int device, lm_ctx** out) {
     }
     cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device);
     if (const char* v = getenv("LMGPU_READOUT_SLICES")) c->ld_slices_override = std::max(0, std::min(64, atoi(v)));
-    if (const char* v = getenv("LMGPU_UPLOAD_SPLIT")) c->upload_split = std::max(1, std::min(4, atoi(v)));
     *out = c;
     return LM_OK;
 }
@@ -223,10 +222,6 @@ int lm_ctx_destroy(lm_ctx* ctx) {
     cudaStreamSynchronize(ctx->stream);
     if (ctx->d_red) cudaFree(ctx->d_red);
     if (ctx->d_ld_part) cudaFree(ctx->d_ld_part);
-    for (cudaStream_t st : ctx->copy_streams)
-        if (st) cudaStreamDestroy(st);
-    for (cudaEvent_t e : ctx->copy_ev)
-        if (e) cudaEventDestroy(e);
     for (cudaEvent_t e : ctx->ev_pool) cudaEventDestroy(e);
     cudaStreamDestroy(ctx->stream);
     delete ctx;
@@ -653,55 +648,12 @@ int lm_state_destroy(lm_state* s) {
     return LM_OK;
 }
 
-// Side streams and fork/join events of a split upload, created on first use.
-static cudaError_t ensure_copy_streams(lm_ctx* ctx, int parts) {
-    for (int i = 0; i < parts; ++i)
-        if (!ctx->copy_streams[i]) {
-            cudaError_t e = cudaStreamCreateWithFlags(&ctx->copy_streams[i], cudaStreamNonBlocking);
-            if (e != cudaSuccess) return e;
-        }
-    for (int i = 0; i <= parts; ++i)
-        if (!ctx->copy_ev[i]) {
-            cudaError_t e = cudaEventCreateWithFlags(&ctx->copy_ev[i], cudaEventDisableTiming);
-            if (e != cudaSuccess) return e;
-        }
-    return cudaSuccess;
-}
-
-// A state of at least this many bytes is uploaded as several column ranges on side streams,
-// one copy engine each.
-static constexpr size_t kUploadSplitBytes = (size_t)256 << 20;
-
 int lm_state_upload(lm_state* s, const void* host, int64_t ld) {
     if (!s) return LM_ERR_ARG;
     lm_ctx* ctx = s->ctx;
     CHECK_ARG(ctx, host != nullptr, "lm_state_upload: null host buffer");
     CHECK_ARG(ctx, ld >= s->n, "lm_state_upload: leading dimension smaller than n");
     cudaSetDevice(ctx->device);
-    const size_t bytes = s->elem * (size_t)s->n * (size_t)s->m;
-    const int parts = (int)std::min<int64_t>(ctx->upload_split, s->m);
-    bool split = parts > 1 && bytes >= kUploadSplitBytes;
-    if (split && ensure_copy_streams(ctx, parts) != cudaSuccess) {
-        (void)cudaGetLastError();  // no side streams: one copy on the main stream
-        split = false;
-    }
-    if (split) {
-        // fork: every part waits for the work already queued on the main stream (which may still
-        // read or write the state); join: the main stream waits for every part
-        CUDA_TRY(ctx, cudaEventRecord(ctx->copy_ev[parts], ctx->stream), "upload fork");
-        for (int i = 0; i < parts; ++i) {
-            const int64_t c0 = s->m * i / parts, c1 = s->m * (i + 1) / parts;
-            CUDA_TRY(ctx, cudaStreamWaitEvent(ctx->copy_streams[i], ctx->copy_ev[parts], 0), "upload fork");
-            CUDA_TRY(ctx, cudaMemcpy2DAsync((char*)s->d_data + s->elem * (size_t)s->ld * (size_t)c0, s->elem * (size_t)s->ld,
-                                            (const char*)host + s->elem * (size_t)ld * (size_t)c0, s->elem * (size_t)ld,
-                                            s->elem * (size_t)s->n, (size_t)(c1 - c0), cudaMemcpyDefault,
-                                            ctx->copy_streams[i]),
-                     "upload state");
-            CUDA_TRY(ctx, cudaEventRecord(ctx->copy_ev[i], ctx->copy_streams[i]), "upload join");
-            CUDA_TRY(ctx, cudaStreamWaitEvent(ctx->stream, ctx->copy_ev[i], 0), "upload join");
-        }
-        return LM_OK;
-    }
     CUDA_TRY(ctx, cudaMemcpy2DAsync(s->d_data, s->elem * (size_t)s->ld, host, s->elem * (size_t)ld, s->elem * (size_t)s->n,
                                     (size_t)s->m, cudaMemcpyDefault, ctx->stream),
              "upload state");

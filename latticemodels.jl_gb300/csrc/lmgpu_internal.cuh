@@ -112,11 +112,6 @@ struct lm_ctx {
     double* d_ld_part = nullptr;   // per-slice partial densities of the ket readout (owned)
     size_t ld_part_cap = 0;
     int ld_slices_override = 0;    // LMGPU_READOUT_SLICES: fixed ket-slice count of the readout (0 = chosen)
-    // side streams of large state uploads (created on first use): the copy is split by columns
-    // so that several copy engines move it; events order it after and before the main stream
-    cudaStream_t copy_streams[4] = {nullptr, nullptr, nullptr, nullptr};
-    cudaEvent_t copy_ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
-    int upload_split = 4;          // LMGPU_UPLOAD_SPLIT: side streams of a large upload (1 = one copy)
 };
 
 struct lm_lattice {
