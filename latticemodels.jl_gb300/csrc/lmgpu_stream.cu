@@ -216,6 +216,9 @@ cheb_stream_c32_kernel(const FusedInst D, const StreamPairs SP, const float4* __
     // sigma_k sigma_{k-1} = (-1)^(k+1), taken from the negated column records for even k.  Round
     // to nearest is symmetric under negation, so S_k is exactly sigma_k T_k of the other modes.
     constexpr bool PAIRED = MODE == 3;
+    // orders per accumulator update: 3 with uniform columns; 1 (an update per order) in the
+    // per-site coefficient modes, whose windows leave no registers to hold T_j longer
+    constexpr int AG = UC ? 3 : 1;
     constexpr int H = stream_halo(K);
     constexpr int YR = K + 1;          // accumulator ring: columns x .. x+K in flight
     constexpr int XS = K + 1 + SPF;    // ket ring: column s+SPF staged, column s-K still read
@@ -464,41 +467,63 @@ cheb_stream_c32_kernel(const FusedInst D, const StreamPairs SP, const float4* __
                         W[k][c0][1] = tk[1];
                     }
 
-                    // accumulator of column x
+                    // Accumulator y(x) = sum_k c_k T_k(x), added up in groups of AG orders when
+                    // the last order e of a group has produced column x = s - e: T_j(x) of every
+                    // order j <= e of the group is then still in its window (age e - j < AG <= 3).
+                    // Each column gets the same FMAs in the same order as one update per order
+                    // gives; the shared ring carries y(x) from one group to the next.
+                    if (k % AG != 0 && k != K) continue;
+                    const int gb = ((k - 1) / AG) * AG + 1;  // first order of the group
                     int ys_k = yslot - k;
                     if (ys_k < 0) ys_k += YR;
                     float4* yr = &yring[ys_k * 32 + lane];
-                    const float sk = D.s[k];
+                    // T_jj(x) (S_jj in the paired mode) for gb <= jj <= k
+                    auto tval = [&](int jj, int j) -> float2 {
+                        return jj == k ? tk[j] : (jj == k - 1 ? W[jj][c1][j] : W[jj][c2][j]);
+                    };
                     float2 yv[2];
-                    if (k == 1) {  // y = -i s_1 T1 + g0 T0 + g1 T1
+                    if (gb == 1) {  // y = -i s_1 T1 + g0 T0 + g1 T1
+                        float2 t0[2] = {tc[0], tc[1]};  // T_0(s - 1): order 1's centre column
+                        if (k > 1) {
+                            int x0s = xslot - k;
+                            if (x0s < 0) x0s += XS;
+                            const float4 q0 = xring[x0s * 32 + lane];
+                            t0[0] = make_float2(q0.x, q0.y);
+                            t0[1] = make_float2(q0.z, q0.w);
+                        }
                         const ChebLo lo = D.lo;
+                        const float s1 = D.s[1];
 #pragma unroll
                         for (int j = 0; j < 2; ++j) {
-                            const float2 x0 = tc[j], t = tk[j];
+                            const float2 x0 = t0[j], t = tval(1, j);
                             const float lx = fmaf(lo.g0_re, x0.x, fmaf(-lo.g0_im, x0.y, fmaf(lo.g1_re, t.x, -lo.g1_im * t.y)));
                             const float ly = fmaf(lo.g0_re, x0.y, fmaf(lo.g0_im, x0.x, fmaf(lo.g1_re, t.y, lo.g1_im * t.x)));
-                            yv[j].x = fmaf(sk, t.y, lx);
-                            yv[j].y = fmaf(-sk, t.x, ly);
+                            yv[j].x = fmaf(s1, t.y, lx);
+                            yv[j].y = fmaf(-s1, t.x, ly);
                         }
                     } else {
                         const float4 q = *yr;
                         yv[0] = make_float2(q.x, q.y);
                         yv[1] = make_float2(q.z, q.w);
+                    }
+#pragma unroll
+                    for (int jj = (gb == 1 ? 2 : gb); jj <= k; ++jj) {
+                        const float sk = D.s[jj];
 #pragma unroll
                         for (int j = 0; j < 2; ++j) {
-                            const float2 t = tk[j];
-                            if (PAIRED) {  // t = S_k = sigma_k T_k
-                                const float sks = (k & 2) ? -sk : sk;
-                                if (k & 1) {
+                            const float2 t = tval(jj, j);
+                            if (PAIRED) {  // t = S_jj = sigma_jj T_jj
+                                const float sks = (jj & 2) ? -sk : sk;
+                                if (jj & 1) {
                                     yv[j].x = fmaf(sks, t.y, yv[j].x);
                                     yv[j].y = fmaf(-sks, t.x, yv[j].y);
                                 } else {
-                                    yv[j] = ffma2(SP.s2[k], t, yv[j]);
+                                    yv[j] = ffma2(SP.s2[jj], t, yv[j]);
                                 }
-                            } else if (k & 1) {  // c_k = -i s_k
+                            } else if (jj & 1) {  // c_jj = -i s_jj
                                 yv[j].x = fmaf(sk, t.y, yv[j].x);
                                 yv[j].y = fmaf(-sk, t.x, yv[j].y);
-                            } else {      // c_k = s_k
+                            } else {      // c_jj = s_jj
                                 yv[j].x = fmaf(sk, t.x, yv[j].x);
                                 yv[j].y = fmaf(sk, t.y, yv[j].y);
                             }
