@@ -8,8 +8,11 @@
 // same step.  So each order keeps the last three columns of its T in registers (a rotation
 // of period three), the y-neighbours come from the adjacent lanes by shuffles,
 // and the accumulator y(x) = sum_k c_k T_k(x) waits in a per-warp shared-memory ring of
-// K+1 columns until order K completes it.  Column s + 3 of the ket is staged into a second
-// ring by cp.async while column s is being used.
+// K+1 columns until order K completes it.  With uniform columns it is updated once per group
+// of three orders, from the windows, which still hold T_j(x) of the group's earlier orders.
+// Column s + 3 of the ket is staged into a second ring by cp.async while column s is being
+// used.  On a periodic y axis with uniform columns the stencil runs on (re, im) float pairs
+// (fma.rn.f32x2).
 //
 // Only the y direction has a halo: after K orders the sites K .. 63-K of a strip are exact
 // (at an open lattice edge the strip sits on the edge and writes up to it), while along x a
