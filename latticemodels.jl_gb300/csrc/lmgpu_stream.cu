@@ -47,6 +47,10 @@ namespace lmgpu {
 #ifndef LM_STREAM_WARPS
 #define LM_STREAM_WARPS 16
 #endif
+// 1: the periodic uniform-column mode computes on float pairs (fma.rn.f32x2); 0: scalar FMAs.
+#ifndef LM_STREAM_PAIRED
+#define LM_STREAM_PAIRED 1
+#endif
 // 1: the three-column windows rotate by register moves at the end of every step; 0: the
 // step loop is unrolled three times and the rotation is renaming (more code in flight);
 // 2: unrolled in the uniform-column modes (few coefficient registers), rotating otherwise.
@@ -218,7 +222,7 @@ cheb_stream_c32_kernel(const FusedInst D, const StreamPairs SP, const float4* __
     // plus sign (sigma_k = -sigma_{k-2}); the hops of order k then carry the sign
     // sigma_k sigma_{k-1} = (-1)^(k+1), taken from the negated column records for even k.  Round
     // to nearest is symmetric under negation, so S_k is exactly sigma_k T_k of the other modes.
-    constexpr bool PAIRED = MODE == 3;
+    constexpr bool PAIRED = LM_STREAM_PAIRED && MODE == 3;
     // orders per accumulator update: 3 with uniform columns; 1 (an update per order) in the
     // per-site coefficient modes, whose windows leave no registers to hold T_j longer
     constexpr int AG = UC ? 3 : 1;
