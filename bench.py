@@ -720,6 +720,10 @@ def main():
     else:
         kname = "cheb_fused_c32_kernel (region form: all K orders of one step per launch)"
         traffic = profile_traffic()
+    # the summaries hold the 256x256-site, 2048-ket launch; the traffic grows with sites x kets
+    traffic_scale = (N * M) / (65536.0 * 2048.0)
+    if traffic is not None:
+        traffic *= traffic_scale
     line = {
         "metric": METRIC, "value": value, "unit": "ket-steps/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms32 / args.steps,
@@ -740,6 +744,9 @@ def main():
                      "kernel": kname,
                      "alg_bytes_per_launch": alg_bytes_launch, "avg_launch_ms": avg_launch_ms,
                      "launches_timed": sweeps,
+                     "traffic_source": ("ncu dram__bytes_read.sum + dram__bytes_write.sum of the 256^2 x 2048-ket "
+                                        "launch (512-ket capture x 4), scaled by sites x kets"
+                                        + ("" if traffic_scale == 1.0 else f" (x {traffic_scale:g})")),
                      # the temporally blocked kernel moves ~1.8 block passes per step instead of
                      # the 5 K of the per-order formula: its DRAM rate is far below the peak
                      "dram_gbs": (traffic / (avg_launch_ms / 1000.0) / 1e9) if traffic else None,
