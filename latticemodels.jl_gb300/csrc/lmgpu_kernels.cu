@@ -409,6 +409,8 @@ __global__ void __launch_bounds__(32 * kReadWarps) bond_currents_kets_kernel(
         nb = neighbours(g, s);
         // absent bonds read the site itself (always in bounds) and are not written
         const int64_t jx = nb.hxp ? nb.xp : s, jy = nb.hyp ? nb.yp : s;
+        // unrolled so that four kets' loads are in flight per thread; the sums keep their order
+#pragma unroll 4
         for (int64_t k = warp; k < m; k += kReadWarps) {
             const V b = x[k * ld + s];
             const V cx = x[k * ld + jx], cy = x[k * ld + jy];  // c * conj(b)
