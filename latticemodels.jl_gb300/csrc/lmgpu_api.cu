@@ -212,6 +212,7 @@ int lm_ctx_create(int device, lm_ctx** out) {
     }
     cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device);
     if (const char* v = getenv("LMGPU_READOUT_SLICES")) c->ld_slices_override = std::max(0, std::min(64, atoi(v)));
+    if (const char* v = getenv("LMGPU_CURRENTS_SCALAR")) c->currents_scalar = atoi(v) != 0;
     *out = c;
     return LM_OK;
 }

@@ -112,6 +112,7 @@ struct lm_ctx {
     double* d_ld_part = nullptr;   // per-slice partial densities of the ket readout (owned)
     size_t ld_part_cap = 0;
     int ld_slices_override = 0;    // LMGPU_READOUT_SLICES: fixed ket-slice count of the readout (0 = chosen)
+    int currents_scalar = 0;       // LMGPU_CURRENTS_SCALAR=1: c32 bond currents with one site per lane
 };
 
 struct lm_lattice {

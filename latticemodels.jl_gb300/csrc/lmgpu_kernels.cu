@@ -292,16 +292,28 @@ __global__ void slice_sum_kernel(const double* __restrict__ part, int64_t n, int
     out[s] = t;
 }
 
-// Number of ket slices for a readout grid of `chunks` site chunks: the most slices whose blocks
-// all fit in one wave of resident blocks, with at least 64 kets (8 per warp) in a slice.  A grid
-// smaller than a wave leaves SMs idle or unevenly loaded (N = 65536 sites: 256 chunks of 256
-// sites against 152 SMs x 4 blocks); a grid of several waves gains nothing on this HBM-bound
-// read and pays the partial planes.  Measured on 256x256 sites x 2048 c32 kets: 0.215 ms with
-// one slice, 0.173 ms with two; on 512x512 x 1024 one slice (1024 chunks) is fastest.
+// Number of ket slices S for a readout grid of `chunks` site chunks, `wave` resident blocks:
+// the S <= 8 (at least 64 kets per slice) that minimises waves(chunks S) / S x (1 + 0.06 S).
+// The first factor is the work per SM including the last, partly filled wave; the second the
+// cost of shorter blocks and of the partial planes.  Measured (c32, ms per readout):
+//   density, 256^2 sites x 2048 kets, S = 1 / 2 / 4 / 7 / 19: 0.215 / 0.173 / 0.182 / 0.180 / 0.197
+//     (the rule: 2); 512^2 x 1024: 0.338 / 0.364 / 0.347 / 0.357 / 0.401 (the rule: 1);
+//   bond currents, 256^2 x 2048, S = 1 / 4 / 8: 0.653 / 0.483 / 0.495 (the rule: 4).
+// The model ranks the measured slice counts of each case in the measured order.
 static int readout_slices(int64_t chunks, int64_t m, int64_t wave) {
     if (wave <= 0 || chunks <= 0) return 1;
-    const int64_t by_wave = wave / chunks, by_kets = m / 64;
-    return (int)std::max<int64_t>(1, std::min<int64_t>(64, std::min(by_wave, by_kets)));
+    const int smax = (int)std::max<int64_t>(1, std::min<int64_t>(8, m / 64));
+    int best = 1;
+    double tbest = 1e300;
+    for (int S = 1; S <= smax; ++S) {
+        const double waves = (double)((chunks * S + wave - 1) / wave);
+        const double t = waves / S * (1.0 + 0.06 * S);
+        if (t < tbest * (1.0 - 1e-9)) {
+            tbest = t;
+            best = S;
+        }
+    }
+    return best;
 }
 
 static cudaError_t ensure_readout_part(lm_ctx* ctx, size_t n) {
@@ -463,6 +475,129 @@ __global__ void bond_currents_dm_kernel(Geom g, const double2* __restrict__ hop,
     }
 }
 
+// c32 ket blocks with Ly % 4 == 0: a lane owns 4 consecutive sites of one lattice column, so
+// a warp reads 1 KB of a ket per load (the 256-byte pieces of the kernel above, from kets
+// 512 KB apart, held DRAM to about a quarter of its bandwidth).  The +x neighbours are the
+// same 4 rows of the next column (contiguous); the +y neighbours are the lane's own next sites
+// and, for the fourth, one extra 8-byte load.  Each site gets the products of the kernel above
+// in the same ket order within a slice.  Block y takes the kets of slice y and writes its
+// 4 partial sums per site to plane y of `part`; bond_currents_slices_kernel adds the planes in
+// slice order and writes the bonds.
+template <bool WEIGHTED>
+__global__ void __launch_bounds__(32 * kReadWarps) bond_currents_kets4_kernel(
+    Geom g, const float2* __restrict__ x, int64_t m, int64_t ld, const double* __restrict__ w, int64_t kslice,
+    double* __restrict__ part) {
+    __shared__ double red[kReadWarps][4][128];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int64_t s0 = (int64_t)blockIdx.x * 128 + (int64_t)lane * 4;
+    const int64_t k0 = (int64_t)blockIdx.y * kslice;
+    const int64_t k1 = k0 + kslice < m ? k0 + kslice : m;
+    Acc<float> a[4][4];
+    double aw[4][4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) aw[j][q] = 0.0;
+    if (s0 < g.N) {
+        const int64_t xi = s0 / g.Ly, yi0 = s0 - xi * g.Ly;
+        // +x: the same rows of the next column (absent bonds read the sites themselves and are
+        // not written); +y of the fourth site: the next row, the column start, or itself
+        const int64_t jx = xi + 1 < g.Lx ? s0 + g.Ly : (g.per_x ? yi0 : s0);
+        const int64_t jy3 = yi0 + 4 < g.Ly ? s0 + 4 : (g.per_y ? s0 - yi0 : s0 + 3);
+#pragma unroll 2
+        for (int64_t k = k0 + warp; k < k1; k += kReadWarps) {
+            const float4* xb = reinterpret_cast<const float4*>(x + k * ld + s0);
+            const float4* xc = reinterpret_cast<const float4*>(x + k * ld + jx);
+            const float4 b01 = __ldg(xb), b23 = __ldg(xb + 1), c01 = __ldg(xc), c23 = __ldg(xc + 1);
+            const float2 y3 = __ldg(x + k * ld + jy3);
+            const float2 b[4] = {make_float2(b01.x, b01.y), make_float2(b01.z, b01.w), make_float2(b23.x, b23.y),
+                                 make_float2(b23.z, b23.w)};
+            const float2 cxs[4] = {make_float2(c01.x, c01.y), make_float2(c01.z, c01.w), make_float2(c23.x, c23.y),
+                                   make_float2(c23.z, c23.w)};
+            const float2 cys[4] = {b[1], b[2], b[3], y3};
+            const double wk = WEIGHTED ? w[k] : 1.0;
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const float2 bb = b[j], cx = cxs[j], cy = cys[j];  // c * conj(b)
+                if (WEIGHTED) {
+                    aw[j][0] += wk * ((double)cx.x * (double)bb.x + (double)cx.y * (double)bb.y);
+                    aw[j][1] += wk * ((double)cx.y * (double)bb.x - (double)cx.x * (double)bb.y);
+                    aw[j][2] += wk * ((double)cy.x * (double)bb.x + (double)cy.y * (double)bb.y);
+                    aw[j][3] += wk * ((double)cy.y * (double)bb.x - (double)cy.x * (double)bb.y);
+                } else {
+                    a[j][0].add_prod(cx.x, bb.x);
+                    a[j][0].add_prod(cx.y, bb.y);
+                    a[j][1].add_prod(cx.y, bb.x);
+                    a[j][1].add_prod(-cx.x, bb.y);
+                    a[j][2].add_prod(cy.x, bb.x);
+                    a[j][2].add_prod(cy.y, bb.y);
+                    a[j][3].add_prod(cy.y, bb.x);
+                    a[j][3].add_prod(-cy.x, bb.y);
+                }
+            }
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) red[warp][q][lane * 4 + j] = WEIGHTED ? aw[j][q] : a[j][q].get();
+    __syncthreads();
+    if (threadIdx.x < 128) {
+        const int64_t s = (int64_t)blockIdx.x * 128 + threadIdx.x;
+        if (s < g.N) {
+            double* pl = part + (int64_t)blockIdx.y * 4 * g.N;
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                double t = 0.0;
+                for (int r = 0; r < kReadWarps; ++r) t += red[r][q][threadIdx.x];
+                pl[(int64_t)q * g.N + s] = t;
+            }
+        }
+    }
+}
+
+// Adds the S slice planes of bond_currents_kets4_kernel in slice order and writes the bonds.
+__global__ void bond_currents_slices_kernel(Geom g, const double2* __restrict__ hop, const double* __restrict__ part,
+                                            int S, double* __restrict__ out) {
+    const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= g.N) return;
+    double v[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        double t = part[(int64_t)q * g.N + s];
+        for (int y = 1; y < S; ++y) t += part[((int64_t)y * 4 + q) * g.N + s];
+        v[q] = t;
+    }
+    const Nbr nb = neighbours(g, s);
+    if (nb.hxp) bond_write(g, hop, s, 0, nb, v[0], v[1], out);
+    if (nb.hyp) bond_write(g, hop, s, 1, nb, v[2], v[3], out);
+}
+
+template <bool WEIGHTED>
+static cudaError_t launch_bond_currents4(lm_ctx* ctx, const Geom& g, const double2* hop, const float2* x, int64_t m,
+                                         int64_t ld, const double* w, double* out) {
+    const int64_t chunks = (g.N + 127) / 128;
+    static const int per_sm = [] {  // resident blocks per SM of this instantiation
+        int b = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, bond_currents_kets4_kernel<WEIGHTED>, 32 * kReadWarps,
+                                                          0) != cudaSuccess) {
+            (void)cudaGetLastError();
+            b = 0;
+        }
+        return b;
+    }();
+    int S = readout_slices(chunks, m, (int64_t)per_sm * ctx->sm_count);
+    if (ctx->ld_slices_override > 0) S = ctx->ld_slices_override;
+    cudaError_t e = ensure_readout_part(ctx, (size_t)S * 4 * (size_t)g.N);
+    if (e != cudaSuccess) return e;  // the caller falls back to the one-site-per-lane kernel
+    const int64_t kslice = (m + S - 1) / S;
+    bond_currents_kets4_kernel<WEIGHTED><<<dim3((unsigned)chunks, (unsigned)S), 32 * kReadWarps, 0, ctx->stream>>>(
+        g, x, m, ld, w, kslice, ctx->d_ld_part);
+    bond_currents_slices_kernel<<<(unsigned)((g.N + 255) / 256), 256, 0, ctx->stream>>>(g, hop, ctx->d_ld_part, S, out);
+    ctx->launches++;
+    return cudaSuccess;
+}
+
 cudaError_t launch_bond_currents(lm_ctx* ctx, const Geom& g, int precision, int kind, const double2* hop,
                                  const void* x, int64_t m, int64_t ld, const double* w, double* out) {
     if (g.N <= 0) return cudaSuccess;
@@ -476,6 +611,16 @@ cudaError_t launch_bond_currents(lm_ctx* ctx, const Geom& g, int precision, int 
         if (precision == LM_C64) {
             if (w) bond_currents_kets_kernel<double, true><<<blocks, thr, 0, ctx->stream>>>(g, hop, (const double2*)x, m, ld, w, out);
             else bond_currents_kets_kernel<double, false><<<blocks, thr, 0, ctx->stream>>>(g, hop, (const double2*)x, m, ld, w, out);
+        } else if (g.Ly % 4 == 0 && ld % 2 == 0 && ((uintptr_t)x & 15) == 0 && !ctx->currents_scalar) {
+            cudaError_t e = w ? launch_bond_currents4<true>(ctx, g, hop, (const float2*)x, m, ld, w, out)
+                              : launch_bond_currents4<false>(ctx, g, hop, (const float2*)x, m, ld, w, out);
+            if (e == cudaErrorMemoryAllocation) {  // no scratch for the partial sums
+                (void)cudaGetLastError();
+                if (w) bond_currents_kets_kernel<float, true><<<blocks, thr, 0, ctx->stream>>>(g, hop, (const float2*)x, m, ld, w, out);
+                else bond_currents_kets_kernel<float, false><<<blocks, thr, 0, ctx->stream>>>(g, hop, (const float2*)x, m, ld, w, out);
+            } else if (e != cudaSuccess) {
+                return e;
+            }
         } else {
             if (w) bond_currents_kets_kernel<float, true><<<blocks, thr, 0, ctx->stream>>>(g, hop, (const float2*)x, m, ld, w, out);
             else bond_currents_kets_kernel<float, false><<<blocks, thr, 0, ctx->stream>>>(g, hop, (const float2*)x, m, ld, w, out);
