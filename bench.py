@@ -515,6 +515,53 @@ def run_general_workload(args):
     return 0
 
 
+def run_readouts_workload(args):
+    """The per-moment readouts of the kets workload, c32: localdensity and DensityCurrents on
+    every bond, each through the readout ring (kernel + asynchronous download), timed with CUDA
+    events over `steps` readouts."""
+    import torch
+    import lmgpu
+    ctx = lmgpu.default_context()
+    ext = torch.cuda.ExternalStream(ctx.stream_ptr(), device=torch.device("cuda", 0))
+    lat = lmgpu.SquareLattice(LX, LY, boundaries={"axis1": True, "axis2": True})
+    N, M = lat.N, args.kets
+    V = np.random.default_rng(SEED + 1).uniform(-1, 1, N)
+    H = lmgpu.tightbinding_hamiltonian(lat, V, field=lmgpu.LandauGauge(B_FIELD))
+    st = lmgpu.KetBlock(lat, make_kets(N, M, dtype=np.complex64), precision="c32")
+    peak, peak_kind = measured_peak_hbm()
+    out = {}
+    for kind in ("density", "currents"):
+        length = N if kind == "density" else int(lat.nbonds())
+        ring = lmgpu.timesequence.ReadoutRing(length, 8)
+        push = (lambda t: ring.push_density(st, t)) if kind == "density" else (lambda t: ring.push_currents(H, st, t))
+        for i in range(args.warmup):
+            ring.wait(push(float(i)))
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        pending = []
+        e0.record(ext)
+        for i in range(args.steps):
+            pending.append(push(float(i)))
+            if len(pending) == 8:
+                ring.wait(pending.pop(0))
+        e1.record(ext)
+        e1.synchronize()
+        for q in pending:
+            ring.wait(q)
+        ms = e0.elapsed_time(e1) / args.steps
+        alg = N * M * 8  # one read of the ket block
+        out[kind] = {"ms_per_readout": ms, "achieved_gbs": alg / (ms / 1000.0) / 1e9,
+                     "frac": alg / (ms / 1000.0) / 1e9 / peak}
+    line = {"metric": "ms per readout (density, currents), c32", "value": out["density"]["ms_per_readout"],
+            "unit": "ms", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "higher_is_better": False,
+            "dtype": "c32", "data": "synthetic (seeded PCG64)",
+            "config": {"workload": WORKLOAD, "N": N, "M": M},
+            "readouts": out, "peak": peak, "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
+            "note": "algorithmic bytes = one read of the ket block; each readout includes its ring download"}
+    print(json.dumps(line))
+    return 0
+
+
 # ------------------------------------------------------------------------------------------
 def main():
     ap = argparse.ArgumentParser()
@@ -525,10 +572,11 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--kets", type=int, default=M_KETS)
     ap.add_argument("--workload", default="kets",
-                    choices=["kets", "batch", "adjoint", "kpm", "densitymatrix", "general"],
+                    choices=["kets", "batch", "adjoint", "kpm", "densitymatrix", "general", "readouts"],
                     help="kets: the 256^2 ket-block workload (default); batch: 512 uneven dense-P lattices; "
                          "adjoint: loss_and_grad of the 64^2 differentiation workload; kpm: DOS moments; "
-                         "densitymatrix: P_0 at T > 0, Chebyshev vs eigensolver; general: honeycomb via ELL")
+                         "densitymatrix: P_0 at T > 0, Chebyshev vs eigensolver; general: honeycomb via ELL; "
+                         "readouts: localdensity and DensityCurrents of the kets workload")
     ap.add_argument("--instances", type=int, default=512)
     ap.add_argument("--panel", type=int, default=None,
                     help="batch: column-panel width of the per-order path (default 1024 for c64, off for c32)")
@@ -560,6 +608,8 @@ def main():
         return run_densitymatrix_workload(args)
     if args.workload == "general":
         return run_general_workload(args)
+    if args.workload == "readouts":
+        return run_readouts_workload(args)
 
     rank, world, local = dist_info()
     import torch
