@@ -303,8 +303,9 @@ int lm_ham_lanczos_bounds(lm_ham *ham, int iters, unsigned long long seed, doubl
 
 /* ---- readout ring (device side of TimeSequence(f, ev(times)), src/timesequence.jl:41-43) -- */
 /* Per-moment readouts computed into the slots of a device ring and downloaded asynchronously
- * into pinned host memory: pushing never waits for the device, so an evolution loop that
- * records every step keeps the GPU busy.  Entry s lives in slot s % nslots; its host copy is
+ * into pinned host memory: pushing does not wait for the device, so an evolution loop that
+ * records every step keeps the GPU busy.  (The first readout of a context, or the first of a
+ * larger shape, allocates the readout's slice scratch, which synchronises the device once.)  Entry s lives in slot s % nslots; its host copy is
  * valid from lm_ring_wait(s) until entry s + nslots is pushed.  Extension of the reference:
  * it has no asynchronous readout. */
 typedef struct lm_ring lm_ring;
