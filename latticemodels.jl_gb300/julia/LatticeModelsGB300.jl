@@ -462,8 +462,146 @@ function ChainRulesCore.rrule(::typeof(density_loss), V, B, p::DensityLossProble
     return loss, pullback
 end
 
+# ---- context options, state utilities -----------------------------------------------------------
+const LM_OPT_FUSED = Cint(1)   # 0: one launch per Chebyshev order for ComplexF32 states
+const LM_OPT_STREAM = Cint(2)  # 0: the region form of the fused step instead of the x-streaming form
+
+gpu_synchronize(ctx::Context=default_context()) =
+    check(ccall((:lm_ctx_synchronize, LIB), Cint, (Ptr{Cvoid},), ctx.handle), ctx.handle)
+set_option!(ctx::Context, option::Cint, value::Integer) =
+    check(ccall((:lm_ctx_set_option, LIB), Cint, (Ptr{Cvoid}, Cint, Cint), ctx.handle, option, value), ctx.handle)
+
+# Ensemble weights: P = sum_k w_k |psi_k><psi_k| for the readouts (nothing: all ones).
+function set_weights!(st::DeviceState, w)
+    wv = w === nothing ? Ptr{Float64}(C_NULL) : Vector{Float64}(w)
+    check(ccall((:lm_state_set_weights, LIB), Cint, (Ptr{Cvoid}, Ptr{Float64}), st.handle, wv), st.lat.ctx.handle)
+    return st
+end
+function gpu_trace(st::DeviceState)
+    out = Ref{Cdouble}(0.0)
+    check(ccall((:lm_trace, LIB), Cint, (Ptr{Cvoid}, Ref{Cdouble}), st.handle, out), st.lat.ctx.handle)
+    return out[]
+end
+function gpu_norms(st::DeviceState)
+    out = Vector{Float64}(undef, st.m)
+    check(ccall((:lm_state_norms, LIB), Cint, (Ptr{Cvoid}, Ptr{Float64}), st.handle, out), st.lat.ctx.handle)
+    return out
+end
+gpu_renormalize!(st::DeviceState, target::AbstractVector{<:Real}) =
+    check(ccall((:lm_state_renormalize, LIB), Cint, (Ptr{Cvoid}, Ptr{Float64}), st.handle, Vector{Float64}(target)),
+          st.lat.ctx.handle)
+# (pointer, leading dimension) of the device block, e.g. for unsafe_wrap(CuArray, ...); it
+# changes when a step swaps buffers
+function device_pointer(st::DeviceState)
+    p = Ref{Ptr{Cvoid}}(C_NULL)
+    ld = Ref{Int64}(0)
+    check(ccall((:lm_state_device_ptr, LIB), Cint, (Ptr{Cvoid}, Ref{Ptr{Cvoid}}, Ref{Int64}), st.handle, p, ld),
+          st.lat.ctx.handle)
+    return p[], ld[]
+end
+# (K, a, b): Chebyshev order and the interval [b - a, b + a] of the last update_solver!
+function solver_order(s::ChebyshevGPU)
+    K = Ref{Cint}(0)
+    a = Ref{Cdouble}(0.0)
+    b = Ref{Cdouble}(0.0)
+    check(ccall((:lm_solver_order, LIB), Cint, (Ptr{Cvoid}, Ref{Cint}, Ref{Cdouble}, Ref{Cdouble}), s.handle, K, a, b),
+          s.ctx.handle)
+    return Int(K[]), a[], b[]
+end
+
+# ---- spectral bounds, KPM and the Fermi operator (no eigensystem) --------------------------------
+# :gershgorin always encloses the spectrum; :lanczos is tighter (FP64 Lanczos, the Ritz values
+# padded by their residuals and 1 % of the width, clipped to Gershgorin).
+function spectral_bounds(H::DeviceHamiltonian; method=:gershgorin, iters=64, seed=0x5eed)
+    lo = Ref{Cdouble}(0.0)
+    hi = Ref{Cdouble}(0.0)
+    ctx = H.lat.ctx.handle
+    if method === :lanczos
+        check(ccall((:lm_ham_lanczos_bounds, LIB), Cint, (Ptr{Cvoid}, Cint, Culonglong, Ref{Cdouble}, Ref{Cdouble}),
+                    H.handle, iters, seed, lo, hi), ctx)
+    else
+        check(ccall((:lm_ham_bounds, LIB), Cint, (Ptr{Cvoid}, Ref{Cdouble}, Ref{Cdouble}), H.handle, lo, hi), ctx)
+    end
+    return lo[], hi[]
+end
+function padded_bounds(H::DeviceHamiltonian; method=:gershgorin)
+    lo, hi = spectral_bounds(H; method=method)
+    pad = 1e-3 * (hi - lo)
+    return lo - pad, hi + pad
+end
+
+"""
+    kpm_moments(H, nmom; vecs=nothing, per_column=false, bounds=padded_bounds(H))
+
+KPM moments mu_n = sum_v <v|T_n(H~)|v>, n < nmom, in FP64, on the interval `bounds`
+(H~ = (H - b)/a).  `vecs`: a ComplexF64 `DeviceState` of starting vectors (stochastic
+trace), or `nothing` for the N unit vectors (exact trace).  `per_column=true` keeps one
+column of moments per vector (with unit vectors: the local moments of every site, the LDOS).
+The density of states follows from the moments without an eigensystem (the reference
+computes `dos` from an Eigensystem, src/greenfunction.jl:306).
+"""
+function kpm_moments(H::DeviceHamiltonian, nmom::Integer; vecs=nothing, per_column=false, bounds=padded_bounds(H))
+    ncol = per_column ? (vecs === nothing ? size(H, 1) : vecs.m) : 1
+    out = Vector{Float64}(undef, nmom * ncol)
+    vh = vecs === nothing ? C_NULL : vecs.handle
+    check(ccall((:lm_kpm_moments, LIB), Cint, (Ptr{Cvoid}, Cdouble, Cdouble, Cint, Ptr{Cvoid}, Cint, Ptr{Float64}),
+                H.handle, bounds[1], bounds[2], nmom, vh, per_column, out), H.lat.ctx.handle)
+    return per_column ? reshape(out, nmom, ncol) : out
+end
+
+"""
+    chebyshev_coefficients(f, (emin, emax); tol=1e-13)
+
+Real Chebyshev coefficients c_n of x -> f(a x + b) on [-1, 1], with [b - a, b + a] =
+(emin, emax), truncated where the tail sum_{n >= K} |c_n| is below `tol`.  They come from the
+Chebyshev-Gauss nodes (a type-II DCT, summed directly); the node count doubles until the
+series has converged within the first quarter of the coefficients.
+"""
+function chebyshev_coefficients(f, bounds; tol=1e-13, max_nodes=1 << 16)
+    emin, emax = bounds
+    a, b = (emax - emin) / 2, (emax + emin) / 2
+    nodes = 4096
+    while true
+        theta = [pi * (k + 0.5) / nodes for k in 0:nodes-1]
+        fx = [f(a * cos(t) + b) for t in theta]
+        nc = nodes ÷ 4 + 1
+        c = [2 / nodes * sum(fx[k] * cos(n * theta[k]) for k in 1:nodes) for n in 0:nc-1]
+        c[1] /= 2
+        tail = reverse(cumsum(reverse(abs.(c))))
+        K = findfirst(<=(tol), tail)
+        K !== nothing && return c[1:max(K - 1, 1)]
+        nodes >= max_nodes && throw(ArgumentError("the Chebyshev series of f does not converge on the spectral interval"))
+        nodes *= 2
+    end
+end
+
+"""
+    gpu_densitymatrix(H; mu, T, precision=LM_C64, tol=1e-13, bounds=padded_bounds(H))
+
+`densitymatrix(H; mu, T)` for T > 0 (src/spectrum.jl:252-257) without an eigensystem: the
+Chebyshev series of the FermiDirac occupation f(E) = 1 / (exp((E - mu)/T) + 1)
+(src/spectrum.jl:230-232) applied to the identity on the device.  At T = 0 the occupation is a
+step and its series does not converge; that case keeps the eigensystem route.
+"""
+function gpu_densitymatrix(H::DeviceHamiltonian; mu, T, precision=LM_C64, tol=1e-13, bounds=padded_bounds(H))
+    T > 0 || throw(ArgumentError("the Chebyshev Fermi operator needs T > 0"))
+    c = chebyshev_coefficients(E -> (1 - tanh((E - mu) / (2T))) / 2, bounds; tol=tol)
+    n = size(H, 1)
+    ctx = H.lat.ctx.handle
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:lm_state_create, LIB), Cint, (Ptr{Cvoid}, Int64, Int64, Cint, Cint, Ref{Ptr{Cvoid}}),
+                ctx, n, n, LM_DENSITY, precision, h), ctx)
+    out = DeviceState(H.lat, h[], n, n, LM_DENSITY, precision)
+    finalizer(s -> ccall((:lm_state_destroy, LIB), Cint, (Ptr{Cvoid},), s.handle), out)
+    check(ccall((:lm_cheb_apply, LIB), Cint, (Ptr{Cvoid}, Cdouble, Cdouble, Ptr{Float64}, Cint, Ptr{Cvoid}, Ptr{Cvoid}),
+                H.handle, bounds[1], bounds[2], c, length(c), C_NULL, out.handle), ctx)
+    return out
+end
+
 export ChebyshevGPU, DeviceLattice, DeviceState, gpu_tightbinding, bond_currents, ReadoutRing,
        gpu_timesequence, GPUBatch, DensityLossProblem, density_loss, GPUSparseHamiltonian, set_values!, gpu_operator_currents,
-       gpu_operator_timesequence
+       gpu_operator_timesequence, gpu_synchronize, set_option!, set_weights!, gpu_trace, gpu_norms, gpu_renormalize!,
+       device_pointer, solver_order, spectral_bounds, padded_bounds, kpm_moments, chebyshev_coefficients,
+       gpu_densitymatrix, LM_OPT_FUSED, LM_OPT_STREAM
 
 end # module

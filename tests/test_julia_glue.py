@@ -21,7 +21,9 @@ SCALARS = {
     "int64_t": {"Int64"},
     "double": {"Cdouble", "Float64"},
     "size_t": {"Csize_t", "UInt64"},
+    "unsigned long long": {"Culonglong", "UInt64"},
 }
+TYPE_WORDS = {"int", "long", "unsigned", "double", "float", "char", "short", "int64_t", "size_t", "void"}
 POINTER_JL = re.compile(r"^(Ptr|Ref)\{.*\}$|^Cstring$")
 
 
@@ -81,9 +83,10 @@ def _c_kind(ctype):
     if "*" in ctype:
         return "ptr", None
     words = [w for w in ctype.replace("const", " ").split() if w]
-    # a named parameter: "int ndof" -> "int"; an unnamed one: "int"
-    base = words[0] if words else ctype
-    return "scalar", base
+    # a named parameter: "int ndof" -> "int", "unsigned long long seed" -> "unsigned long long"
+    if len(words) > 1 and words[-1] not in TYPE_WORDS:
+        words = words[:-1]
+    return "scalar", " ".join(words)
 
 
 def test_glue_present_and_has_ccalls():
@@ -116,5 +119,6 @@ def test_glue_binds_the_plugin_and_readout_entry_points():
     bound = {c[0] for c in glue_ccalls()}
     for fn in ("lm_solver_update", "lm_solver_step", "lm_localdensity", "lm_bond_currents",
                "lm_ring_push_localdensity", "lm_ring_push_currents", "lm_ring_push_op_currents",
-               "lm_ell_op_currents", "lm_state_upload", "lm_state_download"):
+               "lm_ell_op_currents", "lm_state_upload", "lm_state_download", "lm_kpm_moments",
+               "lm_cheb_apply", "lm_ham_lanczos_bounds", "lm_state_set_weights", "lm_trace"):
         assert fn in bound, fn
