@@ -8,7 +8,7 @@ module LatticeModelsGB300
 
 using LatticeModels
 import LatticeModels: EvolutionSolver, update_solver!, step!, evolution_cache, localdensity
-using SparseArrays: SparseMatrixCSC
+using SparseArrays: SparseMatrixCSC, nnz, nzrange, rowvals, sparse
 
 const LIB = get(ENV, "LMGPU_LIB", joinpath(@__DIR__, "..", "lmgpu", "liblmgpu.so"))
 
@@ -214,6 +214,15 @@ update_solver!(s::ChebyshevGPU, H::GPUSparseHamiltonian, dt, force=false) =
     check(ccall((:lm_ell_solver_update, LIB), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Cdouble, Cint), s.handle, H.handle, dt, force),
           s.ctx.handle)
 
+# DensityCurrents(H, state)[i, j] = 2 Im(H[i,j] P[j,i]) (src/zoo/currents.jl:92-102) for every
+# stored entry of A (the CSC the device table was made from), in its order; 0 on the diagonal.
+function gpu_entry_currents(H::GPUSparseHamiltonian, A::SparseMatrixCSC{ComplexF64,Int64}, st)
+    out = Vector{Float64}(undef, nnz(A))
+    check(ccall((:lm_ell_currents, LIB), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Float64}), H.handle, st.handle, out),
+          H.ctx.handle)
+    return SparseMatrixCSC(size(A)..., copy(A.colptr), copy(A.rowval), out)
+end
+
 # LocalOperatorCurrents(H, state, op) (src/zoo/currents.jl:150-184) on a general Hamiltonian with
 # ndof internal states per site: one device pass gives every stored entry's share, the site-pair
 # value is the sum over its block (`sparse` adds the duplicates).  op === nothing: DensityCurrents.
@@ -275,7 +284,7 @@ function push_op_currents!(r::ReadoutRing, H::GPUSparseHamiltonian, st, ndof::In
                 r.handle, H.handle, st.handle, ndof, opm, t, seq), r.ctx.handle)
     return seq[]
 end
-function take!(r::ReadoutRing, seq::Integer, len::Integer)
+function ring_take!(r::ReadoutRing, seq::Integer, len::Integer)
     out = Vector{Float64}(undef, len)
     n = Ref{Int64}(0)
     t = Ref{Cdouble}(0.0)
@@ -305,14 +314,14 @@ function gpu_timesequence(kind::Symbol, ev_iter; nslots=8)
             ring = ReadoutRing(max(len, 1), nslots; ctx=st.lat.ctx)
         end
         if length(pending) == nslots
-            t, v = take!(ring, popfirst!(pending), len)
+            t, v = ring_take!(ring, popfirst!(pending), len)
             push!(ts, t); push!(vals, v)
         end
         push!(pending, kind === :density ? push_density!(ring, st, moment.t) :
                                            push_currents!(ring, moment.H.data::DeviceHamiltonian, st, moment.t))
     end
     for seq in pending
-        t, v = take!(ring, seq, len)
+        t, v = ring_take!(ring, seq, len)
         push!(ts, t); push!(vals, v)
     end
     return LatticeModels.TimeSequence(ts, vals)
@@ -334,13 +343,13 @@ function gpu_operator_timesequence(H::GPUSparseHamiltonian, A::SparseMatrixCSC{C
     vals = Any[]
     for moment in ev_iter
         if length(pending) == nslots
-            t, v = take!(ring, popfirst!(pending), nnz(A))
+            t, v = ring_take!(ring, popfirst!(pending), nnz(A))
             push!(ts, t); push!(vals, site_pair_currents(A, v, ndof))
         end
         push!(pending, push_op_currents!(ring, H, moment.state.data, ndof, moment.t, op))
     end
     for seq in pending
-        t, v = take!(ring, seq, nnz(A))
+        t, v = ring_take!(ring, seq, nnz(A))
         push!(ts, t); push!(vals, site_pair_currents(A, v, ndof))
     end
     return LatticeModels.TimeSequence(ts, vals)
@@ -602,6 +611,6 @@ export ChebyshevGPU, DeviceLattice, DeviceState, gpu_tightbinding, bond_currents
        gpu_timesequence, GPUBatch, DensityLossProblem, density_loss, GPUSparseHamiltonian, set_values!, gpu_operator_currents,
        gpu_operator_timesequence, gpu_synchronize, set_option!, set_weights!, gpu_trace, gpu_norms, gpu_renormalize!,
        device_pointer, solver_order, spectral_bounds, padded_bounds, kpm_moments, chebyshev_coefficients,
-       gpu_densitymatrix, LM_OPT_FUSED, LM_OPT_STREAM
+       gpu_densitymatrix, gpu_entry_currents, LM_OPT_FUSED, LM_OPT_STREAM
 
 end # module

@@ -122,3 +122,22 @@ def test_glue_binds_the_plugin_and_readout_entry_points():
                "lm_ell_op_currents", "lm_state_upload", "lm_state_download", "lm_kpm_moments",
                "lm_cheb_apply", "lm_ham_lanczos_bounds", "lm_state_set_weights", "lm_trace"):
         assert fn in bound, fn
+
+
+# Base functions a module must qualify (Base.f) to add methods to; defining them bare shadows
+# Base and fails once the module has used the Base binding.
+BASE_FUNCS = {"take!", "put!", "push!", "pop!", "append!", "copy", "size", "length", "getindex", "setindex!",
+              "show", "print", "close", "wait", "fill!", "resize!", "empty!", "isready", "reset"}
+SPARSE_FUNCS = ("nnz", "nzrange", "rowvals", "nonzeros", "sparse", "spzeros", "findnz")
+
+
+def test_glue_imports_and_definitions():
+    text = open(GLUE).read()
+    m = re.search(r"^using SparseArrays:(.*)$", text, re.M)
+    imported = {w.strip() for w in m.group(1).split(",")} if m else set()
+    for f in SPARSE_FUNCS:
+        if re.search(r"(?<![\w.])" + f + r"\(", text):
+            assert f in imported, f"{f} is used but not imported from SparseArrays"
+    defined = set(re.findall(r"^function ([A-Za-z_][\w!]*)\(", text, re.M))
+    defined |= set(re.findall(r"^([A-Za-z_][\w!]*)\([^)]*\)\s*=", text, re.M))
+    assert not (defined & BASE_FUNCS), f"unqualified Base functions defined: {defined & BASE_FUNCS}"
