@@ -385,6 +385,18 @@ def run_kpm_workload(args):
     e1.synchronize()
     clocks = clk.stop()
     ms = e0.elapsed_time(e1) / reps
+    # the same call with the double-float recurrence (LM_OPT_KPM = 1)
+    ctx.set_kpm_doublefloat(True)
+    try:
+        lmgpu.kpm.moments(H, 64, vecs, bounds=bounds)
+        e0.record(ext)
+        for _ in range(reps):
+            mu_df, _ = lmgpu.kpm.moments(H, nmom, vecs, bounds=bounds)
+        e1.record(ext)
+        e1.synchronize()
+        ms_df = e0.elapsed_time(e1) / reps
+    finally:
+        ctx.set_kpm_doublefloat(False)
     passes = (nmom + 1) // 2 + 1
     # per pass: the recurrence reads T_{n+1} and T_n and writes T_{n+2}; the two dot products
     # read T_n (twice) and T_{n+1}: six block passes of N*R*16 bytes
@@ -399,7 +411,12 @@ def run_kpm_workload(args):
                          "frac": alg / (ms / 1000.0) / 1e9 / peak, "traffic": None,
                          "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
                          "alg_bytes_per_call": alg, "note": "whole call (recurrence + dot kernels)"},
-            "mu0_over_N": float(mu[0] / (N * R)), "clocks": clocks}
+            "mu0_over_N": float(mu[0] / (N * R)), "clocks": clocks,
+            "doublefloat": {"value": R * nmom / (ms_df / 1000.0), "ms_per_step": ms_df, "speedup": ms / ms_df,
+                            "roofline_frac": alg / (ms_df / 1000.0) / 1e9 / peak,
+                            "max_moment_diff_over_mu0": float(np.abs(mu_df - mu).max() / abs(mu[0])),
+                            "note": "LM_OPT_KPM = 1: the recurrence in FP32 pairs; the dots accumulate in "
+                                    "double-float and reduce in FP64"}}
     print(json.dumps(line))
     return 0
 

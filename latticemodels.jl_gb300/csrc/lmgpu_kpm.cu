@@ -14,11 +14,14 @@
 #include <cuda_runtime.h>
 #include <math.h>
 
+#include <algorithm>
+
 #include <new>
 #include <utility>
 #include <vector>
 
 #include "lmgpu_internal.cuh"
+#include "lmgpu_order.cuh"
 
 namespace lmgpu {
 
@@ -83,6 +86,142 @@ __global__ void start_vector_kernel(double2* __restrict__ v, int64_t n, unsigned
         sincos(phi, &sn, &cs);
         const double r = rsqrt((double)n);
         v[i] = make_double2(r * cs, r * sn);
+    }
+}
+
+
+// ------------------------------------------------------------------------------------------
+// Double-float ("df") form of the moment recurrence (LM_OPT_KPM = 1).  A real number is an
+// unevaluated sum hi + lo of two FP32 values (about 48 significant bits), so the recurrence
+// runs on the FP32 pipe instead of GB300's 1/64-rate FP64 pipe.  A complex df value is a float4
+// {re.hi, re.lo, im.hi, im.lo}, the size of a double2, so the FP64 buffers are reused in place.
+// Products take the exact FMA error term (p + e = a*b exactly); sums use the double-word
+// addition of Dekker and of Knuth's TwoSum.  Every step is an explicit round-to-nearest
+// intrinsic, which nvcc never contracts into an FMA or reorders, so the error-free
+// transformations stay exact.  An exact emulation of this arithmetic keeps the moments within
+// about 1e-14 of FP64 after 1024 passes.
+// ------------------------------------------------------------------------------------------
+struct DF {
+    float h, l;
+};
+__device__ __forceinline__ DF df_fast_two_sum(float a, float b) {
+    const float s = __fadd_rn(a, b);
+    return DF{s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ DF df_add(DF x, DF y) {
+    const float s = __fadd_rn(x.h, y.h);
+    const float bb = __fsub_rn(s, x.h);
+    float e = __fadd_rn(__fsub_rn(x.h, __fsub_rn(s, bb)), __fsub_rn(y.h, bb));
+    e = __fadd_rn(e, __fadd_rn(x.l, y.l));
+    return df_fast_two_sum(s, e);
+}
+__device__ __forceinline__ DF df_mul(DF x, DF y) {
+    const float p = __fmul_rn(x.h, y.h);
+    float e = __fmaf_rn(x.h, y.h, -p);
+    e = __fmaf_rn(x.h, y.l, e);
+    e = __fmaf_rn(x.l, y.h, e);
+    return df_fast_two_sum(p, e);
+}
+__device__ __forceinline__ DF df_neg(DF x) { return DF{-x.h, -x.l}; }
+__device__ __forceinline__ DF df_re(float4 v) { return DF{v.x, v.y}; }
+__device__ __forceinline__ DF df_im(float4 v) { return DF{v.z, v.w}; }
+__device__ __forceinline__ DF df_from(double x) {
+    const float h = (float)x;
+    return DF{h, (float)(x - (double)h)};
+}
+__device__ __forceinline__ double df_value(DF x) { return (double)x.h + (double)x.l; }
+
+// acc += h v on complex df values (h real when RE).
+template <bool RE>
+__device__ __forceinline__ void df_cfma(DF& ar, DF& ai, float4 h, float4 v) {
+    ar = df_add(ar, df_mul(df_re(h), df_re(v)));
+    if (!RE) ar = df_add(ar, df_neg(df_mul(df_im(h), df_im(v))));
+    ai = df_add(ai, df_mul(df_re(h), df_im(v)));
+    if (!RE) ai = df_add(ai, df_mul(df_im(h), df_re(v)));
+}
+
+// In place: n double2 values -> n float4 df values (same bytes per element).
+__global__ void to_df_kernel(double2* __restrict__ a, int64_t n) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double2 v = a[i];
+        const DF r = df_from(v.x), m = df_from(v.y);
+        reinterpret_cast<float4*>(a)[i] = make_float4(r.h, r.l, m.h, m.l);
+    }
+}
+
+// The stencil tables in df form: hop (2N double2) -> 2N float4, diag (N double) -> N float2.
+__global__ void df_tables_kernel(const double2* __restrict__ hop2, const double* __restrict__ diag2, int64_t N,
+                                 float4* __restrict__ hopd, float2* __restrict__ diagd) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < 2 * N; i += (int64_t)gridDim.x * blockDim.x) {
+        const DF r = df_from(hop2[i].x), m = df_from(hop2[i].y);
+        hopd[i] = make_float4(r.h, r.l, m.h, m.l);
+        if (i < N) {
+            const DF d = df_from(diag2[i]);
+            diagd[i] = make_float2(d.h, d.l);
+        }
+    }
+}
+
+// out = (2H~) tp - tpp on df blocks (the tables hold 2H/a and 2(V-b)/a); out may alias tpp.
+// XR: every x-hop is real.
+template <bool XR>
+__global__ void __launch_bounds__(256) df_recur_kernel(Geom g, const float4* __restrict__ hopd,
+                                                       const float2* __restrict__ diagd, const float4* tp,
+                                                       const float4* tpp, float4* out, int64_t ld, int64_t M) {
+    const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= g.N) return;
+    const Nbr nb = neighbours(g, s);
+    const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+    const float4 hxp = nb.hxp ? hopd[s] : z, hyp = nb.hyp ? hopd[g.N + s] : z;
+    float4 t = nb.hxm ? hopd[nb.xm] : z;
+    const float4 hxm = make_float4(t.x, t.y, -t.z, -t.w);  // conj of the hop from x-1
+    t = nb.hym ? hopd[g.N + nb.ym] : z;
+    const float4 hym = make_float4(t.x, t.y, -t.z, -t.w);
+    const float2 dd = diagd[s];
+    const float4 d = make_float4(dd.x, dd.y, 0.f, 0.f);
+    for (int64_t m = blockIdx.y; m < M; m += gridDim.y) {
+        const int64_t o = m * ld;
+        const float4 q = tpp[o + s];
+        DF ar = DF{-q.x, -q.y}, ai = DF{-q.z, -q.w};
+        df_cfma<XR>(ar, ai, hxp, tp[o + nb.xp]);
+        df_cfma<XR>(ar, ai, hxm, tp[o + nb.xm]);
+        df_cfma<false>(ar, ai, hyp, tp[o + nb.yp]);
+        df_cfma<false>(ar, ai, hym, tp[o + nb.ym]);
+        df_cfma<true>(ar, ai, d, tp[o + s]);
+        out[o + s] = make_float4(ar.h, ar.l, ai.h, ai.l);
+    }
+}
+
+// out[col] = Re <A, A>, out[M + col] = Re <B, A> per column, in df per thread and then the
+// fixed-order FP64 block reduction of column_dots_kernel.
+__global__ void __launch_bounds__(256) column_dots2_df_kernel(const float4* __restrict__ A,
+                                                              const float4* __restrict__ B, int64_t n, int64_t ld,
+                                                              int64_t M, double* __restrict__ out) {
+    __shared__ double red[2][8];
+    for (int64_t col = blockIdx.x; col < M; col += gridDim.x) {
+        const float4* a = A + col * ld;
+        const float4* b = B + col * ld;
+        DF aa = DF{0.f, 0.f}, ba = DF{0.f, 0.f};
+        for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+            const float4 x = a[i], y = b[i];
+            aa = df_add(aa, df_mul(df_re(x), df_re(x)));
+            aa = df_add(aa, df_mul(df_im(x), df_im(x)));
+            ba = df_add(ba, df_mul(df_re(y), df_re(x)));
+            ba = df_add(ba, df_mul(df_im(y), df_im(x)));
+        }
+        double v[2] = {df_value(aa), df_value(ba)};
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+            for (int o = 16; o > 0; o >>= 1) v[q] += __shfl_down_sync(0xffffffffu, v[q], o);
+            if ((threadIdx.x & 31) == 0) red[q][threadIdx.x >> 5] = v[q];
+        }
+        __syncthreads();
+        if (threadIdx.x < 2) {
+            double t = 0.0;
+            for (int w = 0; w < 8; ++w) t += red[threadIdx.x][w];
+            out[threadIdx.x * M + col] = t;
+        }
+        __syncthreads();
     }
 }
 
@@ -190,12 +329,15 @@ int lm_kpm_moments(lm_ham* h, double emin, double emax, int nmom, const lm_state
     double2* TA = nullptr;
     double2* TB = nullptr;
     double* dots = nullptr;
+    float4* hopd = nullptr;  // double-float tables (LM_OPT_KPM)
+    float2* diagd = nullptr;
+    const bool use_df = ctx->kpm_df != 0;
     const size_t blk = sizeof(double2) * (size_t)ld * (size_t)M;
     const size_t ndots = (size_t)(nsteps + 1) * 2 * (size_t)M;
     auto release = [&]() {
         cudaStreamSynchronize(ctx->stream);
         cudaFree(hop2); cudaFree(diag2); cudaFree(hop2f); cudaFree(diag2f);
-        cudaFree(TA); cudaFree(TB); cudaFree(dots);
+        cudaFree(TA); cudaFree(TB); cudaFree(dots); cudaFree(hopd); cudaFree(diagd);
     };
     cudaError_t e = cudaMalloc((void**)&hop2, sizeof(double2) * 2 * (size_t)N);
     if (e == cudaSuccess) e = cudaMalloc((void**)&diag2, sizeof(double) * (size_t)N);
@@ -204,6 +346,8 @@ int lm_kpm_moments(lm_ham* h, double emin, double emax, int nmom, const lm_state
     if (e == cudaSuccess) e = cudaMalloc((void**)&TA, blk);
     if (e == cudaSuccess) e = cudaMalloc((void**)&TB, blk);
     if (e == cudaSuccess) e = cudaMalloc((void**)&dots, sizeof(double) * ndots);
+    if (e == cudaSuccess && use_df) e = cudaMalloc((void**)&hopd, sizeof(float4) * 2 * (size_t)N);
+    if (e == cudaSuccess && use_df) e = cudaMalloc((void**)&diagd, sizeof(float2) * (size_t)N);
     if (e != cudaSuccess) {
         cudaGetLastError();
         release();
@@ -232,19 +376,44 @@ int lm_kpm_moments(lm_ham* h, double emin, double emax, int nmom, const lm_state
     e = launch_stencil_recur(ctx, g, LM_C64, hop2, diag2, TA, nullptr, nullptr, TB, ld, M, 0.5, 0.0, 0.0, nullptr, 0.0,
                              xr);
     if (e != cudaSuccess) return fail(e, "lm_kpm_moments: recurrence");
+    if (use_df) {  // T_0 and T_1 (FP64) become double-float in place; so do the tables
+        const unsigned cgrid = (unsigned)std::min<int64_t>((ld * M + 255) / 256, 65535);
+        df_tables_kernel<<<(unsigned)std::min<int64_t>((2 * N + 255) / 256, 65535), 256, 0, ctx->stream>>>(
+            hop2, diag2, N, hopd, diagd);
+        to_df_kernel<<<cgrid, 256, 0, ctx->stream>>>(TA, ld * M);
+        to_df_kernel<<<cgrid, 256, 0, ctx->stream>>>(TB, ld * M);
+        ctx->launches += 3;
+        e = cudaGetLastError();
+        if (e != cudaSuccess) return fail(e, "lm_kpm_moments: double-float conversion");
+    }
+    const dim3 rgrid((unsigned)((N + 255) / 256), (unsigned)(M < 65535 ? M : 65535));
     double2* Tn = TA;   // T_n
     double2* Tn1 = TB;  // T_{n+1}
     for (int64_t n = 0; n <= nsteps; ++n) {
         double* d = dots + (size_t)n * 2 * (size_t)M;
-        column_dots_kernel<<<dgrid, 256, 0, ctx->stream>>>(Tn, Tn, N, ld, M, d);
-        column_dots_kernel<<<dgrid, 256, 0, ctx->stream>>>(Tn1, Tn, N, ld, M, d + M);
-        ctx->launches += 2;
+        if (use_df) {
+            column_dots2_df_kernel<<<dgrid, 256, 0, ctx->stream>>>((const float4*)Tn, (const float4*)Tn1, N, ld, M, d);
+            ctx->launches += 1;
+        } else {
+            column_dots_kernel<<<dgrid, 256, 0, ctx->stream>>>(Tn, Tn, N, ld, M, d);
+            column_dots_kernel<<<dgrid, 256, 0, ctx->stream>>>(Tn1, Tn, N, ld, M, d + M);
+            ctx->launches += 2;
+        }
         e = cudaGetLastError();
         if (e != cudaSuccess) return fail(e, "lm_kpm_moments: dots");
         if (n == nsteps) break;
         // T_{n+2} = 2 H~ T_{n+1} - T_n, written over T_n
-        e = launch_stencil_recur(ctx, g, LM_C64, hop2, diag2, Tn1, Tn, nullptr, Tn, ld, M, 1.0, 0.0, 0.0, nullptr,
-                                 0.0, xr);
+        if (use_df) {
+            if (xr) df_recur_kernel<true><<<rgrid, 256, 0, ctx->stream>>>(g, hopd, diagd, (const float4*)Tn1,
+                                                                          (const float4*)Tn, (float4*)Tn, ld, M);
+            else df_recur_kernel<false><<<rgrid, 256, 0, ctx->stream>>>(g, hopd, diagd, (const float4*)Tn1,
+                                                                        (const float4*)Tn, (float4*)Tn, ld, M);
+            ctx->launches++;
+            e = cudaGetLastError();
+        } else {
+            e = launch_stencil_recur(ctx, g, LM_C64, hop2, diag2, Tn1, Tn, nullptr, Tn, ld, M, 1.0, 0.0, 0.0, nullptr,
+                                     0.0, xr);
+        }
         if (e != cudaSuccess) return fail(e, "lm_kpm_moments: recurrence");
         std::swap(Tn, Tn1);
     }

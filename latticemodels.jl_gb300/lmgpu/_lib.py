@@ -26,6 +26,7 @@ ERR_NAMES = {1: "bad argument", 2: "out of device memory", 3: "CUDA error", 4: "
 LM_C64, LM_C32 = 0, 1
 LM_OPT_FUSED = 1
 LM_OPT_STREAM = 2
+LM_OPT_KPM = 3
 LM_KETS, LM_DENSITY = 0, 1
 LM_FIELD_LANDAU, LM_FIELD_SYMMETRIC, LM_FIELD_POINTFLUX_AXIAL, LM_FIELD_POINTFLUX_SINGULAR = 1, 2, 3, 4
 

@@ -46,6 +46,34 @@ def test_moments_match_oracle(lm, L, per, field):
     assert np.abs(muv - refv).max() <= 1e-11 * abs(refv[0])
 
 
+@pytest.mark.parametrize("L,per,field", [(9, False, "pf"), (12, True, "landau"), (16, False, "landau")])
+def test_doublefloat_moments_match_oracle(lm, L, per, field):
+    """LM_OPT_KPM = 1: the recurrence in double-float (FP32 pairs) keeps the moments of the FP64
+    path's tolerances against the oracle, and within 1e-12 mu_0 of the device FP64 moments."""
+    ol, Ho, Hl = case(lm, L, per, field)
+    ctx = lm.default_context()
+    bounds = lm.kpm._bounds(Hl, ctx)
+    nm = 301
+    mu64, _ = lm.kpm.moments(Hl, nm, bounds=bounds)
+    R = o.random_kets(ol.N, 7, 5)
+    muv64, _ = lm.kpm.moments(Hl, 101, vecs=R, bounds=bounds)
+    try:
+        ctx.set_kpm_doublefloat(True)
+        mu, _ = lm.kpm.moments(Hl, nm, bounds=bounds)
+        mus, _ = lm.kpm.moments(Hl, 40, per_site=True, bounds=bounds)
+        muv, _ = lm.kpm.moments(Hl, 101, vecs=R, bounds=bounds)
+    finally:
+        ctx.set_kpm_doublefloat(False)
+    ref = o.kpm_moments(Ho, *bounds, nm)
+    assert np.abs(mu - ref).max() <= 1e-11 * ref[0]
+    assert np.abs(mu - mu64).max() <= 1e-12 * ref[0]
+    refs = o.kpm_moments(Ho, *bounds, 40, per_column=True)
+    assert np.abs(mus - refs).max() <= 1e-12
+    refv = o.kpm_moments(Ho, *bounds, 101, vecs=R)
+    assert np.abs(muv - refv).max() <= 1e-11 * abs(refv[0])
+    assert np.abs(muv - muv64).max() <= 1e-12 * abs(refv[0])
+
+
 @pytest.mark.parametrize("broaden", [0.05, 0.2])
 def test_dos_ldos_match_eigensystem(lm, broaden):
     ol, Ho, Hl = case(lm, 14, False, "pf")
