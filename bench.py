@@ -380,31 +380,33 @@ def run_kpm_workload(args):
     clk.start()
     e0.record(ext)
     for _ in range(reps):
-        mu, _ = lmgpu.kpm.moments(H, nmom, vecs, bounds=bounds)
+        mu, _ = lmgpu.kpm.moments(H, nmom, vecs, bounds=bounds)  # the default: double-float recurrence
     e1.record(ext)
     e1.synchronize()
     clocks = clk.stop()
     ms = e0.elapsed_time(e1) / reps
-    # the same call with the double-float recurrence (LM_OPT_KPM = 1)
-    ctx.set_kpm_doublefloat(True)
+    # the same call with the FP64 recurrence (LM_OPT_KPM = 0)
+    ctx.set_kpm_doublefloat(False)
     try:
         lmgpu.kpm.moments(H, 64, vecs, bounds=bounds)
         e0.record(ext)
         for _ in range(reps):
-            mu_df, _ = lmgpu.kpm.moments(H, nmom, vecs, bounds=bounds)
+            mu64, _ = lmgpu.kpm.moments(H, nmom, vecs, bounds=bounds)
         e1.record(ext)
         e1.synchronize()
-        ms_df = e0.elapsed_time(e1) / reps
+        ms64 = e0.elapsed_time(e1) / reps
     finally:
-        ctx.set_kpm_doublefloat(False)
+        ctx.set_kpm_doublefloat(True)
     passes = (nmom + 1) // 2 + 1
     # per pass: the recurrence reads T_{n+1} and T_n and writes T_{n+2}; the two dot products
     # read T_n (twice) and T_{n+1}: six block passes of N*R*16 bytes
     alg = 6.0 * N * R * 16 * passes
     peak, peak_kind = measured_peak_hbm()
-    line = {"metric": "KPM vector-moments/s (FP64 Chebyshev moments)", "value": R * nmom / (ms / 1000.0),
+    line = {"metric": "KPM vector-moments/s (Chebyshev moments, double-float recurrence)",
+            "value": R * nmom / (ms / 1000.0),
             "unit": "vector-moments/s", "n_gpus": 1, "steps": reps, "warmup": args.warmup, "ms_per_step": ms,
-            "higher_is_better": True, "dtype": "c64", "data": "synthetic (seeded PCG64 random-phase vectors)",
+            "higher_is_better": True, "dtype": "df32 pairs (recurrence), f64 (dots, moments)",
+            "data": "synthetic (seeded PCG64 random-phase vectors)",
             "config": {"workload": KPM_WORKLOAD, "N": N, "vectors": R, "moments": nmom, "passes": passes,
                        "step_unit": "one lm_kpm_moments call"},
             "roofline": {"bound": "hbm", "achieved": alg / (ms / 1000.0) / 1e9, "peak": peak, "unit": "GB/s",
@@ -412,11 +414,10 @@ def run_kpm_workload(args):
                          "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
                          "alg_bytes_per_call": alg, "note": "whole call (recurrence + dot kernels)"},
             "mu0_over_N": float(mu[0] / (N * R)), "clocks": clocks,
-            "doublefloat": {"value": R * nmom / (ms_df / 1000.0), "ms_per_step": ms_df, "speedup": ms / ms_df,
-                            "roofline_frac": alg / (ms_df / 1000.0) / 1e9 / peak,
-                            "max_moment_diff_over_mu0": float(np.abs(mu_df - mu).max() / abs(mu[0])),
-                            "note": "LM_OPT_KPM = 1: the recurrence in FP32 pairs; the dots accumulate in "
-                                    "double-float and reduce in FP64"}}
+            "fp64": {"value": R * nmom / (ms64 / 1000.0), "ms_per_step": ms64, "speedup_of_default": ms64 / ms,
+                     "roofline_frac": alg / (ms64 / 1000.0) / 1e9 / peak,
+                     "max_moment_diff_over_mu0": float(np.abs(mu64 - mu).max() / abs(mu[0])),
+                     "note": "LM_OPT_KPM = 0: the recurrence in FP64 (GB300 runs FP64 at 1/64 of FP32)"}}
     print(json.dumps(line))
     return 0
 

@@ -100,7 +100,7 @@ struct lm_ctx {
     unsigned stream_attr = 0;           // the same for the x-streaming form (bit K, +8 for real x-hops)
     int fused_form = 1;                 // LM_OPT_STREAM: 1 = x-streaming form where supported, 0 = region form
     int64_t stream_launches = 0;        // fused steps run in the x-streaming form
-    int kpm_df = 0;                     // LM_OPT_KPM: double-float recurrence in lm_kpm_moments
+    int kpm_df = 1;                     // LM_OPT_KPM: double-float recurrence in lm_kpm_moments
     std::vector<double> h_norms;        // pageable staging of lm_state_renormalize's targets
     std::vector<cudaEvent_t> ev_pool;   // pairs (start, stop) of timed Chebyshev sweeps
     std::vector<int> ev_launches;       // launches covered by each recorded pair

@@ -91,7 +91,7 @@ __global__ void start_vector_kernel(double2* __restrict__ v, int64_t n, unsigned
 
 
 // ------------------------------------------------------------------------------------------
-// Double-float ("df") form of the moment recurrence (LM_OPT_KPM = 1).  A real number is an
+// Double-float ("df") form of the moment recurrence (LM_OPT_KPM = 1, the default).  A real number is an
 // unevaluated sum hi + lo of two FP32 values (about 48 significant bits), so the recurrence
 // runs on the FP32 pipe instead of GB300's 1/64-rate FP64 pipe.  A complex df value is a float4
 // {re.hi, re.lo, im.hi, im.lo}, the size of a double2, so the FP64 buffers are reused in place.
@@ -329,7 +329,7 @@ int lm_kpm_moments(lm_ham* h, double emin, double emax, int nmom, const lm_state
     double2* TA = nullptr;
     double2* TB = nullptr;
     double* dots = nullptr;
-    float4* hopd = nullptr;  // double-float tables (LM_OPT_KPM)
+    float4* hopd = nullptr;  // double-float tables (LM_OPT_KPM, default on)
     float2* diagd = nullptr;
     const bool use_df = ctx->kpm_df != 0;
     const size_t blk = sizeof(double2) * (size_t)ld * (size_t)M;

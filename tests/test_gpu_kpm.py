@@ -48,22 +48,25 @@ def test_moments_match_oracle(lm, L, per, field):
 
 @pytest.mark.parametrize("L,per,field", [(9, False, "pf"), (12, True, "landau"), (16, False, "landau")])
 def test_doublefloat_moments_match_oracle(lm, L, per, field):
-    """LM_OPT_KPM = 1: the recurrence in double-float (FP32 pairs) keeps the moments of the FP64
-    path's tolerances against the oracle, and within 1e-12 mu_0 of the device FP64 moments."""
+    """LM_OPT_KPM = 1 (the default): the recurrence in double-float (FP32 pairs) keeps the
+    moments within the FP64 path's tolerances against the oracle, and within 1e-12 mu_0 of the
+    device FP64 moments (LM_OPT_KPM = 0)."""
     ol, Ho, Hl = case(lm, L, per, field)
     ctx = lm.default_context()
     bounds = lm.kpm._bounds(Hl, ctx)
     nm = 301
-    mu64, _ = lm.kpm.moments(Hl, nm, bounds=bounds)
     R = o.random_kets(ol.N, 7, 5)
-    muv64, _ = lm.kpm.moments(Hl, 101, vecs=R, bounds=bounds)
     try:
-        ctx.set_kpm_doublefloat(True)
-        mu, _ = lm.kpm.moments(Hl, nm, bounds=bounds)
-        mus, _ = lm.kpm.moments(Hl, 40, per_site=True, bounds=bounds)
-        muv, _ = lm.kpm.moments(Hl, 101, vecs=R, bounds=bounds)
-    finally:
         ctx.set_kpm_doublefloat(False)
+        mu64, _ = lm.kpm.moments(Hl, nm, bounds=bounds)
+        muv64, _ = lm.kpm.moments(Hl, 101, vecs=R, bounds=bounds)
+        ref = o.kpm_moments(Ho, *bounds, nm)
+        assert np.abs(mu64 - ref).max() <= 1e-11 * ref[0]
+    finally:
+        ctx.set_kpm_doublefloat(True)
+    mu, _ = lm.kpm.moments(Hl, nm, bounds=bounds)
+    mus, _ = lm.kpm.moments(Hl, 40, per_site=True, bounds=bounds)
+    muv, _ = lm.kpm.moments(Hl, 101, vecs=R, bounds=bounds)
     ref = o.kpm_moments(Ho, *bounds, nm)
     assert np.abs(mu - ref).max() <= 1e-11 * ref[0]
     assert np.abs(mu - mu64).max() <= 1e-12 * ref[0]
