@@ -474,6 +474,7 @@ end
 # ---- context options, state utilities -----------------------------------------------------------
 const LM_OPT_FUSED = Cint(1)   # 0: one launch per Chebyshev order for ComplexF32 states
 const LM_OPT_STREAM = Cint(2)  # 0: the region form of the fused step instead of the x-streaming form
+const LM_OPT_KPM = Cint(3)     # 0: the FP64 KPM recurrence instead of double-float
 
 gpu_synchronize(ctx::Context=default_context()) =
     check(ccall((:lm_ctx_synchronize, LIB), Cint, (Ptr{Cvoid},), ctx.handle), ctx.handle)
@@ -611,6 +612,6 @@ export ChebyshevGPU, DeviceLattice, DeviceState, gpu_tightbinding, bond_currents
        gpu_timesequence, GPUBatch, DensityLossProblem, density_loss, GPUSparseHamiltonian, set_values!, gpu_operator_currents,
        gpu_operator_timesequence, gpu_synchronize, set_option!, set_weights!, gpu_trace, gpu_norms, gpu_renormalize!,
        device_pointer, solver_order, spectral_bounds, padded_bounds, kpm_moments, chebyshev_coefficients,
-       gpu_densitymatrix, gpu_entry_currents, LM_OPT_FUSED, LM_OPT_STREAM
+       gpu_densitymatrix, gpu_entry_currents, LM_OPT_FUSED, LM_OPT_STREAM, LM_OPT_KPM
 
 end # module
