@@ -356,7 +356,7 @@ def run_adjoint_workload(args):
 
 # ------------------------------------------------------------------------------------------
 KPM_WORKLOAD = ("SquareLattice(256,256) periodic x/y, t1=1, LandauGauge(0.01), Anderson U[-1,1], "
-                "256 random-phase vectors, 2048 Chebyshev moments (FP64)")
+                "256 random-phase vectors, 2048 Chebyshev moments")
 
 
 def run_kpm_workload(args):
