@@ -75,9 +75,9 @@ int lm_ctx_stream(lm_ctx *ctx, void **stream);
  * fused step in its x-streaming form (a warp walks one ket along x with a halo only in y);
  * 0 selects the region form (a halo on both axes).  Both give bit-identical results. */
 #define LM_OPT_STREAM 2
-/* LM_OPT_KPM (default 1): the recurrence of lm_kpm_moments runs in double-float arithmetic
- * (pairs of FP32 values, about 48 significant bits) on the FP32 pipe; 0 selects FP64.  The
- * moments agree to about 1e-15 mu_0. */
+/* LM_OPT_KPM (default 1): the recurrences of lm_kpm_moments and lm_cheb_apply run in
+ * double-float arithmetic (pairs of FP32 values, about 48 significant bits) on the FP32 pipe;
+ * 0 selects FP64.  KPM moments agree to about 1e-15 mu_0. */
 #define LM_OPT_KPM 3
 int lm_ctx_set_option(lm_ctx *ctx, int option, int value);
 /* Number of fused steps that ran in the x-streaming form on this context so far. */

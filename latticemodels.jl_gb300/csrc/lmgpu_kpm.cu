@@ -162,12 +162,22 @@ __global__ void df_tables_kernel(const double2* __restrict__ hop2, const double*
     }
 }
 
+// In place: n float4 df values -> n double2 values.
+__global__ void from_df_kernel(double2* __restrict__ a, int64_t n) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const float4 v = reinterpret_cast<const float4*>(a)[i];
+        a[i] = make_double2(df_value(DF{v.x, v.y}), df_value(DF{v.z, v.w}));
+    }
+}
+
 // out = (2H~) tp - tpp on df blocks (the tables hold 2H/a and 2(V-b)/a); out may alias tpp.
-// XR: every x-hop is real.
+// XR: every x-hop is real.  With y non-null also y += c out (c = c_hi + c_lo, the real
+// coefficient of a Chebyshev series, lm_cheb_apply).
 template <bool XR>
 __global__ void __launch_bounds__(256) df_recur_kernel(Geom g, const float4* __restrict__ hopd,
                                                        const float2* __restrict__ diagd, const float4* tp,
-                                                       const float4* tpp, float4* out, int64_t ld, int64_t M) {
+                                                       const float4* tpp, float4* out, int64_t ld, int64_t M,
+                                                       float4* __restrict__ y, float c_hi, float c_lo) {
     const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= g.N) return;
     const Nbr nb = neighbours(g, s);
@@ -189,6 +199,12 @@ __global__ void __launch_bounds__(256) df_recur_kernel(Geom g, const float4* __r
         df_cfma<false>(ar, ai, hym, tp[o + nb.ym]);
         df_cfma<true>(ar, ai, d, tp[o + s]);
         out[o + s] = make_float4(ar.h, ar.l, ai.h, ai.l);
+        if (y) {
+            const float4 u = y[o + s];
+            const DF c = DF{c_hi, c_lo};
+            const DF yr = df_add(DF{u.x, u.y}, df_mul(c, ar)), yi = df_add(DF{u.z, u.w}, df_mul(c, ai));
+            y[o + s] = make_float4(yr.h, yr.l, yi.h, yi.l);
+        }
     }
 }
 
@@ -405,9 +421,11 @@ int lm_kpm_moments(lm_ham* h, double emin, double emax, int nmom, const lm_state
         // T_{n+2} = 2 H~ T_{n+1} - T_n, written over T_n
         if (use_df) {
             if (xr) df_recur_kernel<true><<<rgrid, 256, 0, ctx->stream>>>(g, hopd, diagd, (const float4*)Tn1,
-                                                                          (const float4*)Tn, (float4*)Tn, ld, M);
+                                                                          (const float4*)Tn, (float4*)Tn, ld, M,
+                                                                          nullptr, 0.f, 0.f);
             else df_recur_kernel<false><<<rgrid, 256, 0, ctx->stream>>>(g, hopd, diagd, (const float4*)Tn1,
-                                                                        (const float4*)Tn, (float4*)Tn, ld, M);
+                                                                        (const float4*)Tn, (float4*)Tn, ld, M,
+                                                                        nullptr, 0.f, 0.f);
             ctx->launches++;
             e = cudaGetLastError();
         } else {
@@ -470,12 +488,15 @@ int lm_cheb_apply(lm_ham* h, double emin, double emax, const double* coef, int n
     double2* TA = nullptr;
     double2* TB = nullptr;
     double2* Y = nullptr;
+    float4* hopd = nullptr;  // double-float tables (LM_OPT_KPM, default on)
+    float2* diagd = nullptr;
+    const bool use_df = ctx->kpm_df != 0 && ncoef > 2;
     const int64_t ld = N;
     const size_t blk = sizeof(double2) * (size_t)ld * (size_t)M;
     auto release = [&]() {
         cudaStreamSynchronize(ctx->stream);
         cudaFree(hop2); cudaFree(diag2); cudaFree(hop2f); cudaFree(diag2f);
-        cudaFree(TA); cudaFree(TB); cudaFree(Y);
+        cudaFree(TA); cudaFree(TB); cudaFree(Y); cudaFree(hopd); cudaFree(diagd);
     };
     cudaError_t e = cudaMalloc((void**)&hop2, sizeof(double2) * 2 * (size_t)N);
     if (e == cudaSuccess) e = cudaMalloc((void**)&diag2, sizeof(double) * (size_t)N);
@@ -484,6 +505,8 @@ int lm_cheb_apply(lm_ham* h, double emin, double emax, const double* coef, int n
     if (e == cudaSuccess) e = cudaMalloc((void**)&TA, blk);
     if (e == cudaSuccess && ncoef > 1) e = cudaMalloc((void**)&TB, blk);
     if (e == cudaSuccess) e = cudaMalloc((void**)&Y, blk);
+    if (e == cudaSuccess && use_df) e = cudaMalloc((void**)&hopd, sizeof(float4) * 2 * (size_t)N);
+    if (e == cudaSuccess && use_df) e = cudaMalloc((void**)&diagd, sizeof(float2) * (size_t)N);
     if (e != cudaSuccess) {
         cudaGetLastError();
         release();
@@ -521,11 +544,41 @@ int lm_cheb_apply(lm_ham* h, double emin, double emax, const double* coef, int n
         if (e != cudaSuccess) return fail(e, "lm_cheb_apply: recurrence");
         double2* Tprev = TA;
         double2* Tn = TB;
+        const unsigned cgrid = (unsigned)std::min<int64_t>((ld * M + 255) / 256, 65535);
+        if (use_df) {  // T_0, T_1 and Y (FP64 so far) become double-float in place; so do the tables
+            df_tables_kernel<<<(unsigned)std::min<int64_t>((2 * N + 255) / 256, 65535), 256, 0, ctx->stream>>>(
+                hop2, diag2, N, hopd, diagd);
+            to_df_kernel<<<cgrid, 256, 0, ctx->stream>>>(TA, ld * M);
+            to_df_kernel<<<cgrid, 256, 0, ctx->stream>>>(TB, ld * M);
+            to_df_kernel<<<cgrid, 256, 0, ctx->stream>>>(Y, ld * M);
+            ctx->launches += 4;
+            e = cudaGetLastError();
+            if (e != cudaSuccess) return fail(e, "lm_cheb_apply: double-float conversion");
+        }
+        const dim3 rgrid((unsigned)((N + 255) / 256), (unsigned)(M < 65535 ? M : 65535));
         for (int k = 2; k < ncoef; ++k) {
-            e = launch_stencil_recur(ctx, g, LM_C64, hop2, diag2, Tn, Tprev, nullptr, Tprev, ld, M, 1.0, 0.0, 0.0, Y,
-                                     coef[k], xr);
+            if (use_df) {
+                const float c_hi = (float)coef[k], c_lo = (float)(coef[k] - (double)c_hi);
+                if (xr) df_recur_kernel<true><<<rgrid, 256, 0, ctx->stream>>>(g, hopd, diagd, (const float4*)Tn,
+                                                                              (const float4*)Tprev, (float4*)Tprev,
+                                                                              ld, M, (float4*)Y, c_hi, c_lo);
+                else df_recur_kernel<false><<<rgrid, 256, 0, ctx->stream>>>(g, hopd, diagd, (const float4*)Tn,
+                                                                            (const float4*)Tprev, (float4*)Tprev,
+                                                                            ld, M, (float4*)Y, c_hi, c_lo);
+                ctx->launches++;
+                e = cudaGetLastError();
+            } else {
+                e = launch_stencil_recur(ctx, g, LM_C64, hop2, diag2, Tn, Tprev, nullptr, Tprev, ld, M, 1.0, 0.0, 0.0,
+                                         Y, coef[k], xr);
+            }
             if (e != cudaSuccess) return fail(e, "lm_cheb_apply: recurrence");
             std::swap(Tprev, Tn);
+        }
+        if (use_df) {
+            from_df_kernel<<<cgrid, 256, 0, ctx->stream>>>(Y, ld * M);
+            ctx->launches++;
+            e = cudaGetLastError();
+            if (e != cudaSuccess) return fail(e, "lm_cheb_apply: double-float conversion");
         }
     }
     if (out->precision == LM_C64)
