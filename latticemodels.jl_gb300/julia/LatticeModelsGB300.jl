@@ -474,7 +474,7 @@ end
 # ---- context options, state utilities -----------------------------------------------------------
 const LM_OPT_FUSED = Cint(1)   # 0: one launch per Chebyshev order for ComplexF32 states
 const LM_OPT_STREAM = Cint(2)  # 0: the region form of the fused step instead of the x-streaming form
-const LM_OPT_KPM = Cint(3)     # 0: the FP64 KPM recurrence instead of double-float
+const LM_OPT_KPM = Cint(3)     # 0: FP64 KPM and Fermi-operator recurrences instead of double-float
 
 gpu_synchronize(ctx::Context=default_context()) =
     check(ccall((:lm_ctx_synchronize, LIB), Cint, (Ptr{Cvoid},), ctx.handle), ctx.handle)

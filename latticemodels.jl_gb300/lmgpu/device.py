@@ -36,8 +36,8 @@ class Context:
         self.check(self.lib.lm_ctx_set_option(self.handle, _lib.LM_OPT_STREAM, 1 if on else 0))
 
     def set_kpm_doublefloat(self, on: bool):
-        """KPM moment recurrence in double-float (FP32 pairs, on the FP32 pipe; the default) or
-        FP64; the moments agree to about 1e-15 mu_0."""
+        """KPM and Fermi-operator (lm_cheb_apply) recurrences in double-float (FP32 pairs, on the
+        FP32 pipe; the default) or FP64; KPM moments agree to about 1e-15 mu_0."""
         self.check(self.lib.lm_ctx_set_option(self.handle, _lib.LM_OPT_KPM, 1 if on else 0))
 
     def stream_launches(self) -> int:
