@@ -136,18 +136,32 @@ def measured_peak_hbm():
     return 6800.0, "fallback"
 
 
-def profile_traffic(summary: str = "cheb_fused_c32_256x256.md"):
-    """DRAM bytes per launch of the dominant kernel from the committed ncu summary, if any."""
-    f = ROOT / "profiles" / summary
+TRAFFIC_RECORD = "cheb_stream_c32_256x256.traffic.json"
+
+
+def kernel_source_hash(sources):
+    """sha256 over the kernel's source files (repo-relative paths), in the listed order."""
+    import hashlib
+    h = hashlib.sha256()
+    for rel in sources:
+        h.update((ROOT / rel).read_bytes())
+    return h.hexdigest()
+
+
+def profile_traffic(record: str = TRAFFIC_RECORD):
+    """DRAM bytes per launch of the dominant kernel from the committed ncu record, valid only
+    while the kernel's sources hash to the value the record was captured with.
+
+    Returns (bytes per captured launch, sites x kets of the captured launch, record) or
+    (None, None, reason)."""
+    f = ROOT / "profiles" / record
     if not f.exists():
-        return None
-    for ln in f.read_text().splitlines():
-        if ln.startswith("traffic_bytes_per_launch_full:"):
-            try:
-                return float(ln.split(":", 1)[1].strip().split()[0])
-            except ValueError:
-                return None
-    return None
+        return None, None, "no ncu record"
+    rec = json.loads(f.read_text())
+    if kernel_source_hash(rec["sources"]) != rec["source_sha256"]:
+        return None, None, "stale ncu record: the kernel's sources changed since the capture"
+    return (float(rec["dram_bytes_read"]) + float(rec["dram_bytes_write"]),
+            float(rec["sites"]) * float(rec["kets"]), rec)
 
 
 def dist_info():
@@ -157,17 +171,17 @@ def dist_info():
     return rank, world, local
 
 
-def cpu_reference(steps, warmup, sample_kets=None, cpu_seconds=None):
+def cpu_reference(steps, warmup, sample_kets=None, cpu_seconds=None, nthreads=None):
     """Times the oracle's C restatement of KrylovKitExp on a bounded sample of the workload.
 
     With ``cpu_seconds`` the number of timed steps is chosen so that the sample costs about
-    that much CPU time (wall time x threads)."""
+    that much CPU time (wall time x threads).  ``nthreads`` None: all host threads."""
     from oracle import krylov, lm_oracle as o
     lat = o.SquareLattice(LX, LY, periodic=(True, True))
     V = make_disorder(lat.N)
     H, _, _, _ = o.tightbinding_hamiltonian_fast(lat, field=o.LandauGauge(B_FIELD), onsite=V)
     csr = krylov.CSR(H)
-    threads = krylov.max_threads()
+    threads = nthreads or krylov.max_threads()
     mk = sample_kets or 2 * threads
     X = make_kets(lat.N, mk)
     t_one = None
@@ -605,6 +619,9 @@ def main():
                     help="kets workload: side of the periodic square lattice (512 with --kets 1024 is config 3)")
     ap.add_argument("--fused-form", default="stream", choices=["stream", "region"],
                     help="form of the fused c32 step: x-streaming (where the lattice allows) or region")
+    ap.add_argument("--err-steps", type=int, default=400,
+                    help="steps of the untimed pass that measures the chosen form's error against FP64 "
+                         "(400: the plain-method configuration's full length)")
     ap.add_argument("--tol32", type=float, default=1e-9,
                     help="series truncation of the FP32 form (1e-9 keeps 200-step runs within 1e-6; "
                          "1e-7 is one order cheaper and enough for short runs)")
@@ -698,73 +715,77 @@ def main():
     clocks["window"] = "sampled every 100 ms over the timed c32 and c64 passes"
     K64, _, _ = solver64.order(s64)
 
-    # ---- error of the chosen form against FP64 after the same steps --------------------
-    # s32 ran 2*(warmup+steps) steps; bring s64 to the same time
-    for _ in range(args.warmup + args.steps):
-        solver64.step(s64)
-    r32 = lmgpu.localdensity(s32).values
-    r64 = lmgpu.localdensity(s64).values
-    J32 = lmgpu.DensityCurrents(H, s32).bond_values()
-    J64 = lmgpu.DensityCurrents(H, s64).bond_values()
-    nrm32 = s32.norms()
-    err = {"density": float(np.linalg.norm(r32 - r64) / np.linalg.norm(r64)),
-           "currents": float(np.linalg.norm(J32 - J64) / np.linalg.norm(J64)),
-           "norm_drift": float(np.abs(nrm32 - 1.0).max()),
-           "steps": 2 * (args.warmup + args.steps)}
     del s64
 
     # ---- end to end through the public API with host buffers ----------------------------
+    # The reference README's loop: every moment of ev(times) yields localdensity(P) and
+    # DensityCurrents(H, P), and h(t) is a genuinely time-dependent Hamiltonian (the Landau
+    # amplitude and the on-site potential both change every step; the potential is written
+    # into pinned host memory each step, uploaded and assembled on the device).
     pin_X = torch.empty((M, N), dtype=torch.complex64, pin_memory=True)
     Xh = pin_X.numpy().T  # (N, M) Fortran view of pinned memory
     Xh[:] = X.astype(np.complex64)
-    pin_V = [torch.empty(N, dtype=torch.float64, pin_memory=True) for _ in range(2)]
-    for pv in pin_V:
-        pv.numpy()[:] = V
-    pin_rho = torch.empty(N, dtype=torch.float64, pin_memory=True).numpy()
-    field = lmgpu.LandauGauge(B_FIELD)
-    # a fresh host view every call: the on-site term is re-uploaded and H re-assembled each step
-    h = lambda t: lmgpu.tightbinding_hamiltonian(lat, pin_V[int(round(t / DT)) % 2].numpy(), field=field)
-    from lmgpu.observables import localdensity_into
+    pin_V = [torch.empty(N, dtype=torch.float64, pin_memory=True).numpy() for _ in range(2)]
+    nb = int(lat.nbonds())
+
+    def h(t):
+        k = int(round(t / DT))
+        pv = pin_V[k % 2]
+        np.add(V, 0.05 * math.sin(0.5 * t), out=pv)
+        return lmgpu.tightbinding_hamiltonian(lat, pv, field=lmgpu.LandauGauge(B_FIELD * (1.0 + 0.1 * math.sin(t))))
+
     e2e_state = lmgpu.DeviceState(lat, None, 0, "c32", shape=(N, M))
     ev = lmgpu.Evolution(lmgpu.ChebyshevGPU(tol=args.tol32, renorm_every=20), h, e2e_state)
     evs = ev.current_states()[0]
     times = [DT * (k + 1) for k in range(args.steps)]
-    evs.upload_from(Xh)  # untimed warm-up of the pinned-buffer upload (its first use can be slow)
-    for _ in ev([DT * (k + 1) for k in range(args.warmup)]):
-        localdensity_into(evs, pin_rho)
-    lmgpu.TimeSequence(lmgpu.moment_density, ev([ev.time + DT]), nslots=8)  # ring allocated once, untimed
+    readouts = [lmgpu.moment_density, lmgpu.moment_currents]
+    evs.upload_from(Xh)  # untimed warm-up of the pinned-buffer upload and of both readout rings
+    lmgpu.timesequences(readouts, ev([DT * (k + 1) for k in range(args.warmup)]), nslots=8)
     e0 = torch.cuda.Event(enable_timing=True)
     eu = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
 
-    def timed_e2e(ring):
-        # ring: TimeSequence(moment_density, ev(times)) -- readouts through the device ring,
-        # downloaded asynchronously; otherwise one synchronous localdensity per moment
-        ev.time = 0.0
-        barrier()
-        e0.record(ext)
-        evs.upload_from(Xh)
-        eu.record(ext)
-        if ring:
-            ts = lmgpu.TimeSequence(lmgpu.moment_density, ev(times), nslots=8)
-            assert len(ts) == args.steps
-        else:
-            for _ in ev(times):
-                localdensity_into(evs, pin_rho)
-        e1.record(ext)
-        e1.synchronize()
-        ms = e0.elapsed_time(e1)
-        up = e0.elapsed_time(eu)
-        if dist is not None:
-            t = torch.tensor([ms], device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            ms = float(t.item())
-        return ms, up
-
-    ms_e2e_sync, _ = timed_e2e(False)
-    ms_e2e, ms_upload = timed_e2e(True)
+    ev.time = 0.0
+    barrier()
+    e0.record(ext)
+    evs.upload_from(Xh)
+    eu.record(ext)
+    ts_rho, ts_J = lmgpu.timesequences(readouts, ev(times), nslots=8)
+    e1.record(ext)
+    e1.synchronize()
+    assert len(ts_rho) == args.steps and len(ts_J) == args.steps
+    ms_e2e = e0.elapsed_time(e1)
+    ms_upload = e0.elapsed_time(eu)
+    if dist is not None:
+        t_ = torch.tensor([ms_e2e], device="cuda")
+        dist.all_reduce(t_, op=dist.ReduceOp.MAX)
+        ms_e2e = float(t_.item())
     h2d = (N * M * 8 + args.steps * N * 8) / args.steps
-    d2h = N * 8
+    d2h = N * 8 + nb * 8
+    del e2e_state, ev, evs
+
+    # ---- error of the chosen form against FP64 over the configuration's full length -----
+    # an untimed pass: both forms from the same kets, err_steps steps of the same H and dt
+    s32e = lmgpu.KetBlock(lat, X, precision="c32")
+    s64e = lmgpu.KetBlock(lat, X, precision="c64")
+    sol32e = lmgpu.ChebyshevGPU(tol=args.tol32, renorm_every=20)
+    sol64e = lmgpu.ChebyshevGPU()
+    c32e = sol32e.evolution_cache(s32e)
+    sol32e.update_solver(H, DT)
+    sol64e.update_solver(H, DT)
+    for _ in range(args.err_steps):
+        sol32e.step(s32e, c32e)
+        sol64e.step(s64e)
+    r32 = lmgpu.localdensity(s32e).values
+    r64 = lmgpu.localdensity(s64e).values
+    J32 = lmgpu.DensityCurrents(H, s32e).bond_values()
+    J64 = lmgpu.DensityCurrents(H, s64e).bond_values()
+    err = {"density": float(np.linalg.norm(r32 - r64) / np.linalg.norm(r64)),
+           "currents": float(np.linalg.norm(J32 - J64) / np.linalg.norm(J64)),
+           "norm_drift": float(np.abs(s32e.norms() - 1.0).max()),
+           "norm_drift_fp64": float(np.abs(s64e.norms() - 1.0).max()),
+           "steps": args.err_steps, "kets": M}
+    del s32e, s64e
 
     # ---- report ----------------------------------------------------------------------
     if rank != 0:
@@ -782,16 +803,27 @@ def main():
     avg_launch_ms = order_ms / sweeps
     achieved = alg_bytes_launch / (avg_launch_ms / 1000.0) / 1e9
     peak, peak_kind = measured_peak_hbm()
+    traffic, traffic_src = None, None
     if streamed:
-        kname = "cheb_stream_c32_kernel (x-streaming form: all K orders of one step per launch)"
-        traffic = profile_traffic("cheb_stream_c32_256x256.md")
+        kname = f"cheb_stream_c32_kernel<{K32}, 3> (x-streaming form: all K orders of one step per launch)"
+        t_cap, units_cap, rec = profile_traffic()
+        if t_cap is not None and rec.get("K") == K32:
+            traffic = t_cap * (N * M) / units_cap
+            traffic_src = (f"ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch at {rec['sites']} sites x "
+                           f"{rec['kets']} kets (profiles/{TRAFFIC_RECORD}, source sha256 {rec['source_sha256'][:12]} "
+                           f"matches), scaled by sites x kets")
+        else:
+            traffic_src = rec if isinstance(rec, str) else "ncu record is for another order"
     else:
         kname = "cheb_fused_c32_kernel (region form: all K orders of one step per launch)"
-        traffic = profile_traffic()
-    # the summaries hold the 256x256-site, 2048-ket launch; the traffic grows with sites x kets
-    traffic_scale = (N * M) / (65536.0 * 2048.0)
-    if traffic is not None:
-        traffic *= traffic_scale
+        traffic_src = "no ncu record for the region form in this build"
+    # FP32 FMA pipe: the useful FMAs of a site-order are the real diagonal (2), the real x-hops
+    # of the Landau gauge (2 x 2), the complex y-hops (2 x 4) and the accumulator term (2)
+    fma_site_order = 16
+    props = torch.cuda.get_device_properties(local)
+    sm_mhz = clocks.get("sm_mhz") or clocks.get("sm_max_mhz") or 2070.0
+    fma_peak = props.multi_processor_count * 128 * sm_mhz * 1e6
+    fma_rate = fma_site_order * N * M * K32 / (avg_launch_ms / 1000.0)
     line = {
         "metric": METRIC, "value": value, "unit": "ket-steps/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms32 / args.steps,
@@ -811,30 +843,31 @@ def main():
                      "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
                      "kernel": kname,
                      "alg_bytes_per_launch": alg_bytes_launch, "avg_launch_ms": avg_launch_ms,
-                     "launches_timed": sweeps,
-                     "traffic_source": ("ncu dram__bytes_read.sum + dram__bytes_write.sum of the 256^2 x 2048-ket "
-                                        "launch (512-ket capture x 4), scaled by sites x kets"
-                                        + ("" if traffic_scale == 1.0 else f" (x {traffic_scale:g})")),
-                     # the temporally blocked kernel moves ~1.8 block passes per step instead of
-                     # the 5 K of the per-order formula: its DRAM rate is far below the peak
+                     "launches_timed": sweeps, "traffic_source": traffic_src,
+                     # physical fractions: what the temporally blocked kernel really moves and
+                     # computes per launch
                      "dram_gbs": (traffic / (avg_launch_ms / 1000.0) / 1e9) if traffic else None,
                      "dram_frac": (traffic / (avg_launch_ms / 1000.0) / 1e9 / peak) if traffic else None,
-                     "note": "frac > 1: all K orders of a step run on chip, so the per-order algorithmic "
-                             "bytes exceed the DRAM bytes moved (see dram_gbs); the kernel is issue-bound"},
+                     "fma_frac": fma_rate / fma_peak,
+                     "fma_note": (f"{fma_site_order} useful FP32 FMAs per site-order x N x M x K per launch / "
+                                  f"({props.multi_processor_count} SMs x 128 FMA/clk x {sm_mhz:.0f} MHz median "
+                                  f"SM clock of the run)"),
+                     "note": "frac is the per-order formula 5*K*N*M*s: all K orders of a step run on chip, so "
+                             "it exceeds 1; dram_frac and fma_frac are the physical fractions"},
         "e2e": {"value": world * M * args.steps / (ms_e2e / 1000.0), "unit": "ket-steps/s",
                 "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                 "ms_per_step": ms_e2e / args.steps,
-                "path": "Evolution(ChebyshevGPU, t -> tightbinding_hamiltonian(l, V(t); field)) over "
-                        "TimeSequence(moment_density, ev(times)): readout ring, asynchronous downloads",
-                "upload_ms": ms_upload,
-                "sync_readout": {"value": world * M * args.steps / (ms_e2e_sync / 1000.0),
-                                 "ms_per_step": ms_e2e_sync / args.steps,
-                                 "path": "one synchronous localdensity per moment"}},
+                "path": "Evolution(ChebyshevGPU, t -> tightbinding_hamiltonian(l, V(t); LandauGauge(B(t)))) "
+                        "over timesequences([moment_density, moment_currents], ev(times)): both readouts "
+                        "every moment through readout rings, asynchronous downloads",
+                "upload_ms": ms_upload},
         "gpu_launches": int(launches32),
         "clocks": clocks,
     }
     if world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_reference(1, 1, cpu_seconds=20.0)
+        one = cpu_reference(1, 1, sample_kets=2, cpu_seconds=8.0, nthreads=1)
+        line["cpu_baseline"]["single_core"] = {k: one[k] for k in ("value", "unit", "cores", "sample")}
     print(json.dumps(line))
     if dist is not None:
         dist.barrier()

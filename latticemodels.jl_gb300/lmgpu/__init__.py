@@ -19,7 +19,7 @@ from .sparse import LocalOperatorCurrents, SiteCurrents, Sites, SparseHamiltonia
 from .spectrum import densitymatrix, diagonalize
 from .states import DensityMatrix, DeviceState, Ket, KetBlock, Operator
 from .timesequence import (ReadoutRing, TimeSequence, differentiate, integrate, moment_currents,
-                           moment_density)
+                           moment_density, timesequences)
 
 __all__ = [
     "adjoint", "kpm", "DensityLossAdjoint", "Batch", "LMError", "load_library", "Context", "default_context",
@@ -29,4 +29,5 @@ __all__ = [
     "Currents", "DensityCurrents", "SubCurrents", "currentsfrom", "currentsfromto", "localdensity", "densitymatrix", "diagonalize",
     "DensityMatrix", "DeviceState", "Ket", "KetBlock", "Operator",
     "LocalOperatorCurrents", "SiteCurrents", "Sites", "SparseHamiltonian", "entry_currents", "ReadoutRing", "TimeSequence", "differentiate", "integrate", "moment_currents", "moment_density",
+    "timesequences",
 ]

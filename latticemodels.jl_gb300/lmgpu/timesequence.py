@@ -84,9 +84,9 @@ class ReadoutRing:
 _rings: dict = {}
 
 
-def _ring_for(ctx, length: int, nslots: int) -> ReadoutRing:
+def _ring_for(ctx, length: int, nslots: int, index: int = 0) -> ReadoutRing:
     """A ring reused across TimeSequence calls (its pinned slots are allocated once)."""
-    key = (id(ctx), int(length), int(nslots))
+    key = (id(ctx), int(length), int(nslots), int(index))
     r = _rings.get(key)
     if r is None:
         if len(_rings) >= 8:
@@ -110,6 +110,79 @@ def moment_currents(moment):
 
 moment_density._lm_readout = "density"
 moment_currents._lm_readout = "currents"
+
+
+def _collect_rings(pairs, it, nslots):
+    """Feeds every moment of ``it`` to the ring readouts of ``pairs`` [(f, TimeSequence)]: each
+    readout is pushed into its own ring, and an entry is collected only when its slot is about
+    to be reused (or at the end), so the loop never waits for a step."""
+    from .observables import _site_sum
+    from .sparse import SparseHamiltonian
+    slots = [None] * len(pairs)  # per readout: (ring, pending sequence numbers, wrap)
+    for moment in it:
+        st = moment.state
+        general = isinstance(moment.H, SparseHamiltonian)
+        for i, (f, ts) in enumerate(pairs):
+            kind = f._lm_readout
+            if slots[i] is None:
+                if kind == "density":
+                    length = st.n
+                elif general:
+                    length = max(len(moment.H.rowval), 1)
+                else:
+                    length = max(st.lattice.nbonds(), 1)
+                wrap = ((lambda v, lat=st.lattice: LatticeValue(lat, _site_sum(lat, v))) if kind == "density"
+                        else (lambda v: v))
+                # two readouts of the same kind and length would share a ring: give each its own
+                same = sum(1 for j in range(i) if slots[j] is not None and slots[j][0].length == length)
+                slots[i] = (_ring_for(st.ctx, length, nslots, same), [], wrap)
+            ring, pending, wrap = slots[i]
+            if len(pending) == ring.nslots:  # the oldest slot is about to be reused
+                _take(ts, ring, pending.pop(0), wrap)
+            if kind == "density":
+                pending.append(ring.push_density(st, moment.t))
+            elif general:
+                pending.append(ring.push_op_currents(moment.H, st, moment.t))
+            else:
+                pending.append(ring.push_currents(moment.H, st, moment.t))
+    for (f, ts), sl in zip(pairs, slots):
+        if sl is None:
+            continue
+        ring, pending, wrap = sl
+        for seq in pending:
+            _take(ts, ring, seq, wrap)
+
+
+def _take(ts, ring, seq, wrap):
+    t, v = ring.wait(seq)
+    ts.times.append(t)
+    ts.values.append(wrap(v))
+
+
+def timesequences(fs, it, nslots: int = 8):
+    """One ``TimeSequence`` per readout in ``fs``, all filled from a single pass over the
+    evolution iterator ``it``: the loop of the reference's README example, which computes
+    ``localdensity(P)`` and ``DensityCurrents(H, P)`` at every moment of ``ev(times)``.
+
+    ``moment_density`` and ``moment_currents`` go through device readout rings (asynchronous
+    downloads); any other callable is applied to each moment as it is yielded."""
+    out = [TimeSequence() for _ in fs]
+    ring_pairs = [(f, ts) for f, ts in zip(fs, out) if getattr(f, "_lm_readout", None) is not None]
+    plain = [(f, ts) for f, ts in zip(fs, out) if getattr(f, "_lm_readout", None) is None]
+    if plain:
+        def tee(src):
+            for moment in src:
+                for f, ts in plain:
+                    ts.times.append(float(moment.t))
+                    ts.values.append(f(moment))
+                yield moment
+        it = tee(it)
+    if ring_pairs:
+        _collect_rings(ring_pairs, it, nslots)
+    else:
+        for _ in it:
+            pass
+    return out
 
 
 class TimeSequence:
@@ -137,45 +210,12 @@ class TimeSequence:
         self.values = vs
 
     def _collect(self, f, it, nslots):
-        kind = getattr(f, "_lm_readout", None)
-        if kind is None:
+        if getattr(f, "_lm_readout", None) is None:
             for moment in it:
                 self.times.append(float(moment.t))
                 self.values.append(f(moment))
             return
-        ring = None
-        pending = []  # sequence numbers not yet collected
-        wrap = None
-        from .observables import _site_sum
-        from .sparse import SparseHamiltonian
-        for moment in it:
-            st = moment.state
-            general = isinstance(moment.H, SparseHamiltonian)
-            if ring is None:
-                if kind == "density":
-                    length = st.n
-                elif general:
-                    length = max(len(moment.H.rowval), 1)
-                else:
-                    length = max(st.lattice.nbonds(), 1)
-                ring = _ring_for(st.ctx, length, nslots)
-                wrap = ((lambda v, lat=st.lattice: LatticeValue(lat, _site_sum(lat, v))) if kind == "density"
-                        else (lambda v: v))
-            if len(pending) == ring.nslots:  # the oldest slot is about to be reused
-                self._take(ring, pending.pop(0), wrap)
-            if kind == "density":
-                pending.append(ring.push_density(st, moment.t))
-            elif general:
-                pending.append(ring.push_op_currents(moment.H, st, moment.t))
-            else:
-                pending.append(ring.push_currents(moment.H, st, moment.t))
-        for seq in pending:
-            self._take(ring, seq, wrap)
-
-    def _take(self, ring, seq, wrap):
-        t, v = ring.wait(seq)
-        self.times.append(t)
-        self.values.append(wrap(v))
+        _collect_rings([(f, self)], it, nslots)
 
     # --- AbstractDict{Float64, ET} surface of the reference --------------------------------
     def timestamps(self):

@@ -1,5 +1,5 @@
 """Host-side helpers of bench.py (no GPU): the synthetic inputs, the profiled DRAM traffic
-read from the committed ncu summaries, and the roofline peak lookup."""
+read from the committed ncu record, and the roofline peak lookup."""
 import importlib.util
 import os
 
@@ -26,11 +26,29 @@ def test_kets_are_seeded_normalised_and_column_major(bench):
     assert not np.array_equal(X, bench.make_kets(300, 7, rank=1, dtype=np.complex64))
 
 
-def test_profiled_traffic_of_the_streaming_kernel(bench):
-    """The bench's roofline `traffic` is the committed ncu figure of the full launch."""
-    t = bench.profile_traffic("cheb_stream_c32_256x256.md")
-    assert t is not None and 2.0e9 < t < 4.0e9  # about 1.7 reads + 0.9 writes of a 1.07 GB block
-    assert bench.profile_traffic("no_such_summary.md") is None
+def test_profiled_traffic_of_the_streaming_kernel(bench, tmp_path, monkeypatch):
+    """The bench's roofline `traffic` comes from a committed ncu record that names the kernel's
+    sources and their sha256; a record whose sources changed is refused."""
+    import json
+    t, units, rec = bench.profile_traffic()
+    if t is None:  # the kernel changed since the capture: the record must say so, not be used
+        assert rec.startswith("stale") or rec == "no ncu record"
+    else:
+        per_unit = t / units  # bytes per site-ket of one launch
+        assert 8 * 1.5 < per_unit < 8 * 4.0, per_unit  # between 1.5 and 4 passes over a c32 block
+    assert bench.profile_traffic("no_such_record.json") == (None, None, "no ncu record")
+    # a record whose hash does not match its sources
+    src = json.loads((bench.ROOT / "profiles" / bench.TRAFFIC_RECORD).read_text())
+    src["source_sha256"] = "0" * 64
+    fake = tmp_path / "profiles"
+    fake.mkdir()
+    (fake / "x.json").write_text(json.dumps(src))
+    monkeypatch.setattr(bench, "ROOT", tmp_path)
+    for rel in src["sources"]:
+        (tmp_path / rel).parent.mkdir(parents=True, exist_ok=True)
+        (tmp_path / rel).write_text("changed kernel")
+    t, _, why = bench.profile_traffic("x.json")
+    assert t is None and why.startswith("stale")
 
 
 def test_peak_lookup(bench):
@@ -44,5 +62,8 @@ def test_every_profile_names_a_committed_command():
     pdir = os.path.join(ROOT, "profiles")
     for name in os.listdir(pdir):
         text = open(os.path.join(pdir, name)).read()
+        if name.endswith(".json"):
+            import json
+            text = json.loads(text)["command"]
         assert "python bench.py" in text, name
         assert "_work/" not in text, name

@@ -107,16 +107,27 @@ def test_differentiation_workload_fd(lm):
     h = 1e-4
     iv = rng.choice(L * L, size=24, replace=False)
     ib = rng.choice(50, size=8, replace=False)
-    errs = []
+    _, gV64, gB64 = p64.loss_and_grad(V, B)  # the FP64 adjoint separates FP32 error from FD error
+    fd, g32, g64 = [], [], []
     for i in iv:
         e = np.zeros(L * L); e[i] = h
-        fd = (p64.loss(V + e, B) - p64.loss(V - e, B)) / (2 * h)
-        errs.append(abs(gV[i] - fd) / max(abs(fd), 1e-12))
+        fd.append((p64.loss(V + e, B) - p64.loss(V - e, B)) / (2 * h))
+        g32.append(gV[i]); g64.append(gV64[i])
     for j in ib:
         e = np.zeros(50); e[j] = h
-        fd = (p64.loss(V, B + e) - p64.loss(V, B - e)) / (2 * h)
-        errs.append(abs(gB[j] - fd) / max(abs(fd), 1e-12))
-    errs = np.array(errs)
-    print(f"differentiation workload: loss {loss32:.6e}, max rel err {errs.max():.3e}, median {np.median(errs):.3e}")
-    assert np.median(errs) <= 1e-5
-    assert errs.max() <= 1e-3
+        fd.append((p64.loss(V, B + e) - p64.loss(V, B - e)) / (2 * h))
+        g32.append(gB[j]); g64.append(gB64[j])
+    fd, g32, g64 = np.array(fd), np.array(g32), np.array(g64)
+    err32 = np.abs(g32 - fd) / np.maximum(np.abs(fd), 1e-12)
+    err64 = np.abs(g64 - fd) / np.maximum(np.abs(fd), 1e-12)
+    err3264 = np.abs(g32 - g64) / np.maximum(np.abs(g64), 1e-12)
+    np.set_printoptions(precision=3, linewidth=200)
+    print(f"differentiation workload: loss {loss32:.6e}; |gV| {np.linalg.norm(gV64):.3e}, |gB| {np.linalg.norm(gB64):.3e}")
+    print("  |fd|            ", np.abs(fd))
+    print("  c32 vs fd       ", err32)
+    print("  c64 vs fd       ", err64)
+    print("  c32 vs c64      ", err3264)
+    print(f"  max/median: c32-fd {err32.max():.3e}/{np.median(err32):.3e}  c64-fd {err64.max():.3e}/"
+          f"{np.median(err64):.3e}  c32-c64 {err3264.max():.3e}/{np.median(err3264):.3e}")
+    assert np.median(err32) <= 1e-5
+    assert err32.max() <= 1e-3

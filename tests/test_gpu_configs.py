@@ -97,3 +97,51 @@ def test_plain_config_256_properties(lm):
     for _ in range(400):
         s.step(st)
     assert rel(st.to_numpy(), X) <= 1e-10
+
+
+@pytest.mark.parametrize("L", [256, 512])
+def test_config_size_vs_oracle(lm, L):
+    """The plain-method (256^2) and precision (512^2) lattices at full size against the oracle.
+
+    SquareLattice(L, L) periodic on both axes, Landau 0.01 with the reference's seam on the
+    torus, Anderson disorder U[-1, 1], 8 complex-Gaussian kets, 8 steps of dt = 0.05.  The
+    oracle applies exp(-i H 8 dt) to the same kets with scipy's expm_multiply on its own
+    restatement of the Hamiltonian.  ComplexF64 (per-order kernels) must agree to 1e-10 on the
+    kets, local densities and bond currents; the ComplexF32 streaming kernel runs the same kets
+    and is held to the FP32 bar."""
+    from oracle import lm_oracle as o
+    ol = o.SquareLattice(L, L, periodic=(True, True))
+    lat = lm.SquareLattice(L, L, boundaries={"axis1": True, "axis2": True})
+    V = o.anderson_disorder(ol.N, 2.0, 100 + L)
+    Ho, _, _, _ = o.tightbinding_hamiltonian_fast(ol, field=o.LandauGauge(0.01), onsite=V)
+    X = o.random_kets(ol.N, 8, 200 + L)
+    steps, dt = 8, 0.05
+    Y = o.expm_multiply(Ho, dt * steps, X)
+    src, dst = lat.bonds()
+    rho_o = o.localdensity(Y)
+    J_o = o.bond_currents(Ho, Y, src, dst)
+    H = lm.tightbinding_hamiltonian(lat, V, field=lm.LandauGauge(0.01))
+    ctx = lm.default_context()
+    out = {}
+    for prec in ("c64", "c32"):
+        st = lm.KetBlock(lat, X, precision=prec)
+        s = lm.ChebyshevGPU()
+        s.update_solver(H, dt)
+        n0 = ctx.stream_launches()
+        for _ in range(steps):
+            s.step(st)
+        streamed = ctx.stream_launches() - n0
+        e = {"K": s.order(st)[0], "kets": rel(st.to_numpy(), Y),
+             "density": rel(lm.localdensity(st).values, rho_o),
+             "currents": rel(lm.DensityCurrents(H, st).bond_values(), J_o),
+             "norm": float(np.abs(st.norms() - 1).max()), "stream_launches": streamed}
+        out[prec] = e
+        print(f"{L}^2 periodic Landau, 8 kets x {steps} steps, {prec} vs oracle expm_multiply:", e)
+    assert out["c64"]["kets"] <= 1e-10, out
+    assert out["c64"]["density"] <= 1e-10, out
+    assert out["c64"]["currents"] <= 1e-10, out
+    assert out["c64"]["norm"] <= 1e-12, out
+    assert out["c32"]["stream_launches"] == steps, out  # the chosen form ran the streaming kernel
+    assert out["c32"]["kets"] <= 2e-6, out
+    assert out["c32"]["density"] <= 1e-6, out
+    assert out["c32"]["currents"] <= 2e-6, out

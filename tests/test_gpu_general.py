@@ -203,3 +203,31 @@ def test_local_operator_rejects(lm):
     hs = lm.Sites(18, coords, "honeycomb")
     with pytest.raises(ValueError):
         lm.LocalOperatorCurrents(lm.SparseHamiltonian(hs, Hh), lm.KetBlock(hs, o.random_kets(18, 1, 0)), np.eye(1))
+
+
+@pytest.mark.parametrize("timedomain", [False, True])
+def test_timedeps_evolution_qwz(lm, timedomain):
+    """The reference's own evolution test through the device (test/test_timedeps.jl:42-68):
+    qwz(SquareLattice(10, 10)) with two internal states per site, psi = the ground state of the
+    dense H, ts = 0:0.1:10 through Evolution(ChebyshevGPU, H, psi); psi.data[2] (1-based: site
+    1, second internal state) of every moment against exp(-i 0.1 H) applied step by step, with
+    the reference's bar: Julia's `≈ atol=1e-10` on the vector of values, i.e. norm <= 1e-10."""
+    Hs = o.qwz_hamiltonian(10, 10)
+    Hd = Hs.toarray()
+    psi = np.linalg.eigh(Hd)[1][:, 0]
+    ts = [round(0.1 * k, 10) for k in range(101)]
+    correct_ev = o.expm_exact(Hd, 0.1)
+    correct, p = [], psi.copy()
+    for _ in ts:
+        correct.append(p[1])
+        p = correct_ev @ p
+    sites = lm.Sites(200, None, "qwz", internal=2)
+    H = lm.SparseHamiltonian(sites, Hs)
+    if timedomain:  # `for st in Evolution(solver, Hs, psi, timedomain=ts)`
+        ev = lm.Evolution(lm.ChebyshevGPU(), H, lm.Ket(sites, psi), timedomain=ts)
+        vals = [m.state.to_numpy()[1, 0] for m in ev]
+    else:           # `for state in Evolution(solver, Hs, psi)(ts)`
+        ev = lm.Evolution(lm.ChebyshevGPU(), H, lm.Ket(sites, psi))
+        vals = [m[0].to_numpy()[1, 0] for m in ev(ts)]
+    assert len(vals) == 101
+    assert np.linalg.norm(np.array(vals) - np.array(correct)) <= 1e-10

@@ -145,7 +145,7 @@ def test_densitymatrix_groundstate_and_trace():
     assert abs(np.trace(P0).real - np.sum(w0 <= 0)) < 1e-10
 
 
-# --- evolution vs exact exponent (test/test_timedeps.jl:253-279; TB + Landau instead of QWZ) ---
+# --- evolution vs exact exponent (test/test_timedeps.jl:42-68) ---
 def test_evolution_matches_exact_exponent():
     l = o.SquareLattice(10, 10)
     Hs = o.tightbinding_hamiltonian(l, field=o.LandauGauge(0.1))
@@ -167,6 +167,35 @@ def test_evolution_matches_exact_exponent():
         kv.append(p[1])
     assert np.allclose(val1, correct, atol=1e-10)
     assert np.allclose(kv, correct, atol=1e-10)
+
+
+def test_timedeps_evolution_qwz():
+    """The reference's own evolution test, restated exactly (test/test_timedeps.jl:42-68):
+    qwz(SquareLattice(10, 10)) (two internal states per site), psi = groundstate(dense H),
+    ts = 0:0.1:10; psi.data[2] (1-based: site 1, second internal state) of KrylovKitExp and of
+    CachedExp(threshold = 1e-12) against exp(-i 0.1 H) applied step by step, atol 1e-10."""
+    Hs = o.qwz_hamiltonian(10, 10)
+    Hd = Hs.toarray()
+    w, V = np.linalg.eigh(Hd)
+    psi = V[:, 0]
+    ts = np.round(np.arange(0, 10.0 + 1e-9, 0.1), 10)
+    correct_ev = o.expm_exact(Hd, 0.1)
+    correct, p = [], psi.copy()
+    for _ in ts:
+        correct.append(p[1])
+        p = correct_ev @ p
+    from oracle import krylov
+    csr = krylov.CSR(Hs)
+    val1, p = [], psi.copy()
+    for i, _ in enumerate(ts):
+        if i > 0:
+            p = krylov.krylov_expv_block(csr, 0.1, p)[:, 0]
+        val1.append(p[1])
+    val2 = [st[1] for _, st, _ in o.evolve(lambda t: Hs, psi, ts, o.OracleCachedExpSolver(threshold=1e-12))]
+    assert len(val1) == len(val2) == len(correct) == 101
+    # Julia's `a ≈ b atol=1e-10` on vectors is norm(a - b) <= 1e-10 (rtol is 0 once atol is set)
+    assert np.linalg.norm(np.array(val1) - correct) <= 1e-10
+    assert np.linalg.norm(np.array(val2) - correct) <= 1e-10
 
 
 def test_evolution_iterator_semantics():
