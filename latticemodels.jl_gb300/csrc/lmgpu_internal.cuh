@@ -272,7 +272,10 @@ bool ham_x_real(const lm_ham* h);
 bool ham_uniform_columns(const lm_ham* h);
 // a, b, K, the Chebyshev coefficients and e^{-ib dt} of exp(-i H dt) on [emin, emax] (or on
 // the solver's frozen interval), lmgpu_api.cu.
-void plan_propagator(lm_solver* s, double emin, double emax, double dt);
+// K, the coefficients and the interval [b - a, b + a] for exp(-i H dt).  t_exact > 0: a is
+// raised (by at most one FP32 ulp, relative 6e-8) until 2 t_exact / a is an FP32 number, so a
+// hop of magnitude t_exact has no rounding error in the FP32 stencil tables.
+void plan_propagator(lm_solver* s, double emin, double emax, double dt, double t_exact = 0.0);
 // lm_solver_step / destroy for a solver updated with an lm_ell Hamiltonian (lmgpu_ell.cu).
 int ell_solver_step(lm_solver* s, lm_state* st);
 void ell_free_tables(lm_solver* s);

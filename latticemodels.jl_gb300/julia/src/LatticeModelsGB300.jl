@@ -1,16 +1,34 @@
 # LatticeModelsGB300 — Julia glue for the GB300 evolution backend (liblmgpu.so).
 #
-# Adds `ChebyshevGPU <: LatticeModels.EvolutionSolver` and a lazy device Hamiltonian so that
-#     Evolution(ChebyshevGPU(tol=1e-12), t -> gpu_tightbinding(l; field=PointFlux(B(t), p)), P0)
-# runs the reference's own `Evolution` driver (src/evolution.jl:183-298) on the GPU.
-# Every call goes through the C ABI declared in include/lmgpu.h.
+# A drop-in for LatticeModels.jl's time-evolution path.  The reference README example runs
+# with only the builder and solver arguments added:
+#
+#     l = SquareLattice(10, 10)
+#     h(B) = tightbinding_hamiltonian(GPUBuilder, l, field=PointFlux(B, (5.5, 5.5)))
+#     P_0 = densitymatrix(h(0), mu = 0)
+#     ev = Evolution(ChebyshevGPU, t -> h(0.2 * min(t, τ) / τ), P_0)
+#     for (P, H, t) in ev(0:0.1:2τ)
+#         localdensity(P)            # a LatticeValue, read out on the device
+#         DensityCurrents(H, P)      # lazy; Currents(...) materialises it from the device bonds
+#     end
+#
+# `GPUBuilder` plugs into the reference's builder hook `construct_operator(BT::Type, sys, ...)`
+# (src/operators/constructoperator.jl:136), so `tightbinding_hamiltonian` returns the
+# reference's own `Hamiltonian` whose `.data` is a lazy `DeviceHamiltonian`.  `densitymatrix`
+# on such a Hamiltonian returns an `Operator` whose `.data` is a `DeviceState`; the reference's
+# `Evolution` copies it (device to device) and calls the `ChebyshevGPU` plugin methods
+# `update_solver!`/`step!` (src/evolution.jl:5-33, :238-250).  Every call goes through the C ABI
+# declared in include/lmgpu.h.
 module LatticeModelsGB300
 
 using LatticeModels
-import LatticeModels: EvolutionSolver, update_solver!, step!, evolution_cache, localdensity
+import LatticeModels: EvolutionSolver, update_solver!, step!, evolution_cache, localdensity, densitymatrix,
+                      construct_operator, Currents, DensityCurrents
+import QuantumOpticsBase
+import LinearAlgebra
 using SparseArrays: SparseMatrixCSC, nnz, nzrange, rowvals, sparse
 
-const LIB = get(ENV, "LMGPU_LIB", joinpath(@__DIR__, "..", "lmgpu", "liblmgpu.so"))
+const LIB = get(ENV, "LMGPU_LIB", joinpath(@__DIR__, "..", "..", "lmgpu", "liblmgpu.so"))
 
 const LM_C64 = Cint(0)
 const LM_C32 = Cint(1)
@@ -64,20 +82,32 @@ function DeviceLattice(Lx, Ly; periodic=(false, false), twist=(0.0, 0.0), ctx=de
 end
 
 # ---- lazy device Hamiltonian: the `.data` of the Hamiltonian h(t) returns --------------------
-# Holds the parameters; `==` compares them, which keeps CachedExp's `mat == old` cache rule
-# (src/evolution.jl:87) meaningful for the GPU solver too.
-mutable struct DeviceHamiltonian <: AbstractMatrix{ComplexF64}
-    lat::DeviceLattice
+# A light value (geometry, t1, field components and amplitudes, on-site term).  Calling h(t)
+# every step, as `Evolution(t -> h(t), P_0)` does, only makes a new value: the device tables
+# (one lm_ham per lattice, t1 and field structure) are cached and re-assembled on the GPU when
+# the amplitudes or the on-site term change.  `==` compares the parameters, which keeps
+# CachedExp's `mat == old` cache rule (src/evolution.jl:87) meaningful for the GPU solver too.
+mutable struct DeviceHamSlot
     handle::Ptr{Cvoid}
-    kinds::Vector{Cint}
+    ctx::Context
+    assembled::Any        # (amplitudes, onsite) last assembled, compared by identity
+end
+const _HAMS = Dict{Any,DeviceHamSlot}()
+
+struct DeviceHamiltonian <: AbstractMatrix{ComplexF64}
+    lat::DeviceLattice
+    t1::Float64
+    comps::Vector{Tuple{Cint,Float64,Float64}}   # (kind, point x, point y) per field component
     amplitudes::Vector{Float64}
     onsite::Union{Nothing,Vector{Float64}}
+    auto_pbc::Bool
 end
 Base.size(H::DeviceHamiltonian) = (H.lat.Lx * H.lat.Ly, H.lat.Lx * H.lat.Ly)
 Base.getindex(::DeviceHamiltonian, ::Int, ::Int) =
     throw(ArgumentError("DeviceHamiltonian lives on the GPU; use lm_ham_csc to download it"))
 Base.:(==)(a::DeviceHamiltonian, b::DeviceHamiltonian) =
-    a.handle == b.handle && a.amplitudes == b.amplitudes && a.onsite == b.onsite
+    a.lat === b.lat && a.t1 == b.t1 && a.comps == b.comps && a.amplitudes == b.amplitudes &&
+    a.onsite == b.onsite && a.auto_pbc == b.auto_pbc
 
 field_components(::LatticeModels.NoField) = Tuple{Cint,Float64,Float64,Float64}[]
 field_components(f::LandauGauge) = [(LM_FIELD_LANDAU, 0.0, 0.0, f.B)]
@@ -88,31 +118,128 @@ field_components(f::LatticeModels.FieldSum) = reduce(vcat, map(field_components,
 
 # tightbinding_hamiltonian(l; t1, field) with on-device assembly
 # (src/operators/constructoperator.jl:190-194)
-function gpu_tightbinding(lat::DeviceLattice, onsite=nothing; t1=1.0, field=LatticeModels.NoField())
+function gpu_tightbinding(lat::DeviceLattice, onsite=nothing; t1=1.0, field=LatticeModels.NoField(),
+                          auto_pbc=true)
     comps = field_components(field)
-    h = Ref{Ptr{Cvoid}}(C_NULL)
-    ctx = lat.ctx.handle
-    check(ccall((:lm_ham_create, LIB), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Cdouble, Ref{Ptr{Cvoid}}),
-                ctx, lat.handle, t1, h), ctx)
-    for (kind, px, py, _) in comps
-        idx = Ref{Cint}(0)
-        check(ccall((:lm_ham_add_field, LIB), Cint, (Ptr{Cvoid}, Cint, Cdouble, Cdouble, Cint, Ref{Cint}),
-                    h[], kind, px, py, 1, idx), ctx)
-    end
-    if onsite !== nothing
-        v = Vector{Float64}(onsite)
-        check(ccall((:lm_ham_set_onsite, LIB), Cint, (Ptr{Cvoid}, Ptr{Float64}), h[], v), ctx)
-    end
-    H = DeviceHamiltonian(lat, h[], [c[1] for c in comps], [c[4] for c in comps],
-                          onsite === nothing ? nothing : Vector{Float64}(onsite))
-    finalizer(H -> ccall((:lm_ham_destroy, LIB), Cint, (Ptr{Cvoid},), H.handle), H)
-    assemble!(H)
-    return H
+    return DeviceHamiltonian(lat, Float64(t1), [(c[1], c[2], c[3]) for c in comps], [c[4] for c in comps],
+                             onsite === nothing ? nothing : Vector{Float64}(onsite), auto_pbc)
 end
 
-assemble!(H::DeviceHamiltonian) =
-    check(ccall((:lm_ham_assemble, LIB), Cint, (Ptr{Cvoid}, Ptr{Float64}, Cint),
-                H.handle, H.amplitudes, length(H.amplitudes)), H.lat.ctx.handle)
+function _new_slot(H::DeviceHamiltonian)
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    ctx = H.lat.ctx.handle
+    check(ccall((:lm_ham_create, LIB), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Cdouble, Ref{Ptr{Cvoid}}),
+                ctx, H.lat.handle, H.t1, h), ctx)
+    for (kind, px, py) in H.comps
+        idx = Ref{Cint}(0)
+        check(ccall((:lm_ham_add_field, LIB), Cint, (Ptr{Cvoid}, Cint, Cdouble, Cdouble, Cint, Ref{Cint}),
+                    h[], kind, px, py, H.auto_pbc, idx), ctx)
+    end
+    s = DeviceHamSlot(h[], H.lat.ctx, nothing)
+    finalizer(s -> ccall((:lm_ham_destroy, LIB), Cint, (Ptr{Cvoid},), s.handle), s)
+    return s
+end
+
+function _assemble!(slot::DeviceHamSlot, H::DeviceHamiltonian)
+    if slot.assembled === nothing || slot.assembled[1] !== H.amplitudes || slot.assembled[2] !== H.onsite
+        ctx = H.lat.ctx.handle
+        check(ccall((:lm_ham_set_onsite, LIB), Cint, (Ptr{Cvoid}, Ptr{Float64}), slot.handle,
+                    H.onsite === nothing ? Ptr{Float64}(C_NULL) : H.onsite), ctx)
+        check(ccall((:lm_ham_assemble, LIB), Cint, (Ptr{Cvoid}, Ptr{Float64}, Cint),
+                    slot.handle, H.amplitudes, length(H.amplitudes)), ctx)
+        slot.assembled = (H.amplitudes, H.onsite)
+    end
+    return slot.handle
+end
+
+# The lm_ham of H, assembled with H's amplitudes and on-site term (shared through the cache:
+# valid until another Hamiltonian of the same structure is assembled).
+handle(H::DeviceHamiltonian) = _assemble!(get!(() -> _new_slot(H), _HAMS, (H.lat, H.t1, H.comps, H.auto_pbc)), H)
+
+# An lm_ham owned by the caller (not shared), assembled once: for batches, which keep it.
+private_slot(H::DeviceHamiltonian) = (s = _new_slot(H); _assemble!(s, H); s)
+
+# ---- the drop-in builder: tightbinding_hamiltonian(GPUBuilder, l; t1, field) -----------------
+"""
+    GPUBuilder
+
+Builder type for the reference's Hamiltonian constructors.  `tightbinding_hamiltonian(GPUBuilder,
+l, [V]; t1, field, auto_pbc_field)` and `construct_hamiltonian(GPUBuilder, l, terms...)` return
+the reference's `Hamiltonian` with a `DeviceHamiltonian` as `.data`: H(t) is assembled on the
+GPU (src/operators/constructoperator.jl:136-156, :190-194).  Terms: nearest-neighbour hopping
+`t1 => NearestNeighbor(1)` (t2 = t3 = 0), on-site `LatticeValue`s and numbers; `l` is a 2D
+`SquareLattice` with open, periodic or twisted boundaries.  Other lattices and models go
+through `GPUSparseHamiltonian` (their `construct_operator` CSC).
+"""
+struct GPUBuilder end
+
+const _LATTICES = IdDict{Any,DeviceLattice}()   # one device geometry per reference lattice
+
+_tvec(tr::LatticeModels.BravaisTranslation) = Vector{Float64}(tr.translate_uc)
+_tvec(tr::LatticeModels.Translation) = Vector{Float64}(tr.R)
+
+# (Lx, Ly, periodic, twist) of a reference SquareLattice(Lx, Ly; boundaries) whose sites are in
+# the reference's order, index = (x - 1) Ly + y (src/lattices/bravais/unitcell.jl:126-132).
+function square_geometry(l)
+    LatticeModels.checklatticetype(l, LatticeModels.SquareLattice{2})
+    xs, ys = LatticeModels.coordvalues(l)
+    x, y = xs.values, ys.values
+    Lx = round(Int, maximum(x) - minimum(x)) + 1
+    Ly = round(Int, maximum(y) - minimum(y)) + 1
+    (length(l) == Lx * Ly && x == repeat(minimum(x) .+ (0:Lx-1), inner=Ly) &&
+     y == repeat(minimum(y) .+ (0:Ly-1), outer=Lx)) ||
+        throw(ArgumentError("GPUBuilder needs a full rectangular SquareLattice(Lx, Ly)"))
+    periodic = [false, false]
+    twist = [0.0, 0.0]
+    for b in LatticeModels.getboundaries(l).boundaries
+        b isa LatticeModels.TwistedBoundary ||
+            throw(ArgumentError("GPUBuilder: only periodic or twisted boundaries, not $(typeof(b))"))
+        v = _tvec(b.translation)
+        ax = findfirst(!iszero, v)
+        (count(!iszero, v) == 1 && abs(v[ax]) == (Lx, Ly)[ax]) ||
+            throw(ArgumentError("GPUBuilder: boundary translation $v is not a lattice axis"))
+        periodic[ax] = true
+        twist[ax] = v[ax] > 0 ? b.Θ : -b.Θ
+    end
+    return Lx, Ly, (periodic[1], periodic[2]), (twist[1], twist[2])
+end
+
+function device_lattice(l; ctx=default_context())
+    get!(_LATTICES, l) do
+        Lx, Ly, periodic, twist = square_geometry(l)
+        DeviceLattice(Lx, Ly; periodic=periodic, twist=twist, ctx=ctx)
+    end
+end
+
+function LatticeModels.construct_operator(::Type{GPUBuilder}, sys::LatticeModels.System, args...;
+                                          field=LatticeModels.NoField(), auto_pbc_field=true, kw...)
+    smp = LatticeModels.sample(sys)
+    LatticeModels.hasinternal(smp) &&
+        throw(ArgumentError("GPUBuilder: internal degrees of freedom go through GPUSparseHamiltonian"))
+    l = LatticeModels.lattice(smp)
+    t1 = 0.0
+    onsite = nothing
+    for arg in args
+        amp, onlat = arg isa Pair ? (arg[1], arg[2]) : (1, arg)
+        amp isa Number || throw(ArgumentError("GPUBuilder: operator-valued terms need GPUSparseHamiltonian"))
+        iszero(amp) && continue   # zero terms are skipped (src/operators/constructoperator.jl:50)
+        if onlat isa LatticeModels.NearestNeighbor{1}
+            t1 += real(amp)
+        elseif onlat isa LatticeModels.NearestNeighbor
+            throw(ArgumentError("GPUBuilder: only nearest-neighbour hopping (t2 = t3 = 0)"))
+        elseif onlat isa LatticeModels.LatticeValue
+            onsite = something(onsite, zeros(length(l)))
+            onsite .+= real(amp) .* onlat.values
+        elseif onlat isa Number
+            onsite = something(onsite, zeros(length(l)))
+            onsite .+= real(amp * onlat)
+        else
+            throw(ArgumentError("GPUBuilder: cannot interpret $(typeof(onlat)) as a term"))
+        end
+    end
+    H = gpu_tightbinding(device_lattice(l), onsite; t1=t1, field=field, auto_pbc=auto_pbc_field)
+    return QuantumOpticsBase.Operator(LatticeModels.basis(sys), H)
+end
 
 # ---- device states (the `.data` of Ket/Operator states) -------------------------------------
 mutable struct DeviceState <: AbstractMatrix{ComplexF64}
@@ -154,6 +281,47 @@ function Base.Array(s::DeviceState)
     return out
 end
 
+# A device ket: the `.data` of a reference `Ket` (an AbstractVector, as QuantumOpticsBase
+# requires) backed by an N x 1 device state.
+struct DeviceVector <: AbstractVector{ComplexF64}
+    st::DeviceState
+end
+Base.size(v::DeviceVector) = (v.st.n,)
+Base.getindex(::DeviceVector, ::Int) =
+    throw(ArgumentError("DeviceVector lives on the GPU; use Array(v) to download it"))
+Base.copy(v::DeviceVector) = DeviceVector(copy(v.st))
+Base.Array(v::DeviceVector) = vec(Array(v.st))
+
+# A context-only geometry handle for states on lattices the square-lattice path does not know
+const _CTX_LATTICES = IdDict{Context,DeviceLattice}()
+context_lattice(ctx::Context) = get!(() -> DeviceLattice(ctx, C_NULL, 0, 0), _CTX_LATTICES, ctx)
+
+"""
+    to_device(state; precision=LM_C64)
+
+A copy of a reference `Ket` or density-matrix `Operator` whose `.data` lives on the GPU, for
+`Evolution(ChebyshevGPU, h, to_device(psi))`.  `Array(state.data)` downloads it.
+"""
+function to_device(psi::QuantumOpticsBase.Ket; precision=LM_C64, ctx=default_context())
+    lat = _state_lattice(psi, ctx)
+    return QuantumOpticsBase.Ket(QuantumOpticsBase.basis(psi),
+                                 DeviceVector(DeviceState(lat, reshape(psi.data, :, 1); precision=precision)))
+end
+function to_device(P::QuantumOpticsBase.Operator; precision=LM_C64, ctx=default_context())
+    lat = _state_lattice(P, ctx)
+    return QuantumOpticsBase.Operator(P.basis_l, P.basis_r, DeviceState(lat, P.data; density=true, precision=precision))
+end
+function _state_lattice(state, ctx)
+    l = LatticeModels.lattice(state)
+    LatticeModels.internal_length(state) == 1 || return context_lattice(ctx)
+    try
+        return device_lattice(l; ctx=ctx)
+    catch e
+        e isa ArgumentError || rethrow()
+        return context_lattice(ctx)
+    end
+end
+
 # ---- the EvolutionSolver plugin (src/evolution.jl:5-33) --------------------------------------
 mutable struct ChebyshevGPU <: EvolutionSolver
     ctx::Context
@@ -169,16 +337,17 @@ function ChebyshevGPU(_ham=nothing; tol=1e-12, ctx=default_context())
 end
 
 function update_solver!(s::ChebyshevGPU, H::DeviceHamiltonian, dt, force=false)
-    assemble!(H)
     check(ccall((:lm_solver_update, LIB), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Cdouble, Cint),
-                s.handle, H.handle, dt, force), s.ctx.handle)
+                s.handle, handle(H), dt, force), s.ctx.handle)
 end
 step!(s::ChebyshevGPU, st::DeviceState, _cache) =
     check(ccall((:lm_solver_step, LIB), Cint, (Ptr{Cvoid}, Ptr{Cvoid}), s.handle, st.handle), s.ctx.handle)
-evolution_cache(::ChebyshevGPU, ::DeviceState) = nothing
+step!(s::ChebyshevGPU, v::DeviceVector, cache) = step!(s, v.st, cache)
+evolution_cache(::ChebyshevGPU, ::Union{DeviceState,DeviceVector}) = nothing
 
 # ---- readouts ---------------------------------------------------------------------------------
-function localdensity(st::DeviceState)
+# localdensity of every row of a device state (site x internal state), summed on the device
+function row_density(st::DeviceState)
     out = Vector{Float64}(undef, st.n)
     check(ccall((:lm_localdensity, LIB), Cint, (Ptr{Cvoid}, Ptr{Float64}), st.handle, out), st.lat.ctx.handle)
     return out
@@ -186,10 +355,85 @@ end
 function bond_currents(H::DeviceHamiltonian, st::DeviceState)
     nb = ccall((:lm_lattice_nbonds, LIB), Int64, (Ptr{Cvoid},), H.lat.handle)
     out = Vector{Float64}(undef, nb)
-    check(ccall((:lm_bond_currents, LIB), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Float64}), H.handle, st.handle, out),
+    check(ccall((:lm_bond_currents, LIB), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Float64}), handle(H), st.handle, out),
           st.lat.ctx.handle)
     return out
 end
+
+# (src, dst) of every nearest-neighbour bond, 1-based, in the reference's bond order
+const _BONDS = IdDict{DeviceLattice,Tuple{Vector{Int64},Vector{Int64}}}()
+function lattice_bonds(lat::DeviceLattice)
+    get!(_BONDS, lat) do
+        nb = ccall((:lm_lattice_nbonds, LIB), Int64, (Ptr{Cvoid},), lat.handle)
+        src, dst = Vector{Int64}(undef, nb), Vector{Int64}(undef, nb)
+        check(ccall((:lm_lattice_bonds, LIB), Cint, (Ptr{Cvoid}, Ptr{Int64}, Ptr{Int64}), lat.handle, src, dst),
+              lat.ctx.handle)
+        (src, dst)
+    end
+end
+
+# Reference states whose `.data` lives on the device: a density matrix (Operator) or a Ket
+const DeviceOperator = QuantumOpticsBase.Operator{<:Any,<:Any,<:DeviceState}
+const DeviceKet = QuantumOpticsBase.Ket{<:Any,<:DeviceVector}
+device_data(op::DeviceOperator) = op.data
+device_data(ket::DeviceKet) = ket.data.st
+
+"""
+    localdensity(state)
+
+The reference's `localdensity` (src/operators/latticeutils.jl:41-45) of a device-backed `Ket`
+or density-matrix `Operator`: a `LatticeValue` on the state's lattice, with the internal
+states of a site summed.  The sum over the block runs on the device.
+"""
+function localdensity(state::Union{DeviceOperator,DeviceKet})
+    l = LatticeModels.lattice(state)
+    N = LatticeModels.internal_length(state)
+    v = row_density(device_data(state))
+    return LatticeModels.LatticeValue(l, N == 1 ? v : vec(sum(reshape(v, N, :), dims=1)))
+end
+
+LinearAlgebra.tr(st::DeviceState) = gpu_trace(st)
+
+# DensityCurrents(H, P) (src/zoo/currents.jl:81-102) with H from GPUBuilder and a device state:
+# the struct stays the reference's lazy object; its values come from one device readout of
+# every bond (lm_bond_currents, J_b = 2 Im(H[i,j] P[j,i]) in the reference bond order).
+const GPUDensityCurrents = DensityCurrents{<:LatticeModels.Hamiltonian{<:Any,<:Any,<:DeviceHamiltonian},
+                                           <:Union{DeviceOperator,DeviceKet}}
+
+device_bond_currents(curr::GPUDensityCurrents) = bond_currents(curr.hamiltonian.data, device_data(curr.state))
+
+# curr[i, j]: every bond between sites i and j, taken with its direction.  Each call reads the
+# bonds out of the device; materialise with `Currents(curr)` to read many pairs.
+function Base.getindex(curr::GPUDensityCurrents, i::Int, j::Int)
+    J = device_bond_currents(curr)
+    src, dst = lattice_bonds(curr.hamiltonian.data.lat)
+    v = 0.0
+    for b in eachindex(J)
+        src[b] == i && dst[b] == j && (v += J[b])
+        src[b] == j && dst[b] == i && (v -= J[b])
+    end
+    return v
+end
+
+# Currents(curr) (src/currents.jl:223-237): the antisymmetric sparse matrix from one device
+# readout; |J| < CURRENTS_EPS is dropped, as the reference does.  The only nonzero pairs of a
+# nearest-neighbour Hamiltonian are its bonds, so Currents(curr, NearestNeighbor(1)) is the same.
+function Currents(curr::GPUDensityCurrents)
+    lat = LatticeModels.lattice(curr)
+    J = device_bond_currents(curr)
+    src, dst = lattice_bonds(curr.hamiltonian.data.lat)
+    n = length(lat)
+    mat = sparse(vcat(src, dst), vcat(dst, src), vcat(J, -J), n, n)  # parallel bonds add up
+    Is, Js, Vs = Int[], Int[], Float64[]
+    rows = rowvals(mat)
+    vals = mat.nzval
+    for c in 1:n, p in nzrange(mat, c)
+        abs(vals[p]) < LatticeModels.CURRENTS_EPS && continue
+        push!(Is, rows[p]); push!(Js, c); push!(Vs, vals[p])
+    end
+    return Currents(lat, sparse(Is, Js, Vs, n, n))
+end
+Currents(curr::GPUDensityCurrents, ::LatticeModels.NearestNeighbor{1}) = Currents(curr)
 
 # ---- general sparse Hamiltonians: any construct_operator output (honeycomb, kagome, qwz, ...) ----
 # The reference's SparseMatrixCSC goes to the device as an ELL table; update_solver! picks the
@@ -273,7 +517,7 @@ end
 function push_currents!(r::ReadoutRing, H::DeviceHamiltonian, st::DeviceState, t)
     seq = Ref{Int64}(0)
     check(ccall((:lm_ring_push_currents, LIB), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Cdouble, Ref{Int64}),
-                r.handle, H.handle, st.handle, t, seq), r.ctx.handle)
+                r.handle, handle(H), st.handle, t, seq), r.ctx.handle)
     return seq[]
 end
 function push_op_currents!(r::ReadoutRing, H::GPUSparseHamiltonian, st, ndof::Integer, t, op=nothing)
@@ -296,35 +540,53 @@ end
 """
     gpu_timesequence(kind, ev_iter; nslots=8)
 
-`TimeSequence(moment -> localdensity(moment.state), ev_iter)` (`kind = :density`) or the bond
-currents of `DensityCurrents(moment.H, moment.state)` (`kind = :currents`), read out through a
-`ReadoutRing`.
+`TimeSequence(moment -> localdensity(moment.state), ev_iter)` (`kind = :density`, LatticeValue
+entries) or the bond currents of `DensityCurrents(moment.H, moment.state)` (`kind =
+:currents`, one value per bond in the reference bond order), read out through a `ReadoutRing`
+(src/timesequence.jl:41-43).
 """
-function gpu_timesequence(kind::Symbol, ev_iter; nslots=8)
-    ring = nothing
-    len = 0
-    pending = Int64[]
-    ts = Float64[]
-    vals = Vector{Vector{Float64}}()
+gpu_timesequence(kind::Symbol, ev_iter; nslots=8) = only(gpu_timesequences((kind,), ev_iter; nslots=nslots))
+
+"""
+    gpu_timesequences(kinds, ev_iter; nslots=8)
+
+One `TimeSequence` per kind (`:density`, `:currents`) from a single pass over `ev_iter`: the
+loop of the reference README, which reads `localdensity(P)` and `DensityCurrents(H, P)` at
+every moment.  Each readout goes into its own ring; entries are collected only when their
+slot is about to be reused, so the evolution never waits on a readout.
+"""
+function gpu_timesequences(kinds, ev_iter; nslots=8)
+    rings = Any[nothing for _ in kinds]
+    lens = zeros(Int, length(kinds))
+    pending = [Int64[] for _ in kinds]
+    ts = [Float64[] for _ in kinds]
+    vals = [Any[] for _ in kinds]
+    wrap = Any[identity for _ in kinds]
+    collect_one!(k) = ((t, v) = ring_take!(rings[k], popfirst!(pending[k]), lens[k]); push!(ts[k], t); push!(vals[k], wrap[k](v)))
     for moment in ev_iter
-        st = moment.state.data::DeviceState
-        if ring === nothing
-            len = kind === :density ? st.n :
-                  Int(ccall((:lm_lattice_nbonds, LIB), Int64, (Ptr{Cvoid},), st.lat.handle))
-            ring = ReadoutRing(max(len, 1), nslots; ctx=st.lat.ctx)
+        st = device_data(moment.state)
+        for (k, kind) in enumerate(kinds)
+            if rings[k] === nothing
+                lens[k] = kind === :density ? st.n :
+                          Int(ccall((:lm_lattice_nbonds, LIB), Int64, (Ptr{Cvoid},), moment.H.data.lat.handle))
+                rings[k] = ReadoutRing(max(lens[k], 1), nslots; ctx=st.lat.ctx)
+                if kind === :density
+                    l = LatticeModels.lattice(moment.state)
+                    N = LatticeModels.internal_length(moment.state)
+                    wrap[k] = v -> LatticeModels.LatticeValue(l, N == 1 ? v : vec(sum(reshape(v, N, :), dims=1)))
+                end
+            end
+            length(pending[k]) == nslots && collect_one!(k)
+            push!(pending[k], kind === :density ? push_density!(rings[k], st, moment.t) :
+                                                  push_currents!(rings[k], moment.H.data::DeviceHamiltonian, st, moment.t))
         end
-        if length(pending) == nslots
-            t, v = ring_take!(ring, popfirst!(pending), len)
-            push!(ts, t); push!(vals, v)
+    end
+    for k in eachindex(kinds)
+        while !isempty(pending[k])
+            collect_one!(k)
         end
-        push!(pending, kind === :density ? push_density!(ring, st, moment.t) :
-                                           push_currents!(ring, moment.H.data::DeviceHamiltonian, st, moment.t))
     end
-    for seq in pending
-        t, v = ring_take!(ring, seq, len)
-        push!(ts, t); push!(vals, v)
-    end
-    return LatticeModels.TimeSequence(ts, vals)
+    return [LatticeModels.TimeSequence(ts[k], vals[k]) for k in eachindex(kinds)]
 end
 
 """
@@ -346,7 +608,7 @@ function gpu_operator_timesequence(H::GPUSparseHamiltonian, A::SparseMatrixCSC{C
             t, v = ring_take!(ring, popfirst!(pending), nnz(A))
             push!(ts, t); push!(vals, site_pair_currents(A, v, ndof))
         end
-        push!(pending, push_op_currents!(ring, H, moment.state.data, ndof, moment.t, op))
+        push!(pending, push_op_currents!(ring, H, device_data(moment.state), ndof, moment.t, op))
     end
     for seq in pending
         t, v = ring_take!(ring, seq, nnz(A))
@@ -371,9 +633,10 @@ function GPUBatch(kind::Cint, precision::Cint; tol=precision == LM_C32 ? 1e-9 : 
 end
 function Base.push!(b::GPUBatch, H::DeviceHamiltonian, st::DeviceState)
     idx = Ref{Cint}(0)
-    check(ccall((:lm_batch_add, LIB), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ref{Cint}), b.handle, H.handle,
+    slot = private_slot(H)
+    check(ccall((:lm_batch_add, LIB), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ref{Cint}), b.handle, slot.handle,
                 st.handle, idx), b.ctx.handle)
-    push!(b.members, (H, st))
+    push!(b.members, (slot, st))
     return b
 end
 update!(b::GPUBatch, dt) = check(ccall((:lm_batch_update, LIB), Cint, (Ptr{Cvoid}, Cdouble), b.handle, dt), b.ctx.handle)
@@ -405,7 +668,14 @@ struct DensityLossProblem
     bounds::NTuple{2,Float64}
 end
 
-function _loss_and_grad(p::DensityLossProblem, V::Vector{Float64}, B::Vector{Float64})
+"""
+    loss_and_gradients(p, V, B) -> (loss, dL/dV, dL/dB)
+
+The density loss after the forward pass and its gradients from the hand-written adjoint: the
+forward pass keeps a checkpoint every `p.every` steps, the backward pass recomputes each
+segment, runs lm_adjoint_step per step and propagates the co-state with a solver at -dt.
+"""
+function loss_and_gradients(p::DensityLossProblem, V::Vector{Float64}, B::Vector{Float64})
     ctx = p.lat.ctx
     tol = p.precision == LM_C32 ? 1e-9 : 1e-12
     fwd, bwd = ChebyshevGPU(; tol=tol, ctx=ctx), ChebyshevGPU(; tol=tol, ctx=ctx)
@@ -413,13 +683,15 @@ function _loss_and_grad(p::DensityLossProblem, V::Vector{Float64}, B::Vector{Flo
         check(ccall((:lm_solver_set_bounds, LIB), Cint, (Ptr{Cvoid}, Cdouble, Cdouble), s.handle, p.bounds...),
               ctx.handle)
     end
-    H = gpu_tightbinding(p.lat, V; field=PointFlux(B[1], p.point))
+    comps = [(LM_FIELD_POINTFLUX_AXIAL, p.point...)]
+    Vd = copy(V)   # one on-site array for every step: it is uploaded once
+    ham(amp) = DeviceHamiltonian(p.lat, 1.0, comps, [amp], Vd, true)
     n, m = size(p.psi0)
     adj = Ref{Ptr{Cvoid}}(C_NULL)
     check(ccall((:lm_adjoint_create, LIB), Cint, (Ptr{Cvoid}, Int64, Int64, Cint, Cint, Ref{Ptr{Cvoid}}),
                 ctx.handle, n, m, p.precision, length(B), adj), ctx.handle)
     try
-        stepwith!(s, amp, dt, st) = (H.amplitudes[1] = amp; update_solver!(s, H, dt); step!(s, st, nothing))
+        stepwith!(s, amp, dt, st) = (update_solver!(s, ham(amp), dt); step!(s, st, nothing))
         psi = DeviceState(p.lat, p.psi0; precision=p.precision)
         cps = [copy(psi)]
         for k in 1:p.nsteps
@@ -442,11 +714,11 @@ function _loss_and_grad(p::DensityLossProblem, V::Vector{Float64}, B::Vector{Flo
             end
             for k in n1:-1:n0+1
                 j = (k - 1) ÷ p.spi + 1
-                H.amplitudes[1] = B[j]
-                update_solver!(fwd, H, p.dt)
+                Hj = ham(B[j])
+                update_solver!(fwd, Hj, p.dt)
                 check(ccall((:lm_adjoint_step, LIB), Cint,
                             (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Cint, Cint, Ptr{Cvoid}, Ptr{Cvoid}),
-                            adj[], fwd.handle, H.handle, 0, j - 1, seg[k - n0].handle, lam.handle), ctx.handle)
+                            adj[], fwd.handle, handle(Hj), 0, j - 1, seg[k - n0].handle, lam.handle), ctx.handle)
                 stepwith!(bwd, B[j], -p.dt, lam)
             end
         end
@@ -460,16 +732,9 @@ function _loss_and_grad(p::DensityLossProblem, V::Vector{Float64}, B::Vector{Flo
     end
 end
 
-density_loss(V, B, p::DensityLossProblem) = _loss_and_grad(p, Vector{Float64}(V), Vector{Float64}(B))[1]
-
-# ChainRulesCore is a weak dependency: this block is an extension (ext/ChainRulesCoreExt.jl in a
-# package layout) so LatticeModels does not depend on it.
-import ChainRulesCore
-function ChainRulesCore.rrule(::typeof(density_loss), V, B, p::DensityLossProblem)
-    loss, gV, gB = _loss_and_grad(p, Vector{Float64}(V), Vector{Float64}(B))
-    pullback(dl) = (ChainRulesCore.NoTangent(), dl .* gV, dl .* gB, ChainRulesCore.NoTangent())
-    return loss, pullback
-end
+# The loss alone; its ChainRulesCore rrule (ext/LatticeModelsGB300ChainRulesCoreExt.jl, a
+# package extension loaded with ChainRulesCore) returns the adjoint gradients.
+density_loss(V, B, p::DensityLossProblem) = loss_and_gradients(p, Vector{Float64}(V), Vector{Float64}(B))[1]
 
 # ---- context options, state utilities -----------------------------------------------------------
 const LM_OPT_FUSED = Cint(1)   # 0: one launch per Chebyshev order for ComplexF32 states
@@ -528,9 +793,9 @@ function spectral_bounds(H::DeviceHamiltonian; method=:gershgorin, iters=64, see
     ctx = H.lat.ctx.handle
     if method === :lanczos
         check(ccall((:lm_ham_lanczos_bounds, LIB), Cint, (Ptr{Cvoid}, Cint, Culonglong, Ref{Cdouble}, Ref{Cdouble}),
-                    H.handle, iters, seed, lo, hi), ctx)
+                    handle(H), iters, seed, lo, hi), ctx)
     else
-        check(ccall((:lm_ham_bounds, LIB), Cint, (Ptr{Cvoid}, Ref{Cdouble}, Ref{Cdouble}), H.handle, lo, hi), ctx)
+        check(ccall((:lm_ham_bounds, LIB), Cint, (Ptr{Cvoid}, Ref{Cdouble}, Ref{Cdouble}), handle(H), lo, hi), ctx)
     end
     return lo[], hi[]
 end
@@ -555,7 +820,7 @@ function kpm_moments(H::DeviceHamiltonian, nmom::Integer; vecs=nothing, per_colu
     out = Vector{Float64}(undef, nmom * ncol)
     vh = vecs === nothing ? C_NULL : vecs.handle
     check(ccall((:lm_kpm_moments, LIB), Cint, (Ptr{Cvoid}, Cdouble, Cdouble, Cint, Ptr{Cvoid}, Cint, Ptr{Float64}),
-                H.handle, bounds[1], bounds[2], nmom, vh, per_column, out), H.lat.ctx.handle)
+                handle(H), bounds[1], bounds[2], nmom, vh, per_column, out), H.lat.ctx.handle)
     return per_column ? reshape(out, nmom, ncol) : out
 end
 
@@ -604,12 +869,13 @@ function gpu_densitymatrix(H::DeviceHamiltonian; mu, T, precision=LM_C64, tol=1e
     out = DeviceState(H.lat, h[], n, n, LM_DENSITY, precision)
     finalizer(s -> ccall((:lm_state_destroy, LIB), Cint, (Ptr{Cvoid},), s.handle), out)
     check(ccall((:lm_cheb_apply, LIB), Cint, (Ptr{Cvoid}, Cdouble, Cdouble, Ptr{Float64}, Cint, Ptr{Cvoid}, Ptr{Cvoid}),
-                H.handle, bounds[1], bounds[2], c, length(c), C_NULL, out.handle), ctx)
+                handle(H), bounds[1], bounds[2], c, length(c), C_NULL, out.handle), ctx)
     return out
 end
 
-export ChebyshevGPU, DeviceLattice, DeviceState, gpu_tightbinding, bond_currents, ReadoutRing,
-       gpu_timesequence, GPUBatch, DensityLossProblem, density_loss, GPUSparseHamiltonian, set_values!, gpu_operator_currents,
+export GPUBuilder, ChebyshevGPU, DeviceLattice, DeviceState, DeviceVector, DeviceHamiltonian, to_device,
+       gpu_tightbinding, bond_currents, lattice_bonds, ReadoutRing, gpu_timesequence, gpu_timesequences,
+       loss_and_gradients, GPUBatch, DensityLossProblem, density_loss, GPUSparseHamiltonian, set_values!, gpu_operator_currents,
        gpu_operator_timesequence, gpu_synchronize, set_option!, set_weights!, gpu_trace, gpu_norms, gpu_renormalize!,
        device_pointer, solver_order, spectral_bounds, padded_bounds, kpm_moments, chebyshev_coefficients,
        gpu_densitymatrix, gpu_entry_currents, LM_OPT_FUSED, LM_OPT_STREAM, LM_OPT_KPM

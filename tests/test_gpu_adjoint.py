@@ -84,7 +84,15 @@ def test_differentiation_workload_fd(lm):
     """SquareLattice(64,64) open, M = 2048 lowest eigenstates, V ~ U[-0.1,0.1], 50 flux
     intervals of 8 steps (init 0.1) through (32.5, 32.5), T = 20 (400 steps of 0.05),
     checkpoint every 20 steps, FP32 forward + adjoint; gradient against FP64 central
-    differences (h = 1e-4) on 32 random parameters."""
+    differences (h = 1e-4) on 32 random parameters (24 potentials, 8 flux amplitudes).
+
+    Bar: every checked component within 1e-5 of the finite difference, relative to
+    max(|fd_i|, RMS of its group's gradient).  The floor matters only for components far below
+    their group's typical size (one potential gradient here is below 5e-4 against an RMS of
+    0.024): the FP32 error is about the same in absolute terms for every component, so such a
+    component would otherwise report that error divided by its own small size.  The FP64
+    adjoint is held to 1e-6 of FD with no floor, which shows that the FD reference itself is
+    good to that level and that the remaining error is the FP32 arithmetic's."""
     torch = pytest.importorskip("torch")
     L, M, dt, nsteps, spi = 64, 2048, 0.05, 400, 8
     point = (32.5, 32.5)
@@ -118,16 +126,17 @@ def test_differentiation_workload_fd(lm):
         fd.append((p64.loss(V, B + e) - p64.loss(V, B - e)) / (2 * h))
         g32.append(gB[j]); g64.append(gB64[j])
     fd, g32, g64 = np.array(fd), np.array(g32), np.array(g64)
-    err32 = np.abs(g32 - fd) / np.maximum(np.abs(fd), 1e-12)
-    err64 = np.abs(g64 - fd) / np.maximum(np.abs(fd), 1e-12)
-    err3264 = np.abs(g32 - g64) / np.maximum(np.abs(g64), 1e-12)
+    # floor: the RMS of the group's FP64 adjoint gradient (4096 potentials, 50 flux amplitudes)
+    floor = np.concatenate([np.full(len(iv), np.sqrt(np.mean(gV64 ** 2))), np.full(len(ib), np.sqrt(np.mean(gB64 ** 2)))])
+    err32 = np.abs(g32 - fd) / np.maximum(np.abs(fd), floor)
+    err64 = np.abs(g64 - fd) / np.maximum(np.abs(fd), 1e-300)
+    err3264 = np.abs(g32 - g64) / np.maximum(np.abs(g64), floor)
     np.set_printoptions(precision=3, linewidth=200)
     print(f"differentiation workload: loss {loss32:.6e}; |gV| {np.linalg.norm(gV64):.3e}, |gB| {np.linalg.norm(gB64):.3e}")
     print("  |fd|            ", np.abs(fd))
     print("  c32 vs fd       ", err32)
     print("  c64 vs fd       ", err64)
-    print("  c32 vs c64      ", err3264)
     print(f"  max/median: c32-fd {err32.max():.3e}/{np.median(err32):.3e}  c64-fd {err64.max():.3e}/"
-          f"{np.median(err64):.3e}  c32-c64 {err3264.max():.3e}/{np.median(err3264):.3e}")
-    assert np.median(err32) <= 1e-5
-    assert err32.max() <= 1e-3
+          f"{np.median(err64):.3e}  c32-c64 {err3264.max():.3e}")
+    assert err64.max() <= 1e-6   # measured 1.05e-7
+    assert err32.max() <= 1e-5   # measured 1.4e-6 against the floored scale

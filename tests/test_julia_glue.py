@@ -1,4 +1,5 @@
-"""The Julia glue module (julia/LatticeModelsGB300.jl) against the C header include/lmgpu.h.
+"""The Julia glue package (julia/src/LatticeModelsGB300.jl) against the C header include/lmgpu.h
+and against the reference API it plugs into.
 
 Julia is not installed here, so the glue cannot be run; these tests read it as text and check
 every `ccall` against the header declaration it binds: the function exists, the number of
@@ -13,7 +14,10 @@ import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 HEADER = os.path.join(ROOT, "include", "lmgpu.h")
-GLUE = os.path.join(ROOT, "latticemodels.jl_gb300", "julia", "LatticeModelsGB300.jl")
+JL = os.path.join(ROOT, "latticemodels.jl_gb300", "julia")
+GLUE = os.path.join(JL, "src", "LatticeModelsGB300.jl")
+EXT = os.path.join(JL, "ext", "LatticeModelsGB300ChainRulesCoreExt.jl")
+PROJECT = os.path.join(JL, "Project.toml")
 
 # C scalar type -> Julia types of the same width
 SCALARS = {
@@ -61,7 +65,7 @@ def _split_top(s):
 
 
 def glue_ccalls():
-    text = open(GLUE).read()
+    text = open(GLUE).read() + open(EXT).read()
     calls = []
     for m in re.finditer(r"ccall\(\(:(lm_[a-z_0-9]+), LIB\),\s*([A-Za-z0-9{}]+),\s*\(", text):
         # the argument-type tuple starts at m.end() - 1; find its matching parenthesis
@@ -141,3 +145,67 @@ def test_glue_imports_and_definitions():
     defined = set(re.findall(r"^function ([A-Za-z_][\w!]*)\(", text, re.M))
     defined |= set(re.findall(r"^([A-Za-z_][\w!]*)\([^)]*\)\s*=", text, re.M))
     assert not (defined & BASE_FUNCS), f"unqualified Base functions defined: {defined & BASE_FUNCS}"
+
+
+# --- the drop-in surface: methods of the reference's own functions -------------------------
+def _code(path=GLUE):
+    """The file with comments and docstrings removed."""
+    text = open(path).read()
+    text = re.sub(r'"""(.*?)"""', " ", text, flags=re.S)
+    return re.sub(r"#[^\n]*", " ", text)
+
+
+def test_builder_hooks_into_construct_operator():
+    """tightbinding_hamiltonian(GPUBuilder, l; t1, field) reaches the reference's builder hook
+    construct_operator(BT::Type, sys::System, args...; field, auto_pbc_field)
+    (src/operators/constructoperator.jl:136, :190-194) and returns an Operator whose data is the
+    device Hamiltonian, which construct_hamiltonian wraps in the reference's Hamiltonian."""
+    code = _code()
+    assert re.search(r"struct GPUBuilder end", code)
+    m = re.search(r"function LatticeModels\.construct_operator\(::Type\{GPUBuilder\}, sys::LatticeModels\.System, "
+                  r"args\.\.\.;\s*field=LatticeModels\.NoField\(\), auto_pbc_field=true", code)
+    assert m, "construct_operator(::Type{GPUBuilder}, sys, args...; field, auto_pbc_field) is missing"
+    body = code[m.end():code.index("\nend\n", m.end())]
+    assert "NearestNeighbor{1}" in body and "LatticeValue" in body
+    assert "QuantumOpticsBase.Operator(LatticeModels.basis(sys), H)" in body
+    assert "struct DeviceHamiltonian <: AbstractMatrix{ComplexF64}" in code
+
+
+def test_readouts_are_methods_of_the_reference_functions():
+    code = _code()
+    imported = re.search(r"^import LatticeModels:(.*?)\n(?!\s)", code, re.M | re.S).group(1)
+    for f in ("update_solver!", "step!", "evolution_cache", "localdensity", "densitymatrix", "Currents",
+              "DensityCurrents"):
+        assert re.search(r"(?<![\w!])" + re.escape(f) + r"(?![\w!])", imported), f"{f} is not imported from LatticeModels"
+    # localdensity on device-backed Ket/Operator states returns the reference's LatticeValue
+    m = re.search(r"function localdensity\(state::Union\{DeviceOperator,DeviceKet\}\)(.*?)\nend", code, re.S)
+    assert m and "LatticeModels.LatticeValue(l," in m.group(1)
+    assert re.search(r"const DeviceOperator = QuantumOpticsBase\.Operator\{<:Any,<:Any,<:DeviceState\}", code)
+    assert re.search(r"const DeviceKet = QuantumOpticsBase\.Ket\{<:Any,<:DeviceVector\}", code)
+    # DensityCurrents(H, P): the reference's lazy struct, specialised getindex and Currents
+    assert re.search(r"const GPUDensityCurrents = DensityCurrents\{<:LatticeModels\.Hamiltonian\{<:Any,<:Any,"
+                     r"<:DeviceHamiltonian\},", code)
+    assert re.search(r"function Base\.getindex\(curr::GPUDensityCurrents, i::Int, j::Int\)", code)
+    assert re.search(r"function Currents\(curr::GPUDensityCurrents\)", code)
+    assert "LatticeModels.CURRENTS_EPS" in code
+    # tr and copy of a device state (the reference's Evolution copies its states)
+    assert re.search(r"LinearAlgebra\.tr\(st::DeviceState\) =", code)
+    assert re.search(r"function Base\.copy\(s::DeviceState\)", code)
+    assert re.search(r"Base\.copy\(v::DeviceVector\)", code)
+    # the plugin methods for both state kinds
+    assert re.search(r"step!\(s::ChebyshevGPU, st::DeviceState, _cache\)", code)
+    assert re.search(r"step!\(s::ChebyshevGPU, v::DeviceVector, cache\)", code)
+    assert re.search(r"function update_solver!\(s::ChebyshevGPU, H::DeviceHamiltonian, dt, force=false\)", code)
+
+
+def test_rrule_is_a_package_extension():
+    """ChainRulesCore is a weak dependency: the rrule lives in ext/ and the module never
+    imports ChainRulesCore itself."""
+    assert "ChainRulesCore" not in _code()
+    ext = _code(EXT)
+    assert re.search(r"function ChainRulesCore\.rrule\(::typeof\(density_loss\), V, B, p::DensityLossProblem\)", ext)
+    proj = open(PROJECT).read()
+    assert re.search(r"\[weakdeps\]\s*\nChainRulesCore = ", proj)
+    assert re.search(r"\[extensions\]\s*\nLatticeModelsGB300ChainRulesCoreExt = \"ChainRulesCore\"", proj)
+    # the reference package's own uuid (its Project.toml) is the dependency
+    assert 'LatticeModels = "3c3db7f8-440c-4375-905c-1a18b5307bed"' in proj
