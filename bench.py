@@ -330,12 +330,12 @@ def run_adjoint_workload(args):
     V = rng.uniform(-0.1, 0.1, L * L)
     B = np.full(50, 0.1)
     lat = lmgpu.SquareLattice(L, L)
-    if args.adjoint_init == "random":  # same cost, no cuSOLVER (profilers that cannot load it)
+    if args.adjoint_init == "random":  # same cost, no eigensystem
         psi0 = (rng.standard_normal((L * L, M)) + 1j * rng.standard_normal((L * L, M))) / math.sqrt(2 * L * L)
-    else:
-        w, vecs = lmgpu.diagonalize(lmgpu.tightbinding_hamiltonian(lat, V, field=lmgpu.PointFlux(B[0], point)))
-        psi0 = vecs[:, :M].cpu().numpy()
-        del vecs
+    else:  # the M lowest eigenstates from the library's eigensystem
+        eig = lmgpu.diagonalize(lmgpu.tightbinding_hamiltonian(lat, V, field=lmgpu.PointFlux(B[0], point)))
+        psi0 = eig.vectors(0, M).to_numpy()
+        del eig
     c = rng.uniform(20, 44, size=2)
     r2 = ((lat.coords() - c) ** 2).sum(axis=1)
     target = 0.5 + 0.2 * np.exp(-r2 / (2 * 6.0 ** 2))
@@ -358,7 +358,7 @@ def run_adjoint_workload(args):
     line = {"metric": "forward ket-steps/s of loss_and_grad (forward + checkpointed adjoint)",
             "value": M * nsteps / (ms / 1000.0), "unit": "ket-steps/s", "n_gpus": 1, "steps": reps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "dtype": args.precision,
-            "data": ("synthetic (seeded; psi_0 = lowest eigenstates of h(V0) from cuSOLVER eigh)"
+            "data": ("synthetic (seeded; psi_0 = lowest eigenstates of h(V0) from the library's eigensystem)"
                      if args.adjoint_init == "eigh" else "synthetic (seeded; psi_0 = random complex-Gaussian kets)"),
             "config": {"workload": ADJOINT_WORKLOAD, "N": L * L, "M": M, "tol": prob.tol,
                        "step_unit": "one loss_and_grad"},
@@ -412,9 +412,11 @@ def run_kpm_workload(args):
     finally:
         ctx.set_kpm_doublefloat(True)
     passes = (nmom + 1) // 2 + 1
-    # per pass: the recurrence reads T_{n+1} and T_n and writes T_{n+2}; the two dot products
-    # read T_n (twice) and T_{n+1}: six block passes of N*R*16 bytes
-    alg = 6.0 * N * R * 16 * passes
+    # per pass, FP64 path: the recurrence reads T_{n+1} and T_n and writes T_{n+2}; the two
+    # dot products read T_n (twice) and T_{n+1}: six block passes of N*R*16 bytes.  The
+    # double-float path forms both dots in one read of T_n and T_{n+1}: five passes.
+    alg = 5.0 * N * R * 16 * passes
+    alg64 = 6.0 * N * R * 16 * passes
     peak, peak_kind = measured_peak_hbm()
     line = {"metric": "KPM vector-moments/s (Chebyshev moments, double-float recurrence)",
             "value": R * nmom / (ms / 1000.0),
@@ -426,10 +428,12 @@ def run_kpm_workload(args):
             "roofline": {"bound": "hbm", "achieved": alg / (ms / 1000.0) / 1e9, "peak": peak, "unit": "GB/s",
                          "frac": alg / (ms / 1000.0) / 1e9 / peak, "traffic": None,
                          "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
-                         "alg_bytes_per_call": alg, "note": "whole call (recurrence + dot kernels)"},
+                         "alg_bytes_per_call": alg,
+                         "note": "whole call (recurrence + dot kernels): 5 block passes per pass (the double-float "
+                                 "dots read T_n and T_n+1 once for both moments)"},
             "mu0_over_N": float(mu[0] / (N * R)), "clocks": clocks,
             "fp64": {"value": R * nmom / (ms64 / 1000.0), "ms_per_step": ms64, "speedup_of_default": ms64 / ms,
-                     "roofline_frac": alg / (ms64 / 1000.0) / 1e9 / peak,
+                     "roofline_frac": alg64 / (ms64 / 1000.0) / 1e9 / peak,
                      "max_moment_diff_over_mu0": float(np.abs(mu64 - mu).max() / abs(mu[0])),
                      "note": "LM_OPT_KPM = 0: the recurrence in FP64 (GB300 runs FP64 at 1/64 of FP32)"}}
     print(json.dumps(line))
@@ -438,13 +442,18 @@ def run_kpm_workload(args):
 
 # ------------------------------------------------------------------------------------------
 DM_WORKLOAD = ("SquareLattice(96,96) open (the largest lattice of the batching workload), t1=1, "
-               "PointFlux(0.2, (48.5, 48.5)), disorder U[-1.5,1.5]; densitymatrix(H; mu=0, T=0.1)")
+               "PointFlux(0.2, (48.5, 48.5)), disorder U[-1.5,1.5]; densitymatrix(H; mu=0, T=0.1) and "
+               "densitymatrix(H; mu=0) at T = 0")
 
 
 def run_densitymatrix_workload(args):
-    """P_0 = f(H) at T = 0.1: the Chebyshev series of the occupation applied to the identity by
-    the library's kernels, against cuSOLVER's dense eigensolver (torch.linalg.eigh) on the same
-    GPU.  `value` = matrices per second of the Chebyshev route."""
+    """P_0 = densitymatrix(H; mu, T) on the library's kernels, N = 9216:
+    * T = 0.1: the Chebyshev series of the occupation applied to the identity (double-float
+      recurrence by default, FP64 with LM_OPT_KPM = 0);
+    * T = 0: the library's FP64 eigensystem (Householder tridiagonalisation, bisection, inverse
+      iteration, back-transformation, weighted projector);
+    each against cuSOLVER's dense eigensolver on the same GPU (torch.linalg.eigh, timed here as
+    a baseline only).  `value` = matrices per second of the T = 0 route."""
     import torch
     import lmgpu
     ctx = lmgpu.default_context()
@@ -453,26 +462,54 @@ def run_densitymatrix_workload(args):
     V = np.random.default_rng(SEED + 3).uniform(-1.5, 1.5, L * L)
     H = lmgpu.tightbinding_hamiltonian(lat, V, field=lmgpu.PointFlux(0.2, (48.5, 48.5)))
 
-    def timed(method):
-        lmgpu.densitymatrix(H, mu=0.0, T=0.1, method=method)  # warm-up
+    def sync():
         ctx.synchronize()
         torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        P = lmgpu.densitymatrix(H, mu=0.0, T=0.1, method=method)
-        ctx.synchronize()
-        torch.cuda.synchronize()
-        return time.perf_counter() - t0, P
 
-    t_cheb, Pc = timed("chebyshev")
-    t_eig, Pe = timed("eigh")
-    a, b = Pc.to_numpy(), Pe.to_numpy()
-    err = float(np.linalg.norm(a - b) / np.linalg.norm(b))
-    line = {"metric": "densitymatrix at T > 0: matrices/s (Chebyshev route on the library's kernels)",
-            "value": 1.0 / t_cheb, "unit": "matrices/s", "n_gpus": 1, "steps": 1, "warmup": 1,
-            "ms_per_step": t_cheb * 1e3, "higher_is_better": True, "dtype": "c64",
+    def timed(fn, warm=True):
+        if warm:
+            fn()
+        sync()
+        t0 = time.perf_counter()
+        out = fn()
+        sync()
+        return time.perf_counter() - t0, out
+
+    # cuSOLVER baseline: dense H from the library's CSC, eigh, projector by matmul (FP64)
+    colptr, rowval, nz = H.csc()
+    cols = np.repeat(np.arange(L * L), np.diff(colptr))
+    Hd = torch.sparse_coo_tensor(torch.as_tensor(np.stack([rowval - 1, cols])), torch.as_tensor(nz),
+                                 (L * L, L * L)).to_dense().to("cuda")
+
+    def cusolver(T):
+        w, U = torch.linalg.eigh(Hd)
+        occ = (w <= 0.0).double() if T == 0 else 0.5 * (1.0 - torch.tanh(w / (2 * T)))
+        return (U * occ) @ U.conj().T
+
+    t_cheb, Pc = timed(lambda: lmgpu.densitymatrix(H, mu=0.0, T=0.1, method="chebyshev"))
+    ctx.set_kpm_doublefloat(False)
+    try:
+        t_cheb64, Pc64 = timed(lambda: lmgpu.densitymatrix(H, mu=0.0, T=0.1, method="chebyshev"), warm=False)
+    finally:
+        ctx.set_kpm_doublefloat(True)
+    t_zero, Pz = timed(lambda: lmgpu.densitymatrix(H, mu=0.0), warm=False)
+    t_cu0, Pcu0 = timed(lambda: cusolver(0.0))
+    t_cu1, Pcu1 = timed(lambda: cusolver(0.1), warm=False)
+    a = torch.as_tensor(Pc.to_numpy(), device="cuda")
+    a64 = torch.as_tensor(Pc64.to_numpy(), device="cuda")
+    z = torch.as_tensor(Pz.to_numpy(), device="cuda")
+    r = lambda x, y: float(torch.linalg.norm(x - y) / torch.linalg.norm(y))
+    line = {"metric": "densitymatrix at T = 0 on the library's eigensystem: matrices/s",
+            "value": 1.0 / t_zero, "unit": "matrices/s", "n_gpus": 1, "steps": 1, "warmup": 1,
+            "ms_per_step": t_zero * 1e3, "higher_is_better": True, "dtype": "f64 (c64 matrices)",
             "data": "synthetic (seeded disorder)", "config": {"workload": DM_WORKLOAD, "N": L * L},
-            "eigh_ms": t_eig * 1e3, "speedup_over_eigh": t_eig / t_cheb, "rel_diff_vs_eigh": err,
-            "note": "wall clock, host timer around fully synchronised calls"}
+            "zero_temperature": {"ms": t_zero * 1e3, "cusolver_ms": t_cu0 * 1e3, "speedup_over_cusolver": t_cu0 / t_zero,
+                                 "rel_diff_vs_cusolver": r(z, Pcu0), "trace": float(torch.trace(z).real)},
+            "chebyshev_T01": {"ms": t_cheb * 1e3, "fp64_recurrence_ms": t_cheb64 * 1e3,
+                              "cusolver_ms": t_cu1 * 1e3, "speedup_over_cusolver": t_cu1 / t_cheb,
+                              "rel_diff_vs_cusolver": r(a, Pcu1), "fp64_rel_diff_vs_cusolver": r(a64, Pcu1)},
+            "note": "wall clock, host timer around fully synchronised calls; cuSOLVER (torch.linalg.eigh) and "
+                    "its projector are a timed baseline, not part of the library's path"}
     print(json.dumps(line))
     return 0
 

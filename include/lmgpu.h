@@ -305,6 +305,29 @@ int lm_cheb_apply(lm_ham *ham, double emin, double emax, const double *coef, int
  * pass it to lm_solver_set_bounds, lm_kpm_moments or lm_cheb_apply. */
 int lm_ham_lanczos_bounds(lm_ham *ham, int iters, unsigned long long seed, double *emin, double *emax);
 
+/* ---- eigensystem (diagonalize / densitymatrix, src/spectrum.jl:48-55, :226-257, :317-333) ---- */
+/* The Hermitian eigensystem of an assembled Hamiltonian, computed on the device in FP64 with
+ * the library's own kernels (Householder tridiagonalisation, bisection, inverse iteration,
+ * back-transformation; no vendor eigensolver).  Replaces the reference's dense LAPACK
+ * `eigen` in `diagonalize` (src/spectrum.jl:48-55).  The object holds the N x N reduced
+ * matrix (16 N^2 bytes) until destroyed; every call synchronises the context's stream. */
+typedef struct lm_eigsys lm_eigsys;
+/* Square-lattice Hamiltonian (as last assembled) or general sparse Hamiltonian. */
+int lm_eigsys_create(lm_ham *ham, lm_eigsys **out);
+int lm_eigsys_create_ell(lm_ell *ham, lm_eigsys **out);
+int lm_eigsys_destroy(lm_eigsys *e);
+int lm_eigsys_size(const lm_eigsys *e, int64_t *n);
+/* The N eigenvalues in ascending order (host array of N doubles). */
+int lm_eigsys_values(const lm_eigsys *e, double *out);
+/* Eigenvectors first .. first + m - 1 (ascending eigenvalue order) into the columns of a
+ * ket state out (N x m, ComplexF64 or ComplexF32), each of unit norm; the sign is fixed by
+ * making the largest component of the tridiagonal eigenvector positive. */
+int lm_eigsys_vectors(lm_eigsys *e, int64_t first, lm_state *out);
+/* out (an N x N density state) = sum_k weights[k] v_k v_k^H over the eigenvectors whose weight
+ * is nonzero (weights: host array of N doubles in eigenvalue order).  With the occupations of
+ * src/spectrum.jl:226-257 as weights this is densitymatrix(eigensystem; mu, T). */
+int lm_eigsys_projector(lm_eigsys *e, const double *weights, lm_state *out);
+
 /* ---- readout ring (device side of TimeSequence(f, ev(times)), src/timesequence.jl:41-43) -- */
 /* Per-moment readouts computed into the slots of a device ring and downloaded asynchronously
  * into pinned host memory: pushing does not wait for the device, so an evolution loop that

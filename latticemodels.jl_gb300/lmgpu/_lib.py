@@ -114,6 +114,13 @@ SIGNATURES = {
     "lm_kpm_moments": (_INT, [_P, _D, _D, _INT, _P, _INT, _PD]),
     "lm_cheb_apply": (_INT, [_P, _D, _D, _PD, _INT, _P, _P]),
     "lm_ham_lanczos_bounds": (_INT, [_P, _INT, C.c_ulonglong, _PD, _PD]),
+    "lm_eigsys_create": (_INT, [_P, C.POINTER(_P)]),
+    "lm_eigsys_create_ell": (_INT, [_P, C.POINTER(_P)]),
+    "lm_eigsys_destroy": (_INT, [_P]),
+    "lm_eigsys_size": (_INT, [_P, _PI64]),
+    "lm_eigsys_values": (_INT, [_P, _PD]),
+    "lm_eigsys_vectors": (_INT, [_P, _I64, _P]),
+    "lm_eigsys_projector": (_INT, [_P, _PD, _P]),
     "lm_ring_create": (_INT, [_P, _INT, _I64, C.POINTER(_P)]),
     "lm_ring_destroy": (_INT, [_P]),
     "lm_ring_push_localdensity": (_INT, [_P, _P, _D, _PI64]),

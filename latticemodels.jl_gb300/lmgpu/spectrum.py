@@ -1,60 +1,96 @@
 """``diagonalize`` / ``densitymatrix`` on the device (src/spectrum.jl:48-55, :226-257, :317-333).
 
-Two routes to P = f(H) = sum_i f(E_i) |psi_i><psi_i| with the FermiDirac occupation f:
-* T > 0: the Chebyshev series of f on the spectral interval, applied to the identity by the
-  library's own stencil kernels (``lm_cheb_apply``): no eigensystem, O(K N^2) work for K
-  terms, exact to the series tolerance.
-* T = 0 (a step function, whose series does not converge), or on request: the dense
-  Hermitian eigensolver cuSOLVER (through torch.linalg.eigh on the GPU), with the reference's
-  occupation rule (E == mu counts as occupied).
-Both run on the GPU only (no host eigensolver).
+Two routes to P = f(H) = sum_i f(E_i) |psi_i><psi_i|, both on the library's own kernels:
+* T > 0 FermiDirac ensemble: the Chebyshev series of f on the spectral interval, applied to
+  the identity (``lm_cheb_apply``): no eigensystem, O(K N^2) work for K terms, exact to the
+  series tolerance.
+* every other case (T = 0, BoseEinstein, the Gibbs state, fixed N) or on request: the device
+  eigensystem (``lm_eigsys_*``: Householder tridiagonalisation, bisection, inverse
+  iteration, all FP64) weighted by the reference's occupations.  At T = 0 "E == mu" means
+  |E - mu| <= DEGENERATE_TOL max(1, |E|max): a level exactly degenerate at mu is occupied as a
+  whole instead of being split by the rounding of its computed eigenvalues.
 """
 from __future__ import annotations
 
 import ctypes as C
 import math
+import weakref
 
 import numpy as np
 
 from . import _lib
 from .device import default_context
 from .hamiltonian import Hamiltonian
-from .states import DensityMatrix
+from .states import DensityMatrix, DeviceState, KetBlock
+
+# relative width of "E == mu" at T = 0 (src/spectrum.jl:230-232)
+DEGENERATE_TOL = 1e-12
 
 
-def _torch_cuda():
-    import torch
-    if not torch.cuda.is_available():
-        raise RuntimeError("densitymatrix runs on the GPU and no CUDA device is available")
-    return torch
+class Eigensystem:
+    """The eigensystem of a device Hamiltonian, ``diagonalize(H)`` (src/spectrum.jl:48-55,
+    :108-116): ``values`` (ascending, host FP64), eigenvectors and weighted projectors computed
+    on the device on demand."""
+
+    def __init__(self, H, ctx=None):
+        from .sparse import SparseHamiltonian
+        ctx = ctx or default_context()
+        self.ctx = ctx
+        self.hamiltonian = H
+        self.lattice = H.lattice
+        dh = H.device(ctx)
+        p = C.c_void_p()
+        if isinstance(H, SparseHamiltonian):
+            ctx.check(ctx.lib.lm_eigsys_create_ell(dh.handle, C.byref(p)))
+        elif isinstance(H, Hamiltonian):
+            ctx.check(ctx.lib.lm_eigsys_create(dh.handle, C.byref(p)))
+        else:
+            raise TypeError("diagonalize takes a device Hamiltonian (tightbinding_hamiltonian, SparseHamiltonian)")
+        self.handle = p
+        self._fin = weakref.finalize(self, ctx.lib.lm_eigsys_destroy, p)
+        n = C.c_int64()
+        ctx.check(ctx.lib.lm_eigsys_size(p, C.byref(n)))
+        self.n = n.value
+        self.values = np.empty(self.n, dtype=np.float64)
+        ctx.check(ctx.lib.lm_eigsys_values(p, _lib.dptr(self.values)))
+
+    def __len__(self):
+        return self.n
+
+    def vectors(self, first: int = 0, count=None, precision="c64") -> KetBlock:
+        """Eigenvectors first .. first + count - 1 as the columns of a device ket block."""
+        count = self.n - first if count is None else int(count)
+        if first < 0 or count < 1 or first + count > self.n:
+            raise ValueError("eigenvector range outside the spectrum")
+        out = DeviceState(self.lattice, None, _lib.LM_KETS, precision, ctx=self.ctx, shape=(self.n, count))
+        out.__class__ = KetBlock
+        self.ctx.check(self.ctx.lib.lm_eigsys_vectors(self.handle, int(first), out.handle))
+        return out
+
+    def projector(self, weights, precision="c64") -> DensityMatrix:
+        """sum_k w_k |v_k><v_k| as a device density matrix (weights in eigenvalue order)."""
+        w = np.ascontiguousarray(weights, dtype=np.float64)
+        if w.shape != (self.n,):
+            raise ValueError("one weight per eigenvalue")
+        out = DensityMatrix(self.lattice, None, precision, ctx=self.ctx)
+        self.ctx.check(self.ctx.lib.lm_eigsys_projector(self.handle, _lib.dptr(w), out.handle))
+        return out
 
 
-def _dense_on_device(H: Hamiltonian, torch):
-    colptr, rowval, nz = H.csc()
-    N = H.N
-    cols = np.repeat(np.arange(N), np.diff(colptr))
-    rows = rowval - 1
-    idx = torch.as_tensor(np.stack([rows, cols]), device="cuda")
-    vals = torch.as_tensor(nz, device="cuda")
-    return torch.sparse_coo_tensor(idx, vals, (N, N)).to_dense()
+def diagonalize(H) -> Eigensystem:
+    """``diagonalize(H)``: the device eigensystem (values ascending, vectors on demand)."""
+    return Eigensystem(H)
 
 
-def diagonalize(H: Hamiltonian):
-    """Eigenvalues (ascending, FP64 host array) and eigenvectors (device tensor)."""
-    torch = _torch_cuda()
-    A = _dense_on_device(H, torch)
-    w, V = torch.linalg.eigh(A)
-    return w.cpu().numpy(), V
-
-
-def densfun(T: float, mu: float, statistics: str = "FermiDirac"):
+def densfun(T: float, mu: float, statistics: str = "FermiDirac", degenerate_tol: float = 0.0):
     """E -> (E - mu == T == 0) ? 1 : 1 / (exp((E - mu)/T) + s), s = +1 FermiDirac, -1
-    BoseEinstein (src/spectrum.jl:230-232).  At T = 0 a level below mu gets 1/s."""
+    BoseEinstein (src/spectrum.jl:230-232).  At T = 0 a level below mu gets 1/s, and "E == mu"
+    means |E - mu| <= degenerate_tol."""
     sgn = 1.0 if statistics == "FermiDirac" else -1.0
 
     def f(E):
         d = E - mu
-        if d == 0 and T == 0:
+        if T == 0 and abs(d) <= degenerate_tol:
             return 1.0
         if T == 0:
             return 1.0 / sgn if d < 0 else 0.0
@@ -92,7 +128,13 @@ def fermi_occupation(mu: float, T: float):
 _STATISTICS = ("FermiDirac", "BoseEinstein")
 
 
-def occupations(w, mu=None, T: float = 0.0, N=None, statistics=None) -> np.ndarray:
+def degenerate_tol(w) -> float:
+    """Width of "E == mu" for the eigenvalues w: DEGENERATE_TOL max(1, |E|max)."""
+    w = np.asarray(w, dtype=np.float64)
+    return DEGENERATE_TOL * max(1.0, float(np.abs(w).max()) if len(w) else 1.0)
+
+
+def occupations(w, mu=None, T: float = 0.0, N=None, statistics=None, tol=None) -> np.ndarray:
     """Weights f(E_i) of the eigenvalues ``w`` (ascending) that ``densitymatrix`` puts on the
     eigenvectors, following the reference's dispatch for a one-particle system
     (src/spectrum.jl:239-333):
@@ -136,7 +178,7 @@ def occupations(w, mu=None, T: float = 0.0, N=None, statistics=None) -> np.ndarr
             newmu += dmu
         raise ValueError("did not converge")
     if mu is not None or statistics is not None:
-        f = densfun(T, 0.0 if mu is None else mu, stat)
+        f = densfun(T, 0.0 if mu is None else mu, stat, degenerate_tol(w) if tol is None else tol)
         return np.array([f(e) for e in w])
     occ = np.zeros(len(w))
     if abs(T) < 1e-10:
@@ -146,13 +188,14 @@ def occupations(w, mu=None, T: float = 0.0, N=None, statistics=None) -> np.ndarr
     return occ / occ.sum()
 
 
-def densitymatrix(H: Hamiltonian, mu=None, T: float = 0.0, *, N=None, statistics=None, precision="c64",
+def densitymatrix(H, mu=None, T: float = 0.0, *, N=None, statistics=None, precision="c64",
                   method: str = "auto", tol: float = 1e-13, bounds: str = "gershgorin") -> DensityMatrix:
     """``densitymatrix(H; mu, T, N, statistics)`` of a one-particle system (src/spectrum.jl:239-333;
     the dispatch is ``occupations``).  The FermiDirac ensemble at T > 0 runs the Chebyshev
     Fermi operator on the device (``lm_cheb_apply``) unless method="eigh"; every other case
-    weights the device eigensystem (cuSOLVER).  bounds: the spectral interval of the
+    weights the device eigensystem (``diagonalize``).  bounds: the spectral interval of the
     Chebyshev route, "gershgorin" or "lanczos" (tighter: fewer terms)."""
+    from .sparse import SparseHamiltonian
     if method not in ("auto", "chebyshev", "eigh"):
         raise ValueError("method must be auto, chebyshev or eigh")
     if N is not None and mu is not None:
@@ -161,10 +204,10 @@ def densitymatrix(H: Hamiltonian, mu=None, T: float = 0.0, *, N=None, statistics
     if stat not in _STATISTICS:
         raise ValueError("statistics must be FermiDirac or BoseEinstein")
     fermi_ensemble = N is None and (mu is not None or statistics is not None) and stat == "FermiDirac"
-    if method == "chebyshev" and not (fermi_ensemble and T > 0):
-        raise ValueError("the Chebyshev route covers the FermiDirac ensemble at T > 0 (the T = 0 occupation "
-                         "is a step)")
-    if fermi_ensemble and T > 0 and method != "eigh":
+    if method == "chebyshev" and not (fermi_ensemble and T > 0 and isinstance(H, Hamiltonian)):
+        raise ValueError("the Chebyshev route covers the FermiDirac ensemble at T > 0 of a square-lattice "
+                         "Hamiltonian (the T = 0 occupation is a step)")
+    if fermi_ensemble and T > 0 and method != "eigh" and isinstance(H, Hamiltonian):
         mu = 0.0 if mu is None else mu
         ctx = default_context()
         lo, hi = H.bounds(ctx, method=bounds)
@@ -176,17 +219,7 @@ def densitymatrix(H: Hamiltonian, mu=None, T: float = 0.0, *, N=None, statistics
         ctx.check(ctx.lib.lm_cheb_apply(dh.handle, float(bounds[0]), float(bounds[1]), _lib.dptr(coef), len(coef),
                                         None, out.handle))
         return out
-    torch = _torch_cuda()
-    w, V = diagonalize(H)
-    occ = torch.as_tensor(occupations(w, mu, T, N, statistics), device="cuda", dtype=torch.float64)
-    P = (V * occ) @ V.conj().T
-    if precision == "c32":
-        P = P.to(torch.complex64)
-    # the library's layout is column-major: a row-major copy of P^T holds P column-major
-    Pc = P.transpose(0, 1).contiguous()
-    torch.cuda.current_stream().synchronize()
-    ctx = default_context()
-    out = DensityMatrix(H.lattice, None, precision, ctx=ctx)
-    ctx.check(ctx.lib.lm_state_upload(out.handle, C.c_void_p(Pc.data_ptr()), H.lattice.N))
-    ctx.synchronize()  # Pc stays alive until the device copy is done
-    return out
+    if not isinstance(H, (Hamiltonian, SparseHamiltonian)):
+        raise TypeError("densitymatrix takes a device Hamiltonian (tightbinding_hamiltonian, SparseHamiltonian)")
+    eig = Eigensystem(H)
+    return eig.projector(occupations(eig.values, mu, T, N, statistics), precision)

@@ -412,13 +412,18 @@ def diagonalize(H):
     return vals[order], vecs[:, order]
 
 
-def densfun(T: float, mu: float, statistics: str = "FermiDirac"):
+def densfun(T: float, mu: float, statistics: str = "FermiDirac", degenerate_tol: float = 0.0):
     """src/spectrum.jl:230-232: E -> (E - mu == T == 0) ? 1 : 1 / (exp((E - mu)/T) + s) with
-    s = Int(statistics): +1 FermiDirac, -1 BoseEinstein."""
+    s = Int(statistics): +1 FermiDirac, -1 BoseEinstein.
+
+    degenerate_tol > 0 reads "E == mu" as |E - mu| <= degenerate_tol.  With the exact test (0,
+    the reference's rule) a level that is exactly degenerate at mu is split by the eigensolver's
+    rounding: each of its computed eigenvalues lands a few ulps above or below mu, and only
+    those below are occupied.  The tolerance occupies the whole level."""
     sgn = 1.0 if statistics == "FermiDirac" else -1.0
 
     def f(E):
-        if E - mu == 0 and T == 0:
+        if T == 0 and abs(E - mu) <= degenerate_tol:
             return 1.0
         with np.errstate(over="ignore", divide="ignore"):
             z = (E - mu) / T if T != 0 else (math.inf if E > mu else -math.inf)
@@ -439,7 +444,7 @@ def ddensfun(T: float, mu: float, statistics: str = "FermiDirac"):
     return f
 
 
-def densitymatrix_dispatch(H, mu=None, T: float = 0.0, N=None, statistics=None):
+def densitymatrix_dispatch(H, mu=None, T: float = 0.0, N=None, statistics=None, degenerate_tol: float = 0.0):
     """``densitymatrix(ham; kw...)`` of a one-particle system (src/spectrum.jl:226-333):
     * N given: fixn_densitymatrix -- at T = 0 the Fermi sphere (the lowest N states;
       BoseEinstein: N times the ground state), else mu by the reference's Newton iteration on
@@ -471,7 +476,7 @@ def densitymatrix_dispatch(H, mu=None, T: float = 0.0, N=None, statistics=None):
             newmu += dmu
         raise ValueError("did not converge")
     if mu is not None or statistics is not None:
-        f = densfun(T, 0.0 if mu is None else mu, stat)
+        f = densfun(T, 0.0 if mu is None else mu, stat, degenerate_tol)
         w = np.array([f(e) for e in vals])
         return (vecs * w) @ vecs.conj().T
     if abs(T) < 1e-10:
@@ -481,10 +486,10 @@ def densitymatrix_dispatch(H, mu=None, T: float = 0.0, N=None, statistics=None):
     return (vecs * w) @ vecs.conj().T
 
 
-def densitymatrix(H, mu: float = 0.0, T: float = 0.0):
+def densitymatrix(H, mu: float = 0.0, T: float = 0.0, degenerate_tol: float = 0.0):
     """projector(densfun(T, mu), eig) = V * (f(E) .* V') (src/spectrum.jl:226-228)."""
     vals, vecs = diagonalize(H)
-    f = densfun(T, mu)
+    f = densfun(T, mu, degenerate_tol=degenerate_tol)
     w = np.array([f(e) for e in vals])
     return (vecs * w) @ vecs.conj().T, vals, vecs
 

@@ -93,21 +93,17 @@ def test_differentiation_workload_fd(lm):
     component would otherwise report that error divided by its own small size.  The FP64
     adjoint is held to 1e-6 of FD with no floor, which shows that the FD reference itself is
     good to that level and that the remaining error is the FP32 arithmetic's."""
-    torch = pytest.importorskip("torch")
     L, M, dt, nsteps, spi = 64, 2048, 0.05, 400, 8
     point = (32.5, 32.5)
     rng = np.random.default_rng(5)
     V = rng.uniform(-0.1, 0.1, L * L)
     B = np.full(50, 0.1)
     ol = o.SquareLattice(L, L)
-    H0 = o.tightbinding_hamiltonian(ol, field=o.PointFlux(B[0], point), onsite=V)
-    Hd = torch.as_tensor(H0.toarray(), device="cuda")
-    w, Vec = torch.linalg.eigh(Hd)
-    psi0 = Vec[:, :M].cpu().numpy()
-    del Hd, Vec
+    lat = lm.SquareLattice(L, L)
+    # the M lowest eigenstates of h(V0) from the library's eigensystem
+    psi0 = lm.diagonalize(lm.tightbinding_hamiltonian(lat, V, field=lm.PointFlux(B[0], point))).vectors(0, M).to_numpy()
     c = rng.uniform(20, 44, size=2)
     target = bump(ol.coords, c, 6.0)
-    lat = lm.SquareLattice(L, L)
     p32 = lm.adjoint.DensityLossAdjoint(lat, psi0, target, dt, nsteps, spi, point, precision="c32")
     loss32, gV, gB = p32.loss_and_grad(V, B)
     p64 = lm.adjoint.DensityLossAdjoint(lat, psi0, target, dt, nsteps, spi, point, precision="c64",
