@@ -269,6 +269,24 @@ int lm_ell_set_values(lm_ell *h, const double *nzval);
 int lm_ell_bounds(const lm_ell *h, double *emin, double *emax);
 /* update_solver!(solver, H, dt, force) for a general Hamiltonian (src/evolution.jl:83-92);
  * lm_solver_step then applies its propagator to kets or density matrices. */
+/* A general lattice Hamiltonian assembled on the device from its bonds, the way the
+ * reference's builder assembles it (src/operators/builder.jl:296-309,
+ * src/operators/constructoperator.jl:4-47): bond b joins sites src[b] -> dst[b] (1-based)
+ * with real-space endpoints xy[4b .. 4b+3] = (x1, y1, x2, y2), the destination unwrapped across
+ * a periodic boundary, and base value base[2b], base[2b+1] (t1 times the boundary's twist
+ * factor).  lm_ell_assemble sets H[src, dst] += base exp(-2 pi i LI(field; r1 -> r2)) and
+ * H[dst, src] += its conjugate for every bond, H[i, i] = the on-site term, on the device:
+ * the Hamiltonian of every step of a time-dependent field is assembled without a host
+ * upload.  Field components: LM_FIELD_*, without boundary images (the reference's
+ * adapt_field replication applies to the square-lattice path).  Replaces passing the
+ * construct_operator CSC of HoneycombLattice / KagomeLattice / TriangularLattice models. */
+int lm_ell_create_bonds(lm_ctx *ctx, int64_t n, int64_t nbonds, const int64_t *src, const int64_t *dst,
+                        const double *xy, const double *base, lm_ell **out);
+int lm_ell_add_field(lm_ell *ham, int kind, double px, double py, int *component);
+/* n on-site values, or NULL for none (copied during the call). */
+int lm_ell_set_onsite(lm_ell *ham, const double *onsite);
+/* One amplitude per field component; asynchronous on the context's stream. */
+int lm_ell_assemble(lm_ell *ham, const double *amplitudes, int namp);
 int lm_ell_solver_update(lm_solver *s, lm_ell *h, double dt, int force);
 /* DensityCurrents(H, state)[i, j] = 2 Im(H[i,j] P[j,i]) (src/zoo/currents.jl:92-102) for every
  * stored entry of the CSC, in its order (0 for the diagonal): nnz doubles. */

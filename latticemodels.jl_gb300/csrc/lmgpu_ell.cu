@@ -374,6 +374,46 @@ cudaError_t launch_ell_op_currents(lm_ctx* ctx, const lm_ell* h, const lm_state*
     return cudaGetLastError();
 }
 
+// Values of a Hamiltonian built from a bond list (lm_ell_create_bonds), thread per CSC entry:
+// the sum, in bond order, of base * exp(-2 pi i LI(field; r_src -> r_dst)) over the bonds that
+// land on the entry (conjugated for the reverse entry H[dst, src]), the phase formed as the
+// square-lattice assembly forms it; the diagonal entry adds the on-site term.  The field
+// components of such Hamiltonians have no boundary images, so the geometry is not used.
+__global__ void ell_assemble_kernel(int64_t nnz, FieldSet f, const double* __restrict__ bxy,
+                                    const double2* __restrict__ bbase, const int64_t* __restrict__ eptr,
+                                    const int64_t* __restrict__ eterm, const int64_t* __restrict__ emap,
+                                    const double* __restrict__ onsite, double2* __restrict__ cval,
+                                    double2* __restrict__ vals, double* __restrict__ diag) {
+    const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= nnz) return;
+    const Geom g0{};
+    double2 v = make_double2(0.0, 0.0);
+    for (int64_t q = eptr[p]; q < eptr[p + 1]; ++q) {
+        const int64_t t = eterm[q], b = t >> 1;
+        const double* r = bxy + 4 * b;
+        const double li = f.n > 0 ? field_line_integral(g0, f, r[0], r[1], r[2], r[3]) : 0.0;
+        const double theta = __dmul_rn(-2.0 * M_PI, li);
+        double sn, cs;
+        sincos(theta, &sn, &cs);
+        const double2 base = bbase[b];
+        const double wx = __dsub_rn(__dmul_rn(base.x, cs), __dmul_rn(base.y, sn));
+        double wy = __dadd_rn(__dmul_rn(base.x, sn), __dmul_rn(base.y, cs));
+        if (t & 1) wy = -wy;
+        v.x = __dadd_rn(v.x, wx);
+        v.y = __dadd_rn(v.y, wy);
+    }
+    const int64_t slot = emap[p];
+    if (slot < 0) {
+        const int64_t i = -slot - 1;
+        const double d = __dadd_rn(onsite ? onsite[i] : 0.0, v.x);
+        cval[p] = make_double2(d, 0.0);
+        diag[i] = d;
+    } else {
+        cval[p] = v;
+        vals[slot] = v;
+    }
+}
+
 }  // namespace lmgpu
 
 using namespace lmgpu;
@@ -536,6 +576,12 @@ int lm_ell_destroy(lm_ell* h) {
     cudaFree(h->d_crow);
     cudaFree(h->d_ccol);
     cudaFree(h->d_cval);
+    cudaFree(h->d_bxy);
+    cudaFree(h->d_bbase);
+    cudaFree(h->d_eptr);
+    cudaFree(h->d_eterm);
+    cudaFree(h->d_emap);
+    cudaFree(h->d_onsite);
     delete h;
     return LM_OK;
 }
@@ -554,6 +600,168 @@ int lm_ell_bounds(const lm_ell* h, double* emin, double* emax) {
     CHECK_ARG(h->ctx, emin && emax, "lm_ell_bounds: null output");
     *emin = h->emin;
     *emax = h->emax;
+    return LM_OK;
+}
+
+static void ell_bond_bounds(lm_ell* h) {
+    h->emin = h->emax = 0.0;
+    for (int64_t i = 0; i < h->n; ++i) {
+        const double d = h->h_onsite.empty() ? 0.0 : h->h_onsite[(size_t)i];
+        const double lo = d - h->rad[(size_t)i], hi = d + h->rad[(size_t)i];
+        if (i == 0 || lo < h->emin) h->emin = lo;
+        if (i == 0 || hi > h->emax) h->emax = hi;
+    }
+}
+
+int lm_ell_create_bonds(lm_ctx* ctx, int64_t n, int64_t nbonds, const int64_t* src, const int64_t* dst,
+                        const double* xy, const double* base, lm_ell** out) {
+    if (!ctx) return LM_ERR_ARG;
+    CHECK_ARG(ctx, out != nullptr, "lm_ell_create_bonds: null output");
+    *out = nullptr;
+    CHECK_ARG(ctx, n >= 1 && n < ((int64_t)1 << 31), "lm_ell_create_bonds: bad size");
+    CHECK_ARG(ctx, nbonds >= 0, "lm_ell_create_bonds: negative bond count");
+    CHECK_ARG(ctx, nbonds == 0 || (src && dst && xy && base), "lm_ell_create_bonds: null bond arrays");
+    for (int64_t b = 0; b < nbonds; ++b) {
+        CHECK_ARG(ctx, src[b] >= 1 && src[b] <= n && dst[b] >= 1 && dst[b] <= n, "lm_ell_create_bonds: site out of range");
+        for (int k = 0; k < 4; ++k) CHECK_ARG(ctx, isfinite(xy[4 * b + k]), "lm_ell_create_bonds: non-finite coordinate");
+        CHECK_ARG(ctx, isfinite(base[2 * b]) && isfinite(base[2 * b + 1]), "lm_ell_create_bonds: non-finite hop");
+    }
+    // the pattern: every diagonal entry and both entries of every bond, in CSC order
+    std::vector<std::pair<int64_t, int64_t>> keys;  // (column, row), 0-based
+    keys.reserve((size_t)(n + 2 * nbonds));
+    for (int64_t i = 0; i < n; ++i) keys.push_back({i, i});
+    for (int64_t b = 0; b < nbonds; ++b) {
+        keys.push_back({dst[b] - 1, src[b] - 1});
+        keys.push_back({src[b] - 1, dst[b] - 1});
+    }
+    std::sort(keys.begin(), keys.end());
+    keys.erase(std::unique(keys.begin(), keys.end()), keys.end());
+    const int64_t nnz = (int64_t)keys.size();
+    std::vector<int64_t> colptr((size_t)n + 1, 0), rowval((size_t)nnz);
+    for (int64_t p = 0; p < nnz; ++p) {
+        colptr[(size_t)keys[(size_t)p].first + 1]++;
+        rowval[(size_t)p] = keys[(size_t)p].second + 1;
+    }
+    colptr[0] = 1;
+    for (int64_t j = 0; j < n; ++j) colptr[(size_t)j + 1] += colptr[(size_t)j];
+    std::vector<double> zeros((size_t)(2 * nnz), 0.0);
+    lm_ell* h = nullptr;
+    int rc = lm_ell_create_csc(ctx, n, colptr.data(), rowval.data(), zeros.data(), &h);
+    if (rc != LM_OK) return rc;
+    // contributions of every entry, in bond order (forward entry, then reverse)
+    auto entry = [&](int64_t row, int64_t col) {
+        return (int64_t)(std::lower_bound(keys.begin(), keys.end(), std::make_pair(col, row)) - keys.begin());
+    };
+    std::vector<int64_t> cnt((size_t)nnz + 1, 0);
+    std::vector<int64_t> pf((size_t)nbonds), pr((size_t)nbonds);
+    for (int64_t b = 0; b < nbonds; ++b) {
+        pf[(size_t)b] = entry(src[b] - 1, dst[b] - 1);
+        pr[(size_t)b] = entry(dst[b] - 1, src[b] - 1);
+        cnt[(size_t)pf[(size_t)b] + 1]++;
+        cnt[(size_t)pr[(size_t)b] + 1]++;
+    }
+    for (int64_t p = 0; p < nnz; ++p) cnt[(size_t)p + 1] += cnt[(size_t)p];
+    std::vector<int64_t> term((size_t)(2 * nbonds)), fillp(cnt.begin(), cnt.end() - 1);
+    h->rad.assign((size_t)n, 0.0);
+    for (int64_t b = 0; b < nbonds; ++b) {
+        term[(size_t)fillp[(size_t)pf[(size_t)b]]++] = b << 1;
+        term[(size_t)fillp[(size_t)pr[(size_t)b]]++] = (b << 1) | 1;
+        const double a = hypot(base[2 * b], base[2 * b + 1]);
+        h->rad[(size_t)(src[b] - 1)] += a;
+        h->rad[(size_t)(dst[b] - 1)] += a;
+    }
+    h->nbonds = nbonds;
+    cudaSetDevice(ctx->device);
+    cudaError_t e = cudaMalloc((void**)&h->d_bxy, sizeof(double) * (size_t)std::max<int64_t>(4 * nbonds, 1));
+    if (e == cudaSuccess) e = cudaMalloc((void**)&h->d_bbase, sizeof(double2) * (size_t)std::max<int64_t>(nbonds, 1));
+    if (e == cudaSuccess) e = cudaMalloc((void**)&h->d_eptr, sizeof(int64_t) * (size_t)(nnz + 1));
+    if (e == cudaSuccess) e = cudaMalloc((void**)&h->d_eterm, sizeof(int64_t) * (size_t)std::max<int64_t>(2 * nbonds, 1));
+    if (e == cudaSuccess) e = cudaMalloc((void**)&h->d_emap, sizeof(int64_t) * (size_t)nnz);
+    if (e == cudaSuccess && nbonds > 0) {
+        e = cudaMemcpy(h->d_bxy, xy, sizeof(double) * (size_t)(4 * nbonds), cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) e = cudaMemcpy(h->d_bbase, base, sizeof(double2) * (size_t)nbonds, cudaMemcpyHostToDevice);
+        if (e == cudaSuccess)
+            e = cudaMemcpy(h->d_eterm, term.data(), sizeof(int64_t) * term.size(), cudaMemcpyHostToDevice);
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(h->d_eptr, cnt.data(), sizeof(int64_t) * cnt.size(), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(h->d_emap, h->map.data(), sizeof(int64_t) * (size_t)nnz, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        rc = check_cuda(ctx, e, "lm_ell_create_bonds: device tables");
+        lm_ell_destroy(h);
+        return rc;
+    }
+    ell_bond_bounds(h);
+    *out = h;
+    return LM_OK;
+}
+
+int lm_ell_add_field(lm_ell* h, int kind, double px, double py, int* component) {
+    if (!h) return LM_ERR_ARG;
+    lm_ctx* ctx = h->ctx;
+    CHECK_ARG(ctx, h->d_eptr != nullptr, "lm_ell_add_field: the Hamiltonian was not built from bonds");
+    CHECK_ARG(ctx, kind >= LM_FIELD_LANDAU && kind <= LM_FIELD_POINTFLUX_SINGULAR, "lm_ell_add_field: unknown field kind");
+    CHECK_ARG(ctx, isfinite(px) && isfinite(py), "lm_ell_add_field: non-finite point");
+    if (h->fields.n >= kMaxFields) return set_err(ctx, LM_ERR_NOTSUP, "lm_ell_add_field: too many field components");
+    FieldComp fc{};
+    fc.kind = kind;
+    fc.px = px;
+    fc.py = py;
+    fc.replicate = 0;
+    const int idx = h->fields.n;
+    h->fields.c[idx] = fc;
+    h->fields.amp[idx] = 0.0;
+    h->fields.n++;
+    h->assembled = 0;
+    if (component) *component = idx;
+    return LM_OK;
+}
+
+int lm_ell_set_onsite(lm_ell* h, const double* v) {
+    if (!h) return LM_ERR_ARG;
+    lm_ctx* ctx = h->ctx;
+    CHECK_ARG(ctx, h->d_eptr != nullptr, "lm_ell_set_onsite: the Hamiltonian was not built from bonds");
+    cudaSetDevice(ctx->device);
+    if (!v) {
+        h->h_onsite.clear();
+    } else {
+        for (int64_t i = 0; i < h->n; ++i) CHECK_ARG(ctx, isfinite(v[i]), "lm_ell_set_onsite: non-finite value");
+        if (!h->d_onsite) {
+            cudaError_t e = cudaMalloc((void**)&h->d_onsite, sizeof(double) * (size_t)h->n);
+            if (e != cudaSuccess) {
+                cudaGetLastError();
+                h->d_onsite = nullptr;
+                return check_cuda(ctx, e, "lm_ell_set_onsite: allocation");
+            }
+        }
+        h->h_onsite.assign(v, v + h->n);
+        // synchronous copy: the caller's array is free when the call returns
+        CUDA_TRY(ctx, cudaMemcpyAsync(h->d_onsite, h->h_onsite.data(), sizeof(double) * (size_t)h->n,
+                                      cudaMemcpyHostToDevice, ctx->stream), "lm_ell_set_onsite: upload");
+        CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream), "lm_ell_set_onsite: synchronize");
+    }
+    ell_bond_bounds(h);
+    h->assembled = 0;
+    return LM_OK;
+}
+
+int lm_ell_assemble(lm_ell* h, const double* amplitudes, int namp) {
+    if (!h) return LM_ERR_ARG;
+    lm_ctx* ctx = h->ctx;
+    CHECK_ARG(ctx, h->d_eptr != nullptr, "lm_ell_assemble: the Hamiltonian was not built from bonds");
+    CHECK_ARG(ctx, namp == h->fields.n, "lm_ell_assemble: one amplitude per field component");
+    for (int c = 0; c < namp; ++c) {
+        CHECK_ARG(ctx, amplitudes && isfinite(amplitudes[c]), "lm_ell_assemble: non-finite amplitude");
+        h->fields.amp[c] = amplitudes[c];
+    }
+    cudaSetDevice(ctx->device);
+    ell_assemble_kernel<<<(unsigned)((h->nnz + 255) / 256), 256, 0, ctx->stream>>>(
+        h->nnz, h->fields, h->d_bxy, h->d_bbase, h->d_eptr, h->d_eterm, h->d_emap,
+        h->h_onsite.empty() ? nullptr : h->d_onsite, h->d_cval, h->d_vals, h->d_diag);
+    ctx->launches++;
+    CUDA_TRY(ctx, cudaGetLastError(), "lm_ell_assemble");
+    h->version++;
+    h->assembled = 1;
     return LM_OK;
 }
 

@@ -207,6 +207,20 @@ struct lm_ell {
     uint64_t version = 0;
     std::vector<double2> h_vals;       // host staging of the ELL values
     std::vector<double> h_diag;
+    // device assembly from a bond list (lm_ell_create_bonds): every CSC entry sums, in a fixed
+    // order, the bonds that land on it (base * exp(-2 pi i LI(r_src -> r_dst)), or its
+    // conjugate for the reverse entry); the diagonal adds the on-site term
+    int64_t nbonds = 0;
+    double* d_bxy = nullptr;           // 4 per bond: x1 y1 x2 y2 (destination unwrapped)
+    double2* d_bbase = nullptr;        // base value per bond (t1 times the boundary twist)
+    int64_t* d_eptr = nullptr;         // CSR over CSC entries: contributions of entry p
+    int64_t* d_eterm = nullptr;        // contribution: (bond << 1) | conjugate
+    int64_t* d_emap = nullptr;         // ELL slot of entry p, or -(row + 1) for the diagonal
+    double* d_onsite = nullptr;        // on-site term (n) or null
+    std::vector<double> h_onsite;      // its host copy (for the bounds)
+    std::vector<double> rad;           // Gershgorin radius per row: sum of |base| (field-free)
+    lmgpu::FieldSet fields{};
+    int assembled = 0;
 };
 
 // Argument and CUDA-status checks that return the status from the calling C-ABI function.

@@ -856,7 +856,7 @@ end
 `densitymatrix(H; mu, T)` for T > 0 (src/spectrum.jl:252-257) without an eigensystem: the
 Chebyshev series of the FermiDirac occupation f(E) = 1 / (exp((E - mu)/T) + 1)
 (src/spectrum.jl:230-232) applied to the identity on the device.  At T = 0 the occupation is a
-step and its series does not converge; that case keeps the eigensystem route.
+step and its series does not converge; `densitymatrix` takes the device eigensystem there.
 """
 function gpu_densitymatrix(H::DeviceHamiltonian; mu, T, precision=LM_C64, tol=1e-13, bounds=padded_bounds(H))
     T > 0 || throw(ArgumentError("the Chebyshev Fermi operator needs T > 0"))
@@ -873,9 +873,94 @@ function gpu_densitymatrix(H::DeviceHamiltonian; mu, T, precision=LM_C64, tol=1e
     return out
 end
 
+# ---- eigensystem: diagonalize / densitymatrix at T = 0 (src/spectrum.jl:48-55, :226-257) -----
+"""
+    GPUEigensystem(H)
+
+The FP64 eigensystem of a device Hamiltonian on the library's own kernels (lm_eigsys_*):
+`values` in ascending order, eigenvectors and weighted projectors on demand.
+"""
+mutable struct GPUEigensystem
+    ctx::Context
+    handle::Ptr{Cvoid}
+    lat::DeviceLattice
+    values::Vector{Float64}
+end
+function GPUEigensystem(H::DeviceHamiltonian)
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    ctx = H.lat.ctx
+    check(ccall((:lm_eigsys_create, LIB), Cint, (Ptr{Cvoid}, Ref{Ptr{Cvoid}}), handle(H), h), ctx.handle)
+    return _eigsys(ctx, h[], H.lat)
+end
+function GPUEigensystem(H::GPUSparseHamiltonian)
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:lm_eigsys_create_ell, LIB), Cint, (Ptr{Cvoid}, Ref{Ptr{Cvoid}}), H.handle, h), H.ctx.handle)
+    return _eigsys(H.ctx, h[], context_lattice(H.ctx))
+end
+function _eigsys(ctx::Context, h::Ptr{Cvoid}, lat::DeviceLattice)
+    n = Ref{Int64}(0)
+    check(ccall((:lm_eigsys_size, LIB), Cint, (Ptr{Cvoid}, Ref{Int64}), h, n), ctx.handle)
+    w = Vector{Float64}(undef, n[])
+    check(ccall((:lm_eigsys_values, LIB), Cint, (Ptr{Cvoid}, Ptr{Float64}), h, w), ctx.handle)
+    e = GPUEigensystem(ctx, h, lat, w)
+    finalizer(e -> ccall((:lm_eigsys_destroy, LIB), Cint, (Ptr{Cvoid},), e.handle), e)
+    return e
+end
+# eigenvectors first .. first + m - 1 as an n x m device ket block
+function eigenvectors(e::GPUEigensystem, first::Integer=1, m::Integer=length(e.values) - first + 1; precision=LM_C64)
+    n = length(e.values)
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:lm_state_create, LIB), Cint, (Ptr{Cvoid}, Int64, Int64, Cint, Cint, Ref{Ptr{Cvoid}}),
+                e.ctx.handle, n, m, LM_KETS, precision, h), e.ctx.handle)
+    out = DeviceState(e.lat, h[], n, m, LM_KETS, precision)
+    finalizer(s -> ccall((:lm_state_destroy, LIB), Cint, (Ptr{Cvoid},), s.handle), out)
+    check(ccall((:lm_eigsys_vectors, LIB), Cint, (Ptr{Cvoid}, Int64, Ptr{Cvoid}), e.handle, first - 1, out.handle),
+          e.ctx.handle)
+    return out
+end
+# sum_k w_k v_k v_k^H as an n x n device density matrix
+function projector(e::GPUEigensystem, w::AbstractVector{<:Real}; precision=LM_C64)
+    n = length(e.values)
+    length(w) == n || throw(DimensionMismatch("one weight per eigenvalue"))
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:lm_state_create, LIB), Cint, (Ptr{Cvoid}, Int64, Int64, Cint, Cint, Ref{Ptr{Cvoid}}),
+                e.ctx.handle, n, n, LM_DENSITY, precision, h), e.ctx.handle)
+    out = DeviceState(e.lat, h[], n, n, LM_DENSITY, precision)
+    finalizer(s -> ccall((:lm_state_destroy, LIB), Cint, (Ptr{Cvoid},), s.handle), out)
+    check(ccall((:lm_eigsys_projector, LIB), Cint, (Ptr{Cvoid}, Ptr{Float64}, Ptr{Cvoid}), e.handle,
+                Vector{Float64}(w), out.handle), e.ctx.handle)
+    return out
+end
+
+# "E == mu" at T = 0 (src/spectrum.jl:230-232) is |E - mu| <= 1e-12 max(1, |E|max): a level
+# that is exactly degenerate at mu is occupied as a whole, not split by rounding.
+degenerate_tol(w) = 1e-12 * max(1.0, maximum(abs, w; init=0.0))
+
+"""
+    densitymatrix(H; mu, T=0, precision=LM_C64)
+
+The reference's `densitymatrix` (src/spectrum.jl:226-257, :317-333) for a Hamiltonian built
+with `GPUBuilder`: an `Operator` whose `.data` is a `DeviceState`.  T > 0: the Chebyshev series
+of the FermiDirac occupation on the device (`gpu_densitymatrix`); T = 0: the device eigensystem
+with the occupied levels E <= mu (E == mu occupied, as the reference's densfun does).
+"""
+function densitymatrix(ham::LatticeModels.Hamiltonian{<:Any,<:Any,<:DeviceHamiltonian}; mu=nothing, μ=mu, T=0,
+                       precision=LM_C64)
+    mu = something(μ, 0.0)
+    H = ham.data
+    st = if T > 0
+        gpu_densitymatrix(H; mu=mu, T=T, precision=precision)
+    else
+        e = GPUEigensystem(H)
+        tol = degenerate_tol(e.values)
+        projector(e, [E - mu <= tol ? 1.0 : 0.0 for E in e.values]; precision=precision)
+    end
+    return QuantumOpticsBase.Operator(QuantumOpticsBase.basis(ham), st)
+end
+
 export GPUBuilder, ChebyshevGPU, DeviceLattice, DeviceState, DeviceVector, DeviceHamiltonian, to_device,
        gpu_tightbinding, bond_currents, lattice_bonds, ReadoutRing, gpu_timesequence, gpu_timesequences,
-       loss_and_gradients, GPUBatch, DensityLossProblem, density_loss, GPUSparseHamiltonian, set_values!, gpu_operator_currents,
+       loss_and_gradients, GPUEigensystem, eigenvectors, projector, GPUBatch, DensityLossProblem, density_loss, GPUSparseHamiltonian, set_values!, gpu_operator_currents,
        gpu_operator_timesequence, gpu_synchronize, set_option!, set_weights!, gpu_trace, gpu_norms, gpu_renormalize!,
        device_pointer, solver_order, spectral_bounds, padded_bounds, kpm_moments, chebyshev_coefficients,
        gpu_densitymatrix, gpu_entry_currents, LM_OPT_FUSED, LM_OPT_STREAM, LM_OPT_KPM

@@ -9,6 +9,7 @@ from ._lib import LMError, load as load_library
 from . import adjoint, kpm
 from .adjoint import DensityLossAdjoint
 from .batch import Batch
+from .bravais import BravaisLattice, HoneycombLattice, KagomeLattice, LatticeHamiltonian, TriangularLattice
 from .device import Context, default_context
 from .evolution import ChebyshevGPU, Evolution, EvolutionIterator, EvolutionSolver, EvolutionTimestamp
 from .fields import FieldSum, LandauGauge, NoField, PointFlux, PointFluxes, SymmetricGauge
@@ -29,5 +30,5 @@ __all__ = [
     "Currents", "DensityCurrents", "SubCurrents", "currentsfrom", "currentsfromto", "localdensity", "densitymatrix", "diagonalize",
     "DensityMatrix", "DeviceState", "Ket", "KetBlock", "Operator",
     "LocalOperatorCurrents", "SiteCurrents", "Sites", "SparseHamiltonian", "entry_currents", "ReadoutRing", "TimeSequence", "differentiate", "integrate", "moment_currents", "moment_density",
-    "timesequences",
+    "timesequences", "BravaisLattice", "HoneycombLattice", "KagomeLattice", "TriangularLattice", "LatticeHamiltonian",
 ]

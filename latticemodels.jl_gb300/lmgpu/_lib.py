@@ -107,6 +107,10 @@ SIGNATURES = {
     "lm_ell_destroy": (_INT, [_P]),
     "lm_ell_set_values": (_INT, [_P, _PD]),
     "lm_ell_bounds": (_INT, [_P, _PD, _PD]),
+    "lm_ell_create_bonds": (_INT, [_P, _I64, _I64, _PI64, _PI64, _PD, _PD, C.POINTER(_P)]),
+    "lm_ell_add_field": (_INT, [_P, _INT, _D, _D, _PINT]),
+    "lm_ell_set_onsite": (_INT, [_P, _PD]),
+    "lm_ell_assemble": (_INT, [_P, _PD, _INT]),
     "lm_ell_solver_update": (_INT, [_P, _P, _D, _INT]),
     "lm_ell_currents": (_INT, [_P, _P, _PD]),
     "lm_ell_op_currents": (_INT, [_P, _P, C.c_int, _PD, _PD]),

@@ -157,6 +157,9 @@ def tightbinding_hamiltonian(lattice: SquareLattice, *args, t1=1, t2=0, t3=0, fi
     ``LatticeValue => 1`` pair of the reference.  Next-nearest (t2) and third-neighbour (t3)
     hopping are outside this backend.
     """
+    from .bravais import BravaisLattice, bravais_tightbinding
+    if isinstance(lattice, BravaisLattice):  # HoneycombLattice, KagomeLattice, TriangularLattice
+        return bravais_tightbinding(lattice, *args, t1=t1, t2=t2, t3=t3, field=field)
     if t2 != 0 or t3 != 0:
         raise NotImplementedError("t2/t3 hopping is not implemented by the GPU backend")
     onsite = None

@@ -197,8 +197,9 @@ class PointFlux:
         x1, y1 = p1[0] - px, p1[1] - py
         x2, y2 = p2[0] - px, p2[1] - py
         if self.gauge == "axial":  # :72-85
-            n1 = math.hypot(x1, y1)
-            n2 = math.hypot(x2, y2)
+            # norm(p) of a 2-vector: sqrt(x^2 + y^2) with separate products (no hypot scaling)
+            n1 = math.sqrt(x1 * x1 + y1 * y1)
+            n2 = math.sqrt(x2 * x2 + y2 * y2)
             if n1 < FLUX_EPS or n2 < FLUX_EPS:
                 return 0.0 * self.flux
             nnorm = n1 * n2
@@ -835,11 +836,45 @@ def honeycomb_sites(a: int, b: int):
     return coords, idx
 
 
-def honeycomb_hamiltonian(a: int, b: int, t1: float = 1.0, B: float = 0.0, onsite=None):
+def _bond_matrix(N, pairs, coords, t1, field, onsite):
+    """H[i,j] += t1 e^{-2 pi i LI(r_i -> r_j)}, H[j,i] += its conjugate for every (i, j) in pairs,
+    plus the on-site term (src/operators/builder.jl:296-309)."""
+    H = sp.lil_matrix((N, N), dtype=np.complex128)
+    for i, j in pairs:
+        r1 = (float(coords[i][0]), float(coords[i][1]))
+        r2 = (float(coords[j][0]), float(coords[j][1]))
+        li = 0.0 if field is None else field.line_integral(r1, r2)
+        v = t1 * np.exp(-2j * math.pi * li)
+        H[i, j] += v
+        H[j, i] += np.conj(v)
+    if onsite is not None:
+        H.setdiag(H.diagonal() + np.asarray(onsite))
+    return H.tocsc()
+
+
+def honeycomb_hamiltonian(a: int, b: int, t1: float = 1.0, B: float = 0.0, onsite=None, field=None):
     """Nearest-neighbour tight-binding on HoneycombLattice(a, b), open boundaries: site A of
     cell (j1, j2) bonds to B of (j1, j2), (j1-1, j2) and (j1, j2-1) (distance 1/sqrt(3)), with
-    H[i,j] = t1 e^{-2 pi i LI(r_i -> r_j)} for LandauGauge(B), LI = (x1+x2)(y2-y1)B/2
+    H[i,j] = t1 e^{-2 pi i LI(r_i -> r_j)} for LandauGauge(B) (or ``field``), LI = (x1+x2)(y2-y1)B/2
     (src/zoo/magneticfields.jl:11-15), H[j,i] its conjugate, and the on-site term."""
+    coords, idx = honeycomb_sites(a, b)
+    pairs = []
+    for j1 in range(1, a + 1):
+        for j2 in range(1, b + 1):
+            for (k1, k2) in ((j1, j2), (j1 - 1, j2), (j1, j2 - 1)):
+                if 1 <= k1 <= a and 1 <= k2 <= b:
+                    pairs.append((idx(j1, j2, 1), idx(k1, k2, 2)))
+    fld = field if field is not None else (LandauGauge(B) if B else None)
+    return _bond_matrix(2 * a * b, pairs, coords, t1, fld, onsite), coords
+
+
+def honeycomb_hamiltonian_periodic(a: int, b: int, periodic=(True, True), twist=(0.0, 0.0), t1: float = 1.0,
+                                   field=None, onsite=None):
+    """HoneycombLattice(a, b) with periodic axes (translations a a1, b a2) and twists: the bond
+    from A of cell j to B of cell k = j, j - (1,0), j - (0,1) wraps k back into the patch
+    (k1 < 1: k1 + a, factor e^{-i Theta_1}; k2 < 1: k2 + b, e^{-i Theta_2}, the phase of a
+    boundary crossed backwards), the line integral runs to the unwrapped position of k
+    (src/core/boundaries.jl:251-289)."""
     coords, idx = honeycomb_sites(a, b)
     N = 2 * a * b
     H = sp.lil_matrix((N, N), dtype=np.complex128)
@@ -847,16 +882,73 @@ def honeycomb_hamiltonian(a: int, b: int, t1: float = 1.0, B: float = 0.0, onsit
         for j2 in range(1, b + 1):
             i = idx(j1, j2, 1)
             for (k1, k2) in ((j1, j2), (j1 - 1, j2), (j1, j2 - 1)):
-                if 1 <= k1 <= a and 1 <= k2 <= b:
-                    j = idx(k1, k2, 2)
-                    (x1, y1), (x2, y2) = coords[i], coords[j]
-                    li = (x1 + x2) * (y2 - y1) * B / 2
-                    v = t1 * np.exp(-2j * math.pi * li)
-                    H[i, j] += v
-                    H[j, i] += np.conj(v)
+                f = 1.0 + 0.0j
+                w1, w2 = k1, k2
+                if w1 < 1:
+                    if not periodic[0]:
+                        continue
+                    w1 += a
+                    f *= complex(math.cos(twist[0]), -math.sin(twist[0]))
+                if w2 < 1:
+                    if not periodic[1]:
+                        continue
+                    w2 += b
+                    f *= complex(math.cos(twist[1]), -math.sin(twist[1]))
+                j = idx(w1, w2, 2)
+                r2 = HONEYCOMB_BASIS[:, 1] + HONEYCOMB_T @ np.array([k1, k2], dtype=float)
+                li = 0.0 if field is None else field.line_integral((float(coords[i][0]), float(coords[i][1])),
+                                                                   (float(r2[0]), float(r2[1])))
+                v = t1 * f * np.exp(-2j * math.pi * li)
+                H[i, j] += v
+                H[j, i] += np.conj(v)
     if onsite is not None:
         H.setdiag(H.diagonal() + np.asarray(onsite))
     return H.tocsc(), coords
+
+
+KAGOME_BASIS = np.array([[0.0, 0.5, 0.25], [0.0, 0.0, math.sqrt(3) / 4]])
+
+
+def kagome_hamiltonian(a: int, b: int, t1: float = 1.0, field=None, onsite=None):
+    """Nearest-neighbour tight-binding on KagomeLattice(a, b) (src/zoo/lattices.jl:200-211),
+    open boundaries: sites A (0,0), B (1/2,0), C (1/4, sqrt(3)/4) per cell, sites ordered by
+    (j1, j2, basis); bonds of length 1/2: A-B, A-C, B-C in the cell, B(j) - A(j + (1,0)),
+    C(j) - A(j + (0,1)), C(j) - B(j + (-1,1))."""
+    idx = lambda j1, j2, s: ((j1 - 1) * b + (j2 - 1)) * 3 + (s - 1)
+    coords = np.zeros((3 * a * b, 2))
+    for j1 in range(1, a + 1):
+        for j2 in range(1, b + 1):
+            for s in (1, 2, 3):
+                coords[idx(j1, j2, s)] = KAGOME_BASIS[:, s - 1] + HONEYCOMB_T @ np.array([j1, j2], dtype=float)
+    pairs = []
+    ok = lambda k1, k2: 1 <= k1 <= a and 1 <= k2 <= b
+    for j1 in range(1, a + 1):
+        for j2 in range(1, b + 1):
+            pairs += [(idx(j1, j2, 1), idx(j1, j2, 2)), (idx(j1, j2, 1), idx(j1, j2, 3)), (idx(j1, j2, 2), idx(j1, j2, 3))]
+            if ok(j1 + 1, j2):
+                pairs.append((idx(j1, j2, 2), idx(j1 + 1, j2, 1)))
+            if ok(j1, j2 + 1):
+                pairs.append((idx(j1, j2, 3), idx(j1, j2 + 1, 1)))
+            if ok(j1 - 1, j2 + 1):
+                pairs.append((idx(j1, j2, 3), idx(j1 - 1, j2 + 1, 2)))
+    return _bond_matrix(3 * a * b, pairs, coords, t1, field, onsite), coords
+
+
+def triangular_hamiltonian(a: int, b: int, t1: float = 1.0, field=None, onsite=None):
+    """Nearest-neighbour tight-binding on TriangularLattice(a, b) (src/zoo/lattices.jl:136-143),
+    open boundaries: site (j1, j2) bonds to (j1+1, j2), (j1, j2+1) and (j1-1, j2+1)."""
+    idx = lambda j1, j2: (j1 - 1) * b + (j2 - 1)
+    coords = np.zeros((a * b, 2))
+    for j1 in range(1, a + 1):
+        for j2 in range(1, b + 1):
+            coords[idx(j1, j2)] = HONEYCOMB_T @ np.array([j1, j2], dtype=float)
+    pairs = []
+    for j1 in range(1, a + 1):
+        for j2 in range(1, b + 1):
+            for (k1, k2) in ((j1 + 1, j2), (j1, j2 + 1), (j1 - 1, j2 + 1)):
+                if 1 <= k1 <= a and 1 <= k2 <= b:
+                    pairs.append((idx(j1, j2), idx(k1, k2)))
+    return _bond_matrix(a * b, pairs, coords, t1, field, onsite), coords
 
 
 def qwz_hamiltonian(Lx: int, Ly: int, m=1.0, field=None):

@@ -192,6 +192,11 @@ def test_readouts_are_methods_of_the_reference_functions():
     assert re.search(r"LinearAlgebra\.tr\(st::DeviceState\) =", code)
     assert re.search(r"function Base\.copy\(s::DeviceState\)", code)
     assert re.search(r"Base\.copy\(v::DeviceVector\)", code)
+    # densitymatrix on a GPUBuilder Hamiltonian: the device eigensystem at T = 0
+    m = re.search(r"function densitymatrix\(ham::LatticeModels\.Hamiltonian\{<:Any,<:Any,<:DeviceHamiltonian\};(.*?)\nend",
+                  code, re.S)
+    assert m and "GPUEigensystem(H)" in m.group(1) and "gpu_densitymatrix" in m.group(1)
+    assert "QuantumOpticsBase.Operator(QuantumOpticsBase.basis(ham), st)" in m.group(1)
     # the plugin methods for both state kinds
     assert re.search(r"step!\(s::ChebyshevGPU, st::DeviceState, _cache\)", code)
     assert re.search(r"step!\(s::ChebyshevGPU, v::DeviceVector, cache\)", code)
