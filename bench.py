@@ -137,6 +137,7 @@ def measured_peak_hbm():
 
 
 TRAFFIC_RECORD = "cheb_stream_c32_256x256.traffic.json"
+TRAFFIC_RECORD_COMP = "cheb_stream_c32_comp_256x256.traffic.json"
 
 
 def kernel_source_hash(sources):
@@ -732,7 +733,7 @@ def main():
             ms = float(t.item())
         return ms, order_ms, order_launches, launches
 
-    # ---- chosen form (c32) -------------------------------------------------------------
+    # ---- FP32 form (c32) ---------------------------------------------------------------
     s32 = lmgpu.KetBlock(lat, X, precision="c32")
     solver32 = lmgpu.ChebyshevGPU(tol=args.tol32, renorm_every=20)
     clk = ClockSampler(local)
@@ -744,15 +745,56 @@ def main():
     # dominant kernel timing pass (events around every Chebyshev sweep, resolved lazily)
     _, order_ms, order_launches, _ = timed_steps(s32, solver32, args.steps, timing=True)
 
+    # ---- compensated FP32 form (value + rounding residual per amplitude) --------------
+    del s32
+    s32c = lmgpu.KetBlock(lat, X, precision="c32", compensated=True)
+    solver32c = lmgpu.ChebyshevGPU(tol=args.tol32, renorm_every=20)
+    n_stream0 = ctx.stream_launches()
+    ms32c, _, _, launches32c = timed_steps(s32c, solver32c, args.steps)
+    streamed_c = ctx.stream_launches() - n_stream0 > 0
+    _, order_ms_c, order_launches_c, _ = timed_steps(s32c, solver32c, args.steps, timing=True)
+    del s32c
+
     # ---- plain form (c64) --------------------------------------------------------------
     s64 = lmgpu.KetBlock(lat, X, precision="c64")
     solver64 = lmgpu.ChebyshevGPU()
     ms64, _, _, _ = timed_steps(s64, solver64, args.steps)
     clocks = clk.stop()
-    clocks["window"] = "sampled every 100 ms over the timed c32 and c64 passes"
+    clocks["window"] = "sampled every 100 ms over the timed c32, compensated c32 and c64 passes"
     K64, _, _ = solver64.order(s64)
 
     del s64
+
+    # ---- error of the FP32 forms against FP64 over the configuration's full length ------
+    # an untimed pass: all forms from the same kets, err_steps steps of the same H and dt
+    def fp32_error(compensated):
+        s32e = lmgpu.KetBlock(lat, X, precision="c32", compensated=compensated)
+        sol32e = lmgpu.ChebyshevGPU(tol=args.tol32, renorm_every=20)
+        c32e = sol32e.evolution_cache(s32e)
+        sol32e.update_solver(H, DT)
+        for _ in range(args.err_steps):
+            sol32e.step(s32e, c32e)
+        r32 = lmgpu.localdensity(s32e).values
+        J32 = lmgpu.DensityCurrents(H, s32e).bond_values()
+        return {"density": float(np.linalg.norm(r32 - r64) / np.linalg.norm(r64)),
+                "currents": float(np.linalg.norm(J32 - J64) / np.linalg.norm(J64)),
+                "norm_drift": float(np.abs(s32e.norms() - 1.0).max()),
+                "norm_drift_fp64": drift64, "steps": args.err_steps, "kets": M}
+
+    s64e = lmgpu.KetBlock(lat, X, precision="c64")
+    sol64e = lmgpu.ChebyshevGPU()
+    sol64e.update_solver(H, DT)
+    for _ in range(args.err_steps):
+        sol64e.step(s64e)
+    r64 = lmgpu.localdensity(s64e).values
+    J64 = lmgpu.DensityCurrents(H, s64e).bond_values()
+    drift64 = float(np.abs(s64e.norms() - 1.0).max())
+    del s64e
+    err_plain32 = fp32_error(False)
+    err_comp = fp32_error(True) if streamed_c else None
+    # the chosen form: the compensated one where it meets the metric's 1e-6 bar, else plain FP32
+    use_comp = err_comp is not None and max(err_comp["density"], err_comp["currents"]) <= 1e-6
+    err = err_comp if use_comp else err_plain32
 
     # ---- end to end through the public API with host buffers ----------------------------
     # The reference README's loop: every moment of ev(times) yields localdensity(P) and
@@ -772,6 +814,8 @@ def main():
         return lmgpu.tightbinding_hamiltonian(lat, pv, field=lmgpu.LandauGauge(B_FIELD * (1.0 + 0.1 * math.sin(t))))
 
     e2e_state = lmgpu.DeviceState(lat, None, 0, "c32", shape=(N, M))
+    if use_comp:
+        e2e_state.set_compensation(True)
     ev = lmgpu.Evolution(lmgpu.ChebyshevGPU(tol=args.tol32, renorm_every=20), h, e2e_state)
     evs = ev.current_states()[0]
     times = [DT * (k + 1) for k in range(args.steps)]
@@ -801,49 +845,33 @@ def main():
     d2h = N * 8 + nb * 8
     del e2e_state, ev, evs
 
-    # ---- error of the chosen form against FP64 over the configuration's full length -----
-    # an untimed pass: both forms from the same kets, err_steps steps of the same H and dt
-    s32e = lmgpu.KetBlock(lat, X, precision="c32")
-    s64e = lmgpu.KetBlock(lat, X, precision="c64")
-    sol32e = lmgpu.ChebyshevGPU(tol=args.tol32, renorm_every=20)
-    sol64e = lmgpu.ChebyshevGPU()
-    c32e = sol32e.evolution_cache(s32e)
-    sol32e.update_solver(H, DT)
-    sol64e.update_solver(H, DT)
-    for _ in range(args.err_steps):
-        sol32e.step(s32e, c32e)
-        sol64e.step(s64e)
-    r32 = lmgpu.localdensity(s32e).values
-    r64 = lmgpu.localdensity(s64e).values
-    J32 = lmgpu.DensityCurrents(H, s32e).bond_values()
-    J64 = lmgpu.DensityCurrents(H, s64e).bond_values()
-    err = {"density": float(np.linalg.norm(r32 - r64) / np.linalg.norm(r64)),
-           "currents": float(np.linalg.norm(J32 - J64) / np.linalg.norm(J64)),
-           "norm_drift": float(np.abs(s32e.norms() - 1.0).max()),
-           "norm_drift_fp64": float(np.abs(s64e.norms() - 1.0).max()),
-           "steps": args.err_steps, "kets": M}
-    del s32e, s64e
-
     # ---- report ----------------------------------------------------------------------
     if rank != 0:
         if dist is not None:
             dist.barrier()
             dist.destroy_process_group()
         return 0
+    ms32_plain = ms32
+    value_plain32 = world * M * args.steps / (ms32 / 1000.0)
+    value_comp = world * M * args.steps / (ms32c / 1000.0)
+    if use_comp:
+        ms32, order_ms, order_launches, launches32, streamed = ms32c, order_ms_c, order_launches_c, launches32c, streamed_c
     value = world * M * args.steps / (ms32 / 1000.0)
     plain = world * M * args.steps / (ms64 / 1000.0)
     # one launch of the temporally blocked kernel applies all K32 orders of a step; its
-    # algorithmic bytes are the per-ket-step figure 5*K*N*s times the M kets it advances
+    # algorithmic bytes are the per-ket-step figure 5*K*N*s times the M kets it advances, plus
+    # for the compensated form the residual plane read and written once (2 x 8 B per site-ket)
     s_bytes = 8
     sweeps = max(order_launches // max(K32, 1), 1)
-    alg_bytes_launch = 5.0 * K32 * N * M * s_bytes
+    alg_bytes_launch = 5.0 * K32 * N * M * s_bytes + (2.0 * N * M * s_bytes if use_comp else 0.0)
     avg_launch_ms = order_ms / sweeps
     achieved = alg_bytes_launch / (avg_launch_ms / 1000.0) / 1e9
     peak, peak_kind = measured_peak_hbm()
     traffic, traffic_src = None, None
     if streamed:
-        kname = f"cheb_stream_c32_kernel<{K32}, 3> (x-streaming form: all K orders of one step per launch)"
-        t_cap, units_cap, rec = profile_traffic()
+        kname = (f"cheb_stream_c32_kernel<{K32}, 3, {'true' if use_comp else 'false'}> (x-streaming form: all K "
+                 f"orders of one step per launch{', compensated state' if use_comp else ''})")
+        t_cap, units_cap, rec = profile_traffic(TRAFFIC_RECORD_COMP if use_comp else TRAFFIC_RECORD)
         if t_cap is not None and rec.get("K") == K32:
             traffic = t_cap * (N * M) / units_cap
             traffic_src = (f"ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch at {rec['sites']} sites x "
@@ -874,7 +902,15 @@ def main():
         "plain_fp64": {"value": plain, "unit": "ket-steps/s", "ms_per_step": ms64 / args.steps,
                        "dtype": "c64"},
         "chosen_over_plain": value / plain,
+        "chosen_form": ("c32 compensated (FP32 value + its rounding residual as a bfloat16 pair per site, "
+                        "error-free TwoProd/TwoSum on FP32 pairs in the x-streaming kernel)" if use_comp else "c32"),
         "rel_err_vs_fp64": err,
+        "fp32_forms": {
+            "plain_c32": {"value": value_plain32, "ms_per_step": ms32_plain / args.steps,
+                          "rel_err_vs_fp64": err_plain32},
+            "compensated_c32": {"value": value_comp, "ms_per_step": ms32c / args.steps,
+                                "rel_err_vs_fp64": err_comp, "streamed": streamed_c},
+        },
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic,
                      "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",

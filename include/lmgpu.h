@@ -156,6 +156,17 @@ int lm_state_norms(lm_state *st, double *out);
  * Stream-ordered: returns without waiting for the device; target_norms is copied during the
  * call. */
 int lm_state_renormalize(lm_state *st, const double *target_norms);
+/* Compensated ComplexF32 kets (enable != 0): the state keeps, beside each FP32 amplitude,
+ * the residual of its last rounding (a bfloat16 pair per site: 8 significant bits of the
+ * residual), and the fused Chebyshev step forms the new amplitude from the (value, residual)
+ * pair with error-free FP32 transformations (Dekker TwoProd via fmaf, Knuth TwoSum).  The
+ * state then carries about 32 significant bits from step to step, so the rounding walk of
+ * long FP32 runs (the 400-step current) shrinks, at the cost of 8 more bytes per site-ket of
+ * traffic (the residual read and written once per step).  ComplexF32 ket blocks on square lattices
+ * whose columns are uniform (Landau gauge, no twist along y) stepped by lm_solver_step
+ * only; other paths return LM_ERR_NOTSUP.  Uploads clear the residual; copies carry it;
+ * norms and renormalize use value + residual.  enable == 0 drops it. */
+int lm_state_set_compensation(lm_state *st, int enable);
 
 /* ---- evolution solver (the EvolutionSolver plugin, src/evolution.jl:5-33) ------------ */
 /* ChebyshevGPU(; tol): Chebyshev propagator exp(-i H dt) with truncation `tol`. */

@@ -648,7 +648,30 @@ int lm_state_destroy(lm_state* s) {
     if (s->d_a) cudaFree(s->d_a);
     if (s->d_y) cudaFree(s->d_y);
     if (s->d_w) cudaFree(s->d_w);
+    if (s->d_lo) cudaFree(s->d_lo);
     delete s;
+    return LM_OK;
+}
+
+int lm_state_set_compensation(lm_state* s, int enable) {
+    if (!s) return LM_ERR_ARG;
+    lm_ctx* ctx = s->ctx;
+    cudaSetDevice(ctx->device);
+    if (!enable) {
+        if (s->d_lo) {
+            cudaStreamSynchronize(ctx->stream);
+            cudaFree(s->d_lo);
+        }
+        s->d_lo = nullptr;
+        return LM_OK;
+    }
+    CHECK_ARG(ctx, s->kind == LM_KETS && s->precision == LM_C32,
+              "lm_state_set_compensation: applies to ComplexF32 ket blocks");
+    if (s->d_lo) return LM_OK;
+    const size_t bytes = sizeof(uint32_t) * (size_t)s->ld * (size_t)s->m;
+    int rc = dalloc(ctx, (void**)&s->d_lo, bytes, "compensation plane");
+    if (rc != LM_OK) return rc;
+    CUDA_TRY(ctx, cudaMemsetAsync(s->d_lo, 0, bytes, ctx->stream), "clear compensation plane");
     return LM_OK;
 }
 
@@ -661,6 +684,9 @@ int lm_state_upload(lm_state* s, const void* host, int64_t ld) {
     CUDA_TRY(ctx, cudaMemcpy2DAsync(s->d_data, s->elem * (size_t)s->ld, host, s->elem * (size_t)ld, s->elem * (size_t)s->n,
                                     (size_t)s->m, cudaMemcpyDefault, ctx->stream),
              "upload state");
+    if (s->d_lo)  // uploaded FP32 values are exact: no residual
+        CUDA_TRY(ctx, cudaMemsetAsync(s->d_lo, 0, sizeof(uint32_t) * (size_t)s->ld * (size_t)s->m, ctx->stream),
+                 "clear compensation plane");
     return LM_OK;
 }
 
@@ -687,6 +713,14 @@ int lm_state_copy(lm_state* dst, const lm_state* src) {
     CUDA_TRY(ctx, cudaMemcpy2DAsync(dst->d_data, dst->elem * (size_t)dst->ld, src->d_data, src->elem * (size_t)src->ld,
                                     dst->elem * (size_t)dst->n, (size_t)dst->m, cudaMemcpyDeviceToDevice, ctx->stream),
              "copy state");
+    if (dst->d_lo && src->d_lo)
+        CUDA_TRY(ctx, cudaMemcpy2DAsync(dst->d_lo, sizeof(uint32_t) * (size_t)dst->ld, src->d_lo,
+                                        sizeof(uint32_t) * (size_t)src->ld, sizeof(uint32_t) * (size_t)dst->n,
+                                        (size_t)dst->m, cudaMemcpyDeviceToDevice, ctx->stream),
+                 "copy compensation plane");
+    else if (dst->d_lo)
+        CUDA_TRY(ctx, cudaMemsetAsync(dst->d_lo, 0, sizeof(uint32_t) * (size_t)dst->ld * (size_t)dst->m, ctx->stream),
+                 "clear compensation plane");
     return LM_OK;
 }
 
@@ -728,7 +762,11 @@ int lm_state_norms(lm_state* s, double* out) {
     cudaSetDevice(ctx->device);
     int rc = ensure_red(ctx, (size_t)s->m);
     if (rc != LM_OK) return rc;
-    CUDA_TRY(ctx, launch_column_norms(ctx, s->precision, s->d_data, s->n, s->m, s->ld, ctx->d_red), "column norms");
+    if (s->d_lo)
+        CUDA_TRY(ctx, launch_column_norms_comp(ctx, (const float2*)s->d_data, s->d_lo, s->n, s->m, s->ld, ctx->d_red),
+                 "column norms");
+    else
+        CUDA_TRY(ctx, launch_column_norms(ctx, s->precision, s->d_data, s->n, s->m, s->ld, ctx->d_red), "column norms");
     CUDA_TRY(ctx, cudaMemcpyAsync(out, ctx->d_red, sizeof(double) * (size_t)s->m, cudaMemcpyDeviceToHost, ctx->stream), "download norms");
     CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream), "sync");
     return LM_OK;
@@ -748,6 +786,14 @@ int lm_state_renormalize(lm_state* s, const double* target) {
     CUDA_TRY(ctx, cudaMemcpyAsync(ctx->d_red + s->m, ctx->h_norms.data(), sizeof(double) * (size_t)s->m,
                                   cudaMemcpyHostToDevice, ctx->stream),
              "upload target norms");
+    if (s->d_lo) {
+        CUDA_TRY(ctx, launch_column_norms_comp(ctx, (const float2*)s->d_data, s->d_lo, s->n, s->m, s->ld, ctx->d_red),
+                 "column norms");
+        CUDA_TRY(ctx, launch_rescale_columns_comp(ctx, (float2*)s->d_data, s->d_lo, s->n, s->m, s->ld, ctx->d_red,
+                                                  ctx->d_red + s->m),
+                 "rescale columns");
+        return LM_OK;
+    }
     CUDA_TRY(ctx, launch_column_norms(ctx, s->precision, s->d_data, s->n, s->m, s->ld, ctx->d_red), "column norms");
     CUDA_TRY(ctx, launch_rescale_columns(ctx, s->precision, s->d_data, s->n, s->m, s->ld, ctx->d_red, ctx->d_red + s->m),
              "rescale columns");
@@ -891,7 +937,7 @@ int lm_solver_order(const lm_solver* s, int* K, double* a, double* b) {
 // buffers S (input T0), A, Y.  The result lands in S when K is even and in A when K is
 // odd; the return value says which (0 = S, 1 = A).
 static int cheb_apply(lm_solver* s, const Geom& g, int precision, int site_fast, int conj, void* S, void* A,
-                      void* Y, int64_t ld, int64_t m, int* where) {
+                      void* Y, int64_t ld, int64_t m, int* where, uint32_t* comp = nullptr) {
     lm_ctx* ctx = s->ctx;
     const void* hop2 = precision == LM_C64 ? (const void*)s->d_hop2 : (const void*)s->d_hop2f;
     const void* diag2 = precision == LM_C64 ? (const void*)s->d_diag2 : (const void*)s->d_diag2f;
@@ -919,8 +965,12 @@ static int cheb_apply(lm_solver* s, const Geom& g, int precision, int site_fast,
             if (rc != LM_OK) return rc;
             spack = s->d_spack;
         }
+        if (comp && !(spack && stream_comp_supported(g, K, mode)))
+            return set_err(ctx, LM_ERR_NOTSUP,
+                           "lm_solver_step: a compensated state needs the x-streaming form with uniform columns "
+                           "(Landau gauge, no twist along y)");
         CUDA_TRY(ctx, launch_cheb_fused_c32(ctx, g, (const float2*)hop2, (const float*)diag2, (const float2*)S,
-                                            (float2*)A, ld, m, K, xr, s->coef.data(), pr, pi, spack, mode),
+                                            (float2*)A, ld, m, K, xr, s->coef.data(), pr, pi, spack, mode, comp),
                  "fused chebyshev step");
         if (ctx->timing) {
             CUDA_TRY(ctx, cudaEventRecord(t1, ctx->stream), "cudaEventRecord");
@@ -930,6 +980,9 @@ static int cheb_apply(lm_solver* s, const Geom& g, int precision, int site_fast,
         *where = 1;
         return LM_OK;
     }
+    if (comp)
+        return set_err(ctx, LM_ERR_NOTSUP,
+                       "lm_solver_step: a compensated state needs the x-streaming form (fused step enabled)");
     const ChebLo lo = cheb_lo(pr, pi, c0, coef(1).s, false);
     const bool xr = ham_x_real(s->ham);
     CUDA_TRY(ctx, launch_cheb_order(ctx, g, precision, site_fast, conj, CHEB_FIRST, hop2, diag2, S, A, Y, ld, m, c0, coef(1), pr, pi, lo, xr),
@@ -970,7 +1023,7 @@ int lm_solver_step(lm_solver* s, lm_state* st) {
     }
     int where = 0;
     // psi <- U psi on the columns (kets, or the columns of P)
-    int rc = cheb_apply(s, g, st->precision, 1, 0, st->d_data, st->d_a, st->d_y, st->ld, st->m, &where);
+    int rc = cheb_apply(s, g, st->precision, 1, 0, st->d_data, st->d_a, st->d_y, st->ld, st->m, &where, st->d_lo);
     if (rc != LM_OK) return rc;
     if (where == 1) std::swap(st->d_data, st->d_a);
     if (st->kind == LM_DENSITY) {

@@ -700,6 +700,7 @@ int lm_batch_add(lm_batch* b, lm_ham* ham, lm_state* st, int* index) {
     if (st->kind != b->kind || st->precision != b->precision)
         return set_err(ctx, LM_ERR_ARG, "lm_batch_add: state kind/precision differ from the batch");
     if (st->n != ham->lat->g.N) return set_err(ctx, LM_ERR_ARG, "lm_batch_add: state size does not match the lattice");
+    if (st->d_lo) return set_err(ctx, LM_ERR_NOTSUP, "lm_batch_add: compensated states are stepped one by one");
     for (auto* s : b->states)
         if (s == st) return set_err(ctx, LM_ERR_ARG, "lm_batch_add: state already in the batch");
     lm_solver* s = nullptr;

@@ -228,6 +228,8 @@ static int ell_apply(lm_solver* s, int precision, int site_fast, int conj, void*
 int ell_solver_step(lm_solver* s, lm_state* st) {
     lm_ctx* ctx = s->ctx;
     CHECK_ARG(ctx, st->n == s->ell->n, "lm_solver_step: state size does not match the Hamiltonian");
+    if (st->d_lo)
+        return set_err(ctx, LM_ERR_NOTSUP, "lm_solver_step: compensated states run on square-lattice Hamiltonians only");
     cudaSetDevice(ctx->device);
     {
         int rc0 = ensure_scratch(st);

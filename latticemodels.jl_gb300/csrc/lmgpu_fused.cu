@@ -510,7 +510,7 @@ cudaError_t launch_fused_table(lm_ctx* ctx, int K, bool xreal, const FusedInst* 
 cudaError_t launch_cheb_fused_c32(lm_ctx* ctx, const Geom& g, const float2* hop2, const float* diag2,
                                   const float2* x, float2* out, int64_t ld, int64_t m, int K, bool xreal,
                                   const ChebCoef* coef, double ph_re, double ph_im, const float4* spack,
-                                  int stream_mode) {
+                                  int stream_mode, uint32_t* comp) {
     FusedInst d{};
     d.g = g;
     d.hop2 = hop2;
@@ -521,7 +521,9 @@ cudaError_t launch_cheb_fused_c32(lm_ctx* ctx, const Geom& g, const float2* hop2
     d.M = m;
     d.item_begin = 0;
     fused_fill_coef(d, K, coef, ph_re, ph_im);
+    d.comp = comp;
     if (spack) return launch_cheb_stream_c32(ctx, d, K, stream_mode, spack);
+    if (comp) return cudaErrorNotSupported;  // the compensation plane is carried by the streaming form only
     const int64_t nitems = fused_items(g, K, m, &d.ntx, &d.nty);
     return launch_fused_table(ctx, K, xreal, &d, nullptr, 1, nitems, nullptr, 0);
 }

@@ -82,6 +82,7 @@ struct FusedInst {
     float ph_re, ph_im;   // e^{-ib dt}
     float a0_re, a0_im;   // e^{-ib dt} c_0
     ChebLo lo;            // fused-form second words
+    uint32_t* comp;       // encoded residual plane of x, updated in place (x-streaming form only), or null
 };
 
 }  // namespace lmgpu
@@ -97,7 +98,8 @@ struct lm_ctx {
     int timing = 0;
     int fused = 1;                      // LM_OPT_FUSED: temporally blocked c32 step enabled
     unsigned fused_attr = 0;            // bit K (+16 for real x-hops): shared-memory attribute set
-    unsigned stream_attr = 0;           // the same for the x-streaming form (bit K, +8 for real x-hops)
+    unsigned stream_attr = 0;           // the same for the x-streaming form (bit K + 8 mode)
+    unsigned stream_attr_comp = 0;      // the same for its compensated-state variant
     int fused_form = 1;                 // LM_OPT_STREAM: 1 = x-streaming form where supported, 0 = region form
     int64_t stream_launches = 0;        // fused steps run in the x-streaming form
     int kpm_df = 1;                     // LM_OPT_KPM: double-float recurrence in lm_kpm_moments
@@ -150,6 +152,11 @@ struct lm_state {
     void* d_y = nullptr;      // accumulator scratch
     double* d_w = nullptr;    // ket weights (m) or null (= all ones)
     size_t elem = 16;
+    // compensated ComplexF32 ket block (lm_state_set_compensation): the rounding residual of
+    // every element as a bfloat16 pair (res_encode), so that the state carries about 32
+    // significant bits; element i of ket k at d_lo[k ld + i], updated in place by the
+    // x-streaming step (null when off)
+    uint32_t* d_lo = nullptr;
 };
 
 struct lm_solver {
@@ -259,6 +266,37 @@ cudaError_t launch_column_norms(lm_ctx* ctx, int precision, const void* x, int64
                                 int64_t ld, double* out);
 cudaError_t launch_rescale_columns(lm_ctx* ctx, int precision, void* x, int64_t n, int64_t m,
                                    int64_t ld, const double* norms, const double* target);
+// The same for a compensated ComplexF32 block: norms of hi + lo, and hi + lo rescaled and split
+// again into hi and its encoded residual, both in FP32-pair arithmetic (no FP64 per element).
+cudaError_t launch_column_norms_comp(lm_ctx* ctx, const float2* hi, const uint32_t* lo, int64_t n, int64_t m,
+                                     int64_t ld, double* out);
+cudaError_t launch_rescale_columns_comp(lm_ctx* ctx, float2* hi, uint32_t* lo, int64_t n, int64_t m, int64_t ld,
+                                        const double* norms, const double* target);
+
+// Error-free transformations (round to nearest): p + e = a b exactly; s + e = a + b exactly.
+__device__ __forceinline__ void two_prod(float a, float b, float& p, float& e) {
+    p = a * b;
+    e = fmaf(a, b, -p);
+}
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+    const float r = a + b;
+    const float bb = r - a;
+    e = (a - (r - bb)) + (b - bb);
+    s = r;
+}
+
+// Residual encoding of a compensated ComplexF32 amplitude (value hi + lo per real component,
+// |lo| <= ulp(hi)/2): the residual pair rounded to bfloat16 (8 significant bits, the FP32
+// exponent range), lo.x in bits 15..0 and lo.y in bits 31..16 of one word per site.  The
+// stored residual is within 2^-9 |lo| <= 2^-10 ulp(hi) of the exact one, one conversion
+// encodes a site and two bit operations decode it.
+__device__ __forceinline__ unsigned res_encode(float lx, float ly) {
+    unsigned w;
+    asm("cvt.rn.bf16x2.f32 %0, %1, %2;" : "=r"(w) : "f"(ly), "f"(lx));
+    return w;
+}
+__device__ __forceinline__ float res_lo_x(unsigned w) { return __uint_as_float(w << 16); }
+__device__ __forceinline__ float res_lo_y(unsigned w) { return __uint_as_float(w & 0xFFFF0000u); }
 cudaError_t launch_sum(lm_ctx* ctx, const double* v, int64_t n, double* out1);
 int fused_supported(int precision, int K);
 int fused_supported_geom(const Geom& g);
@@ -277,7 +315,10 @@ cudaError_t launch_cheb_stream_c32(lm_ctx* ctx, const FusedInst& d, int K, int m
 cudaError_t launch_cheb_fused_c32(lm_ctx* ctx, const Geom& g, const float2* hop2, const float* diag2,
                                   const float2* x, float2* out, int64_t ld, int64_t m, int K, bool xreal,
                                   const ChebCoef* coef, double ph_re, double ph_im, const float4* spack = nullptr,
-                                  int stream_mode = 0);
+                                  int stream_mode = 0, uint32_t* comp = nullptr);
+// Whether the x-streaming step can carry a compensation plane for this geometry and order
+// (the uniform-column modes, whose shared memory leaves room for it).
+bool stream_comp_supported(const Geom& g, int K, int mode);
 // Every x-hop of H is real: Landau-gauge field components only (or none) and no twist across
 // a periodic x axis.  The fused kernel then skips the imaginary parts of the x-hops.
 bool ham_x_real(const lm_ham* h);

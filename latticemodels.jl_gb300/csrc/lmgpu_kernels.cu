@@ -726,6 +726,96 @@ cudaError_t launch_rescale_columns(lm_ctx* ctx, int precision, void* x, int64_t 
     return cudaGetLastError();
 }
 
+// Norms of hi + lo (compensated ComplexF32 columns).  Each thread sums |hi + lo|^2 =
+// hi^2 + (the rounding error of hi^2) + 2 hi lo over its elements as an FP32 pair (TwoProd and
+// TwoSum), which keeps about 44 bits without an FP64 operation per element (GB300's FP64 and
+// FP32<->FP64 conversion rates are a small fraction of its FP32 rate); the threads' pairs are
+// then summed in FP64 in a fixed order.
+__global__ void __launch_bounds__(512) column_norms_comp_kernel(const float2* __restrict__ hi,
+                                                                const uint32_t* __restrict__ lo, int64_t n,
+                                                                int64_t ld, double* __restrict__ out) {
+    __shared__ double red[16];
+    const int64_t k = blockIdx.x;
+    float S = 0.0f, C = 0.0f;
+    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+        const float2 a = hi[k * ld + i];
+        const unsigned code = lo[k * ld + i];
+        const float lx = res_lo_x(code), ly = res_lo_y(code);
+        float px, ex, py, ey, t;
+        two_prod(a.x, a.x, px, ex);
+        two_prod(a.y, a.y, py, ey);
+        const float e = (ex + ey) + 2.0f * fmaf(a.x, lx, a.y * ly);
+        two_sum(S, px, S, t);
+        C += t;
+        two_sum(S, py, S, t);
+        C += t + e;
+    }
+    double t = (double)S + (double)C;
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = t;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        t = (threadIdx.x < (blockDim.x >> 5)) ? red[threadIdx.x] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+        if (threadIdx.x == 0) out[k] = sqrt(t);
+    }
+}
+
+cudaError_t launch_column_norms_comp(lm_ctx* ctx, const float2* hi, const uint32_t* lo, int64_t n, int64_t m,
+                                     int64_t ld, double* out) {
+    if (m <= 0) return cudaSuccess;
+    column_norms_comp_kernel<<<(unsigned)m, 512, 0, ctx->stream>>>(hi, lo, n, ld, out);
+    ctx->launches++;
+    return cudaGetLastError();
+}
+
+// (hi + lo)[:, k] *= f = target[k] / norms[k]: f as an FP32 pair (fh + fl, formed once per block
+// and column), the product hi fh exact by TwoProd, the small terms hi fl + lo fh added to its
+// error, and the sum split again into hi and its encoded residual.
+__global__ void __launch_bounds__(256) rescale_columns_comp_kernel(float2* hi, uint32_t* lo, int64_t n, int64_t m,
+                                                                   int64_t ld, const double* __restrict__ norms,
+                                                                   const double* __restrict__ target) {
+    __shared__ float2 fs;
+    for (int64_t k = blockIdx.y; k < m; k += gridDim.y) {
+        __syncthreads();  // the previous column's factor has been read
+        if (threadIdx.x == 0) {
+            const double nk = norms[k];
+            const double f = nk > 0.0 ? target[k] / nk : 1.0;
+            const float fh = (float)f;
+            fs = make_float2(fh, (float)(f - (double)fh));
+        }
+        __syncthreads();
+        const float fh = fs.x, fl = fs.y;
+        for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+            const float2 a = hi[k * ld + i];
+            const unsigned code = lo[k * ld + i];
+            const float l[2] = {res_lo_x(code), res_lo_y(code)};
+            const float h[2] = {a.x, a.y};
+            float o[2], r[2];
+#pragma unroll
+            for (int c = 0; c < 2; ++c) {
+                float p, e;
+                two_prod(h[c], fh, p, e);
+                e = fmaf(h[c], fl, fmaf(l[c], fh, e));
+                o[c] = p + e;
+                r[c] = e - (o[c] - p);
+            }
+            hi[k * ld + i] = make_float2(o[0], o[1]);
+            lo[k * ld + i] = res_encode(r[0], r[1]);
+        }
+    }
+}
+
+cudaError_t launch_rescale_columns_comp(lm_ctx* ctx, float2* hi, uint32_t* lo, int64_t n, int64_t m, int64_t ld,
+                                        const double* norms, const double* target) {
+    if (m <= 0) return cudaSuccess;
+    const int64_t bx = std::min<int64_t>((n + 255) / 256, 1024);
+    const dim3 grid((unsigned)bx, (unsigned)(m < 65535 ? m : 65535));
+    rescale_columns_comp_kernel<<<grid, 256, 0, ctx->stream>>>(hi, lo, n, m, ld, norms, target);
+    ctx->launches++;
+    return cudaGetLastError();
+}
+
 // Single-block FP64 sum (deterministic order).
 __global__ void sum_kernel(const double* __restrict__ v, int64_t n, double* __restrict__ out) {
     __shared__ double red[32];

@@ -82,6 +82,10 @@ constexpr int kStreamSmemMax = 232448;  // bytes of shared memory a CTA may use
 // Column records per lattice column in shared memory: MODE 2 keeps {hx, hxm, hy.re, hy.im};
 // MODE 3 keeps the pair forms {hx, hx, hxm, hxm}, {hy.re, hy.re, hy.im, 0} and their negatives.
 __host__ __device__ constexpr int stream_crec_f4(int mode) { return mode == 3 ? 4 : 1; }
+// Compensated blocks: a per-warp ring of the residual words (two per lane: its two sites) of
+// the columns that the next SPF + 1 steps complete, staged with the ket columns.
+constexpr int kResRing = SPF + 1;
+static_assert(kResRing == 4, "the residual ring is indexed with & 3");
 }  // namespace
 
 // Accumulator coefficients of the paired form (MODE 3): {sigma_k s_k, sigma_k s_k}.
@@ -115,6 +119,40 @@ __device__ __forceinline__ float2 ffma2(float2 a, float2 b, float2 c) {
 }
 template <int N>
 __device__ __forceinline__ void cp_async_wait_s() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+// Packed FP32 pairs: one instruction each for both halves, the same rounding as the scalar
+// operation on each half.
+#define LM_F32X2_BINOP(NAME, OP)                                                                     \
+    __device__ __forceinline__ float2 NAME(float2 a, float2 b) {                                     \
+        float2 d;                                                                                    \
+        asm("{\n\t.reg .b64 ra, rb, rd;\n\t"                                                          \
+            "mov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\t" OP                                   \
+            " rd, ra, rb;\n\tmov.b64 {%0, %1}, rd;\n\t}"                                               \
+            : "=f"(d.x), "=f"(d.y)                                                                   \
+            : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));                                               \
+        return d;                                                                                    \
+    }
+LM_F32X2_BINOP(fadd2, "add.rn.f32x2")
+LM_F32X2_BINOP(fsub2, "sub.rn.f32x2")
+LM_F32X2_BINOP(fmul2, "mul.rn.f32x2")
+#undef LM_F32X2_BINOP
+
+// (hi + lo) = a1 x1 + a2 x2 + r + a1 l on both components of a compensated output at once:
+// a1 x1 (the dominant term for the workloads' small spectral centres: a1 + i a2 = e^{-ib dt} c_0)
+// exact by TwoProd (a1n = -a1 gives its error negated), its sum with q = a2 x2 + r by TwoSum,
+// the decoded residual l and both errors in FP32, and the final FastTwoSum split.
+__device__ __forceinline__ void comp_sum2(float2 a1, float2 a1n, float2 x1, float2 a2, float2 x2, float2 r, float2 l,
+                                          float2& hi, float2& lo) {
+    const float2 p = fmul2(a1, x1);
+    const float2 en = ffma2(a1n, x1, p);  // -(a1 x1 - p)
+    const float2 q = ffma2(a2, x2, r);
+    const float2 s = fadd2(p, q);
+    const float2 bb = fsub2(s, p);
+    const float2 f = fadd2(fsub2(p, fsub2(s, bb)), fsub2(q, bb));
+    const float2 t = ffma2(a1, l, fsub2(f, en));
+    hi = fadd2(s, t);
+    lo = fsub2(t, fsub2(hi, s));
+}
 
 __device__ __forceinline__ int wrap_axis_i(int64_t c, int64_t L, int per) {
     if (c >= 0 && c < L) return (int)c;
@@ -209,7 +247,12 @@ __global__ void stream_pack_kernel(const Geom g, const float2* __restrict__ hop2
 // real x-hops and every hop of a column equal (the Landau gauge without a twist along y), so an
 // order reads the diagonal pair of its sites and one column record shared by the warp; 3: the
 // same on a periodic y axis (no edge rows).
-template <int K, int MODE>
+// CMP: the ket block carries a residual plane D.comp (a bfloat16 pair per site, res_encode),
+// staged with the ket columns: the output a0 (x + x_lo) + e^{-ib dt} y is formed with
+// error-free products and sums (comp_sum2) and written as hi (the block) and its encoded
+// residual (the plane, in place), so the state's own FP32 rounding does not accumulate from
+// step to step.
+template <int K, int MODE, bool CMP>
 __global__ void __launch_bounds__(SW * 32, 1)
 cheb_stream_c32_kernel(const FusedInst D, const StreamPairs SP, const float4* __restrict__ pk,
                        const float2* __restrict__ pd, const float4* __restrict__ pc, int npair, long long plane,
@@ -246,6 +289,8 @@ cheb_stream_c32_kernel(const FusedInst D, const StreamPairs SP, const float4* __
     // uniform columns: diagonal-pair ring per warp, column records per CTA
     float2* dring = reinterpret_cast<float2*>(smem + SW * stream_ring_f4(K)) + warp * XS * 32;
     float4* ctab = smem + SW * (stream_ring_f4(K) + stream_dring_f4(K));
+    uint2* rring = reinterpret_cast<uint2*>(ctab + ((int)D.g.Lx + kPadL + kPadR) * stream_crec_f4(MODE)) +
+                   warp * kResRing * 32;
     if (UC) {
         const int Xp = Lx + kPadL + kPadR;
         for (int i = threadIdx.x; i < Xp; i += SW * 32) {
@@ -295,6 +340,8 @@ cheb_stream_c32_kernel(const FusedInst D, const StreamPairs SP, const float4* __
         const float2* xk = D.x + ket * D.ld;
         float2* outk = D.out + ket * D.ld;
 
+        // residual words of my site pair in the ket's columns (output columns lie in [xa, xb))
+        uint32_t* const rbase = CMP ? D.comp + ket * D.ld + (ys >= 0 ? ys : 0) : nullptr;
         auto column = [&](int x) -> int {  // lattice column of x, or -1 outside an open axis
             if (per_x) return x < 0 ? x + Lx : (x >= Lx ? x - Lx : x);
             return (x >= 0 && x < Lx) ? x : -1;
@@ -309,6 +356,12 @@ cheb_stream_c32_kernel(const FusedInst D, const StreamPairs SP, const float4* __
                 const bool vd = idx < nsteps;
                 cp_async8s(&dring[stage_slot * 32 + lane], vd ? pd + loff + (long long)(s0 + idx + kPadL) * lstep : pd,
                            vd);
+            }
+            if (CMP) {  // the residual words of the column that step idx completes (xo < xb: idx < nsteps)
+                const int xo = s0 + idx - K;
+                const bool vr = wr && xo >= xa && xo < xb;
+                cp_async8s(reinterpret_cast<float2*>(&rring[(idx & 3) * 32 + lane]),
+                           vr ? rbase + (long long)xo * Ly : D.comp, vr);
             }
             cp_async_commit_s();
             stage_slot = stage_slot + 1 == XS ? 0 : stage_slot + 1;
@@ -547,15 +600,37 @@ cheb_stream_c32_kernel(const FusedInst D, const StreamPairs SP, const float4* __
                         const float2 x0[2] = {make_float2(q.x, q.y), make_float2(q.z, q.w)};
                         const float ph_re = D.ph_re, ph_im = D.ph_im, a0_re = D.a0_re, a0_im = D.a0_im;
                         float2 o[2];
+                        if (CMP) {
+                            // the two sites' residuals, staged with the ket columns
+                            uint2* lp = reinterpret_cast<uint2*>(rbase + (long long)x * Ly);
+                            const uint2 lq = rring[(idx & 3) * 32 + lane];
+                            const float2 a1 = make_float2(a0_re, a0_re), a1n = make_float2(-a0_re, -a0_re);
+                            const float2 a2 = make_float2(-a0_im, a0_im);
+                            unsigned enc[2];
 #pragma unroll
-                        for (int j = 0; j < 2; ++j) {
-                            float2 r;
-                            r.x = fmaf(ph_re, yv[j].x, -ph_im * yv[j].y);
-                            r.y = fmaf(ph_re, yv[j].y, ph_im * yv[j].x);
-                            r.x = fmaf(-a0_im, x0[j].y, r.x);
-                            r.y = fmaf(a0_im, x0[j].x, r.y);
-                            o[j].x = fmaf(a0_re, x0[j].x, r.x);
-                            o[j].y = fmaf(a0_re, x0[j].y, r.y);
+                            for (int j = 0; j < 2; ++j) {
+                                const unsigned lw = j == 0 ? lq.x : lq.y;
+                                const float lx = res_lo_x(lw), ly = res_lo_y(lw);
+                                // the series and a0 l's cross term go with the small terms
+                                const float rx = fmaf(-a0_im, ly, fmaf(ph_re, yv[j].x, -ph_im * yv[j].y));
+                                const float ry = fmaf(a0_im, lx, fmaf(ph_re, yv[j].y, ph_im * yv[j].x));
+                                float2 ol;
+                                comp_sum2(a1, a1n, x0[j], a2, make_float2(x0[j].y, x0[j].x), make_float2(rx, ry),
+                                          make_float2(lx, ly), o[j], ol);
+                                enc[j] = res_encode(ol.x, ol.y);
+                            }
+                            *lp = make_uint2(enc[0], enc[1]);
+                        } else {
+#pragma unroll
+                            for (int j = 0; j < 2; ++j) {
+                                float2 r;
+                                r.x = fmaf(ph_re, yv[j].x, -ph_im * yv[j].y);
+                                r.y = fmaf(ph_re, yv[j].y, ph_im * yv[j].x);
+                                r.x = fmaf(-a0_im, x0[j].y, r.x);
+                                r.y = fmaf(a0_im, x0[j].x, r.y);
+                                o[j].x = fmaf(a0_re, x0[j].x, r.x);
+                                o[j].y = fmaf(a0_re, x0[j].y, r.y);
+                            }
                         }
                         *reinterpret_cast<float4*>(outk + (long long)xs * Ly + ys) = make_float4(o[0].x, o[0].y, o[1].x, o[1].y);
                     }
@@ -643,11 +718,17 @@ int ensure_stream_pack(lm_solver* s, const Geom& g) {
     return LM_OK;
 }
 
-static int stream_smem_bytes(int K, int mode, int Xp) {
-    return SW * stream_ring_f4(K) * 16 + (mode >= 2 ? SW * stream_dring_f4(K) * 16 + Xp * 16 * stream_crec_f4(mode) : 0);
+static int stream_smem_bytes(int K, int mode, int Xp, bool cmp = false) {
+    return SW * stream_ring_f4(K) * 16 + (mode >= 2 ? SW * stream_dring_f4(K) * 16 + Xp * 16 * stream_crec_f4(mode) : 0) +
+           (cmp ? SW * kResRing * 32 * 8 : 0);
 }
 
-template <int MODE>
+bool stream_comp_supported(const Geom& g, int K, int mode) {
+    const int m = (mode == 2 && g.per_y) ? 3 : mode;
+    return m >= 2 && stream_smem_bytes(K, m, (int)g.Lx + kPadL + kPadR, true) <= kStreamSmemMax;
+}
+
+template <int MODE, bool CMP>
 static cudaError_t launch_stream_k(lm_ctx* ctx, int K, int grid, const FusedInst& d, const StreamPairs& sp,
                                    const float4* spack, int nty, long long ncols, long long nwarps) {
     int npair, Xp;
@@ -655,17 +736,18 @@ static cudaError_t launch_stream_k(lm_ctx* ctx, int K, int grid, const FusedInst
     pack_dims(d.g, &npair, &Xp, &plane);
     const PackPtrs pp = pack_ptrs(const_cast<float4*>(spack), d.g);
     const unsigned bit = 1u << (K + 8 * MODE);
+    unsigned& attr = CMP ? ctx->stream_attr_comp : ctx->stream_attr;
     switch (K) {
 #define LM_STREAM_CASE(KK)                                                                                       \
     case KK: {                                                                                                   \
-        const int smem = stream_smem_bytes(KK, MODE, Xp);                                                        \
-        if (!(ctx->stream_attr & bit)) {                                                                         \
-            cudaError_t e = cudaFuncSetAttribute(cheb_stream_c32_kernel<KK, MODE>,                               \
+        const int smem = stream_smem_bytes(KK, MODE, Xp, CMP);                                                   \
+        if (!(attr & bit)) {                                                                                     \
+            cudaError_t e = cudaFuncSetAttribute(cheb_stream_c32_kernel<KK, MODE, CMP>,                          \
                                                  cudaFuncAttributeMaxDynamicSharedMemorySize, kStreamSmemMax);   \
             if (e != cudaSuccess) return e;                                                                      \
-            ctx->stream_attr |= bit;                                                                             \
+            attr |= bit;                                                                                         \
         }                                                                                                        \
-        cheb_stream_c32_kernel<KK, MODE><<<(unsigned)grid, SW * 32, smem, ctx->stream>>>(                       \
+        cheb_stream_c32_kernel<KK, MODE, CMP><<<(unsigned)grid, SW * 32, smem, ctx->stream>>>(                  \
             d, sp, pp.pk, pp.pd, pp.pc, npair, plane, nty, ncols, nwarps);                                           \
         return cudaGetLastError();                                                                               \
     }
@@ -693,10 +775,17 @@ cudaError_t launch_cheb_stream_c32(lm_ctx* ctx, const FusedInst& d, int K, int m
         const float v = k <= K ? ((k & 2) ? -d.s[k] : d.s[k]) : 0.f;  // sigma_k s_k
         sp.s2[k] = make_float2(v, v);
     }
-    const cudaError_t e = m == 3   ? launch_stream_k<3>(ctx, K, grid, d, sp, spack, (int)nty, ncols, nwarps)
-                          : m == 2 ? launch_stream_k<2>(ctx, K, grid, d, sp, spack, (int)nty, ncols, nwarps)
-                          : m == 1 ? launch_stream_k<1>(ctx, K, grid, d, sp, spack, (int)nty, ncols, nwarps)
-                                   : launch_stream_k<0>(ctx, K, grid, d, sp, spack, (int)nty, ncols, nwarps);
+    cudaError_t e;
+    if (d.comp) {  // compensated block: the uniform-column modes only (checked by the caller)
+        if (m < 2) return cudaErrorNotSupported;
+        e = m == 3 ? launch_stream_k<3, true>(ctx, K, grid, d, sp, spack, (int)nty, ncols, nwarps)
+                   : launch_stream_k<2, true>(ctx, K, grid, d, sp, spack, (int)nty, ncols, nwarps);
+    } else {
+        e = m == 3   ? launch_stream_k<3, false>(ctx, K, grid, d, sp, spack, (int)nty, ncols, nwarps)
+            : m == 2 ? launch_stream_k<2, false>(ctx, K, grid, d, sp, spack, (int)nty, ncols, nwarps)
+            : m == 1 ? launch_stream_k<1, false>(ctx, K, grid, d, sp, spack, (int)nty, ncols, nwarps)
+                     : launch_stream_k<0, false>(ctx, K, grid, d, sp, spack, (int)nty, ncols, nwarps);
+    }
     ctx->launches++;
     ctx->stream_launches++;
     return e;

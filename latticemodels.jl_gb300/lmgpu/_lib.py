@@ -76,6 +76,7 @@ SIGNATURES = {
     "lm_state_set_weights": (_INT, [_P, _PD]),
     "lm_state_norms": (_INT, [_P, _PD]),
     "lm_state_renormalize": (_INT, [_P, _PD]),
+    "lm_state_set_compensation": (_INT, [_P, _INT]),
     "lm_solver_create": (_INT, [_P, _D, C.POINTER(_P)]),
     "lm_solver_destroy": (_INT, [_P]),
     "lm_solver_update": (_INT, [_P, _P, _D, _INT]),

@@ -49,8 +49,19 @@ class DeviceState:
         if arr is not None:
             self.upload(arr)
         self.weights = None
+        self.compensated = False
         if weights is not None:
             self.set_weights(weights)
+
+    def set_compensation(self, enable: bool = True):
+        """Keep the FP32 rounding residual of every amplitude beside it (ComplexF32 kets on
+        square lattices with uniform columns): the fused step then adds each Chebyshev order
+        to the (value, residual) pair with error-free transformations, so a long FP32 run
+        accumulates far less rounding.  Norms and renormalize read value + residual; the
+        readouts and to_numpy read the FP32 value."""
+        self.ctx.check(self.ctx.lib.lm_state_set_compensation(self.handle, int(bool(enable))))
+        self.compensated = bool(enable)
+        return self
 
     @property
     def dtype(self):
@@ -116,6 +127,8 @@ class DeviceState:
         c = object.__new__(type(self))
         DeviceState.__init__(c, self.lattice, None, self.kind, self.precision, self.weights, self.ctx,
                              shape=(self.n, self.m))
+        if self.compensated:
+            c.set_compensation(True)
         self.ctx.check(self.ctx.lib.lm_state_copy(c.handle, self.handle))
         return c
 
@@ -134,8 +147,10 @@ class Ket(DeviceState):
 class KetBlock(DeviceState):
     """N x M block of kets (column m = ket m), optional weights w_m."""
 
-    def __init__(self, lattice, data, weights=None, precision="c64", ctx=None):
+    def __init__(self, lattice, data, weights=None, precision="c64", ctx=None, compensated=False):
         super().__init__(lattice, data, _lib.LM_KETS, precision, weights, ctx)
+        if compensated:
+            self.set_compensation(True)
 
 
 

@@ -1,0 +1,164 @@
+"""Compensated ComplexF32 kets (lm_state_set_compensation): the x-streaming Chebyshev step
+keeps each amplitude as an FP32 value plus the residual of its rounding, stored as a bfloat16
+pair (8 significant bits of the residual, about 32 of the amplitude).
+
+Bars: against the oracle's exact exponent (scipy expm_multiply on its own restatement of the
+Hamiltonian, src/evolution.jl:69-80 applied step by step) the compensated block stays within
+the FP32 form's bar; over the plain-method length (400 steps of dt = 0.05 on the periodic
+256 x 256 Landau lattice) its local densities and bond currents stay within 1e-6 of the FP64
+run of the same kets, and its error is below the plain FP32 form's.  Paths that cannot carry
+the residual refuse a compensated state with LM_ERR_NOTSUP instead of dropping it.
+"""
+import numpy as np
+import pytest
+
+from oracle import lm_oracle as o
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def lm():
+    import lmgpu
+    lmgpu.default_context()
+    return lmgpu
+
+
+def rel(a, b):
+    return float(np.linalg.norm(np.asarray(a) - np.asarray(b)) / np.linalg.norm(np.asarray(b)))
+
+
+def pair(lm, Lx, Ly, per):
+    ol = o.SquareLattice(Lx, Ly, periodic=per)
+    b = {name: True for ax, name in enumerate(("axis1", "axis2")) if per[ax]}
+    return ol, lm.SquareLattice(Lx, Ly, boundaries=b)
+
+
+CASES = [
+    (32, 32, True, True, 0.05, 4),
+    (40, 18, True, False, 0.02, 3),    # open y: uniform columns without the y seam
+    (17, 64, False, True, 0.05, 5),    # open x
+]
+
+
+@pytest.mark.parametrize("case", CASES, ids=[f"{c[0]}x{c[1]}" for c in CASES])
+def test_compensated_step_vs_oracle(lm, case):
+    Lx, Ly, px, py, dt, M = case
+    ol, ll = pair(lm, Lx, Ly, (px, py))
+    V = o.anderson_disorder(ol.N, 2.0, Lx + Ly)
+    Ho = o.tightbinding_hamiltonian(ol, field=o.LandauGauge(0.02), onsite=V)
+    Hl = lm.tightbinding_hamiltonian(ll, V, field=lm.LandauGauge(0.02))
+    X = o.random_kets(ol.N, M, 5)
+    ctx = lm.default_context()
+    out = {}
+    for comp in (False, True):
+        st = lm.KetBlock(ll, X, precision="c32", compensated=comp)
+        s = lm.ChebyshevGPU()
+        s.update_solver(Hl, dt)
+        n0 = ctx.stream_launches()
+        for _ in range(4):
+            s.step(st)
+        assert ctx.stream_launches() - n0 == 4
+        out[comp] = st
+    Y = X
+    for _ in range(4):
+        Y = o.expm_multiply(Ho, dt, Y)
+    e_plain = rel(out[False].to_numpy().astype(np.complex128), Y)
+    e_comp = rel(out[True].to_numpy().astype(np.complex128), Y)
+    assert e_comp <= 3e-6, e_comp
+    assert e_plain <= 3e-6, e_plain
+    # the FP64 norms of value + residual hold the unitary evolution's norms closer than FP32
+    assert np.abs(out[True].norms() - np.linalg.norm(X, axis=0)).max() <= 1e-7
+
+
+def test_compensated_copy_upload_renormalize(lm):
+    """A copy carries the residual (the copy steps exactly like the original); an upload
+    clears it (stepping after a re-upload repeats the first step bit for bit); renormalize
+    reaches the target norms on value + residual."""
+    ol, ll = pair(lm, 24, 16, (True, True))
+    V = o.anderson_disorder(ol.N, 2.0, 9)
+    Hl = lm.tightbinding_hamiltonian(ll, V, field=lm.LandauGauge(0.03))
+    X = o.random_kets(ol.N, 3, 10)
+    s = lm.ChebyshevGPU()
+    s.update_solver(Hl, 0.05)
+    a = lm.KetBlock(ll, X, precision="c32", compensated=True)
+    s.step(a)
+    first = a.to_numpy()
+    s.step(a)
+    b = a.copy()
+    assert b.compensated
+    s.step(a)
+    s.step(b)
+    assert np.array_equal(a.to_numpy(), b.to_numpy())
+    a.upload(X)
+    s.step(a)
+    assert np.array_equal(a.to_numpy(), first)
+    a.renormalize(np.full(3, 2.0))
+    assert np.abs(a.norms() - 2.0).max() <= 1e-10  # the residual keeps ~9 bits below the FP32 ulp
+    a.set_compensation(False)
+    assert not a.compensated
+    s.step(a)  # the plain form again
+
+
+def test_compensated_refusals(lm):
+    from lmgpu import _lib as L
+    ctx = lm.default_context()
+    ol, ll = pair(lm, 24, 24, (True, True))
+    V = o.anderson_disorder(ol.N, 1.0, 3)
+    X = o.random_kets(ol.N, 2, 4)
+    # non-uniform columns (PointFlux): the streaming kernel has no compensated form
+    Hp = lm.tightbinding_hamiltonian(ll, V, field=lm.PointFlux(0.2, (12.5, 12.5)))
+    st = lm.KetBlock(ll, X, precision="c32", compensated=True)
+    s = lm.ChebyshevGPU()
+    s.update_solver(Hp, 0.05)
+    with pytest.raises(L.LMError) as e:
+        s.step(st)
+    assert e.value.code == L.LM_ERR_NOTSUP
+    # ComplexF64 kets and density matrices have no residual plane
+    with pytest.raises(L.LMError):
+        lm.KetBlock(ll, X, precision="c64", compensated=True)
+    # with the fused step switched off the per-order path refuses it
+    Hl = lm.tightbinding_hamiltonian(ll, V, field=lm.LandauGauge(0.02))
+    s.update_solver(Hl, 0.05)
+    ctx.set_fused(False)
+    try:
+        with pytest.raises(L.LMError) as e:
+            s.step(st)
+        assert e.value.code == L.LM_ERR_NOTSUP
+    finally:
+        ctx.set_fused(True)
+    s.step(st)
+
+
+def test_compensated_plain_config_400_steps(lm):
+    """The plain-method lattice at its full length: SquareLattice(256, 256) periodic, Landau
+    0.01, Anderson U[-1, 1], 64 complex-Gaussian kets, 400 steps of dt = 0.05 at tol 1e-9 with
+    the norm correction every 20 steps, against the FP64 run of the same kets."""
+    L, M, steps, dt = 256, 64, 400, 0.05
+    lat = lm.SquareLattice(L, L, boundaries={"axis1": True, "axis2": True})
+    V = np.random.default_rng(1).uniform(-1, 1, size=lat.N)
+    H = lm.tightbinding_hamiltonian(lat, V, field=lm.LandauGauge(0.01))
+    X = o.random_kets(lat.N, M, 2)
+
+    def run(st, tol):
+        solver = lm.ChebyshevGPU(tol=tol, renorm_every=20)
+        cache = solver.evolution_cache(st)
+        solver.update_solver(H, dt)
+        for _ in range(steps):
+            solver.step(st, cache)
+        return st
+
+    s64 = run(lm.KetBlock(lat, X, precision="c64"), None)
+    r64 = lm.localdensity(s64).values
+    J64 = lm.DensityCurrents(H, s64).bond_values()
+    del s64
+    errs = {}
+    for comp in (False, True):
+        st = run(lm.KetBlock(lat, X, precision="c32", compensated=comp), 1e-9)
+        errs[comp] = {"density": rel(lm.localdensity(st).values, r64),
+                      "currents": rel(lm.DensityCurrents(H, st).bond_values(), J64)}
+        del st
+    print("400 steps, 256^2, 64 kets: plain", errs[False], "compensated", errs[True])
+    assert errs[True]["density"] <= 1e-6, errs
+    assert errs[True]["currents"] <= 1e-6, errs
+    assert errs[True]["currents"] < errs[False]["currents"], errs

@@ -120,6 +120,35 @@ def test_fermi_operator_densitymatrix(lm, mu, T, precision):
     assert abs(P.trace() - np.trace(Pref).real) <= (1e-10 if precision == "c64" else 1e-5) * np.trace(Pref).real
 
 
+def test_fermi_operator_low_temperature_doublefloat(lm):
+    """T = 0.005 on the 12 x 12 PointFlux lattice: the Fermi function's Chebyshev series runs to
+    about ten thousand terms, so the recurrence's rounding has the longest run to build up.  The
+    double-float recurrence (LM_OPT_KPM = 1, about 48 significant bits) against the FP64 one
+    (LM_OPT_KPM = 0) and both against the oracle's eigensystem projector
+    (src/spectrum.jl:226-257) at the FP64 route's 1e-11 bar."""
+    from lmgpu.spectrum import chebyshev_coefficients, fermi_occupation
+    ol, Ho, Hl = case(lm, 12, False, "pf")
+    mu, T = 0.1, 0.005
+    ctx = lm.default_context()
+    lo, hi = Hl.bounds(ctx)
+    pad = 1e-3 * (hi - lo)
+    K = len(chebyshev_coefficients(fermi_occupation(mu, T), (lo - pad, hi + pad), 1e-13))
+    Pref, _, _ = o.densitymatrix(Ho, mu=mu, T=T)
+    try:
+        ctx.set_kpm_doublefloat(False)
+        P64 = lm.densitymatrix(Hl, mu=mu, T=T).to_numpy()
+    finally:
+        ctx.set_kpm_doublefloat(True)
+    Pdf = lm.densitymatrix(Hl, mu=mu, T=T).to_numpy()
+    r = lambda a, b: float(np.linalg.norm(a - b) / np.linalg.norm(b))
+    gaps = {"K": K, "df_vs_fp64": r(Pdf, P64), "fp64_vs_oracle": r(P64, Pref), "df_vs_oracle": r(Pdf, Pref)}
+    print("low-T Fermi operator (12x12, T = 0.005):", gaps)
+    assert K >= 2000, gaps
+    assert gaps["fp64_vs_oracle"] <= 1e-11, gaps
+    assert gaps["df_vs_oracle"] <= 1e-11, gaps
+    assert gaps["df_vs_fp64"] <= 1e-11, gaps
+
+
 @pytest.mark.parametrize("precision", ["c64", "c32"])
 def test_zero_temperature_densitymatrix(lm, precision):
     """densitymatrix(H; mu) at T = 0: the device eigensystem (cuSOLVER) and the projector
