@@ -224,32 +224,24 @@ BATCH_WORKLOAD = ("{n} independent LxL open lattices, L ~ U{{16..96}}, t1=1, Poi
                   "B ~ U[0,0.3], disorder U[-W/2,W/2] with W ~ U[0,3], dense P_0 per lattice, dt=0.1")
 
 
-def run_batch_workload(args):
-    """The batching workload: uneven dense-P lattices stepped together (one graph per step).
-
-    P_0 of every lattice is a principal submatrix of one seeded random Hermitian matrix (a
-    stand-in of the right shape: the step's cost does not depend on P_0's values; parity of
-    the batched path with true densitymatrix P_0 is covered by the GPU tests).  Ket-steps: a
-    dense-P step U P U^dagger counts 2N per lattice."""
+def _batch_instances(n, prec, panel, p0="random", budget_frac=0.85):
+    """The first n lattices of the seeded batching workload, each with its dense P_0, in one
+    lmgpu.Batch (not yet updated).  p0 "random": principal submatrices of one seeded random
+    Hermitian matrix (the step's cost does not depend on P_0's values); "densitymatrix": the
+    FermiDirac ensemble of each lattice at mu = 0, T = 0.1 (densitymatrix on the device)."""
     import ctypes as C
     import torch
     import lmgpu
     from lmgpu import _lib
     ctx = lmgpu.default_context()
-    ext = torch.cuda.ExternalStream(ctx.stream_ptr(), device=torch.device("cuda", 0))
     rng = np.random.default_rng(SEED + 7)
-    n = args.instances
     Ls = rng.integers(16, 97, size=n)
     Bs = rng.uniform(0, 0.3, size=n)
     Ws = rng.uniform(0, 3, size=n)
-    prec = args.precision
     dtype = np.complex64 if prec == "c32" else np.complex128
     elem = 8 if prec == "c32" else 16
-    # c64 runs the per-order kernels on column panels in place (P + 2 N w scratch per lattice);
-    # c32 runs the fused kernel on full buffers (P + one recurrence buffer)
-    panel = args.panel if args.panel is not None else (1024 if prec == "c64" else 0)
     free = torch.cuda.mem_get_info()[0]
-    budget = 0.85 * free
+    budget = budget_frac * free
     take, used = [], 0
     for i, L in enumerate(Ls):
         N_i = int(L) ** 2
@@ -258,26 +250,86 @@ def run_batch_workload(args):
             break
         take.append(i)
         used += need
-    Nmax = int(max(Ls[take])) ** 2
-    R = (rng.standard_normal((Nmax, Nmax), dtype=np.float32)
-         + 1j * rng.standard_normal((Nmax, Nmax), dtype=np.float32)).astype(dtype)
-    Pbig = np.asfortranarray((R + R.conj().T) * (0.5 / math.sqrt(Nmax)))
-    del R
+    Pbig, Nmax = None, 0
+    if p0 == "random":
+        Nmax = int(max(Ls[take])) ** 2
+        R = (rng.standard_normal((Nmax, Nmax), dtype=np.float32)
+             + 1j * rng.standard_normal((Nmax, Nmax), dtype=np.float32)).astype(dtype)
+        Pbig = np.asfortranarray((R + R.conj().T) * (0.5 / math.sqrt(Nmax)))
+        del R
     batch = lmgpu.Batch("density", prec)
     if panel:
         batch.set_panel(panel)
     states = []
-    t_setup = time.perf_counter()
     for i in take:
         L = int(Ls[i])
         lat = lmgpu.SquareLattice(L, L)
         V = np.random.default_rng(SEED + 1000 + i).uniform(-Ws[i] / 2, Ws[i] / 2, size=L * L)
         H = lmgpu.tightbinding_hamiltonian(lat, V, field=lmgpu.PointFlux(float(Bs[i]), (L // 2 + 0.5, L // 2 + 0.5)))
-        st = lmgpu.DensityMatrix.__new__(lmgpu.DensityMatrix)
-        lmgpu.DeviceState.__init__(st, lat, None, _lib.LM_DENSITY, prec, None, ctx, shape=(L * L, L * L))
-        ctx.check(ctx.lib.lm_state_upload(st.handle, Pbig.ctypes.data_as(C.c_void_p), Nmax))
+        if p0 == "random":
+            st = lmgpu.DensityMatrix.__new__(lmgpu.DensityMatrix)
+            lmgpu.DeviceState.__init__(st, lat, None, _lib.LM_DENSITY, prec, None, ctx, shape=(L * L, L * L))
+            ctx.check(ctx.lib.lm_state_upload(st.handle, Pbig.ctypes.data_as(C.c_void_p), Nmax))
+        else:
+            st = lmgpu.densitymatrix(H, mu=0.0, T=0.1, precision=prec)
         batch.add(H, st)
         states.append(st)
+    return batch, states, Ls, take, used
+
+
+def batch_subrecord(n, steps, warmup):
+    """A small instance of the batching workload for the default line: the first n lattices,
+    P_0 from densitymatrix (mu = 0, T = 0.1), tuned, stepped through the captured graphs."""
+    import torch
+    import lmgpu
+    ctx = lmgpu.default_context()
+    ext = torch.cuda.ExternalStream(ctx.stream_ptr(), device=torch.device("cuda", 0))
+    t0 = time.perf_counter()
+    batch, states, Ls, take, used = _batch_instances(n, "c32", 0, p0="densitymatrix", budget_frac=0.5)
+    tr0 = np.array([s.trace() for s in states])
+    batch.update(0.1)
+    tune = batch.tune(steps=1)
+    info = batch.info()
+    setup = time.perf_counter() - t0
+    for _ in range(warmup):
+        batch.step()
+    ctx.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(ext)
+    for _ in range(steps):
+        batch.step()
+    e1.record(ext)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1)
+    tr1 = np.array([s.trace() for s in states])
+    ket_steps = sum(2 * int(Ls[i]) ** 2 for i in take)
+    return {"value": ket_steps * steps / (ms / 1000.0), "unit": "ket-steps/s", "ms_per_step": ms / steps,
+            "steps": steps, "warmup": warmup, "instances": len(take),
+            "sum_N2": int(sum(int(Ls[i]) ** 4 for i in take)), "chebyshev_order": info["K"], "tuned": tune,
+            "p0": "densitymatrix(h, mu=0, T=0.1) per lattice (device Chebyshev Fermi operator)",
+            "trace_drift_max": float(np.abs(tr1 - tr0).max() / np.abs(tr0).max()), "setup_s": setup,
+            "workload": BATCH_WORKLOAD.format(n=len(take)) + " (the first lattices of the seeded 512)"}
+
+
+def run_batch_workload(args):
+    """The batching workload: uneven dense-P lattices stepped together (one graph per step).
+
+    P_0 of every lattice is a principal submatrix of one seeded random Hermitian matrix (a
+    stand-in of the right shape: the step's cost does not depend on P_0's values; parity of
+    the batched path with true densitymatrix P_0 is covered by the GPU tests).  Ket-steps: a
+    dense-P step U P U^dagger counts 2N per lattice."""
+    import torch
+    import lmgpu
+    ctx = lmgpu.default_context()
+    ext = torch.cuda.ExternalStream(ctx.stream_ptr(), device=torch.device("cuda", 0))
+    n = args.instances
+    prec = args.precision
+    # c64 runs the per-order kernels on column panels in place (P + 2 N w scratch per lattice);
+    # c32 runs the fused kernel on full buffers (P + one recurrence buffer)
+    panel = args.panel if args.panel is not None else (1024 if prec == "c64" else 0)
+    t_setup = time.perf_counter()
+    batch, states, Ls, take, used = _batch_instances(n, prec, panel)
     batch.update(0.1)
     tune = batch.tune(steps=1)
     info = batch.info()
@@ -648,6 +700,8 @@ def main():
                          "densitymatrix: P_0 at T > 0, Chebyshev vs eigensolver; general: honeycomb via ELL; "
                          "readouts: localdensity and DensityCurrents of the kets workload")
     ap.add_argument("--instances", type=int, default=512)
+    ap.add_argument("--batch-instances", type=int, default=64,
+                    help="lattices of the batch sub-record of the default line (0: none)")
     ap.add_argument("--panel", type=int, default=None,
                     help="batch: column-panel width of the per-order path (default 1024 for c64, off for c32)")
     ap.add_argument("--precision", default="c32", choices=["c32", "c64"])
@@ -845,6 +899,11 @@ def main():
     d2h = N * 8 + nb * 8
     del e2e_state, ev, evs
 
+    # ---- a small instance of the batching workload (observed on every default run) ----
+    batch_rec = None
+    if world == 1 and args.batch_instances > 0:
+        batch_rec = batch_subrecord(args.batch_instances, steps=3, warmup=max(args.warmup, 3))
+
     # ---- report ----------------------------------------------------------------------
     if rank != 0:
         if dist is not None:
@@ -937,6 +996,8 @@ def main():
         "gpu_launches": int(launches32),
         "clocks": clocks,
     }
+    if batch_rec is not None:
+        line["batch"] = batch_rec
     if world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_reference(1, 1, cpu_seconds=20.0)
         one = cpu_reference(1, 1, sample_kets=2, cpu_seconds=8.0, nthreads=1)
