@@ -930,11 +930,12 @@ def main():
     if streamed:
         kname = (f"cheb_stream_c32_kernel<{K32}, 3, {'true' if use_comp else 'false'}> (x-streaming form: all K "
                  f"orders of one step per launch{', compensated state' if use_comp else ''})")
-        t_cap, units_cap, rec = profile_traffic(TRAFFIC_RECORD_COMP if use_comp else TRAFFIC_RECORD)
+        rec_name = TRAFFIC_RECORD_COMP if use_comp else TRAFFIC_RECORD
+        t_cap, units_cap, rec = profile_traffic(rec_name)
         if t_cap is not None and rec.get("K") == K32:
             traffic = t_cap * (N * M) / units_cap
             traffic_src = (f"ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch at {rec['sites']} sites x "
-                           f"{rec['kets']} kets (profiles/{TRAFFIC_RECORD}, source sha256 {rec['source_sha256'][:12]} "
+                           f"{rec['kets']} kets (profiles/{rec_name}, source sha256 {rec['source_sha256'][:12]} "
                            f"matches), scaled by sites x kets")
         else:
             traffic_src = rec if isinstance(rec, str) else "ncu record is for another order"
