@@ -765,6 +765,11 @@ end
 gpu_renormalize!(st::DeviceState, target::AbstractVector{<:Real}) =
     check(ccall((:lm_state_renormalize, LIB), Cint, (Ptr{Cvoid}, Ptr{Float64}), st.handle, Vector{Float64}(target)),
           st.lat.ctx.handle)
+# Compensated ComplexF32 kets: keep each amplitude's rounding residual so that long FP32 runs
+# do not accumulate the state's rounding (uniform-column lattices: Landau gauge, no y twist)
+gpu_compensate!(st::DeviceState, enable::Bool=true) =
+    check(ccall((:lm_state_set_compensation, LIB), Cint, (Ptr{Cvoid}, Cint), st.handle, Cint(enable)),
+          st.lat.ctx.handle)
 # (pointer, leading dimension) of the device block, e.g. for unsafe_wrap(CuArray, ...); it
 # changes when a step swaps buffers
 function device_pointer(st::DeviceState)
@@ -961,7 +966,7 @@ end
 export GPUBuilder, ChebyshevGPU, DeviceLattice, DeviceState, DeviceVector, DeviceHamiltonian, to_device,
        gpu_tightbinding, bond_currents, lattice_bonds, ReadoutRing, gpu_timesequence, gpu_timesequences,
        loss_and_gradients, GPUEigensystem, eigenvectors, projector, GPUBatch, DensityLossProblem, density_loss, GPUSparseHamiltonian, set_values!, gpu_operator_currents,
-       gpu_operator_timesequence, gpu_synchronize, set_option!, set_weights!, gpu_trace, gpu_norms, gpu_renormalize!,
+       gpu_operator_timesequence, gpu_synchronize, set_option!, set_weights!, gpu_trace, gpu_norms, gpu_renormalize!, gpu_compensate!,
        device_pointer, solver_order, spectral_bounds, padded_bounds, kpm_moments, chebyshev_coefficients,
        gpu_densitymatrix, gpu_entry_currents, LM_OPT_FUSED, LM_OPT_STREAM, LM_OPT_KPM
 
