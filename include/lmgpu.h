@@ -298,6 +298,18 @@ int lm_ell_add_field(lm_ell *ham, int kind, double px, double py, int *component
 int lm_ell_set_onsite(lm_ell *ham, const double *onsite);
 /* One amplitude per field component; asynchronous on the context's stream. */
 int lm_ell_assemble(lm_ell *ham, const double *amplitudes, int namp);
+/* Site layout of a general Hamiltonian that a temporally blocked kernel can step.
+ * LM_LAYOUT_HONEYCOMB: an a x b HoneycombLattice (2ab sites) in the reference's site order
+ * ((j1, j2, s) -> 2((j1-1) b + j2 - 1) + s - 1, src/lattices/bravais/unitcell.jl:113-132;
+ * basis [0, 0] and [1/2, sqrt(3)/6], src/zoo/lattices.jl:145-160) with nearest-neighbour
+ * bonds only; periodic_a / periodic_b: the boundaries along a a1 / b a2.  Every stored entry is
+ * checked to be one of the three bonds of its site (LM_ERR_ARG otherwise).  ComplexF32 ket
+ * blocks are then stepped by the x-streaming kernel as an a x 2b lattice (a >= 2K + 3;
+ * otherwise, and for ComplexF64 or density matrices, the per-order ELL kernels run).
+ * LM_LAYOUT_NONE drops the layout. */
+#define LM_LAYOUT_NONE 0
+#define LM_LAYOUT_HONEYCOMB 1
+int lm_ell_set_layout(lm_ell *h, int layout, int64_t a, int64_t b, int periodic_a, int periodic_b);
 int lm_ell_solver_update(lm_solver *s, lm_ell *h, double dt, int force);
 /* DensityCurrents(H, state)[i, j] = 2 Im(H[i,j] P[j,i]) (src/zoo/currents.jl:92-102) for every
  * stored entry of the CSC, in its order (0 for the diagonal): nnz doubles. */

@@ -1105,3 +1105,8 @@ int lm_trace(lm_state* s, double* out) {
 }
 
 }  // extern "C"
+
+namespace lmgpu {
+// The timing event pair of one step launch, for the step paths outside this file.
+int timing_event_pair(lm_ctx* ctx, cudaEvent_t* e0, cudaEvent_t* e1) { return timing_pair(ctx, e0, e1); }
+}  // namespace lmgpu

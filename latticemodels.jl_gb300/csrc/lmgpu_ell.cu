@@ -244,6 +244,37 @@ int ell_solver_step(lm_solver* s, lm_state* st) {
         }
     }
     int where = 0;
+    const lm_ell* h = s->ell;
+    if (h->brick && st->precision == LM_C32 && st->kind == LM_KETS && ctx->fused && ctx->fused_form == 1) {
+        // the honeycomb as an a x 2b brick lattice: the x-streaming kernel, all K orders per launch
+        Geom g{};
+        g.Lx = h->brick_a;
+        g.Ly = 2 * h->brick_b;
+        g.N = h->n;
+        g.per_x = h->brick_px;
+        g.per_y = h->brick_py;
+        if (stream_supported(g, s->K, 4, st->d_data, st->d_a, st->ld)) {
+            int rc0 = ensure_brick_pack(s, g, h->d_bmap);
+            if (rc0 != LM_OK) return rc0;
+            cudaEvent_t t0 = nullptr, t1 = nullptr;
+            if (ctx->timing) {
+                rc0 = timing_event_pair(ctx, &t0, &t1);
+                if (rc0 != LM_OK) return rc0;
+                CUDA_TRY(ctx, cudaEventRecord(t0, ctx->stream), "cudaEventRecord");
+            }
+            CUDA_TRY(ctx, launch_cheb_fused_c32(ctx, g, nullptr, nullptr, (const float2*)st->d_data, (float2*)st->d_a,
+                                                st->ld, st->m, s->K, false, s->coef.data(), s->phase_re, s->phase_im,
+                                                s->d_spack, 4),
+                     "honeycomb x-streaming step");
+            if (ctx->timing) {
+                CUDA_TRY(ctx, cudaEventRecord(t1, ctx->stream), "cudaEventRecord");
+                ctx->ev_launches[ctx->ev_used] = s->K;
+                ctx->ev_used++;
+            }
+            std::swap(st->d_data, st->d_a);
+            return LM_OK;
+        }
+    }
     int rc = ell_apply(s, st->precision, 1, 0, st->d_data, st->d_a, st->d_y, st->ld, st->m, &where);
     if (rc != LM_OK) return rc;
     if (where == 1) std::swap(st->d_data, st->d_a);
@@ -584,7 +615,72 @@ int lm_ell_destroy(lm_ell* h) {
     cudaFree(h->d_eterm);
     cudaFree(h->d_emap);
     cudaFree(h->d_onsite);
+    cudaFree(h->d_bmap);
     delete h;
+    return LM_OK;
+}
+
+int lm_ell_set_layout(lm_ell* h, int layout, int64_t a, int64_t b, int periodic_a, int periodic_b) {
+    if (!h) return LM_ERR_ARG;
+    lm_ctx* ctx = h->ctx;
+    if (layout == LM_LAYOUT_NONE) {
+        cudaStreamSynchronize(ctx->stream);
+        cudaFree(h->d_bmap);
+        h->d_bmap = nullptr;
+        h->brick = 0;
+        return LM_OK;
+    }
+    CHECK_ARG(ctx, layout == LM_LAYOUT_HONEYCOMB, "lm_ell_set_layout: unknown layout");
+    CHECK_ARG(ctx, a >= 1 && b >= 1 && 2 * a * b == h->n, "lm_ell_set_layout: a x b unit cells of 2 sites must be the n sites");
+    // a periodic axis of one or two cells would merge distinct bonds into one stored entry
+    CHECK_ARG(ctx, (!periodic_a || a >= 3) && (!periodic_b || b >= 3),
+              "lm_ell_set_layout: periodic axes need at least 3 unit cells");
+    const int64_t Ly = 2 * b;
+    std::vector<int> bm((size_t)(a * b) * 5, -1);
+    for (size_t p = 0; p < h->map.size(); ++p) {
+        const int64_t e = h->map[p];
+        if (e < 0) continue;  // diagonal
+        const int64_t r = h->csc_row[p], c = h->csc_col[p];
+        const int64_t xr = r / Ly, yr = r % Ly, xc = c / Ly, yc = c % Ly;
+        const int sr = (int)(yr & 1), sc = (int)(yc & 1);
+        const int64_t lr = yr >> 1, lc = yc >> 1;
+        int slot = -1;
+        if (sr == 0 && sc == 1) {  // A -> B
+            if (xc == xr && lc == lr) slot = 0;
+            else if (xc == xr && (lc == lr - 1 || (periodic_b && lr == 0 && lc == b - 1))) slot = 1;
+            else if (lc == lr && (xc == xr - 1 || (periodic_a && xr == 0 && xc == a - 1))) slot = 2;
+        } else if (sr == 1 && sc == 0) {  // B -> A
+            if (xc == xr && lc == lr) continue;  // conj of the A -> B entry of the same cell
+            if (lc == lr && (xc == xr + 1 || (periodic_a && xr == a - 1 && xc == 0))) slot = 3;
+            else if (xc == xr && (lc == lr + 1 || (periodic_b && lr == b - 1 && lc == 0))) slot = 4;
+        }
+        if (slot < 0) return set_err(ctx, LM_ERR_ARG, "lm_ell_set_layout: an entry is not a honeycomb nearest-neighbour bond");
+        const int64_t cell = xr * b + lr;
+        int& dst = bm[(size_t)cell * 5 + slot];
+        if (dst >= 0) return set_err(ctx, LM_ERR_ARG, "lm_ell_set_layout: two entries for one honeycomb bond");
+        CHECK_ARG(ctx, e < (int64_t)1 << 31, "lm_ell_set_layout: ELL table too large");
+        dst = (int)e;
+    }
+    cudaSetDevice(ctx->device);
+    int* d = nullptr;
+    if (cudaMalloc((void**)&d, sizeof(int) * bm.size()) != cudaSuccess) {
+        cudaGetLastError();
+        return set_err(ctx, LM_ERR_OOM, "lm_ell_set_layout: bond map");
+    }
+    const cudaError_t ce = cudaMemcpy(d, bm.data(), sizeof(int) * bm.size(), cudaMemcpyHostToDevice);
+    if (ce != cudaSuccess) {
+        cudaFree(d);
+        return check_cuda(ctx, ce, "lm_ell_set_layout: bond map upload");
+    }
+    cudaStreamSynchronize(ctx->stream);
+    cudaFree(h->d_bmap);
+    h->d_bmap = d;
+    h->brick = 1;
+    h->brick_a = a;
+    h->brick_b = b;
+    h->brick_px = periodic_a ? 1 : 0;
+    h->brick_py = periodic_b ? 1 : 0;
+    h->version++;  // solvers rebuild their tables (and the brick planes)
     return LM_OK;
 }
 
@@ -796,6 +892,7 @@ int lm_ell_solver_update(lm_solver* s, lm_ell* h, double dt, int force) {
     const unsigned grid = (unsigned)std::min<int64_t>((tab + h->n + 255) / 256, 4096);
     ell_normalise_kernel<<<grid, 256, 0, ctx->stream>>>(h->n, h->w, h->d_vals, h->d_diag, s->a, s->b, s->d_ev2, s->d_ed2,
                                                         s->d_ev2f, s->d_ed2f);
+    s->bpack_valid = 0;
     ctx->launches++;
     CUDA_TRY(ctx, cudaGetLastError(), "ell normalise kernel");
     s->ell = h;

@@ -98,8 +98,8 @@ struct lm_ctx {
     int timing = 0;
     int fused = 1;                      // LM_OPT_FUSED: temporally blocked c32 step enabled
     unsigned fused_attr = 0;            // bit K (+16 for real x-hops): shared-memory attribute set
-    unsigned stream_attr = 0;           // the same for the x-streaming form (bit K + 8 mode)
-    unsigned stream_attr_comp = 0;      // the same for its compensated-state variant
+    unsigned long long stream_attr = 0;       // the same for the x-streaming form (bit K + 8 mode)
+    unsigned long long stream_attr_comp = 0;  // the same for its compensated-state variant
     int fused_form = 1;                 // LM_OPT_STREAM: 1 = x-streaming form where supported, 0 = region form
     int64_t stream_launches = 0;        // fused steps run in the x-streaming form
     int kpm_df = 1;                     // LM_OPT_KPM: double-float recurrence in lm_kpm_moments
@@ -182,6 +182,7 @@ struct lm_solver {
     float4* d_spack = nullptr;
     size_t spack_f4 = 0;
     uint64_t spack_version = ~0ull;
+    int bpack_valid = 0;         // d_spack holds the honeycomb brick planes of the current ELL tables
     int has_onsite = 0;
     int fixed_bounds = 0;        // lm_solver_set_bounds: use [fix_emin, fix_emax] instead of Gershgorin
     double fix_emin = 0.0, fix_emax = 0.0;
@@ -228,6 +229,13 @@ struct lm_ell {
     std::vector<double> rad;           // Gershgorin radius per row: sum of |base| (field-free)
     lmgpu::FieldSet fields{};
     int assembled = 0;
+    // honeycomb brick layout (lm_ell_set_layout): an a x b HoneycombLattice in the reference's
+    // site order, stepped by the x-streaming kernel (MODE 4) as an a x 2b lattice; per unit
+    // cell the ELL value indices of its five distinct bonds (-1 = none)
+    int brick = 0;
+    int64_t brick_a = 0, brick_b = 0;
+    int brick_px = 0, brick_py = 0;
+    int* d_bmap = nullptr;
 };
 
 // Argument and CUDA-status checks that return the status from the calling C-ABI function.
@@ -311,6 +319,9 @@ cudaError_t ensure_fused_attr(lm_ctx* ctx, int K, bool xreal);
 // packed coefficient planes (rebuilt from the FP32 tables when they change) and the launch.
 bool stream_supported(const Geom& g, int K, int mode, const void* x, const void* out, int64_t ld);
 int ensure_stream_pack(lm_solver* s, const Geom& g);
+int ensure_brick_pack(lm_solver* s, const Geom& g, const int* d_bmap);
+// Next (start, stop) event pair of the context's per-launch timing (lm_ctx_set_timing).
+int timing_event_pair(lm_ctx* ctx, cudaEvent_t* e0, cudaEvent_t* e1);
 cudaError_t launch_cheb_stream_c32(lm_ctx* ctx, const FusedInst& d, int K, int mode, const float4* spack);
 cudaError_t launch_cheb_fused_c32(lm_ctx* ctx, const Geom& g, const float2* hop2, const float* diag2,
                                   const float2* x, float2* out, int64_t ld, int64_t m, int K, bool xreal,

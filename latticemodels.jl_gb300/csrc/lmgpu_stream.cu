@@ -60,6 +60,14 @@ namespace lmgpu {
 
 namespace {
 constexpr int SW = LM_STREAM_WARPS;
+// The brick stencil at K = 6 needs more than 128 registers a thread (its three-column windows of
+// complex values): it runs 12 warps per CTA (up to 170 registers).
+#ifndef LM_STREAM_WARPS_BRICK6
+#define LM_STREAM_WARPS_BRICK6 12
+#endif
+__host__ __device__ constexpr int stream_warps(int K, int mode) {
+    return (mode == 4 && K >= 6) ? LM_STREAM_WARPS_BRICK6 : SW;
+}
 constexpr int SR = 64;       // strip width along y: 32 lanes x 2 sites
 constexpr int SPF = 3;       // columns of the ket staged ahead
 constexpr int kStreamMaxK = 6;
@@ -243,6 +251,10 @@ __global__ void stream_pack_kernel(const Geom g, const float2* __restrict__ hop2
     }
 }
 
+// MODE 4: the honeycomb in the reference's site order, (j1, j2, s) -> (j1 - 1) 2b + 2(j2 - 1) + s - 1,
+// read as an a x 2b "brick" lattice: a lane's pair is one unit cell (A, B); A's neighbours are
+// B of its cell, B of the cell below (lane - 1) and B of column x - 1, B's are A of its cell, A
+// of the cell above (lane + 1) and A of column x + 1 (planes 0-2 of ensure_brick_pack).
 // MODE 0: complex x-hops (planes 1-4); 1: real x-hops (planes 0, 3, 4); 2: uniform columns --
 // real x-hops and every hop of a column equal (the Landau gauge without a twist along y), so an
 // order reads the diagonal pair of its sites and one column record shared by the warp; 3: the
@@ -253,12 +265,13 @@ __global__ void stream_pack_kernel(const Geom g, const float2* __restrict__ hop2
 // residual (the plane, in place), so the state's own FP32 rounding does not accumulate from
 // step to step.
 template <int K, int MODE, bool CMP>
-__global__ void __launch_bounds__(SW * 32, 1)
+__global__ void __launch_bounds__(stream_warps(K, MODE) * 32, 1)
 cheb_stream_c32_kernel(const FusedInst D, const StreamPairs SP, const float4* __restrict__ pk,
                        const float2* __restrict__ pd, const float4* __restrict__ pc, int npair, long long plane,
                        int nty, long long ncols, long long nwarps) {
-    constexpr bool XR = MODE >= 1;
-    constexpr bool UC = MODE >= 2;
+    constexpr bool BRICK = MODE == 4;
+    constexpr bool XR = MODE >= 1 && !BRICK;
+    constexpr bool UC = MODE == 2 || MODE == 3;
     constexpr bool YEDGE = MODE == 2;
     // MODE 3 runs the stencil on float pairs (ffma2).  It keeps S_k = sigma_k T_k with sigma_k = +1
     // for k mod 4 in {0, 1} and -1 otherwise, so that the T_{k-2} term enters every chain with a
@@ -272,7 +285,7 @@ cheb_stream_c32_kernel(const FusedInst D, const StreamPairs SP, const float4* __
     constexpr int H = stream_halo(K);
     constexpr int YR = K + 1;          // accumulator ring: columns x .. x+K in flight
     constexpr int XS = K + 1 + SPF;    // ket ring: column s+SPF staged, column s-K still read
-    constexpr bool ROT = LM_STREAM_ROTATE == 1 || (LM_STREAM_ROTATE == 2 && MODE < 2);
+    constexpr bool ROT = LM_STREAM_ROTATE == 1 || (LM_STREAM_ROTATE == 2 && !UC);
     constexpr int NP = ROT ? 1 : 3;    // steps per unrolled loop body
     extern __shared__ float4 smem[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -287,13 +300,14 @@ cheb_stream_c32_kernel(const FusedInst D, const StreamPairs SP, const float4* __
     const float4* __restrict__ P3 = pk + 3 * plane;
     const float4* __restrict__ P4 = pk + 4 * plane;
     // uniform columns: diagonal-pair ring per warp, column records per CTA
-    float2* dring = reinterpret_cast<float2*>(smem + SW * stream_ring_f4(K)) + warp * XS * 32;
-    float4* ctab = smem + SW * (stream_ring_f4(K) + stream_dring_f4(K));
+    constexpr int NW = stream_warps(K, MODE);
+    float2* dring = reinterpret_cast<float2*>(smem + NW * stream_ring_f4(K)) + warp * XS * 32;
+    float4* ctab = smem + NW * (stream_ring_f4(K) + stream_dring_f4(K));
     uint2* rring = reinterpret_cast<uint2*>(ctab + ((int)D.g.Lx + kPadL + kPadR) * stream_crec_f4(MODE)) +
                    warp * kResRing * 32;
     if (UC) {
         const int Xp = Lx + kPadL + kPadR;
-        for (int i = threadIdx.x; i < Xp; i += SW * 32) {
+        for (int i = threadIdx.x; i < Xp; i += NW * 32) {
             const float4 q = __ldg(pc + i);  // {hx, hxm, hy.re, hy.im}
             if (PAIRED) {
                 ctab[4 * i + 0] = make_float4(q.x, q.x, q.y, q.y);
@@ -310,7 +324,7 @@ cheb_stream_c32_kernel(const FusedInst D, const StreamPairs SP, const float4* __
     // Work: the columns of every (strip, ket) item, items in the order strip-major, ket-minor;
     // warp w takes the contiguous share [w ncols / nwarps, (w+1) ncols / nwarps) of them, i.e.
     // column ranges [xa, xb) of one or more consecutive items.
-    const long long w = (long long)blockIdx.x * SW + warp;
+    const long long w = (long long)blockIdx.x * NW + warp;
     if (w >= nwarps) return;
     const long long c_end = (w + 1) * ncols / nwarps;  // ncols * nwarps < 2^63
     for (long long c = w * ncols / nwarps; c < c_end;) {
@@ -412,6 +426,18 @@ cheb_stream_c32_kernel(const FusedInst D, const StreamPairs SP, const float4* __
                         hy[1] = (YEDGE && y_last) ? make_float2(0.f, 0.f) : hy[0];
                         hym[0] = (YEDGE && y_first) ? make_float2(0.f, 0.f) : make_float2(qc.z, -qc.w);
                         hym[1] = make_float2(qc.z, -qc.w);
+                    } else if (BRICK && o >= 0) {
+                        // brick planes: {h_AB, h_A,B(lane-1)}, {h_A,B(x-1), h_B,A(x+1)}, {h_B,A(lane+1), dA, dB}
+                        const float4 q0 = __ldg(P0 + o), q1 = __ldg(P1 + o), q2 = __ldg(P2 + o);
+                        hy[0] = make_float2(q0.x, q0.y);   // A -> B of the same cell (y + 1)
+                        hym[1] = make_float2(q0.x, -q0.y); // B -> A of the same cell (y - 1)
+                        hym[0] = make_float2(q0.z, q0.w);  // A -> B of the cell below (lane - 1)
+                        hxm[0] = make_float2(q1.x, q1.y);  // A -> B of column x - 1
+                        hx[1] = make_float2(q1.z, q1.w);   // B -> A of column x + 1
+                        hy[1] = make_float2(q2.x, q2.y);   // B -> A of the cell above (lane + 1)
+                        hx[0] = hxm[1] = make_float2(0.f, 0.f);
+                        d[0] = q2.z;
+                        d[1] = q2.w;
                     } else if (o >= 0) {
                         const float4 qy = __ldg(P3 + o), qd = __ldg(P4 + o);
                         hy[0] = make_float2(qy.x, qy.y);
@@ -502,7 +528,12 @@ cheb_stream_c32_kernel(const FusedInst D, const StreamPairs SP, const float4* __
                             acc = make_float2(-t2.x, -t2.y);
                         }
                         const float2 vxp = tp[j], vxm = tm[j];
-                        if (XR) {
+                        if (BRICK) {  // A's x-neighbour is B of column x-1, B's is A of column x+1
+                            const float2 hb = j == 0 ? hxm[0] : hx[1];
+                            const float2 vb = j == 0 ? tm[1] : tp[0];
+                            acc.x = fmaf(hb.x, vb.x, acc.x); acc.x = fmaf(-hb.y, vb.y, acc.x);
+                            acc.y = fmaf(hb.x, vb.y, acc.y); acc.y = fmaf(hb.y, vb.x, acc.y);
+                        } else if (XR) {
                             acc.x = fmaf(hx[j].x, vxp.x, acc.x);
                             acc.y = fmaf(hx[j].x, vxp.y, acc.y);
                             acc.x = fmaf(hxm[j].x, vxm.x, acc.x);
@@ -652,6 +683,8 @@ cheb_stream_c32_kernel(const FusedInst D, const StreamPairs SP, const float4* __
 }
 
 bool stream_supported(const Geom& g, int K, int mode, const void* x, const void* out, int64_t ld) {
+    // complex x-hops (MODE 0) leave registers for K <= 5; the brick stencil (MODE 4) has three
+    // neighbours per site and fits K = 6
     return K >= 2 && K <= (mode >= 1 ? kStreamMaxK : kStreamMaxK - 1) && g.Ly % 2 == 0 && g.Lx >= 2 * K + 3 && g.N < ((int64_t)1 << 31) &&
            ld % 2 == 0 && ((uintptr_t)x & 15) == 0 && ((uintptr_t)out & 15) == 0;
 }
@@ -718,14 +751,79 @@ int ensure_stream_pack(lm_solver* s, const Geom& g) {
     return LM_OK;
 }
 
+// Honeycomb brick planes from the normalised ELL values: record (padded column xp, pair l) of
+// plane q holds the values that `bmap` (5 ELL value indices per unit cell, -1 = no bond)
+// names, periodic columns wrapped and open ones zero, plus the zero record at the end.
+__global__ void brick_pack_kernel(int64_t Lx, int per_x, const int* __restrict__ bmap, const float2* __restrict__ v2f,
+                                  const float* __restrict__ d2f, float4* __restrict__ pk, int npair, int Xp,
+                                  long long plane) {
+    const long long n = (long long)Xp * npair + 1;
+    const float2 z = make_float2(0.f, 0.f);
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        float2 h[5] = {z, z, z, z, z};
+        float dA = 0.f, dB = 0.f;
+        if (i < n - 1) {
+            const int xp = (int)(i / npair), l = (int)(i % npair);
+            const int64_t x = (int64_t)xp - kPadL;
+            const int xs = per_x ? wrap_mod(x, Lx) : ((x >= 0 && x < Lx) ? (int)x : -1);
+            if (xs >= 0) {
+                const long long cell = (long long)xs * npair + l;
+#pragma unroll
+                for (int q = 0; q < 5; ++q) {
+                    const int e = bmap[cell * 5 + q];
+                    if (e >= 0) h[q] = v2f[e];
+                }
+                dA = d2f[2 * cell];
+                dB = d2f[2 * cell + 1];
+            }
+        }
+        pk[i] = make_float4(h[0].x, h[0].y, h[1].x, h[1].y);
+        pk[plane + i] = make_float4(h[2].x, h[2].y, h[3].x, h[3].y);
+        pk[2 * plane + i] = make_float4(h[4].x, h[4].y, dA, dB);
+    }
+}
+
+int ensure_brick_pack(lm_solver* s, const Geom& g, const int* d_bmap) {
+    lm_ctx* ctx = s->ctx;
+    int npair, Xp;
+    long long plane;
+    pack_dims(g, &npair, &Xp, &plane);
+    const size_t need = pack_f4(g);
+    if (s->spack_f4 != need) {
+        if (s->d_spack) cudaFree(s->d_spack);
+        s->d_spack = nullptr;
+        s->spack_f4 = 0;
+        const cudaError_t e = cudaMalloc((void**)&s->d_spack, sizeof(float4) * need);
+        if (e != cudaSuccess) {
+            s->d_spack = nullptr;
+            cudaGetLastError();
+            return set_err(ctx, LM_ERR_OOM, "brick coefficient planes: out of device memory");
+        }
+        s->spack_f4 = need;
+        s->bpack_valid = 0;
+    }
+    s->spack_version = ~0ull;  // the square-lattice planes are no longer in the buffer
+    if (s->bpack_valid) return LM_OK;
+    const unsigned grid = (unsigned)std::min<long long>((plane + 255) / 256, 4096);
+    brick_pack_kernel<<<grid, 256, 0, ctx->stream>>>(g.Lx, g.per_x, d_bmap, s->d_ev2f, s->d_ed2f, s->d_spack, npair, Xp,
+                                                     plane);
+    ctx->launches++;
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return check_cuda(ctx, e, "brick coefficient planes");
+    s->bpack_valid = 1;
+    return LM_OK;
+}
+
 static int stream_smem_bytes(int K, int mode, int Xp, bool cmp = false) {
-    return SW * stream_ring_f4(K) * 16 + (mode >= 2 ? SW * stream_dring_f4(K) * 16 + Xp * 16 * stream_crec_f4(mode) : 0) +
-           (cmp ? SW * kResRing * 32 * 8 : 0);
+    const bool uc = mode == 2 || mode == 3;
+    const int nw = stream_warps(K, mode);
+    return nw * stream_ring_f4(K) * 16 + (uc ? nw * stream_dring_f4(K) * 16 + Xp * 16 * stream_crec_f4(mode) : 0) +
+           (cmp ? nw * kResRing * 32 * 8 : 0);
 }
 
 bool stream_comp_supported(const Geom& g, int K, int mode) {
     const int m = (mode == 2 && g.per_y) ? 3 : mode;
-    return m >= 2 && stream_smem_bytes(K, m, (int)g.Lx + kPadL + kPadR, true) <= kStreamSmemMax;
+    return (m == 2 || m == 3) && stream_smem_bytes(K, m, (int)g.Lx + kPadL + kPadR, true) <= kStreamSmemMax;
 }
 
 template <int MODE, bool CMP>
@@ -735,8 +833,8 @@ static cudaError_t launch_stream_k(lm_ctx* ctx, int K, int grid, const FusedInst
     long long plane;
     pack_dims(d.g, &npair, &Xp, &plane);
     const PackPtrs pp = pack_ptrs(const_cast<float4*>(spack), d.g);
-    const unsigned bit = 1u << (K + 8 * MODE);
-    unsigned& attr = CMP ? ctx->stream_attr_comp : ctx->stream_attr;
+    const unsigned long long bit = 1ull << (K + 8 * MODE);
+    unsigned long long& attr = CMP ? ctx->stream_attr_comp : ctx->stream_attr;
     switch (K) {
 #define LM_STREAM_CASE(KK)                                                                                       \
     case KK: {                                                                                                   \
@@ -747,7 +845,7 @@ static cudaError_t launch_stream_k(lm_ctx* ctx, int K, int grid, const FusedInst
             if (e != cudaSuccess) return e;                                                                      \
             attr |= bit;                                                                                         \
         }                                                                                                        \
-        cheb_stream_c32_kernel<KK, MODE, CMP><<<(unsigned)grid, SW * 32, smem, ctx->stream>>>(                  \
+        cheb_stream_c32_kernel<KK, MODE, CMP><<<(unsigned)grid, stream_warps(KK, MODE) * 32, smem, ctx->stream>>>( \
             d, sp, pp.pk, pp.pd, pp.pc, npair, plane, nty, ncols, nwarps);                                           \
         return cudaGetLastError();                                                                               \
     }
@@ -765,11 +863,12 @@ cudaError_t launch_cheb_stream_c32(lm_ctx* ctx, const FusedInst& d, int K, int m
     if (ncols <= 0) return cudaSuccess;
     // one warp per SM slot, but at least 8K columns per warp (a share costs 2K extra steps
     // for every item it touches)
-    const long long slots = (long long)(ctx->sm_count > 0 ? ctx->sm_count : 152) * SW;
-    const long long nwarps = std::max<long long>(1, std::min<long long>(slots, ncols / (8 * K)));
-    const int grid = (int)((nwarps + SW - 1) / SW);
     int m = (mode == 2 && d.g.per_y) ? 3 : mode;
-    if (m >= 2 && stream_smem_bytes(K, m, (int)d.g.Lx + kPadL + kPadR) > kStreamSmemMax) m = 1;  // very long x
+    if ((m == 2 || m == 3) && stream_smem_bytes(K, m, (int)d.g.Lx + kPadL + kPadR) > kStreamSmemMax) m = 1;  // very long x
+    const int nw = stream_warps(K, m);
+    const long long slots = (long long)(ctx->sm_count > 0 ? ctx->sm_count : 152) * nw;
+    const long long nwarps = std::max<long long>(1, std::min<long long>(slots, ncols / (8 * K)));
+    const int grid = (int)((nwarps + nw - 1) / nw);
     StreamPairs sp;
     for (int k = 0; k <= kStreamMaxK; ++k) {
         const float v = k <= K ? ((k & 2) ? -d.s[k] : d.s[k]) : 0.f;  // sigma_k s_k
@@ -777,11 +876,12 @@ cudaError_t launch_cheb_stream_c32(lm_ctx* ctx, const FusedInst& d, int K, int m
     }
     cudaError_t e;
     if (d.comp) {  // compensated block: the uniform-column modes only (checked by the caller)
-        if (m < 2) return cudaErrorNotSupported;
+        if (m != 2 && m != 3) return cudaErrorNotSupported;
         e = m == 3 ? launch_stream_k<3, true>(ctx, K, grid, d, sp, spack, (int)nty, ncols, nwarps)
                    : launch_stream_k<2, true>(ctx, K, grid, d, sp, spack, (int)nty, ncols, nwarps);
     } else {
-        e = m == 3   ? launch_stream_k<3, false>(ctx, K, grid, d, sp, spack, (int)nty, ncols, nwarps)
+        e = m == 4   ? launch_stream_k<4, false>(ctx, K, grid, d, sp, spack, (int)nty, ncols, nwarps)
+            : m == 3 ? launch_stream_k<3, false>(ctx, K, grid, d, sp, spack, (int)nty, ncols, nwarps)
             : m == 2 ? launch_stream_k<2, false>(ctx, K, grid, d, sp, spack, (int)nty, ncols, nwarps)
             : m == 1 ? launch_stream_k<1, false>(ctx, K, grid, d, sp, spack, (int)nty, ncols, nwarps)
                      : launch_stream_k<0, false>(ctx, K, grid, d, sp, spack, (int)nty, ncols, nwarps);

@@ -29,6 +29,7 @@ LM_OPT_STREAM = 2
 LM_OPT_KPM = 3
 LM_KETS, LM_DENSITY = 0, 1
 LM_FIELD_LANDAU, LM_FIELD_SYMMETRIC, LM_FIELD_POINTFLUX_AXIAL, LM_FIELD_POINTFLUX_SINGULAR = 1, 2, 3, 4
+LM_LAYOUT_NONE, LM_LAYOUT_HONEYCOMB = 0, 1
 
 HEADER = Path(__file__).resolve().parent.parent.parent / "include" / "lmgpu.h"
 
@@ -77,6 +78,7 @@ SIGNATURES = {
     "lm_state_norms": (_INT, [_P, _PD]),
     "lm_state_renormalize": (_INT, [_P, _PD]),
     "lm_state_set_compensation": (_INT, [_P, _INT]),
+    "lm_ell_set_layout": (_INT, [_P, _INT, _I64, _I64, _INT, _INT]),
     "lm_solver_create": (_INT, [_P, _D, C.POINTER(_P)]),
     "lm_solver_destroy": (_INT, [_P]),
     "lm_solver_update": (_INT, [_P, _P, _D, _INT]),

@@ -212,6 +212,13 @@ class _DeviceBondEll:
         for kind, px, py in comps:
             idx = C.c_int()
             ctx.check(ctx.lib.lm_ell_add_field(p, kind, px, py, C.byref(idx)))
+        # the honeycomb in the reference's site order is a brick lattice: ComplexF32 kets then
+        # step through the temporally blocked kernel (periodic axes need 3 or more cells)
+        self.brick = (lat.name == "HoneycombLattice" and (not lat.periodic[0] or lat.a >= 3)
+                      and (not lat.periodic[1] or lat.b >= 3))
+        if self.brick:
+            ctx.check(ctx.lib.lm_ell_set_layout(p, _lib.LM_LAYOUT_HONEYCOMB, lat.a, lat.b, int(lat.periodic[0]),
+                                                int(lat.periodic[1])))
         self.onsite_ref = None
         self.amps = None
 
