@@ -454,6 +454,12 @@ function GPUSparseHamiltonian(A::SparseMatrixCSC{ComplexF64,Int64}; ctx=default_
 end
 set_values!(H::GPUSparseHamiltonian, A::SparseMatrixCSC{ComplexF64,Int64}) =
     check(ccall((:lm_ell_set_values, LIB), Cint, (Ptr{Cvoid}, Ptr{ComplexF64}), H.handle, A.nzval), H.ctx.handle)
+# An a x b HoneycombLattice in the reference's site order (unit cells (j1, j2), j2 fastest, two
+# basis sites): ComplexF32 kets then step through the temporally blocked streaming kernel as an
+# a x 2b brick lattice.  The library checks that every stored entry is a nearest-neighbour bond.
+honeycomb_layout!(H::GPUSparseHamiltonian, a::Integer, b::Integer; periodic=(false, false)) =
+    check(ccall((:lm_ell_set_layout, LIB), Cint, (Ptr{Cvoid}, Cint, Int64, Int64, Cint, Cint),
+                H.handle, Cint(1), a, b, Cint(periodic[1]), Cint(periodic[2])), H.ctx.handle)
 update_solver!(s::ChebyshevGPU, H::GPUSparseHamiltonian, dt, force=false) =
     check(ccall((:lm_ell_solver_update, LIB), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Cdouble, Cint), s.handle, H.handle, dt, force),
           s.ctx.handle)
@@ -966,7 +972,7 @@ end
 export GPUBuilder, ChebyshevGPU, DeviceLattice, DeviceState, DeviceVector, DeviceHamiltonian, to_device,
        gpu_tightbinding, bond_currents, lattice_bonds, ReadoutRing, gpu_timesequence, gpu_timesequences,
        loss_and_gradients, GPUEigensystem, eigenvectors, projector, GPUBatch, DensityLossProblem, density_loss, GPUSparseHamiltonian, set_values!, gpu_operator_currents,
-       gpu_operator_timesequence, gpu_synchronize, set_option!, set_weights!, gpu_trace, gpu_norms, gpu_renormalize!, gpu_compensate!,
+       gpu_operator_timesequence, gpu_synchronize, set_option!, set_weights!, gpu_trace, gpu_norms, gpu_renormalize!, gpu_compensate!, honeycomb_layout!,
        device_pointer, solver_order, spectral_bounds, padded_bounds, kpm_moments, chebyshev_coefficients,
        gpu_densitymatrix, gpu_entry_currents, LM_OPT_FUSED, LM_OPT_STREAM, LM_OPT_KPM
 
