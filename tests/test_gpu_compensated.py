@@ -130,6 +130,30 @@ def test_compensated_refusals(lm):
     s.step(st)
 
 
+def test_compensated_time_dependent_h_through_evolution(lm):
+    """Evolution over h(t) with a Landau amplitude and an on-site term that change every step
+    (the e2e loop of the kets workload) on a compensated block: the coefficient planes are
+    rebuilt every step and the residual is carried across the updates; against the oracle
+    stepping the same left-endpoint Hamiltonians with the exact exponent."""
+    L, M, dt, n = 32, 4, 0.05, 6
+    ol, ll = pair(lm, L, L, (True, True))
+    V = o.anderson_disorder(ol.N, 2.0, 21)
+    Bt = lambda t: 0.01 * (1.0 + 0.1 * np.sin(t))
+    Vt = lambda t: V + 0.05 * np.sin(0.5 * t)
+    X = o.random_kets(ol.N, M, 22)
+    st = lm.KetBlock(ll, X, precision="c32", compensated=True)
+    ev = lm.Evolution(lm.ChebyshevGPU(), lambda t: lm.tightbinding_hamiltonian(ll, Vt(t), field=lm.LandauGauge(Bt(t))),
+                      st)
+    assert ev.current_states()[0].compensated
+    times = [dt * (k + 1) for k in range(n)]
+    Y, t0 = X, 0.0
+    for moment, t in zip(ev(times), times):
+        Ho = o.tightbinding_hamiltonian(ol, field=o.LandauGauge(Bt(t0)), onsite=Vt(t0))
+        Y = o.expm_multiply(Ho, t - t0, Y)
+        t0 = t
+        assert rel(moment.state.to_numpy().astype(np.complex128), Y) <= 3e-6
+
+
 def test_compensated_plain_config_400_steps(lm):
     """The plain-method lattice at its full length: SquareLattice(256, 256) periodic, Landau
     0.01, Anderson U[-1, 1], 64 complex-Gaussian kets, 400 steps of dt = 0.05 at tol 1e-9 with
