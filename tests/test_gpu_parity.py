@@ -430,8 +430,11 @@ STREAM_CASES = [
     (40, 70, True, False, "pointflux", 0.03, 7),  # complex x-hops (K <= 5)
     (33, 64, False, True, "pointflux", 0.03, 3),
     (20, 200, True, True, "landau", 0.05, 1),     # one ket, many strips
-    (24, 128, True, True, "landau", 0.05, 7),     # ring groups of 2 warps
-    (16, 512, True, True, "landau", 0.05, 3),     # ring groups of 8 warps
+    (24, 128, True, True, "landau", 0.05, 7),     # 3 strips on a 128-row ring
+    (16, 512, True, True, "landau", 0.05, 3),     # 10 strips on a 512-row ring
+    (30, 128, False, False, "landau", 0.05, 5),   # open y, edge strips on both edges
+    (21, 256, False, True, "pointflux", 0.03, 4), # complex hops on a periodic y axis
+    (19, 1024, True, True, "landau", 0.05, 2),    # a tall ring
     (40, 64, True, True, "pointflux", 0.03, 5),   # periodic 64 rows, complex hops: strips
     (41, 30, False, False, "landau", 0.05, 5),    # Ly < 64 open: lanes outside the lattice
     (33, 50, True, False, "landau", 0.05, 3),
