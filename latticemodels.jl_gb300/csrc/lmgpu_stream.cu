@@ -288,7 +288,9 @@ cheb_stream_c32_kernel(const FusedInst D, const StreamPairs SP, const float4* __
     constexpr bool ROT = LM_STREAM_ROTATE == 1 || (LM_STREAM_ROTATE == 2 && !UC);
     constexpr int NP = ROT ? 1 : 3;    // steps per unrolled loop body
     extern __shared__ float4 smem[];
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    // the warp index through a shuffle, so that the compiler sees it (and the item, column and
+    // ring-slot arithmetic derived from it) as warp-uniform and can keep that on the uniform pipe
+    const int warp = __shfl_sync(0xffffffffu, (int)(threadIdx.x >> 5), 0), lane = threadIdx.x & 31;
     float4* yring = smem + warp * stream_ring_f4(K);
     float4* xring = yring + YR * 32;
     const Geom g = D.g;
