@@ -117,6 +117,9 @@ def test_compensated_refusals(lm):
     # ComplexF64 kets and density matrices have no residual plane
     with pytest.raises(L.LMError):
         lm.KetBlock(ll, X, precision="c64", compensated=True)
+    dm = lm.DensityMatrix(ll, None, precision="c32")
+    with pytest.raises(L.LMError):
+        dm.set_compensation(True)
     # with the fused step switched off the per-order path refuses it
     Hl = lm.tightbinding_hamiltonian(ll, V, field=lm.LandauGauge(0.02))
     s.update_solver(Hl, 0.05)

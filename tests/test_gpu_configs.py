@@ -32,11 +32,13 @@ def phase_kets(N, M, seed, dtype):
 
 def test_precision_config_512(lm):
     """SquareLattice(512,512) periodic, Landau 0.01, Anderson U[-1,1], M = 1024 random-phase
-    kets, dt = 0.05, 200 steps: FP32 form against the FP64 run of the same seed.
+    kets, dt = 0.05, 200 steps: FP32 form (and its compensated state) against the FP64 run of the
+    same seed.
 
     The series truncation error of a step is coherent: it adds up linearly over the steps.  At
     tol 1e-7 (K = 5) it dominates the currents after 200 steps (~2e-6); at the FP32 default
-    tol 1e-9 (K = 6) every output stays within 1e-6."""
+    tol 1e-9 (K = 6) every output stays within 1e-6 (currents 7.5e-7); the compensated state
+    brings the currents to 2.6e-7 and the norms to 1e-12."""
     L, M, steps, dt = 512, 1024, 200, 0.05
     lat = lm.SquareLattice(L, L, boundaries={"axis1": True, "axis2": True})
     V = np.random.default_rng(7).uniform(-1, 1, size=lat.N)
@@ -60,22 +62,25 @@ def test_precision_config_512(lm):
     assert np.abs(s64.norms() / n0 - 1).max() <= 1e-12  # FP64: norms conserved to 1e-12
     del s64
     errs = {}
-    for tol in (1e-7, None):
-        s32 = lm.KetBlock(lat, X, precision="c32")
-        K = run(s32, tol)
+    for tol in (1e-7, None, "compensated"):
+        s32 = lm.KetBlock(lat, X, precision="c32", compensated=tol == "compensated")
+        K = run(s32, None if tol == "compensated" else tol)
         r32 = lm.localdensity(s32).values
         J32 = lm.DensityCurrents(H, s32).bond_values()
         err = {"K": K, "density": rel(r32, r64), "currents": rel(J32, J64),
                "norm_drift": float(np.abs(s32.norms() / n0 - 1).max()), "trace_drift": abs(s32.trace() - tr64) / tr64}
         errs[tol] = err
-        print(f"precision config (512^2, M=1024, 200 steps), c32 tol {tol or 1e-9:g}:", err)
+        print(f"precision config (512^2, M=1024, 200 steps), c32 {tol or 1e-9}:", err)
         del s32
     for tol, err in errs.items():
         assert err["density"] <= 1e-6, err
         assert err["norm_drift"] <= 1e-6, err
         assert err["trace_drift"] <= 1e-6, err
     assert errs[1e-7]["currents"] <= 5e-6, errs[1e-7]  # measured 2.3e-6: truncation at tol 1e-7
-    assert errs[None]["currents"] <= 1e-6, errs[None]  # measured 6.2e-7 at the default 1e-9
+    assert errs[None]["currents"] <= 1e-6, errs[None]  # measured 7.5e-7 at the default 1e-9
+    # the compensated form keeps the state's rounding: below the FP32 form on every output
+    c = errs["compensated"]
+    assert c["currents"] < errs[None]["currents"] and c["density"] < errs[None]["density"], errs
 
 
 def test_plain_config_256_properties(lm):
