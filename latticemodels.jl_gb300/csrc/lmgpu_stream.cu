@@ -358,20 +358,26 @@ cheb_stream_c32_kernel(const FusedInst D, const StreamPairs SP, const float4* __
 
         // residual words of my site pair in the ket's columns (output columns lie in [xa, xb))
         uint32_t* const rbase = CMP ? D.comp + ket * D.ld + (ys >= 0 ? ys : 0) : nullptr;
-        auto column = [&](int x) -> int {  // lattice column of x, or -1 outside an open axis
-            if (per_x) return x < 0 ? x + Lx : (x >= Lx ? x - Lx : x);
-            return (x >= 0 && x < Lx) ? x : -1;
-        };
         int stage_slot = 0;  // ring slot of the next staged column
+        // the next column to stage (stage() runs for idx = 0, 1, 2, ... in turn): its lattice
+        // column (wrapped once at most on a periodic axis: -K-2 <= s0 < Lx; outside [0, Lx) on an
+        // open one), the offset of my pair in it and its diagonal-pair record, advanced per call
+        int sxc = (per_x && s0 < 0) ? s0 + Lx : s0;
+        long long soff = (long long)sxc * Ly + ys;
+        long long doff = loff + (long long)(s0 + kPadL) * lstep;
         auto stage = [&](int idx) {
-            const int xs = column(s0 + idx);
-            const bool v = idx < nsteps && xs >= 0 && ys >= 0;
-            const float2* src = v ? xk + (long long)xs * Ly + ys : xk;
-            cp_async16(&xring[stage_slot * 32 + lane], src, v);
+            const bool v = idx < nsteps && sxc >= 0 && sxc < Lx && ys >= 0;
+            cp_async16(&xring[stage_slot * 32 + lane], v ? xk + soff : xk, v);
             if (UC) {  // the diagonal pair of the same column (padded records: always in range)
                 const bool vd = idx < nsteps;
-                cp_async8s(&dring[stage_slot * 32 + lane], vd ? pd + loff + (long long)(s0 + idx + kPadL) * lstep : pd,
-                           vd);
+                cp_async8s(&dring[stage_slot * 32 + lane], vd ? pd + doff : pd, vd);
+            }
+            ++sxc;
+            soff += Ly;
+            doff += lstep;
+            if (per_x && sxc == Lx) {
+                sxc = 0;
+                soff -= (long long)Lx * Ly;
             }
             if (CMP) {  // the residual words of the column that step idx completes (xo < xb: idx < nsteps)
                 const int xo = s0 + idx - K;
@@ -393,9 +399,22 @@ cheb_stream_c32_kernel(const FusedInst D, const StreamPairs SP, const float4* __
 #pragma unroll
             for (int cc = 0; cc < 3; ++cc) W[j][cc][0] = W[j][cc][1] = make_float2(0.f, 0.f);
 
-        int xslot = 0;  // idx mod XS
+        int xslot = 0;  // base mod XS: the ket-ring slot of column s0 + base
         int yslot = 0;  // idx mod YR
         for (int base = 0; base < nsteps; base += NP) {
+            // ket-ring slots of the columns s0 + base - K .. s0 + base + NP - 1 (xslot holds
+            // column s0 + base): column s - k of step p sits in xsl[p - k + K], so no order
+            // wraps a slot index of its own
+            int xsl[K + NP];
+            {
+                int v = xslot - K;
+                if (v < 0) v += XS;  // K < XS
+#pragma unroll
+                for (int j = 0; j < K + NP; ++j) {
+                    xsl[j] = v;
+                    v = v + 1 == XS ? 0 : v + 1;
+                }
+            }
 #pragma unroll
             for (int p = 0; p < NP; ++p) {
                 // window slots of the columns produced at this step, one and two steps ago
@@ -405,8 +424,8 @@ cheb_stream_c32_kernel(const FusedInst D, const StreamPairs SP, const float4* __
                 stage(idx + SPF);
                 cp_async_wait_s<SPF>();  // the group of column idx has landed
                 // ket ring slots of columns s-1 and s-2 (T_0 of order 1's x and x-1)
-                const int xs1 = xslot == 0 ? XS - 1 : xslot - 1;
-                const int xs2 = xs1 == 0 ? XS - 1 : xs1 - 1;
+                const int xs1 = xsl[p - 1 + K];
+                const int xs2 = xsl[p - 2 + K];
                 const int ro = loff + (s + kPadL) * lstep;  // records of column s
 #pragma unroll
                 for (int k = 1; k <= K; ++k) {
@@ -415,9 +434,7 @@ cheb_stream_c32_kernel(const FusedInst D, const StreamPairs SP, const float4* __
                     float2 hx[2], hxm[2], hy[2], hym[2];
                     float d[2];
                     if (UC) {
-                        int dsl = xslot - k;
-                        if (dsl < 0) dsl += XS;
-                        const float2 qd = dring[dsl * 32 + lane];
+                        const float2 qd = dring[xsl[p - k + K] * 32 + lane];
                         d[0] = qd.x;
                         d[1] = qd.y;
                         // MODE 3 reads its paired records in the stencil below
@@ -469,7 +486,7 @@ cheb_stream_c32_kernel(const FusedInst D, const StreamPairs SP, const float4* __
                     // T_{k-1} at x+1 (this step), x and x-1
                     float2 tp[2], tc[2], tm[2];
                     if (k == 1) {
-                        const float4 a = xring[xslot * 32 + lane], b = xring[xs1 * 32 + lane], c = xring[xs2 * 32 + lane];
+                        const float4 a = xring[xsl[p + K] * 32 + lane], b = xring[xs1 * 32 + lane], c = xring[xs2 * 32 + lane];
                         tp[0] = make_float2(a.x, a.y); tp[1] = make_float2(a.z, a.w);
                         tc[0] = make_float2(b.x, b.y); tc[1] = make_float2(b.z, b.w);
                         tm[0] = make_float2(c.x, c.y); tm[1] = make_float2(c.z, c.w);
@@ -578,9 +595,7 @@ cheb_stream_c32_kernel(const FusedInst D, const StreamPairs SP, const float4* __
                     if (gb == 1) {  // y = -i s_1 T1 + g0 T0 + g1 T1
                         float2 t0[2] = {tc[0], tc[1]};  // T_0(s - 1): order 1's centre column
                         if (k > 1) {
-                            int x0s = xslot - k;
-                            if (x0s < 0) x0s += XS;
-                            const float4 q0 = xring[x0s * 32 + lane];
+                            const float4 q0 = xring[xsl[p - k + K] * 32 + lane];
                             t0[0] = make_float2(q0.x, q0.y);
                             t0[1] = make_float2(q0.z, q0.w);
                         }
@@ -625,11 +640,9 @@ cheb_stream_c32_kernel(const FusedInst D, const StreamPairs SP, const float4* __
                     if (k < K) {
                         *yr = make_float4(yv[0].x, yv[0].y, yv[1].x, yv[1].y);
                     } else if (wr && x >= xa && x < xb) {
-                        const int xs = column(x);
+                        const int xs = x;  // an output column lies in [xa, xb), inside the lattice
                         // out = e^{-ib dt} y + a0 x (a0 = e^{-ib dt} c_0): the small terms first
-                        int xo = xslot - K;
-                        if (xo < 0) xo += XS;
-                        const float4 q = xring[xo * 32 + lane];
+                        const float4 q = xring[xsl[p] * 32 + lane];
                         const float2 x0[2] = {make_float2(q.x, q.y), make_float2(q.z, q.w)};
                         const float ph_re = D.ph_re, ph_im = D.ph_im, a0_re = D.a0_re, a0_im = D.a0_im;
                         float2 o[2];
@@ -668,7 +681,6 @@ cheb_stream_c32_kernel(const FusedInst D, const StreamPairs SP, const float4* __
                         *reinterpret_cast<float4*>(outk + (long long)xs * Ly + ys) = make_float4(o[0].x, o[0].y, o[1].x, o[1].y);
                     }
                 }
-                xslot = xslot + 1 == XS ? 0 : xslot + 1;
                 yslot = yslot + 1 == YR ? 0 : yslot + 1;
                 if (ROT) {
 #pragma unroll
@@ -678,6 +690,8 @@ cheb_stream_c32_kernel(const FusedInst D, const StreamPairs SP, const float4* __
                     }
                 }
             }
+            xslot += NP;  // NP < XS
+            if (xslot >= XS) xslot -= XS;
         }
         cp_async_wait_s<0>();
         __syncwarp();  // the next item reuses this warp's rings
