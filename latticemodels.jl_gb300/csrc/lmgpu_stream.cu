@@ -400,6 +400,7 @@ cheb_stream_c32_kernel(const FusedInst D, const StreamPairs SP, const float4* __
             for (int cc = 0; cc < 3; ++cc) W[j][cc][0] = W[j][cc][1] = make_float2(0.f, 0.f);
 
         int xslot = 0;  // base mod XS: the ket-ring slot of column s0 + base
+        long long xoff = (long long)(s0 - K) * Ly;  // column offset of this step's output column s - K
         int yslot = 0;  // idx mod YR
         for (int base = 0; base < nsteps; base += NP) {
             // ket-ring slots of the columns s0 + base - K .. s0 + base + NP - 1 (xslot holds
@@ -421,6 +422,8 @@ cheb_stream_c32_kernel(const FusedInst D, const StreamPairs SP, const float4* __
                 const int c0 = ROT ? 0 : p, c1 = ROT ? 1 : (p + 2) % 3, c2 = ROT ? 2 : (p + 1) % 3;
                 const int idx = base + p;
                 const int s = s0 + idx;
+                // the column records of column s (column s - k sits k records before)
+                const float4* const cs = ctab + (s + kPadL) * stream_crec_f4(MODE);
                 stage(idx + SPF);
                 cp_async_wait_s<SPF>();  // the group of column idx has landed
                 // ket ring slots of columns s-1 and s-2 (T_0 of order 1's x and x-1)
@@ -438,7 +441,7 @@ cheb_stream_c32_kernel(const FusedInst D, const StreamPairs SP, const float4* __
                         d[0] = qd.x;
                         d[1] = qd.y;
                         // MODE 3 reads its paired records in the stencil below
-                        const float4 qc = PAIRED ? make_float4(0.f, 0.f, 0.f, 0.f) : ctab[s - k + kPadL];
+                        const float4 qc = PAIRED ? make_float4(0.f, 0.f, 0.f, 0.f) : cs[-k];
                         hx[0] = hx[1] = make_float2(qc.x, 0.f);
                         hxm[0] = hxm[1] = make_float2(qc.y, 0.f);
                         hy[0] = make_float2(qc.z, qc.w);
@@ -506,7 +509,7 @@ cheb_stream_c32_kernel(const FusedInst D, const StreamPairs SP, const float4* __
                     float2 tk[2];
                     if (PAIRED) {
                         // signed records of column x: {h hx, h hx, h hxm, h hxm}, {h hy.re, h hy.re, h hy.im, 0}
-                        const float4* cr = ctab + 4 * (s - k + kPadL) + ((k & 1) ? 0 : 2);
+                        const float4* cr = cs - 4 * k + ((k & 1) ? 0 : 2);
                         const float4 r0 = cr[0], r1 = cr[1];
                         const float2 px = make_float2(r0.x, r0.y), pxm = make_float2(r0.z, r0.w);
                         const float2 py = make_float2(r1.x, r1.y);
@@ -640,7 +643,7 @@ cheb_stream_c32_kernel(const FusedInst D, const StreamPairs SP, const float4* __
                     if (k < K) {
                         *yr = make_float4(yv[0].x, yv[0].y, yv[1].x, yv[1].y);
                     } else if (wr && x >= xa && x < xb) {
-                        const int xs = x;  // an output column lies in [xa, xb), inside the lattice
+                        // x lies in [xa, xb), inside the lattice: its offset is xoff, unwrapped
                         // out = e^{-ib dt} y + a0 x (a0 = e^{-ib dt} c_0): the small terms first
                         const float4 q = xring[xsl[p] * 32 + lane];
                         const float2 x0[2] = {make_float2(q.x, q.y), make_float2(q.z, q.w)};
@@ -648,7 +651,7 @@ cheb_stream_c32_kernel(const FusedInst D, const StreamPairs SP, const float4* __
                         float2 o[2];
                         if (CMP) {
                             // the two sites' residuals, staged with the ket columns
-                            uint2* lp = reinterpret_cast<uint2*>(rbase + (long long)x * Ly);
+                            uint2* lp = reinterpret_cast<uint2*>(rbase + xoff);
                             const uint2 lq = rring[(idx & 3) * 32 + lane];
                             const float2 a1 = make_float2(a0_re, a0_re), a1n = make_float2(-a0_re, -a0_re);
                             const float2 a2 = make_float2(-a0_im, a0_im);
@@ -678,10 +681,11 @@ cheb_stream_c32_kernel(const FusedInst D, const StreamPairs SP, const float4* __
                                 o[j].y = fmaf(a0_re, x0[j].y, r.y);
                             }
                         }
-                        *reinterpret_cast<float4*>(outk + (long long)xs * Ly + ys) = make_float4(o[0].x, o[0].y, o[1].x, o[1].y);
+                        *reinterpret_cast<float4*>(outk + xoff + ys) = make_float4(o[0].x, o[0].y, o[1].x, o[1].y);
                     }
                 }
                 yslot = yslot + 1 == YR ? 0 : yslot + 1;
+                xoff += Ly;
                 if (ROT) {
 #pragma unroll
                     for (int j = 1; j < K; ++j) {
