@@ -937,6 +937,9 @@ def main():
             dist.destroy_process_group()
         return 0
     ms32_plain = ms32
+    # per-launch time of the step kernel of each FP32 form (its event-timed pass)
+    launch_ms_plain = order_ms / max(order_launches // max(K32, 1), 1)
+    launch_ms_comp = order_ms_c / max(order_launches_c // max(K32, 1), 1)
     value_plain32 = world * M * args.steps / (ms32 / 1000.0)
     value_comp = world * M * args.steps / (ms32c / 1000.0)
     if use_comp:
@@ -993,9 +996,10 @@ def main():
         "rel_err_vs_fp64": err,
         "fp32_forms": {
             "plain_c32": {"value": value_plain32, "ms_per_step": ms32_plain / args.steps,
-                          "rel_err_vs_fp64": err_plain32},
+                          "ms_per_launch": launch_ms_plain, "rel_err_vs_fp64": err_plain32},
             "compensated_c32": {"value": value_comp, "ms_per_step": ms32c / args.steps,
-                                "rel_err_vs_fp64": err_comp, "streamed": streamed_c},
+                                "ms_per_launch": launch_ms_comp, "rel_err_vs_fp64": err_comp,
+                                "streamed": streamed_c},
         },
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic,
