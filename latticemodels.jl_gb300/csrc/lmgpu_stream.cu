@@ -365,6 +365,7 @@ cheb_stream_c32_kernel(const FusedInst D, const StreamPairs SP, const float4* __
         int sxc = (per_x && s0 < 0) ? s0 + Lx : s0;
         long long soff = (long long)sxc * Ly + ys;
         long long doff = loff + (long long)(s0 + kPadL) * lstep;
+        long long roff = (long long)(s0 - K) * Ly;  // compensated blocks: residual offset of column s0 - K
         auto stage = [&](int idx) {
             const bool v = idx < nsteps && sxc >= 0 && sxc < Lx && ys >= 0;
             cp_async16(&xring[stage_slot * 32 + lane], v ? xk + soff : xk, v);
@@ -382,8 +383,8 @@ cheb_stream_c32_kernel(const FusedInst D, const StreamPairs SP, const float4* __
             if (CMP) {  // the residual words of the column that step idx completes (xo < xb: idx < nsteps)
                 const int xo = s0 + idx - K;
                 const bool vr = wr && xo >= xa && xo < xb;
-                cp_async8s(reinterpret_cast<float2*>(&rring[(idx & 3) * 32 + lane]),
-                           vr ? rbase + (long long)xo * Ly : D.comp, vr);
+                cp_async8s(reinterpret_cast<float2*>(&rring[(idx & 3) * 32 + lane]), vr ? rbase + roff : D.comp, vr);
+                roff += Ly;  // the next call stages column xo + 1 (its offset unwrapped: only [xa, xb) is read)
             }
             cp_async_commit_s();
             stage_slot = stage_slot + 1 == XS ? 0 : stage_slot + 1;
