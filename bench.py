@@ -688,6 +688,85 @@ def run_general_workload(args):
     return 0
 
 
+REFBENCH_WORKLOAD = ("the reference's evolution benchmarks (benchmarks/benchmark_evolution_const.jl, "
+                     "benchmark_evolution_dynamic.jl, model benchmarks/models.jl:3-12) on HoneycombLattice(224,224) "
+                     "(N = 100,352; a parallelogram patch standing in for the Circle shape), t1 = -2.8, "
+                     "pn-junction potential 0.2 inside r/2, SymmetricGauge(3.0 x 1.519e-3) constant or ramped as "
+                     "3.0 min(t/5, 1), one ket, t = 0:0.1:10 (101 moments), localdensity at every moment, ComplexF64")
+
+
+def run_refbench_workload(args):
+    """The reference's own evolution benchmark loop: one ket of a ~1e5-site graphene patch evolved
+    over t = 0:0.1:10 with localdensity at every moment, for a constant H and for a field ramp;
+    timed on the device from the host ket to the last density, and the oracle's Krylov port of
+    KrylovKitExp (one host thread: one ket) timed on the constant-H loop.  The reference's
+    starting state is the ground state; a seeded random ket stands in (the cost does not depend
+    on it)."""
+    import torch
+    import lmgpu
+    from oracle import krylov, lm_oracle as o
+    ctx = lmgpu.default_context()
+    ext = torch.cuda.ExternalStream(ctx.stream_ptr(), device=torch.device("cuda", 0))
+    a = b = 224
+    lat = lmgpu.HoneycombLattice(a, b)
+    N = lat.N
+    xy = lat.coords()
+    c = xy.mean(axis=0)
+    r = math.sqrt(N * (math.sqrt(3) / 4) / math.pi)  # radius of a disk of N sites (area sqrt(3)/4 per site)
+    V = np.where(((xy - c) ** 2).sum(axis=1) < (r / 2) ** 2, 0.2, 0.0)
+    B0 = 3.0 * 1.519e-3
+    times = [0.1 * k for k in range(101)]
+    rng = np.random.default_rng(SEED + 11)
+    psi = rng.standard_normal(N) + 1j * rng.standard_normal(N)
+    psi /= np.linalg.norm(psi)
+    h_const = lmgpu.tightbinding_hamiltonian(lat, V, t1=-2.8, field=lmgpu.SymmetricGauge(B0))
+    h_dyn = lambda t: lmgpu.tightbinding_hamiltonian(lat, V, t1=-2.8,
+                                                      field=lmgpu.SymmetricGauge(B0 * min(t / 5.0, 1.0)))
+
+    def run(h):
+        ev = lmgpu.Evolution(lmgpu.ChebyshevGPU(), h, lmgpu.Ket(lat, psi))
+        (ts,) = lmgpu.timesequences([lmgpu.moment_density], ev(times), nslots=8)
+        return ts
+
+    for h in (h_const, h_dyn):  # warm-up: builds, tables, rings
+        run(h)
+    res = {}
+    for name, h in (("constant", h_const), ("dynamic", h_dyn)):
+        ms = []
+        for _ in range(max(args.steps, 1)):
+            ctx.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(ext)
+            ts = run(h)
+            e1.record(ext)
+            e1.synchronize()
+            assert len(ts) == len(times)
+            ms.append(e0.elapsed_time(e1))
+        res[name] = {"ms_per_run": float(np.median(ms)), "runs": len(ms),
+                     "moments_per_s": len(times) / (float(np.median(ms)) / 1000.0)}
+    # the oracle's Krylov port on the same constant-H loop (its matrix from the oracle's
+    # restatement of the lattice and field)
+    Ho, _ = o.honeycomb_hamiltonian(a, b, t1=-2.8, field=o.SymmetricGauge(B0), onsite=V)
+    csr = krylov.CSR(Ho)
+    X = psi.reshape(-1, 1).astype(np.complex128)
+    t0 = time.perf_counter()
+    for _ in range(len(times) - 1):
+        X = krylov.krylov_expv_block(csr, 0.1, X, tol=1e-12, kdim=30, nthreads=1)
+        _ = np.abs(X[:, 0]) ** 2
+    cpu_ms = (time.perf_counter() - t0) * 1000.0
+    line = {"metric": "ms per run of the reference's evolution benchmark loop (101 moments)",
+            "value": res["constant"]["ms_per_run"], "unit": "ms", "n_gpus": 1, "steps": args.steps,
+            "higher_is_better": False, "dtype": "c64", "data": "synthetic (seeded random ket; the patch stands "
+            "in for the Circle shape)", "config": {"workload": REFBENCH_WORKLOAD, "N": N},
+            "gpu": res, "cpu_port_constant": {"ms_per_run": cpu_ms, "cores": 1, "kind": "port",
+                                             "sample": "the whole 100-step constant-H loop, Lanczos exponentiate "
+                                                       "(tol 1e-12, krylovdim 30) and |psi|^2 per step"},
+            "gpu_over_cpu_constant": cpu_ms / res["constant"]["ms_per_run"]}
+    print(json.dumps(line))
+    return 0
+
+
 def run_readouts_workload(args):
     """The per-moment readouts of the kets workload, c32: localdensity and DensityCurrents on
     every bond, each through the readout ring (kernel + asynchronous download), timed with CUDA
@@ -745,11 +824,12 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--kets", type=int, default=M_KETS)
     ap.add_argument("--workload", default="kets",
-                    choices=["kets", "batch", "adjoint", "kpm", "densitymatrix", "general", "readouts"],
+                    choices=["kets", "batch", "adjoint", "kpm", "densitymatrix", "general", "readouts", "refbench"],
                     help="kets: the 256^2 ket-block workload (default); batch: 512 uneven dense-P lattices; "
                          "adjoint: loss_and_grad of the 64^2 differentiation workload; kpm: DOS moments; "
                          "densitymatrix: P_0 at T > 0, Chebyshev vs eigensolver; general: honeycomb via ELL; "
-                         "readouts: localdensity and DensityCurrents of the kets workload")
+                         "readouts: localdensity and DensityCurrents of the kets workload; refbench: the "
+                         "reference's own evolution benchmark loop (one graphene ket, 101 moments)")
     ap.add_argument("--instances", type=int, default=512)
     ap.add_argument("--batch-instances", type=int, default=64,
                     help="lattices of the batch sub-record of the default line (0: none)")
@@ -786,6 +866,8 @@ def main():
         return run_densitymatrix_workload(args)
     if args.workload == "general":
         return run_general_workload(args)
+    if args.workload == "refbench":
+        return run_refbench_workload(args)
     if args.workload == "readouts":
         return run_readouts_workload(args)
 

@@ -255,8 +255,11 @@ class LatticeHamiltonian(SparseHamiltonian):
                 raise ValueError("on-site term must have one value per site")
             onsite = v
         self.onsite = onsite
-        src, dst, _, _ = lattice.bonds()
-        self.colptr, self.rowval = _pattern(lattice.N, src, dst)
+        pat = getattr(lattice, "_csc_pattern", None)
+        if pat is None:  # built once per lattice: h(t) makes a new Hamiltonian every step
+            src, dst, _, _ = lattice.bonds()
+            pat = lattice._csc_pattern = _pattern(lattice.N, src, dst)
+        self.colptr, self.rowval = pat
         self.nzval = None
         self._pattern = ("bonds",) + lattice.key()
 
