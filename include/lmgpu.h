@@ -162,9 +162,10 @@ int lm_state_renormalize(lm_state *st, const double *target_norms);
  * pair with error-free FP32 transformations (Dekker TwoProd via fmaf, Knuth TwoSum).  The
  * state then carries about 32 significant bits from step to step, so the rounding walk of
  * long FP32 runs (the 400-step current) shrinks, at the cost of 8 more bytes per site-ket of
- * traffic (the residual read and written once per step).  ComplexF32 ket blocks on square lattices
- * whose columns are uniform (Landau gauge, no twist along y) stepped by lm_solver_step
- * only; other paths return LM_ERR_NOTSUP.  Uploads clear the residual; copies carry it;
+ * traffic (the residual read and written once per step).  ComplexF32 ket blocks stepped by
+ * lm_solver_step through the x-streaming form: square lattices with Ly even and Lx >= 2K + 3
+ * (K <= 5 with complex x-hops) and honeycomb lattices in the brick layout; other paths return
+ * LM_ERR_NOTSUP.  Uploads clear the residual; copies carry it;
  * norms and renormalize use value + residual.  enable == 0 drops it. */
 int lm_state_set_compensation(lm_state *st, int enable);
 

@@ -967,8 +967,8 @@ static int cheb_apply(lm_solver* s, const Geom& g, int precision, int site_fast,
         }
         if (comp && !(spack && stream_comp_supported(g, K, mode)))
             return set_err(ctx, LM_ERR_NOTSUP,
-                           "lm_solver_step: a compensated state needs the x-streaming form with uniform columns "
-                           "(Landau gauge, no twist along y)");
+                           "lm_solver_step: a compensated state needs the x-streaming form (Ly even, Lx >= 2K + 3, "
+                           "K <= 6; K <= 5 with complex x-hops)");
         CUDA_TRY(ctx, launch_cheb_fused_c32(ctx, g, (const float2*)hop2, (const float*)diag2, (const float2*)S,
                                             (float2*)A, ld, m, K, xr, s->coef.data(), pr, pi, spack, mode, comp),
                  "fused chebyshev step");

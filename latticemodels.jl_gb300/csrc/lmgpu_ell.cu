@@ -228,8 +228,6 @@ static int ell_apply(lm_solver* s, int precision, int site_fast, int conj, void*
 int ell_solver_step(lm_solver* s, lm_state* st) {
     lm_ctx* ctx = s->ctx;
     CHECK_ARG(ctx, st->n == s->ell->n, "lm_solver_step: state size does not match the Hamiltonian");
-    if (st->d_lo)
-        return set_err(ctx, LM_ERR_NOTSUP, "lm_solver_step: compensated states run on square-lattice Hamiltonians only");
     cudaSetDevice(ctx->device);
     {
         int rc0 = ensure_scratch(st);
@@ -253,7 +251,8 @@ int ell_solver_step(lm_solver* s, lm_state* st) {
         g.N = h->n;
         g.per_x = h->brick_px;
         g.per_y = h->brick_py;
-        if (stream_supported(g, s->K, 4, st->d_data, st->d_a, st->ld)) {
+        if (stream_supported(g, s->K, 4, st->d_data, st->d_a, st->ld) &&
+            (!st->d_lo || stream_comp_supported(g, s->K, 4))) {
             int rc0 = ensure_brick_pack(s, g, h->d_bmap);
             if (rc0 != LM_OK) return rc0;
             cudaEvent_t t0 = nullptr, t1 = nullptr;
@@ -264,7 +263,7 @@ int ell_solver_step(lm_solver* s, lm_state* st) {
             }
             CUDA_TRY(ctx, launch_cheb_fused_c32(ctx, g, nullptr, nullptr, (const float2*)st->d_data, (float2*)st->d_a,
                                                 st->ld, st->m, s->K, false, s->coef.data(), s->phase_re, s->phase_im,
-                                                s->d_spack, 4),
+                                                s->d_spack, 4, st->d_lo),
                      "honeycomb x-streaming step");
             if (ctx->timing) {
                 CUDA_TRY(ctx, cudaEventRecord(t1, ctx->stream), "cudaEventRecord");
@@ -275,6 +274,10 @@ int ell_solver_step(lm_solver* s, lm_state* st) {
             return LM_OK;
         }
     }
+    if (st->d_lo)
+        return set_err(ctx, LM_ERR_NOTSUP,
+                       "lm_solver_step: a compensated state on a general Hamiltonian needs the honeycomb brick layout "
+                       "and the x-streaming form");
     int rc = ell_apply(s, st->precision, 1, 0, st->d_data, st->d_a, st->d_y, st->ld, st->m, &where);
     if (rc != LM_OK) return rc;
     if (where == 1) std::swap(st->d_data, st->d_a);

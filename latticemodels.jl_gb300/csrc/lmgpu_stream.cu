@@ -60,13 +60,15 @@ namespace lmgpu {
 
 namespace {
 constexpr int SW = LM_STREAM_WARPS;
-// The brick stencil at K = 6 needs more than 128 registers a thread (its three-column windows of
-// complex values): it runs 12 warps per CTA (up to 170 registers).
+// The per-site-plane modes need more than 128 registers a thread at their largest orders (the
+// brick stencil at K = 6; the compensated output on top of MODE 0/1 at K >= 5): they run 12 warps
+// per CTA (up to 170 registers).
 #ifndef LM_STREAM_WARPS_BRICK6
 #define LM_STREAM_WARPS_BRICK6 12
 #endif
-__host__ __device__ constexpr int stream_warps(int K, int mode) {
-    return (mode == 4 && K >= 6) ? LM_STREAM_WARPS_BRICK6 : SW;
+__host__ __device__ constexpr int stream_warps(int K, int mode, bool cmp = false) {
+    return ((mode == 4 && K >= 6) || (cmp && (mode == 0 || mode == 1 || mode == 4) && K >= 5)) ? LM_STREAM_WARPS_BRICK6
+                                                                                               : SW;
 }
 constexpr int SR = 64;       // strip width along y: 32 lanes x 2 sites
 constexpr int SPF = 3;       // columns of the ket staged ahead
@@ -94,6 +96,11 @@ __host__ __device__ constexpr int stream_crec_f4(int mode) { return mode == 3 ? 
 // the columns that the next SPF + 1 steps complete, staged with the ket columns.
 constexpr int kResRing = SPF + 1;
 static_assert(kResRing == 4, "the residual ring is indexed with & 3");
+// float4 offset, in a CTA's dynamic shared memory, of what follows the rings and (uniform-column
+// modes) the diagonal-pair rings and column records: the residual rings of a compensated block
+__host__ __device__ constexpr int stream_base_f4(int K, int mode, int Xp, int nw) {
+    return nw * stream_ring_f4(K) + ((mode == 2 || mode == 3) ? nw * stream_dring_f4(K) + Xp * stream_crec_f4(mode) : 0);
+}
 }  // namespace
 
 // Accumulator coefficients of the paired form (MODE 3): {sigma_k s_k, sigma_k s_k}.
@@ -265,7 +272,7 @@ __global__ void stream_pack_kernel(const Geom g, const float2* __restrict__ hop2
 // residual (the plane, in place), so the state's own FP32 rounding does not accumulate from
 // step to step.
 template <int K, int MODE, bool CMP>
-__global__ void __launch_bounds__(stream_warps(K, MODE) * 32, 1)
+__global__ void __launch_bounds__(stream_warps(K, MODE, CMP) * 32, 1)
 cheb_stream_c32_kernel(const FusedInst D, const StreamPairs SP, const float4* __restrict__ pk,
                        const float2* __restrict__ pd, const float4* __restrict__ pc, int npair, long long plane,
                        int nty, long long ncols, long long nwarps) {
@@ -302,10 +309,10 @@ cheb_stream_c32_kernel(const FusedInst D, const StreamPairs SP, const float4* __
     const float4* __restrict__ P3 = pk + 3 * plane;
     const float4* __restrict__ P4 = pk + 4 * plane;
     // uniform columns: diagonal-pair ring per warp, column records per CTA
-    constexpr int NW = stream_warps(K, MODE);
+    constexpr int NW = stream_warps(K, MODE, CMP);
     float2* dring = reinterpret_cast<float2*>(smem + NW * stream_ring_f4(K)) + warp * XS * 32;
     float4* ctab = smem + NW * (stream_ring_f4(K) + stream_dring_f4(K));
-    uint2* rring = reinterpret_cast<uint2*>(ctab + ((int)D.g.Lx + kPadL + kPadR) * stream_crec_f4(MODE)) +
+    uint2* rring = reinterpret_cast<uint2*>(smem + stream_base_f4(K, MODE, (int)D.g.Lx + kPadL + kPadR, NW)) +
                    warp * kResRing * 32;
     if (UC) {
         const int Xp = Lx + kPadL + kPadR;
@@ -837,14 +844,15 @@ int ensure_brick_pack(lm_solver* s, const Geom& g, const int* d_bmap) {
 
 static int stream_smem_bytes(int K, int mode, int Xp, bool cmp = false) {
     const bool uc = mode == 2 || mode == 3;
-    const int nw = stream_warps(K, mode);
+    const int nw = stream_warps(K, mode, cmp);
     return nw * stream_ring_f4(K) * 16 + (uc ? nw * stream_dring_f4(K) * 16 + Xp * 16 * stream_crec_f4(mode) : 0) +
            (cmp ? nw * kResRing * 32 * 8 : 0);
 }
 
 bool stream_comp_supported(const Geom& g, int K, int mode) {
-    const int m = (mode == 2 && g.per_y) ? 3 : mode;
-    return (m == 2 || m == 3) && stream_smem_bytes(K, m, (int)g.Lx + kPadL + kPadR, true) <= kStreamSmemMax;
+    int m = (mode == 2 && g.per_y) ? 3 : mode;
+    if ((m == 2 || m == 3) && stream_smem_bytes(K, m, (int)g.Lx + kPadL + kPadR) > kStreamSmemMax) m = 1;  // as launched
+    return stream_smem_bytes(K, m, (int)g.Lx + kPadL + kPadR, true) <= kStreamSmemMax;
 }
 
 template <int MODE, bool CMP>
@@ -866,7 +874,7 @@ static cudaError_t launch_stream_k(lm_ctx* ctx, int K, int grid, const FusedInst
             if (e != cudaSuccess) return e;                                                                      \
             attr |= bit;                                                                                         \
         }                                                                                                        \
-        cheb_stream_c32_kernel<KK, MODE, CMP><<<(unsigned)grid, stream_warps(KK, MODE) * 32, smem, ctx->stream>>>( \
+        cheb_stream_c32_kernel<KK, MODE, CMP><<<(unsigned)grid, stream_warps(KK, MODE, CMP) * 32, smem, ctx->stream>>>( \
             d, sp, pp.pk, pp.pd, pp.pc, npair, plane, nty, ncols, nwarps);                                           \
         return cudaGetLastError();                                                                               \
     }
@@ -886,7 +894,7 @@ cudaError_t launch_cheb_stream_c32(lm_ctx* ctx, const FusedInst& d, int K, int m
     // for every item it touches)
     int m = (mode == 2 && d.g.per_y) ? 3 : mode;
     if ((m == 2 || m == 3) && stream_smem_bytes(K, m, (int)d.g.Lx + kPadL + kPadR) > kStreamSmemMax) m = 1;  // very long x
-    const int nw = stream_warps(K, m);
+    const int nw = stream_warps(K, m, d.comp != nullptr);
     const long long slots = (long long)(ctx->sm_count > 0 ? ctx->sm_count : 152) * nw;
     const long long nwarps = std::max<long long>(1, std::min<long long>(slots, ncols / (8 * K)));
     const int grid = (int)((nwarps + nw - 1) / nw);
@@ -896,10 +904,12 @@ cudaError_t launch_cheb_stream_c32(lm_ctx* ctx, const FusedInst& d, int K, int m
         sp.s2[k] = make_float2(v, v);
     }
     cudaError_t e;
-    if (d.comp) {  // compensated block: the uniform-column modes only (checked by the caller)
-        if (m != 2 && m != 3) return cudaErrorNotSupported;
-        e = m == 3 ? launch_stream_k<3, true>(ctx, K, grid, d, sp, spack, (int)nty, ncols, nwarps)
-                   : launch_stream_k<2, true>(ctx, K, grid, d, sp, spack, (int)nty, ncols, nwarps);
+    if (d.comp) {  // compensated block (stream_comp_supported checked by the caller)
+        e = m == 4   ? launch_stream_k<4, true>(ctx, K, grid, d, sp, spack, (int)nty, ncols, nwarps)
+            : m == 3 ? launch_stream_k<3, true>(ctx, K, grid, d, sp, spack, (int)nty, ncols, nwarps)
+            : m == 2 ? launch_stream_k<2, true>(ctx, K, grid, d, sp, spack, (int)nty, ncols, nwarps)
+            : m == 1 ? launch_stream_k<1, true>(ctx, K, grid, d, sp, spack, (int)nty, ncols, nwarps)
+                     : launch_stream_k<0, true>(ctx, K, grid, d, sp, spack, (int)nty, ncols, nwarps);
     } else {
         e = m == 4   ? launch_stream_k<4, false>(ctx, K, grid, d, sp, spack, (int)nty, ncols, nwarps)
             : m == 3 ? launch_stream_k<3, false>(ctx, K, grid, d, sp, spack, (int)nty, ncols, nwarps)

@@ -772,7 +772,7 @@ gpu_renormalize!(st::DeviceState, target::AbstractVector{<:Real}) =
     check(ccall((:lm_state_renormalize, LIB), Cint, (Ptr{Cvoid}, Ptr{Float64}), st.handle, Vector{Float64}(target)),
           st.lat.ctx.handle)
 # Compensated ComplexF32 kets: keep each amplitude's rounding residual so that long FP32 runs
-# do not accumulate the state's rounding (uniform-column lattices: Landau gauge, no y twist)
+# do not accumulate the state's rounding (states the x-streaming step takes)
 gpu_compensate!(st::DeviceState, enable::Bool=true) =
     check(ccall((:lm_state_set_compensation, LIB), Cint, (Ptr{Cvoid}, Cint), st.handle, Cint(enable)),
           st.lat.ctx.handle)

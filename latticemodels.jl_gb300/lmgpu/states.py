@@ -54,11 +54,12 @@ class DeviceState:
             self.set_weights(weights)
 
     def set_compensation(self, enable: bool = True):
-        """Keep the FP32 rounding residual of every amplitude beside it (ComplexF32 kets on
-        square lattices with uniform columns): the fused step then adds each Chebyshev order
-        to the (value, residual) pair with error-free transformations, so a long FP32 run
-        accumulates far less rounding.  Norms and renormalize read value + residual; the
-        readouts and to_numpy read the FP32 value."""
+        """Keep the FP32 rounding residual of every amplitude beside it (ComplexF32 kets that
+        the x-streaming step takes: square lattices with Ly even and Lx >= 2K + 3, honeycomb
+        lattices in the brick layout): the step then forms each new amplitude from the (value,
+        residual) pair with error-free transformations, so a long FP32 run accumulates far less
+        rounding.  Norms and renormalize read value + residual; the readouts and to_numpy read
+        the FP32 value."""
         self.ctx.check(self.ctx.lib.lm_state_set_compensation(self.handle, int(bool(enable))))
         self.compensated = bool(enable)
         return self

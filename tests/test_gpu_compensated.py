@@ -35,19 +35,28 @@ def pair(lm, Lx, Ly, per):
 
 
 CASES = [
-    (32, 32, True, True, 0.05, 4),
-    (40, 18, True, False, 0.02, 3),    # open y: uniform columns without the y seam
-    (17, 64, False, True, 0.05, 5),    # open x
+    (32, 32, True, True, 0.05, 4, "landau"),
+    (40, 18, True, False, 0.02, 3, "landau"),    # open y: uniform columns without the y seam
+    (17, 64, False, True, 0.05, 5, "landau"),    # open x
+    (30, 40, False, False, 0.02, 3, "pointflux"),  # complex x-hops (per-site planes, K <= 5)
+    (26, 32, True, True, 0.02, 2, "symmetric"),    # complex hops on both axes, periodic
 ]
 
 
-@pytest.mark.parametrize("case", CASES, ids=[f"{c[0]}x{c[1]}" for c in CASES])
+@pytest.mark.parametrize("case", CASES, ids=[f"{c[0]}x{c[1]}-{c[6]}" for c in CASES])
 def test_compensated_step_vs_oracle(lm, case):
-    Lx, Ly, px, py, dt, M = case
+    Lx, Ly, px, py, dt, M, fk = case
     ol, ll = pair(lm, Lx, Ly, (px, py))
     V = o.anderson_disorder(ol.N, 2.0, Lx + Ly)
-    Ho = o.tightbinding_hamiltonian(ol, field=o.LandauGauge(0.02), onsite=V)
-    Hl = lm.tightbinding_hamiltonian(ll, V, field=lm.LandauGauge(0.02))
+    if fk == "landau":
+        fo, fl = o.LandauGauge(0.02), lm.LandauGauge(0.02)
+    elif fk == "symmetric":
+        fo, fl = o.SymmetricGauge(0.015), lm.SymmetricGauge(0.015)
+    else:
+        pt = (Lx / 2 + 0.5, Ly / 2 + 0.5)
+        fo, fl = o.PointFlux(0.3, pt), lm.PointFlux(0.3, pt)
+    Ho = o.tightbinding_hamiltonian(ol, field=fo, onsite=V)
+    Hl = lm.tightbinding_hamiltonian(ll, V, field=fl)
     X = o.random_kets(ol.N, M, 5)
     ctx = lm.default_context()
     out = {}
@@ -69,6 +78,32 @@ def test_compensated_step_vs_oracle(lm, case):
     assert e_plain <= 3e-6, e_plain
     # the FP64 norms of value + residual hold the unitary evolution's norms closer than FP32
     assert np.abs(out[True].norms() - np.linalg.norm(X, axis=0)).max() <= 1e-7
+
+
+def test_compensated_honeycomb_brick(lm):
+    """A compensated ket block on a HoneycombLattice: the brick layout of the streaming kernel
+    carries the residual; against the oracle's exact exponent, and below the FP32 form's error
+    over 60 steps."""
+    a, b, dt, M, steps = 20, 16, 0.05, 3, 60
+    lat = lm.HoneycombLattice(a, b, boundaries={"axis1": True, "axis2": True})
+    V = o.anderson_disorder(lat.N, 1.0, 13)
+    Ho = o.honeycomb_hamiltonian_periodic(a, b, field=o.LandauGauge(0.03), onsite=V)[0]
+    H = lm.tightbinding_hamiltonian(lat, V, field=lm.LandauGauge(0.03))
+    X = o.random_kets(lat.N, M, 14)
+    ctx = lm.default_context()
+    errs = {}
+    for comp in (False, True):
+        st = lm.KetBlock(lat, X, precision="c32", compensated=comp)
+        s = lm.ChebyshevGPU()
+        s.update_solver(H, dt)
+        n0 = ctx.stream_launches()
+        for _ in range(steps):
+            s.step(st)
+        assert ctx.stream_launches() - n0 == steps
+        errs[comp] = st.to_numpy().astype(np.complex128)
+    Y = o.expm_multiply(Ho, dt * steps, X)
+    e_plain, e_comp = rel(errs[False], Y), rel(errs[True], Y)
+    assert e_comp <= 3e-6 and e_comp < e_plain, (e_plain, e_comp)
 
 
 def test_compensated_copy_upload_renormalize(lm):
@@ -106,14 +141,17 @@ def test_compensated_refusals(lm):
     ol, ll = pair(lm, 24, 24, (True, True))
     V = o.anderson_disorder(ol.N, 1.0, 3)
     X = o.random_kets(ol.N, 2, 4)
-    # non-uniform columns (PointFlux): the streaming kernel has no compensated form
-    Hp = lm.tightbinding_hamiltonian(ll, V, field=lm.PointFlux(0.2, (12.5, 12.5)))
-    st = lm.KetBlock(ll, X, precision="c32", compensated=True)
+    # an odd number of rows: no x-streaming form, so no compensated step
+    ol3, ll3 = pair(lm, 24, 25, (True, True))
+    V3 = o.anderson_disorder(ol3.N, 1.0, 3)
+    H3 = lm.tightbinding_hamiltonian(ll3, V3, field=lm.LandauGauge(0.02))
+    st3 = lm.KetBlock(ll3, o.random_kets(ol3.N, 2, 4), precision="c32", compensated=True)
     s = lm.ChebyshevGPU()
-    s.update_solver(Hp, 0.05)
+    s.update_solver(H3, 0.05)
     with pytest.raises(L.LMError) as e:
-        s.step(st)
+        s.step(st3)
     assert e.value.code == L.LM_ERR_NOTSUP
+    st = lm.KetBlock(ll, X, precision="c32", compensated=True)
     # ComplexF64 kets and density matrices have no residual plane
     with pytest.raises(L.LMError):
         lm.KetBlock(ll, X, precision="c64", compensated=True)
