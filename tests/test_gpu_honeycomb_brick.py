@@ -41,6 +41,9 @@ CASES = [
     (19, 9, (True, False), (0.7, 0.0), 0.2, 3),
     (17, 23, (False, True), (0.0, -0.4), 0.3, 2),
     (32, 40, (True, True), (0.3, 0.9), 0.02, 6),
+    (20, 1, (False, False), (0.0, 0.0), 0.05, 3),   # one cell high: a single lane pair per column
+    (21, 2, (True, False), (0.0, 0.0), 0.05, 2),
+    (15, 33, (False, False), (0.0, 0.0), 0.05, 2),  # a = 2K + 3 at K = 6: the smallest streaming a
 ]
 
 
