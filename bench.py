@@ -328,6 +328,7 @@ def run_batch_workload(args):
     # c64 runs the per-order kernels on column panels in place (P + 2 N w scratch per lattice);
     # c32 runs the fused kernel on full buffers (P + one recurrence buffer)
     panel = args.panel if args.panel is not None else (1024 if prec == "c64" else 0)
+    ctx.set_resident_form(args.batch_form == "resident")
     t_setup = time.perf_counter()
     batch, states, Ls, take, used = _batch_instances(n, prec, panel)
     batch.update(0.1)
@@ -357,7 +358,7 @@ def run_batch_workload(args):
             "config": {"workload": BATCH_WORKLOAD.format(n=n), "instances_run": len(take),
                        "instances_requested": n, "sum_N2": int(sum(int(Ls[i]) ** 4 for i in take)),
                        "chebyshev_order": info["K"], "tuned": tune, "setup_s": t_setup,
-                       "device_bytes": used, "panel_columns": panel},
+                       "device_bytes": used, "panel_columns": panel, "fused_form": args.batch_form},
             "clocks": clocks, "trace_sample": tr}
     print(json.dumps(line))
     return 0
@@ -833,6 +834,9 @@ def main():
     ap.add_argument("--instances", type=int, default=512)
     ap.add_argument("--batch-instances", type=int, default=64,
                     help="lattices of the batch sub-record of the default line (0: none)")
+    ap.add_argument("--batch-form", default="resident", choices=["resident", "region"],
+                    help="batch: lattices that fit on chip in the lattice-resident form (default) or all in "
+                         "the region form (bit-identical results)")
     ap.add_argument("--panel", type=int, default=None,
                     help="batch: column-panel width of the per-order path (default 1024 for c64, off for c32)")
     ap.add_argument("--precision", default="c32", choices=["c32", "c64"])

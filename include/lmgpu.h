@@ -79,6 +79,11 @@ int lm_ctx_stream(lm_ctx *ctx, void **stream);
  * double-float arithmetic (pairs of FP32 values, about 48 significant bits) on the FP32 pipe;
  * 0 selects FP64.  KPM moments agree to about 1e-15 mu_0. */
 #define LM_OPT_KPM 3
+/* LM_OPT_RESIDENT (default 1): in a ComplexF32 batch's fused pass, lattices of up to 4608
+ * sites (one CTA; smaller ones several kets per CTA) or 9216 sites (a cluster of two CTAs)
+ * keep a whole ket on chip for all K orders (K <= 40); 0 runs them in the region form.  Both
+ * give bit-identical results.  Takes effect at the next lm_batch_update. */
+#define LM_OPT_RESIDENT 4
 int lm_ctx_set_option(lm_ctx *ctx, int option, int value);
 /* Number of fused steps that ran in the x-streaming form on this context so far. */
 int lm_ctx_stream_launches(lm_ctx *ctx, int64_t *n);

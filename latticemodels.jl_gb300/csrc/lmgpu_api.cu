@@ -290,6 +290,9 @@ int lm_ctx_set_option(lm_ctx* ctx, int option, int value) {
         case LM_OPT_KPM:
             ctx->kpm_df = value ? 1 : 0;
             return LM_OK;
+        case LM_OPT_RESIDENT:
+            ctx->resident = value ? 1 : 0;
+            return LM_OK;
         default:
             return set_err(ctx, LM_ERR_ARG, "lm_ctx_set_option: unknown option");
     }

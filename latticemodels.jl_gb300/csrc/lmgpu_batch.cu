@@ -9,9 +9,10 @@
 //   kets         : one pass  x -> U x
 //   density P    : U P (columns), conjugate transpose, U (P U^dagger)   (= U P U^dagger)
 //
-// where a pass is either one temporally blocked launch (ComplexF32, K <= 8; items pulled
-// from an atomic work queue) or K launches of the per-order kernel over (instance, site
-// block, ket group) items.  The step is captured once per buffer parity into a CUDA graph and
+// where a pass is either the temporally blocked launches (ComplexF32; items pulled from an
+// atomic work queue per launch: lattices that fit on chip in the lattice-resident form, on one
+// CTA or a cluster of two, for any K <= 40, the rest in the region form for K <= 8) or K
+// launches of the per-order kernel over (instance, site block, ket group) items.  The step is captured once per buffer parity into a CUDA graph and
 // replayed.  `lm_batch_tune` times the candidate pass shapes (orders per pass: all K in one
 // launch or one per launch; kets per thread 2/4/8) on scratch copies and keeps the fastest.
 #include <cuda_runtime.h>
@@ -118,8 +119,10 @@ __global__ void __launch_bounds__(256) transpose_conj_batch_kernel(const TransIn
     typedef typename CT<R>::V V;
     __shared__ V tile[32][33];
     const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 x 8
+    int inst = 0;  // a CTA's items increase: the owning instance is found by a forward scan
     for (int64_t item = blockIdx.x; item < nitems; item += gridDim.x) {
-        const TransInst& D = table[find_item_owner(table, ninst, item)];
+        while (inst + 1 < ninst && __ldg(&table[inst + 1].item_begin) <= item) ++inst;
+        const TransInst& D = table[inst];
         const int64_t local = item - D.item_begin;
         const int64_t tr = local / D.tiles, tc = local % D.tiles;
         const V* in = (const V*)D.in;
@@ -222,14 +225,22 @@ struct lm_batch {
     std::vector<FusedInst> hf[2];
     std::vector<OrderInst> ho1[2], ho2[2];
     std::vector<TransInst> ht[2];
-    int64_t f_items = 0, o_items = 0, t_items = 0;
+    int64_t f_items = 0, o_items = 0, t_items = 0;  // f_items: the region form's (fused pass)
+    // lattice-resident part of the fused pass, per parity and cluster size (index cl - 1)
+    std::vector<ResidentInst> hr[2][2];
+    ResidentInst* dr[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
+    size_t cap_r[2][2] = {{0, 0}, {0, 0}};
+    int64_t r_items[2] = {0, 0};
+    int r_smem[2] = {0, 0};
+    int r_xreal = 0, f_xreal = 0;  // every instance of the resident / region part has real x-hops
     // device tables
     FusedInst* df[2] = {nullptr, nullptr};
     OrderInst* do1[2] = {nullptr, nullptr};
     OrderInst* do2[2] = {nullptr, nullptr};
     TransInst* dt_[2] = {nullptr, nullptr};
     size_t cap_f[2] = {0, 0}, cap_o1[2] = {0, 0}, cap_o2[2] = {0, 0}, cap_t[2] = {0, 0};
-    unsigned long long* dqueue = nullptr;  // two work-queue counters
+    unsigned long long* dqueue = nullptr;  // work-queue counters: 3 per pass (resident 1, 2, region);
+                                           // dqueue[6]: error bits of the resident kernel
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
     int parity = 0;                         // 1: every state's data currently in its A buffer
     std::vector<void*> base_S, base_A;      // pointers at update time (parity 0)
@@ -260,6 +271,11 @@ static void free_tables(lm_batch* b) {
         if (b->do1[p]) cudaFree(b->do1[p]);
         if (b->do2[p]) cudaFree(b->do2[p]);
         if (b->dt_[p]) cudaFree(b->dt_[p]);
+        for (int c = 0; c < 2; ++c) {
+            if (b->dr[p][c]) cudaFree(b->dr[p][c]);
+            b->dr[p][c] = nullptr;
+            b->cap_r[p][c] = 0;
+        }
         b->df[p] = nullptr;
         b->do1[p] = b->do2[p] = nullptr;
         b->dt_[p] = nullptr;
@@ -287,10 +303,20 @@ static void free_panel(lm_batch* b) {
 
 static int inner_of(int cfg) { return cfg == 1 ? 2 : (cfg == 3 ? 8 : 4); }
 
+// Whether instance i runs in the lattice-resident form (its cluster size in *cl).
+static bool batch_resident(const lm_batch* b, size_t i, ResidentInst* d, int* cl) {
+    if (!b->ctx->resident || b->precision != LM_C32 || b->K < 2 || b->K > kResMaxK) return false;
+    ResidentInst tmp{};
+    return resident_plan(b->hams[i]->lat->g, b->states[i]->m, d ? *d : tmp, cl);
+}
+
 static int batch_fused_ok(const lm_batch* b) {
-    if (!b->ctx->fused || b->precision != LM_C32 || !fused_supported(b->precision, b->K)) return 0;
-    for (auto* h : b->hams)
-        if (!fused_supported_geom(h->lat->g)) return 0;
+    if (!b->ctx->fused || b->precision != LM_C32) return 0;
+    for (size_t i = 0; i < b->hams.size(); ++i) {
+        int cl = 0;
+        if (batch_resident(b, i, nullptr, &cl)) continue;
+        if (!fused_supported(b->precision, b->K) || !fused_supported_geom(b->hams[i]->lat->g)) return 0;
+    }
     return 1;
 }
 
@@ -330,11 +356,15 @@ static int build_tables(lm_batch* b) {
         make_coefs(J, K, b->dt >= 0 ? 1.0 : -1.0, coefs[i]);
     }
     for (int p = 0; p < 2; ++p) {
-        b->hf[p].assign(n, FusedInst{});
+        b->hf[p].clear();
+        b->hr[p][0].clear();
+        b->hr[p][1].clear();
         b->ho1[p].assign(n, OrderInst{});
         b->ho2[p].assign(n, OrderInst{});
         b->ht[p].assign(n, TransInst{});
-        int64_t fi = 0, oi = 0, ti = 0;
+        int64_t fi = 0, oi = 0, ti = 0, ri[2] = {0, 0};
+        int rsmem[2] = {0, 0};
+        bool rxr = true, fxr = true;
         for (size_t i = 0; i < n; ++i) {
             lm_state* st = b->states[i];
             lm_solver* s = b->solvers[i];
@@ -344,19 +374,40 @@ static int build_tables(lm_batch* b) {
             const bool f32 = b->precision == LM_C32;
             const void* hop2 = f32 ? (const void*)s->d_hop2f : (const void*)s->d_hop2;
             const void* diag2 = f32 ? (const void*)s->d_diag2f : (const void*)s->d_diag2;
-            // fused table (x = S -> out = A)
-            FusedInst& f = b->hf[p][i];
-            f.g = g;
-            f.hop2 = (const float2*)s->d_hop2f;
-            f.diag2 = s->d_diag2f;
-            f.x = (const float2*)S;
-            f.out = (float2*)A;
-            f.ld = st->ld;
-            f.M = st->m;
-            f.item_begin = fi;
-            if (K <= kFusedMaxK) {
-                fi += fused_items(g, K, st->m, &f.ntx, &f.nty);
-                fused_fill_coef(f, K, coefs[i].data(), s->phase_re, s->phase_im);
+            // fused tables (x = S -> out = A): the lattice-resident form where the lattice fits,
+            // the region form otherwise
+            ResidentInst rd{};
+            int cl = 0;
+            if (batch_resident(b, i, &rd, &cl)) {
+                rd.hop2 = (const float2*)s->d_hop2f;
+                rd.diag2 = s->d_diag2f;
+                rd.x = (const float2*)S;
+                rd.out = (float2*)A;
+                rd.ld = st->ld;
+                rd.M = st->m;
+                rd.item_begin = ri[cl - 1];
+                ri[cl - 1] += (st->m + rd.G - 1) / rd.G;
+                rd.item_end = ri[cl - 1];
+                resident_fill_coef(rd, K, coefs[i].data(), s->phase_re, s->phase_im);
+                rsmem[cl - 1] = std::max(rsmem[cl - 1], rd.smem);
+                rxr = rxr && ham_x_real(b->hams[i]);
+                b->hr[p][cl - 1].push_back(rd);
+            } else {
+                FusedInst f{};
+                f.g = g;
+                f.hop2 = (const float2*)s->d_hop2f;
+                f.diag2 = s->d_diag2f;
+                f.x = (const float2*)S;
+                f.out = (float2*)A;
+                f.ld = st->ld;
+                f.M = st->m;
+                f.item_begin = fi;
+                if (K <= kFusedMaxK) {
+                    fi += fused_items(g, K, st->m, &f.ntx, &f.nty);
+                    fused_fill_coef(f, K, coefs[i].data(), s->phase_re, s->phase_im);
+                }
+                fxr = fxr && ham_x_real(b->hams[i]);
+                b->hf[p].push_back(f);
             }
             // per-order tables
             auto fill_order = [&](OrderInst& o, void* So, void* Ao) {
@@ -398,7 +449,14 @@ static int build_tables(lm_batch* b) {
         b->f_items = fi;
         b->o_items = oi;
         b->t_items = ti;
+        b->r_items[0] = ri[0];
+        b->r_items[1] = ri[1];
+        b->r_smem[0] = rsmem[0];
+        b->r_smem[1] = rsmem[1];
+        b->r_xreal = rxr;
+        b->f_xreal = fxr;
         int rc = upload_table(ctx, &b->df[p], &b->cap_f[p], b->hf[p]);
+        for (int c = 0; c < 2 && rc == LM_OK; ++c) rc = upload_table(ctx, &b->dr[p][c], &b->cap_r[p][c], b->hr[p][c]);
         if (rc == LM_OK) rc = upload_table(ctx, &b->do1[p], &b->cap_o1[p], b->ho1[p]);
         if (rc == LM_OK) rc = upload_table(ctx, &b->do2[p], &b->cap_o2[p], b->ho2[p]);
         if (rc == LM_OK) rc = upload_table(ctx, &b->dt_[p], &b->cap_t[p], b->ht[p]);
@@ -574,19 +632,18 @@ static cudaError_t launch_transpose(lm_batch* b, const TransInst* table) {
     return cudaGetLastError();
 }
 
-// Real x-hops in every instance: the fused launch takes the 2-FMA x-neighbour form.
-static bool batch_x_real(const lm_batch* b) {
-    for (const lm_ham* h : b->hams)
-        if (!ham_x_real(h)) return false;
-    return true;
-}
-
 static cudaError_t launch_fused_pass(lm_batch* b, int p, int q) {
     lm_ctx* ctx = b->ctx;
-    cudaError_t e = cudaMemsetAsync(b->dqueue + q, 0, sizeof(unsigned long long), ctx->stream);
-    if (e != cudaSuccess) return e;
-    return launch_fused_table(ctx, b->K, batch_x_real(b), nullptr, b->df[p], (int)b->states.size(), b->f_items,
-                              b->dqueue + q, 0);
+    unsigned long long* qc = b->dqueue + 3 * q;
+    cudaError_t e = cudaMemsetAsync(qc, 0, 3 * sizeof(unsigned long long), ctx->stream);
+    for (int c = 0; c < 2 && e == cudaSuccess; ++c)
+        if (b->r_items[c] > 0)
+            e = launch_resident_table(ctx, b->K, b->r_xreal, c + 1, b->dr[p][c], (int)b->hr[p][c].size(),
+                                      b->r_items[c], qc + c, b->dqueue + 6, b->r_smem[c]);
+    if (e == cudaSuccess && b->f_items > 0)
+        e = launch_fused_table(ctx, b->K, b->f_xreal, nullptr, b->df[p], (int)b->hf[p].size(), b->f_items, qc + 2,
+                               0);
+    return e;
 }
 
 // Panelled step: per pass, every column panel runs the K orders in place (an odd-K result is
@@ -670,8 +727,10 @@ int lm_batch_create(lm_ctx* ctx, int kind, int precision, double tol, lm_batch**
     b->precision = precision;
     b->tol = tol;
     cudaSetDevice(ctx->device);
-    if (cudaMalloc((void**)&b->dqueue, 2 * sizeof(unsigned long long)) != cudaSuccess) {
+    if (cudaMalloc((void**)&b->dqueue, 7 * sizeof(unsigned long long)) != cudaSuccess ||
+        cudaMemset(b->dqueue, 0, 7 * sizeof(unsigned long long)) != cudaSuccess) {
         cudaGetLastError();
+        if (b->dqueue) cudaFree(b->dqueue);
         delete b;
         return set_err(ctx, LM_ERR_OOM, "lm_batch_create: queue allocation failed");
     }
@@ -779,7 +838,12 @@ int lm_batch_step(lm_batch* b) {
     const int p = b->parity;
     int moved = 0;
     if (b->cfg == 0) {  // kernel attributes are set outside any stream capture
-        int rc = check_cuda(ctx, ensure_fused_attr(ctx, b->K, batch_x_real(b)), "lm_batch_step: kernel attribute");
+        int rc = LM_OK;
+        if (b->f_items > 0)
+            rc = check_cuda(ctx, ensure_fused_attr(ctx, b->K, b->f_xreal), "lm_batch_step: kernel attribute");
+        for (int c = 0; c < 2 && rc == LM_OK; ++c)
+            if (b->r_items[c] > 0)
+                rc = check_cuda(ctx, ensure_resident_attr(ctx, b->r_xreal, c + 1), "lm_batch_step: kernel attribute");
         if (rc != LM_OK) return rc;
     }
     if (b->use_graph) {
@@ -840,7 +904,8 @@ int lm_batch_set_config(lm_batch* b, int cfg) {
     if (!b) return LM_ERR_ARG;
     if (cfg < -1 || cfg > 3) return set_err(b->ctx, LM_ERR_ARG, "lm_batch_set_config: config must be -1..3");
     if (cfg == 0 && b->valid && !batch_fused_ok(b))
-        return set_err(b->ctx, LM_ERR_NOTSUP, "lm_batch_set_config: the fused pass needs ComplexF32 and K <= 8");
+        return set_err(b->ctx, LM_ERR_NOTSUP,
+                       "lm_batch_set_config: the fused pass needs ComplexF32, and K <= 8 for lattices that do not fit on chip");
     b->cfg = cfg;
     free_graphs(b);
     if (b->valid) {
@@ -852,12 +917,20 @@ int lm_batch_set_config(lm_batch* b, int cfg) {
 
 int lm_batch_info(lm_batch* b, int* K, int* cfg, int64_t* items, int* ninst) {
     if (!b) return LM_ERR_ARG;
+    {  // a halo exchange of the lattice-resident kernel that timed out (its results are not valid)
+        unsigned long long errbits = 0;
+        cudaSetDevice(b->ctx->device);
+        int rc = check_cuda(b->ctx, cudaMemcpy(&errbits, b->dqueue + 6, sizeof(errbits), cudaMemcpyDeviceToHost),
+                            "lm_batch_info: error word");
+        if (rc != LM_OK) return rc;
+        if (errbits) return set_err(b->ctx, LM_ERR_TIMEOUT, "lm_batch: a halo exchange between the CTAs of a cluster timed out");
+    }
     if (K) *K = b->K;
     if (cfg) *cfg = b->cfg;
     if (items) {
         int64_t pitems = 0;
         for (int64_t v : b->po_items) pitems += v;
-        *items = b->panel_w > 0 ? pitems : (b->cfg == 0 ? b->f_items : b->o_items);
+        *items = b->panel_w > 0 ? pitems : (b->cfg == 0 ? b->f_items + b->r_items[0] + b->r_items[1] : b->o_items);
     }
     if (ninst) *ninst = (int)b->states.size();
     return LM_OK;

@@ -13,7 +13,8 @@ CSRC = PKG_DIR.parent / "csrc"
 INCLUDE = PKG_DIR.parent.parent / "include"
 LIB_PATH = PKG_DIR / "liblmgpu.so"
 SOURCES = ["lmgpu_api.cu", "lmgpu_kernels.cu", "lmgpu_fused.cu", "lmgpu_noalloc.cu", "lmgpu_batch.cu", "lmgpu_adjoint.cu",
-           "lmgpu_ring.cu", "lmgpu_kpm.cu", "lmgpu_ell.cu", "lmgpu_stream.cu", "lmgpu_eigh.cu"]
+           "lmgpu_ring.cu", "lmgpu_kpm.cu", "lmgpu_ell.cu", "lmgpu_stream.cu", "lmgpu_eigh.cu",
+           "lmgpu_resident.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", f"-I{INCLUDE}"]
 # extra nvcc flags for tuning builds (e.g. LMGPU_NVCC_FLAGS=-DLM_FUSED_SITES=2); the default

@@ -27,6 +27,7 @@ LM_C64, LM_C32 = 0, 1
 LM_OPT_FUSED = 1
 LM_OPT_STREAM = 2
 LM_OPT_KPM = 3
+LM_OPT_RESIDENT = 4
 LM_KETS, LM_DENSITY = 0, 1
 LM_FIELD_LANDAU, LM_FIELD_SYMMETRIC, LM_FIELD_POINTFLUX_AXIAL, LM_FIELD_POINTFLUX_SINGULAR = 1, 2, 3, 4
 LM_LAYOUT_NONE, LM_LAYOUT_HONEYCOMB = 0, 1

@@ -40,6 +40,12 @@ class Context:
         FP32 pipe; the default) or FP64; KPM moments agree to about 1e-15 mu_0."""
         self.check(self.lib.lm_ctx_set_option(self.handle, _lib.LM_OPT_KPM, 1 if on else 0))
 
+    def set_resident_form(self, on: bool):
+        """Lattice-resident form of a c32 batch's fused pass for lattices that fit on chip (the
+        default), or the region form; both give bit-identical results.  Applies from the next
+        batch update."""
+        self.check(self.lib.lm_ctx_set_option(self.handle, _lib.LM_OPT_RESIDENT, 1 if on else 0))
+
     def stream_launches(self) -> int:
         """Fused steps that ran in the x-streaming form so far."""
         n = C.c_int64()
