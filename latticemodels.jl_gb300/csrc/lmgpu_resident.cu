@@ -109,6 +109,18 @@ __device__ __forceinline__ void res_sync() {
     if (CL == 2) res_cluster_sync();
     else __syncthreads();
 }
+// The item barrier in two halves: the arrival (release) right after an item's last order, so
+// that it does not wait for the item's output stores, and the wait (acquire) before the next
+// item; the CTA barrier after it publishes the staged kets within the CTA.
+template <int CL>
+__device__ __forceinline__ void res_arrive() {
+    if (CL == 2) asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory");
+}
+template <int CL>
+__device__ __forceinline__ void res_wait() {
+    if (CL == 2) asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory");
+    __syncthreads();
+}
 __device__ __forceinline__ void res_cp8(float2* dst, const float2* src, bool valid) {
     const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
     asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(d), "l"(src), "r"(valid ? 8 : 0));
@@ -322,45 +334,57 @@ __device__ __forceinline__ void res_put(const float2 (&B)[C][R], int c, unsigned
 }
 
 // One order: B <- T_k = 2H~ T_{k-1} - T_{k-2} (A = T_{k-1}, B = T_{k-2} on entry; FIRST: A = T_0
-// and T_1 = H~ T_0), Y += c_k T_k, and T_k into the exchange buffer when wr.  The operation
+// and T_1 = H~ T_0), Y += c_k T_k, and T_k into the exchange buffer when WR.  The operation
 // order per site is the region form's.  On a cluster a thread that reads a halo column first
 // waits for the phase `parity` of mbarrier mb (the buffer Er).
-template <bool XR, bool FIRST, bool ODD, int CL>
+template <bool XR, bool FIRST, bool ODD, bool WR, int CL>
 __device__ __forceinline__ void res_order(const float2 (&A)[C][R], float2 (&B)[C][R], float2 (&Y)[C][R],
                                           const float2 (&hx)[C][R], const float2 (&hy)[C][R], unsigned Er, unsigned Ew,
-                                          unsigned peerEw, unsigned peerMb, bool wr, unsigned ct, const ResMap& m,
+                                          unsigned peerEw, unsigned peerMb, unsigned ct, const ResMap& m,
                                           float sk, const ChebLo& lo, unsigned mb, unsigned parity,
                                           unsigned long long* err) {
     const unsigned ro = Er + m.eo, rb = Er + m.eb, rt = Er + m.et;
+    // per column: the diagonal, the neighbours across the block's lower and upper y edges and
+    // the y-hop from below; column c + 1's are loaded before column c is computed, so that
+    // their latency overlaps the arithmetic (the exchange stores of column c come after)
+    auto load_col = [&](int c, float4& dq, float2& bot, float2& top, float2& hym0) {
+        dq = res_lds4(ct + (4u + c) * NT * 16u);
+        bot = res_lds2(rb + 32u * c + 24u);  // row 3 of the block row below
+        top = res_lds2(rt + 32u * c);        // row 0 of the block row above
+        hym0 = res_lds2(ct + (c < 2 ? 2u : 3u) * NT * 16u + 8u * (c & 1));
+    };
+    float4 dqn;
+    float2 botn, topn, hymn;
+    if (CL == 2 && (m.hw & 1)) res_mbar_wait(mb, parity, err);
+    load_col(0, dqn, botn, topn, hymn);
+    float2 lft[R], hxm0[R], rgt[R];
+    {
+        const float4 l0 = res_lds4(ro - 32u), l1 = res_lds4(ro - 16u);
+        lft[0] = make_float2(l0.x, l0.y);
+        lft[1] = make_float2(l0.z, l0.w);
+        lft[2] = make_float2(l1.x, l1.y);
+        lft[3] = make_float2(l1.z, l1.w);
+        const float4 e0 = res_lds4(ct), e1 = res_lds4(ct + NT * 16u);
+        hxm0[0] = make_float2(e0.x, e0.y);
+        hxm0[1] = make_float2(e0.z, e0.w);
+        hxm0[2] = make_float2(e1.x, e1.y);
+        hxm0[3] = make_float2(e1.z, e1.w);
+    }
 #pragma unroll
     for (int c = 0; c < C; ++c) {
-        const float4 dq = res_lds4(ct + (4u + c) * NT * 16u);
+        const float4 dq = dqn;
+        const float2 bot = botn, top = topn, hym0 = hymn;
         const float d[R] = {dq.x, dq.y, dq.z, dq.w};
-        const float2 bot = res_lds2(rb + 32u * c + 24u);  // row 3 of the block row below
-        const float2 top = res_lds2(rt + 32u * c);        // row 0 of the block row above
-        const float2 hym0 = res_lds2(ct + (c < 2 ? 2u : 3u) * NT * 16u + 8u * (c & 1));
-        float2 lft[R], hxm0[R];
-        if (c == 0) {
-            if (CL == 2 && (m.hw & 1)) res_mbar_wait(mb, parity, err);
-            const float4 l0 = res_lds4(ro - 32u), l1 = res_lds4(ro - 16u);
-            lft[0] = make_float2(l0.x, l0.y);
-            lft[1] = make_float2(l0.z, l0.w);
-            lft[2] = make_float2(l1.x, l1.y);
-            lft[3] = make_float2(l1.z, l1.w);
-            const float4 e0 = res_lds4(ct), e1 = res_lds4(ct + NT * 16u);
-            hxm0[0] = make_float2(e0.x, e0.y);
-            hxm0[1] = make_float2(e0.z, e0.w);
-            hxm0[2] = make_float2(e1.x, e1.y);
-            hxm0[3] = make_float2(e1.z, e1.w);
-        }
-        float2 rgt[R];
-        if (c == C - 1) {
-            if (CL == 2 && m.hw == 2) res_mbar_wait(mb, parity, err);
-            const float4 r0 = res_lds4(ro + 32u * C), r1 = res_lds4(ro + 32u * C + 16u);
-            rgt[0] = make_float2(r0.x, r0.y);
-            rgt[1] = make_float2(r0.z, r0.w);
-            rgt[2] = make_float2(r1.x, r1.y);
-            rgt[3] = make_float2(r1.z, r1.w);
+        if (c + 1 < C) {
+            if (c + 1 == C - 1) {
+                if (CL == 2 && m.hw == 2) res_mbar_wait(mb, parity, err);
+                const float4 r0 = res_lds4(ro + 32u * C), r1 = res_lds4(ro + 32u * C + 16u);
+                rgt[0] = make_float2(r0.x, r0.y);
+                rgt[1] = make_float2(r0.z, r0.w);
+                rgt[2] = make_float2(r1.x, r1.y);
+                rgt[3] = make_float2(r1.z, r1.w);
+            }
+            load_col(c + 1, dqn, botn, topn, hymn);
         }
 #pragma unroll
         for (int j = 0; j < R; ++j) {
@@ -408,7 +432,7 @@ __device__ __forceinline__ void res_order(const float2 (&A)[C][R], float2 (&B)[C
                 Y[c][j].y = fmaf(sk, acc.y, Y[c][j].y);
             }
         }
-        if (wr) res_put<CL>(B, c, Ew, peerEw, peerMb, m);
+        if (WR) res_put<CL>(B, c, Ew, peerEw, peerMb, m);
     }
 }
 
@@ -469,6 +493,7 @@ cheb_resident_c32_kernel(const ResidentInst* __restrict__ table, int ninst, long
     float2 hx[C][R], hy[C][R];
     res_setup<CL>(s_desc[0], rank, t, E, ct, m, hx, hy);
     res_stage<CL>(stage, s_desc[0], rank, (item - s_desc[0].item_begin) * s_desc[0].G, t);
+    res_arrive<CL>();  // the buffers are zeroed before the other CTA writes into them
     int sb = 0;
 
     while (true) {
@@ -478,7 +503,7 @@ cheb_resident_c32_kernel(const ResidentInst* __restrict__ table, int ninst, long
         int xs0, ncols;
         res_columns<CL>(D, rank, &xs0, &ncols);
         res_cp_wait();
-        res_sync<CL>();  // staged kets visible; every thread of the cluster is done with the previous item
+        res_wait<CL>();  // staged kets visible; every thread of the cluster is done with the previous item
 
         const bool live = m.on && k0 + m.g < D.M;
         const float2* st = stage + sb * STAGE_F2 + m.g * D.slab;
@@ -513,34 +538,35 @@ cheb_resident_c32_kernel(const ResidentInst* __restrict__ table, int ninst, long
             if (CL == 2 && t == 0) res_mbar_expect(mb_loc[b], xbytes);
         };
         const unsigned E1 = Es + par, pE1 = peerE + par;
-#define LM_RES_ORDER(FI, OD, AA, BB, ER, EW, PEW, PMB, WR, SK, MB, PAR) \
-    res_order<XR, FI, OD, CL>(AA, BB, Y, hx, hy, ER, EW, PEW, PMB, WR, cts, m, SK, D.lo, MB, PAR, err)
+#define LM_RES_ORDER(FI, OD, WR, AA, BB, ER, EW, PEW, PMB, SK, MB, PAR) \
+    if (live) res_order<XR, FI, OD, WR, CL>(AA, BB, Y, hx, hy, ER, EW, PEW, PMB, cts, m, SK, D.lo, MB, PAR, err)
+        // orders k (even): T_{k-1} in B and buffer 1 -> T_k in A and buffer 0; k (odd, k > 1): T_{k-1}
+        // in A and buffer 0 -> T_k in B and buffer 1; the last order writes no buffer
         xdone(0);  // T_0 in buffer 0
-        if (live) LM_RES_ORDER(true, true, A, B, Es, E1, pE1, mb_peer[1], true, D.s[1], mb_loc[0], ph & 1u);
+        LM_RES_ORDER(true, true, true, A, B, Es, E1, pE1, mb_peer[1], D.s[1], mb_loc[0], ph & 1u);
         ph ^= 1u;
         xdone(1);
         int k = 2;
-        for (; k + 1 <= K; k += 2) {
-            // order k (even): T_{k-1} in B and buffer 1 -> T_k in A and buffer 0
-            if (live)
-                LM_RES_ORDER(false, false, B, A, E1, Es, peerE, mb_peer[0], true, D.s[k], mb_loc[1],
-                             (ph >> 1) & 1u);
+        for (; k + 1 < K; k += 2) {
+            LM_RES_ORDER(false, false, true, B, A, E1, Es, peerE, mb_peer[0], D.s[k], mb_loc[1], (ph >> 1) & 1u);
             ph ^= 2u;
             xdone(0);
-            // order k + 1 (odd): T_k in A and buffer 0 -> T_{k+1} in B and buffer 1
-            const bool wr = k + 1 < K;
-            if (live)
-                LM_RES_ORDER(false, true, A, B, Es, E1, pE1, mb_peer[1], wr, D.s[k + 1], mb_loc[0], ph & 1u);
+            LM_RES_ORDER(false, true, true, A, B, Es, E1, pE1, mb_peer[1], D.s[k + 1], mb_loc[0], ph & 1u);
             ph ^= 1u;
-            if (wr) xdone(1);
+            xdone(1);
         }
-        if (k == K) {  // K even: the last order
-            if (live)
-                LM_RES_ORDER(false, false, B, A, E1, Es, peerE, mb_peer[0], false, D.s[k], mb_loc[1],
-                             (ph >> 1) & 1u);
+        if (k == K) {  // K even
+            LM_RES_ORDER(false, false, false, B, A, E1, Es, peerE, mb_peer[0], D.s[k], mb_loc[1], (ph >> 1) & 1u);
             ph ^= 2u;
+        } else {  // K odd: orders K - 1 and K
+            LM_RES_ORDER(false, false, true, B, A, E1, Es, peerE, mb_peer[0], D.s[k], mb_loc[1], (ph >> 1) & 1u);
+            ph ^= 2u;
+            xdone(0);
+            LM_RES_ORDER(false, true, false, A, B, Es, E1, pE1, mb_peer[1], D.s[k + 1], mb_loc[0], ph & 1u);
+            ph ^= 1u;
         }
 #undef LM_RES_ORDER
+        res_arrive<CL>();  // this item's reads of the exchange buffers are done
 
         // out = e^{-ib dt} y + a0 x (a0 = e^{-ib dt} c_0): the small terms first, the dominant one last
         if (live) {
@@ -567,15 +593,16 @@ cheb_resident_c32_kernel(const ResidentInst* __restrict__ table, int ninst, long
         }
         if (!have_next) break;
         if (!same) {
-            res_sync<CL>();  // every thread of the cluster is done with this instance's exchange buffers
+            res_wait<CL>();  // every thread of the cluster is done with this instance's exchange buffers
             dslot ^= 1;
             res_setup<CL>(s_desc[dslot], rank, t, E, ct, m, hx, hy);
+            res_arrive<CL>();
         }
         item = nxt;
         sb ^= 1;
     }
     res_cp_wait();
-    res_sync<CL>();  // no CTA of the cluster exits while the other may still write into it
+    res_wait<CL>();  // the pending arrival: no CTA of the cluster exits while the other may still write into it
 }
 
 bool resident_plan(const Geom& g, int64_t m, ResidentInst& d, int* cl) {
