@@ -113,36 +113,69 @@ __global__ void __launch_bounds__(256) cheb_order_batch_kernel(const OrderInst* 
 }
 
 // out = in^dagger for every instance (32 x 32 tiles through shared memory).
+// out = in^dagger per instance over 32 x 32 tiles.  A CTA's items increase, so the owning
+// instance is found by a forward scan; the next tile's elements are loaded into registers before
+// the current tile is written out, so that loads stay in flight while the CTA stores.
 template <typename R>
 __global__ void __launch_bounds__(256) transpose_conj_batch_kernel(const TransInst* __restrict__ table, int ninst,
                                                                    int64_t nitems) {
     typedef typename CT<R>::V V;
     __shared__ V tile[32][33];
     const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 x 8
-    int inst = 0;  // a CTA's items increase: the owning instance is found by a forward scan
-    for (int64_t item = blockIdx.x; item < nitems; item += gridDim.x) {
+    struct Tile {
+        const V* in;
+        V* out;
+        int64_t n, ld, tr, tc;
+    };
+    int inst = 0;
+    auto tile_of = [&](int64_t item) {
         while (inst + 1 < ninst && __ldg(&table[inst + 1].item_begin) <= item) ++inst;
         const TransInst& D = table[inst];
         const int64_t local = item - D.item_begin;
-        const int64_t tr = local / D.tiles, tc = local % D.tiles;
-        const V* in = (const V*)D.in;
-        V* out = (V*)D.out;
-        const int64_t n = D.n, ld = D.ld;
+        Tile T;
+        T.in = (const V*)D.in;
+        T.out = (V*)D.out;
+        T.n = D.n;
+        T.ld = D.ld;
+        T.tr = local / D.tiles;
+        T.tc = local % D.tiles;
+        return T;
+    };
+    auto load = [&](const Tile& T, V (&v)[4]) {
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
-            const int64_t r = tr * 32 + tx, c = tc * 32 + ty + 8 * j;
-            if (r < n && c < n) tile[ty + 8 * j][tx] = in[r + c * ld];
+            const int64_t r = T.tr * 32 + tx, c = T.tc * 32 + ty + 8 * j;
+            if (r < T.n && c < T.n) v[j] = T.in[r + c * T.ld];
         }
+    };
+    int64_t item = blockIdx.x;
+    if (item >= nitems) return;
+    Tile cur = tile_of(item);
+    V v[4];
+    load(cur, v);
+    while (true) {
+#pragma unroll
+        for (int j = 0; j < 4; ++j) tile[ty + 8 * j][tx] = v[j];
         __syncthreads();
+        const int64_t next = item + gridDim.x;
+        const bool more = next < nitems;
+        Tile nt;
+        if (more) {
+            nt = tile_of(next);
+            load(nt, v);
+        }
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
-            const int64_t r2 = tc * 32 + tx, c2 = tr * 32 + ty + 8 * j;
-            if (r2 < n && c2 < n) {
-                const V v = tile[tx][ty + 8 * j];
-                out[r2 + c2 * ld] = CT<R>::make(v.x, -v.y);
+            const int64_t r2 = cur.tc * 32 + tx, c2 = cur.tr * 32 + ty + 8 * j;
+            if (r2 < cur.n && c2 < cur.n) {
+                const V w = tile[tx][ty + 8 * j];
+                cur.out[r2 + c2 * cur.ld] = CT<R>::make(w.x, -w.y);
             }
         }
         __syncthreads();
+        if (!more) break;
+        cur = nt;
+        item = next;
     }
 }
 

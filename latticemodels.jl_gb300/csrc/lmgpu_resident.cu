@@ -386,50 +386,71 @@ __device__ __forceinline__ void res_order(const float2 (&A)[C][R], float2 (&B)[C
             }
             load_col(c + 1, dqn, botn, topn, hymn);
         }
+        // the stencil term by term over the column's R sites (R independent accumulation chains
+        // side by side); per site the operation order is the region form's
+        float2 acc[R];
 #pragma unroll
-        for (int j = 0; j < R; ++j) {
+        for (int j = 0; j < R; ++j) acc[j] = FIRST ? make_float2(0.f, 0.f) : make_float2(-B[c][j].x, -B[c][j].y);
+#pragma unroll
+        for (int j = 0; j < R; ++j) {  // x + 1
             const float2 vxp = c < C - 1 ? A[c + 1][j] : rgt[j];
+            const float2 h = hx[c][j];
+            if (XR) {
+                acc[j].x = fmaf(h.x, vxp.x, acc[j].x);
+                acc[j].y = fmaf(h.x, vxp.y, acc[j].y);
+            } else {
+                acc[j].x = fmaf(h.x, vxp.x, acc[j].x); acc[j].x = fmaf(-h.y, vxp.y, acc[j].x);
+                acc[j].y = fmaf(h.x, vxp.y, acc[j].y); acc[j].y = fmaf(h.y, vxp.x, acc[j].y);
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < R; ++j) {  // x - 1
             const float2 vxm = c > 0 ? A[c - 1][j] : lft[j];
             const float2 hxm = c > 0 ? make_float2(hx[c - 1][j].x, -hx[c - 1][j].y) : hxm0[j];
+            if (XR) {
+                acc[j].x = fmaf(hxm.x, vxm.x, acc[j].x);
+                acc[j].y = fmaf(hxm.x, vxm.y, acc[j].y);
+            } else {
+                acc[j].x = fmaf(hxm.x, vxm.x, acc[j].x); acc[j].x = fmaf(-hxm.y, vxm.y, acc[j].x);
+                acc[j].y = fmaf(hxm.x, vxm.y, acc[j].y); acc[j].y = fmaf(hxm.y, vxm.x, acc[j].y);
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < R; ++j) {  // y + 1
             const float2 vyp = j < R - 1 ? A[c][j + 1] : top;
+            const float2 v = hy[c][j];
+            acc[j].x = fmaf(v.x, vyp.x, acc[j].x); acc[j].x = fmaf(-v.y, vyp.y, acc[j].x);
+            acc[j].y = fmaf(v.x, vyp.y, acc[j].y); acc[j].y = fmaf(v.y, vyp.x, acc[j].y);
+        }
+#pragma unroll
+        for (int j = 0; j < R; ++j) {  // y - 1
             const float2 vym = j > 0 ? A[c][j - 1] : bot;
             const float2 hym = j > 0 ? make_float2(hy[c][j - 1].x, -hy[c][j - 1].y) : hym0;
-            const float2 h = hx[c][j], v = hy[c][j];
-            float2 acc = FIRST ? make_float2(0.f, 0.f) : make_float2(-B[c][j].x, -B[c][j].y);
-            if (XR) {
-                acc.x = fmaf(h.x, vxp.x, acc.x);
-                acc.y = fmaf(h.x, vxp.y, acc.y);
-                acc.x = fmaf(hxm.x, vxm.x, acc.x);
-                acc.y = fmaf(hxm.x, vxm.y, acc.y);
-            } else {
-                acc.x = fmaf(h.x, vxp.x, acc.x); acc.x = fmaf(-h.y, vxp.y, acc.x);
-                acc.y = fmaf(h.x, vxp.y, acc.y); acc.y = fmaf(h.y, vxp.x, acc.y);
-                acc.x = fmaf(hxm.x, vxm.x, acc.x); acc.x = fmaf(-hxm.y, vxm.y, acc.x);
-                acc.y = fmaf(hxm.x, vxm.y, acc.y); acc.y = fmaf(hxm.y, vxm.x, acc.y);
-            }
-            acc.x = fmaf(v.x, vyp.x, acc.x); acc.x = fmaf(-v.y, vyp.y, acc.x);
-            acc.y = fmaf(v.x, vyp.y, acc.y); acc.y = fmaf(v.y, vyp.x, acc.y);
-            acc.x = fmaf(hym.x, vym.x, acc.x); acc.x = fmaf(-hym.y, vym.y, acc.x);
-            acc.y = fmaf(hym.x, vym.y, acc.y); acc.y = fmaf(hym.y, vym.x, acc.y);
-            acc.x = fmaf(d[j], A[c][j].x, acc.x);
-            acc.y = fmaf(d[j], A[c][j].y, acc.y);
+            acc[j].x = fmaf(hym.x, vym.x, acc[j].x); acc[j].x = fmaf(-hym.y, vym.y, acc[j].x);
+            acc[j].y = fmaf(hym.x, vym.y, acc[j].y); acc[j].y = fmaf(hym.y, vym.x, acc[j].y);
+        }
+#pragma unroll
+        for (int j = 0; j < R; ++j) {  // diagonal, the first order's 1/2, the accumulator
+            acc[j].x = fmaf(d[j], A[c][j].x, acc[j].x);
+            acc[j].y = fmaf(d[j], A[c][j].y, acc[j].y);
             if (FIRST) {  // the tables hold 2H/a
-                acc.x *= 0.5f;
-                acc.y *= 0.5f;
+                acc[j].x *= 0.5f;
+                acc[j].y *= 0.5f;
             }
             const float2 x = A[c][j];  // T_0 when FIRST
-            B[c][j] = acc;
+            const float2 a = acc[j];
+            B[c][j] = a;
             if (FIRST) {  // y = -i s_1 T1 + g0 T0 + g1 T1
-                const float lx = fmaf(lo.g0_re, x.x, fmaf(-lo.g0_im, x.y, fmaf(lo.g1_re, acc.x, -lo.g1_im * acc.y)));
-                const float ly = fmaf(lo.g0_re, x.y, fmaf(lo.g0_im, x.x, fmaf(lo.g1_re, acc.y, lo.g1_im * acc.x)));
-                Y[c][j].x = fmaf(sk, acc.y, lx);
-                Y[c][j].y = fmaf(-sk, acc.x, ly);
+                const float lx = fmaf(lo.g0_re, x.x, fmaf(-lo.g0_im, x.y, fmaf(lo.g1_re, a.x, -lo.g1_im * a.y)));
+                const float ly = fmaf(lo.g0_re, x.y, fmaf(lo.g0_im, x.x, fmaf(lo.g1_re, a.y, lo.g1_im * a.x)));
+                Y[c][j].x = fmaf(sk, a.y, lx);
+                Y[c][j].y = fmaf(-sk, a.x, ly);
             } else if (ODD) {  // c_k = -i s_k
-                Y[c][j].x = fmaf(sk, acc.y, Y[c][j].x);
-                Y[c][j].y = fmaf(-sk, acc.x, Y[c][j].y);
+                Y[c][j].x = fmaf(sk, a.y, Y[c][j].x);
+                Y[c][j].y = fmaf(-sk, a.x, Y[c][j].y);
             } else {  // c_k = s_k
-                Y[c][j].x = fmaf(sk, acc.x, Y[c][j].x);
-                Y[c][j].y = fmaf(sk, acc.y, Y[c][j].y);
+                Y[c][j].x = fmaf(sk, a.x, Y[c][j].x);
+                Y[c][j].y = fmaf(sk, a.y, Y[c][j].y);
             }
         }
         if (WR) res_put<CL>(B, c, Ew, peerEw, peerMb, m);
