@@ -29,6 +29,9 @@
 namespace lmgpu {
 
 constexpr int kBatchMaxK = 40;
+// side of the out-of-place conjugate-transpose tiles: 64 for ComplexF32 (33 KB of shared memory),
+// 32 for ComplexF64 (a 64-tile would exceed the static shared-memory limit)
+constexpr int trans_tile(int precision) { return precision == LM_C64 ? 32 : 64; }
 
 struct OrderInst {
     Geom g;
@@ -50,7 +53,7 @@ struct TransInst {
     void* out;
     int64_t n, ld;
     int64_t item_begin;
-    int64_t tiles;  // tiles per dimension (32 x 32)
+    int64_t tiles;  // tiles per dimension (trans_tile x trans_tile)
 };
 
 // Panelled batches: dst = src over n x m columns (an odd-K result moved back into place).
@@ -113,14 +116,17 @@ __global__ void __launch_bounds__(256) cheb_order_batch_kernel(const OrderInst* 
 }
 
 // out = in^dagger for every instance (32 x 32 tiles through shared memory).
-// out = in^dagger per instance over 32 x 32 tiles.  A CTA's items increase, so the owning
-// instance is found by a forward scan; the next tile's elements are loaded into registers before
-// the current tile is written out, so that loads stay in flight while the CTA stores.
-template <typename R>
+// out = in^dagger per instance over TS x TS tiles (TS = 64: each warp access is a contiguous
+// 512-byte run of a column on both sides).  A CTA's items increase, so the owning instance is
+// found by a forward scan; the next tile's elements are loaded into registers before the current
+// tile is written out, so that loads stay in flight while the CTA stores.
+template <typename R, int TS>
 __global__ void __launch_bounds__(256) transpose_conj_batch_kernel(const TransInst* __restrict__ table, int ninst,
                                                                    int64_t nitems) {
     typedef typename CT<R>::V V;
-    __shared__ V tile[32][33];
+    constexpr int NJ = TS / 8;  // columns per thread (8 warps), TS / 32 elements per column
+    constexpr int NI = TS / 32;
+    __shared__ V tile[TS][TS + 1];
     const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 x 8
     struct Tile {
         const V* in;
@@ -141,21 +147,25 @@ __global__ void __launch_bounds__(256) transpose_conj_batch_kernel(const TransIn
         T.tc = local % D.tiles;
         return T;
     };
-    auto load = [&](const Tile& T, V (&v)[4]) {
+    auto load = [&](const Tile& T, V (&v)[NJ][NI]) {
 #pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            const int64_t r = T.tr * 32 + tx, c = T.tc * 32 + ty + 8 * j;
-            if (r < T.n && c < T.n) v[j] = T.in[r + c * T.ld];
-        }
+        for (int j = 0; j < NJ; ++j)
+#pragma unroll
+            for (int i = 0; i < NI; ++i) {
+                const int64_t r = T.tr * TS + tx + 32 * i, c = T.tc * TS + ty + 8 * j;
+                if (r < T.n && c < T.n) v[j][i] = T.in[r + c * T.ld];
+            }
     };
     int64_t item = blockIdx.x;
     if (item >= nitems) return;
     Tile cur = tile_of(item);
-    V v[4];
+    V v[NJ][NI];
     load(cur, v);
     while (true) {
 #pragma unroll
-        for (int j = 0; j < 4; ++j) tile[ty + 8 * j][tx] = v[j];
+        for (int j = 0; j < NJ; ++j)
+#pragma unroll
+            for (int i = 0; i < NI; ++i) tile[ty + 8 * j][tx + 32 * i] = v[j][i];
         __syncthreads();
         const int64_t next = item + gridDim.x;
         const bool more = next < nitems;
@@ -165,13 +175,15 @@ __global__ void __launch_bounds__(256) transpose_conj_batch_kernel(const TransIn
             load(nt, v);
         }
 #pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            const int64_t r2 = cur.tc * 32 + tx, c2 = cur.tr * 32 + ty + 8 * j;
-            if (r2 < cur.n && c2 < cur.n) {
-                const V w = tile[tx][ty + 8 * j];
-                cur.out[r2 + c2 * cur.ld] = CT<R>::make(w.x, -w.y);
+        for (int j = 0; j < NJ; ++j)
+#pragma unroll
+            for (int i = 0; i < NI; ++i) {
+                const int64_t r2 = cur.tc * TS + tx + 32 * i, c2 = cur.tr * TS + ty + 8 * j;
+                if (r2 < cur.n && c2 < cur.n) {
+                    const V w = tile[tx + 32 * i][ty + 8 * j];
+                    cur.out[r2 + c2 * cur.ld] = CT<R>::make(w.x, -w.y);
+                }
             }
-        }
         __syncthreads();
         if (!more) break;
         cur = nt;
@@ -475,7 +487,7 @@ static int build_tables(lm_batch* b) {
             tr.out = from_S ? A : S;
             tr.n = st->n;
             tr.ld = st->ld;
-            tr.tiles = (st->n + 31) / 32;
+            tr.tiles = (st->n + trans_tile(b->precision) - 1) / trans_tile(b->precision);
             tr.item_begin = ti;
             ti += tr.tiles * tr.tiles;
         }
@@ -659,8 +671,10 @@ static cudaError_t launch_transpose(lm_batch* b, const TransInst* table) {
     lm_ctx* ctx = b->ctx;
     const int n = (int)b->states.size();
     const int grid = grid_for(ctx, b->t_items, 8);
-    if (b->precision == LM_C64) transpose_conj_batch_kernel<double><<<grid, 256, 0, ctx->stream>>>(table, n, b->t_items);
-    else transpose_conj_batch_kernel<float><<<grid, 256, 0, ctx->stream>>>(table, n, b->t_items);
+    if (b->precision == LM_C64)
+        transpose_conj_batch_kernel<double, trans_tile(LM_C64)><<<grid, 256, 0, ctx->stream>>>(table, n, b->t_items);
+    else
+        transpose_conj_batch_kernel<float, trans_tile(LM_C32)><<<grid, 256, 0, ctx->stream>>>(table, n, b->t_items);
     ctx->launches++;
     return cudaGetLastError();
 }
