@@ -430,6 +430,7 @@ static int build_tables(lm_batch* b) {
                 rd.out = (float2*)A;
                 rd.ld = st->ld;
                 rd.M = st->m;
+                rd.vec = g.Ly % 2 == 0 && st->ld % 2 == 0 && ((uintptr_t)S & 15) == 0 && ((uintptr_t)A & 15) == 0;
                 rd.item_begin = ri[cl - 1];
                 ri[cl - 1] += (st->m + rd.G - 1) / rd.G;
                 rd.item_end = ri[cl - 1];

@@ -109,6 +109,7 @@ struct ResidentInst {
     int rs, gs;     // bytes of a row of exchange entries, (ncl + 2) 32 + 16, and of a thread group, (nby + 2) rs
     int slab;       // float2 words per ket of the staging buffer, ncl * Ly
     int smem;       // dynamic shared memory the instance needs (bytes)
+    int vec;        // site pairs move as 16-byte units (even Ly and ld, 16-byte aligned x and out)
     float s[kResMaxK + 1];
     float ph_re, ph_im;   // e^{-ib dt}
     float a0_re, a0_im;   // e^{-ib dt} c_0

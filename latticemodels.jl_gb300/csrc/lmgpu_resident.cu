@@ -125,6 +125,10 @@ __device__ __forceinline__ void res_cp8(float2* dst, const float2* src, bool val
     const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
     asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(d), "l"(src), "r"(valid ? 8 : 0));
 }
+__device__ __forceinline__ void res_cp16(float2* dst, const float2* src, bool valid) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(d), "l"(src), "r"(valid ? 16 : 0));
+}
 __device__ __forceinline__ void res_cp_commit() { asm volatile("cp.async.commit_group;\n" ::); }
 __device__ __forceinline__ void res_cp_wait() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
 
@@ -306,7 +310,11 @@ __device__ __forceinline__ void res_stage(float2* buf, const ResidentInst& D, un
         const bool ok = ket < D.M;
         const float2* src = D.x + (ok ? ket * D.ld + (int64_t)xs0 * D.Ly : 0);
         float2* dst = buf + g * D.slab;
-        for (int s = t; s < n; s += NT) res_cp8(dst + s, ok ? src + s : D.x, ok);
+        if (D.vec) {  // site pairs: 16-byte aligned on both sides (even Ly, ld and slab)
+            for (int s = 2 * t; s < n; s += 2 * NT) res_cp16(dst + s, ok ? src + s : D.x, ok);
+        } else {
+            for (int s = t; s < n; s += NT) res_cp8(dst + s, ok ? src + s : D.x, ok);
+        }
     }
     res_cp_commit();
 }
@@ -531,10 +539,22 @@ cheb_resident_c32_kernel(const ResidentInst* __restrict__ table, int ninst, long
         float2 A[C][R], B[C][R], Y[C][R];
 #pragma unroll
         for (int c = 0; c < C; ++c) {
+            const int x = m.x0 + c;
+            if (D.vec) {  // even Ly: a site pair lies in the lattice or outside it as a whole
 #pragma unroll
-            for (int j = 0; j < R; ++j) {
-                const int x = m.x0 + c, y = m.y0 + j;
-                A[c][j] = (m.on && x < D.Lx && y < D.Ly) ? st[(x - xs0) * D.Ly + y] : make_float2(0.f, 0.f);
+                for (int h = 0; h < R / 2; ++h) {
+                    const int y = m.y0 + 2 * h;
+                    float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
+                    if (m.on && x < D.Lx && y < D.Ly) q = *reinterpret_cast<const float4*>(st + (x - xs0) * D.Ly + y);
+                    A[c][2 * h] = make_float2(q.x, q.y);
+                    A[c][2 * h + 1] = make_float2(q.z, q.w);
+                }
+            } else {
+#pragma unroll
+                for (int j = 0; j < R; ++j) {
+                    const int y = m.y0 + j;
+                    A[c][j] = (m.on && x < D.Lx && y < D.Ly) ? st[(x - xs0) * D.Ly + y] : make_float2(0.f, 0.f);
+                }
             }
             if (live) res_put<CL>(A, c, Es, peerE, mb_peer[0], m);
         }
@@ -547,7 +567,7 @@ cheb_resident_c32_kernel(const ResidentInst* __restrict__ table, int ninst, long
             if (!same) load_desc(dslot ^ 1, nxt);
             if (t == 0 && rank == 0) fetch(nslot ^ 1);
             nslot ^= 1;
-            __syncthreads();  // the next descriptor is visible in this CTA
+            if (!same) __syncthreads();  // the next descriptor is visible in this CTA
             const ResidentInst& Dn = same ? D : s_desc[dslot ^ 1];
             res_stage<CL>(stage + (sb ^ 1) * STAGE_F2, Dn, rank, (nxt - Dn.item_begin) * Dn.G, t);
         }
@@ -593,24 +613,40 @@ cheb_resident_c32_kernel(const ResidentInst* __restrict__ table, int ninst, long
         if (live) {
             const float ph_re = D.ph_re, ph_im = D.ph_im, a0_re = D.a0_re, a0_im = D.a0_im;
             float2* outk = D.out + (k0 + m.g) * D.ld;
+            auto out_site = [&](float2 yv, float2 x0) {
+                float2 r;
+                r.x = fmaf(ph_re, yv.x, -ph_im * yv.y);
+                r.y = fmaf(ph_re, yv.y, ph_im * yv.x);
+                r.x = fmaf(-a0_im, x0.y, r.x);
+                r.y = fmaf(a0_im, x0.x, r.y);
+                float2 o;
+                o.x = fmaf(a0_re, x0.x, r.x);
+                o.y = fmaf(a0_re, x0.y, r.y);
+                return o;
+            };
 #pragma unroll
-            for (int c = 0; c < C; ++c)
+            for (int c = 0; c < C; ++c) {
+                const int x = m.x0 + c;
+                if (x >= D.Lx) continue;
+                if (D.vec) {
 #pragma unroll
-                for (int j = 0; j < R; ++j) {
-                    const int x = m.x0 + c, y = m.y0 + j;
-                    if (x < D.Lx && y < D.Ly) {
-                        const float2 x0 = st[(x - xs0) * D.Ly + y];
-                        float2 r;
-                        r.x = fmaf(ph_re, Y[c][j].x, -ph_im * Y[c][j].y);
-                        r.y = fmaf(ph_re, Y[c][j].y, ph_im * Y[c][j].x);
-                        r.x = fmaf(-a0_im, x0.y, r.x);
-                        r.y = fmaf(a0_im, x0.x, r.y);
-                        float2 o;
-                        o.x = fmaf(a0_re, x0.x, r.x);
-                        o.y = fmaf(a0_re, x0.y, r.y);
-                        outk[(int64_t)x * D.Ly + y] = o;
+                    for (int h = 0; h < R / 2; ++h) {
+                        const int y = m.y0 + 2 * h;
+                        if (y < D.Ly) {
+                            const float4 q = *reinterpret_cast<const float4*>(st + (x - xs0) * D.Ly + y);
+                            const float2 o0 = out_site(Y[c][2 * h], make_float2(q.x, q.y));
+                            const float2 o1 = out_site(Y[c][2 * h + 1], make_float2(q.z, q.w));
+                            *reinterpret_cast<float4*>(outk + (int64_t)x * D.Ly + y) = make_float4(o0.x, o0.y, o1.x, o1.y);
+                        }
+                    }
+                } else {
+#pragma unroll
+                    for (int j = 0; j < R; ++j) {
+                        const int y = m.y0 + j;
+                        if (y < D.Ly) outk[(int64_t)x * D.Ly + y] = out_site(Y[c][j], st[(x - xs0) * D.Ly + y]);
                     }
                 }
+            }
         }
         if (!have_next) break;
         if (!same) {
