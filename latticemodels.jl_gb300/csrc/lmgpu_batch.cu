@@ -24,6 +24,7 @@
 #include <vector>
 
 #include "lmgpu_internal.cuh"
+#include "lmgpu_resident.cuh"
 #include "lmgpu_order.cuh"
 
 namespace lmgpu {

@@ -42,6 +42,7 @@
 #include <cuda_runtime.h>
 
 #include "lmgpu_internal.cuh"
+#include "lmgpu_resident.cuh"
 
 namespace lmgpu {
 
