@@ -746,6 +746,7 @@ density_loss(V, B, p::DensityLossProblem) = loss_and_gradients(p, Vector{Float64
 const LM_OPT_FUSED = Cint(1)   # 0: one launch per Chebyshev order for ComplexF32 states
 const LM_OPT_STREAM = Cint(2)  # 0: the region form of the fused step instead of the x-streaming form
 const LM_OPT_KPM = Cint(3)     # 0: FP64 KPM and Fermi-operator recurrences instead of double-float
+const LM_OPT_RESIDENT = Cint(4)  # 0: a ComplexF32 batch's lattices in the region form instead of the lattice-resident form
 
 gpu_synchronize(ctx::Context=default_context()) =
     check(ccall((:lm_ctx_synchronize, LIB), Cint, (Ptr{Cvoid},), ctx.handle), ctx.handle)
@@ -974,6 +975,6 @@ export GPUBuilder, ChebyshevGPU, DeviceLattice, DeviceState, DeviceVector, Devic
        loss_and_gradients, GPUEigensystem, eigenvectors, projector, GPUBatch, DensityLossProblem, density_loss, GPUSparseHamiltonian, set_values!, gpu_operator_currents,
        gpu_operator_timesequence, gpu_synchronize, set_option!, set_weights!, gpu_trace, gpu_norms, gpu_renormalize!, gpu_compensate!, honeycomb_layout!,
        device_pointer, solver_order, spectral_bounds, padded_bounds, kpm_moments, chebyshev_coefficients,
-       gpu_densitymatrix, gpu_entry_currents, LM_OPT_FUSED, LM_OPT_STREAM, LM_OPT_KPM
+       gpu_densitymatrix, gpu_entry_currents, LM_OPT_FUSED, LM_OPT_STREAM, LM_OPT_KPM, LM_OPT_RESIDENT
 
 end # module
