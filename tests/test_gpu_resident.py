@@ -110,33 +110,39 @@ def test_resident_vs_oracle(lm, dt):
 
 
 def test_resident_density_matrices(lm):
-    """U P U^dagger with P = densitymatrix(h, mu = 0): column pass, conjugate transpose, column pass."""
+    """U P U^dagger with P = densitymatrix(h, mu = 0): column pass, conjugate transpose, column pass.
+    The 70 x 70 lattice (4900 sites) runs on a cluster of two CTAs; it is compared with the region
+    form bit for bit, the smaller ones also with the oracle's exact exponent."""
+    rng = np.random.default_rng(8)
+    insts = []
+    for i, (L, per) in enumerate([(12, True), (19, False), (36, True), (44, False), (70, False)]):
+        ol, ll, Ho, Hl = instance(lm, L, L, rng.uniform(0, 0.3), rng.uniform(0, 3), 700 + i, (per, per))
+        P0, _, _ = o.densitymatrix(Ho, mu=0.0)
+        insts.append((Ho, Hl, ll, P0))
     outs = {}
     for resident in (True, False):
-        rng = np.random.default_rng(8)
         lm.default_context().set_resident_form(resident)
         try:
             batch = lm.Batch("density", "c32")
-            refs = []
-            for i, (L, per) in enumerate([(12, True), (19, False), (36, True), (44, False)]):
-                ol, ll, Ho, Hl = instance(lm, L, L, rng.uniform(0, 0.3), rng.uniform(0, 3), 700 + i, (per, per))
-                P0, _, _ = o.densitymatrix(Ho, mu=0.0)
+            sts = []
+            for Ho, Hl, ll, P0 in insts:
                 st = lm.DensityMatrix(ll, P0, precision="c32")
                 batch.add(Hl, st)
-                refs.append((Ho, P0, st))
+                sts.append(st)
             batch.update(0.1)
             for _ in range(3):
                 batch.step()
-            outs[resident] = [st.to_numpy() for _, _, st in refs]
+            outs[resident] = [st.to_numpy() for st in sts]
         finally:
             lm.default_context().set_resident_form(True)
-        if resident:
-            for Ho, P0, st in refs:
-                U = o.expm_exact(Ho, 0.1)
-                P = P0
-                for _ in range(3):
-                    P = U @ P @ U.conj().T
-                assert rel(st.to_numpy(), P) <= 5e-6
+    for (Ho, Hl, ll, P0), got in zip(insts, outs[True]):
+        if Ho.shape[0] > 2500:
+            continue
+        U = o.expm_exact(Ho, 0.1)
+        P = P0
+        for _ in range(3):
+            P = U @ P @ U.conj().T
+        assert rel(got, P) <= 5e-6
     for x, y in zip(outs[True], outs[False]):
         assert np.array_equal(x, y)
 
