@@ -307,6 +307,8 @@ def batch_subrecord(n, steps, warmup):
     return {"value": ket_steps * steps / (ms / 1000.0), "unit": "ket-steps/s", "ms_per_step": ms / steps,
             "steps": steps, "warmup": warmup, "instances": len(take),
             "sum_N2": int(sum(int(Ls[i]) ** 4 for i in take)), "chebyshev_order": info["K"], "tuned": tune,
+            "fused_form": ("lattice-resident (csrc/lmgpu_resident.cu): a whole ket on chip for all K orders, one CTA "
+                           "up to 4608 sites, a cluster of two CTAs up to 9216; the region form for the rest"),
             "p0": "densitymatrix(h, mu=0, T=0.1) per lattice (device Chebyshev Fermi operator)",
             "trace_drift_max": float(np.abs(tr1 - tr0).max() / np.abs(tr0).max()), "setup_s": setup,
             "workload": BATCH_WORKLOAD.format(n=len(take)) + " (the first lattices of the seeded 512)"}
