@@ -277,6 +277,31 @@ def _batch_instances(n, prec, panel, p0="random", budget_frac=0.85):
     return batch, states, Ls, take, used
 
 
+def batch_roofline(sum_n2, K, ms_per_step, sm_mhz=None):
+    """Roofline fields of a dense-P batch step (c32): two fused passes and a conjugate transpose.
+
+    * frac: the per-order formula 5*K*sum N^2*8 B per pass (the bytes of K unfused order passes);
+      the fused passes keep all K orders on chip, so it exceeds 1.
+    * dram_frac: the physical bytes, each pass and the transpose reading and writing every
+      lattice's block once (3 x 2 x sum N^2 x 8 B), which is the traffic the counters measure for
+      the lattice-resident form (profiles/cheb_resident_c32_batch_uneven_lattices.md).
+    * fma_frac: the useful FP32 FMAs (20 per site-order with complex hops) of both passes against
+      152 SMs x 128 FMA/clk at the SM clock."""
+    peak, kind = measured_peak_hbm()
+    sec = ms_per_step / 1000.0
+    alg = 2 * 5.0 * K * sum_n2 * 8
+    phys = 3 * 2.0 * sum_n2 * 8
+    mhz = sm_mhz or 2070.0
+    fma = 2 * 20.0 * K * sum_n2 / sec / (152 * 128 * mhz * 1e6)
+    return {"bound": "compute (the stencil arithmetic's latency at 12 warps per SM; DRAM traffic is the "
+                     "algorithmic minimum)",
+            "achieved_formula_gbs": alg / sec / 1e9, "frac": alg / sec / 1e9 / peak,
+            "dram_gbs": phys / sec / 1e9, "dram_frac": phys / sec / 1e9 / peak, "fma_frac": fma,
+            "peak": peak, "unit": "GB/s", "peak_source": f"{kind} (MEASURED_PEAKS.json hbm_gbs)",
+            "note": "frac: the per-order formula 5*K*sum N^2*s per pass; dram_frac: 3 x 2 x sum N^2 x 8 B per "
+                    "step (two passes and the transpose); fma_frac: 20 useful FMAs per site-order"}
+
+
 def batch_subrecord(n, steps, warmup):
     """A small instance of the batching workload for the default line: the first n lattices,
     P_0 from densitymatrix (mu = 0, T = 0.1), tuned, stepped through the captured graphs."""
@@ -309,6 +334,7 @@ def batch_subrecord(n, steps, warmup):
             "sum_N2": int(sum(int(Ls[i]) ** 4 for i in take)), "chebyshev_order": info["K"], "tuned": tune,
             "fused_form": ("lattice-resident (csrc/lmgpu_resident.cu): a whole ket on chip for all K orders, one CTA "
                            "up to 4608 sites, a cluster of two CTAs up to 9216; the region form for the rest"),
+            "roofline": batch_roofline(sum(int(Ls[i]) ** 4 for i in take), info["K"], ms / steps),
             "p0": "densitymatrix(h, mu=0, T=0.1) per lattice (device Chebyshev Fermi operator)",
             "trace_drift_max": float(np.abs(tr1 - tr0).max() / np.abs(tr0).max()), "setup_s": setup,
             "workload": BATCH_WORKLOAD.format(n=len(take)) + " (the first lattices of the seeded 512)"}
@@ -361,6 +387,8 @@ def run_batch_workload(args):
                        "instances_requested": n, "sum_N2": int(sum(int(Ls[i]) ** 4 for i in take)),
                        "chebyshev_order": info["K"], "tuned": tune, "setup_s": t_setup,
                        "device_bytes": used, "panel_columns": panel, "fused_form": args.batch_form},
+            "roofline": batch_roofline(sum(int(Ls[i]) ** 4 for i in take), info["K"], ms / args.steps,
+                                       clocks.get("sm_mhz")),
             "clocks": clocks, "trace_sample": tr}
     print(json.dumps(line))
     return 0
