@@ -286,13 +286,15 @@ def batch_roofline(sum_n2, K, ms_per_step, sm_mhz=None):
       lattice's block once (3 x 2 x sum N^2 x 8 B), which is the traffic the counters measure for
       the lattice-resident form (profiles/cheb_resident_c32_batch_uneven_lattices.md).
     * fma_frac: the useful FP32 FMAs (20 per site-order with complex hops) of both passes against
-      152 SMs x 128 FMA/clk at the SM clock."""
+      the device's SMs x 128 FMA/clk at the SM clock."""
+    import torch
     peak, kind = measured_peak_hbm()
     sec = ms_per_step / 1000.0
     alg = 2 * 5.0 * K * sum_n2 * 8
     phys = 3 * 2.0 * sum_n2 * 8
     mhz = sm_mhz or 2070.0
-    fma = 2 * 20.0 * K * sum_n2 / sec / (152 * 128 * mhz * 1e6)
+    sms = torch.cuda.get_device_properties(0).multi_processor_count if torch.cuda.is_available() else 152
+    fma = 2 * 20.0 * K * sum_n2 / sec / (sms * 128 * mhz * 1e6)
     return {"bound": "compute (the stencil arithmetic's latency at 12 warps per SM; DRAM traffic is the "
                      "algorithmic minimum)",
             "achieved_formula_gbs": alg / sec / 1e9, "frac": alg / sec / 1e9 / peak,
